@@ -1,0 +1,459 @@
+// Context, device arena, the shared certification tail and the C ABI entry
+// points of libhdgpu.so (declared in include/hd_gpu.h).
+//
+// The C ABI replaces the reference's algorithm seam
+// HausdorffDistance<COORD_T,N_DIMS>::CalculateDistance
+// (src/hausdorff_distance.h:21-32) and the driver's variant factory and
+// repeat loop (src/run_hausdorff_distance.cu:220-357).  Errors never escape
+// as exceptions (the reference aborts through glog CHECK or throws
+// hd::Exception from CUDA_CHECK, utils/exception.h:151-160); every call
+// returns an hd_status and keeps a message for hd_last_error.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+
+#include "hd_common.cuh"
+#include "hd_internal.h"
+
+namespace hdg {
+
+hd_status fail(Ctx& c, hd_status s, const std::string& msg) {
+  if (c.last_error.empty()) c.last_error = msg;
+  return s;
+}
+
+hd_status cuda_fail(Ctx& c, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return fail(c, HD_ERR_OOM, m);
+  if (e == cudaErrorNoKernelImageForDevice || e == cudaErrorNoDevice ||
+      e == cudaErrorInsufficientDriver)
+    return fail(c, HD_ERR_NO_DEVICE, m);
+  return fail(c, HD_ERR_CUDA, m);
+}
+
+hd_status ensure(Ctx& c, BufSlot slot, size_t bytes, void** out) {
+  DevBuf& b = c.bufs[slot];
+  if (bytes == 0) bytes = 16;
+  if (b.bytes < bytes) {
+    if (b.p) {
+      cudaError_t e = cudaStreamSynchronize(c.stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "sync before realloc");
+      cudaFree(b.p);
+      b.p = nullptr;
+      b.bytes = 0;
+    }
+    // Grow geometrically so that repeated solves of slightly larger inputs
+    // do not reallocate every call.
+    size_t want = std::max(bytes, b.bytes + b.bytes / 4);
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+      (void) cudaGetLastError();
+      e = cudaMalloc(&b.p, bytes);
+      if (e != cudaSuccess) {
+        (void) cudaGetLastError();
+        b.p = nullptr;
+        return fail(c, HD_ERR_OOM,
+                    "device allocation of " + std::to_string(bytes) + " bytes failed");
+      }
+      want = bytes;
+    }
+    b.bytes = want;
+  }
+  *out = b.p;
+  return HD_OK;
+}
+
+hd_status after_launch(Ctx& c, const char* what) {
+  ++c.launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(c, e, what);
+  return HD_OK;
+}
+
+DevScalars* scalars(Ctx& c, int dir) {
+  return reinterpret_cast<DevScalars*>(c.bufs[kBufScalars].p) + dir;
+}
+
+void mark(Ctx& c, int k) {
+  if (!c.timing || k < 0 || k >= 12) return;
+  cudaEventRecord(c.ev[k], c.stream);
+  c.ev_used = std::max(c.ev_used, k + 1);
+}
+
+uint64_t pick_multiplier(uint64_t n, uint64_t seed) {
+  if (n <= 2) return 1;
+  // Near n / golden ratio, nudged by the seed, then moved to the next value
+  // coprime with n so that j -> j*mul mod n is a bijection.
+  uint64_t m = (uint64_t) ((double) n * 0.6180339887498949) + (seed % 97) * 2 + 1;
+  m %= n;
+  if (m == 0) m = 1;
+  while (std::gcd(m, n) != 1) m = (m + 1) % n ? (m + 1) % n : 1;
+  return m;
+}
+
+namespace {
+
+__global__ void k_init_scalars(DevScalars* sc, int n) {
+  int i = threadIdx.x;
+  if (i < n) {
+    DevScalars z;
+    memset(&z, 0, sizeof(z));
+    z.min_key = ~0ull;
+    for (int s = 0; s < 2; ++s)
+      for (int d = 0; d < 4; ++d) {
+        z.mbr_ord[s][0][d] = 0xFFFFFFFFu;  // lower corner: atomicMin target
+        z.mbr_ord[s][1][d] = 0u;           // upper corner: atomicMax target
+      }
+    sc[i] = z;
+  }
+}
+
+// Exact argmin over B for the certifying A point.  Scans the caller's B in
+// its own order so that ib is the caller's index; among equal squared
+// distances the lowest index wins (atomicMin on (d2 bits, index)).
+__global__ void k_argmin(const float* __restrict__ A, const float* __restrict__ B,
+                         uint64_t nB, int D, DevScalars* sc) {
+  const unsigned long long key = sc->max_key;
+  if (key == 0) return;
+  const uint32_t ia = unpack_max_index(key);
+  float a[4] = {0, 0, 0, 0};
+  const bool small = D <= 4;
+  if (small)
+    for (int k = 0; k < D; ++k) a[k] = A[(uint64_t) ia * D + k];
+  unsigned long long best = ~0ull;
+  for (uint64_t j = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; j < nB;
+       j += (uint64_t) gridDim.x * blockDim.x) {
+    float d2;
+    if (D == 2) {
+      d2 = d2_2(a[0], a[1], B[2 * j], B[2 * j + 1]);
+    } else if (D == 3) {
+      d2 = d2_3(a[0], a[1], a[2], B[3 * j], B[3 * j + 1], B[3 * j + 2]);
+    } else {
+      d2 = d2_n(A + (uint64_t) ia * D, B + j * D, D);
+    }
+    unsigned long long k = pack_min(d2, (uint32_t) j);
+    best = k < best ? k : best;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    unsigned long long v = __shfl_xor_sync(0xFFFFFFFFu, best, o);
+    best = v < best ? v : best;
+  }
+  if ((threadIdx.x & 31) == 0 && best != ~0ull) atomicMin(&sc->min_key, best);
+}
+
+__global__ void k_finalize(const float* __restrict__ A, const float* __restrict__ B,
+                           int D, DevScalars* sc) {
+  const unsigned long long key = sc->max_key;
+  if (key == 0) {
+    sc->status |= kErrInternal;
+    return;
+  }
+  const uint32_t ia = unpack_max_index(key);
+  const uint32_t d2bits = (uint32_t) (key >> 32);
+  const unsigned long long mk = sc->min_key;
+  const uint32_t ib = (uint32_t) (mk & 0xFFFFFFFFull);
+  // The argmin over B of A[ia] must reproduce the maximum exactly: it is the
+  // same FP32 formula over the same coordinates.
+  if ((uint32_t) (mk >> 32) != d2bits) sc->status |= kErrInternal;
+  double s = 0.0;
+  for (int k = 0; k < D; ++k) {
+    double t = (double) A[(uint64_t) ia * D + k] - (double) B[(uint64_t) ib * D + k];
+    s += t * t;
+  }
+  sc->d2_64 = s;
+  sc->d2 = __uint_as_float(d2bits);
+  sc->ia = ia;
+  sc->ib = ib;
+}
+
+}  // namespace
+
+hd_status certify(Ctx& c, const DirInput& in) {
+  DevScalars* sc = scalars(c, in.dir);
+  int grid = (int) std::min<uint64_t>((in.nB + 255) / 256, (uint64_t) c.num_sms * 4);
+  grid = std::max(grid, 1);
+  k_argmin<<<grid, 256, 0, c.stream>>>(in.A, in.B, in.nB, in.dims, sc);
+  hd_status s = after_launch(c, "argmin");
+  if (s != HD_OK) return s;
+  k_finalize<<<1, 1, 0, c.stream>>>(in.A, in.B, in.dims, sc);
+  return after_launch(c, "finalize");
+}
+
+hd_status init_scalars(Ctx& c) {
+  void* p = nullptr;
+  hd_status s = ensure(c, kBufScalars, 2 * sizeof(DevScalars), &p);
+  if (s != HD_OK) return s;
+  k_init_scalars<<<1, 32, 0, c.stream>>>((DevScalars*) p, 2);
+  return after_launch(c, "init_scalars");
+}
+
+}  // namespace hdg
+
+using namespace hdg;
+
+namespace {
+
+// Host staging of the two DevScalars.
+struct HostScalars {
+  DevScalars s[2];
+};
+
+hd_status copy_in(Ctx& c, const float* src, uint64_t n, int dims, BufSlot slot,
+                  const float** out) {
+  void* p = nullptr;
+  size_t bytes = (size_t) n * dims * sizeof(float);
+  hd_status s = ensure(c, slot, bytes, &p);
+  if (s != HD_OK) return s;
+  cudaError_t e = cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, c.stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "copy inputs to device");
+  *out = (const float*) p;
+  return HD_OK;
+}
+
+hd_status run_direction(Ctx& c, const DirInput& in, int variant, int* used,
+                        DirResult* extra) {
+  int v = variant;
+  hd_status s;
+  if (v == HD_VARIANT_AUTO) {
+    if ((s = select_variant(c, in, &v)) != HD_OK) return s;
+  }
+  *used = v;
+  switch (v) {
+  case HD_VARIANT_EB: return run_eb(c, in);
+  case HD_VARIANT_BRUTE: return run_brute(c, in);
+  case HD_VARIANT_LBVH: return run_lbvh(c, in);
+  case HD_VARIANT_GRID: return run_grid(c, in);
+  case HD_VARIANT_BF16: return run_bf16(c, in, extra);
+  default: return fail(c, HD_ERR_INVALID_ARG, "unknown variant");
+  }
+}
+
+hd_status check_status(Ctx& c, const HostScalars& h, int ndir) {
+  for (int d = 0; d < ndir; ++d) {
+    uint32_t st = h.s[d].status;
+    if (st & kErrWaitTimeout)
+      return fail(c, HD_ERR_DEVICE_TIMEOUT, "a bounded device wait ran out");
+    if (st & kErrQueueOverflow) return fail(c, HD_ERR_CUDA, "device queue overflow");
+    if (st & kErrInternal)
+      return fail(c, HD_ERR_CUDA, "internal consistency check failed");
+  }
+  return HD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void hd_default_options(hd_options* opt) {
+  if (!opt) return;
+  memset(opt, 0, sizeof(*opt));
+  opt->device = 0;
+  opt->variant = HD_VARIANT_AUTO;
+  opt->seed = 0;
+  opt->sample_rate = 0.01;
+  opt->n_points_cell = 8;
+  opt->leaf_size = 16;
+  opt->eb_only_threshold = 0;
+}
+
+hd_status hd_create(hd_ctx** out, const hd_options* opt) {
+  if (!out) return HD_ERR_INVALID_ARG;
+  *out = nullptr;
+  hd_ctx* c = new (std::nothrow) hd_ctx();
+  if (!c) return HD_ERR_OOM;
+  if (opt)
+    c->opt = *opt;
+  else
+    hd_default_options(&c->opt);
+  if (c->opt.leaf_size == 0 || c->opt.leaf_size > 32) c->opt.leaf_size = 16;
+  if (c->opt.n_points_cell == 0) c->opt.n_points_cell = 8;
+  if (!(c->opt.sample_rate > 0.0)) c->opt.sample_rate = 0.01;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0 || c->opt.device < 0 || c->opt.device >= n) {
+    (void) cudaGetLastError();
+    delete c;
+    return HD_ERR_NO_DEVICE;
+  }
+  c->device = c->opt.device;
+  if ((e = cudaSetDevice(c->device)) != cudaSuccess) {
+    delete c;
+    return HD_ERR_NO_DEVICE;
+  }
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, c->device);
+  if (prop.major * 10 + prop.minor != 103) {
+    // The library carries sm_103a code only.
+    delete c;
+    return HD_ERR_NO_DEVICE;
+  }
+  c->num_sms = prop.multiProcessorCount;
+  if ((e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    delete c;
+    return HD_ERR_CUDA;
+  }
+  c->stream = c->own_stream;
+  for (auto& ev : c->ev) cudaEventCreate(&ev);
+  if (cudaMallocHost(&c->host_pinned, 4096) != cudaSuccess) {
+    hd_destroy(c);
+    return HD_ERR_OOM;
+  }
+  c->host_pinned_bytes = 4096;
+  *out = c;
+  return HD_OK;
+}
+
+hd_status hd_destroy(hd_ctx* c) {
+  if (!c) return HD_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto& b : c->bufs)
+    if (b.p) cudaFree(b.p);
+  for (auto& ev : c->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
+  if (c->host_pinned) cudaFreeHost(c->host_pinned);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+  return HD_OK;
+}
+
+hd_status hd_set_stream(hd_ctx* c, void* stream) {
+  if (!c) return HD_ERR_INVALID_ARG;
+  c->stream = stream ? (cudaStream_t) stream : c->own_stream;
+  return HD_OK;
+}
+
+hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
+                   uint64_t n_b, int n_dims, uint32_t flags, int variant,
+                   hd_result* out) {
+  if (!c) return HD_ERR_INVALID_ARG;
+  c->last_error.clear();
+  if (!out || !A || !B) return fail(*c, HD_ERR_INVALID_ARG, "null pointer argument");
+  if (n_a == 0 || n_b == 0) return fail(*c, HD_ERR_INVALID_ARG, "empty point set");
+  if (n_a >= 0xFFFFFFFFull || n_b >= 0xFFFFFFFFull)
+    return fail(*c, HD_ERR_INVALID_ARG, "point sets are limited to 2^32-2 points");
+  if (n_dims < 1 || n_dims > 256)
+    return fail(*c, HD_ERR_INVALID_ARG, "n_dims must be in [1, 256]");
+  if (flags & ~(HD_UNDIRECTED | HD_DEVICE_PTRS | HD_COUNT_PAIRS | HD_TIMING))
+    return fail(*c, HD_ERR_INVALID_ARG, "unknown flag bits");
+  if (variant < 0) variant = c->opt.variant;
+  if (variant > HD_VARIANT_BRUTE)
+    return fail(*c, HD_ERR_INVALID_ARG, "unknown variant");
+  const bool spatial = variant == HD_VARIANT_GRID || variant == HD_VARIANT_LBVH;
+  if (spatial && n_dims != 2 && n_dims != 3)
+    return fail(*c, HD_ERR_UNSUPPORTED, "grid and LBVH variants need n_dims 2 or 3");
+  if (variant == HD_VARIANT_BF16 && (n_dims % 16) != 0)
+    return fail(*c, HD_ERR_UNSUPPORTED, "the BF16 variant needs n_dims % 16 == 0");
+  cudaSetDevice(c->device);
+  memset(out, 0, sizeof(*out));
+  out->hd_ba = -1.0;
+  c->timing = (flags & HD_TIMING) != 0;
+  c->ev_used = 0;
+
+  hd_status s;
+  const float* dA = A;
+  const float* dB = B;
+  mark(*c, 11);  // start of the whole call (copies included)
+  if (!(flags & HD_DEVICE_PTRS)) {
+    if ((s = copy_in(*c, A, n_a, n_dims, kBufA, &dA)) != HD_OK) return s;
+    if ((s = copy_in(*c, B, n_b, n_dims, kBufB, &dB)) != HD_OK) return s;
+  }
+  if ((s = init_scalars(*c)) != HD_OK) return s;
+  const bool undirected = (flags & HD_UNDIRECTED) != 0;
+  const bool count = (flags & HD_COUNT_PAIRS) != 0;
+  DirResult ex[2];
+  int used[2] = {variant, -1};
+  float ms_phase[2][8] = {};
+  for (int d = 0; d < (undirected ? 2 : 1); ++d) {
+    DirInput in{d == 0 ? dA : dB, d == 0 ? n_a : n_b, d == 0 ? dB : dA,
+                d == 0 ? n_b : n_a, n_dims, d, count};
+    c->ev_used = 0;
+    mark(*c, 10);
+    if ((s = run_direction(*c, in, variant, &used[d], &ex[d])) != HD_OK) return s;
+    mark(*c, 5);
+    if (c->timing) {
+      cudaError_t e = cudaEventSynchronize(c->ev[5]);
+      if (e != cudaSuccess) return cuda_fail(*c, e, "solve");
+      float t;
+      // Phases: 0 prep (10->0), 1 build (0->1), 2 sample/seed (1->2),
+      // 3 query/main (2->3), 4 tail (3->4), 5 certify (4->5).
+      const int from[6] = {10, 0, 1, 2, 3, 4};
+      const int to[6] = {0, 1, 2, 3, 4, 5};
+      for (int p = 0; p < 6; ++p) {
+        if (cudaEventElapsedTime(&t, c->ev[from[p]], c->ev[to[p]]) == cudaSuccess)
+          ms_phase[d][p] = t;
+        else
+          (void) cudaGetLastError();
+      }
+    }
+  }
+  HostScalars* h = reinterpret_cast<HostScalars*>(c->host_pinned);
+  cudaError_t e = cudaMemcpyAsync(h, c->bufs[kBufScalars].p, sizeof(HostScalars),
+                                  cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(*c, e, "copy result");
+  mark(*c, 9);
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(*c, e, "solve");
+  if ((s = check_status(*c, *h, undirected ? 2 : 1)) != HD_OK) return s;
+
+  const DevScalars& r0 = h->s[0];
+  out->hd_ab = std::sqrt(r0.d2_64);
+  int win = 0;
+  if (undirected) {
+    const DevScalars& r1 = h->s[1];
+    out->hd_ba = std::sqrt(r1.d2_64);
+    // The larger FP32 squared distance decides; ties keep A->B.
+    if (r1.d2 > r0.d2) win = 1;
+  }
+  const DevScalars& w = h->s[win];
+  out->hd_f32 = std::sqrt(w.d2);
+  out->hd = std::sqrt(w.d2_64);
+  out->direction = win;
+  out->ia = w.ia;
+  out->ib = w.ib;
+  out->visited_pairs = r0.pairs + (undirected ? h->s[1].pairs : 0);
+  out->visited_nodes = r0.nodes + (undirected ? h->s[1].nodes : 0);
+  out->variant_used = used[0];
+  out->variant_used_ba = undirected ? used[1] : -1;
+  out->err_bound = std::max(ex[0].err_bound, ex[1].err_bound);
+  out->rechecked = ex[0].rechecked + ex[1].rechecked;
+  if (c->timing) {
+    float t = 0;
+    if (cudaEventElapsedTime(&t, c->ev[11], c->ev[9]) == cudaSuccess) out->ms = t;
+    for (int p = 0; p < 6; ++p) out->phase_ms[p] = ms_phase[0][p] + ms_phase[1][p];
+  }
+  (void) count;
+  return HD_OK;
+}
+
+const char* hd_last_error(hd_ctx* c) {
+  if (!c) return "null context";
+  return c->last_error.c_str();
+}
+
+const char* hd_status_string(hd_status s) {
+  switch (s) {
+  case HD_OK: return "HD_OK";
+  case HD_ERR_INVALID_ARG: return "HD_ERR_INVALID_ARG";
+  case HD_ERR_OOM: return "HD_ERR_OOM";
+  case HD_ERR_DEVICE_TIMEOUT: return "HD_ERR_DEVICE_TIMEOUT";
+  case HD_ERR_CUDA: return "HD_ERR_CUDA";
+  case HD_ERR_UNSUPPORTED: return "HD_ERR_UNSUPPORTED";
+  case HD_ERR_NO_DEVICE: return "HD_ERR_NO_DEVICE";
+  }
+  return "HD_ERR_UNKNOWN";
+}
+
+uint64_t hd_kernel_launches(hd_ctx* c) { return c ? c->launches : 0; }
+
+const char* hd_version(void) { return "hd-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,387 @@
+// Persistent early-break (EB) scan for 2-D and 3-D inputs.
+//
+// Replaces the reference's GPU early-break kernel
+// (src/hd_impl/hausdorff_distance_early_break.h:117-219: one block per A
+// point, threads striding over B, a cub::BlockReduce every 32 iterations and
+// a CAS-loop float atomicMax) and the hybrid's block / cooperative-grid EB
+// kernels (src/hd_impl/hausdorff_distance_hybrid.h:519-694).
+//
+// Design (GB300-first):
+//  * B is copied once into a visit-ordered, padded array of float2 (2-D) or
+//    float4 (3-D) points: coalesced 16-byte loads, 16-byte aligned tiles.
+//  * k_eb_main is persistent: every CTA streams B tiles of 256 points into a
+//    shared-memory double buffer with the TMA bulk-copy engine
+//    (cp.async.bulk + mbarrier), and each thread carries 4 A points ("slots")
+//    against every point of the tile (shared-memory broadcast reads).  A slot
+//    that stops — its running minimum at or below the running maximum (early
+//    break), a full cycle over B (completed: atomicMax), or more than the
+//    per-point cap of tiles (deferred) — is refilled at the next tile boundary
+//    from a global visit queue with one warp-aggregated atomicAdd.  Because
+//    B's visit order is a pseudo-random permutation, a slot may start at any
+//    tile and wrap around: no slot waits for a CTA-wide restart.
+//  * Deferred ("heavy") points — the ones whose nearest neighbour is farther
+//    than the running maximum — are finished by k_eb_heavy, one point per CTA
+//    with all 256 threads over B, the block-per-point shape of the reference
+//    but with a CTA reduction only every 32 tiles.  The same kernel seeds the
+//    running maximum with the first 152 visited points before the main pass,
+//    which keeps the main pass from starting with a zero threshold (the
+//    reference's hybrid seeds it with an MBR lower bound and a sample,
+//    hybrid.h:111-142).
+//  * The running maximum is one 64-bit word (squared-distance bits, ~index):
+//    a single atomicMax on the bit pattern — no CAS loop — which also keeps
+//    the certifying A index.
+#include <cfloat>
+
+#include "hd_common.cuh"
+#include "hd_internal.h"
+
+namespace hdg {
+namespace {
+
+constexpr int kEbThreads = 256;
+constexpr int kEbTile = 256;          // B points per tile (== kEbThreads)
+constexpr int kEbSlots = 4;           // A points carried per thread
+constexpr int kHeavyStepTiles = 32;   // tiles between CTA reductions (heavy)
+constexpr uint32_t kCapPairs = 32768; // per-point pairs before deferral
+constexpr uint32_t kWaitLimit = 1u << 26;
+
+template <int D>
+struct EbPt;
+template <>
+struct EbPt<2> {
+  using T = float2;
+};
+template <>
+struct EbPt<3> {
+  using T = float4;
+};
+
+struct HeavyEntry {
+  uint32_t ia;         // caller's index of the A point
+  uint32_t next_tile;  // first tile still to visit
+  uint32_t remaining;  // tiles still to visit
+  float cmin;          // running minimum so far
+};
+
+template <int D>
+__device__ __forceinline__ void load_a(const float* __restrict__ A, uint64_t i,
+                                       float& x, float& y, float& z) {
+  if constexpr (D == 2) {
+    float2 v = *reinterpret_cast<const float2*>(A + 2 * i);
+    x = v.x;
+    y = v.y;
+    z = 0.0f;
+  } else {
+    x = A[3 * i];
+    y = A[3 * i + 1];
+    z = A[3 * i + 2];
+  }
+}
+
+template <int D>
+__global__ void k_eb_pack(const float* __restrict__ B, uint64_t nB, Perm perm,
+                          typename EbPt<D>::T* __restrict__ out, uint64_t nPad) {
+  for (uint64_t j = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; j < nPad;
+       j += (uint64_t) gridDim.x * blockDim.x) {
+    if constexpr (D == 2) {
+      float2 v = make_float2(INFINITY, INFINITY);
+      if (j < nB) v = *reinterpret_cast<const float2*>(B + 2 * perm(j));
+      out[j] = v;
+    } else {
+      float4 v = make_float4(INFINITY, INFINITY, INFINITY, 0.0f);
+      if (j < nB) {
+        uint64_t s = perm(j);
+        v = make_float4(B[3 * s], B[3 * s + 1], B[3 * s + 2], 0.0f);
+      }
+      out[j] = v;
+    }
+  }
+}
+
+template <int D>
+__device__ __forceinline__ float tile_d2(float ax, float ay, float az,
+                                         float bx, float by, float bz) {
+  if constexpr (D == 2) {
+    return d2_2(ax, ay, bx, by);
+  } else {
+    return d2_3(ax, ay, az, bx, by, bz);
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kEbThreads)
+    k_eb_main(const float* __restrict__ A, Perm permA, uint64_t a_begin,
+              uint64_t a_end, const typename EbPt<D>::T* __restrict__ Bp,
+              uint32_t nTiles, uint32_t capTiles, DevScalars* sc,
+              HeavyEntry* heavy, uint32_t heavy_cap) {
+  using PT = typename EbPt<D>::T;
+  constexpr uint32_t kTileBytes = kEbTile * sizeof(PT);
+  __shared__ __align__(128) PT tile[2][kEbTile];
+  __shared__ __align__(8) uint64_t full[2];
+
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  float ax[kEbSlots], ay[kEbSlots], az[kEbSlots], cm[kEbSlots];
+  uint32_t ia[kEbSlots], vis[kEbSlots];
+  bool act[kEbSlots];
+  unsigned long long pairs = 0;
+  bool exhausted = false;
+#pragma unroll
+  for (int r = 0; r < kEbSlots; ++r) {
+    act[r] = false;
+    ax[r] = ay[r] = az[r] = 0.0f;
+    cm[r] = FLT_MAX;
+    ia[r] = 0;
+    vis[r] = 0;
+  }
+
+  // Warp-aggregated refill of every free slot from the visit queue.
+  auto refill = [&]() {
+    if (exhausted) return;
+    uint32_t masks[kEbSlots];
+    uint32_t total = 0;
+#pragma unroll
+    for (int r = 0; r < kEbSlots; ++r) {
+      masks[r] = __ballot_sync(0xFFFFFFFFu, !act[r]);
+      total += __popc(masks[r]);
+    }
+    if (total == 0) return;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&sc->next, (unsigned long long) total);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t before = 0;
+#pragma unroll
+    for (int r = 0; r < kEbSlots; ++r) {
+      if (!act[r]) {
+        uint64_t v = a_begin + base + before + __popc(masks[r] & lt);
+        if (v < a_end) {
+          uint64_t i = permA(v);
+          ia[r] = (uint32_t) i;
+          load_a<D>(A, i, ax[r], ay[r], az[r]);
+          cm[r] = FLT_MAX;
+          vis[r] = 0;
+          act[r] = true;
+        }
+      }
+      before += __popc(masks[r]);
+    }
+    if (a_begin + base + total >= a_end) exhausted = true;
+  };
+
+  if (tid == 0) {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  refill();
+
+  uint32_t tcur = (uint32_t) (((uint64_t) blockIdx.x * nTiles) / gridDim.x);
+  if (tid == 0) {
+    mbar_expect_tx(&full[0], kTileBytes);
+    tma_load_1d(&tile[0][0], Bp + (uint64_t) tcur * kEbTile, kTileBytes, &full[0]);
+  }
+
+  uint32_t i = 0;
+  bool failed = false;
+  for (;; ++i) {
+    const int buf = i & 1;
+    const uint32_t tnext = (tcur + 1 == nTiles) ? 0 : tcur + 1;
+    if (tid == 0) {
+      // Buffer buf^1 was released by every thread at the end of iteration i-1.
+      mbar_expect_tx(&full[buf ^ 1], kTileBytes);
+      tma_load_1d(&tile[buf ^ 1][0], Bp + (uint64_t) tnext * kEbTile, kTileBytes,
+                  &full[buf ^ 1]);
+    }
+    bool ok = mbar_wait(&full[buf], (i >> 1) & 1, &sc->status, kWaitLimit);
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+
+    if constexpr (D == 2) {
+      const float4* t4 = reinterpret_cast<const float4*>(&tile[buf][0]);
+#pragma unroll 4
+      for (int p = 0; p < kEbTile / 2; ++p) {
+        float4 b = t4[p];
+#pragma unroll
+        for (int r = 0; r < kEbSlots; ++r) {
+          cm[r] = fminf(cm[r], d2_2(ax[r], ay[r], b.x, b.y));
+          cm[r] = fminf(cm[r], d2_2(ax[r], ay[r], b.z, b.w));
+        }
+      }
+    } else {
+#pragma unroll 4
+      for (int p = 0; p < kEbTile; ++p) {
+        float4 b = tile[buf][p];
+#pragma unroll
+        for (int r = 0; r < kEbSlots; ++r)
+          cm[r] = fminf(cm[r], d2_3(ax[r], ay[r], az[r], b.x, b.y, b.z));
+      }
+    }
+
+    // Slot bookkeeping at the tile boundary.
+    unsigned long long key = 0;
+    if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
+    key = __shfl_sync(0xFFFFFFFFu, key, 0);
+    const float thr = threshold_of(key);
+#pragma unroll
+    for (int r = 0; r < kEbSlots; ++r) {
+      if (!act[r]) continue;
+      pairs += kEbTile;
+      vis[r] += 1;
+      if (cm[r] <= thr) {
+        act[r] = false;  // early break: cannot raise the maximum
+      } else if (vis[r] == nTiles) {
+        atomicMax(&sc->max_key, pack_max(cm[r], ia[r]));
+        act[r] = false;  // full cycle: exact minimum
+      } else if (vis[r] >= capTiles) {
+        uint32_t s = atomicAdd(&sc->heavy_count, 1u);
+        if (s < heavy_cap) {
+          heavy[s] = HeavyEntry{ia[r], tnext, nTiles - vis[r], cm[r]};
+        } else {
+          atomicOr(&sc->status, kErrQueueOverflow);
+        }
+        act[r] = false;
+      }
+    }
+    refill();
+    bool any = false;
+#pragma unroll
+    for (int r = 0; r < kEbSlots; ++r) any |= act[r];
+    tcur = tnext;
+    if (!__syncthreads_or(any)) break;
+  }
+  // One prefetch is still in flight (issued at the top of the last
+  // iteration); wait for it so the CTA never exits with a copy pending.
+  if (tid == 0 && !failed) mbar_wait(&full[(i & 1) ^ 1], ((i + 1) >> 1) & 1, &sc->status, kWaitLimit);
+  if (pairs) atomicAdd(&sc->pairs, pairs);
+}
+
+// One A point per CTA, all threads over B.  list == nullptr: seed mode, the
+// entries are the first n visit positions starting from the beginning of B.
+template <int D>
+__global__ void __launch_bounds__(kEbThreads)
+    k_eb_heavy(const float* __restrict__ A, Perm permA,
+               const typename EbPt<D>::T* __restrict__ Bp, uint32_t nTiles,
+               DevScalars* sc, const HeavyEntry* __restrict__ list,
+               uint32_t n_host, const uint32_t* n_dev) {
+  __shared__ float red[kEbThreads / 32];
+  __shared__ float s_thr;
+  const int tid = threadIdx.x;
+  const uint32_t n = n_dev ? *n_dev : n_host;
+  unsigned long long pairs = 0;
+  for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
+    HeavyEntry h;
+    if (list) {
+      h = list[e];
+    } else {
+      h = HeavyEntry{(uint32_t) permA(e), 0u, nTiles, FLT_MAX};
+    }
+    float ax, ay, az;
+    load_a<D>(A, h.ia, ax, ay, az);
+    float m = FLT_MAX;
+    float cmin = h.cmin;
+    uint32_t done = 0;
+    uint32_t t = h.next_tile;
+    bool broke = false;
+    while (done < h.remaining) {
+      uint32_t step = min((uint32_t) kHeavyStepTiles, h.remaining - done);
+      for (uint32_t s = 0; s < step; ++s) {
+        const auto b = Bp[(uint64_t) t * kEbTile + tid];
+        if constexpr (D == 2) {
+          m = fminf(m, d2_2(ax, ay, b.x, b.y));
+        } else {
+          m = fminf(m, d2_3(ax, ay, az, b.x, b.y, b.z));
+        }
+        t = (t + 1 == nTiles) ? 0 : t + 1;
+      }
+      done += step;
+      pairs += step;
+      float w = m;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) w = fminf(w, __shfl_xor_sync(0xFFFFFFFFu, w, o));
+      if ((tid & 31) == 0) red[tid >> 5] = w;
+      // One thread reads the shared maximum so that every thread of the CTA
+      // takes the same break decision.
+      if (tid == 0) s_thr = threshold_of(ld_relaxed_u64(&sc->max_key));
+      __syncthreads();
+      float bm = red[0];
+#pragma unroll
+      for (int k = 1; k < kEbThreads / 32; ++k) bm = fminf(bm, red[k]);
+      cmin = fminf(cmin, bm);
+      const float thr = s_thr;
+      __syncthreads();
+      if (cmin <= thr) {
+        broke = true;
+        break;
+      }
+    }
+    if (!broke && tid == 0) atomicMax(&sc->max_key, pack_max(cmin, h.ia));
+  }
+  if (tid == 0 && pairs) atomicAdd(&sc->pairs, pairs * kEbTile);
+}
+
+template <int D>
+hd_status run_eb_dim(Ctx& c, const DirInput& in) {
+  using PT = typename EbPt<D>::T;
+  const uint64_t nTiles64 = (in.nB + kEbTile - 1) / kEbTile;
+  if (nTiles64 >= 0xFFFFFFFFull) return fail(c, HD_ERR_INVALID_ARG, "B too large");
+  const uint32_t nTiles = (uint32_t) nTiles64;
+  const uint64_t nPad = nTiles64 * kEbTile;
+  void *pb = nullptr, *ph = nullptr;
+  hd_status s;
+  if ((s = ensure(c, kBufPackB, nPad * sizeof(PT), &pb)) != HD_OK) return s;
+  if ((s = ensure(c, kBufHeavy, in.nA * sizeof(HeavyEntry), &ph)) != HD_OK) return s;
+  DevScalars* sc = scalars(c, in.dir);
+  const uint64_t seed = c.opt.seed;
+  Perm pB{in.nB, pick_multiplier(in.nB, seed + 1), (seed * 7919u) % in.nB};
+  Perm pA{in.nA, pick_multiplier(in.nA, seed + 2), (seed * 104729u) % in.nA};
+
+  mark(c, 0);
+  {
+    int grid = (int) std::min<uint64_t>((nPad + 255) / 256, (uint64_t) c.num_sms * 16);
+    k_eb_pack<D><<<grid, 256, 0, c.stream>>>(in.B, in.nB, pB, (PT*) pb, nPad);
+    if ((s = after_launch(c, "eb_pack")) != HD_OK) return s;
+  }
+  mark(c, 1);
+  // Seeds: the first visited A points, one CTA each, no early break until a
+  // first point completes.
+  const uint32_t n_seed = (uint32_t) std::min<uint64_t>(in.nA, (uint64_t) c.num_sms);
+  k_eb_heavy<D><<<n_seed, kEbThreads, 0, c.stream>>>(in.A, pA, (const PT*) pb, nTiles,
+                                                     sc, nullptr, n_seed, nullptr);
+  if ((s = after_launch(c, "eb_seed")) != HD_OK) return s;
+  mark(c, 2);
+  if (in.nA > n_seed) {
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_eb_main<D>, kEbThreads, 0);
+    occ = std::max(1, occ);
+    uint64_t per_cta = (uint64_t) kEbThreads * kEbSlots;
+    uint64_t want = (in.nA - n_seed + per_cta - 1) / per_cta;
+    int grid = (int) std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t) c.num_sms * occ));
+    uint32_t capTiles = std::max<uint32_t>(1, kCapPairs / kEbTile);
+    k_eb_main<D><<<grid, kEbThreads, 0, c.stream>>>(in.A, pA, n_seed, in.nA, (const PT*) pb,
+                                                    nTiles, capTiles, sc,
+                                                    (HeavyEntry*) ph, (uint32_t) in.nA);
+    if ((s = after_launch(c, "eb_main")) != HD_OK) return s;
+    mark(c, 3);
+    k_eb_heavy<D><<<c.num_sms * 4, kEbThreads, 0, c.stream>>>(
+        in.A, pA, (const PT*) pb, nTiles, sc, (const HeavyEntry*) ph, 0, &sc->heavy_count);
+    if ((s = after_launch(c, "eb_heavy")) != HD_OK) return s;
+  } else {
+    mark(c, 3);
+  }
+  mark(c, 4);
+  return certify(c, in);
+}
+
+}  // namespace
+
+hd_status run_eb(Ctx& c, const DirInput& in) {
+  if (in.dims == 2) return run_eb_dim<2>(c, in);
+  if (in.dims == 3) return run_eb_dim<3>(c, in);
+  return run_brute(c, in);
+}
+
+}  // namespace hdg

@@ -1,0 +1,19 @@
+// Variants not built yet report HD_ERR_UNSUPPORTED.
+#include "hd_internal.h"
+namespace hdg {
+hd_status run_brute(Ctx& c, const DirInput&) { return fail(c, HD_ERR_UNSUPPORTED, "brute not built"); }
+hd_status run_lbvh(Ctx& c, const DirInput&) { return fail(c, HD_ERR_UNSUPPORTED, "lbvh not built"); }
+hd_status run_grid(Ctx& c, const DirInput&) { return fail(c, HD_ERR_UNSUPPORTED, "grid not built"); }
+hd_status run_bf16(Ctx& c, const DirInput&, DirResult*) { return fail(c, HD_ERR_UNSUPPORTED, "bf16 not built"); }
+hd_status select_variant(Ctx&, const DirInput&, int* v) { *v = HD_VARIANT_EB; return HD_OK; }
+}
+extern "C" {
+hd_status hd_solve_batch(hd_ctx* c, const float*, uint64_t, const float*, uint64_t, int,
+                         const hd_problem*, uint64_t, uint32_t, hd_batch_result*) {
+  return hdg::fail(*c, HD_ERR_UNSUPPORTED, "batch not built");
+}
+hd_status hd_solve_batch_plain(hd_ctx* c, const float*, uint64_t, const float*, uint64_t, int,
+                               const hd_problem*, uint64_t, uint32_t, hd_batch_result*) {
+  return hdg::fail(*c, HD_ERR_UNSUPPORTED, "batch not built");
+}
+}

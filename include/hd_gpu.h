@@ -1,0 +1,176 @@
+/*
+ * hd_gpu.h — C ABI of libhdgpu.so, the GB300 (sm_103a) Hausdorff-distance
+ * engine.
+ *
+ * It replaces the reference's algorithm seam
+ *   hd::HausdorffDistance<COORD_T,N_DIMS>::CalculateDistance(...)
+ *   (src/hausdorff_distance.h:21-32)
+ * and the variant factory + repeat loop that drive it
+ *   (src/run_hausdorff_distance.cu:220-357).
+ * Plain pointers and sizes only; no C++ types cross the boundary, no
+ * exceptions escape.  Every call returns an hd_status.
+ *
+ * Semantics (identical to the reference's -execution=cpu result):
+ *   directed   h(A,B) = max_{a in A} min_{b in B} ||a - b||
+ *   undirected H(A,B) = max(h(A,B), h(B,A))
+ * Squared distances are formed in FP32 as the reference forms them
+ * (src/geoms/distance.h:17-24: per-dimension difference, squared, summed left
+ * to right, no FMA), min/max are exact, and hd_f32 is the correctly rounded
+ * float square root: bit-identical to the reference CPU early-break.  The
+ * certifying pair (ia, ib) achieves it; hd is its distance recomputed in FP64.
+ *
+ * Threading: one hd_ctx per host thread.  A context owns one CUDA stream
+ * (or borrows the caller's, see hd_set_stream) and a cached device arena.
+ * Inputs are const: unlike the reference (which shuffles its inputs in place,
+ * early_break.h:50-52), nothing the caller passes is modified.
+ */
+#ifndef HD_GPU_H
+#define HD_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define HD_API __attribute__((visibility("default")))
+#else
+#define HD_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum hd_status {
+  HD_OK = 0,
+  HD_ERR_INVALID_ARG = 1,    /* null pointer, zero size, bad n_dims/flags     */
+  HD_ERR_OOM = 2,            /* device or pinned allocation failed            */
+  HD_ERR_DEVICE_TIMEOUT = 3, /* a bounded device wait ran out (status word)   */
+  HD_ERR_CUDA = 4,           /* any other CUDA runtime error                  */
+  HD_ERR_UNSUPPORTED = 5,    /* variant not available for these inputs       */
+  HD_ERR_NO_DEVICE = 6       /* no CUDA device or the library was built for   */
+                             /* another architecture                          */
+} hd_status;
+
+/* Variants.  The reference's -variant names map as: eb -> HD_VARIANT_EB,
+ * hybrid -> HD_VARIANT_AUTO, rt -> HD_VARIANT_LBVH (GB300 has no RT cores;
+ * the OptiX search of src/hd_impl/hausdorff_distance_ray_tracing.h:63-236 is
+ * rebuilt as a plain-CUDA LBVH). */
+typedef enum hd_variant {
+  HD_VARIANT_AUTO = 0,  /* sampler-driven selector (hybrid.h:86-409 analogue) */
+  HD_VARIANT_EB = 1,    /* persistent early-break scan (early_break.h:117-219)*/
+  HD_VARIANT_GRID = 2,  /* Morton-sorted uniform grid + ring search           */
+  HD_VARIANT_LBVH = 3,  /* LBVH nearest-neighbour with early break            */
+  HD_VARIANT_BF16 = 4,  /* split-BF16 tcgen05 tiles + exact FP32 recheck      */
+  HD_VARIANT_BRUTE = 5  /* plain FP32 all-pairs (no early break)              */
+} hd_variant;
+
+/* hd_solve flags */
+#define HD_DIRECTED 0u
+#define HD_UNDIRECTED 1u   /* max(h(A,B), h(B,A))                              */
+#define HD_DEVICE_PTRS 2u  /* A and B are device pointers (no H2D copy)        */
+#define HD_COUNT_PAIRS 4u  /* instrumented run: fill visited_pairs/nodes       */
+#define HD_TIMING 8u       /* record per-phase CUDA-event times in hd_result   */
+
+typedef struct hd_options {
+  int device;              /* CUDA device ordinal                             */
+  int variant;             /* hd_variant used when a call does not override   */
+  uint64_t seed;           /* visit-order permutation / sampler seed          */
+  double sample_rate;      /* selector sample fraction of |A| (hybrid.h:134)  */
+  uint32_t n_points_cell;  /* grid: target points per cell (uniform_grid.h:222)*/
+  uint32_t leaf_size;      /* LBVH: points per leaf (<= 32)                    */
+  uint32_t eb_only_threshold; /* selector: p80 sample iterations below which  */
+                              /* plain EB is chosen (hybrid.h:171); 0 = table */
+  uint32_t reserved[8];
+} hd_options;
+
+typedef struct hd_result {
+  double hd;               /* FP64 distance of the certifying pair            */
+  float hd_f32;            /* FP32 result, bit-identical to reference CPU EB   */
+  int32_t direction;       /* 0: pair is (A[ia], B[ib]); 1: (B[ib'], A[ia'])  */
+                           /* i.e. for direction 1, ia indexes B, ib indexes A */
+  uint64_t ia, ib;         /* certifying pair indices (caller's order)         */
+  double hd_ab, hd_ba;     /* FP64 directed distances (hd_ba < 0 if directed)  */
+  uint64_t visited_pairs;  /* pair distances evaluated (HD_COUNT_PAIRS)        */
+  uint64_t visited_nodes;  /* index nodes/cells visited (HD_COUNT_PAIRS)       */
+  double ms;               /* device time of the whole solve (HD_TIMING)       */
+  double phase_ms[8];      /* HD_TIMING: prep, build, sample, query, tail,     */
+                           /* certify, copy-in, other                          */
+  int32_t variant_used;    /* hd_variant actually run (direction A->B)         */
+  int32_t variant_used_ba; /* and for B->A when undirected                     */
+  double err_bound;        /* BF16: bound on |approx - exact| squared distance */
+  uint64_t rechecked;      /* BF16: rows rechecked exactly in FP32             */
+} hd_result;
+
+/* One problem of a batch: A[offset_a .. offset_a+n_a), B[offset_b ..).
+ * Offsets are in points, into the arrays given to hd_solve_batch. */
+typedef struct hd_problem {
+  uint64_t offset_a, n_a;
+  uint64_t offset_b, n_b;
+} hd_problem;
+
+typedef struct hd_batch_result {
+  float hd_f32;            /* per-problem result (same semantics as hd_result) */
+  uint32_t ia, ib;         /* certifying pair, relative to the problem's start */
+  int32_t direction;
+} hd_batch_result;
+
+typedef struct hd_ctx hd_ctx;
+
+/* Fills *opt with defaults (device 0, AUTO, seed 0, sample_rate 0.01,
+ * n_points_cell 8, leaf_size 16). */
+HD_API void hd_default_options(hd_options* opt);
+
+/* Creates a context on opt->device (opt may be NULL for defaults).
+ * Replaces the variant construction in run_hausdorff_distance.cu:220-334. */
+HD_API hd_status hd_create(hd_ctx** ctx, const hd_options* opt);
+
+/* Destroys the context and releases its arena and stream. */
+HD_API hd_status hd_destroy(hd_ctx* ctx);
+
+/* Makes the context launch on a caller-owned stream (a cudaStream_t passed
+ * as void*); NULL restores the context's own stream. */
+HD_API hd_status hd_set_stream(hd_ctx* ctx, void* cuda_stream);
+
+/* Computes the Hausdorff distance of A (n_a x n_dims floats, row-major) and
+ * B (n_b x n_dims).  n_dims 2 or 3 for every variant; any n_dims in [1, 256]
+ * for EB, BRUTE and BF16 (BF16 needs n_dims % 16 == 0).  variant < 0 uses the
+ * context default.  Synchronous: returns after the result is on the host.
+ * Replaces HausdorffDistance::CalculateDistance (hausdorff_distance.h:21-32),
+ * both the CPU and the GPU overload. */
+HD_API hd_status hd_solve(hd_ctx* ctx, const float* A, uint64_t n_a, const float* B,
+                   uint64_t n_b, int n_dims, uint32_t flags, int variant,
+                   hd_result* out);
+
+/* Solves many independent problems (2-D or 3-D) in one graph-captured
+ * persistent launch.  A/B hold all problems' points back to back; probs[i]
+ * gives each problem's ranges; out[i] receives its result.  flags as for
+ * hd_solve (HD_UNDIRECTED, HD_DEVICE_PTRS).  No counterpart in the
+ * reference, which solves one pair per hd_exec run. */
+HD_API hd_status hd_solve_batch(hd_ctx* ctx, const float* A, uint64_t total_a,
+                         const float* B, uint64_t total_b, int n_dims,
+                         const hd_problem* probs, uint64_t n_problems,
+                         uint32_t flags, hd_batch_result* out);
+
+/* Same batch computed with one plain early-break launch per problem and
+ * direction (the per-pair baseline the batched form is compared against). */
+HD_API hd_status hd_solve_batch_plain(hd_ctx* ctx, const float* A, uint64_t total_a,
+                               const float* B, uint64_t total_b, int n_dims,
+                               const hd_problem* probs, uint64_t n_problems,
+                               uint32_t flags, hd_batch_result* out);
+
+/* Message for the last failing call on this context (never NULL). */
+HD_API const char* hd_last_error(hd_ctx* ctx);
+
+/* Name of a status code. */
+HD_API const char* hd_status_string(hd_status s);
+
+/* Number of kernels of this library launched by the context so far. */
+HD_API uint64_t hd_kernel_launches(hd_ctx* ctx);
+
+/* Library version string. */
+HD_API const char* hd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HD_GPU_H */

@@ -1,0 +1,23 @@
+#!/usr/bin/env bash
+# Builds the reference's own CPU early-break path from its sources where they
+# lie (read-only) into oracle/_ref/ref_eb.  Test infrastructure: used to pin
+# the oracle restatement and to generate tests/golden/.  Needs nvcc (the
+# reference header mixes host code with thrust/CUDA device lambdas).  The
+# shims in oracle/shim/ stand in for glog, nlohmann::json, HdrHistogram and
+# OptiX, none of which the CPU path calls at run time.
+set -euo pipefail
+here="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+ref="${HD_REFERENCE_SRC:-/root/reference/src}"
+if [ ! -f "$ref/hd_impl/hausdorff_distance_early_break.h" ]; then
+  echo "reference sources not found at $ref; skipping oracle/_ref" >&2
+  exit 0
+fi
+mkdir -p "$here/_ref"
+# --fmad=false and -ffp-contract=off: the reference builds with fmad off
+# (CMakeLists.txt:122) and its squared distances must not be contracted.
+nvcc -std=c++17 -O2 --extended-lambda --expt-relaxed-constexpr --fmad=false \
+  -Xcompiler -ffp-contract=off -Xcompiler -pthread \
+  -gencode arch=compute_103a,code=sm_103a \
+  -I "$here/shim" -I "$ref" -include "$here/shim/prelude.h" \
+  "$here/ref_eb_main.cu" -o "$here/_ref/ref_eb"
+echo "built $here/_ref/ref_eb"

@@ -1,0 +1,116 @@
+"""Generates the golden vectors in tests/golden/ from the reference's own CPU
+early-break implementation (src/hd_impl/hausdorff_distance_early_break.h:44-115),
+compiled from the reference sources by oracle/build_ref.sh into
+oracle/_ref/ref_eb.
+
+For every case it writes the two inputs in the reference's point-cache layout
+(inputs/<name>_{a,b}.bin) and records, in golden.json, what the reference
+returned: the float distance (and its bit pattern) and the compared-pair
+count for n_threads=1 (deterministic: it depends only on the seeded shuffle),
+and the distance for n_threads=4.
+
+Run from the repository root, in a container that has the reference sources:
+    oracle/build_ref.sh && python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from hausdorffdistance_gb300 import synth  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref", "ref_eb")
+
+
+def cases():
+    rng = np.random.Generator(np.random.PCG64(20240601))
+    out = []
+
+    def add(name, a, b, dims, seed=0):
+        out.append((name, np.ascontiguousarray(a, np.float32),
+                    np.ascontiguousarray(b, np.float32), dims, seed))
+
+    a, b = synth.uniform2d(3000, seed=11)
+    add("uniform2d_3k_ab", a, b, 2, 0)
+    add("uniform2d_3k_ba", b, a, 2, 7)
+    a, b = synth.clusters3d(4000, seed=12)
+    add("clusters3d_4k_ab", a, b, 3, 0)
+    add("clusters3d_4k_ba", b, a, 3, 3)
+    add("uniform3d_2000x1500", rng.random((2000, 3)), rng.random((1500, 3)), 3, 5)
+    add("uniform2d_1000x1000", rng.random((1000, 2)), rng.random((1000, 2)), 2, 1)
+    a, b = synth.planes3d(3000, seed=13, n_planes=20)
+    add("planes3d_3k_ab", a, b, 3, 0)
+    add("planes3d_3k_ba", b, a, 3, 0)
+    a, b, off = synth.polylines(sizes=[300, 8], seed=14)
+    add("polyline_300", a[:300], b[:300], 2, 0)
+    add("polyline_8", a[300:], b[300:], 2, 0)
+    # Edge cases: single points, one side single, exact duplicates.
+    add("single_single_2d", [[0.25, 0.5]], [[0.75, -0.5]], 2, 0)
+    add("single_vs_many_3d", [[0.5, 0.5, 0.5]], rng.random((100, 3)), 3, 0)
+    add("many_vs_single_3d", rng.random((100, 3)), [[0.5, 0.5, 0.5]], 3, 0)
+    d = rng.random((500, 2))
+    add("identical_2d", d, d[rng.permutation(500)], 2, 0)
+    # Ties: integer lattice against a shifted lattice, all distances equal.
+    g = np.stack(np.meshgrid(np.arange(12), np.arange(12)), -1).reshape(-1, 2)
+    add("lattice_ties_2d", g, g + 0.5, 2, 0)
+    g3 = np.stack(np.meshgrid(np.arange(6), np.arange(6), np.arange(6)), -1).reshape(-1, 3)
+    add("lattice_ties_3d", g3, g3[::2] + 0.5, 3, 0)
+    # Degenerate extents: all-equal points, collinear sets, coplanar 3-D.
+    add("all_equal_2d", np.full((50, 2), 3.0), np.full((40, 2), 3.0), 2, 0)
+    t = rng.random(400)
+    add("collinear_2d", np.stack([t, 2 * t], 1), np.stack([t[::-1] * 0.9, 1.8 * t[::-1]], 1), 2, 0)
+    add("coplanar_3d", np.c_[rng.random((300, 2)), np.zeros(300)],
+        np.c_[rng.random((200, 2)), np.full(200, 0.1)], 3, 0)
+    # Large offsets and negative coordinates.
+    add("offset_large_3d", rng.random((800, 3)) * 10 + 1.0e4,
+        rng.random((700, 3)) * 10 + 1.0e4 - 3.0, 3, 0)
+    add("negative_2d", -rng.random((600, 2)) * 5, -rng.random((900, 2)) * 5 + 0.25, 2, 0)
+    return out
+
+
+def run_ref(a_path, b_path, dims, seed, threads):
+    r = subprocess.run([REF, a_path, b_path, str(dims), str(seed), str(threads)],
+                       check=True, capture_output=True, text=True)
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1]
+    return json.loads(line)["runs"][0]
+
+
+def main():
+    if not os.path.exists(REF):
+        sys.exit("oracle/_ref/ref_eb is missing: run oracle/build_ref.sh first")
+    inp = os.path.join(HERE, "inputs")
+    os.makedirs(inp, exist_ok=True)
+    records = []
+    for name, a, b, dims, seed in cases():
+        pa = os.path.join(inp, f"{name}_a.bin")
+        pb = os.path.join(inp, f"{name}_b.bin")
+        synth.write_bin(pa, a)
+        synth.write_bin(pb, b)
+        r1 = run_ref(pa, pb, dims, seed, 1)
+        r4 = run_ref(pa, pb, dims, seed, 4)
+        records.append({
+            "name": name, "dims": dims, "seed": seed,
+            "n_a": int(a.shape[0]), "n_b": int(b.shape[0]),
+            "a": f"inputs/{name}_a.bin", "b": f"inputs/{name}_b.bin",
+            "hd": r1["hd"], "hd_bits": r1["hd_bits"],
+            "compared_pairs_t1": r1["compared_pairs"],
+            "hd_bits_t4": r4["hd_bits"],
+        })
+        print(name, r1["hd"], r1["compared_pairs"])
+    with open(os.path.join(HERE, "golden.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py",
+                   "reference": "src/hd_impl/hausdorff_distance_early_break.h:44-115 "
+                                "built by oracle/build_ref.sh",
+                   "cases": records}, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

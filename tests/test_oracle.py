@@ -1,0 +1,85 @@
+"""The oracle (oracle/hd_oracle.cpp) against golden vectors produced by the
+reference's own CPU early-break code (tests/golden/make_golden.py)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import hd_oracle
+from hausdorffdistance_gb300 import synth
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = json.load(open(os.path.join(HERE, "golden", "golden.json")))
+CASES = GOLDEN["cases"]
+
+
+def load_case(c):
+    a = synth.read_bin(os.path.join(HERE, "golden", c["a"]), c["dims"])
+    b = synth.read_bin(os.path.join(HERE, "golden", c["b"]), c["dims"])
+    return a, b
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_eb_port_matches_reference_bit_for_bit(case):
+    a, b = load_case(case)
+    r = hd_oracle.eb(a, b, seed=case["seed"], n_threads=1)
+    assert int(np.float32(r["hd"]).view(np.uint32)) == case["hd_bits"]
+    # The compared-pair count depends on the seeded shuffle of both inputs and
+    # on the break rule, so equality pins the whole restatement.
+    assert r["compared_pairs"] == case["compared_pairs_t1"]
+    r4 = hd_oracle.eb(a, b, seed=case["seed"], n_threads=4)
+    assert int(np.float32(r4["hd"]).view(np.uint32)) == case["hd_bits_t4"]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_exact_oracle_matches_reference(case):
+    a, b = load_case(case)
+    h2, ia, ib = hd_oracle.exact(a, b, 32)
+    assert int(np.sqrt(np.float32(h2)).view(np.uint32)) == case["hd_bits"]
+    # Certifying pair: achieves the maximum and is A[ia]'s nearest neighbour.
+    assert hd_oracle.dist2_f32(a[ia], b[ib]) == np.float32(h2)
+    d = ((a[ia].astype(np.float64) - b.astype(np.float64)) ** 2).sum(1)
+    assert d.min() == pytest.approx(float(h2), rel=1e-6, abs=1e-30)
+
+
+def brute_f64(a, b):
+    a = a.astype(np.float64)
+    b = b.astype(np.float64)
+    best = np.full(len(a), np.inf)
+    for s in range(0, len(b), 4096):
+        d = ((a[:, None, :] - b[None, s:s + 4096, :]) ** 2).sum(-1)
+        best = np.minimum(best, d.min(1))
+    return best.max(), int(best.argmax())
+
+
+@pytest.mark.parametrize("dims,na,nb,seed", [(2, 700, 900, 1), (3, 800, 500, 2),
+                                             (5, 300, 400, 3), (64, 200, 300, 4)])
+def test_exact_fp64_against_numpy(dims, na, nb, seed):
+    rng = np.random.default_rng(seed)
+    a = rng.random((na, dims)).astype(np.float32)
+    b = rng.random((nb, dims)).astype(np.float32)
+    h2, ia, ib = hd_oracle.exact(a, b, 64)
+    want, wia = brute_f64(a, b)
+    assert h2 == pytest.approx(want, rel=1e-12)
+    assert ia == wia
+
+
+def test_exact_clustered_kdtree_vs_brute():
+    a, b = synth.clusters3d(20000, seed=9)
+    h2, ia, ib = hd_oracle.exact(a, b, 32)
+    a64 = a.astype(np.float64)
+    # Check the certifying pair by brute force on A[ia] and a sample of rows.
+    d = ((a64[ia] - b) ** 2).sum(1)
+    assert d.argmin() == ib
+    rows = np.random.default_rng(0).choice(len(a), 200, replace=False)
+    for r in rows:
+        assert ((a64[r] - b) ** 2).sum(1).min() <= h2 * (1 + 1e-6)
+
+
+def test_bounded_sample_eb():
+    a, b = synth.uniform2d(5000, seed=5)
+    full = hd_oracle.eb(a, b, n_threads=2)
+    part = hd_oracle.eb(a, b, n_threads=2, limit_a=500)
+    assert part["compared_pairs"] < full["compared_pairs"]
+    assert part["hd"] <= full["hd"]

@@ -1,0 +1,126 @@
+"""GPU parity: libhdgpu.so through its C ABI against the golden vectors of the
+reference's own CPU early-break and against the oracle.
+
+Bar: the FP32 result is bit-identical to the reference's -execution=cpu
+result; the certifying pair (ia, ib) achieves it and ib is A[ia]'s nearest
+neighbour (ties allowed); the FP64 distance is within 1e-6 relative of the
+FP64 oracle."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import hd_oracle
+from hausdorffdistance_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = json.load(open(os.path.join(HERE, "golden", "golden.json")))["cases"]
+SPATIAL = ["eb", "auto"]
+REL_TOL_F64 = 1e-6
+
+
+def load_case(c):
+    a = synth.read_bin(os.path.join(HERE, "golden", c["a"]), c["dims"])
+    b = synth.read_bin(os.path.join(HERE, "golden", c["b"]), c["dims"])
+    return a, b
+
+
+def check_pair(a, b, r, d2_expected):
+    """The certifying pair achieves d2 and is the argmin of its row."""
+    src, dst = (a, b) if r.direction == 0 else (b, a)
+    ia, ib = int(r.ia), int(r.ib)
+    assert hd_oracle.dist2_f32(src[ia], dst[ib]) == np.float32(d2_expected)
+    diff = src[ia][None, :].astype(np.float32) - dst.astype(np.float32)
+    d2 = (diff * diff).sum(1, dtype=np.float64)
+    assert d2.min() == pytest.approx(float(d2_expected), rel=1e-6, abs=1e-30)
+
+
+@pytest.mark.parametrize("variant", SPATIAL)
+@pytest.mark.parametrize("case", GOLDEN, ids=[c["name"] for c in GOLDEN])
+def test_golden_directed(engine, case, variant):
+    a, b = load_case(case)
+    r = engine.solve(a, b, variant=variant)
+    got = int(np.float32(r.hd_f32).view(np.uint32))
+    assert got == case["hd_bits"], (r.hd_f32, case["hd"])
+    check_pair(a, b, r, hd_oracle.exact(a, b, 32)[0])
+    want64 = hd_oracle.hd_f64(a, b)
+    assert r.hd == pytest.approx(want64, rel=REL_TOL_F64, abs=1e-12)
+
+
+@pytest.mark.parametrize("variant", SPATIAL)
+@pytest.mark.parametrize("dims", [2, 3])
+def test_undirected_random(engine, variant, dims):
+    rng = np.random.default_rng(100 + dims)
+    a = rng.random((3000, dims)).astype(np.float32)
+    b = (rng.random((2500, dims)) * 1.1).astype(np.float32)
+    r = engine.solve(a, b, undirected=True, variant=variant)
+    want = hd_oracle.hd_f32(a, b, undirected=True)
+    assert np.float32(r.hd_f32) == want["hd_f32"]
+    assert r.direction == want["direction"]
+    check_pair(a, b, r, want["d2"])
+    assert r.hd == pytest.approx(hd_oracle.hd_f64(a, b, True), rel=REL_TOL_F64)
+    assert r.hd_ab == pytest.approx(hd_oracle.hd_f64(a, b), rel=REL_TOL_F64)
+    assert r.hd_ba == pytest.approx(hd_oracle.hd_f64(b, a), rel=REL_TOL_F64)
+
+
+@pytest.mark.parametrize("variant", SPATIAL)
+@pytest.mark.parametrize("na,nb", [(1, 1), (1, 1000), (1000, 1), (257, 255), (33, 7000),
+                                   (70000, 300)])
+def test_sizes_ragged(engine, variant, na, nb):
+    rng = np.random.default_rng(na * 7 + nb)
+    a = rng.normal(size=(na, 3)).astype(np.float32)
+    b = rng.normal(size=(nb, 3)).astype(np.float32)
+    r = engine.solve(a, b, variant=variant)
+    want = hd_oracle.hd_f32(a, b)
+    assert np.float32(r.hd_f32) == want["hd_f32"]
+    check_pair(a, b, r, want["d2"])
+
+
+@pytest.mark.parametrize("variant", SPATIAL)
+def test_config1_workload_both_directions(engine, variant):
+    a, b = synth.uniform2d(200_000, seed=1)
+    r = engine.solve(a, b, undirected=True, variant=variant)
+    want = hd_oracle.hd_f32(a, b, undirected=True)
+    assert np.float32(r.hd_f32) == want["hd_f32"]
+    check_pair(a, b, r, want["d2"])
+
+
+@pytest.mark.parametrize("variant", SPATIAL)
+def test_device_pointers_match_host(engine, variant):
+    torch = pytest.importorskip("torch")
+    a, b = synth.clusters3d(50_000, seed=8)
+    rh = engine.solve(a, b, undirected=True, variant=variant)
+    ta = torch.from_numpy(a).cuda()
+    tb = torch.from_numpy(b).cuda()
+    rd = engine.solve(ta, tb, undirected=True, variant=variant)
+    assert rd.hd_f32 == rh.hd_f32 and rd.hd == rh.hd
+    # Inputs are never modified (the reference shuffles them in place).
+    assert np.array_equal(ta.cpu().numpy(), a) and np.array_equal(tb.cpu().numpy(), b)
+
+
+def test_reference_interface_classes():
+    import hausdorffdistance_gb300 as hd
+    a, b = synth.uniform2d(5000, seed=2)
+    want = hd_oracle.eb(a, b, seed=0, n_threads=1)["hd"]
+    for cls in (hd.HausdorffDistanceEarlyBreak, hd.HausdorffDistanceHybrid):
+        impl = cls(seed=0)
+        got = impl.CalculateDistance(a.copy(), b.copy())
+        assert got == want
+        st = impl.get_stats()
+        assert {"Algorithm", "Execution", "ReportedTime"} <= set(st)
+        assert st["Execution"] == "GPU" and st["ReportedTime"] > 0
+
+
+def test_invalid_arguments_raise(engine):
+    import hausdorffdistance_gb300 as hd
+    a = np.zeros((0, 2), np.float32)
+    b = np.ones((5, 2), np.float32)
+    with pytest.raises(hd.HDError) as ei:
+        engine.solve(a, b)
+    assert ei.value.status == 1
+    with pytest.raises(hd.HDError) as ei:
+        engine.solve(np.ones((5, 5), np.float32), np.ones((5, 5), np.float32), variant="lbvh")
+    assert ei.value.status == 5
