@@ -82,8 +82,11 @@ DevScalars* scalars(Ctx& c, int dir) {
 
 void mark(Ctx& c, int k) {
   if (!c.timing || k < 0 || k >= 12) return;
-  cudaEventRecord(c.ev[k], c.stream);
-  c.ev_used = std::max(c.ev_used, k + 1);
+  cudaEventRecord(c.ev[c.ev_base + k], c.stream);
+}
+
+static void mark_abs(Ctx& c, int idx) {
+  if (c.timing) cudaEventRecord(c.ev[idx], c.stream);
 }
 
 uint64_t pick_multiplier(uint64_t n, uint64_t seed) {
@@ -176,6 +179,7 @@ __global__ void k_finalize(const float* __restrict__ A, const float* __restrict_
 }  // namespace
 
 hd_status certify(Ctx& c, const DirInput& in) {
+  mark(c, 5);
   DevScalars* sc = scalars(c, in.dir);
   int grid = (int) std::min<uint64_t>((in.nB + 255) / 256, (uint64_t) c.num_sms * 4);
   grid = std::max(grid, 1);
@@ -188,7 +192,7 @@ hd_status certify(Ctx& c, const DirInput& in) {
 
 hd_status init_scalars(Ctx& c) {
   void* p = nullptr;
-  hd_status s = ensure(c, kBufScalars, 2 * sizeof(DevScalars), &p);
+  hd_status s = ensure(c, kBufScalars, scalars_bytes(), &p);
   if (s != HD_OK) return s;
   k_init_scalars<<<1, 32, 0, c.stream>>>((DevScalars*) p, 2);
   return after_launch(c, "init_scalars");
@@ -356,12 +360,13 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   memset(out, 0, sizeof(*out));
   out->hd_ba = -1.0;
   c->timing = (flags & HD_TIMING) != 0;
-  c->ev_used = 0;
+  c->sorted_valid = false;
+  c->ev_base = 0;
 
   hd_status s;
   const float* dA = A;
   const float* dB = B;
-  mark(*c, 11);  // start of the whole call (copies included)
+  mark_abs(*c, 24);  // start of the whole call (copies included)
   if (!(flags & HD_DEVICE_PTRS)) {
     if ((s = copy_in(*c, A, n_a, n_dims, kBufA, &dA)) != HD_OK) return s;
     if ((s = copy_in(*c, B, n_b, n_dims, kBufB, &dB)) != HD_OK) return s;
@@ -369,40 +374,25 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   if ((s = init_scalars(*c)) != HD_OK) return s;
   const bool undirected = (flags & HD_UNDIRECTED) != 0;
   const bool count = (flags & HD_COUNT_PAIRS) != 0;
+  const int ndir = undirected ? 2 : 1;
   DirResult ex[2];
   int used[2] = {variant, -1};
-  float ms_phase[2][8] = {};
-  for (int d = 0; d < (undirected ? 2 : 1); ++d) {
+  for (int d = 0; d < ndir; ++d) {
     DirInput in{d == 0 ? dA : dB, d == 0 ? n_a : n_b, d == 0 ? dB : dA,
                 d == 0 ? n_b : n_a, n_dims, d, count};
-    c->ev_used = 0;
-    mark(*c, 10);
+    c->ev_base = 12 * d;
+    mark(*c, 0);
     if ((s = run_direction(*c, in, variant, &used[d], &ex[d])) != HD_OK) return s;
-    mark(*c, 5);
-    if (c->timing) {
-      cudaError_t e = cudaEventSynchronize(c->ev[5]);
-      if (e != cudaSuccess) return cuda_fail(*c, e, "solve");
-      float t;
-      // Phases: 0 prep (10->0), 1 build (0->1), 2 sample/seed (1->2),
-      // 3 query/main (2->3), 4 tail (3->4), 5 certify (4->5).
-      const int from[6] = {10, 0, 1, 2, 3, 4};
-      const int to[6] = {0, 1, 2, 3, 4, 5};
-      for (int p = 0; p < 6; ++p) {
-        if (cudaEventElapsedTime(&t, c->ev[from[p]], c->ev[to[p]]) == cudaSuccess)
-          ms_phase[d][p] = t;
-        else
-          (void) cudaGetLastError();
-      }
-    }
+    mark(*c, 6);
   }
   HostScalars* h = reinterpret_cast<HostScalars*>(c->host_pinned);
   cudaError_t e = cudaMemcpyAsync(h, c->bufs[kBufScalars].p, sizeof(HostScalars),
                                   cudaMemcpyDeviceToHost, c->stream);
   if (e != cudaSuccess) return cuda_fail(*c, e, "copy result");
-  mark(*c, 9);
+  mark_abs(*c, 25);
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(*c, e, "solve");
-  if ((s = check_status(*c, *h, undirected ? 2 : 1)) != HD_OK) return s;
+  if ((s = check_status(*c, *h, ndir)) != HD_OK) return s;
 
   const DevScalars& r0 = h->s[0];
   out->hd_ab = std::sqrt(r0.d2_64);
@@ -421,16 +411,28 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   out->ib = w.ib;
   out->visited_pairs = r0.pairs + (undirected ? h->s[1].pairs : 0);
   out->visited_nodes = r0.nodes + (undirected ? h->s[1].nodes : 0);
+  out->visited_leaves = r0.leaves + (undirected ? h->s[1].leaves : 0);
   out->variant_used = used[0];
   out->variant_used_ba = undirected ? used[1] : -1;
   out->err_bound = std::max(ex[0].err_bound, ex[1].err_bound);
   out->rechecked = ex[0].rechecked + ex[1].rechecked;
   if (c->timing) {
     float t = 0;
-    if (cudaEventElapsedTime(&t, c->ev[11], c->ev[9]) == cudaSuccess) out->ms = t;
-    for (int p = 0; p < 6; ++p) out->phase_ms[p] = ms_phase[0][p] + ms_phase[1][p];
+    if (cudaEventElapsedTime(&t, c->ev[24], c->ev[25]) == cudaSuccess) out->ms = t;
+    // Phases per direction (event k marks the end of phase k-1):
+    // 0 prep/sort, 1 index build, 2 sample or seed, 3 main pass, 4 tail,
+    // 5 certify.
+    const int from[6] = {0, 1, 2, 3, 4, 5};
+    const int to[6] = {1, 2, 3, 4, 5, 6};
+    for (int d = 0; d < ndir; ++d)
+      for (int p = 0; p < 6; ++p) {
+        if (cudaEventElapsedTime(&t, c->ev[12 * d + from[p]], c->ev[12 * d + to[p]]) ==
+            cudaSuccess)
+          out->phase_ms[p] += t;
+        else
+          (void) cudaGetLastError();
+      }
   }
-  (void) count;
   return HD_OK;
 }
 

@@ -339,20 +339,20 @@ hd_status run_eb_dim(Ctx& c, const DirInput& in) {
   Perm pB{in.nB, pick_multiplier(in.nB, seed + 1), (seed * 7919u) % in.nB};
   Perm pA{in.nA, pick_multiplier(in.nA, seed + 2), (seed * 104729u) % in.nA};
 
-  mark(c, 0);
   {
     int grid = (int) std::min<uint64_t>((nPad + 255) / 256, (uint64_t) c.num_sms * 16);
     k_eb_pack<D><<<grid, 256, 0, c.stream>>>(in.B, in.nB, pB, (PT*) pb, nPad);
     if ((s = after_launch(c, "eb_pack")) != HD_OK) return s;
   }
   mark(c, 1);
+  mark(c, 2);
   // Seeds: the first visited A points, one CTA each, no early break until a
   // first point completes.
   const uint32_t n_seed = (uint32_t) std::min<uint64_t>(in.nA, (uint64_t) c.num_sms);
   k_eb_heavy<D><<<n_seed, kEbThreads, 0, c.stream>>>(in.A, pA, (const PT*) pb, nTiles,
                                                      sc, nullptr, n_seed, nullptr);
   if ((s = after_launch(c, "eb_seed")) != HD_OK) return s;
-  mark(c, 2);
+  mark(c, 3);
   if (in.nA > n_seed) {
     int occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_eb_main<D>, kEbThreads, 0);
@@ -365,14 +365,13 @@ hd_status run_eb_dim(Ctx& c, const DirInput& in) {
                                                     nTiles, capTiles, sc,
                                                     (HeavyEntry*) ph, (uint32_t) in.nA);
     if ((s = after_launch(c, "eb_main")) != HD_OK) return s;
-    mark(c, 3);
+    mark(c, 4);
     k_eb_heavy<D><<<c.num_sms * 4, kEbThreads, 0, c.stream>>>(
         in.A, pA, (const PT*) pb, nTiles, sc, (const HeavyEntry*) ph, 0, &sc->heavy_count);
     if ((s = after_launch(c, "eb_heavy")) != HD_OK) return s;
   } else {
-    mark(c, 3);
+    mark(c, 4);
   }
-  mark(c, 4);
   return certify(c, in);
 }
 

@@ -17,7 +17,7 @@ struct DevScalars {
   unsigned long long next;        // work-queue head (visit index)
   unsigned long long pairs;       // pair distances evaluated
   unsigned long long nodes;       // index nodes / cells visited
-  unsigned long long next2;       // second queue head
+  unsigned long long leaves;      // leaf / cell visits (HD_COUNT_PAIRS)
   uint32_t heavy_count;           // deferred points
   uint32_t status;                // error bits (kErr*)
   uint32_t sample_count;
@@ -42,13 +42,18 @@ enum BufSlot {
   kBufPackB,      // packed / permuted B (float2, float4 or padded rows)
   kBufPackA,
   kBufHeavy,      // deferred early-break entries
-  kBufScalars,    // DevScalars[2] (one per direction)
-  kBufKeys,       // sort keys
+  kBufScalars,    // DevScalars[2] (one per direction) + spatial frame
+  kBufKeys,       // sort keys (scratch)
   kBufKeysAlt,
-  kBufVals,       // sort values
+  kBufVals,       // sort values (scratch)
   kBufValsAlt,
-  kBufNodes,      // LBVH nodes / grid cell table
-  kBufLeafBox,
+  kBufSorted0,    // Morton-sorted points of set 0 / set 1 (float4 x,y,z,index)
+  kBufSorted1,
+  kBufCodes0,     // sorted Morton codes of set 0 / set 1
+  kBufCodes1,
+  kBufNodes0,     // LBVH nodes or grid cell table of set 0 / set 1
+  kBufNodes1,
+  kBufBoxes,      // LBVH build scratch: per-node boxes
   kBufAux,        // parents / flags / cell offsets
   kBufAux2,
   kBufCubTemp,
@@ -64,6 +69,23 @@ enum BufSlot {
   kNumBufs
 };
 
+// Common cubic frame of both point sets (device resident, after the two
+// DevScalars in the scalars buffer).
+struct Frame {
+  float lo[3], hi[3];
+  float scale, extent;  // quantisation scale (cells per unit), max extent
+  int bits, dims;       // Morton bits per axis, dimensionality
+};
+
+// A point set in Morton order: float4 (x, y, z|0, caller index as bits).
+struct SortedSet {
+  float4* pts = nullptr;
+  uint32_t* codes = nullptr;
+  uint64_t n = 0;
+  int dims = 0;
+  const float* src = nullptr;  // device pointer it was sorted from
+};
+
 struct Ctx {
   int device = 0;
   int num_sms = 0;
@@ -75,10 +97,16 @@ struct Ctx {
   size_t host_pinned_bytes = 0;
   std::string last_error;
   uint64_t launches = 0;
-  cudaEvent_t ev[12] = {};
+  // Timing events (HD_TIMING): [12*dir + phase] per direction, 24/25 = the
+  // whole call.  Read after the call's final synchronisation.
+  cudaEvent_t ev[26] = {};
   bool timing = false;
-  int ev_used = 0;
+  int ev_base = 0;
   cudaGraphExec_t batch_graph = nullptr;
+  // Per-solve cache: the Morton-sorted sets (slot 0 = call's A, 1 = call's B)
+  // are shared by both directions of an undirected solve.
+  SortedSet sorted[2];
+  bool sorted_valid = false;
 };
 
 // Result of one directed solve, on the host.
@@ -131,6 +159,16 @@ hd_status certify(Ctx& c, const DirInput& in);
 void mark(Ctx& c, int phase_event);
 
 uint64_t pick_multiplier(uint64_t n, uint64_t seed);
+
+// Spatial preparation (hd_spatial.cu).
+Frame* frame(Ctx& c);
+size_t scalars_bytes();
+// Morton-sorts the call's two point sets (both, once per hd_solve) and
+// returns the ones matching a directed input: *q = in.A, *t = in.B.
+hd_status spatial_prepare(Ctx& c, const DirInput& in, const SortedSet** q,
+                          const SortedSet** t);
+// k random positions in [0, n) (with replacement), k from opt.sample_rate.
+hd_status make_sample(Ctx& c, uint64_t n, uint64_t seed, uint32_t* k, uint32_t** list);
 
 }  // namespace hdg
 

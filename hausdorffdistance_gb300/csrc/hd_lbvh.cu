@@ -1,0 +1,390 @@
+// LBVH variant: a linear BVH over Morton-sorted B, built with Karras' radix
+// tree construction (T. Karras, "Maximizing Parallelism in the Construction
+// of BVHs, Octrees, and k-d Trees", HPG 2012) and bottom-up box fitting, and
+// a warp-packet nearest-neighbour traversal with early break.
+//
+// It replaces the reference's OptiX/RT-core search
+// (src/hd_impl/hausdorff_distance_ray_tracing.h:63-236 with the programs of
+// src/rt/shaders/shaders_nn_uniform_grid_3d.cu:16-180 and the accel
+// build/refit of src/rt/rt_engine.h:290-314): GB300 has no RT cores.  The
+// reference grows a search radius over rounds and refits its BVH each round
+// (hybrid.h:349-371); a nearest-neighbour traversal needs no radius, so the
+// tree is built once and every A point is finished in one pass.
+//
+// Semantics per A point (as the reference's intersection program,
+// shaders_nn_uniform_grid_3d.cu:69-105): stop as soon as some B point is at
+// or below the running maximum (it cannot raise it), stop a subtree when its
+// box is no nearer than the current minimum, and stop outright when a whole
+// non-empty box lies within the running maximum (maxDist^2 <= cmax2, the
+// shader's :83-86 shortcut, taken here with a relative safety margin so that
+// FP32 rounding can never wrongly stop a point).  A point that is never
+// stopped ends with its exact nearest-neighbour distance and raises the
+// maximum with one 64-bit atomicMax.
+//
+// Layout in HBM:
+//   sorted points  float4 (x, y, z, caller index)       16 B / point
+//   leaves         implicit: leaf i = points [i*L, i*L+L), L <= 32
+//   nodes          4 x float4 per internal node: the boxes of both children
+//                  and the two child references (bit 31 set = leaf)   64 B
+// A traversal step loads one 64-byte node (all lanes the same address:
+// one broadcast) and tests both children for every lane of the packet.
+#include <cfloat>
+
+#include "hd_common.cuh"
+#include "hd_internal.h"
+
+namespace hdg {
+namespace {
+
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr int kQueryWarps = 4;
+constexpr int kStack = 64;
+
+__device__ __forceinline__ int delta(const uint32_t* __restrict__ codes, uint32_t L,
+                                     int64_t nL, int64_t i, int64_t j) {
+  if (j < 0 || j >= nL) return -1;
+  uint64_t ki = ((uint64_t) codes[(uint64_t) i * L] << 32) | (uint64_t) i;
+  uint64_t kj = ((uint64_t) codes[(uint64_t) j * L] << 32) | (uint64_t) j;
+  return __clzll(ki ^ kj);
+}
+
+// Leaf boxes: one thread per leaf over its (at most 32) points.
+__global__ void k_leaf_boxes(const float4* __restrict__ pts, uint64_t n, uint32_t L,
+                             uint32_t nL, uint32_t nI, float4* __restrict__ boxes) {
+  uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
+  if (leaf >= nL) return;
+  uint64_t s = (uint64_t) leaf * L;
+  uint64_t e = min(s + L, n);
+  float4 lo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f);
+  float4 hi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
+  for (uint64_t i = s; i < e; ++i) {
+    float4 p = pts[i];
+    lo.x = fminf(lo.x, p.x); lo.y = fminf(lo.y, p.y); lo.z = fminf(lo.z, p.z);
+    hi.x = fmaxf(hi.x, p.x); hi.y = fmaxf(hi.y, p.y); hi.z = fmaxf(hi.z, p.z);
+  }
+  boxes[2 * ((uint64_t) nI + leaf)] = lo;
+  boxes[2 * ((uint64_t) nI + leaf) + 1] = hi;
+}
+
+// Karras 2012, one thread per internal node.  Node ids: internal [0, nI),
+// leaves nI + [0, nL).  Keys are the leaves' first Morton codes augmented
+// with the leaf index, which makes them distinct.
+__global__ void k_karras(const uint32_t* __restrict__ codes, uint32_t L, uint32_t nL,
+                         uint2* __restrict__ child, uint32_t* __restrict__ parent) {
+  const int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x;
+  const int64_t nI = (int64_t) nL - 1;
+  if (i >= nI) return;
+  const int d = (delta(codes, L, nL, i, i + 1) - delta(codes, L, nL, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = delta(codes, L, nL, i, i - d);
+  int64_t lmax = 2;
+  while (delta(codes, L, nL, i, i + lmax * d) > dmin) lmax <<= 1;
+  int64_t l = 0;
+  for (int64_t t = lmax >> 1; t >= 1; t >>= 1)
+    if (delta(codes, L, nL, i, i + (l + t) * d) > dmin) l += t;
+  const int64_t j = i + l * d;
+  const int dnode = delta(codes, L, nL, i, j);
+  int64_t s = 0;
+  int64_t div = 2;
+  for (;;) {
+    int64_t t = (l + div - 1) / div;
+    if (delta(codes, L, nL, i, i + (s + t) * d) > dnode) s += t;
+    if (t <= 1) break;
+    div <<= 1;
+  }
+  const int64_t gamma = i + s * d + min(d, 0);
+  const int64_t lo = min(i, j), hi = max(i, j);
+  uint32_t left = (lo == gamma) ? ((uint32_t) gamma | kLeafBit) : (uint32_t) gamma;
+  uint32_t right = (hi == gamma + 1) ? ((uint32_t) (gamma + 1) | kLeafBit) : (uint32_t) (gamma + 1);
+  child[i] = make_uint2(left, right);
+  parent[(left & kLeafBit) ? nI + (left & ~kLeafBit) : left] = (uint32_t) i;
+  parent[(right & kLeafBit) ? nI + (right & ~kLeafBit) : right] = (uint32_t) i;
+}
+
+__device__ __forceinline__ uint32_t node_id(uint32_t ref, uint32_t nI) {
+  return (ref & kLeafBit) ? nI + (ref & ~kLeafBit) : ref;
+}
+
+// Bottom-up boxes: a thread per leaf climbs; the second child to arrive at a
+// parent computes its box (Karras 2012, section 4).
+__global__ void k_bottom_up(const uint2* __restrict__ child, const uint32_t* __restrict__ parent,
+                            uint32_t nL, uint32_t nI, float4* boxes, uint32_t* flags) {
+  uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
+  if (leaf >= nL || nI == 0) return;
+  uint32_t node = nI + leaf;
+  for (;;) {
+    uint32_t p = parent[node];
+    __threadfence();
+    if (atomicAdd(&flags[p], 1u) == 0) return;
+    __threadfence();
+    uint2 ch = child[p];
+    uint32_t a = node_id(ch.x, nI), b = node_id(ch.y, nI);
+    float4 alo = __ldcg(&boxes[2 * (uint64_t) a]), ahi = __ldcg(&boxes[2 * (uint64_t) a + 1]);
+    float4 blo = __ldcg(&boxes[2 * (uint64_t) b]), bhi = __ldcg(&boxes[2 * (uint64_t) b + 1]);
+    float4 lo = make_float4(fminf(alo.x, blo.x), fminf(alo.y, blo.y), fminf(alo.z, blo.z), 0.f);
+    float4 hi = make_float4(fmaxf(ahi.x, bhi.x), fmaxf(ahi.y, bhi.y), fmaxf(ahi.z, bhi.z), 0.f);
+    __stcg(&boxes[2 * (uint64_t) p], lo);
+    __stcg(&boxes[2 * (uint64_t) p + 1], hi);
+    if (p == 0) return;
+    node = p;
+  }
+}
+
+// Packs every internal node as 4 float4: both children's boxes and refs.
+__global__ void k_pack_nodes(const uint2* __restrict__ child, const float4* __restrict__ boxes,
+                             uint32_t nI, float4* __restrict__ nodes) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nI == 0) {
+    // Single leaf: a root whose right child is an empty box (never visited).
+    if (i == 0) {
+      float4 lo = boxes[0], hi = boxes[1];
+      nodes[0] = make_float4(lo.x, lo.y, lo.z, hi.x);
+      nodes[1] = make_float4(hi.y, hi.z, FLT_MAX, FLT_MAX);
+      nodes[2] = make_float4(FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX);
+      nodes[3] = make_float4(__uint_as_float(kLeafBit), __uint_as_float(kLeafBit), 0.f, 0.f);
+    }
+    return;
+  }
+  if (i >= nI) return;
+  uint2 ch = child[i];
+  uint32_t a = node_id(ch.x, nI), b = node_id(ch.y, nI);
+  float4 alo = boxes[2 * (uint64_t) a], ahi = boxes[2 * (uint64_t) a + 1];
+  float4 blo = boxes[2 * (uint64_t) b], bhi = boxes[2 * (uint64_t) b + 1];
+  float4* o = nodes + 4 * (uint64_t) i;
+  o[0] = make_float4(alo.x, alo.y, alo.z, ahi.x);
+  o[1] = make_float4(ahi.y, ahi.z, blo.x, blo.y);
+  o[2] = make_float4(blo.z, bhi.x, bhi.y, bhi.z);
+  o[3] = make_float4(__uint_as_float(ch.x), __uint_as_float(ch.y), 0.f, 0.f);
+}
+
+// Squared distance from p to the box [lo, hi] (0 inside), rounded exactly
+// like the pair formula (same non-fused operations in the same order).
+// Rounding is monotone, so for every point b in the box this value is <= the
+// FP32 squared distance of (p, b): pruning a box whose value is >= the current
+// minimum can never skip a strictly smaller pair distance.
+template <int D>
+__device__ __forceinline__ float box_min_d2(float px, float py, float pz, float lx, float ly,
+                                            float lz, float hx, float hy, float hz) {
+  float dx = fmaxf(fmaxf(__fsub_rn(lx, px), __fsub_rn(px, hx)), 0.0f);
+  float dy = fmaxf(fmaxf(__fsub_rn(ly, py), __fsub_rn(py, hy)), 0.0f);
+  float s = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+  if constexpr (D == 3) {
+    float dz = fmaxf(fmaxf(__fsub_rn(lz, pz), __fsub_rn(pz, hz)), 0.0f);
+    s = __fadd_rn(s, __fmul_rn(dz, dz));
+  }
+  return s;
+}
+
+template <int D>
+__device__ __forceinline__ float box_max_d2(float px, float py, float pz, float lx, float ly,
+                                            float lz, float hx, float hy, float hz) {
+  float dx = fmaxf(fabsf(px - lx), fabsf(hx - px));
+  float dy = fmaxf(fabsf(py - ly), fabsf(hy - py));
+  float s = dx * dx + dy * dy;
+  if constexpr (D == 3) {
+    float dz = fmaxf(fabsf(pz - lz), fabsf(hz - pz));
+    s += dz * dz;
+  }
+  return s;
+}
+
+// Safety factor for the "whole box within the maximum" shortcut: the FP32
+// box bound and the FP32 pair formula each carry a few ulps of rounding.
+constexpr float kMaxDistMargin = 1.0f + 1.0f / 65536.0f;
+
+// Warp-packet traversal.  A packet is 32 consecutive Morton-sorted queries
+// (or 32 entries of a sample list).
+template <int D, bool COUNT>
+__global__ void __launch_bounds__(kQueryWarps * 32)
+    k_lbvh_query(const float4* __restrict__ Q, uint64_t nItems,
+                 const uint32_t* __restrict__ qlist, const float4* __restrict__ nodes,
+                 const float4* __restrict__ B, uint64_t nB, uint32_t L, DevScalars* sc) {
+  __shared__ uint32_t stk[kQueryWarps][kStack];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint64_t packet = (uint64_t) blockIdx.x * kQueryWarps + warp;
+  if (packet * 32 >= nItems) return;
+  const uint64_t item = packet * 32 + lane;
+  bool active = item < nItems;
+  float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (active) q = Q[qlist ? qlist[item] : item];
+  float cmin = INFINITY;
+  float dstk[kStack];
+  unsigned long long key = 0;
+  if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
+  float thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
+  unsigned long long pairs = 0, visits = 0, leafv = 0;
+
+  int sp = 0;
+  uint32_t next = 0;  // root (internal node 0)
+  bool have = true;
+  for (;;) {
+    if (!__any_sync(0xFFFFFFFFu, active)) break;
+    if (have && !(next & kLeafBit)) {
+      // Internal node: test both children for every lane.
+      const float4* nd = nodes + 4 * (uint64_t) next;
+      const float4 n0 = nd[0], n1 = nd[1], n2 = nd[2], n3 = nd[3];
+      if (COUNT) ++visits;
+      const float dL = box_min_d2<D>(q.x, q.y, q.z, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
+      const float dR = box_min_d2<D>(q.x, q.y, q.z, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+      if (active && thr >= 0.0f) {
+        const float mL = box_max_d2<D>(q.x, q.y, q.z, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
+        const float mR = box_max_d2<D>(q.x, q.y, q.z, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+        if (fminf(mL, mR) * kMaxDistMargin <= thr) active = false;
+      }
+      const bool wL = active && dL < cmin;
+      const bool wR = active && dR < cmin;
+      const uint32_t bL = __ballot_sync(0xFFFFFFFFu, wL);
+      const uint32_t bR = __ballot_sync(0xFFFFFFFFu, wR);
+      const uint32_t left = __float_as_uint(n3.x), right = __float_as_uint(n3.y);
+      if (bL && bR) {
+        const int preferL = __popc(__ballot_sync(0xFFFFFFFFu, wL && (!wR || dL <= dR)));
+        const int preferR = __popc(__ballot_sync(0xFFFFFFFFu, wR && (!wL || dR < dL)));
+        const bool nearL = preferL >= preferR;
+        if (sp < kStack) {
+          if (lane == 0) stk[warp][sp] = nearL ? right : left;
+          dstk[sp] = nearL ? (wR ? dR : INFINITY) : (wL ? dL : INFINITY);
+          ++sp;
+        } else if (lane == 0) {
+          // Cannot happen: the tree is at most 64 levels deep (distinct
+          // 64-bit keys) and one entry is pushed per level.
+          atomicOr(&sc->status, kErrInternal);
+        }
+        __syncwarp();
+        next = nearL ? left : right;
+      } else if (bL) {
+        next = left;
+      } else if (bR) {
+        next = right;
+      } else {
+        have = false;
+      }
+      continue;
+    }
+    if (have) {
+      // Leaf: every lane of the packet scans its points.
+      const uint64_t s = (uint64_t) (next & ~kLeafBit) * L;
+      const int cnt = (int) min((uint64_t) L, nB - s);
+      float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (lane < cnt) p = B[s + lane];
+      float m = cmin;
+      for (int k = 0; k < cnt; ++k) {
+        const float bx = __shfl_sync(0xFFFFFFFFu, p.x, k);
+        const float by = __shfl_sync(0xFFFFFFFFu, p.y, k);
+        if constexpr (D == 2) {
+          m = fminf(m, d2_2(q.x, q.y, bx, by));
+        } else {
+          const float bz = __shfl_sync(0xFFFFFFFFu, p.z, k);
+          m = fminf(m, d2_3(q.x, q.y, q.z, bx, by, bz));
+        }
+      }
+      if (active) cmin = m;
+      if (COUNT) {
+        ++leafv;
+        pairs += (unsigned long long) cnt * __popc(__ballot_sync(0xFFFFFFFFu, active));
+      }
+      if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
+      thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
+      if (active && cmin <= thr) active = false;
+      have = false;
+      continue;
+    }
+    // Pop the next subtree any lane still needs.
+    if (sp == 0) break;
+    --sp;
+    next = stk[warp][sp];
+    const bool want = active && dstk[sp] < cmin;
+    have = __any_sync(0xFFFFFFFFu, want);
+  }
+  if (active) atomicMax(&sc->max_key, pack_max(cmin, __float_as_uint(q.w)));
+  if (COUNT && lane == 0) {
+    atomicAdd(&sc->pairs, pairs);
+    atomicAdd(&sc->nodes, visits);
+    atomicAdd(&sc->leaves, leafv);
+  }
+}
+
+}  // namespace
+
+struct Lbvh {
+  const float4* nodes;
+  uint32_t L;
+};
+
+// Builds the LBVH of a sorted set into the node slot of that set.
+static hd_status build_lbvh(Ctx& c, const SortedSet& t, int slot, Lbvh* out) {
+  const uint32_t L = c.opt.leaf_size ? std::min<uint32_t>(c.opt.leaf_size, 32) : 16;
+  const uint64_t nL64 = (t.n + L - 1) / L;
+  const uint32_t nL = (uint32_t) nL64;
+  const uint32_t nI = nL - 1;
+  hd_status s;
+  void *nodes, *boxes, *aux, *aux2;
+  const uint64_t nNodes = (uint64_t) nI + nL;
+  if ((s = ensure(c, slot == 0 ? kBufNodes0 : kBufNodes1,
+                  std::max<uint64_t>(nI, 1) * 4 * sizeof(float4), &nodes)) != HD_OK)
+    return s;
+  if ((s = ensure(c, kBufBoxes, nNodes * 2 * sizeof(float4), &boxes)) != HD_OK) return s;
+  // aux: child (uint2 per internal) ; aux2: parent (u32 per node) + flags (u32 per internal)
+  if ((s = ensure(c, kBufAux, std::max<uint64_t>(nI, 1) * sizeof(uint2), &aux)) != HD_OK) return s;
+  if ((s = ensure(c, kBufAux2, (nNodes + std::max<uint64_t>(nI, 1)) * 4, &aux2)) != HD_OK) return s;
+  uint32_t* parent = (uint32_t*) aux2;
+  uint32_t* flags = parent + nNodes;
+  k_leaf_boxes<<<(nL + 255) / 256, 256, 0, c.stream>>>(t.pts, t.n, L, nL, nI, (float4*) boxes);
+  if ((s = after_launch(c, "leaf_boxes")) != HD_OK) return s;
+  if (nI > 0) {
+    k_karras<<<(nI + 255) / 256, 256, 0, c.stream>>>(t.codes, L, nL, (uint2*) aux, parent);
+    if ((s = after_launch(c, "karras")) != HD_OK) return s;
+    cudaError_t e = cudaMemsetAsync(flags, 0, (size_t) nI * 4, c.stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "memset flags");
+    k_bottom_up<<<(nL + 255) / 256, 256, 0, c.stream>>>((const uint2*) aux, parent, nL, nI,
+                                                        (float4*) boxes, flags);
+    if ((s = after_launch(c, "bottom_up")) != HD_OK) return s;
+  }
+  k_pack_nodes<<<(std::max<uint32_t>(nI, 1) + 255) / 256, 256, 0, c.stream>>>(
+      (const uint2*) aux, (const float4*) boxes, nI, (float4*) nodes);
+  if ((s = after_launch(c, "pack_nodes")) != HD_OK) return s;
+  out->nodes = (const float4*) nodes;
+  out->L = L;
+  return HD_OK;
+}
+
+template <int D>
+static hd_status launch_query(Ctx& c, const SortedSet& q, uint64_t nItems, const uint32_t* list,
+                              const Lbvh& bvh, const SortedSet& t, DevScalars* sc, bool count) {
+  const uint64_t packets = (nItems + 31) / 32;
+  const uint64_t blocks = (packets + kQueryWarps - 1) / kQueryWarps;
+  if (count)
+    k_lbvh_query<D, true><<<(unsigned) blocks, kQueryWarps * 32, 0, c.stream>>>(
+        q.pts, nItems, list, bvh.nodes, t.pts, t.n, bvh.L, sc);
+  else
+    k_lbvh_query<D, false><<<(unsigned) blocks, kQueryWarps * 32, 0, c.stream>>>(
+        q.pts, nItems, list, bvh.nodes, t.pts, t.n, bvh.L, sc);
+  return after_launch(c, "lbvh_query");
+}
+
+hd_status run_lbvh(Ctx& c, const DirInput& in) {
+  if (in.dims != 2 && in.dims != 3) return fail(c, HD_ERR_UNSUPPORTED, "LBVH needs n_dims 2 or 3");
+  hd_status s;
+  const SortedSet *q, *t;
+  if ((s = spatial_prepare(c, in, &q, &t)) != HD_OK) return s;
+  mark(c, 1);
+  Lbvh bvh;
+  if ((s = build_lbvh(c, *t, in.dir, &bvh)) != HD_OK) return s;
+  mark(c, 2);
+  DevScalars* sc = scalars(c, in.dir);
+  // Sampling: exact nearest neighbours of a random subset of A raise the
+  // running maximum before the full pass (the reference's EB sampling,
+  // hybrid.h:128-168, here with the index instead of brute force).
+  uint32_t k = 0;
+  uint32_t* list = nullptr;
+  if ((s = make_sample(c, q->n, c.opt.seed * 31 + 17 + in.dir, &k, &list)) != HD_OK) return s;
+  auto go = [&](uint64_t n, const uint32_t* l) {
+    return in.dims == 2 ? launch_query<2>(c, *q, n, l, bvh, *t, sc, in.count)
+                        : launch_query<3>(c, *q, n, l, bvh, *t, sc, in.count);
+  };
+  if ((s = go(k, list)) != HD_OK) return s;
+  mark(c, 3);
+  if ((s = go(q->n, nullptr)) != HD_OK) return s;
+  mark(c, 4);
+  return certify(c, in);
+}
+
+}  // namespace hdg

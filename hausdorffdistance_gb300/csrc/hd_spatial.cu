@@ -1,0 +1,271 @@
+// Spatial preparation shared by the LBVH and grid variants: one fused pass
+// for both bounding boxes, Morton codes in a common cubic frame, a radix sort
+// per set, and a gather into Morton order as float4 (x, y, z, caller index).
+//
+// Replaces the reference's MBR reduction (src/geoms/mbr.h:307-321: thrust
+// for_each with CAS float atomics per point) and the first half of the grid
+// build (src/index/uniform_grid.h:343-484: occupancy bitset, copy_if, sort,
+// binary-search counting, atomic scatter): here the sort itself produces the
+// cell order, because a cubic Morton frame makes every grid level a prefix of
+// the code.
+#include <cub/device/device_radix_sort.cuh>
+
+#include <cfloat>
+
+#include "hd_common.cuh"
+#include "hd_internal.h"
+
+namespace hdg {
+namespace {
+
+// Per-CTA min/max over one set, then one atomic per CTA and dimension on the
+// order-preserving integer image of the float.
+__global__ void k_mbr(const float* __restrict__ P, uint64_t n, int dims,
+                      uint32_t* __restrict__ ord /* [2][4]: lo, hi */) {
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+  float hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t) gridDim.x * blockDim.x) {
+    for (int k = 0; k < dims; ++k) {
+      float v = P[i * dims + k];
+      lo[k] = fminf(lo[k], v);
+      hi[k] = fmaxf(hi[k], v);
+    }
+  }
+  __shared__ uint32_t s_lo[3], s_hi[3];
+  if (threadIdx.x < 3) {
+    s_lo[threadIdx.x] = 0xFFFFFFFFu;
+    s_hi[threadIdx.x] = 0u;
+  }
+  __syncthreads();
+  for (int k = 0; k < dims; ++k) {
+    float a = lo[k], b = hi[k];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      a = fminf(a, __shfl_xor_sync(0xFFFFFFFFu, a, o));
+      b = fmaxf(b, __shfl_xor_sync(0xFFFFFFFFu, b, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&s_lo[k], f2ord(a));
+      atomicMax(&s_hi[k], f2ord(b));
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < (unsigned) dims) {
+    atomicMin(&ord[threadIdx.x], s_lo[threadIdx.x]);
+    atomicMax(&ord[4 + threadIdx.x], s_hi[threadIdx.x]);
+  }
+}
+
+__global__ void k_frame(const uint32_t* __restrict__ ordA, const uint32_t* __restrict__ ordB,
+                        int dims, int use_a, int use_b, Frame* fr) {
+  if (threadIdx.x != 0) return;
+  float ext = 0.0f;
+  for (int k = 0; k < 3; ++k) {
+    float lo = FLT_MAX, hi = -FLT_MAX;
+    if (k < dims) {
+      if (use_a) {
+        lo = fminf(lo, ord2f(ordA[k]));
+        hi = fmaxf(hi, ord2f(ordA[4 + k]));
+      }
+      if (use_b) {
+        lo = fminf(lo, ord2f(ordB[k]));
+        hi = fmaxf(hi, ord2f(ordB[4 + k]));
+      }
+    } else {
+      lo = hi = 0.0f;
+    }
+    fr->lo[k] = lo;
+    fr->hi[k] = hi;
+    ext = fmaxf(ext, hi - lo);
+  }
+  const int bits = dims == 2 ? 16 : 10;
+  fr->bits = bits;
+  fr->dims = dims;
+  fr->extent = ext;
+  // Cubic frame: one scale for every axis so that Morton levels are cubes.
+  fr->scale = ext > 0.0f ? (float) ((1u << bits) - 1) / ext : 0.0f;
+}
+
+__device__ __forceinline__ uint32_t spread2(uint32_t x) {  // 16 bits -> even bits
+  x &= 0xFFFFu;
+  x = (x | (x << 8)) & 0x00FF00FFu;
+  x = (x | (x << 4)) & 0x0F0F0F0Fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+__device__ __forceinline__ uint32_t spread3(uint32_t x) {  // 10 bits -> every 3rd bit
+  x &= 0x3FFu;
+  x = (x | (x << 16)) & 0x030000FFu;
+  x = (x | (x << 8)) & 0x0300F00Fu;
+  x = (x | (x << 4)) & 0x030C30C3u;
+  x = (x | (x << 2)) & 0x09249249u;
+  return x;
+}
+
+__device__ __forceinline__ uint32_t quant(float v, float lo, float scale, uint32_t maxq) {
+  float q = (v - lo) * scale;
+  q = fminf(fmaxf(q, 0.0f), (float) maxq);
+  return (uint32_t) q;
+}
+
+__global__ void k_morton(const float* __restrict__ P, uint64_t n, int dims,
+                         const Frame* __restrict__ fr, uint32_t* __restrict__ keys,
+                         uint32_t* __restrict__ vals) {
+  const float lo0 = fr->lo[0], lo1 = fr->lo[1], lo2 = fr->lo[2], s = fr->scale;
+  const uint32_t maxq = (1u << fr->bits) - 1u;
+  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t) gridDim.x * blockDim.x) {
+    uint32_t code;
+    if (dims == 2) {
+      code = spread2(quant(P[2 * i], lo0, s, maxq)) |
+             (spread2(quant(P[2 * i + 1], lo1, s, maxq)) << 1);
+    } else {
+      code = spread3(quant(P[3 * i], lo0, s, maxq)) |
+             (spread3(quant(P[3 * i + 1], lo1, s, maxq)) << 1) |
+             (spread3(quant(P[3 * i + 2], lo2, s, maxq)) << 2);
+    }
+    keys[i] = code;
+    vals[i] = (uint32_t) i;
+  }
+}
+
+__global__ void k_gather(const float* __restrict__ P, uint64_t n, int dims,
+                         const uint32_t* __restrict__ order, float4* __restrict__ out) {
+  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t) gridDim.x * blockDim.x) {
+    uint32_t v = order[i];
+    float4 p;
+    p.x = P[(uint64_t) v * dims];
+    p.y = P[(uint64_t) v * dims + 1];
+    p.z = dims == 3 ? P[(uint64_t) v * dims + 2] : 0.0f;
+    p.w = __uint_as_float(v);
+    out[i] = p;
+  }
+}
+
+// Stratified sample of k positions in [0, n): position i lies in stratum
+// [i*n/k, (i+1)*n/k) at an offset drawn from a counter-based hash
+// (splitmix64).  It stands in for the reference's per-sample curand draws
+// with replacement (src/sampler.h:26, :50-65).  Over a Morton-sorted set the
+// positions come out sorted, so 32 consecutive samples form a spatially
+// coherent packet while the sample still covers the whole set.
+__global__ void k_sample(uint64_t n, uint32_t k, uint64_t seed, uint32_t* __restrict__ out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= k) return;
+  uint64_t z = seed + 0x9E3779B97F4A7C15ull * (i + 1);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  const uint64_t lo = (uint64_t) i * n / k, hi = (uint64_t) (i + 1) * n / k;
+  const uint64_t w = hi > lo ? hi - lo : 1;
+  out[i] = (uint32_t) min(lo + z % w, n - 1);
+}
+
+int grid_for(Ctx& c, uint64_t n, int per = 256) {
+  uint64_t g = (n + per - 1) / per;
+  g = std::min<uint64_t>(g, (uint64_t) c.num_sms * 16);
+  return (int) std::max<uint64_t>(g, 1);
+}
+
+}  // namespace
+
+Frame* frame(Ctx& c) {
+  return reinterpret_cast<Frame*>(reinterpret_cast<DevScalars*>(c.bufs[kBufScalars].p) + 2);
+}
+
+static hd_status spatial_sort(Ctx& c, const float* A, uint64_t nA, const float* B,
+                              uint64_t nB, int dims, SortedSet* sa, SortedSet* sb) {
+  const bool need_a = true, need_b = true;
+  hd_status s;
+  DevScalars* sc = scalars(c, 0);
+  // One bounding box per set (both boxes feed the common frame).
+  k_mbr<<<grid_for(c, nA), 256, 0, c.stream>>>(A, nA, dims, &sc->mbr_ord[0][0][0]);
+  if ((s = after_launch(c, "mbr_a")) != HD_OK) return s;
+  k_mbr<<<grid_for(c, nB), 256, 0, c.stream>>>(B, nB, dims, &sc->mbr_ord[1][0][0]);
+  if ((s = after_launch(c, "mbr_b")) != HD_OK) return s;
+  k_frame<<<1, 32, 0, c.stream>>>(&sc->mbr_ord[0][0][0], &sc->mbr_ord[1][0][0], dims, 1, 1,
+                                  frame(c));
+  if ((s = after_launch(c, "frame")) != HD_OK) return s;
+
+  const uint64_t nmax = std::max(need_a ? nA : 0, need_b ? nB : 0);
+  void *keys, *keys2, *vals, *vals2, *tmp;
+  if ((s = ensure(c, kBufKeys, nmax * 4, &keys)) != HD_OK) return s;
+  if ((s = ensure(c, kBufKeysAlt, nmax * 4, &keys2)) != HD_OK) return s;
+  if ((s = ensure(c, kBufVals, nmax * 4, &vals)) != HD_OK) return s;
+  if ((s = ensure(c, kBufValsAlt, nmax * 4, &vals2)) != HD_OK) return s;
+  size_t tmp_bytes = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, (const uint32_t*) keys,
+                                  (uint32_t*) keys2, (const uint32_t*) vals,
+                                  (uint32_t*) vals2, (int64_t) nmax, 0, 32, c.stream);
+  if ((s = ensure(c, kBufCubTemp, tmp_bytes, &tmp)) != HD_OK) return s;
+
+  for (int set = 0; set < 2; ++set) {
+    const bool need = set == 0 ? need_a : need_b;
+    if (!need) continue;
+    const float* P = set == 0 ? A : B;
+    const uint64_t n = set == 0 ? nA : nB;
+    SortedSet* out = set == 0 ? sa : sb;
+    void *pts, *codes;
+    if ((s = ensure(c, set == 0 ? kBufSorted0 : kBufSorted1, n * sizeof(float4), &pts)) != HD_OK)
+      return s;
+    if ((s = ensure(c, set == 0 ? kBufCodes0 : kBufCodes1, n * 4, &codes)) != HD_OK) return s;
+    k_morton<<<grid_for(c, n), 256, 0, c.stream>>>(P, n, dims, frame(c), (uint32_t*) keys,
+                                                   (uint32_t*) vals);
+    if ((s = after_launch(c, "morton")) != HD_OK) return s;
+    size_t tb = tmp_bytes;
+    const int end_bit = dims == 2 ? 32 : 30;
+    cudaError_t e = cub::DeviceRadixSort::SortPairs(
+        tmp, tb, (const uint32_t*) keys, (uint32_t*) codes, (const uint32_t*) vals,
+        (uint32_t*) vals2, (int64_t) n, 0, end_bit, c.stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "radix sort");
+    k_gather<<<grid_for(c, n), 256, 0, c.stream>>>(P, n, dims, (const uint32_t*) vals2,
+                                                   (float4*) pts);
+    if ((s = after_launch(c, "gather")) != HD_OK) return s;
+    out->pts = (float4*) pts;
+    out->codes = (uint32_t*) codes;
+    out->n = n;
+    out->dims = dims;
+    out->src = P;
+  }
+  return HD_OK;
+}
+
+size_t scalars_bytes() { return 2 * sizeof(DevScalars) + sizeof(Frame); }
+
+hd_status spatial_prepare(Ctx& c, const DirInput& in, const SortedSet** q,
+                          const SortedSet** t) {
+  if (!c.sorted_valid) {
+    // Direction 0 of the call: A is the call's A.
+    hd_status s = spatial_sort(c, in.A, in.nA, in.B, in.nB, in.dims, &c.sorted[0], &c.sorted[1]);
+    if (s != HD_OK) return s;
+    c.sorted_valid = true;
+  }
+  const SortedSet* x = (c.sorted[0].src == in.A && c.sorted[0].n == in.nA) ? &c.sorted[0]
+                                                                            : &c.sorted[1];
+  const SortedSet* y = (x == &c.sorted[0]) ? &c.sorted[1] : &c.sorted[0];
+  if (x->src != in.A || y->src != in.B)
+    return fail(c, HD_ERR_CUDA, "spatial cache does not match the directed input");
+  *q = x;
+  *t = y;
+  return HD_OK;
+}
+
+hd_status make_sample(Ctx& c, uint64_t n, uint64_t seed, uint32_t* k_out, uint32_t** list) {
+  double rate = c.opt.sample_rate > 0 ? c.opt.sample_rate : 0.01;
+  uint64_t k = (uint64_t) std::ceil((double) n * rate);
+  k = std::max<uint64_t>(k, std::min<uint64_t>(n, 1024));
+  k = std::min<uint64_t>(k, 1u << 14);
+  void* p;
+  hd_status s = ensure(c, kBufSample, k * 4, &p);
+  if (s != HD_OK) return s;
+  k_sample<<<(unsigned) ((k + 255) / 256), 256, 0, c.stream>>>(n, (uint32_t) k, seed,
+                                                               (uint32_t*) p);
+  if ((s = after_launch(c, "sample")) != HD_OK) return s;
+  *k_out = (uint32_t) k;
+  *list = (uint32_t*) p;
+  return HD_OK;
+}
+
+}  // namespace hdg

@@ -91,7 +91,7 @@ typedef struct hd_result {
   uint64_t ia, ib;         /* certifying pair indices (caller's order)         */
   double hd_ab, hd_ba;     /* FP64 directed distances (hd_ba < 0 if directed)  */
   uint64_t visited_pairs;  /* pair distances evaluated (HD_COUNT_PAIRS)        */
-  uint64_t visited_nodes;  /* index nodes/cells visited (HD_COUNT_PAIRS)       */
+  uint64_t visited_nodes;  /* internal index nodes visited (HD_COUNT_PAIRS)   */
   double ms;               /* device time of the whole solve (HD_TIMING)       */
   double phase_ms[8];      /* HD_TIMING: prep, build, sample, query, tail,     */
                            /* certify, copy-in, other                          */
@@ -99,6 +99,7 @@ typedef struct hd_result {
   int32_t variant_used_ba; /* and for B->A when undirected                     */
   double err_bound;        /* BF16: bound on |approx - exact| squared distance */
   uint64_t rechecked;      /* BF16: rows rechecked exactly in FP32             */
+  uint64_t visited_leaves; /* index leaves / cells scanned (HD_COUNT_PAIRS)    */
 } hd_result;
 
 /* One problem of a batch: A[offset_a .. offset_a+n_a), B[offset_b ..).
