@@ -195,23 +195,82 @@ constexpr float kMaxDistMargin = 1.0f + 1.0f / 65536.0f;
 // (or 32 entries of a sample list).
 template <int D, bool COUNT>
 __global__ void __launch_bounds__(kQueryWarps * 32)
-    k_lbvh_query(const float4* __restrict__ Q, uint64_t nItems,
-                 const uint32_t* __restrict__ qlist, const float4* __restrict__ nodes,
+    k_lbvh_query(const float4* __restrict__ Q, uint64_t nItems, uint32_t pstride, int phase,
+                 const uint32_t* __restrict__ ppos, const float4* __restrict__ nodes,
                  const float4* __restrict__ B, uint64_t nB, uint32_t L, DevScalars* sc) {
   __shared__ uint32_t stk[kQueryWarps][kStack];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint64_t packet = (uint64_t) blockIdx.x * kQueryWarps + warp;
+  // Phase 0 (sample pass) takes every pstride-th packet; phase 1 takes the
+  // rest.  Packets are 32 consecutive Morton-sorted queries either way.
+  const uint64_t w = (uint64_t) blockIdx.x * kQueryWarps + warp;
+  uint64_t packet;
+  if (phase == 0) {
+    packet = w * pstride;
+  } else {
+    packet = w + w / (pstride - 1) + 1;  // skips multiples of pstride
+  }
   if (packet * 32 >= nItems) return;
   const uint64_t item = packet * 32 + lane;
   bool active = item < nItems;
   float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (active) q = Q[qlist ? qlist[item] : item];
+  if (active) q = Q[item];
   float cmin = INFINITY;
   float dstk[kStack];
   unsigned long long key = 0;
   if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
   float thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
   unsigned long long pairs = 0, visits = 0, leafv = 0;
+
+  // Scans one leaf with every lane of the packet (points broadcast by
+  // shuffles, four at a time); stops as soon as no lane still needs a point,
+  // and lets lanes that found a point within the running maximum stop.
+  auto scan_leaf = [&](uint32_t leaf) {
+    const uint64_t s = (uint64_t) leaf * L;
+    const int cnt = (int) min((uint64_t) L, nB - s);
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (lane < cnt) p = B[s + lane];
+    float m = cmin;
+    int k = 0;
+    for (; k < cnt; k += 4) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int src = min(k + u, cnt - 1);
+        const float bx = __shfl_sync(0xFFFFFFFFu, p.x, src);
+        const float by = __shfl_sync(0xFFFFFFFFu, p.y, src);
+        if constexpr (D == 2) {
+          m = fminf(m, d2_2(q.x, q.y, bx, by));
+        } else {
+          const float bz = __shfl_sync(0xFFFFFFFFu, p.z, src);
+          m = fminf(m, d2_3(q.x, q.y, q.z, bx, by, bz));
+        }
+      }
+      if (!__any_sync(0xFFFFFFFFu, active && m > thr)) {
+        k += 4;
+        break;
+      }
+    }
+    if (active) cmin = m;
+    if (COUNT) {
+      ++leafv;
+      pairs += (unsigned long long) min(k, cnt) * __popc(__ballot_sync(0xFFFFFFFFu, active));
+    }
+    if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
+    thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
+    if (active && cmin <= thr) active = false;
+  };
+
+  {
+    // Warm start: queries and B share one Morton frame, so the B leaves at
+    // the packet's position in B's sorted codes (precomputed per packet) are
+    // spatially close.  Scanning that leaf and its neighbours lets most lanes
+    // stop before any traversal, and gives the others a small running
+    // minimum that prunes the traversal.
+    const uint32_t nL = (uint32_t) ((nB + L - 1) / L);
+    const uint32_t leaf0 = (uint32_t) min((uint64_t) ppos[packet] / L, (uint64_t) (nL - 1));
+    scan_leaf(leaf0);
+    if (leaf0 + 1 < nL && __any_sync(0xFFFFFFFFu, active)) scan_leaf(leaf0 + 1);
+    if (leaf0 > 0 && __any_sync(0xFFFFFFFFu, active)) scan_leaf(leaf0 - 1);
+  }
 
   int sp = 0;
   uint32_t next = 0;  // root (internal node 0)
@@ -260,30 +319,7 @@ __global__ void __launch_bounds__(kQueryWarps * 32)
       continue;
     }
     if (have) {
-      // Leaf: every lane of the packet scans its points.
-      const uint64_t s = (uint64_t) (next & ~kLeafBit) * L;
-      const int cnt = (int) min((uint64_t) L, nB - s);
-      float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (lane < cnt) p = B[s + lane];
-      float m = cmin;
-      for (int k = 0; k < cnt; ++k) {
-        const float bx = __shfl_sync(0xFFFFFFFFu, p.x, k);
-        const float by = __shfl_sync(0xFFFFFFFFu, p.y, k);
-        if constexpr (D == 2) {
-          m = fminf(m, d2_2(q.x, q.y, bx, by));
-        } else {
-          const float bz = __shfl_sync(0xFFFFFFFFu, p.z, k);
-          m = fminf(m, d2_3(q.x, q.y, q.z, bx, by, bz));
-        }
-      }
-      if (active) cmin = m;
-      if (COUNT) {
-        ++leafv;
-        pairs += (unsigned long long) cnt * __popc(__ballot_sync(0xFFFFFFFFu, active));
-      }
-      if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
-      thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
-      if (active && cmin <= thr) active = false;
+      scan_leaf(next & ~kLeafBit);
       have = false;
       continue;
     }
@@ -300,6 +336,25 @@ __global__ void __launch_bounds__(kQueryWarps * 32)
     atomicAdd(&sc->nodes, visits);
     atomicAdd(&sc->leaves, leafv);
   }
+}
+
+// Position of every packet's first query in B's sorted codes (lower bound),
+// one binary search per packet.
+__global__ void k_packet_pos(const uint32_t* __restrict__ qcodes, uint64_t nQ,
+                             const uint32_t* __restrict__ bcodes, uint64_t nB,
+                             uint32_t* __restrict__ pos) {
+  const uint64_t p = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+  if (p * 32 >= nQ) return;
+  const uint32_t target = qcodes[p * 32];
+  uint64_t lo = 0, hi = nB;
+  while (lo < hi) {
+    const uint64_t mid = (lo + hi) >> 1;
+    if (bcodes[mid] < target)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  pos[p] = (uint32_t) lo;
 }
 
 }  // namespace
@@ -347,16 +402,20 @@ static hd_status build_lbvh(Ctx& c, const SortedSet& t, int slot, Lbvh* out) {
 }
 
 template <int D>
-static hd_status launch_query(Ctx& c, const SortedSet& q, uint64_t nItems, const uint32_t* list,
-                              const Lbvh& bvh, const SortedSet& t, DevScalars* sc, bool count) {
-  const uint64_t packets = (nItems + 31) / 32;
-  const uint64_t blocks = (packets + kQueryWarps - 1) / kQueryWarps;
+static hd_status launch_query(Ctx& c, const SortedSet& q, uint32_t pstride, int phase,
+                              const uint32_t* ppos, const Lbvh& bvh, const SortedSet& t,
+                              DevScalars* sc, bool count) {
+  const uint64_t packets = (q.n + 31) / 32;
+  const uint64_t warps = phase == 0 ? (packets + pstride - 1) / pstride
+                                    : packets - (packets + pstride - 1) / pstride;
+  if (warps == 0) return HD_OK;
+  const uint64_t blocks = (warps + kQueryWarps - 1) / kQueryWarps;
   if (count)
     k_lbvh_query<D, true><<<(unsigned) blocks, kQueryWarps * 32, 0, c.stream>>>(
-        q.pts, nItems, list, bvh.nodes, t.pts, t.n, bvh.L, sc);
+        q.pts, q.n, pstride, phase, ppos, bvh.nodes, t.pts, t.n, bvh.L, sc);
   else
     k_lbvh_query<D, false><<<(unsigned) blocks, kQueryWarps * 32, 0, c.stream>>>(
-        q.pts, nItems, list, bvh.nodes, t.pts, t.n, bvh.L, sc);
+        q.pts, q.n, pstride, phase, ppos, bvh.nodes, t.pts, t.n, bvh.L, sc);
   return after_launch(c, "lbvh_query");
 }
 
@@ -370,19 +429,25 @@ hd_status run_lbvh(Ctx& c, const DirInput& in) {
   if ((s = build_lbvh(c, *t, in.dir, &bvh)) != HD_OK) return s;
   mark(c, 2);
   DevScalars* sc = scalars(c, in.dir);
-  // Sampling: exact nearest neighbours of a random subset of A raise the
-  // running maximum before the full pass (the reference's EB sampling,
-  // hybrid.h:128-168, here with the index instead of brute force).
-  uint32_t k = 0;
-  uint32_t* list = nullptr;
-  if ((s = make_sample(c, q->n, c.opt.seed * 31 + 17 + in.dir, &k, &list)) != HD_OK) return s;
-  auto go = [&](uint64_t n, const uint32_t* l) {
-    return in.dims == 2 ? launch_query<2>(c, *q, n, l, bvh, *t, sc, in.count)
-                        : launch_query<3>(c, *q, n, l, bvh, *t, sc, in.count);
+  const uint64_t packets = (q->n + 31) / 32;
+  void* ppos;
+  if ((s = ensure(c, kBufSample, packets * 4, &ppos)) != HD_OK) return s;
+  k_packet_pos<<<(unsigned) ((packets + 255) / 256), 256, 0, c.stream>>>(
+      q->codes, q->n, t->codes, t->n, (uint32_t*) ppos);
+  if ((s = after_launch(c, "packet_pos")) != HD_OK) return s;
+  // Sample pass: every pstride-th packet, spread over the whole Morton range,
+  // finishes first and raises the running maximum before the rest run (the
+  // reference samples with EB for the same purpose, hybrid.h:128-168).
+  const uint32_t pstride = packets >= 4096 ? 64 : (packets >= 256 ? 16 : 2);
+  auto go = [&](int phase) {
+    return in.dims == 2 ? launch_query<2>(c, *q, pstride, phase, (const uint32_t*) ppos, bvh, *t,
+                                          sc, in.count)
+                        : launch_query<3>(c, *q, pstride, phase, (const uint32_t*) ppos, bvh, *t,
+                                          sc, in.count);
   };
-  if ((s = go(k, list)) != HD_OK) return s;
+  if ((s = go(0)) != HD_OK) return s;
   mark(c, 3);
-  if ((s = go(q->n, nullptr)) != HD_OK) return s;
+  if ((s = go(1)) != HD_OK) return s;
   mark(c, 4);
   return certify(c, in);
 }

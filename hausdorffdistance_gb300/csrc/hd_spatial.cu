@@ -256,7 +256,7 @@ hd_status make_sample(Ctx& c, uint64_t n, uint64_t seed, uint32_t* k_out, uint32
   double rate = c.opt.sample_rate > 0 ? c.opt.sample_rate : 0.01;
   uint64_t k = (uint64_t) std::ceil((double) n * rate);
   k = std::max<uint64_t>(k, std::min<uint64_t>(n, 1024));
-  k = std::min<uint64_t>(k, 1u << 14);
+  k = std::min<uint64_t>(k, 4096);
   void* p;
   hd_status s = ensure(c, kBufSample, k * 4, &p);
   if (s != HD_OK) return s;

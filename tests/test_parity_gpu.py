@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = json.load(open(os.path.join(HERE, "golden", "golden.json")))["cases"]
-SPATIAL = ["eb", "lbvh", "auto"]
+SPATIAL = ["eb", "lbvh", "grid", "auto"]
 REL_TOL_F64 = 1e-6
 
 
@@ -106,7 +106,7 @@ def test_reference_interface_classes():
     a, b = synth.uniform2d(5000, seed=2)
     want = hd_oracle.eb(a, b, seed=0, n_threads=1)["hd"]
     for cls in (hd.HausdorffDistanceEarlyBreak, hd.HausdorffDistanceHybrid,
-                hd.HausdorffDistanceRayTracing):
+                hd.HausdorffDistanceRayTracing, hd.HausdorffDistanceGrid):
         impl = cls(seed=0)
         got = impl.CalculateDistance(a.copy(), b.copy())
         assert got == want
