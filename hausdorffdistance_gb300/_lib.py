@@ -34,7 +34,7 @@ HD_TIMING = 8
 # Every symbol include/hd_gpu.h declares.
 EXPORTED = ["hd_default_options", "hd_create", "hd_destroy", "hd_set_stream",
             "hd_solve", "hd_solve_batch", "hd_solve_batch_plain", "hd_last_error",
-            "hd_status_string", "hd_kernel_launches", "hd_version"]
+            "hd_status_string", "hd_kernel_launches", "hd_version", "hd_solve_eb_noalloc"]
 
 
 class Options(ctypes.Structure):
@@ -108,6 +108,9 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.hd_status_string.restype = ctypes.c_char_p
     lib.hd_kernel_launches.argtypes = [P]
     lib.hd_kernel_launches.restype = ctypes.c_uint64
+    lib.hd_solve_eb_noalloc.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint64, ctypes.c_int,
+                                        ctypes.c_uint32, P, ctypes.POINTER(Result)]
+    lib.hd_solve_eb_noalloc.restype = ctypes.c_int
     lib.hd_version.argtypes = []
     lib.hd_version.restype = ctypes.c_char_p
     _lib = lib

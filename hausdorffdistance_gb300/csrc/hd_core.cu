@@ -190,6 +190,24 @@ hd_status certify(Ctx& c, const DirInput& in) {
   return after_launch(c, "finalize");
 }
 
+// Stream-level forms of the certification tail and the scalar reset, for
+// callers that run without a context (hd_solve_eb_noalloc).
+cudaError_t certify_on_stream(cudaStream_t st, int num_sms, const float* A, const float* B,
+                              uint64_t nB, int dims, DevScalars* sc) {
+  int grid = (int) std::min<uint64_t>((nB + 255) / 256, (uint64_t) num_sms * 4);
+  grid = std::max(grid, 1);
+  k_argmin<<<grid, 256, 0, st>>>(A, B, nB, dims, sc);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_finalize<<<1, 1, 0, st>>>(A, B, dims, sc);
+  return cudaGetLastError();
+}
+
+cudaError_t init_scalars_on_stream(cudaStream_t st, DevScalars* sc, int n) {
+  k_init_scalars<<<1, 32, 0, st>>>(sc, n);
+  return cudaGetLastError();
+}
+
 hd_status init_scalars(Ctx& c) {
   void* p = nullptr;
   hd_status s = ensure(c, kBufScalars, scalars_bytes(), &p);

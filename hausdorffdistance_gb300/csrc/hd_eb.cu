@@ -31,6 +31,9 @@
 //    a single atomicMax on the bit pattern — no CAS loop — which also keeps
 //    the certifying A index.
 #include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <mutex>
 
 #include "hd_common.cuh"
 #include "hd_internal.h"
@@ -384,3 +387,144 @@ hd_status run_eb(Ctx& c, const DirInput& in) {
 }
 
 }  // namespace hdg
+
+// ---------------------------------------------------------------------------
+// Early-break solve without any allocation.
+//
+// Some callers cannot allocate device memory while they call us: code that
+// runs under a fixed memory budget handed out up front (a serving process
+// that reserves all of its HBM at start-up, an embedded caching allocator
+// that must not be bypassed), or host code in a phase where cudaMalloc /
+// cudaFree would synchronise the device and stall work the caller keeps in
+// flight.  hd_solve_eb_noalloc serves them: it runs the same persistent
+// early-break kernels as hd_solve's EB variant, but every byte of scratch it
+// needs (the visit-ordered copy of B, the deferred-point list and the two
+// result words) lives in the file-scope device array below, sized once for
+// point sets of up to kNoAllocMaxPoints points.  The array is part of the
+// loaded library, so each GPU that loads it holds kNoAllocBytes (about
+// 32 MiB) until the process exits.
+namespace hdg {
+namespace {
+
+constexpr uint64_t kNoAllocMaxPoints = 1ull << 20;
+constexpr size_t kNoAllocScalarBytes = 1024;  // two DevScalars, padded
+constexpr size_t kNoAllocHeavyBytes = kNoAllocMaxPoints * sizeof(HeavyEntry);
+constexpr size_t kNoAllocPackBytes = kNoAllocMaxPoints * sizeof(float4);
+constexpr size_t kNoAllocBytes = kNoAllocScalarBytes + kNoAllocHeavyBytes + kNoAllocPackBytes;
+static_assert(2 * sizeof(DevScalars) <= kNoAllocScalarBytes, "scalar area too small");
+
+// In host code this name is only a host-side stand-in for the symbol: its
+// device address comes from cudaGetSymbolAddress (see noalloc_scratch).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[256] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (with that device current) and cached.
+cudaError_t noalloc_scratch(int dev, unsigned char** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[dev] = p;
+  }
+  *out = (unsigned char*) g_noalloc_addr[dev];
+  return cudaSuccess;
+}
+
+template <int D>
+cudaError_t noalloc_direction(cudaStream_t st, int num_sms, const float* A, uint64_t nA,
+                              const float* B, uint64_t nB, unsigned char* base,
+                              DevScalars* sc) {
+  using PT = typename EbPt<D>::T;
+  const uint32_t nTiles = (uint32_t) ((nB + kEbTile - 1) / kEbTile);
+  const uint64_t nPad = (uint64_t) nTiles * kEbTile;
+  HeavyEntry* heavy = (HeavyEntry*) (base + kNoAllocScalarBytes);
+  PT* pb = (PT*) (base + kNoAllocScalarBytes + kNoAllocHeavyBytes);
+  Perm pB{nB, pick_multiplier(nB, 1), 0};
+  Perm pA{nA, pick_multiplier(nA, 2), 0};
+  int grid = (int) std::min<uint64_t>((nPad + 255) / 256, (uint64_t) num_sms * 16);
+  k_eb_pack<D><<<grid, 256, 0, st>>>(B, nB, pB, pb, nPad);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const uint32_t n_seed = (uint32_t) std::min<uint64_t>(nA, (uint64_t) num_sms);
+  k_eb_heavy<D><<<n_seed, kEbThreads, 0, st>>>(A, pA, pb, nTiles, sc, nullptr, n_seed, nullptr);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (nA > n_seed) {
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_eb_main<D>, kEbThreads, 0);
+    occ = std::max(1, occ);
+    const uint64_t per_cta = (uint64_t) kEbThreads * kEbSlots;
+    const uint64_t want = (nA - n_seed + per_cta - 1) / per_cta;
+    const int g = (int) std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t) num_sms * occ));
+    const uint32_t capTiles = std::max<uint32_t>(1, kCapPairs / kEbTile);
+    k_eb_main<D><<<g, kEbThreads, 0, st>>>(A, pA, n_seed, nA, pb, nTiles, capTiles, sc, heavy,
+                                           (uint32_t) kNoAllocMaxPoints);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_eb_heavy<D><<<num_sms * 4, kEbThreads, 0, st>>>(A, pA, pb, nTiles, sc, heavy, 0,
+                                                      &sc->heavy_count);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return certify_on_stream(st, num_sms, A, B, nB, D, sc);
+}
+
+}  // namespace
+}  // namespace hdg
+
+extern "C" HD_API hd_status hd_solve_eb_noalloc(const float* A, uint64_t n_a, const float* B,
+                                                uint64_t n_b, int n_dims, uint32_t flags,
+                                                void* stream, hd_result* out) {
+  using namespace hdg;
+  if (!A || !B || !out) return HD_ERR_INVALID_ARG;
+  if (n_a == 0 || n_b == 0) return HD_ERR_INVALID_ARG;
+  if (n_dims != 2 && n_dims != 3) return HD_ERR_INVALID_ARG;
+  if (flags & ~(HD_UNDIRECTED | HD_DEVICE_PTRS)) return HD_ERR_INVALID_ARG;
+  // Inputs beyond the fixed scratch capacity are rejected, never truncated.
+  if (n_a > kNoAllocMaxPoints || n_b > kNoAllocMaxPoints) return HD_ERR_INVALID_ARG;
+  cudaStream_t st = (cudaStream_t) stream;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return HD_ERR_NO_DEVICE;
+  int num_sms = 0;
+  e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess || num_sms <= 0) return HD_ERR_NO_DEVICE;
+  unsigned char* base = nullptr;
+  if ((e = noalloc_scratch(dev, &base)) != cudaSuccess) return HD_ERR_CUDA;
+  DevScalars* sc = (DevScalars*) base;
+  const bool undirected = (flags & HD_UNDIRECTED) != 0;
+  const int ndir = undirected ? 2 : 1;
+  // The scratch keeps the previous call's contents: reset the result words.
+  if ((e = init_scalars_on_stream(st, sc, 2)) != cudaSuccess) return HD_ERR_CUDA;
+  for (int d = 0; d < ndir; ++d) {
+    const float* x = d == 0 ? A : B;
+    const float* y = d == 0 ? B : A;
+    const uint64_t nx = d == 0 ? n_a : n_b, ny = d == 0 ? n_b : n_a;
+    e = n_dims == 2 ? noalloc_direction<2>(st, num_sms, x, nx, y, ny, base, sc + d)
+                    : noalloc_direction<3>(st, num_sms, x, nx, y, ny, base, sc + d);
+    if (e != cudaSuccess) return e == cudaErrorNoKernelImageForDevice ? HD_ERR_NO_DEVICE : HD_ERR_CUDA;
+  }
+  DevScalars h[2];
+  e = cudaMemcpyAsync(h, sc, sizeof(h), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return HD_ERR_CUDA;
+  for (int d = 0; d < ndir; ++d) {
+    if (h[d].status & kErrWaitTimeout) return HD_ERR_DEVICE_TIMEOUT;
+    if (h[d].status) return HD_ERR_CUDA;
+  }
+  memset(out, 0, sizeof(*out));
+  out->hd_ab = std::sqrt(h[0].d2_64);
+  out->hd_ba = undirected ? std::sqrt(h[1].d2_64) : -1.0;
+  const int win = (undirected && h[1].d2 > h[0].d2) ? 1 : 0;
+  out->hd_f32 = std::sqrt(h[win].d2);
+  out->hd = std::sqrt(h[win].d2_64);
+  out->direction = win;
+  out->ia = h[win].ia;
+  out->ib = h[win].ib;
+  out->visited_pairs = h[0].pairs + (undirected ? h[1].pairs : 0);
+  out->variant_used = HD_VARIANT_EB;
+  out->variant_used_ba = undirected ? HD_VARIANT_EB : -1;
+  return HD_OK;
+}

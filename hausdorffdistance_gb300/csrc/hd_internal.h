@@ -155,6 +155,11 @@ hd_status select_variant(Ctx& c, const DirInput& in, int* variant);
 // DevScalars[dir].  Used by every variant.
 hd_status certify(Ctx& c, const DirInput& in);
 
+// Context-free forms used by hd_solve_eb_noalloc.
+cudaError_t certify_on_stream(cudaStream_t st, int num_sms, const float* A, const float* B,
+                              uint64_t nB, int dims, DevScalars* sc);
+cudaError_t init_scalars_on_stream(cudaStream_t st, DevScalars* sc, int n);
+
 // Event-based phase timing (HD_TIMING).
 void mark(Ctx& c, int phase_event);
 

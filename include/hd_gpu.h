@@ -159,6 +159,33 @@ HD_API hd_status hd_solve_batch_plain(hd_ctx* ctx, const float* A, uint64_t tota
                                const hd_problem* probs, uint64_t n_problems,
                                uint32_t flags, hd_batch_result* out);
 
+/* Early-break Hausdorff distance that allocates nothing.
+ *
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they call in: a process that hands all of its HBM to its own
+ * pool at start-up, or host code in a phase where a cudaMalloc/cudaFree
+ * (which synchronise the device) would stall work it keeps in flight.  It
+ * runs the EB variant's kernels with all scratch in one fixed device array
+ * inside libhdgpu.so (about 32 MiB, held by every GPU that loads the library
+ * until the process exits) and calls no cudaMalloc, cudaFree or other
+ * allocating routine.
+ *
+ * A and B are DEVICE pointers (n x n_dims floats, n_dims 2 or 3) on the
+ * current device; flags may hold HD_UNDIRECTED (HD_DEVICE_PTRS is implied).
+ * Work is queued on `stream` (a cudaStream_t, NULL = default stream) and the
+ * call returns after the result is in *out (same fields and FP32 bit-exact
+ * result as hd_solve with HD_VARIANT_EB; no timing).  n_a and n_b are limited
+ * to 1,048,576 points each: larger inputs return HD_ERR_INVALID_ARG before any
+ * device work.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  Every call shares the one array, which
+ * keeps the last call's contents (each call resets what must start at zero):
+ * calls that overlap on the GPU — from two host threads, or on two streams —
+ * race on it and must be serialised by the caller. */
+HD_API hd_status hd_solve_eb_noalloc(const float* A, uint64_t n_a, const float* B,
+                                     uint64_t n_b, int n_dims, uint32_t flags,
+                                     void* stream, hd_result* out);
+
 /* Message for the last failing call on this context (never NULL). */
 HD_API const char* hd_last_error(hd_ctx* ctx);
 
