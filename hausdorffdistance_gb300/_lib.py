@@ -34,7 +34,8 @@ HD_TIMING = 8
 # Every symbol include/hd_gpu.h declares.
 EXPORTED = ["hd_default_options", "hd_create", "hd_destroy", "hd_set_stream",
             "hd_solve", "hd_solve_batch", "hd_solve_batch_plain", "hd_last_error",
-            "hd_status_string", "hd_kernel_launches", "hd_version", "hd_solve_eb_noalloc"]
+            "hd_status_string", "hd_kernel_launches", "hd_version", "hd_solve_eb_noalloc",
+            "hd_debug_bf16_rowmin"]
 
 
 class Options(ctypes.Structure):
@@ -111,6 +112,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.hd_solve_eb_noalloc.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint64, ctypes.c_int,
                                         ctypes.c_uint32, P, ctypes.POINTER(Result)]
     lib.hd_solve_eb_noalloc.restype = ctypes.c_int
+    lib.hd_debug_bf16_rowmin.argtypes = [P, P, ctypes.c_uint64, P, ctypes.c_uint64, ctypes.c_int, P]
+    lib.hd_debug_bf16_rowmin.restype = ctypes.c_int
     lib.hd_version.argtypes = []
     lib.hd_version.restype = ctypes.c_char_p
     _lib = lib

@@ -1,0 +1,506 @@
+// Split-BF16 tensor-core variant for high-dimensional inputs (n_dims a
+// multiple of 16, up to 256).  No counterpart in the reference, which only
+// handles n_dims 2 and 3 (src/main.cpp:134-135).
+//
+// ||a - b||^2 = ||a||^2 + ||b||^2 - 2 a.b.  Each coordinate is split into
+// bf16 hi = bf16(x) and lo = bf16(x - hi); a.b is taken as
+// hi.hi + hi.lo + lo.hi (three products, FP32 accumulation in tensor memory)
+// by tcgen05.mma kind::f16 on sm_103a.  Per A row the epilogue keeps the
+// approximate minimum over B of ||b||^2 - 2 a.b.  A rigorous per-row error
+// bound E_i (split residuals, the dropped lo.lo product, FP32 accumulation
+// and the FP32 rounding of the reference formula) then certifies the
+// result: every row whose interval [m_i - E_i, m_i + E_i] can reach the
+// largest lower bound max_j (m_j - E_j) is re-scanned exactly with the FP32
+// reference formula, and the maximum over those rows is the exact FP32
+// Hausdorff distance — bit-identical to the FP32 scans.  The certifying
+// pair's distance is then recomputed in FP64 (certify()).
+//
+// Kernel shape (one CTA per 128 A rows, 6 warps, 1 CTA per SM):
+//   warp 0      producer: TMA bulk copies (cp.async.bulk) of the A block once
+//               and of B tiles (256 rows, hi+lo) into a 2-stage ring
+//   warp 1      allocates 512 TMEM columns; one lane issues the MMAs:
+//               per B tile and 128-row half, 3 products x (Kp/16) MMAs of
+//               M=128, N=128, K=16 into one of two 256-column FP32
+//               accumulators
+//   warps 2-5   epilogue: tcgen05.ld of the accumulator (one TMEM lane per
+//               A row), min over the tile of ||b||^2 - 2 acc
+// Operands are pre-packed in global memory in the no-swizzle K-major
+// core-matrix layout (8 rows x 16 bytes per core matrix), so every tile is
+// one contiguous bulk copy.  No TMA multicast.
+#include <cuda_bf16.h>
+
+#include <cfloat>
+#include <cmath>
+
+#include "hd_common.cuh"
+#include "hd_internal.h"
+
+namespace hdg {
+namespace {
+
+constexpr int kBM = 128;   // A rows per CTA (UMMA M)
+constexpr int kBN = 256;   // B rows per tile: two 128-row halves (UMMA N = 128 each)
+constexpr int kBH = 128;   // rows of one B half / one packed sub-tile
+constexpr int kThreads = 192;
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kWaitLimit = 1u << 24;
+// Dynamic shared memory reserved per CTA.  The operands use 160 KB; the rest
+// keeps every address a descriptor could form (even with its two strides
+// read the other way round) inside this CTA's own window.
+constexpr uint32_t kSmemBytes = 220 * 1024;
+
+// Byte offset of element (row, k) inside one packed operand region of R rows:
+// core matrix (chunk c = k/8, group g = row/8) at (c * R/8 + g) * 128 bytes,
+// row row%8 at 16-byte stride, element k%8 at 2-byte stride.
+__host__ __device__ __forceinline__ uint32_t pack_off(uint32_t row, uint32_t k, uint32_t R) {
+  return ((k >> 3) * (R >> 3) + (row >> 3)) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// One thread per (row, 8-element chunk): splits, writes hi and lo chunks.
+// Tile t of rows [t*R, t*R+R) occupies 2 * R * Kp * 2 bytes: hi then lo.
+__global__ void k_bf16_pack(const float* __restrict__ X, uint64_t n, int D, int Kp, int R,
+                            uint64_t nPad, unsigned char* __restrict__ out,
+                            float* __restrict__ norms, uint32_t* __restrict__ maxnorm_ord,
+                            int pad_norm_inf) {
+  const uint64_t chunks = (uint64_t) Kp / 8;
+  const uint64_t total = nPad * chunks;
+  for (uint64_t t = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t) gridDim.x * blockDim.x) {
+    const uint64_t row = t / chunks;
+    const uint32_t c = (uint32_t) (t % chunks);
+    __align__(16) __nv_bfloat16 hi[8], lo[8];
+    float part = 0.0f;
+    for (int e = 0; e < 8; ++e) {
+      const int k = (int) c * 8 + e;
+      const float v = (row < n && k < D) ? X[row * D + k] : 0.0f;
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      const float r = v - __bfloat162float(h);
+      hi[e] = h;
+      lo[e] = __float2bfloat16_rn(r);
+      part = fmaf(v, v, part);
+    }
+    const uint64_t tile = row / R;
+    const uint32_t rr = (uint32_t) (row % R);
+    unsigned char* base = out + tile * (uint64_t) (2 * R * Kp * 2);
+    const uint32_t off = pack_off(rr, c * 8, (uint32_t) R);
+    *reinterpret_cast<uint4*>(base + off) = *reinterpret_cast<const uint4*>(hi);
+    *reinterpret_cast<uint4*>(base + (uint64_t) R * Kp * 2 + off) =
+        *reinterpret_cast<const uint4*>(lo);
+    // Row norm: reduce the chunk partials of one row (chunks of a row are
+    // consecutive threads).
+    atomicAdd(&norms[row], part);
+  }
+  (void) maxnorm_ord;
+  (void) pad_norm_inf;
+}
+
+__global__ void k_bf16_norm_finish(float* __restrict__ norms, uint64_t n, uint64_t nPad,
+                                   uint32_t* __restrict__ maxnorm_ord, int pad_inf) {
+  uint32_t local = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < nPad;
+       i += (uint64_t) gridDim.x * blockDim.x) {
+    if (i < n) {
+      local = max(local, f2ord(sqrtf(norms[i])));
+    } else if (pad_inf) {
+      norms[i] = INFINITY;  // padded B rows never win a minimum
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) local = max(local, __shfl_xor_sync(0xFFFFFFFFu, local, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(maxnorm_ord, local);
+}
+
+// ---- tcgen05 / mbarrier helpers (inline PTX) --------------------------------
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t) __cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Shared-memory matrix descriptor, no swizzle, K-major.
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t) ((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t) ((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t) ((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t) 1 << 46;  // descriptor version for tcgen05
+  // base offset 0, relative LBO mode, layout type 0 = no swizzle
+  return d;
+}
+
+// Instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major,
+// M = 128, N = 128.
+__host__ __device__ constexpr uint32_t make_idesc() {
+  return (1u << 4)                        // D format F32
+         | (1u << 7)                      // A format BF16
+         | (1u << 10)                     // B format BF16
+         | ((uint32_t) (kBH >> 3) << 17)  // N >> 3
+         | ((uint32_t) (kBM >> 4) << 24);  // M >> 4
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n"
+      " setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(da), "l"(db), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Error bound on |approx - FP32 reference| squared distance for a row of norm
+// a against rows of norm at most b, K = padded dimension.  Terms: the split
+// residuals and the dropped lo.lo product (4 * 2^-18 |a||b|), FP32
+// accumulation of 3K products with truncation allowed ((3K + 16) 2^-23
+// |a||b|), the epilogue's FP32 additions (2^-21 (|a| + |b|)^2) and the
+// reference formula's own rounding ((K + 2) 2^-24 (|a| + |b|)^2); doubled.
+__device__ __forceinline__ double row_bound(double a, double b, int K) {
+  const double c = 4.0 * ldexp(1.0, -18) + (3.0 * K + 16.0) * ldexp(1.0, -23);
+  const double s = (a + b) * (a + b);
+  const double e = 2.0 * c * a * b + ldexp(1.0, -21) * s + (K + 2.0) * ldexp(1.0, -24) * s;
+  return 2.0 * e + 1e-30;
+}
+
+struct Bf16Scalars {
+  uint32_t bmax_ord;   // max ||b|| (order-preserving bits)
+  uint32_t lo_ord;     // max_i (m_i - E_i) (order-preserving bits)
+  uint32_t cand;       // candidate count
+  uint32_t status;
+};
+
+template <int Kp>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_bf16_rowmin(const unsigned char* __restrict__ Apack, const unsigned char* __restrict__ Bpack,
+                  const float* __restrict__ anorm, const float* __restrict__ bnorm, uint64_t nA,
+                  uint32_t nTilesB, float* __restrict__ rowmin, Bf16Scalars* bs) {
+  constexpr uint32_t kAReg = kBM * Kp * 2;   // bytes of one A region (hi or lo)
+  constexpr uint32_t kBHReg = kBH * Kp * 2;  // bytes of one B half region (hi or lo)
+  constexpr uint32_t kATile = 2 * kAReg;     // A block: hi, lo
+  constexpr uint32_t kBTile = 4 * kBHReg;    // B tile: (hi, lo) of half 0, then of half 1
+  static_assert(kATile + 2 * kBTile <= kSmemBytes, "operands exceed shared memory");
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ __align__(8) uint64_t a_full, b_full[2], b_empty[2], acc_full[2], acc_empty[2];
+  __shared__ uint32_t tmem_base;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned char* sA = smem;
+  unsigned char* sB = smem + kATile;
+
+  if (threadIdx.x == 0) {
+    mbar_init(&a_full, 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&b_full[i], 1);
+      mbar_init(&b_empty[i], 1);
+      mbar_init(&acc_full[i], 1);
+      mbar_init(&acc_empty[i], 128);
+    }
+    fence_barrier_init();
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+  uint32_t* status = &bs->status;
+  bool ok = true;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      mbar_expect_tx(&a_full, kATile);
+      tma_load_1d(sA, Apack + (uint64_t) blockIdx.x * kATile, kATile, &a_full);
+      for (uint32_t t = 0; t < nTilesB && ok; ++t) {
+        const int buf = t & 1;
+        if (t >= 2) ok = mbar_wait(&b_empty[buf], ((t >> 1) - 1) & 1, status, kWaitLimit);
+        if (!ok) break;
+        mbar_expect_tx(&b_full[buf], kBTile);
+        tma_load_1d(sB + buf * kBTile, Bpack + (uint64_t) t * kBTile, kBTile, &b_full[buf]);
+      }
+      // Every issued copy must land before the CTA may exit.
+      if (ok && nTilesB >= 1) ok = mbar_wait(&b_empty[(nTilesB - 1) & 1], ((nTilesB - 1) >> 1) & 1,
+                                            status, kWaitLimit);
+      if (ok && nTilesB >= 2) ok = mbar_wait(&b_empty[(nTilesB - 2) & 1], ((nTilesB - 2) >> 1) & 1,
+                                            status, kWaitLimit);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = make_idesc();
+      ok = mbar_wait(&a_full, 0, status, kWaitLimit);
+      const uint32_t a_hi = smem_u32(sA), a_lo = a_hi + kAReg;
+      for (uint32_t t = 0; t < nTilesB && ok; ++t) {
+        const int buf = t & 1;
+        ok = mbar_wait(&b_full[buf], (t >> 1) & 1, status, kWaitLimit);
+        if (ok && t >= 2) ok = mbar_wait(&acc_empty[buf], ((t >> 1) - 1) & 1, status, kWaitLimit);
+        if (!ok) break;
+        tc_fence_after();
+        // K-major, no swizzle: LBO = next 8-element chunk along K (16 core
+        // matrices further in a 128-row region), SBO = next 8-row group (one
+        // core matrix further).  Every region holds 128 rows, so even a
+        // descriptor read with the two strides exchanged stays inside this
+        // CTA's shared-memory window.
+        constexpr uint32_t kLbo = (kBM / 8) * 128u, kSbo = 128u;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const uint32_t b_hi = smem_u32(sB + buf * kBTile + h * 2 * kBHReg);
+          const uint32_t b_lo = b_hi + kBHReg;
+          const uint32_t d = tmem + (uint32_t) buf * kBN + (uint32_t) h * kBH;
+          uint32_t acc = 0;
+#pragma unroll
+          for (int prod = 0; prod < 3; ++prod) {
+            const uint32_t ar = prod == 2 ? a_lo : a_hi;
+            const uint32_t br = prod == 1 ? b_lo : b_hi;
+#pragma unroll
+            for (int s = 0; s < Kp / 16; ++s) {
+              const uint64_t da = make_desc(ar + (uint32_t) s * 2u * kLbo, kLbo, kSbo);
+              const uint64_t db = make_desc(br + (uint32_t) s * 2u * kLbo, kLbo, kSbo);
+              mma_bf16(d, da, db, idesc, acc);
+              acc = 1;
+            }
+          }
+        }
+        mma_commit(&b_empty[buf]);
+        mma_commit(&acc_full[buf]);
+      }
+    }
+  } else {
+    // Epilogue: warp w reads TMEM lanes [32 (w % 4), +32): one A row per thread.
+    const int quad = warp & 3;
+    const uint32_t row_in_block = (uint32_t) (quad * 32 + lane);
+    const uint64_t row = (uint64_t) blockIdx.x * kBM + row_in_block;
+    float m = INFINITY;
+    for (uint32_t t = 0; t < nTilesB; ++t) {
+      const int buf = t & 1;
+      ok = mbar_wait(&acc_full[buf], (t >> 1) & 1, status, kWaitLimit);
+      if (__any_sync(0xFFFFFFFFu, !ok)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const float4* bn4 = reinterpret_cast<const float4*>(bnorm + (uint64_t) t * kBN);
+#pragma unroll 1
+      for (int cc = 0; cc < kBN / 32; ++cc) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t) (quad * 32) << 16) + (uint32_t) buf * kBN + cc * 32, v);
+#pragma unroll
+        for (int j4 = 0; j4 < 8; ++j4) {
+          const float4 bn = __ldg(bn4 + cc * 8 + j4);
+          m = fminf(m, fmaf(-2.0f, v[4 * j4 + 0], bn.x));
+          m = fminf(m, fmaf(-2.0f, v[4 * j4 + 1], bn.y));
+          m = fminf(m, fmaf(-2.0f, v[4 * j4 + 2], bn.z));
+          m = fminf(m, fmaf(-2.0f, v[4 * j4 + 3], bn.w));
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&acc_empty[buf]);
+    }
+    if (ok && row < nA) {
+      const float an = anorm[row];
+      const float mi = an + m;
+      rowmin[row] = mi;
+      const double E = row_bound(sqrt((double) an), (double) ord2f(bs->bmax_ord), Kp);
+      atomicMax(&bs->lo_ord, f2ord((float) ((double) mi - E)));
+    }
+  }
+  // Every MMA of this CTA has completed once the epilogue consumed the last
+  // accumulator (or the loops gave up); only then is TMEM released.
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
+__global__ void k_bf16_candidates(const float* __restrict__ rowmin, const float* __restrict__ anorm,
+                                  uint64_t nA, int Kp, Bf16Scalars* bs, uint32_t* __restrict__ list) {
+  const double L = (double) ord2f(bs->lo_ord);
+  const double bmax = (double) ord2f(bs->bmax_ord);
+  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < nA;
+       i += (uint64_t) gridDim.x * blockDim.x) {
+    const double E = row_bound(sqrt((double) anorm[i]), bmax, Kp);
+    if ((double) rowmin[i] + E >= L) {
+      const uint32_t s = atomicAdd(&bs->cand, 1u);
+      list[s] = (uint32_t) i;
+    }
+  }
+}
+
+// Exact FP32 re-scan of a candidate row (reference formula), one CTA each,
+// with early break against the running maximum of exact row minima.
+__global__ void __launch_bounds__(256)
+    k_bf16_recheck(const float* __restrict__ A, const float* __restrict__ B, uint64_t nB, int D,
+                   const uint32_t* __restrict__ list, const Bf16Scalars* bs, DevScalars* sc) {
+  __shared__ float red[8];
+  __shared__ float s_thr;
+  __shared__ float sa[256];
+  const uint32_t n = bs->cand;
+  for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
+    const uint32_t ia = list[e];
+    __syncthreads();
+    for (int k = threadIdx.x; k < D; k += blockDim.x) sa[k] = A[(uint64_t) ia * D + k];
+    __syncthreads();
+    float cmin = INFINITY;
+    bool broke = false;
+    const uint64_t chunk = 256 * 32;
+    for (uint64_t base = 0; base < nB && !broke; base += chunk) {
+      float m = INFINITY;
+      const uint64_t end = min(nB, base + chunk);
+      for (uint64_t j = base + threadIdx.x; j < end; j += 256) m = fminf(m, d2_n(sa, B + j * D, D));
+#pragma unroll
+      for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+      if (threadIdx.x == 0) s_thr = threshold_of(ld_relaxed_u64(&sc->max_key));
+      __syncthreads();
+      for (int k = 0; k < 8; ++k) cmin = fminf(cmin, red[k]);
+      const float thr = s_thr;
+      __syncthreads();
+      if (cmin <= thr) broke = true;
+    }
+    if (!broke && threadIdx.x == 0) atomicMax(&sc->max_key, pack_max(cmin, ia));
+  }
+}
+
+template <int Kp>
+hd_status run_bf16_k(Ctx& c, const DirInput& in, DirResult* extra, float* rowmin_host) {
+  hd_status s;
+  const uint64_t nTA = (in.nA + kBM - 1) / kBM, nTB = (in.nB + kBN - 1) / kBN;
+  if (nTA >= (1u << 31) || nTB >= 0xFFFFFFFFull) return fail(c, HD_ERR_INVALID_ARG, "too large");
+  const uint64_t padA = nTA * kBM, padB = nTB * kBN;
+  void *pa, *pb, *na, *nb, *rm, *cand, *bsv;
+  if ((s = ensure(c, kBufBf16A, padA * Kp * 4, &pa)) != HD_OK) return s;
+  if ((s = ensure(c, kBufBf16B, padB * Kp * 4, &pb)) != HD_OK) return s;
+  if ((s = ensure(c, kBufNormsA, padA * 4, &na)) != HD_OK) return s;
+  if ((s = ensure(c, kBufNormsB, padB * 4, &nb)) != HD_OK) return s;
+  if ((s = ensure(c, kBufRowMin, padA * 4, &rm)) != HD_OK) return s;
+  if ((s = ensure(c, kBufCand, in.nA * 4 + 64, &cand)) != HD_OK) return s;
+  if ((s = ensure(c, kBufAux2, sizeof(Bf16Scalars), &bsv)) != HD_OK) return s;
+  Bf16Scalars* bs = (Bf16Scalars*) bsv;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(na, 0, padA * 4, c.stream)) != cudaSuccess) return cuda_fail(c, e, "memset");
+  if ((e = cudaMemsetAsync(nb, 0, padB * 4, c.stream)) != cudaSuccess) return cuda_fail(c, e, "memset");
+  if ((e = cudaMemsetAsync(bs, 0, sizeof(Bf16Scalars), c.stream)) != cudaSuccess)
+    return cuda_fail(c, e, "memset");
+  const int g = c.num_sms * 16;
+  k_bf16_pack<<<g, 256, 0, c.stream>>>(in.A, in.nA, in.dims, Kp, kBM, padA, (unsigned char*) pa,
+                                       (float*) na, nullptr, 0);
+  if ((s = after_launch(c, "bf16_pack_a")) != HD_OK) return s;
+  k_bf16_pack<<<g, 256, 0, c.stream>>>(in.B, in.nB, in.dims, Kp, kBH, padB, (unsigned char*) pb,
+                                       (float*) nb, nullptr, 0);
+  if ((s = after_launch(c, "bf16_pack_b")) != HD_OK) return s;
+  // A's norm maximum is not needed; B's gives the bound.
+  k_bf16_norm_finish<<<c.num_sms * 4, 256, 0, c.stream>>>((float*) nb, in.nB, padB, &bs->bmax_ord, 1);
+  if ((s = after_launch(c, "bf16_norms")) != HD_OK) return s;
+  mark(c, 1);
+  mark(c, 2);
+  auto kern = k_bf16_rowmin<Kp>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kSmemBytes);
+  kern<<<(unsigned) nTA, kThreads, kSmemBytes, c.stream>>>(
+      (const unsigned char*) pa, (const unsigned char*) pb, (const float*) na, (const float*) nb,
+      in.nA, (uint32_t) nTB, (float*) rm, bs);
+  if ((s = after_launch(c, "bf16_rowmin")) != HD_OK) return s;
+  mark(c, 3);
+  if (rowmin_host) {
+    e = cudaMemcpyAsync(rowmin_host, rm, in.nA * 4, cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "rowmin copy");
+    Bf16Scalars h;
+    e = cudaMemcpy(&h, bs, sizeof(h), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "bf16 scalars");
+    if (h.status) return fail(c, HD_ERR_DEVICE_TIMEOUT, "a bounded device wait ran out");
+    return HD_OK;
+  }
+  k_bf16_candidates<<<c.num_sms * 4, 256, 0, c.stream>>>((const float*) rm, (const float*) na, in.nA,
+                                                         Kp, bs, (uint32_t*) cand);
+  if ((s = after_launch(c, "bf16_candidates")) != HD_OK) return s;
+  DevScalars* sc = scalars(c, in.dir);
+  k_bf16_recheck<<<c.num_sms * 2, 256, 0, c.stream>>>(in.A, in.B, in.nB, in.dims,
+                                                     (const uint32_t*) cand, bs, sc);
+  if ((s = after_launch(c, "bf16_recheck")) != HD_OK) return s;
+  mark(c, 4);
+  // Bound and recheck statistics for the result (small copy, after the work).
+  Bf16Scalars h;
+  e = cudaMemcpyAsync(&h, bs, sizeof(h), cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "bf16 scalars");
+  if (h.status) {
+    // Propagate a wait timeout to the solve's status word.
+    e = cudaMemsetAsync(&sc->status, 0xFF, 1, c.stream);
+    (void) e;
+    return fail(c, HD_ERR_DEVICE_TIMEOUT, "a bounded device wait ran out in the BF16 kernel");
+  }
+  if (extra) {
+    extra->rechecked = h.cand;
+    // Report the bound of the largest-norm pair (||a|| ~ ||b|| ~ max ||b||).
+    const double b = (double) ord2f(h.bmax_ord);
+    const double cK = 4.0 * std::ldexp(1.0, -18) + (3.0 * Kp + 16.0) * std::ldexp(1.0, -23);
+    const double sq = 4.0 * b * b;
+    extra->err_bound = 2.0 * (2.0 * cK * b * b + std::ldexp(1.0, -21) * sq +
+                              (Kp + 2.0) * std::ldexp(1.0, -24) * sq);
+  }
+  return certify(c, in);
+}
+
+hd_status run_bf16_impl(Ctx& c, const DirInput& in, DirResult* extra, float* rowmin_host) {
+  if (in.dims % 16 != 0 || in.dims > 256)
+    return fail(c, HD_ERR_UNSUPPORTED, "the BF16 variant needs n_dims % 16 == 0 and <= 256");
+  switch (in.dims) {
+  case 16: return run_bf16_k<16>(c, in, extra, rowmin_host);
+  case 32: return run_bf16_k<32>(c, in, extra, rowmin_host);
+  case 48: return run_bf16_k<48>(c, in, extra, rowmin_host);
+  case 64: return run_bf16_k<64>(c, in, extra, rowmin_host);
+  default: return fail(c, HD_ERR_UNSUPPORTED, "BF16 tiles are built for n_dims 16, 32, 48, 64");
+  }
+}
+
+}  // namespace
+
+hd_status run_bf16(Ctx& c, const DirInput& in, DirResult* extra) {
+  return run_bf16_impl(c, in, extra, nullptr);
+}
+
+hd_status bf16_rowmin_debug(Ctx& c, const DirInput& in, float* rowmin_host) {
+  return run_bf16_impl(c, in, nullptr, rowmin_host);
+}
+
+}  // namespace hdg

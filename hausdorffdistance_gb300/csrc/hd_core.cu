@@ -454,6 +454,24 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   return HD_OK;
 }
 
+hd_status hd_debug_bf16_rowmin(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
+                               uint64_t n_b, int n_dims, float* rowmin_out) {
+  if (!c) return HD_ERR_INVALID_ARG;
+  c->last_error.clear();
+  if (!A || !B || !rowmin_out || n_a == 0 || n_b == 0)
+    return fail(*c, HD_ERR_INVALID_ARG, "bad arguments");
+  cudaSetDevice(c->device);
+  c->timing = false;
+  c->sorted_valid = false;
+  hd_status s;
+  const float *dA, *dB;
+  if ((s = copy_in(*c, A, n_a, n_dims, kBufA, &dA)) != HD_OK) return s;
+  if ((s = copy_in(*c, B, n_b, n_dims, kBufB, &dB)) != HD_OK) return s;
+  if ((s = init_scalars(*c)) != HD_OK) return s;
+  DirInput in{dA, n_a, dB, n_b, n_dims, 0, false};
+  return bf16_rowmin_debug(*c, in, rowmin_out);
+}
+
 const char* hd_last_error(hd_ctx* c) {
   if (!c) return "null context";
   return c->last_error.c_str();

@@ -383,7 +383,7 @@ hd_status run_eb_dim(Ctx& c, const DirInput& in) {
 hd_status run_eb(Ctx& c, const DirInput& in) {
   if (in.dims == 2) return run_eb_dim<2>(c, in);
   if (in.dims == 3) return run_eb_dim<3>(c, in);
-  return run_brute(c, in);
+  return run_eb_nd(c, in);
 }
 
 }  // namespace hdg

@@ -107,6 +107,9 @@ struct Ctx {
   // are shared by both directions of an undirected solve.
   SortedSet sorted[2];
   bool sorted_valid = false;
+  // Sampler statistic of the last AUTO decision per direction (p80 of the
+  // sampled early-break iteration counts; 0 when no sample was drawn).
+  double last_p80[2] = {0.0, 0.0};
 };
 
 // Result of one directed solve, on the host.
@@ -146,9 +149,12 @@ DevScalars* scalars(Ctx& c, int dir);
 // Directed solvers; each leaves its result in DevScalars[dir] (finalized).
 hd_status run_eb(Ctx& c, const DirInput& in);
 hd_status run_brute(Ctx& c, const DirInput& in);
+hd_status run_eb_nd(Ctx& c, const DirInput& in);  // EB for n_dims other than 2, 3
 hd_status run_lbvh(Ctx& c, const DirInput& in);
 hd_status run_grid(Ctx& c, const DirInput& in);
 hd_status run_bf16(Ctx& c, const DirInput& in, DirResult* extra);
+// Test hook: the BF16 kernel's approximate row minima (no certification).
+hd_status bf16_rowmin_debug(Ctx& c, const DirInput& in, float* rowmin_host);
 hd_status select_variant(Ctx& c, const DirInput& in, int* variant);
 
 // Common tail: exact argmin of A[ia] over B, FP64 recomputation, written to

@@ -1,0 +1,123 @@
+// AUTO variant selector driven by sampler statistics.
+//
+// Replaces the reference's hybrid decision (src/hd_impl/hausdorff_distance_hybrid.h:
+// 128-199: EB over ceil(|A| * sample_rate) sampled points with per-point
+// iteration counters, percentiles of the sorted counters, and
+// "p80 < eb_only_threshold" from a generated XGBoost tree,
+// src/models/tree_ebonlythreshold_3d.h) with a project-written rule:
+//
+//   1. k points of A (k = sample_rate * |A|, clamped to [256, 2048]) run the
+//      early-break scan against B, one CTA each, B visited in a pseudo-random
+//      order, counting the B points each visited before it stopped (capped at
+//      65,536).  The completed samples also seed the running maximum that the
+//      chosen variant starts from.
+//   2. The EB cost of the full set is ~ |A| * p80 pairs; the index-based cost
+//      is ~ |A| + |B| point operations.  EB is chosen when
+//          ratio = |A| * p80 / (|A| + |B|)  <  eb_only_threshold,
+//      otherwise the LBVH (the grid when the table says so).  The threshold
+//      comes from the autotuner's table (hausdorffdistance_gb300/autotune.py
+//      fits it over a sweep of workloads) unless hd_options overrides it.
+//   3. Tiny problems (|A| * |B| <= 2^22) take EB without sampling; inputs with
+//      n_dims other than 2 or 3 take the split-BF16 tiles when n_dims is a
+//      multiple of 16 and the pair count is large, else the FP32 scan.
+#include <algorithm>
+#include <cfloat>
+#include <vector>
+
+#include "hd_common.cuh"
+#include "hd_internal.h"
+#include "hd_tuning.h"
+
+namespace hdg {
+namespace {
+
+constexpr uint32_t kSampleCap = 65536;
+
+__global__ void __launch_bounds__(256)
+    k_sample_eb(const float* __restrict__ A, Perm pA, const float* __restrict__ B, Perm pB,
+                uint64_t nB, int dims, uint32_t cap, DevScalars* sc, uint32_t* __restrict__ iters) {
+  __shared__ float red[8];
+  __shared__ float s_thr;
+  const uint32_t e = blockIdx.x;
+  const uint32_t ia = (uint32_t) pA(e);
+  float a[3] = {A[(uint64_t) ia * dims], A[(uint64_t) ia * dims + 1],
+                dims == 3 ? A[(uint64_t) ia * dims + 2] : 0.0f};
+  float cmin = INFINITY;
+  const uint64_t limit = min((uint64_t) cap, nB);
+  uint64_t done = 0;
+  bool broke = false;
+  const uint64_t step = 256 * 8;
+  while (done < limit) {
+    float m = INFINITY;
+    const uint64_t end = min(limit, done + step);
+    for (uint64_t j = done + threadIdx.x; j < end; j += 256) {
+      const uint64_t b = pB(j);
+      const float d = dims == 2 ? d2_2(a[0], a[1], B[2 * b], B[2 * b + 1])
+                                : d2_3(a[0], a[1], a[2], B[3 * b], B[3 * b + 1], B[3 * b + 2]);
+      m = fminf(m, d);
+    }
+    done = end;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    if (threadIdx.x == 0) s_thr = threshold_of(ld_relaxed_u64(&sc->max_key));
+    __syncthreads();
+    for (int k = 0; k < 8; ++k) cmin = fminf(cmin, red[k]);
+    const float thr = s_thr;
+    __syncthreads();
+    if (cmin <= thr) {
+      broke = true;
+      break;
+    }
+  }
+  if (threadIdx.x == 0) {
+    iters[e] = (uint32_t) done;
+    // A sample that scanned all of B without stopping has its exact minimum.
+    if (!broke && done == nB) atomicMax(&sc->max_key, pack_max(cmin, ia));
+  }
+}
+
+}  // namespace
+
+hd_status select_variant(Ctx& c, const DirInput& in, int* v) {
+  const Tuning& tu = tuning();
+  if (in.dims != 2 && in.dims != 3) {
+    const double pairs = (double) in.nA * (double) in.nB;
+    *v = (in.dims % 16 == 0 && pairs >= tu.bf16_min_pairs) ? HD_VARIANT_BF16 : HD_VARIANT_EB;
+    return HD_OK;
+  }
+  if ((double) in.nA * (double) in.nB <= tu.eb_small_pairs) {
+    *v = HD_VARIANT_EB;
+    return HD_OK;
+  }
+  const double rate = c.opt.sample_rate > 0 ? c.opt.sample_rate : 0.01;
+  uint32_t k = (uint32_t) std::min<double>(std::max<double>(rate * (double) in.nA, 256.0), 2048.0);
+  k = (uint32_t) std::min<uint64_t>(k, in.nA);
+  void* buf;
+  hd_status s = ensure(c, kBufCand, (size_t) k * 4, &buf);
+  if (s != HD_OK) return s;
+  DevScalars* sc = scalars(c, in.dir);
+  const uint64_t seed = c.opt.seed;
+  Perm pA{in.nA, pick_multiplier(in.nA, seed + 11), (seed * 1299709u) % in.nA};
+  Perm pB{in.nB, pick_multiplier(in.nB, seed + 13), (seed * 15485863u) % in.nB};
+  k_sample_eb<<<k, 256, 0, c.stream>>>(in.A, pA, in.B, pB, in.nB, in.dims, kSampleCap, sc,
+                                       (uint32_t*) buf);
+  if ((s = after_launch(c, "sample_eb")) != HD_OK) return s;
+  std::vector<uint32_t> it(k);
+  cudaError_t e = cudaMemcpyAsync(it.data(), buf, (size_t) k * 4, cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "sample statistics");
+  std::sort(it.begin(), it.end());
+  const double p80 = it[(size_t) (0.8 * (k - 1))];
+  const double ratio = (double) in.nA * p80 / (double) (in.nA + in.nB);
+  const double thr = c.opt.eb_only_threshold ? (double) c.opt.eb_only_threshold : tu.eb_ratio;
+  c.last_p80[in.dir] = p80;
+  if (ratio < thr) {
+    *v = HD_VARIANT_EB;
+  } else {
+    *v = tu.prefer_grid ? HD_VARIANT_GRID : HD_VARIANT_LBVH;
+  }
+  return HD_OK;
+}
+
+}  // namespace hdg

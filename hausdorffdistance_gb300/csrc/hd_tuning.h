@@ -1,0 +1,18 @@
+// Selector and launch constants chosen by the autotuner
+// (hausdorffdistance_gb300/autotune.py writes hd_tuning_table.h).
+#pragma once
+
+namespace hdg {
+
+struct Tuning {
+  double eb_small_pairs;  // |A|*|B| at or below which AUTO takes EB unsampled
+  double eb_ratio;        // EB when |A| * p80 / (|A| + |B|) is below this
+  double bf16_min_pairs;  // n_dims % 16 == 0: BF16 tiles from this |A|*|B| up
+  bool prefer_grid;       // index-based choice: grid instead of LBVH
+  unsigned leaf_size;     // LBVH points per leaf
+  unsigned batch_small;   // batched solver: problems up to this size per warp
+};
+
+const Tuning& tuning();
+
+}  // namespace hdg

@@ -1,0 +1,9 @@
+// Generated by hausdorffdistance_gb300/autotune.py — do not edit by hand.
+// Initial table (before the first sweep on a GB300): conservative values.
+#pragma once
+#define HD_TUNED_EB_SMALL_PAIRS 4194304.0
+#define HD_TUNED_EB_RATIO 64.0
+#define HD_TUNED_BF16_MIN_PAIRS 67108864.0
+#define HD_TUNED_PREFER_GRID 0
+#define HD_TUNED_LEAF_SIZE 16
+#define HD_TUNED_BATCH_SMALL 512

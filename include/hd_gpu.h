@@ -133,8 +133,8 @@ HD_API hd_status hd_destroy(hd_ctx* ctx);
 HD_API hd_status hd_set_stream(hd_ctx* ctx, void* cuda_stream);
 
 /* Computes the Hausdorff distance of A (n_a x n_dims floats, row-major) and
- * B (n_b x n_dims).  n_dims 2 or 3 for every variant; any n_dims in [1, 256]
- * for EB, BRUTE and BF16 (BF16 needs n_dims % 16 == 0).  variant < 0 uses the
+ * B (n_b x n_dims).  n_dims 2 or 3 for every variant; n_dims in [1, 128] for
+ * EB and BRUTE; BF16 takes n_dims 16, 32, 48 or 64.  variant < 0 uses the
  * context default.  Synchronous: returns after the result is on the host.
  * Replaces HausdorffDistance::CalculateDistance (hausdorff_distance.h:21-32),
  * both the CPU and the GPU overload. */
@@ -185,6 +185,14 @@ HD_API hd_status hd_solve_batch_plain(hd_ctx* ctx, const float* A, uint64_t tota
 HD_API hd_status hd_solve_eb_noalloc(const float* A, uint64_t n_a, const float* B,
                                      uint64_t n_b, int n_dims, uint32_t flags,
                                      void* stream, hd_result* out);
+
+/* Test hook for the split-BF16 tensor-core kernel: writes, for every row of
+ * A (host pointers, n_dims % 16 == 0, <= 64), the kernel's approximate
+ * min over B of ||a - b||^2 before certification into rowmin_out[n_a].
+ * No counterpart in the reference. */
+HD_API hd_status hd_debug_bf16_rowmin(hd_ctx* ctx, const float* A, uint64_t n_a,
+                                      const float* B, uint64_t n_b, int n_dims,
+                                      float* rowmin_out);
 
 /* Message for the last failing call on this context (never NULL). */
 HD_API const char* hd_last_error(hd_ctx* ctx);

@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = json.load(open(os.path.join(HERE, "golden", "golden.json")))["cases"]
-SPATIAL = ["eb", "lbvh", "grid", "auto"]
+SPATIAL = ["eb", "lbvh", "grid", "brute", "auto"]
 REL_TOL_F64 = 1e-6
 
 
