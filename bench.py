@@ -50,7 +50,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="clusters3d",
-                   choices=["clusters3d", "uniform2d", "planes3d"])
+                   choices=["clusters3d", "uniform2d", "planes3d", "unit64", "polylines"])
     p.add_argument("--n", type=int, default=0, help="points per set (default: workload size)")
     p.add_argument("--variant", default="auto")
     p.add_argument("--directed", action="store_true")
@@ -61,12 +61,13 @@ def parse():
     return p.parse_args()
 
 
-WORKLOAD_SIZES = {"clusters3d": 10_000_000, "uniform2d": 200_000, "planes3d": 50_000_000}
+WORKLOAD_SIZES = {"clusters3d": 10_000_000, "uniform2d": 200_000, "planes3d": 50_000_000,
+                  "unit64": 1_000_000, "polylines": 100_000}
 
 
 def make_data(name, n):
     from hausdorffdistance_gb300 import synth
-    seed = {"clusters3d": 2, "uniform2d": 1, "planes3d": 5}[name]
+    seed = {"clusters3d": 2, "uniform2d": 1, "planes3d": 5, "unit64": 3}[name]
     return getattr(synth, name)(n, seed=seed)
 
 
@@ -75,6 +76,8 @@ def workload_desc(name, n):
         "clusters3d": f"3-D Gaussian mixture, 64 clusters sigma 0.01, |A|=|B|={n}, B shifted (0.05,0,0)",
         "uniform2d": f"2-D uniform, |A|=|B|={n}, B = jittered permutation of A + 5% outliers",
         "planes3d": f"3-D LiDAR-like planes, |A|=|B|={n}, B = A rotated 1 deg + 0.1% outliers",
+        "unit64": f"64-D unit rows, |A|=|B|={n}, B = A with 1% of rows replaced",
+        "polylines": f"{n} 2-D polyline-pair problems, lognormal sizes (median 200, sigma 1.2)",
     }[name]
 
 
@@ -164,6 +167,25 @@ def cpu_baseline(a, b, undirected, max_seconds=25.0):
     import hd_oracle
     cores = os.cpu_count() or 1
     dirs = [(a, b), (b, a)] if undirected else [(a, b)]
+    if a.shape[1] not in (2, 3):
+        # The reference has no path for n_dims other than 2 and 3: time the
+        # oracle's exact FP32 max-min (not reference code) on the first k rows
+        # of A against all of B and extrapolate linearly (no early break).
+        total_ms = 0.0
+        detail = []
+        for x, y in dirs:
+            k = max(16, min(len(x), 64))
+            t0 = time.perf_counter()
+            hd_oracle.exact(x[:k], y, 32, n_threads=cores)
+            ms = (time.perf_counter() - t0) * 1e3
+            est = ms * len(x) / k
+            total_ms += est
+            detail.append({"sample_rows": k, "sample_ms": ms, "extrapolated_ms": est})
+        return {"value": 1000.0 / total_ms, "unit": "solves/s", "cores": cores, "kind": "port",
+                "sample": ("oracle exact FP32 max-min restatement (not reference code: the "
+                           "reference supports n_dims 2 and 3 only), all host threads, first k "
+                           "rows of A against all of B, extrapolated linearly: "
+                           + json.dumps(detail))}
     total_ms = 0.0
     detail = []
     budget = max_seconds / len(dirs)
@@ -195,12 +217,18 @@ def run_reference(args):
     if rank != 0:
         return
     n = args.n or WORKLOAD_SIZES[args.workload]
-    a, b = make_data(args.workload, n)
     undirected = not args.directed
+    if args.workload == "polylines":
+        from hausdorffdistance_gb300 import synth
+        a, b, off = synth.polylines(n_problems=n, seed=4)
+        measure = lambda: cpu_baseline_batch(a, b, off, undirected, max_seconds=8.0)  # noqa: E731
+    else:
+        a, b = make_data(args.workload, n)
+        measure = lambda: cpu_baseline(a, b, undirected, max_seconds=8.0)  # noqa: E731
     vals = []
     base = None
     for i in range(args.warmup + args.steps):
-        base = cpu_baseline(a, b, undirected, max_seconds=8.0)
+        base = measure()
         if i >= args.warmup:
             vals.append(base["value"])
     v = float(np.median(vals))
@@ -217,10 +245,133 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def cpu_baseline_batch(a, b, off, undirected, max_seconds=20.0):
+    """Reference CPU early-break (oracle restatement), one thread per problem,
+    problems spread over all host cores, on the first k problems of the
+    (randomly ordered) batch; extrapolated to the whole batch by pair count."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import concurrent.futures as cf
+    import hd_oracle
+    cores = os.cpu_count() or 1
+    sizes = np.diff(off)
+    pairs = sizes.astype(np.float64) ** 2
+    k = 0
+    acc = 0.0
+    budget_pairs = 4e9 * max_seconds / 20.0  # ~ what the cores finish in the budget
+    while k < len(sizes) and acc < budget_pairs:
+        acc += pairs[k]
+        k += 1
+
+    def one(p):
+        x, y = a[off[p]:off[p + 1]], b[off[p]:off[p + 1]]
+        hd_oracle.eb(x, y, n_threads=1)
+        if undirected:
+            hd_oracle.eb(y, x, n_threads=1)
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+        list(ex.map(one, range(k)))
+    t = time.perf_counter() - t0
+    est = t * pairs.sum() / pairs[:k].sum()
+    return {"value": len(sizes) / est, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": (f"reference CPU early-break restated (oracle/hd_oracle.cpp), n_threads=1 "
+                       f"per problem, problems spread over {cores} host threads; first {k} of "
+                       f"{len(sizes)} problems ({t:.2f} s), extrapolated by pair count")}
+
+
+def main_batch(args):
+    import torch
+
+    import hausdorffdistance_gb300 as hd
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    n = args.n or WORKLOAD_SIZES["polylines"]
+    from hausdorffdistance_gb300 import synth
+    a, b, off = synth.polylines(n_problems=n, seed=4)
+    undirected = not args.directed
+    stream = torch.cuda.current_stream()
+    eng = hd.Engine(device=local)
+    eng.set_stream(stream.cuda_stream)
+    ta = torch.from_numpy(a).cuda()
+    tb = torch.from_numpy(b).cuda()
+    if args.profile:
+        eng.solve_batch(ta, tb, off, off, undirected=undirected)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_solve": True}), flush=True)
+        return
+    for _ in range(args.warmup):
+        ref = eng.solve_batch(ta, tb, off, off, undirected=undirected)
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = eng.kernel_launches
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        res = eng.solve_batch(ta, tb, off, off, undirected=undirected)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    launches = eng.kernel_launches - l0
+    assert np.array_equal(res["hd_f32"], ref["hd_f32"])
+    value = world * n / (ms / 1e3)
+    pa = torch.from_numpy(a).pin_memory().numpy()
+    pb = torch.from_numpy(b).pin_memory().numpy()
+    eng.solve_batch(pa, pb, off, off, undirected=undirected)
+    t0 = time.perf_counter()
+    ke = max(3, args.steps // 2)
+    for _ in range(ke):
+        eng.solve_batch(pa, pb, off, off, undirected=undirected)
+    t_e2e = (time.perf_counter() - t0) / ke
+    plain = None
+    if not args.no_compare:
+        t0 = time.perf_counter()
+        rp = eng.solve_batch(ta, tb, off, off, undirected=undirected, plain=True)
+        torch.cuda.synchronize()
+        tp = time.perf_counter() - t0
+        assert np.array_equal(rp["hd_f32"], res["hd_f32"]), "plain and batched disagree"
+        plain = {"variant": "per-problem plain EB launches", "ms_per_step": tp * 1e3,
+                 "solves_per_s": n / tp, "speedup_batched_vs_plain": tp * 1e3 / ms}
+    peak, peak_kind = load_peaks()
+    sizes = np.diff(off)
+    alg = float((2 if undirected else 1) * (2 * sizes).sum() * 8)  # both sets, both directions
+    achieved = alg / (ms / 1e3) / 1e9
+    roof = {"bound": "hbm", "kernel": "batch_graph", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "traffic": traffic_from_profiles("batch", 1),
+            "algorithmic_bytes": alg, "kernel_ms": ms, "peak_source": peak_kind + " hbm_gbs"}
+    base = None if (args.no_cpu or world > 1) else cpu_baseline_batch(a, b, off, undirected)
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded numpy PCG64)",
+            "config": {"workload": (f"{n} 2-D polyline-pair problems, sizes round(LogNormal(ln 200,"
+                                    f" 1.2)) clipped to [8, 50000], {int(sizes.sum())} points "
+                                    "per side"), "undirected": undirected,
+                       "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+            "gpairs_per_s_effective": float((sizes.astype(np.float64) ** 2).sum()
+                                            * (2 if undirected else 1) / (ms / 1e3) / 1e9),
+            "plain_per_problem": plain,
+            "e2e": {"value": world * n / t_e2e, "unit": "solves/s",
+                    "h2d_bytes_per_step": int(a.nbytes + b.nbytes + n * 32),
+                    "d2h_bytes_per_step": int(n * 16)},
+            "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": base, "clocks": clk,
+        }), flush=True)
+    eng.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "polylines":
+        main_batch(args)
         return
     import torch
     import torch.distributed as dist
@@ -356,6 +507,24 @@ def main():
                 "kernel_ms": t_ms, "peak_source": peak_kind + " hbm_gbs",
                 "pairs_per_s": rc.visited_pairs / (t_ms / 1e3)}
 
+    if res.variant_used == hd._lib.VARIANT_BF16:
+        # Split-BF16 contraction: 3 products x 2 K FLOP per (a, b) pair per
+        # direction, against the sustained dense BF16 rate (a long kernel).
+        K = ((dims + 15) // 16) * 16
+        flops = (2 if undirected else 1) * 3.0 * 2.0 * K * float(n) * float(n)
+        t_ms = phase_avg[3]
+        try:
+            with open(PEAKS_PATH) as f:
+                pk = json.load(f)
+            tpeak, tkind = float(pk["bf16_tflops_sustained"]), "measured bf16_tflops_sustained"
+        except Exception:
+            tpeak, tkind = 1700.0, "fallback sustained bf16"
+        achieved = flops / (t_ms / 1e3) / 1e12
+        roof = {"bound": "tensor", "kernel": "bf16_rowmin", "achieved": achieved, "peak": tpeak,
+                "unit": "TFLOP/s", "frac": achieved / tpeak,
+                "traffic": traffic_from_profiles("bf16_rowmin", 1), "algorithmic_flops": flops,
+                "kernel_ms": t_ms, "peak_source": tkind,
+                "rechecked_rows": int(res.rechecked), "err_bound": res.err_bound}
     base = None
     if rank == 0 and world == 1 and not args.no_cpu:
         base = cpu_baseline(a, b, undirected)

@@ -164,6 +164,31 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
+// Two 32-column loads, one wait.
+__device__ __forceinline__ void tmem_ld32x2(uint32_t taddr, float* v) {
+  uint32_t r[64];
+#define HD_TMEM_LD32(OFF, BASE)                                                                 \
+  asm volatile(                                                                                 \
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "                                                 \
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"                                 \
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"                \
+      : "=r"(r[BASE + 0]), "=r"(r[BASE + 1]), "=r"(r[BASE + 2]), "=r"(r[BASE + 3]),             \
+        "=r"(r[BASE + 4]), "=r"(r[BASE + 5]), "=r"(r[BASE + 6]), "=r"(r[BASE + 7]),             \
+        "=r"(r[BASE + 8]), "=r"(r[BASE + 9]), "=r"(r[BASE + 10]), "=r"(r[BASE + 11]),           \
+        "=r"(r[BASE + 12]), "=r"(r[BASE + 13]), "=r"(r[BASE + 14]), "=r"(r[BASE + 15]),         \
+        "=r"(r[BASE + 16]), "=r"(r[BASE + 17]), "=r"(r[BASE + 18]), "=r"(r[BASE + 19]),         \
+        "=r"(r[BASE + 20]), "=r"(r[BASE + 21]), "=r"(r[BASE + 22]), "=r"(r[BASE + 23]),         \
+        "=r"(r[BASE + 24]), "=r"(r[BASE + 25]), "=r"(r[BASE + 26]), "=r"(r[BASE + 27]),         \
+        "=r"(r[BASE + 28]), "=r"(r[BASE + 29]), "=r"(r[BASE + 30]), "=r"(r[BASE + 31])          \
+      : "r"(taddr + (OFF)))
+  HD_TMEM_LD32(0u, 0);
+  HD_TMEM_LD32(32u, 32);
+#undef HD_TMEM_LD32
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   uint32_t r[32];
   asm volatile(
@@ -215,6 +240,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t a_full, b_full[2], b_empty[2], acc_full[2], acc_empty[2];
   __shared__ uint32_t tmem_base;
+  __shared__ __align__(16) float s_bn[2][kBN];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned char* sA = smem;
@@ -302,36 +328,51 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else {
-    // Epilogue: warp w reads TMEM lanes [32 (w % 4), +32): one A row per thread.
+    // Epilogue: warp w reads TMEM lanes [32 (w % 4), +32): one A row per
+    // thread.  ||b||^2 of the current tile is staged in shared memory by the
+    // 128 epilogue threads (two floats each) ahead of the accumulator wait;
+    // eight independent partial minima keep the FP32 pipes busy.
     const int quad = warp & 3;
+    const int etid = (warp - 2) * 32 + lane;  // 0..127
     const uint32_t row_in_block = (uint32_t) (quad * 32 + lane);
     const uint64_t row = (uint64_t) blockIdx.x * kBM + row_in_block;
-    float m = INFINITY;
+    float m8[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) m8[q] = INFINITY;
     for (uint32_t t = 0; t < nTilesB; ++t) {
       const int buf = t & 1;
+      const float2 bnv = __ldg(reinterpret_cast<const float2*>(bnorm + (uint64_t) t * kBN) + etid);
+      reinterpret_cast<float2*>(s_bn[buf])[etid] = bnv;
+      // All epilogue threads have written this tile's norms, and all have
+      // finished reading the buffer's previous contents (tile t - 2).
+      asm volatile("bar.sync 1, 128;" ::: "memory");
       ok = mbar_wait(&acc_full[buf], (t >> 1) & 1, status, kWaitLimit);
       if (__any_sync(0xFFFFFFFFu, !ok)) {
         ok = false;
         break;
       }
       tc_fence_after();
-      const float4* bn4 = reinterpret_cast<const float4*>(bnorm + (uint64_t) t * kBN);
+      const float4* bn4 = reinterpret_cast<const float4*>(s_bn[buf]);
 #pragma unroll 1
-      for (int cc = 0; cc < kBN / 32; ++cc) {
-        float v[32];
-        tmem_ld32(tmem + ((uint32_t) (quad * 32) << 16) + (uint32_t) buf * kBN + cc * 32, v);
+      for (int cc = 0; cc < kBN / 64; ++cc) {
+        float v[64];
+        tmem_ld32x2(tmem + ((uint32_t) (quad * 32) << 16) + (uint32_t) buf * kBN + cc * 64, v);
 #pragma unroll
-        for (int j4 = 0; j4 < 8; ++j4) {
-          const float4 bn = __ldg(bn4 + cc * 8 + j4);
-          m = fminf(m, fmaf(-2.0f, v[4 * j4 + 0], bn.x));
-          m = fminf(m, fmaf(-2.0f, v[4 * j4 + 1], bn.y));
-          m = fminf(m, fmaf(-2.0f, v[4 * j4 + 2], bn.z));
-          m = fminf(m, fmaf(-2.0f, v[4 * j4 + 3], bn.w));
+        for (int j4 = 0; j4 < 16; ++j4) {
+          const float4 bn = bn4[cc * 16 + j4];
+          const int q = (j4 & 1) * 4;
+          m8[q + 0] = fminf(m8[q + 0], fmaf(-2.0f, v[4 * j4 + 0], bn.x));
+          m8[q + 1] = fminf(m8[q + 1], fmaf(-2.0f, v[4 * j4 + 1], bn.y));
+          m8[q + 2] = fminf(m8[q + 2], fmaf(-2.0f, v[4 * j4 + 2], bn.z));
+          m8[q + 3] = fminf(m8[q + 3], fmaf(-2.0f, v[4 * j4 + 3], bn.w));
         }
       }
       tc_fence_before();
       mbar_arrive(&acc_empty[buf]);
     }
+    float m = m8[0];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) m = fminf(m, m8[q]);
     if (ok && row < nA) {
       const float an = anorm[row];
       const float mi = an + m;
@@ -366,39 +407,62 @@ __global__ void k_bf16_candidates(const float* __restrict__ rowmin, const float*
   }
 }
 
-// Exact FP32 re-scan of a candidate row (reference formula), one CTA each,
-// with early break against the running maximum of exact row minima.
+// Exact FP32 re-scan of the candidate rows with the reference formula: every
+// CTA takes a slice of B for one candidate (blockIdx.y strides over the
+// candidates), and the slice minima meet in one atomicMin per CTA on the
+// squared distance's bits (non-negative floats order like their bits).
 __global__ void __launch_bounds__(256)
     k_bf16_recheck(const float* __restrict__ A, const float* __restrict__ B, uint64_t nB, int D,
-                   const uint32_t* __restrict__ list, const Bf16Scalars* bs, DevScalars* sc) {
-  __shared__ float red[8];
-  __shared__ float s_thr;
-  __shared__ float sa[256];
+                   const uint32_t* __restrict__ list, const Bf16Scalars* bs,
+                   uint32_t* __restrict__ cand_min) {
+  __shared__ __align__(16) float sa[256];
+  __shared__ uint32_t red[8];
   const uint32_t n = bs->cand;
-  for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
+  const bool vec = (D % 4) == 0 && ((reinterpret_cast<uintptr_t>(B) & 15) == 0);
+  for (uint32_t e = blockIdx.y; e < n; e += gridDim.y) {
     const uint32_t ia = list[e];
     __syncthreads();
     for (int k = threadIdx.x; k < D; k += blockDim.x) sa[k] = A[(uint64_t) ia * D + k];
     __syncthreads();
-    float cmin = INFINITY;
-    bool broke = false;
-    const uint64_t chunk = 256 * 32;
-    for (uint64_t base = 0; base < nB && !broke; base += chunk) {
-      float m = INFINITY;
-      const uint64_t end = min(nB, base + chunk);
-      for (uint64_t j = base + threadIdx.x; j < end; j += 256) m = fminf(m, d2_n(sa, B + j * D, D));
-#pragma unroll
-      for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
-      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-      if (threadIdx.x == 0) s_thr = threshold_of(ld_relaxed_u64(&sc->max_key));
-      __syncthreads();
-      for (int k = 0; k < 8; ++k) cmin = fminf(cmin, red[k]);
-      const float thr = s_thr;
-      __syncthreads();
-      if (cmin <= thr) broke = true;
+    float m = INFINITY;
+    for (uint64_t j = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; j < nB;
+         j += (uint64_t) gridDim.x * blockDim.x) {
+      const float* br = B + j * D;
+      float s = 0.0f;
+      if (vec) {
+        const float4* b4 = reinterpret_cast<const float4*>(br);
+        for (int k4 = 0; k4 < D / 4; ++k4) {
+          const float4 b = __ldg(b4 + k4);
+          const float d0 = __fsub_rn(sa[4 * k4], b.x), d1 = __fsub_rn(sa[4 * k4 + 1], b.y);
+          const float d2 = __fsub_rn(sa[4 * k4 + 2], b.z), d3 = __fsub_rn(sa[4 * k4 + 3], b.w);
+          s = k4 == 0 ? __fmul_rn(d0, d0) : __fadd_rn(s, __fmul_rn(d0, d0));
+          s = __fadd_rn(s, __fmul_rn(d1, d1));
+          s = __fadd_rn(s, __fmul_rn(d2, d2));
+          s = __fadd_rn(s, __fmul_rn(d3, d3));
+        }
+      } else {
+        s = d2_n(sa, br, D);
+      }
+      m = fminf(m, s);
     }
-    if (!broke && threadIdx.x == 0) atomicMax(&sc->max_key, pack_max(cmin, ia));
+    uint32_t u = __float_as_uint(m);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) u = min(u, __shfl_xor_sync(0xFFFFFFFFu, u, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t b = red[0];
+      for (int k = 1; k < 8; ++k) b = min(b, red[k]);
+      atomicMin(&cand_min[e], b);
+    }
   }
+}
+
+__global__ void k_bf16_recheck_final(const uint32_t* __restrict__ list, const Bf16Scalars* bs,
+                                     const uint32_t* __restrict__ cand_min, DevScalars* sc) {
+  const uint32_t n = bs->cand;
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
+    atomicMax(&sc->max_key, pack_max(__uint_as_float(cand_min[e]), list[e]));
 }
 
 template <int Kp>
@@ -413,7 +477,7 @@ hd_status run_bf16_k(Ctx& c, const DirInput& in, DirResult* extra, float* rowmin
   if ((s = ensure(c, kBufNormsA, padA * 4, &na)) != HD_OK) return s;
   if ((s = ensure(c, kBufNormsB, padB * 4, &nb)) != HD_OK) return s;
   if ((s = ensure(c, kBufRowMin, padA * 4, &rm)) != HD_OK) return s;
-  if ((s = ensure(c, kBufCand, in.nA * 4 + 64, &cand)) != HD_OK) return s;
+  if ((s = ensure(c, kBufCand, in.nA * 8 + 128, &cand)) != HD_OK) return s;
   if ((s = ensure(c, kBufAux2, sizeof(Bf16Scalars), &bsv)) != HD_OK) return s;
   Bf16Scalars* bs = (Bf16Scalars*) bsv;
   cudaError_t e;
@@ -433,13 +497,14 @@ hd_status run_bf16_k(Ctx& c, const DirInput& in, DirResult* extra, float* rowmin
   if ((s = after_launch(c, "bf16_norms")) != HD_OK) return s;
   mark(c, 1);
   mark(c, 2);
+  mark(c, 3);
   auto kern = k_bf16_rowmin<Kp>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kSmemBytes);
   kern<<<(unsigned) nTA, kThreads, kSmemBytes, c.stream>>>(
       (const unsigned char*) pa, (const unsigned char*) pb, (const float*) na, (const float*) nb,
       in.nA, (uint32_t) nTB, (float*) rm, bs);
   if ((s = after_launch(c, "bf16_rowmin")) != HD_OK) return s;
-  mark(c, 3);
+  mark(c, 4);
   if (rowmin_host) {
     e = cudaMemcpyAsync(rowmin_host, rm, in.nA * 4, cudaMemcpyDeviceToHost, c.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
@@ -454,10 +519,15 @@ hd_status run_bf16_k(Ctx& c, const DirInput& in, DirResult* extra, float* rowmin
                                                          Kp, bs, (uint32_t*) cand);
   if ((s = after_launch(c, "bf16_candidates")) != HD_OK) return s;
   DevScalars* sc = scalars(c, in.dir);
-  k_bf16_recheck<<<c.num_sms * 2, 256, 0, c.stream>>>(in.A, in.B, in.nB, in.dims,
-                                                     (const uint32_t*) cand, bs, sc);
+  // Candidate minima live after the candidate list (one uint per row of A).
+  uint32_t* cand_min = (uint32_t*) cand + in.nA + 16;
+  if ((e = cudaMemsetAsync(cand_min, 0xFF, in.nA * 4, c.stream)) != cudaSuccess)
+    return cuda_fail(c, e, "memset");
+  k_bf16_recheck<<<dim3(c.num_sms * 2, 16), 256, 0, c.stream>>>(in.A, in.B, in.nB, in.dims,
+                                                               (const uint32_t*) cand, bs, cand_min);
   if ((s = after_launch(c, "bf16_recheck")) != HD_OK) return s;
-  mark(c, 4);
+  k_bf16_recheck_final<<<c.num_sms, 256, 0, c.stream>>>((const uint32_t*) cand, bs, cand_min, sc);
+  if ((s = after_launch(c, "bf16_recheck_final")) != HD_OK) return s;
   // Bound and recheck statistics for the result (small copy, after the work).
   Bf16Scalars h;
   e = cudaMemcpyAsync(&h, bs, sizeof(h), cudaMemcpyDeviceToHost, c.stream);

@@ -127,6 +127,8 @@ __global__ void k_argmin(const float* __restrict__ A, const float* __restrict__ 
   const uint32_t ia = unpack_max_index(key);
   float a[4] = {0, 0, 0, 0};
   const bool small = D <= 4;
+  const bool vec = D > 4 && (D % 4) == 0 && ((reinterpret_cast<uintptr_t>(A) & 15) == 0) &&
+                   ((reinterpret_cast<uintptr_t>(B) & 15) == 0);
   if (small)
     for (int k = 0; k < D; ++k) a[k] = A[(uint64_t) ia * D + k];
   unsigned long long best = ~0ull;
@@ -137,6 +139,21 @@ __global__ void k_argmin(const float* __restrict__ A, const float* __restrict__ 
       d2 = d2_2(a[0], a[1], B[2 * j], B[2 * j + 1]);
     } else if (D == 3) {
       d2 = d2_3(a[0], a[1], a[2], B[3 * j], B[3 * j + 1], B[3 * j + 2]);
+    } else if (vec) {
+      // Same left-to-right formula, 16-byte loads.
+      const float4* b4 = reinterpret_cast<const float4*>(B + j * D);
+      const float4* a4 = reinterpret_cast<const float4*>(A + (uint64_t) ia * D);
+      float s = 0.0f;
+      for (int k4 = 0; k4 < D / 4; ++k4) {
+        const float4 b = __ldg(b4 + k4), a = __ldg(a4 + k4);
+        const float d0 = __fsub_rn(a.x, b.x), d1 = __fsub_rn(a.y, b.y);
+        const float dd2 = __fsub_rn(a.z, b.z), d3 = __fsub_rn(a.w, b.w);
+        s = k4 == 0 ? __fmul_rn(d0, d0) : __fadd_rn(s, __fmul_rn(d0, d0));
+        s = __fadd_rn(s, __fmul_rn(d1, d1));
+        s = __fadd_rn(s, __fmul_rn(dd2, dd2));
+        s = __fadd_rn(s, __fmul_rn(d3, d3));
+      }
+      d2 = s;
     } else {
       d2 = d2_n(A + (uint64_t) ia * D, B + j * D, D);
     }

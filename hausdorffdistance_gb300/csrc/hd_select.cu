@@ -6,10 +6,10 @@
 // "p80 < eb_only_threshold" from a generated XGBoost tree,
 // src/models/tree_ebonlythreshold_3d.h) with a project-written rule:
 //
-//   1. k points of A (k = sample_rate * |A|, clamped to [256, 2048]) run the
+//   1. k points of A (k = sample_rate * |A|, clamped to [64, 256]) run the
 //      early-break scan against B, one CTA each, B visited in a pseudo-random
 //      order, counting the B points each visited before it stopped (capped at
-//      65,536).  The completed samples also seed the running maximum that the
+//      16,384).  The completed samples also seed the running maximum that the
 //      chosen variant starts from.
 //   2. The EB cost of the full set is ~ |A| * p80 pairs; the index-based cost
 //      is ~ |A| + |B| point operations.  EB is chosen when
@@ -31,7 +31,7 @@
 namespace hdg {
 namespace {
 
-constexpr uint32_t kSampleCap = 65536;
+constexpr uint32_t kSampleCap = 16384;
 
 __global__ void __launch_bounds__(256)
     k_sample_eb(const float* __restrict__ A, Perm pA, const float* __restrict__ B, Perm pB,
@@ -91,7 +91,7 @@ hd_status select_variant(Ctx& c, const DirInput& in, int* v) {
     return HD_OK;
   }
   const double rate = c.opt.sample_rate > 0 ? c.opt.sample_rate : 0.01;
-  uint32_t k = (uint32_t) std::min<double>(std::max<double>(rate * (double) in.nA, 256.0), 2048.0);
+  uint32_t k = (uint32_t) std::min<double>(std::max<double>(rate * (double) in.nA, 64.0), 256.0);
   k = (uint32_t) std::min<uint64_t>(k, in.nA);
   void* buf;
   hd_status s = ensure(c, kBufCand, (size_t) k * 4, &buf);
