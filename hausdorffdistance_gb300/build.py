@@ -83,8 +83,13 @@ def build_exec() -> str:
     hdrs = [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")]
     if _newer(EXE, srcs + hdrs + [LIB, os.path.join(INCLUDE, "hd_gpu.h")]):
         return EXE
-    _run(["g++", "-std=c++17", "-O2", "-pthread", f"-I{INCLUDE}", f"-I{HOST}"] + srcs
-         + ["-o", EXE, f"-L{OUT}", "-lhdgpu", "-Wl,-rpath,$ORIGIN"])
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(_nvcc())))
+    libdir = next((d for d in (os.path.join(cuda, "lib64"), os.path.join(cuda, "lib"))
+                   if os.path.isdir(d)), os.path.join(cuda, "lib64"))
+    _run(["g++", "-std=c++17", "-O2", "-pthread", f"-I{INCLUDE}", f"-I{HOST}",
+          f"-I{os.path.join(cuda, 'include')}"] + srcs
+         + ["-o", EXE, f"-L{OUT}", "-lhdgpu", f"-L{libdir}", "-lcudart",
+            "-Wl,-rpath,$ORIGIN", f"-Wl,-rpath,{libdir}"])
     return EXE
 
 

@@ -397,6 +397,7 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   c->timing = (flags & HD_TIMING) != 0;
   c->sorted_valid = false;
   c->ev_base = 0;
+  c->last_p80[0] = c->last_p80[1] = 0.0;
 
   hd_status s;
   const float* dA = A;
@@ -449,6 +450,8 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   out->visited_leaves = r0.leaves + (undirected ? h->s[1].leaves : 0);
   out->variant_used = used[0];
   out->variant_used_ba = undirected ? used[1] : -1;
+  out->sample_p80[0] = c->last_p80[0];
+  out->sample_p80[1] = undirected ? c->last_p80[1] : 0.0;
   out->err_bound = std::max(ex[0].err_bound, ex[1].err_bound);
   out->rechecked = ex[0].rechecked + ex[1].rechecked;
   if (c->timing) {

@@ -1,0 +1,367 @@
+// hd_exec — command-line driver with the reference's flags
+// (src/flags.cc:1-58, src/main.cpp:33-152, src/run_hausdorff_distance.cu:53-402)
+// over libhdgpu.so.  Prints "Time: <avg> ms" and
+// "HausdorffDistance: distance is <d>" and writes the reference's JSON keys.
+//
+// Differences: -execution cpu is not offered (this is the GPU engine; the
+// reference's own build provides its CPU path); -check verifies the result
+// against the engine's plain early-break variant (same exact FP32
+// semantics) instead of the CPU early-break; -undirected computes
+// max(h(A,B), h(B,A)) in one call; -input_type also accepts "bin" (the
+// reference's point-cache layout); -variant accepts eb | hybrid | auto | rt |
+// lbvh | grid | bf16 | brute.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "hausdorff_distance.h"
+#include "hd_gpu.h"
+#include "json.h"
+#include "loaders.h"
+
+namespace {
+
+struct Flags {
+  std::map<std::string, std::string> v;
+  std::string get(const std::string& k, const std::string& def) const {
+    auto it = v.find(k);
+    return it == v.end() ? def : it->second;
+  }
+  long long geti(const std::string& k, long long def) const {
+    auto it = v.find(k);
+    return it == v.end() ? def : std::atoll(it->second.c_str());
+  }
+  double getd(const std::string& k, double def) const {
+    auto it = v.find(k);
+    return it == v.end() ? def : std::atof(it->second.c_str());
+  }
+  bool getb(const std::string& k, bool def) const {
+    auto it = v.find(k);
+    if (it == v.end()) return def;
+    const std::string& s = it->second;
+    return !(s == "false" || s == "0" || s == "no");
+  }
+};
+
+const char* kBoolFlags[] = {"is_double", "normalize", "auto_tune", "auto_tune_eb_only_threshold",
+                            "auto_tune_n_points_cell", "auto_tune_max_hit", "fast_build_bvh",
+                            "rebuild_bvh", "rt_prune", "rt_eb", "overwrite", "check",
+                            "vary_params", "undirected"};
+
+bool is_bool_flag(const std::string& k) {
+  for (const char* b : kBoolFlags)
+    if (k == b) return true;
+  return false;
+}
+
+// gflags syntax: -name=value, --name=value, -name value, -boolflag,
+// -noboolflag.
+Flags parse(int argc, char** argv) {
+  Flags f;
+  for (int i = 1; i < argc; ++i) {
+    std::string a = argv[i];
+    if (a.size() < 2 || a[0] != '-') {
+      std::fprintf(stderr, "unexpected argument %s\n", a.c_str());
+      std::exit(1);
+    }
+    a = a.substr(a[1] == '-' ? 2 : 1);
+    const size_t eq = a.find('=');
+    if (eq != std::string::npos) {
+      f.v[a.substr(0, eq)] = a.substr(eq + 1);
+    } else if (is_bool_flag(a)) {
+      f.v[a] = "true";
+    } else if (a.rfind("no", 0) == 0 && is_bool_flag(a.substr(2))) {
+      f.v[a.substr(2)] = "false";
+    } else if (i + 1 < argc) {
+      f.v[a] = argv[++i];
+    } else {
+      std::fprintf(stderr, "flag -%s needs a value\n", a.c_str());
+      std::exit(1);
+    }
+  }
+  return f;
+}
+
+std::string lower(std::string s) {
+  for (auto& ch : s) ch = (char) std::tolower((unsigned char) ch);
+  return s;
+}
+
+std::string now_string() {
+  std::time_t t = std::time(nullptr);
+  std::tm tmv;
+  localtime_r(&t, &tmv);
+  char buf[64];
+  std::strftime(buf, sizeof(buf), "%Y-%m-%d %H:%M:%S", &tmv);
+  return buf;
+}
+
+void usage(const char* argv0) {
+  std::fprintf(stderr,
+               "Usage: %s -input1 A -input2 B -input_type wkt|off|ply|bin -n_dims 2|3|<d> "
+               "[-variant eb|hybrid|rt|lbvh|grid|bf16|brute] [-execution gpu] [-repeat 5] "
+               "[-seed 0] [-check] [-json out.json] [-serialize dir] [-limit n] [-normalize] "
+               "[-translate r] [-undirected] [-sample_rate 0.01] [-n_points_cell 8] "
+               "[-eb_only_threshold 0] [-device 0]\n",
+               argv0);
+}
+
+std::vector<double> split_doubles(const std::string& s) {
+  std::vector<double> out;
+  std::stringstream ss(s);
+  std::string tok;
+  while (std::getline(ss, tok, ','))
+    if (!tok.empty()) out.push_back(std::atof(tok.c_str()));
+  return out;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc == 1) {
+    usage(argv[0]);
+    return 1;
+  }
+  Flags fl = parse(argc, argv);
+  const std::string input1 = fl.get("input1", ""), input2 = fl.get("input2", "");
+  const std::string input_type = lower(fl.get("input_type", ""));
+  if (input_type != "wkt" && input_type != "off" && input_type != "ply" && input_type != "bin") {
+    std::fprintf(stderr, "Unsupported input type: %s\n", input_type.c_str());
+    return 1;
+  }
+  const int dims = (int) fl.geti("n_dims", 0);
+  if (dims < 1 || dims > 128) {
+    std::fprintf(stderr, "Wrong number of dimensions: %d\n", dims);
+    return 1;
+  }
+  if ((input_type == "wkt" || input_type == "off" || input_type == "ply") && dims != 2 && dims != 3) {
+    std::fprintf(stderr, "%s inputs have 2 or 3 dimensions\n", input_type.c_str());
+    return 1;
+  }
+  if (fl.getb("is_double", false)) {
+    std::fprintf(stderr, "double inputs are not supported (the engine computes in float32)\n");
+    return 1;
+  }
+  if (lower(fl.get("execution", "gpu")) != "gpu") {
+    std::fprintf(stderr,
+                 "-execution cpu: this driver runs the GPU engine only; the reference's own "
+                 "build provides the CPU early-break path\n");
+    return 1;
+  }
+  const std::string vname = lower(fl.get("variant", "eb"));
+  int variant;
+  if (vname == "eb") variant = HD_VARIANT_EB;
+  else if (vname == "hybrid" || vname == "auto") variant = HD_VARIANT_AUTO;
+  else if (vname == "rt" || vname == "lbvh") variant = HD_VARIANT_LBVH;
+  else if (vname == "grid") variant = HD_VARIANT_GRID;
+  else if (vname == "bf16") variant = HD_VARIANT_BF16;
+  else if (vname == "brute") variant = HD_VARIANT_BRUTE;
+  else {
+    std::fprintf(stderr, "Unknown or unsupported variant: %s\n", vname.c_str());
+    return 1;
+  }
+  const long long limit = fl.geti("limit", 0x7FFFFFFF);
+  const int repeat = (int) std::max<long long>(1, fl.geti("repeat", 5));
+  const bool undirected = fl.getb("undirected", false);
+  const bool check = fl.getb("check", true);
+
+  hd::PointSet pa, pb;
+  try {
+    pa = hd::LoadPoints(input1, input_type, dims, limit, fl.get("serialize", ""));
+    pb = hd::LoadPoints(input2, input_type, dims, limit, fl.get("serialize", ""));
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "%s\n", e.what());
+    return 1;
+  }
+  if (pa.size() == 0 || pb.size() == 0) {
+    std::fprintf(stderr, "empty input: %s has %zu points, %s has %zu\n", input1.c_str(), pa.size(),
+                 input2.c_str(), pb.size());
+    return 1;
+  }
+  const bool normalize = fl.getb("normalize", false);
+  const double translate = fl.getd("translate", 0.0);
+  if (normalize) {
+    hd::NormalizePoints(pa);
+    hd::NormalizePoints(pb);
+  }
+  if (translate != 0.0) hd::TranslatePoints(pb, 0, translate);
+  for (size_t i = 0; i < std::min<size_t>(10, std::min(pa.size(), pb.size())); ++i) {
+    std::printf("%zu A", i);
+    for (int k = 0; k < std::min(dims, 3); ++k) std::printf("%s%.6f", k ? "," : " ", pa.xyz[i * dims + k]);
+    std::printf(" B");
+    for (int k = 0; k < std::min(dims, 3); ++k) std::printf("%s%.6f", k ? "," : " ", pb.xyz[i * dims + k]);
+    std::printf("\n");
+  }
+
+  hd_options opt;
+  hd_default_options(&opt);
+  opt.device = (int) fl.geti("device", 0);
+  opt.seed = (uint64_t) fl.geti("seed", 0);
+  opt.sample_rate = fl.getd("sample_rate", 0.01);
+  opt.n_points_cell = (uint32_t) fl.geti("n_points_cell", 8);
+  opt.eb_only_threshold = (uint32_t) fl.geti("eb_only_threshold", 0);
+
+  hd::Json stats = hd::Json::Object();
+  int dev = opt.device;
+  cudaDeviceProp prop;
+  if (cudaSetDevice(dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+    std::fprintf(stderr, "no CUDA device %d\n", dev);
+    return 1;
+  }
+  stats["GPU"]["Device"] = dev;
+  stats["GPU"]["name"] = prop.name;
+  stats["DateTime"] = now_string();
+  hd::Json& input = stats["Input"];
+  hd::Json files = hd::Json::Array();
+  hd::Json f1 = hd::Json::Object(), f2 = hd::Json::Object();
+  f1["Path"] = input1;
+  f1["NumPoints"] = (unsigned long long) pa.size();
+  f2["Path"] = input2;
+  f2["NumPoints"] = (unsigned long long) pb.size();
+  files.push_back(f1);
+  files.push_back(f2);
+  input["Files"] = files;
+  input["Normalize"] = normalize;
+  input["Translate"] = translate;
+  input["SerializationPrefix"] = fl.get("serialize", "");
+  input["Limit"] = limit;
+  input["NumDims"] = dims;
+  input["Type"] = "Float";
+
+  // Inputs go to the device once, before the repeat loop, as in the
+  // reference (run_hausdorff_distance.cu:148); ReportedTime excludes them.
+  float *dA = nullptr, *dB = nullptr;
+  if (cudaMalloc(&dA, pa.xyz.size() * 4) != cudaSuccess ||
+      cudaMalloc(&dB, pb.xyz.size() * 4) != cudaSuccess ||
+      cudaMemcpy(dA, pa.xyz.data(), pa.xyz.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(dB, pb.xyz.data(), pb.xyz.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+    std::fprintf(stderr, "device allocation or copy failed\n");
+    return 1;
+  }
+
+  auto run = [&](const hd_options& o, hd::Json& run_json, float* out_dist) -> int {
+    hd_ctx* ctx = nullptr;
+    hd_status s = hd_create(&ctx, &o);
+    if (s != HD_OK) {
+      std::fprintf(stderr, "hd_create: %s\n", hd_status_string(s));
+      return 1;
+    }
+    double total = 0.0;
+    hd::Json repeats = hd::Json::Array();
+    hd_result r{};
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int i = 0; i < repeat; ++i) {
+      s = hd_solve(ctx, dA, pa.size(), dB, pb.size(), dims,
+                   HD_DEVICE_PTRS | HD_TIMING | HD_COUNT_PAIRS | (undirected ? HD_UNDIRECTED : 0u),
+                   variant, &r);
+      if (s != HD_OK) {
+        std::fprintf(stderr, "hd_solve: %s: %s\n", hd_status_string(s), hd_last_error(ctx));
+        hd_destroy(ctx);
+        return 1;
+      }
+      static const char* names[] = {"Hybrid", "Early Break", "Uniform Grid", "LBVH", "Split BF16",
+                                    "Brute Force"};
+      hd::Json rep = hd::Json::Object();
+      rep["Repeat"] = i + 1;
+      rep["Algorithm"] = names[variant];
+      rep["VariantUsed"] = names[r.variant_used];
+      rep["Execution"] = "GPU";
+      rep["ReportedTime"] = r.ms;
+      rep["ComparedPairs"] = (unsigned long long) r.visited_pairs;
+      rep["HD64"] = r.hd;
+      total += r.ms;
+      repeats.push_back(rep);
+    }
+    const double wall =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    run_json["Seed"] = (unsigned long long) o.seed;
+    run_json["SampleRate"] = o.sample_rate;
+    run_json["NumPointsPerCell"] = o.n_points_cell;
+    run_json["EBOnlyThreshold"] = o.eb_only_threshold;
+    run_json["Undirected"] = undirected;
+    run_json["Repeats"] = repeats;
+    run_json["AvgTime"] = total / repeat;
+    run_json["AvgWallTime"] = wall / repeat;
+    std::printf("Time: %f ms\n", total / repeat);
+    *out_dist = r.hd_f32;
+    hd_destroy(ctx);
+    return 0;
+  };
+
+  const std::string json_path = fl.get("json", "");
+  if (fl.getb("vary_params", false)) {
+    // Parameter sweep over the selector's knobs (the reference's
+    // autotune_hausdorff_distance.cu:208-299), one JSON file per combination.
+    const auto rates = split_doubles(fl.get("sample_rate_list", "0.01"));
+    const auto thresholds = split_doubles(fl.get("eb_only_threshold_list", "0"));
+    const auto cells = split_doubles(fl.get("n_points_cell_list", "8"));
+    for (double sr : rates)
+      for (double th : thresholds)
+        for (double np : cells) {
+          hd_options o = opt;
+          o.sample_rate = sr;
+          o.eb_only_threshold = (uint32_t) th;
+          o.n_points_cell = (uint32_t) np;
+          hd::Json st = stats;
+          float dist = 0.0f;
+          if (run(o, st["Running"], &dist)) return 1;
+          st["HDResult"] = dist;
+          if (!json_path.empty()) {
+            std::ostringstream name;
+            name << json_path << "_sr" << sr << "_th" << th << "_np" << np << ".json";
+            std::ofstream(name.str()) << st.dump(4);
+          }
+        }
+    return 0;
+  }
+
+  float dist = 0.0f;
+  if (run(opt, stats["Running"], &dist)) return 1;
+  stats["HDResult"] = dist;
+  std::printf("HausdorffDistance: distance is %.9g\n", dist);
+
+  if (check) {
+    // Same exact FP32 semantics through the plain early-break kernel.
+    hd_ctx* ctx = nullptr;
+    hd_options o = opt;
+    o.variant = HD_VARIANT_EB;
+    hd_result r{};
+    if (hd_create(&ctx, &o) != HD_OK ||
+        hd_solve(ctx, dA, pa.size(), dB, pb.size(), dims,
+                 HD_DEVICE_PTRS | (undirected ? HD_UNDIRECTED : 0u), HD_VARIANT_EB, &r) != HD_OK) {
+      std::fprintf(stderr, "check solve failed\n");
+      return 1;
+    }
+    hd_destroy(ctx);
+    hd::Json& ck = stats["Check"];
+    ck["HDAnswer"] = r.hd_f32;
+    ck["Diff"] = (double) r.hd_f32 - (double) dist;
+    ck["Pass"] = r.hd_f32 == dist;
+    if (r.hd_f32 != dist) {
+      std::fprintf(stderr, "Wrong HausdorffDistance. Result: %.8f Answer: %.8f\n", dist, r.hd_f32);
+    } else {
+      std::printf("HausdorffDistance is checked\n");
+    }
+  }
+  if (!json_path.empty()) {
+    const bool exists = access(json_path.c_str(), R_OK) == 0;
+    if (!exists || fl.getb("overwrite", false)) {
+      std::ofstream(json_path) << stats.dump(4);
+    } else {
+      std::fprintf(stderr, "Skip writing to JSON file %s\n", json_path.c_str());
+    }
+  }
+  cudaFree(dA);
+  cudaFree(dB);
+  return 0;
+}

@@ -100,6 +100,8 @@ typedef struct hd_result {
   double err_bound;        /* BF16: bound on |approx - exact| squared distance */
   uint64_t rechecked;      /* BF16: rows rechecked exactly in FP32             */
   uint64_t visited_leaves; /* index leaves / cells scanned (HD_COUNT_PAIRS)    */
+  double sample_p80[2];    /* AUTO: 80th percentile of the sampled early-break */
+                           /* iteration counts per direction (0 = no sample)   */
 } hd_result;
 
 /* One problem of a batch: A[offset_a .. offset_a+n_a), B[offset_b ..).

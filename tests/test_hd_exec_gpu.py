@@ -1,0 +1,92 @@
+"""The hd_exec driver and the C++ seam mirror, end to end on the golden
+inputs (GPU), plus argument handling that needs no GPU."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HERE = os.path.join(ROOT, "tests")
+BUILD = os.path.join(ROOT, "hausdorffdistance_gb300", "_build")
+EXE = os.path.join(BUILD, "hd_exec")
+GOLDEN = json.load(open(os.path.join(HERE, "golden", "golden.json")))["cases"]
+
+
+@pytest.fixture(scope="module")
+def exe():
+    from hausdorffdistance_gb300 import build
+    build.build_lib()
+    build.build_exec()
+    return EXE
+
+
+def bits(x):
+    return int(np.float32(x).view(np.uint32))
+
+
+def test_cpu_execution_and_bad_flags_rejected(exe):
+    c = GOLDEN[0]
+    base = [exe, "-input1", os.path.join(HERE, "golden", c["a"]), "-input2",
+            os.path.join(HERE, "golden", c["b"]), "-n_dims", str(c["dims"])]
+    r = subprocess.run(base + ["-input_type", "bin", "-execution", "cpu"], capture_output=True, text=True)
+    assert r.returncode == 1 and "GPU engine only" in r.stderr
+    r = subprocess.run(base + ["-input_type", "shp"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Unsupported input type" in r.stderr
+    r = subprocess.run(base + ["-input_type", "bin", "-variant", "itk"], capture_output=True, text=True)
+    assert r.returncode == 1 and "variant" in r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", ["eb", "hybrid", "rt", "grid"])
+@pytest.mark.parametrize("case", GOLDEN[:8], ids=[c["name"] for c in GOLDEN[:8]])
+def test_hd_exec_matches_reference_golden(exe, tmp_path, case, variant):
+    out = tmp_path / "run.json"
+    r = subprocess.run([exe, "-input1", os.path.join(HERE, "golden", case["a"]),
+                        "-input2", os.path.join(HERE, "golden", case["b"]), "-input_type", "bin",
+                        "-n_dims", str(case["dims"]), "-variant", variant, "-repeat", "2",
+                        "-json", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("HausdorffDistance: distance is")][0]
+    assert bits(float(line.split()[-1])) == case["hd_bits"]
+    assert "Time:" in r.stdout and "HausdorffDistance is checked" in r.stdout
+    js = json.loads(out.read_text())
+    assert js["Check"]["Pass"] is True
+    assert len(js["Running"]["Repeats"]) == 2
+    for rep in js["Running"]["Repeats"]:
+        assert {"Algorithm", "Execution", "ReportedTime"} <= set(rep)
+    assert js["Input"]["Files"][0]["NumPoints"] == case["n_a"]
+
+
+@pytest.mark.gpu
+def test_hd_exec_undirected(exe):
+    c = [g for g in GOLDEN if g["name"] == "uniform2d_3k_ab"][0]
+    d = [g for g in GOLDEN if g["name"] == "uniform2d_3k_ba"][0]
+    r = subprocess.run([exe, "-input1", os.path.join(HERE, "golden", c["a"]), "-input2",
+                        os.path.join(HERE, "golden", c["b"]), "-input_type", "bin", "-n_dims", "2",
+                        "-variant", "hybrid", "-undirected", "-repeat", "1"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("HausdorffDistance")][0]
+    assert bits(float(line.split()[-1])) == max(c["hd_bits"], d["hd_bits"])
+
+
+@pytest.mark.gpu
+def test_cpp_seam_mirror(tmp_path):
+    from hausdorffdistance_gb300 import build
+    build.build_lib()
+    probe = str(tmp_path / "seam_probe")
+    subprocess.run(["g++", "-std=c++17", "-O1", f"-I{os.path.join(ROOT, 'include')}",
+                    f"-I{os.path.join(ROOT, 'hausdorffdistance_gb300', 'host')}",
+                    os.path.join(HERE, "seam_probe.cpp"), "-o", probe, f"-L{BUILD}", "-lhdgpu",
+                    f"-Wl,-rpath,{BUILD}"], check=True)
+    c = [g for g in GOLDEN if g["name"] == "clusters3d_4k_ab"][0]
+    r = subprocess.run([probe, os.path.join(HERE, "golden", c["a"]),
+                        os.path.join(HERE, "golden", c["b"])], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.splitlines()
+    assert all(bits(float(x)) == c["hd_bits"] for x in lines[0].split())
+    stats = json.loads(lines[1])
+    assert stats["Execution"] == "GPU" and stats["Algorithm"] == "LBVH" and stats["ReportedTime"] > 0
+    assert lines[2] == "error 1"
