@@ -132,8 +132,42 @@ __global__ void k_argmin(const float* __restrict__ A, const float* __restrict__ 
   if (small)
     for (int k = 0; k < D; ++k) a[k] = A[(uint64_t) ia * D + k];
   unsigned long long best = ~0ull;
-  for (uint64_t j = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; j < nB;
-       j += (uint64_t) gridDim.x * blockDim.x) {
+  const uint64_t tid = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+  const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+  uint64_t first = 0;
+  if (D == 3 && ((reinterpret_cast<uintptr_t>(B) & 15) == 0)) {
+    // Four 3-D points per three 16-byte loads.
+    const float4* B4 = reinterpret_cast<const float4*>(B);
+    const uint64_t groups = nB / 4;
+    for (uint64_t g = tid; g < groups; g += stride) {
+      const float4 f0 = B4[3 * g], f1 = B4[3 * g + 1], f2 = B4[3 * g + 2];
+      const float d0 = d2_3(a[0], a[1], a[2], f0.x, f0.y, f0.z);
+      const float d1 = d2_3(a[0], a[1], a[2], f0.w, f1.x, f1.y);
+      const float e2 = d2_3(a[0], a[1], a[2], f1.z, f1.w, f2.x);
+      const float d3 = d2_3(a[0], a[1], a[2], f2.y, f2.z, f2.w);
+      unsigned long long k0 = pack_min(d0, (uint32_t) (4 * g));
+      unsigned long long k1 = pack_min(d1, (uint32_t) (4 * g + 1));
+      unsigned long long k2 = pack_min(e2, (uint32_t) (4 * g + 2));
+      unsigned long long k3 = pack_min(d3, (uint32_t) (4 * g + 3));
+      k0 = k1 < k0 ? k1 : k0;
+      k2 = k3 < k2 ? k3 : k2;
+      k0 = k2 < k0 ? k2 : k0;
+      best = k0 < best ? k0 : best;
+    }
+    first = groups * 4;
+  } else if (D == 2 && ((reinterpret_cast<uintptr_t>(B) & 15) == 0)) {
+    const float4* B4 = reinterpret_cast<const float4*>(B);
+    const uint64_t groups = nB / 2;
+    for (uint64_t g = tid; g < groups; g += stride) {
+      const float4 f = B4[g];
+      unsigned long long k0 = pack_min(d2_2(a[0], a[1], f.x, f.y), (uint32_t) (2 * g));
+      unsigned long long k1 = pack_min(d2_2(a[0], a[1], f.z, f.w), (uint32_t) (2 * g + 1));
+      k0 = k1 < k0 ? k1 : k0;
+      best = k0 < best ? k0 : best;
+    }
+    first = groups * 2;
+  }
+  for (uint64_t j = first + tid; j < nB; j += stride) {
     float d2;
     if (D == 2) {
       d2 = d2_2(a[0], a[1], B[2 * j], B[2 * j + 1]);

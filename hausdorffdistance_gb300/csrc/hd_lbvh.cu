@@ -266,9 +266,14 @@ __global__ void __launch_bounds__(kQueryWarps * 32)
     // stop before any traversal, and gives the others a small running
     // minimum that prunes the traversal.
     const uint32_t nL = (uint32_t) ((nB + L - 1) / L);
-    const uint32_t leaf0 = (uint32_t) min((uint64_t) ppos[packet] / L, (uint64_t) (nL - 1));
+    // Both ends of the packet are looked up: a packet can straddle a jump of
+    // the Morton curve, and then its two ends sit in different regions.
+    const uint32_t leaf0 = (uint32_t) min((uint64_t) ppos[2 * packet] / L, (uint64_t) (nL - 1));
+    const uint32_t leaf1 = (uint32_t) min((uint64_t) ppos[2 * packet + 1] / L, (uint64_t) (nL - 1));
     scan_leaf(leaf0);
-    if (leaf0 + 1 < nL && __any_sync(0xFFFFFFFFu, active)) scan_leaf(leaf0 + 1);
+    if (leaf1 != leaf0 && __any_sync(0xFFFFFFFFu, active)) scan_leaf(leaf1);
+    if (leaf0 + 1 < nL && leaf0 + 1 != leaf1 && __any_sync(0xFFFFFFFFu, active))
+      scan_leaf(leaf0 + 1);
     if (leaf0 > 0 && __any_sync(0xFFFFFFFFu, active)) scan_leaf(leaf0 - 1);
   }
 
@@ -340,12 +345,16 @@ __global__ void __launch_bounds__(kQueryWarps * 32)
 
 // Position of every packet's first query in B's sorted codes (lower bound),
 // one binary search per packet.
+// Positions of every packet's first and last query in B's sorted codes
+// (lower bounds), one thread per packet end.
 __global__ void k_packet_pos(const uint32_t* __restrict__ qcodes, uint64_t nQ,
                              const uint32_t* __restrict__ bcodes, uint64_t nB,
                              uint32_t* __restrict__ pos) {
-  const uint64_t p = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+  const uint64_t t = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+  const uint64_t p = t >> 1;
   if (p * 32 >= nQ) return;
-  const uint32_t target = qcodes[p * 32];
+  const uint64_t q = (t & 1) ? min(p * 32 + 31, nQ - 1) : p * 32;
+  const uint32_t target = qcodes[q];
   uint64_t lo = 0, hi = nB;
   while (lo < hi) {
     const uint64_t mid = (lo + hi) >> 1;
@@ -354,7 +363,7 @@ __global__ void k_packet_pos(const uint32_t* __restrict__ qcodes, uint64_t nQ,
     else
       hi = mid;
   }
-  pos[p] = (uint32_t) lo;
+  pos[t] = (uint32_t) lo;
 }
 
 }  // namespace
@@ -431,8 +440,8 @@ hd_status run_lbvh(Ctx& c, const DirInput& in) {
   DevScalars* sc = scalars(c, in.dir);
   const uint64_t packets = (q->n + 31) / 32;
   void* ppos;
-  if ((s = ensure(c, kBufSample, packets * 4, &ppos)) != HD_OK) return s;
-  k_packet_pos<<<(unsigned) ((packets + 255) / 256), 256, 0, c.stream>>>(
+  if ((s = ensure(c, kBufSample, packets * 8, &ppos)) != HD_OK) return s;
+  k_packet_pos<<<(unsigned) ((2 * packets + 255) / 256), 256, 0, c.stream>>>(
       q->codes, q->n, t->codes, t->n, (uint32_t*) ppos);
   if ((s = after_launch(c, "packet_pos")) != HD_OK) return s;
   // Sample pass: every pstride-th packet, spread over the whole Morton range,
