@@ -42,8 +42,8 @@ class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("variant", ctypes.c_int),
                 ("seed", ctypes.c_uint64), ("sample_rate", ctypes.c_double),
                 ("n_points_cell", ctypes.c_uint32), ("leaf_size", ctypes.c_uint32),
-                ("eb_only_threshold", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 8)]
+                ("eb_only_threshold", ctypes.c_uint32), ("always_sample", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 7)]
 
 
 class Result(ctypes.Structure):

@@ -12,8 +12,12 @@ the sampler statistic the selector sees: the 80th percentile of sampled
 early-break iteration counts, p80, and ratio = |A| * p80 / (|A| + |B|).
 It then fits the selector's table:
 
-  eb_ratio     the threshold on ratio below which EB is chosen: the value
-               minimising the total time of the sweep's choices;
+  eb_small_pairs / index_min_pairs
+               size bands (|A| * |B|) below / above which EB / the index is
+               chosen without sampling;
+  eb_ratio     between the bands, the threshold on ratio below which EB is
+               chosen;
+  (each minimising the total time of the sweep's choices);
   prefer_grid  whether the grid beats the LBVH in total over the sweep.
 
 --write regenerates hausdorffdistance_gb300/csrc/hd_tuning_table.h and
@@ -40,8 +44,10 @@ SWEEP_NAME = "tuning_sweep.json"
 
 
 def workloads(quick: bool):
-    sizes2 = [20_000, 200_000] if quick else [20_000, 200_000, 2_000_000]
-    sizes3 = [100_000, 1_000_000] if quick else [100_000, 1_000_000, 10_000_000]
+    sizes2 = [1_000, 3_000, 20_000, 200_000] if quick else [1_000, 3_000, 20_000, 200_000,
+                                                            2_000_000]
+    sizes3 = [2_000, 10_000, 100_000, 1_000_000] if quick else [2_000, 10_000, 100_000,
+                                                               1_000_000, 10_000_000]
     for n in sizes2:
         a, b = synth.uniform2d(n, seed=101)
         yield f"uniform2d_{n}", a, b
@@ -66,7 +72,7 @@ def time_variant(eng, ta, tb, variant, reps=3):
 def sweep(quick: bool):
     import torch
     rows = []
-    with hd.Engine() as eng:
+    with hd.Engine(always_sample=True) as eng:
         for name, a, b in workloads(quick):
             for direction, (x, y) in enumerate([(a, b), (b, a)]):
                 tx = torch.from_numpy(np.ascontiguousarray(x)).cuda()
@@ -85,27 +91,46 @@ def sweep(quick: bool):
 
 
 def fit(rows):
-    index_best = {}
+    """Fits the selector table.  Choice for a row, given the table:
+    EB if pairs <= eb_small; index if pairs >= index_min; else EB iff
+    ratio < eb_ratio.  Each parameter is chosen from the sweep's own values
+    to minimise the sweep's total time (coordinate search, two rounds)."""
     grid_total = sum(r["grid"] for r in rows)
     lbvh_total = sum(r["lbvh"] for r in rows)
     prefer_grid = grid_total < lbvh_total
     idx = "grid" if prefer_grid else "lbvh"
-    cands = sorted({0.0} | {r["ratio"] * 1.0001 for r in rows} | {1e30})
-    best_t, best_cost = None, float("inf")
-    for t in cands:
-        cost = sum(r["eb"] if r["ratio"] < t else r[idx] for r in rows)
-        if cost < best_cost:
-            best_t, best_cost = t, cost
-    index_best["total_ms_chosen"] = best_cost
-    index_best["total_ms_oracle_choice"] = sum(min(r["eb"], r["lbvh"], r["grid"]) for r in rows)
-    return {"eb_ratio": best_t, "prefer_grid": prefer_grid, **index_best}
+    for r in rows:
+        r.setdefault("pairs", float(r.get("n_a", 1)) * float(r.get("n_b", 1)))
+
+    def cost(small, big, t):
+        total = 0.0
+        for r in rows:
+            if r["pairs"] <= small:
+                total += r["eb"]
+            elif r["pairs"] >= big:
+                total += r[idx]
+            else:
+                total += r["eb"] if r["ratio"] < t else r[idx]
+        return total
+
+    pair_cands = sorted({0.0, 1e30} | {r["pairs"] for r in rows})
+    ratio_cands = sorted({0.0, 1e30} | {r["ratio"] * 1.0001 for r in rows})
+    small, big, t = 0.0, 1e30, 0.0
+    for _ in range(2):
+        t = min(ratio_cands, key=lambda x: (cost(small, big, x), x))
+        small = min(pair_cands, key=lambda x: (cost(x, big, t), -x))
+        big = min([b for b in pair_cands if b > small] or [1e30], key=lambda x: (cost(small, x, t), x))
+    return {"eb_ratio": t, "eb_small_pairs": small, "index_min_pairs": big,
+            "prefer_grid": prefer_grid, "total_ms_chosen": cost(small, big, t),
+            "total_ms_oracle_choice": sum(min(r["eb"], r["lbvh"], r["grid"]) for r in rows)}
 
 
 def write_table(params, path):
     with open(path, "w") as f:
         f.write("// Generated by hausdorffdistance_gb300/autotune.py — do not edit by hand.\n")
         f.write("#pragma once\n")
-        f.write("#define HD_TUNED_EB_SMALL_PAIRS 4194304.0\n")
+        f.write(f"#define HD_TUNED_EB_SMALL_PAIRS {params['eb_small_pairs']:.6g}\n")
+        f.write(f"#define HD_TUNED_INDEX_MIN_PAIRS {params['index_min_pairs']:.6g}\n")
         f.write(f"#define HD_TUNED_EB_RATIO {params['eb_ratio']:.6g}\n")
         f.write("#define HD_TUNED_BF16_MIN_PAIRS 67108864.0\n")
         f.write(f"#define HD_TUNED_PREFER_GRID {1 if params['prefer_grid'] else 0}\n")

@@ -195,20 +195,20 @@ constexpr float kMaxDistMargin = 1.0f + 1.0f / 65536.0f;
 // (or 32 entries of a sample list).
 template <int D, bool COUNT>
 __global__ void __launch_bounds__(kQueryWarps * 32)
-    k_lbvh_query(const float4* __restrict__ Q, uint64_t nItems, uint32_t pstride, int phase,
-                 const uint32_t* __restrict__ ppos, const float4* __restrict__ nodes,
-                 const float4* __restrict__ B, uint64_t nB, uint32_t L, DevScalars* sc) {
+    k_lbvh_query(const float4* __restrict__ Q, uint64_t nItems, uint32_t pstride,
+                 uint64_t rows, const uint32_t* __restrict__ ppos,
+                 const float4* __restrict__ nodes, const float4* __restrict__ B, uint64_t nB,
+                 uint32_t L, DevScalars* sc) {
   __shared__ uint32_t stk[kQueryWarps][kStack];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // Phase 0 (sample pass) takes every pstride-th packet; phase 1 takes the
-  // rest.  Packets are 32 consecutive Morton-sorted queries either way.
+  // Packets (32 consecutive Morton-sorted queries) are visited in a
+  // transposed order: warp w takes packet (w mod rows) * pstride + w / rows.
+  // The first `rows` warps — the first wave — are every pstride-th packet,
+  // spread over the whole Morton range, so the running maximum rises to
+  // nearly its final value while the bulk of the packets is still queued
+  // (the reference samples with EB for the same purpose, hybrid.h:128-168).
   const uint64_t w = (uint64_t) blockIdx.x * kQueryWarps + warp;
-  uint64_t packet;
-  if (phase == 0) {
-    packet = w * pstride;
-  } else {
-    packet = w + w / (pstride - 1) + 1;  // skips multiples of pstride
-  }
+  const uint64_t packet = (w % rows) * pstride + w / rows;
   if (packet * 32 >= nItems) return;
   const uint64_t item = packet * 32 + lane;
   bool active = item < nItems;
@@ -411,20 +411,18 @@ static hd_status build_lbvh(Ctx& c, const SortedSet& t, int slot, Lbvh* out) {
 }
 
 template <int D>
-static hd_status launch_query(Ctx& c, const SortedSet& q, uint32_t pstride, int phase,
-                              const uint32_t* ppos, const Lbvh& bvh, const SortedSet& t,
-                              DevScalars* sc, bool count) {
+static hd_status launch_query(Ctx& c, const SortedSet& q, uint32_t pstride, const uint32_t* ppos,
+                              const Lbvh& bvh, const SortedSet& t, DevScalars* sc, bool count) {
   const uint64_t packets = (q.n + 31) / 32;
-  const uint64_t warps = phase == 0 ? (packets + pstride - 1) / pstride
-                                    : packets - (packets + pstride - 1) / pstride;
-  if (warps == 0) return HD_OK;
+  const uint64_t rows = (packets + pstride - 1) / pstride;
+  const uint64_t warps = rows * pstride;
   const uint64_t blocks = (warps + kQueryWarps - 1) / kQueryWarps;
   if (count)
     k_lbvh_query<D, true><<<(unsigned) blocks, kQueryWarps * 32, 0, c.stream>>>(
-        q.pts, q.n, pstride, phase, ppos, bvh.nodes, t.pts, t.n, bvh.L, sc);
+        q.pts, q.n, pstride, rows, ppos, bvh.nodes, t.pts, t.n, bvh.L, sc);
   else
     k_lbvh_query<D, false><<<(unsigned) blocks, kQueryWarps * 32, 0, c.stream>>>(
-        q.pts, q.n, pstride, phase, ppos, bvh.nodes, t.pts, t.n, bvh.L, sc);
+        q.pts, q.n, pstride, rows, ppos, bvh.nodes, t.pts, t.n, bvh.L, sc);
   return after_launch(c, "lbvh_query");
 }
 
@@ -444,19 +442,13 @@ hd_status run_lbvh(Ctx& c, const DirInput& in) {
   k_packet_pos<<<(unsigned) ((2 * packets + 255) / 256), 256, 0, c.stream>>>(
       q->codes, q->n, t->codes, t->n, (uint32_t*) ppos);
   if ((s = after_launch(c, "packet_pos")) != HD_OK) return s;
-  // Sample pass: every pstride-th packet, spread over the whole Morton range,
-  // finishes first and raises the running maximum before the rest run (the
-  // reference samples with EB for the same purpose, hybrid.h:128-168).
-  const uint32_t pstride = packets >= 4096 ? 64 : (packets >= 256 ? 16 : 2);
-  auto go = [&](int phase) {
-    return in.dims == 2 ? launch_query<2>(c, *q, pstride, phase, (const uint32_t*) ppos, bvh, *t,
-                                          sc, in.count)
-                        : launch_query<3>(c, *q, pstride, phase, (const uint32_t*) ppos, bvh, *t,
-                                          sc, in.count);
-  };
-  if ((s = go(0)) != HD_OK) return s;
+  const uint32_t pstride = packets >= 4096 ? 64 : (packets >= 256 ? 16 : 1);
   mark(c, 3);
-  if ((s = go(1)) != HD_OK) return s;
+  if ((s = in.dims == 2 ? launch_query<2>(c, *q, pstride, (const uint32_t*) ppos, bvh, *t, sc,
+                                          in.count)
+                        : launch_query<3>(c, *q, pstride, (const uint32_t*) ppos, bvh, *t, sc,
+                                          in.count)) != HD_OK)
+    return s;
   mark(c, 4);
   return certify(c, in);
 }

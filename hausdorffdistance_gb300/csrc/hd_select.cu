@@ -19,9 +19,12 @@
 //      otherwise the LBVH (the grid when the table says so).  The threshold
 //      comes from the autotuner's table (hausdorffdistance_gb300/autotune.py
 //      fits it over a sweep of workloads) unless hd_options overrides it.
-//   3. Tiny problems (|A| * |B| <= 2^22) take EB without sampling; inputs with
-//      n_dims other than 2 or 3 take the split-BF16 tiles when n_dims is a
-//      multiple of 16 and the pair count is large, else the FP32 scan.
+//   3. Size bands from the same table: problems with |A| * |B| up to
+//      eb_small_pairs take EB and problems from index_min_pairs up take the
+//      index, both without sampling (the sweep shows the choice there does
+//      not depend on the data); inputs with n_dims other than 2 or 3 take the
+//      split-BF16 tiles when n_dims is a multiple of 16 and the pair count is
+//      large, else the FP32 scan.
 #include <algorithm>
 #include <cfloat>
 #include <vector>
@@ -126,8 +129,14 @@ hd_status select_variant(Ctx& c, const DirInput& in, int* v) {
     *v = (in.dims % 16 == 0 && pairs >= tu.bf16_min_pairs) ? HD_VARIANT_BF16 : HD_VARIANT_EB;
     return HD_OK;
   }
-  if ((double) in.nA * (double) in.nB <= tu.eb_small_pairs) {
+  const double pairs = (double) in.nA * (double) in.nB;
+  const bool sample = c.opt.always_sample != 0;
+  if (!sample && pairs <= tu.eb_small_pairs) {
     *v = HD_VARIANT_EB;
+    return HD_OK;
+  }
+  if (!sample && pairs >= tu.index_min_pairs) {
+    *v = tu.prefer_grid ? HD_VARIANT_GRID : HD_VARIANT_LBVH;
     return HD_OK;
   }
   const double rate = c.opt.sample_rate > 0 ? c.opt.sample_rate : 0.01;

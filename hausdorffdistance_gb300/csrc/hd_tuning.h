@@ -6,6 +6,7 @@ namespace hdg {
 
 struct Tuning {
   double eb_small_pairs;  // |A|*|B| at or below which AUTO takes EB unsampled
+  double index_min_pairs; // |A|*|B| from which AUTO takes the index unsampled
   double eb_ratio;        // EB when |A| * p80 / (|A| + |B|) is below this
   double bf16_min_pairs;  // n_dims % 16 == 0: BF16 tiles from this |A|*|B| up
   bool prefer_grid;       // index-based choice: grid instead of LBVH

@@ -2,6 +2,7 @@
 // Initial table (before the first sweep on a GB300): conservative values.
 #pragma once
 #define HD_TUNED_EB_SMALL_PAIRS 4194304.0
+#define HD_TUNED_INDEX_MIN_PAIRS 1e10
 #define HD_TUNED_EB_RATIO 64.0
 #define HD_TUNED_BF16_MIN_PAIRS 67108864.0
 #define HD_TUNED_PREFER_GRID 0

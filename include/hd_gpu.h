@@ -80,7 +80,9 @@ typedef struct hd_options {
   uint32_t leaf_size;      /* LBVH: points per leaf (<= 32)                    */
   uint32_t eb_only_threshold; /* selector: p80 sample iterations below which  */
                               /* plain EB is chosen (hybrid.h:171); 0 = table */
-  uint32_t reserved[8];
+  uint32_t always_sample;  /* selector: draw the sample statistic even where  */
+                           /* the size bands decide alone (autotuning)        */
+  uint32_t reserved[7];
 } hd_options;
 
 typedef struct hd_result {
