@@ -1,9 +1,8 @@
 // Generated by hausdorffdistance_gb300/autotune.py — do not edit by hand.
-// Initial table (before the first sweep on a GB300): conservative values.
 #pragma once
-#define HD_TUNED_EB_SMALL_PAIRS 4194304.0
-#define HD_TUNED_INDEX_MIN_PAIRS 1e10
-#define HD_TUNED_EB_RATIO 64.0
+#define HD_TUNED_EB_SMALL_PAIRS 1e+06
+#define HD_TUNED_INDEX_MIN_PAIRS 4e+06
+#define HD_TUNED_EB_RATIO 0
 #define HD_TUNED_BF16_MIN_PAIRS 67108864.0
 #define HD_TUNED_PREFER_GRID 0
 #define HD_TUNED_LEAF_SIZE 16
