@@ -447,13 +447,31 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   const int ndir = undirected ? 2 : 1;
   DirResult ex[2];
   int used[2] = {variant, -1};
+  DirInput ins[2];
   for (int d = 0; d < ndir; ++d) {
-    DirInput in{d == 0 ? dA : dB, d == 0 ? n_a : n_b, d == 0 ? dB : dA,
-                d == 0 ? n_b : n_a, n_dims, d, count};
-    c->ev_base = 12 * d;
+    ins[d] = DirInput{d == 0 ? dA : dB, d == 0 ? n_a : n_b, d == 0 ? dB : dA,
+                      d == 0 ? n_b : n_a, n_dims, d, count};
+    used[d] = variant;
+    if (variant == HD_VARIANT_AUTO) {
+      c->ev_base = 12 * d;
+      if ((s = select_variant(*c, ins[d], &used[d])) != HD_OK) return s;
+    }
+  }
+  const bool fused = undirected && used[0] == HD_VARIANT_LBVH && used[1] == HD_VARIANT_LBVH;
+  if (fused) {
+    // Fused undirected pass: one sort of both sets, both trees and both
+    // directions' queries in shared launches.
+    c->ev_base = 0;
     mark(*c, 0);
-    if ((s = run_direction(*c, in, variant, &used[d], &ex[d])) != HD_OK) return s;
+    if ((s = run_lbvh_pair(*c, ins[0], ins[1])) != HD_OK) return s;
     mark(*c, 6);
+  } else {
+    for (int d = 0; d < ndir; ++d) {
+      c->ev_base = 12 * d;
+      mark(*c, 0);
+      if ((s = run_direction(*c, ins[d], used[d], &used[d], &ex[d])) != HD_OK) return s;
+      mark(*c, 6);
+    }
   }
   HostScalars* h = reinterpret_cast<HostScalars*>(c->host_pinned);
   cudaError_t e = cudaMemcpyAsync(h, c->bufs[kBufScalars].p, sizeof(HostScalars),
@@ -496,7 +514,8 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
     // 5 certify.
     const int from[6] = {0, 1, 2, 3, 4, 5};
     const int to[6] = {1, 2, 3, 4, 5, 6};
-    for (int d = 0; d < ndir; ++d)
+    // The fused pass records its phases once, on direction 0's events.
+    for (int d = 0; d < (fused ? 1 : ndir); ++d)
       for (int p = 0; p < 6; ++p) {
         if (cudaEventElapsedTime(&t, c->ev[12 * d + from[p]], c->ev[12 * d + to[p]]) ==
             cudaSuccess)

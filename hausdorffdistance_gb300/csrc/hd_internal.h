@@ -151,6 +151,8 @@ hd_status run_eb(Ctx& c, const DirInput& in);
 hd_status run_brute(Ctx& c, const DirInput& in);
 hd_status run_eb_nd(Ctx& c, const DirInput& in);  // EB for n_dims other than 2, 3
 hd_status run_lbvh(Ctx& c, const DirInput& in);
+// Both directions of an undirected solve with shared launches.
+hd_status run_lbvh_pair(Ctx& c, const DirInput& ab, const DirInput& ba);
 hd_status run_grid(Ctx& c, const DirInput& in);
 hd_status run_bf16(Ctx& c, const DirInput& in, DirResult* extra);
 // Test hook: the BF16 kernel's approximate row minima (no certification).

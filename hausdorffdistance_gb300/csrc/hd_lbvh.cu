@@ -49,8 +49,9 @@ __device__ __forceinline__ int delta(const uint32_t* __restrict__ codes, uint32_
 }
 
 // Leaf boxes: one thread per leaf over its (at most 32) points.
-__global__ void k_leaf_boxes(const float4* __restrict__ pts, uint64_t n, uint32_t L,
-                             uint32_t nL, uint32_t nI, float4* __restrict__ boxes) {
+__device__ __forceinline__ void leaf_boxes_body(const float4* __restrict__ pts, uint64_t n,
+                                                uint32_t L, uint32_t nL, uint32_t nI,
+                                                float4* __restrict__ boxes) {
   uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
   if (leaf >= nL) return;
   uint64_t s = (uint64_t) leaf * L;
@@ -69,8 +70,9 @@ __global__ void k_leaf_boxes(const float4* __restrict__ pts, uint64_t n, uint32_
 // Karras 2012, one thread per internal node.  Node ids: internal [0, nI),
 // leaves nI + [0, nL).  Keys are the leaves' first Morton codes augmented
 // with the leaf index, which makes them distinct.
-__global__ void k_karras(const uint32_t* __restrict__ codes, uint32_t L, uint32_t nL,
-                         uint2* __restrict__ child, uint32_t* __restrict__ parent) {
+__device__ __forceinline__ void karras_body(const uint32_t* __restrict__ codes, uint32_t L,
+                                            uint32_t nL, uint2* __restrict__ child,
+                                            uint32_t* __restrict__ parent) {
   const int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x;
   const int64_t nI = (int64_t) nL - 1;
   if (i >= nI) return;
@@ -106,8 +108,9 @@ __device__ __forceinline__ uint32_t node_id(uint32_t ref, uint32_t nI) {
 
 // Bottom-up boxes: a thread per leaf climbs; the second child to arrive at a
 // parent computes its box (Karras 2012, section 4).
-__global__ void k_bottom_up(const uint2* __restrict__ child, const uint32_t* __restrict__ parent,
-                            uint32_t nL, uint32_t nI, float4* boxes, uint32_t* flags) {
+__device__ __forceinline__ void bottom_up_body(const uint2* __restrict__ child,
+                                               const uint32_t* __restrict__ parent, uint32_t nL,
+                                               uint32_t nI, float4* boxes, uint32_t* flags) {
   uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
   if (leaf >= nL || nI == 0) return;
   uint32_t node = nI + leaf;
@@ -130,8 +133,9 @@ __global__ void k_bottom_up(const uint2* __restrict__ child, const uint32_t* __r
 }
 
 // Packs every internal node as 4 float4: both children's boxes and refs.
-__global__ void k_pack_nodes(const uint2* __restrict__ child, const float4* __restrict__ boxes,
-                             uint32_t nI, float4* __restrict__ nodes) {
+__device__ __forceinline__ void pack_nodes_body(const uint2* __restrict__ child,
+                                                const float4* __restrict__ boxes, uint32_t nI,
+                                                float4* __restrict__ nodes) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (nI == 0) {
     // Single leaf: a root whose right child is an empty box (never visited).
@@ -194,8 +198,7 @@ constexpr float kMaxDistMargin = 1.0f + 1.0f / 65536.0f;
 // Warp-packet traversal.  A packet is 32 consecutive Morton-sorted queries
 // (or 32 entries of a sample list).
 template <int D, bool COUNT>
-__global__ void __launch_bounds__(kQueryWarps * 32)
-    k_lbvh_query(const float4* __restrict__ Q, uint64_t nItems, uint32_t pstride,
+__device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, uint64_t nItems, uint32_t pstride,
                  uint64_t rows, const uint32_t* __restrict__ ppos,
                  const float4* __restrict__ nodes, const float4* __restrict__ B, uint64_t nB,
                  uint32_t L, DevScalars* sc) {
@@ -347,9 +350,9 @@ __global__ void __launch_bounds__(kQueryWarps * 32)
 // one binary search per packet.
 // Positions of every packet's first and last query in B's sorted codes
 // (lower bounds), one thread per packet end.
-__global__ void k_packet_pos(const uint32_t* __restrict__ qcodes, uint64_t nQ,
-                             const uint32_t* __restrict__ bcodes, uint64_t nB,
-                             uint32_t* __restrict__ pos) {
+__device__ __forceinline__ void packet_pos_body(const uint32_t* __restrict__ qcodes, uint64_t nQ,
+                                                const uint32_t* __restrict__ bcodes, uint64_t nB,
+                                                uint32_t* __restrict__ pos) {
   const uint64_t t = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
   const uint64_t p = t >> 1;
   if (p * 32 >= nQ) return;
@@ -366,91 +369,199 @@ __global__ void k_packet_pos(const uint32_t* __restrict__ qcodes, uint64_t nQ,
   pos[t] = (uint32_t) lo;
 }
 
-}  // namespace
-
-struct Lbvh {
-  const float4* nodes;
-  uint32_t L;
+// The same kernels over one or two point sets at once (blockIdx.y picks the
+// set): an undirected solve builds both trees and answers both directions'
+// queries in shared launches, so the two halves fill each other's tails.
+struct BuildSet {
+  const float4* pts;
+  const uint32_t* codes;
+  uint64_t n;
+  uint32_t L, nL, nI;
+  float4* boxes;
+  uint2* child;
+  uint32_t* parent;
+  uint32_t* flags;
+  float4* nodes;
+};
+struct BuildSets {
+  BuildSet s[2];
 };
 
-// Builds the LBVH of a sorted set into the node slot of that set.
-static hd_status build_lbvh(Ctx& c, const SortedSet& t, int slot, Lbvh* out) {
+__global__ void k_leaf_boxes(BuildSets b) {
+  const BuildSet& S = b.s[blockIdx.y];
+  leaf_boxes_body(S.pts, S.n, S.L, S.nL, S.nI, S.boxes);
+}
+__global__ void k_karras(BuildSets b) {
+  const BuildSet& S = b.s[blockIdx.y];
+  karras_body(S.codes, S.L, S.nL, S.child, S.parent);
+}
+__global__ void k_bottom_up(BuildSets b) {
+  const BuildSet& S = b.s[blockIdx.y];
+  bottom_up_body(S.child, S.parent, S.nL, S.nI, S.boxes, S.flags);
+}
+__global__ void k_pack_nodes(BuildSets b) {
+  const BuildSet& S = b.s[blockIdx.y];
+  pack_nodes_body(S.child, S.boxes, S.nI, S.nodes);
+}
+
+struct QuerySet {
+  const float4* Q;
+  uint64_t nQ;
+  uint32_t pstride;
+  uint64_t rows;
+  const uint32_t* ppos;
+  const float4* nodes;
+  const float4* B;
+  uint64_t nB;
+  uint32_t L;
+  DevScalars* sc;
+  const uint32_t* qcodes;
+  const uint32_t* bcodes;
+};
+struct QuerySets {
+  QuerySet d[2];
+};
+
+template <int D, bool COUNT>
+__global__ void __launch_bounds__(kQueryWarps * 32) k_lbvh_query(QuerySets qs) {
+  const QuerySet& S = qs.d[blockIdx.y];
+  lbvh_query_body<D, COUNT>(S.Q, S.nQ, S.pstride, S.rows, S.ppos, S.nodes, S.B, S.nB, S.L, S.sc);
+}
+
+__global__ void k_packet_pos(QuerySets qs) {
+  const QuerySet& S = qs.d[blockIdx.y];
+  packet_pos_body(S.qcodes, S.nQ, S.bcodes, S.nB, const_cast<uint32_t*>(S.ppos));
+}
+
+}  // namespace
+
+// Builds the LBVHs of `count` sorted sets (tree k into node slot k).
+static hd_status build_lbvhs(Ctx& c, const SortedSet* const* sets, int count, BuildSets* out) {
   const uint32_t L = c.opt.leaf_size ? std::min<uint32_t>(c.opt.leaf_size, 32) : 16;
-  const uint64_t nL64 = (t.n + L - 1) / L;
-  const uint32_t nL = (uint32_t) nL64;
-  const uint32_t nI = nL - 1;
   hd_status s;
-  void *nodes, *boxes, *aux, *aux2;
-  const uint64_t nNodes = (uint64_t) nI + nL;
-  if ((s = ensure(c, slot == 0 ? kBufNodes0 : kBufNodes1,
-                  std::max<uint64_t>(nI, 1) * 4 * sizeof(float4), &nodes)) != HD_OK)
-    return s;
-  if ((s = ensure(c, kBufBoxes, nNodes * 2 * sizeof(float4), &boxes)) != HD_OK) return s;
-  // aux: child (uint2 per internal) ; aux2: parent (u32 per node) + flags (u32 per internal)
-  if ((s = ensure(c, kBufAux, std::max<uint64_t>(nI, 1) * sizeof(uint2), &aux)) != HD_OK) return s;
-  if ((s = ensure(c, kBufAux2, (nNodes + std::max<uint64_t>(nI, 1)) * 4, &aux2)) != HD_OK) return s;
-  uint32_t* parent = (uint32_t*) aux2;
-  uint32_t* flags = parent + nNodes;
-  k_leaf_boxes<<<(nL + 255) / 256, 256, 0, c.stream>>>(t.pts, t.n, L, nL, nI, (float4*) boxes);
-  if ((s = after_launch(c, "leaf_boxes")) != HD_OK) return s;
-  if (nI > 0) {
-    k_karras<<<(nI + 255) / 256, 256, 0, c.stream>>>(t.codes, L, nL, (uint2*) aux, parent);
-    if ((s = after_launch(c, "karras")) != HD_OK) return s;
-    cudaError_t e = cudaMemsetAsync(flags, 0, (size_t) nI * 4, c.stream);
-    if (e != cudaSuccess) return cuda_fail(c, e, "memset flags");
-    k_bottom_up<<<(nL + 255) / 256, 256, 0, c.stream>>>((const uint2*) aux, parent, nL, nI,
-                                                        (float4*) boxes, flags);
-    if ((s = after_launch(c, "bottom_up")) != HD_OK) return s;
+  uint64_t nodes_total = 0, internal_total = 0;
+  uint64_t nL[2], nI[2];
+  for (int k = 0; k < count; ++k) {
+    nL[k] = (sets[k]->n + L - 1) / L;
+    nI[k] = nL[k] - 1;
+    nodes_total += nI[k] + nL[k];
+    internal_total += std::max<uint64_t>(nI[k], 1);
   }
-  k_pack_nodes<<<(std::max<uint32_t>(nI, 1) + 255) / 256, 256, 0, c.stream>>>(
-      (const uint2*) aux, (const float4*) boxes, nI, (float4*) nodes);
-  if ((s = after_launch(c, "pack_nodes")) != HD_OK) return s;
-  out->nodes = (const float4*) nodes;
-  out->L = L;
+  void *boxes, *aux, *aux2;
+  if ((s = ensure(c, kBufBoxes, nodes_total * 2 * sizeof(float4), &boxes)) != HD_OK) return s;
+  if ((s = ensure(c, kBufAux, internal_total * sizeof(uint2), &aux)) != HD_OK) return s;
+  if ((s = ensure(c, kBufAux2, (nodes_total + internal_total) * 4, &aux2)) != HD_OK) return s;
+  // Flags of all sets are contiguous (first in aux2) so one memset clears them.
+  uint32_t* flags_base = (uint32_t*) aux2;
+  uint32_t* parent_base = flags_base + internal_total;
+  uint64_t off_nodes = 0, off_int = 0;
+  uint64_t maxL = 0, maxI = 1;
+  for (int k = 0; k < count; ++k) {
+    void* nodes;
+    if ((s = ensure(c, k == 0 ? kBufNodes0 : kBufNodes1,
+                    std::max<uint64_t>(nI[k], 1) * 4 * sizeof(float4), &nodes)) != HD_OK)
+      return s;
+    BuildSet& b = out->s[k];
+    b.pts = sets[k]->pts;
+    b.codes = sets[k]->codes;
+    b.n = sets[k]->n;
+    b.L = L;
+    b.nL = (uint32_t) nL[k];
+    b.nI = (uint32_t) nI[k];
+    b.boxes = (float4*) boxes + 2 * off_nodes;
+    b.child = (uint2*) aux + off_int;
+    b.flags = flags_base + off_int;
+    b.parent = parent_base + off_nodes;
+    b.nodes = (float4*) nodes;
+    off_nodes += nI[k] + nL[k];
+    off_int += std::max<uint64_t>(nI[k], 1);
+    maxL = std::max(maxL, nL[k]);
+    maxI = std::max(maxI, nI[k]);
+  }
+  if (count == 1) out->s[1] = out->s[0];
+  const dim3 gl((unsigned) ((maxL + 255) / 256), count), gi((unsigned) ((maxI + 255) / 256), count);
+  k_leaf_boxes<<<gl, 256, 0, c.stream>>>(*out);
+  if ((s = after_launch(c, "leaf_boxes")) != HD_OK) return s;
+  k_karras<<<gi, 256, 0, c.stream>>>(*out);
+  if ((s = after_launch(c, "karras")) != HD_OK) return s;
+  cudaError_t e = cudaMemsetAsync(flags_base, 0, internal_total * 4, c.stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "memset flags");
+  k_bottom_up<<<gl, 256, 0, c.stream>>>(*out);
+  if ((s = after_launch(c, "bottom_up")) != HD_OK) return s;
+  k_pack_nodes<<<gi, 256, 0, c.stream>>>(*out);
+  return after_launch(c, "pack_nodes");
+}
+
+// Directed LBVH solves of `count` directions (1, or 2 for an undirected solve)
+// with shared launches.
+static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
+  const int dims = ins[0].dims;
+  if (dims != 2 && dims != 3) return fail(c, HD_ERR_UNSUPPORTED, "LBVH needs n_dims 2 or 3");
+  hd_status s;
+  const SortedSet *q[2], *t[2];
+  for (int k = 0; k < count; ++k)
+    if ((s = spatial_prepare(c, ins[k], &q[k], &t[k])) != HD_OK) return s;
+  mark(c, 1);
+  BuildSets bs;
+  if ((s = build_lbvhs(c, t, count, &bs)) != HD_OK) return s;
+  mark(c, 2);
+  QuerySets qs;
+  uint64_t packets[2], maxppos = 0;
+  for (int k = 0; k < count; ++k) {
+    packets[k] = (q[k]->n + 31) / 32;
+    maxppos += 2 * packets[k];
+  }
+  void* ppos;
+  if ((s = ensure(c, kBufSample, maxppos * 4, &ppos)) != HD_OK) return s;
+  uint64_t off = 0, max_warps = 0, max_pos_threads = 0;
+  for (int k = 0; k < count; ++k) {
+    QuerySet& d = qs.d[k];
+    const uint32_t pstride = packets[k] >= 4096 ? 64 : (packets[k] >= 256 ? 16 : 1);
+    d.Q = q[k]->pts;
+    d.nQ = q[k]->n;
+    d.pstride = pstride;
+    d.rows = (packets[k] + pstride - 1) / pstride;
+    d.ppos = (const uint32_t*) ppos + off;
+    d.nodes = bs.s[k].nodes;
+    d.B = t[k]->pts;
+    d.nB = t[k]->n;
+    d.L = bs.s[k].L;
+    d.sc = scalars(c, ins[k].dir);
+    d.qcodes = q[k]->codes;
+    d.bcodes = t[k]->codes;
+    off += 2 * packets[k];
+    max_warps = std::max<uint64_t>(max_warps, d.rows * pstride);
+    max_pos_threads = std::max<uint64_t>(max_pos_threads, 2 * packets[k]);
+  }
+  if (count == 1) qs.d[1] = qs.d[0];
+  k_packet_pos<<<dim3((unsigned) ((max_pos_threads + 255) / 256), count), 256, 0, c.stream>>>(qs);
+  if ((s = after_launch(c, "packet_pos")) != HD_OK) return s;
+  mark(c, 3);
+  const dim3 grid((unsigned) ((max_warps + kQueryWarps - 1) / kQueryWarps), count);
+  const bool cnt = ins[0].count;
+  if (dims == 2) {
+    if (cnt)
+      k_lbvh_query<2, true><<<grid, kQueryWarps * 32, 0, c.stream>>>(qs);
+    else
+      k_lbvh_query<2, false><<<grid, kQueryWarps * 32, 0, c.stream>>>(qs);
+  } else {
+    if (cnt)
+      k_lbvh_query<3, true><<<grid, kQueryWarps * 32, 0, c.stream>>>(qs);
+    else
+      k_lbvh_query<3, false><<<grid, kQueryWarps * 32, 0, c.stream>>>(qs);
+  }
+  if ((s = after_launch(c, "lbvh_query")) != HD_OK) return s;
+  mark(c, 4);
+  for (int k = 0; k < count; ++k)
+    if ((s = certify(c, ins[k])) != HD_OK) return s;
   return HD_OK;
 }
 
-template <int D>
-static hd_status launch_query(Ctx& c, const SortedSet& q, uint32_t pstride, const uint32_t* ppos,
-                              const Lbvh& bvh, const SortedSet& t, DevScalars* sc, bool count) {
-  const uint64_t packets = (q.n + 31) / 32;
-  const uint64_t rows = (packets + pstride - 1) / pstride;
-  const uint64_t warps = rows * pstride;
-  const uint64_t blocks = (warps + kQueryWarps - 1) / kQueryWarps;
-  if (count)
-    k_lbvh_query<D, true><<<(unsigned) blocks, kQueryWarps * 32, 0, c.stream>>>(
-        q.pts, q.n, pstride, rows, ppos, bvh.nodes, t.pts, t.n, bvh.L, sc);
-  else
-    k_lbvh_query<D, false><<<(unsigned) blocks, kQueryWarps * 32, 0, c.stream>>>(
-        q.pts, q.n, pstride, rows, ppos, bvh.nodes, t.pts, t.n, bvh.L, sc);
-  return after_launch(c, "lbvh_query");
-}
+hd_status run_lbvh(Ctx& c, const DirInput& in) { return run_lbvh_dirs(c, &in, 1); }
 
-hd_status run_lbvh(Ctx& c, const DirInput& in) {
-  if (in.dims != 2 && in.dims != 3) return fail(c, HD_ERR_UNSUPPORTED, "LBVH needs n_dims 2 or 3");
-  hd_status s;
-  const SortedSet *q, *t;
-  if ((s = spatial_prepare(c, in, &q, &t)) != HD_OK) return s;
-  mark(c, 1);
-  Lbvh bvh;
-  if ((s = build_lbvh(c, *t, in.dir, &bvh)) != HD_OK) return s;
-  mark(c, 2);
-  DevScalars* sc = scalars(c, in.dir);
-  const uint64_t packets = (q->n + 31) / 32;
-  void* ppos;
-  if ((s = ensure(c, kBufSample, packets * 8, &ppos)) != HD_OK) return s;
-  k_packet_pos<<<(unsigned) ((2 * packets + 255) / 256), 256, 0, c.stream>>>(
-      q->codes, q->n, t->codes, t->n, (uint32_t*) ppos);
-  if ((s = after_launch(c, "packet_pos")) != HD_OK) return s;
-  const uint32_t pstride = packets >= 4096 ? 64 : (packets >= 256 ? 16 : 1);
-  mark(c, 3);
-  if ((s = in.dims == 2 ? launch_query<2>(c, *q, pstride, (const uint32_t*) ppos, bvh, *t, sc,
-                                          in.count)
-                        : launch_query<3>(c, *q, pstride, (const uint32_t*) ppos, bvh, *t, sc,
-                                          in.count)) != HD_OK)
-    return s;
-  mark(c, 4);
-  return certify(c, in);
+hd_status run_lbvh_pair(Ctx& c, const DirInput& ab, const DirInput& ba) {
+  const DirInput ins[2] = {ab, ba};
+  return run_lbvh_dirs(c, ins, 2);
 }
 
 }  // namespace hdg

@@ -110,7 +110,9 @@ __global__ void k_frame(const uint32_t* __restrict__ ordA, const uint32_t* __res
     fr->hi[k] = hi;
     ext = fmaxf(ext, hi - lo);
   }
-  const int bits = dims == 2 ? 16 : 10;
+  // 30-bit codes in both cases, leaving bit 30 for the set when both sets
+  // are sorted together.
+  const int bits = dims == 2 ? 15 : 10;
   fr->bits = bits;
   fr->dims = dims;
   fr->extent = ext;
@@ -141,9 +143,15 @@ __device__ __forceinline__ uint32_t quant(float v, float lo, float scale, uint32
   return (uint32_t) q;
 }
 
-__global__ void k_morton(const float* __restrict__ P, uint64_t n, int dims,
-                         const Frame* __restrict__ fr, uint32_t* __restrict__ keys,
-                         uint32_t* __restrict__ vals) {
+// Morton codes of both sets in one launch (blockIdx.y = set); the key carries
+// the set in bit 30 so one radix sort orders A's points and then B's.
+__global__ void k_morton2(const float* __restrict__ A, uint64_t nA, const float* __restrict__ B,
+                          uint64_t nB, int dims, const Frame* __restrict__ fr,
+                          uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const float* P = blockIdx.y ? B : A;
+  const uint64_t n = blockIdx.y ? nB : nA;
+  const uint64_t base = blockIdx.y ? nA : 0;
+  const uint32_t setbit = blockIdx.y ? (1u << 30) : 0u;
   const float lo0 = fr->lo[0], lo1 = fr->lo[1], lo2 = fr->lo[2], s = fr->scale;
   const uint32_t maxq = (1u << fr->bits) - 1u;
   for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
@@ -157,22 +165,30 @@ __global__ void k_morton(const float* __restrict__ P, uint64_t n, int dims,
              (spread3(quant(P[3 * i + 1], lo1, s, maxq)) << 1) |
              (spread3(quant(P[3 * i + 2], lo2, s, maxq)) << 2);
     }
-    keys[i] = code;
-    vals[i] = (uint32_t) i;
+    keys[base + i] = code | setbit;
+    vals[base + i] = (uint32_t) (base + i);
   }
 }
 
-__global__ void k_gather(const float* __restrict__ P, uint64_t n, int dims,
-                         const uint32_t* __restrict__ order, float4* __restrict__ out) {
+// Gathers both sorted sets into float4 (x, y, z, index within its own set)
+// and writes their codes without the set bit.
+__global__ void k_gather2(const float* __restrict__ A, uint64_t nA, const float* __restrict__ B,
+                          uint64_t n, int dims, const uint32_t* __restrict__ skeys,
+                          const uint32_t* __restrict__ order, float4* __restrict__ out,
+                          uint32_t* __restrict__ codes) {
   for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
        i += (uint64_t) gridDim.x * blockDim.x) {
-    uint32_t v = order[i];
+    const uint64_t v = order[i];
+    const bool in_b = v >= nA;
+    const float* P = in_b ? B : A;
+    const uint64_t r = in_b ? v - nA : v;
     float4 p;
-    p.x = P[(uint64_t) v * dims];
-    p.y = P[(uint64_t) v * dims + 1];
-    p.z = dims == 3 ? P[(uint64_t) v * dims + 2] : 0.0f;
-    p.w = __uint_as_float(v);
+    p.x = P[r * dims];
+    p.y = P[r * dims + 1];
+    p.z = dims == 3 ? P[r * dims + 2] : 0.0f;
+    p.w = __uint_as_float((uint32_t) r);
     out[i] = p;
+    codes[i] = skeys[i] & ((1u << 30) - 1u);
   }
 }
 
@@ -222,46 +238,39 @@ static hd_status spatial_sort(Ctx& c, const float* A, uint64_t nA, const float* 
                                   frame(c));
   if ((s = after_launch(c, "frame")) != HD_OK) return s;
 
-  const uint64_t nmax = std::max(need_a ? nA : 0, need_b ? nB : 0);
-  void *keys, *keys2, *vals, *vals2, *tmp;
-  if ((s = ensure(c, kBufKeys, nmax * 4, &keys)) != HD_OK) return s;
-  if ((s = ensure(c, kBufKeysAlt, nmax * 4, &keys2)) != HD_OK) return s;
-  if ((s = ensure(c, kBufVals, nmax * 4, &vals)) != HD_OK) return s;
-  if ((s = ensure(c, kBufValsAlt, nmax * 4, &vals2)) != HD_OK) return s;
+  // One sort of both sets: key = 30-bit code | set << 30, value = global row.
+  const uint64_t n = nA + nB;
+  void *keys, *keys2, *vals, *vals2, *tmp, *pts, *codes;
+  if ((s = ensure(c, kBufKeys, n * 4, &keys)) != HD_OK) return s;
+  if ((s = ensure(c, kBufKeysAlt, n * 4, &keys2)) != HD_OK) return s;
+  if ((s = ensure(c, kBufVals, n * 4, &vals)) != HD_OK) return s;
+  if ((s = ensure(c, kBufValsAlt, n * 4, &vals2)) != HD_OK) return s;
+  if ((s = ensure(c, kBufSorted0, n * sizeof(float4), &pts)) != HD_OK) return s;
+  if ((s = ensure(c, kBufCodes0, n * 4, &codes)) != HD_OK) return s;
   size_t tmp_bytes = 0;
-  cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, (const uint32_t*) keys,
-                                  (uint32_t*) keys2, (const uint32_t*) vals,
-                                  (uint32_t*) vals2, (int64_t) nmax, 0, 32, c.stream);
+  cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, (const uint32_t*) keys, (uint32_t*) keys2,
+                                  (const uint32_t*) vals, (uint32_t*) vals2, (int64_t) n, 0, 31,
+                                  c.stream);
   if ((s = ensure(c, kBufCubTemp, tmp_bytes, &tmp)) != HD_OK) return s;
-
-  for (int set = 0; set < 2; ++set) {
-    const bool need = set == 0 ? need_a : need_b;
-    if (!need) continue;
-    const float* P = set == 0 ? A : B;
-    const uint64_t n = set == 0 ? nA : nB;
-    SortedSet* out = set == 0 ? sa : sb;
-    void *pts, *codes;
-    if ((s = ensure(c, set == 0 ? kBufSorted0 : kBufSorted1, n * sizeof(float4), &pts)) != HD_OK)
-      return s;
-    if ((s = ensure(c, set == 0 ? kBufCodes0 : kBufCodes1, n * 4, &codes)) != HD_OK) return s;
-    k_morton<<<grid_for(c, n), 256, 0, c.stream>>>(P, n, dims, frame(c), (uint32_t*) keys,
-                                                   (uint32_t*) vals);
+  {
+    const int gx = grid_for(c, std::max(nA, nB));
+    k_morton2<<<dim3(gx, 2), 256, 0, c.stream>>>(A, nA, B, nB, dims, frame(c), (uint32_t*) keys,
+                                                (uint32_t*) vals);
     if ((s = after_launch(c, "morton")) != HD_OK) return s;
-    size_t tb = tmp_bytes;
-    const int end_bit = dims == 2 ? 32 : 30;
-    cudaError_t e = cub::DeviceRadixSort::SortPairs(
-        tmp, tb, (const uint32_t*) keys, (uint32_t*) codes, (const uint32_t*) vals,
-        (uint32_t*) vals2, (int64_t) n, 0, end_bit, c.stream);
-    if (e != cudaSuccess) return cuda_fail(c, e, "radix sort");
-    k_gather<<<grid_for(c, n), 256, 0, c.stream>>>(P, n, dims, (const uint32_t*) vals2,
-                                                   (float4*) pts);
-    if ((s = after_launch(c, "gather")) != HD_OK) return s;
-    out->pts = (float4*) pts;
-    out->codes = (uint32_t*) codes;
-    out->n = n;
-    out->dims = dims;
-    out->src = P;
   }
+  size_t tb = tmp_bytes;
+  cudaError_t e = cub::DeviceRadixSort::SortPairs(tmp, tb, (const uint32_t*) keys,
+                                                  (uint32_t*) keys2, (const uint32_t*) vals,
+                                                  (uint32_t*) vals2, (int64_t) n, 0, 31, c.stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "radix sort");
+  k_gather2<<<grid_for(c, n), 256, 0, c.stream>>>(A, nA, B, n, dims, (const uint32_t*) keys2,
+                                                 (const uint32_t*) vals2, (float4*) pts,
+                                                 (uint32_t*) codes);
+  if ((s = after_launch(c, "gather")) != HD_OK) return s;
+  *sa = SortedSet{(float4*) pts, (uint32_t*) codes, nA, dims, A};
+  *sb = SortedSet{(float4*) pts + nA, (uint32_t*) codes + nA, nB, dims, B};
+  (void) need_a;
+  (void) need_b;
   return HD_OK;
 }
 
