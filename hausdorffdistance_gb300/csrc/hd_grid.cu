@@ -105,9 +105,9 @@ __global__ void k_grid_runs(const uint32_t* __restrict__ codes, uint64_t n, int 
   const uint32_t shift = gp->shift, cpa = gp->cpa;
   for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
        i += (uint64_t) gridDim.x * blockDim.x) {
-    const uint32_t c = codes[i] >> shift;
-    const bool first = i == 0 || (codes[i - 1] >> shift) != c;
-    const bool last = i + 1 == n || (codes[i + 1] >> shift) != c;
+    const uint32_t c = (codes[i] & kCodeMask) >> shift;
+    const bool first = i == 0 || ((codes[i - 1] & kCodeMask) >> shift) != c;
+    const bool last = i + 1 == n || ((codes[i + 1] & kCodeMask) >> shift) != c;
     if (first || last) {
       const uint32_t lin = cell_linear(c, dims, cpa);
       if (first) table[lin].x = (uint32_t) i;
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(128)
   if (i >= nQ) return;
   const float4 q4 = Q[i];
   const float p[3] = {q4.x, q4.y, q4.z};
-  const uint32_t cc = qcodes[i] >> gp.shift;
+  const uint32_t cc = (qcodes[i] & kCodeMask) >> gp.shift;
   int home[3];
   if (D == 2) {
     home[0] = (int) compact2(cc);

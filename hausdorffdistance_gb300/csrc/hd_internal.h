@@ -10,6 +10,9 @@
 
 namespace hdg {
 
+// Bits of a sorted key that hold the Morton code (bit 30 marks the set).
+constexpr uint32_t kCodeMask = (1u << 30) - 1u;
+
 // Device scalars of one directed solve, zeroed with one memset per solve.
 struct DevScalars {
   unsigned long long max_key;     // packed (d2 bits, ~ia) running maximum
@@ -49,7 +52,7 @@ enum BufSlot {
   kBufValsAlt,
   kBufSorted0,    // Morton-sorted points of set 0 / set 1 (float4 x,y,z,index)
   kBufSorted1,
-  kBufCodes0,     // sorted Morton codes of set 0 / set 1
+  kBufCodes0,     // leaf boxes of both sorted sets
   kBufCodes1,
   kBufNodes0,     // LBVH nodes or grid cell table of set 0 / set 1
   kBufNodes1,
@@ -80,7 +83,9 @@ struct Frame {
 // A point set in Morton order: float4 (x, y, z|0, caller index as bits).
 struct SortedSet {
   float4* pts = nullptr;
-  uint32_t* codes = nullptr;
+  uint32_t* codes = nullptr;   // sorted keys: Morton code in bits 0-29 (mask kCodeMask)
+  float4* leaf_boxes = nullptr;  // per leaf of leaf_size points: lo, hi
+  uint32_t leaf_size = 16;
   uint64_t n = 0;
   int dims = 0;
   const float* src = nullptr;  // device pointer it was sorted from

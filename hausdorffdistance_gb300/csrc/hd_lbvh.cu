@@ -43,28 +43,9 @@ constexpr int kStack = 64;
 __device__ __forceinline__ int delta(const uint32_t* __restrict__ codes, uint32_t L,
                                      int64_t nL, int64_t i, int64_t j) {
   if (j < 0 || j >= nL) return -1;
-  uint64_t ki = ((uint64_t) codes[(uint64_t) i * L] << 32) | (uint64_t) i;
-  uint64_t kj = ((uint64_t) codes[(uint64_t) j * L] << 32) | (uint64_t) j;
+  uint64_t ki = ((uint64_t) (codes[(uint64_t) i * L] & kCodeMask) << 32) | (uint64_t) i;
+  uint64_t kj = ((uint64_t) (codes[(uint64_t) j * L] & kCodeMask) << 32) | (uint64_t) j;
   return __clzll(ki ^ kj);
-}
-
-// Leaf boxes: one thread per leaf over its (at most 32) points.
-__device__ __forceinline__ void leaf_boxes_body(const float4* __restrict__ pts, uint64_t n,
-                                                uint32_t L, uint32_t nL, uint32_t nI,
-                                                float4* __restrict__ boxes) {
-  uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
-  if (leaf >= nL) return;
-  uint64_t s = (uint64_t) leaf * L;
-  uint64_t e = min(s + L, n);
-  float4 lo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f);
-  float4 hi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
-  for (uint64_t i = s; i < e; ++i) {
-    float4 p = pts[i];
-    lo.x = fminf(lo.x, p.x); lo.y = fminf(lo.y, p.y); lo.z = fminf(lo.z, p.z);
-    hi.x = fmaxf(hi.x, p.x); hi.y = fmaxf(hi.y, p.y); hi.z = fmaxf(hi.z, p.z);
-  }
-  boxes[2 * ((uint64_t) nI + leaf)] = lo;
-  boxes[2 * ((uint64_t) nI + leaf) + 1] = hi;
 }
 
 // Karras 2012, one thread per internal node.  Node ids: internal [0, nI),
@@ -108,9 +89,25 @@ __device__ __forceinline__ uint32_t node_id(uint32_t ref, uint32_t nI) {
 
 // Bottom-up boxes: a thread per leaf climbs; the second child to arrive at a
 // parent computes its box (Karras 2012, section 4).
+// Box of node `id`: leaves' boxes come from the sorted set's gather pass,
+// internal boxes from this build (written by other threads: read around L1).
+__device__ __forceinline__ void node_box(uint32_t id, uint32_t nI, const float4* boxes,
+                                         const float4* __restrict__ leaf_boxes, float4* lo,
+                                         float4* hi) {
+  if (id >= nI) {
+    *lo = leaf_boxes[2 * (uint64_t) (id - nI)];
+    *hi = leaf_boxes[2 * (uint64_t) (id - nI) + 1];
+  } else {
+    *lo = __ldcg(&boxes[2 * (uint64_t) id]);
+    *hi = __ldcg(&boxes[2 * (uint64_t) id + 1]);
+  }
+}
+
 __device__ __forceinline__ void bottom_up_body(const uint2* __restrict__ child,
                                                const uint32_t* __restrict__ parent, uint32_t nL,
-                                               uint32_t nI, float4* boxes, uint32_t* flags) {
+                                               uint32_t nI, float4* boxes,
+                                               const float4* __restrict__ leaf_boxes,
+                                               uint32_t* flags) {
   uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
   if (leaf >= nL || nI == 0) return;
   uint32_t node = nI + leaf;
@@ -121,8 +118,9 @@ __device__ __forceinline__ void bottom_up_body(const uint2* __restrict__ child,
     __threadfence();
     uint2 ch = child[p];
     uint32_t a = node_id(ch.x, nI), b = node_id(ch.y, nI);
-    float4 alo = __ldcg(&boxes[2 * (uint64_t) a]), ahi = __ldcg(&boxes[2 * (uint64_t) a + 1]);
-    float4 blo = __ldcg(&boxes[2 * (uint64_t) b]), bhi = __ldcg(&boxes[2 * (uint64_t) b + 1]);
+    float4 alo, ahi, blo, bhi;
+    node_box(a, nI, boxes, leaf_boxes, &alo, &ahi);
+    node_box(b, nI, boxes, leaf_boxes, &blo, &bhi);
     float4 lo = make_float4(fminf(alo.x, blo.x), fminf(alo.y, blo.y), fminf(alo.z, blo.z), 0.f);
     float4 hi = make_float4(fmaxf(ahi.x, bhi.x), fmaxf(ahi.y, bhi.y), fmaxf(ahi.z, bhi.z), 0.f);
     __stcg(&boxes[2 * (uint64_t) p], lo);
@@ -134,13 +132,14 @@ __device__ __forceinline__ void bottom_up_body(const uint2* __restrict__ child,
 
 // Packs every internal node as 4 float4: both children's boxes and refs.
 __device__ __forceinline__ void pack_nodes_body(const uint2* __restrict__ child,
-                                                const float4* __restrict__ boxes, uint32_t nI,
+                                                const float4* __restrict__ boxes,
+                                                const float4* __restrict__ leaf_boxes, uint32_t nI,
                                                 float4* __restrict__ nodes) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (nI == 0) {
     // Single leaf: a root whose right child is an empty box (never visited).
     if (i == 0) {
-      float4 lo = boxes[0], hi = boxes[1];
+      float4 lo = leaf_boxes[0], hi = leaf_boxes[1];
       nodes[0] = make_float4(lo.x, lo.y, lo.z, hi.x);
       nodes[1] = make_float4(hi.y, hi.z, FLT_MAX, FLT_MAX);
       nodes[2] = make_float4(FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX);
@@ -151,8 +150,9 @@ __device__ __forceinline__ void pack_nodes_body(const uint2* __restrict__ child,
   if (i >= nI) return;
   uint2 ch = child[i];
   uint32_t a = node_id(ch.x, nI), b = node_id(ch.y, nI);
-  float4 alo = boxes[2 * (uint64_t) a], ahi = boxes[2 * (uint64_t) a + 1];
-  float4 blo = boxes[2 * (uint64_t) b], bhi = boxes[2 * (uint64_t) b + 1];
+  float4 alo, ahi, blo, bhi;
+  node_box(a, nI, boxes, leaf_boxes, &alo, &ahi);
+  node_box(b, nI, boxes, leaf_boxes, &blo, &bhi);
   float4* o = nodes + 4 * (uint64_t) i;
   o[0] = make_float4(alo.x, alo.y, alo.z, ahi.x);
   o[1] = make_float4(ahi.y, ahi.z, blo.x, blo.y);
@@ -210,8 +210,11 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   // spread over the whole Morton range, so the running maximum rises to
   // nearly its final value while the bulk of the packets is still queued
   // (the reference samples with EB for the same purpose, hybrid.h:128-168).
-  const uint64_t w = (uint64_t) blockIdx.x * kQueryWarps + warp;
-  const uint64_t packet = (w % rows) * pstride + w / rows;
+  // 32-bit arithmetic: packet counts stay below 2^27 (point sets < 2^32).
+  const uint32_t w = blockIdx.x * kQueryWarps + warp;
+  const uint32_t r32 = (uint32_t) rows;
+  const uint32_t wq = w / r32;
+  const uint64_t packet = (uint64_t) (w - wq * r32) * pstride + wq;
   if (packet * 32 >= nItems) return;
   const uint64_t item = packet * 32 + lane;
   bool active = item < nItems;
@@ -268,11 +271,12 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
     // spatially close.  Scanning that leaf and its neighbours lets most lanes
     // stop before any traversal, and gives the others a small running
     // minimum that prunes the traversal.
-    const uint32_t nL = (uint32_t) ((nB + L - 1) / L);
+    const uint32_t lshift = __ffs(L) - 1;  // L is a power of two
+    const uint32_t nL = (uint32_t) ((nB + L - 1) >> lshift);
     // Both ends of the packet are looked up: a packet can straddle a jump of
     // the Morton curve, and then its two ends sit in different regions.
-    const uint32_t leaf0 = (uint32_t) min((uint64_t) ppos[2 * packet] / L, (uint64_t) (nL - 1));
-    const uint32_t leaf1 = (uint32_t) min((uint64_t) ppos[2 * packet + 1] / L, (uint64_t) (nL - 1));
+    const uint32_t leaf0 = min(ppos[2 * packet] >> lshift, nL - 1);
+    const uint32_t leaf1 = min(ppos[2 * packet + 1] >> lshift, nL - 1);
     scan_leaf(leaf0);
     if (leaf1 != leaf0 && __any_sync(0xFFFFFFFFu, active)) scan_leaf(leaf1);
     if (leaf0 + 1 < nL && leaf0 + 1 != leaf1 && __any_sync(0xFFFFFFFFu, active))
@@ -357,11 +361,11 @@ __device__ __forceinline__ void packet_pos_body(const uint32_t* __restrict__ qco
   const uint64_t p = t >> 1;
   if (p * 32 >= nQ) return;
   const uint64_t q = (t & 1) ? min(p * 32 + 31, nQ - 1) : p * 32;
-  const uint32_t target = qcodes[q];
+  const uint32_t target = qcodes[q] & kCodeMask;
   uint64_t lo = 0, hi = nB;
   while (lo < hi) {
     const uint64_t mid = (lo + hi) >> 1;
-    if (bcodes[mid] < target)
+    if ((bcodes[mid] & kCodeMask) < target)
       lo = mid + 1;
     else
       hi = mid;
@@ -377,7 +381,8 @@ struct BuildSet {
   const uint32_t* codes;
   uint64_t n;
   uint32_t L, nL, nI;
-  float4* boxes;
+  float4* boxes;  // internal nodes only
+  const float4* leaf_boxes;
   uint2* child;
   uint32_t* parent;
   uint32_t* flags;
@@ -387,21 +392,17 @@ struct BuildSets {
   BuildSet s[2];
 };
 
-__global__ void k_leaf_boxes(BuildSets b) {
-  const BuildSet& S = b.s[blockIdx.y];
-  leaf_boxes_body(S.pts, S.n, S.L, S.nL, S.nI, S.boxes);
-}
 __global__ void k_karras(BuildSets b) {
   const BuildSet& S = b.s[blockIdx.y];
   karras_body(S.codes, S.L, S.nL, S.child, S.parent);
 }
 __global__ void k_bottom_up(BuildSets b) {
   const BuildSet& S = b.s[blockIdx.y];
-  bottom_up_body(S.child, S.parent, S.nL, S.nI, S.boxes, S.flags);
+  bottom_up_body(S.child, S.parent, S.nL, S.nI, S.boxes, S.leaf_boxes, S.flags);
 }
 __global__ void k_pack_nodes(BuildSets b) {
   const BuildSet& S = b.s[blockIdx.y];
-  pack_nodes_body(S.child, S.boxes, S.nI, S.nodes);
+  pack_nodes_body(S.child, S.boxes, S.leaf_boxes, S.nI, S.nodes);
 }
 
 struct QuerySet {
@@ -437,7 +438,9 @@ __global__ void k_packet_pos(QuerySets qs) {
 
 // Builds the LBVHs of `count` sorted sets (tree k into node slot k).
 static hd_status build_lbvhs(Ctx& c, const SortedSet* const* sets, int count, BuildSets* out) {
-  const uint32_t L = c.opt.leaf_size ? std::min<uint32_t>(c.opt.leaf_size, 32) : 16;
+  // Leaves hold a power of two of points (at most 32): the query kernel
+  // turns positions into leaf indices with a shift.
+  const uint32_t L = sets[0]->leaf_size;  // fixed by the gather's leaf boxes
   hd_status s;
   uint64_t nodes_total = 0, internal_total = 0;
   uint64_t nL[2], nI[2];
@@ -446,9 +449,10 @@ static hd_status build_lbvhs(Ctx& c, const SortedSet* const* sets, int count, Bu
     nI[k] = nL[k] - 1;
     nodes_total += nI[k] + nL[k];
     internal_total += std::max<uint64_t>(nI[k], 1);
+    if (sets[k]->leaf_size != L) return fail(c, HD_ERR_CUDA, "leaf sizes differ");
   }
   void *boxes, *aux, *aux2;
-  if ((s = ensure(c, kBufBoxes, nodes_total * 2 * sizeof(float4), &boxes)) != HD_OK) return s;
+  if ((s = ensure(c, kBufBoxes, internal_total * 2 * sizeof(float4), &boxes)) != HD_OK) return s;
   if ((s = ensure(c, kBufAux, internal_total * sizeof(uint2), &aux)) != HD_OK) return s;
   if ((s = ensure(c, kBufAux2, (nodes_total + internal_total) * 4, &aux2)) != HD_OK) return s;
   // Flags of all sets are contiguous (first in aux2) so one memset clears them.
@@ -468,7 +472,8 @@ static hd_status build_lbvhs(Ctx& c, const SortedSet* const* sets, int count, Bu
     b.L = L;
     b.nL = (uint32_t) nL[k];
     b.nI = (uint32_t) nI[k];
-    b.boxes = (float4*) boxes + 2 * off_nodes;
+    b.boxes = (float4*) boxes + 2 * off_int;
+    b.leaf_boxes = sets[k]->leaf_boxes;
     b.child = (uint2*) aux + off_int;
     b.flags = flags_base + off_int;
     b.parent = parent_base + off_nodes;
@@ -480,8 +485,6 @@ static hd_status build_lbvhs(Ctx& c, const SortedSet* const* sets, int count, Bu
   }
   if (count == 1) out->s[1] = out->s[0];
   const dim3 gl((unsigned) ((maxL + 255) / 256), count), gi((unsigned) ((maxI + 255) / 256), count);
-  k_leaf_boxes<<<gl, 256, 0, c.stream>>>(*out);
-  if ((s = after_launch(c, "leaf_boxes")) != HD_OK) return s;
   k_karras<<<gi, 256, 0, c.stream>>>(*out);
   if ((s = after_launch(c, "karras")) != HD_OK) return s;
   cudaError_t e = cudaMemsetAsync(flags_base, 0, internal_total * 4, c.stream);

@@ -170,25 +170,50 @@ __global__ void k_morton2(const float* __restrict__ A, uint64_t nA, const float*
   }
 }
 
-// Gathers both sorted sets into float4 (x, y, z, index within its own set)
-// and writes their codes without the set bit.
+// Gathers the sorted sets (blockIdx.y = set) into float4 (x, y, z, index
+// within its own set) and, in the same pass, the bounding box of every leaf
+// of L consecutive sorted points (L a power of two <= 32; lanes of a warp
+// cover whole leaves, reduced with shuffles).
 __global__ void k_gather2(const float* __restrict__ A, uint64_t nA, const float* __restrict__ B,
-                          uint64_t n, int dims, const uint32_t* __restrict__ skeys,
-                          const uint32_t* __restrict__ order, float4* __restrict__ out,
-                          uint32_t* __restrict__ codes) {
-  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t) gridDim.x * blockDim.x) {
-    const uint64_t v = order[i];
-    const bool in_b = v >= nA;
-    const float* P = in_b ? B : A;
-    const uint64_t r = in_b ? v - nA : v;
-    float4 p;
-    p.x = P[r * dims];
-    p.y = P[r * dims + 1];
-    p.z = dims == 3 ? P[r * dims + 2] : 0.0f;
-    p.w = __uint_as_float((uint32_t) r);
-    out[i] = p;
-    codes[i] = skeys[i] & ((1u << 30) - 1u);
+                          uint64_t nB, int dims, const uint32_t* __restrict__ order,
+                          float4* __restrict__ out, uint32_t L, float4* __restrict__ leaf_boxes,
+                          uint64_t leaf_off_b) {
+  const bool setb = blockIdx.y != 0;
+  const float* P = setb ? B : A;
+  const uint64_t n = setb ? nB : nA;
+  const uint64_t base = setb ? nA : 0;
+  float4* lb = leaf_boxes + (setb ? 2 * leaf_off_b : 0);
+  const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+  for (uint64_t j0 = blockIdx.x * (uint64_t) blockDim.x + (threadIdx.x & ~31u); j0 < n; j0 += stride) {
+    const uint64_t j = j0 + (threadIdx.x & 31u);
+    const bool valid = j < n;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    float lx = FLT_MAX, ly = FLT_MAX, lz = FLT_MAX, hx = -FLT_MAX, hy = -FLT_MAX, hz = -FLT_MAX;
+    if (valid) {
+      const uint64_t v = order[base + j];
+      const uint64_t r = setb ? v - nA : v;
+      p.x = P[r * dims];
+      p.y = P[r * dims + 1];
+      p.z = dims == 3 ? P[r * dims + 2] : 0.0f;
+      p.w = __uint_as_float((uint32_t) r);
+      out[base + j] = p;
+      lx = hx = p.x;
+      ly = hy = p.y;
+      lz = hz = p.z;
+    }
+    for (uint32_t o = 1; o < L; o <<= 1) {
+      lx = fminf(lx, __shfl_xor_sync(0xFFFFFFFFu, lx, o));
+      ly = fminf(ly, __shfl_xor_sync(0xFFFFFFFFu, ly, o));
+      lz = fminf(lz, __shfl_xor_sync(0xFFFFFFFFu, lz, o));
+      hx = fmaxf(hx, __shfl_xor_sync(0xFFFFFFFFu, hx, o));
+      hy = fmaxf(hy, __shfl_xor_sync(0xFFFFFFFFu, hy, o));
+      hz = fmaxf(hz, __shfl_xor_sync(0xFFFFFFFFu, hz, o));
+    }
+    if (valid && (j & (L - 1)) == 0) {
+      const uint64_t leaf = j / L;
+      lb[2 * leaf] = make_float4(lx, ly, lz, 0.f);
+      lb[2 * leaf + 1] = make_float4(hx, hy, hz, 0.f);
+    }
   }
 }
 
@@ -240,13 +265,17 @@ static hd_status spatial_sort(Ctx& c, const float* A, uint64_t nA, const float* 
 
   // One sort of both sets: key = 30-bit code | set << 30, value = global row.
   const uint64_t n = nA + nB;
-  void *keys, *keys2, *vals, *vals2, *tmp, *pts, *codes;
+  uint32_t L = c.opt.leaf_size ? std::min<uint32_t>(c.opt.leaf_size, 32) : 16;
+  while (L & (L - 1)) L &= L - 1;
+  const uint64_t leaves_a = (nA + L - 1) / L, leaves_b = (nB + L - 1) / L;
+  void *keys, *keys2, *vals, *vals2, *tmp, *pts, *lboxes;
   if ((s = ensure(c, kBufKeys, n * 4, &keys)) != HD_OK) return s;
   if ((s = ensure(c, kBufKeysAlt, n * 4, &keys2)) != HD_OK) return s;
   if ((s = ensure(c, kBufVals, n * 4, &vals)) != HD_OK) return s;
   if ((s = ensure(c, kBufValsAlt, n * 4, &vals2)) != HD_OK) return s;
   if ((s = ensure(c, kBufSorted0, n * sizeof(float4), &pts)) != HD_OK) return s;
-  if ((s = ensure(c, kBufCodes0, n * 4, &codes)) != HD_OK) return s;
+  if ((s = ensure(c, kBufCodes0, (leaves_a + leaves_b) * 2 * sizeof(float4), &lboxes)) != HD_OK)
+    return s;
   size_t tmp_bytes = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, (const uint32_t*) keys, (uint32_t*) keys2,
                                   (const uint32_t*) vals, (uint32_t*) vals2, (int64_t) n, 0, 31,
@@ -263,12 +292,12 @@ static hd_status spatial_sort(Ctx& c, const float* A, uint64_t nA, const float* 
                                                   (uint32_t*) keys2, (const uint32_t*) vals,
                                                   (uint32_t*) vals2, (int64_t) n, 0, 31, c.stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "radix sort");
-  k_gather2<<<grid_for(c, n), 256, 0, c.stream>>>(A, nA, B, n, dims, (const uint32_t*) keys2,
-                                                 (const uint32_t*) vals2, (float4*) pts,
-                                                 (uint32_t*) codes);
+  k_gather2<<<dim3(grid_for(c, std::max(nA, nB)), 2), 256, 0, c.stream>>>(
+      A, nA, B, nB, dims, (const uint32_t*) vals2, (float4*) pts, L, (float4*) lboxes, leaves_a);
   if ((s = after_launch(c, "gather")) != HD_OK) return s;
-  *sa = SortedSet{(float4*) pts, (uint32_t*) codes, nA, dims, A};
-  *sb = SortedSet{(float4*) pts + nA, (uint32_t*) codes + nA, nB, dims, B};
+  *sa = SortedSet{(float4*) pts, (uint32_t*) keys2, (float4*) lboxes, L, nA, dims, A};
+  *sb = SortedSet{(float4*) pts + nA, (uint32_t*) keys2 + nA, (float4*) lboxes + 2 * leaves_a, L,
+                  nB, dims, B};
   (void) need_a;
   (void) need_b;
   return HD_OK;
