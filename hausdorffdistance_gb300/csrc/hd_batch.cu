@@ -7,11 +7,12 @@
 // Work decomposition.  A problem-direction (problem p, A->B or B->A) is cut
 // into items of 32 query rows; one warp processes one item, one lane per
 // row.  Items are ordered largest problem first (longest-processing-time
-// order over |A|*|B|), and the first item of every problem-direction comes
-// before all other items: these "seed" items finish early and give each
-// problem a running maximum that the rest of its rows break against.  Warps
-// take items in a grid-stride sweep over that order, so there is no queue
-// atomic per item.
+// order over |A|*|B|).  One "seed" item per problem-direction — 32 rows
+// spread evenly over the set — runs first, in its own launch, so that every
+// problem has a running maximum close to its final value before the sweep
+// over all rows starts; sweep rows then break against it.  Warps take items
+// in a grid-stride sweep over that order, so there is no queue atomic per
+// item.
 //
 // Per row: a circular scan of the other set, starting at the row's relative
 // position (row * |Y| / |X|), so that sets stored in a spatially coherent
@@ -78,8 +79,9 @@ __device__ __forceinline__ void decode_item(uint64_t w, uint64_t nseed, int ndir
   }
   const uint64_t local = k - rest_prefix[lo];
   const hd_problem pr = probs[order[lo]];
-  const uint64_t it0 = (pr.n_a + 31) / 32 - 1;  // rest items of direction 0
+  const uint64_t it0 = (pr.n_a + 31) / 32;  // items of direction 0
   *r_out = lo;
+  // Item numbers of the sweep start at 1; item 0 denotes the seed item.
   if (local < it0 || ndir == 1) {
     *d_out = 0;
     *item_out = local + 1;
@@ -93,13 +95,13 @@ template <int D>
 __global__ void __launch_bounds__(kBatchThreads)
     k_batch(const float* __restrict__ A, const float* __restrict__ B,
             const hd_problem* __restrict__ probs, const uint32_t* __restrict__ order,
-            const uint64_t* __restrict__ rest_prefix, uint32_t nprob, int ndir, uint64_t total,
-            unsigned long long* __restrict__ keys) {
+            const uint64_t* __restrict__ rest_prefix, uint32_t nprob, int ndir, uint64_t begin,
+            uint64_t end, unsigned long long* __restrict__ keys) {
   const int lane = threadIdx.x & 31;
   const uint64_t warps = (uint64_t) gridDim.x * (kBatchThreads / 32);
   const uint64_t nseed = (uint64_t) nprob * ndir;
-  for (uint64_t w = (uint64_t) blockIdx.x * (kBatchThreads / 32) + (threadIdx.x >> 5); w < total;
-       w += warps) {
+  for (uint64_t w = begin + (uint64_t) blockIdx.x * (kBatchThreads / 32) + (threadIdx.x >> 5);
+       w < end; w += warps) {
     uint32_t r;
     int d;
     uint64_t item;
@@ -109,8 +111,21 @@ __global__ void __launch_bounds__(kBatchThreads)
     const float* X = d == 0 ? A + pr.offset_a * D : B + pr.offset_b * D;
     const float* Y = d == 0 ? B + pr.offset_b * D : A + pr.offset_a * D;
     const uint64_t nx = d == 0 ? pr.n_a : pr.n_b, ny = d == 0 ? pr.n_b : pr.n_a;
-    const uint64_t row = item * 32 + lane;
-    if (row >= nx) continue;
+    // The seed item takes 32 rows spread evenly over the set (a sample of the
+    // whole problem: its maximum is a good early threshold); sweep items
+    // 1, 2, ... take rows 32 (item - 1) onward, every row once.
+    uint64_t row;
+    if (item == 0) {
+      if (nx <= 32) {
+        if ((uint64_t) lane >= nx) continue;
+        row = lane;
+      } else {
+        row = ((uint64_t) lane * nx) / 32;
+      }
+    } else {
+      row = (item - 1) * 32 + lane;
+      if (row >= nx) continue;
+    }
     unsigned long long* key = keys + 2 * (uint64_t) p + d;
     float thr = threshold_of(ld_relaxed_u64(key));
     float cmin = INFINITY;
@@ -208,8 +223,8 @@ hd_status make_plan(const hd_problem* probs, uint64_t n, int ndir, BatchPlan* pl
   for (uint64_t r = 0; r < n; ++r) {
     plan->rest_prefix[r] = acc;
     const hd_problem& p = probs[plan->order[r]];
-    acc += (p.n_a + 31) / 32 - 1;
-    if (ndir == 2) acc += (p.n_b + 31) / 32 - 1;
+    acc += (p.n_a + 31) / 32;
+    if (ndir == 2) acc += (p.n_b + 31) / 32;
   }
   plan->rest_prefix[n] = acc;
   plan->total = (uint64_t) n * ndir + acc;
@@ -297,12 +312,20 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   if (e != cudaSuccess) return cuda_fail(c, e, "begin capture");
   cudaMemsetAsync(d_keys, 0, b_keys, c.stream);
   cudaMemsetAsync(d_bad, 0, 4, c.stream);
-  if (dims == 2)
-    k_batch<2><<<grid, kBatchThreads, 0, c.stream>>>(dA, dB, d_probs, d_order, d_prefix,
-                                                     (uint32_t) n, ndir, plan.total, d_keys);
-  else
-    k_batch<3><<<grid, kBatchThreads, 0, c.stream>>>(dA, dB, d_probs, d_order, d_prefix,
-                                                     (uint32_t) n, ndir, plan.total, d_keys);
+  // Seed items first, as their own launch: every problem has a running
+  // maximum before any of its sweep rows starts.
+  const uint64_t nseed = n * ndir;
+  for (int part = 0; part < 2; ++part) {
+    const uint64_t b = part == 0 ? 0 : nseed, e2 = part == 0 ? nseed : plan.total;
+    if (e2 <= b) continue;
+    const int g = (int) std::max<uint64_t>(1, std::min<uint64_t>((uint64_t) grid, (e2 - b + 7) / 8));
+    if (dims == 2)
+      k_batch<2><<<g, kBatchThreads, 0, c.stream>>>(dA, dB, d_probs, d_order, d_prefix,
+                                                    (uint32_t) n, ndir, b, e2, d_keys);
+    else
+      k_batch<3><<<g, kBatchThreads, 0, c.stream>>>(dA, dB, d_probs, d_order, d_prefix,
+                                                    (uint32_t) n, ndir, b, e2, d_keys);
+  }
   const uint64_t cw = n * ndir;
   const unsigned cblocks = (unsigned) ((cw * 32 + 255) / 256);
   if (dims == 2)
@@ -318,7 +341,7 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda_fail(c, e, "instantiate graph");
   e = cudaGraphLaunch(exec, c.stream);
-  c.launches += 3;
+  c.launches += 4;
   if (e != cudaSuccess) {
     cudaGraphExecDestroy(exec);
     return cuda_fail(c, e, "graph launch");

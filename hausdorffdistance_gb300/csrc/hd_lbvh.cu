@@ -227,27 +227,24 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   float thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
   unsigned long long pairs = 0, visits = 0, leafv = 0;
 
-  // Scans one leaf with every lane of the packet (points broadcast by
-  // shuffles, four at a time); stops as soon as no lane still needs a point,
+  // Scans one leaf with every lane of the packet (points read as broadcast
+  // loads, four at a time); stops as soon as no lane still needs a point,
   // and lets lanes that found a point within the running maximum stop.
   auto scan_leaf = [&](uint32_t leaf) {
     const uint64_t s = (uint64_t) leaf * L;
     const int cnt = (int) min((uint64_t) L, nB - s);
-    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (lane < cnt) p = B[s + lane];
+    const float4* lp = B + s;
     float m = cmin;
     int k = 0;
     for (; k < cnt; k += 4) {
+      // Every lane reads the same point: one broadcast load per point.
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const int src = min(k + u, cnt - 1);
-        const float bx = __shfl_sync(0xFFFFFFFFu, p.x, src);
-        const float by = __shfl_sync(0xFFFFFFFFu, p.y, src);
+        const float4 b = __ldg(lp + min(k + u, cnt - 1));
         if constexpr (D == 2) {
-          m = fminf(m, d2_2(q.x, q.y, bx, by));
+          m = fminf(m, d2_2(q.x, q.y, b.x, b.y));
         } else {
-          const float bz = __shfl_sync(0xFFFFFFFFu, p.z, src);
-          m = fminf(m, d2_3(q.x, q.y, q.z, bx, by, bz));
+          m = fminf(m, d2_3(q.x, q.y, q.z, b.x, b.y, b.z));
         }
       }
       if (!__any_sync(0xFFFFFFFFu, active && m > thr)) {
