@@ -7,12 +7,16 @@
 // Work decomposition.  A problem-direction (problem p, A->B or B->A) is cut
 // into items of 32 query rows; one warp processes one item, one lane per
 // row.  Items are ordered largest problem first (longest-processing-time
-// order over |A|*|B|).  One "seed" item per problem-direction — 32 rows
-// spread evenly over the set — runs first, in its own launch, so that every
-// problem has a running maximum close to its final value before the sweep
-// over all rows starts; sweep rows then break against it.  Warps take items
-// in a grid-stride sweep over that order, so there is no queue atomic per
-// item.
+// order over |A|*|B|); warps take items in a grid-stride sweep over that
+// order, so there is no queue atomic per item.  Three passes, captured in one
+// graph:
+//   1. window bound: every row takes the minimum over a few points of the
+//      other set around its relative position, an upper bound on its
+//      nearest-neighbour distance; the largest bound per problem-direction
+//      (with its row) is kept;
+//   2. seed: one warp per problem-direction computes the exact nearest
+//      neighbour of that row and starts the running maximum with it;
+//   3. sweep: every row scans with early break against that maximum.
 //
 // Per row: a circular scan of the other set, starting at the row's relative
 // position (row * |Y| / |X|), so that sets stored in a spatially coherent
@@ -56,32 +60,25 @@ __device__ __forceinline__ float pt_d2(const float* __restrict__ X, uint64_t i,
   }
 }
 
-// Decodes a global item index into (sorted problem rank, direction, item).
-__device__ __forceinline__ void decode_item(uint64_t w, uint64_t nseed, int ndir,
+// Decodes a global item index into (sorted problem rank, direction, item);
+// item numbers start at 1.
+__device__ __forceinline__ void decode_item(uint64_t w, int ndir,
                                             const uint64_t* __restrict__ rest_prefix,
                                             uint32_t nprob, const hd_problem* __restrict__ probs,
                                             const uint32_t* __restrict__ order, uint32_t* r_out,
                                             int* d_out, uint64_t* item_out) {
-  if (w < nseed) {
-    *r_out = (uint32_t) (w / ndir);
-    *d_out = (int) (w % ndir);
-    *item_out = 0;
-    return;
-  }
-  const uint64_t k = w - nseed;
-  uint32_t lo = 0, hi = nprob;  // rest_prefix[lo] <= k < rest_prefix[hi]
+  uint32_t lo = 0, hi = nprob;  // rest_prefix[lo] <= w < rest_prefix[hi]
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
-    if (rest_prefix[mid] <= k)
+    if (rest_prefix[mid] <= w)
       lo = mid;
     else
       hi = mid;
   }
-  const uint64_t local = k - rest_prefix[lo];
+  const uint64_t local = w - rest_prefix[lo];
   const hd_problem pr = probs[order[lo]];
   const uint64_t it0 = (pr.n_a + 31) / 32;  // items of direction 0
   *r_out = lo;
-  // Item numbers of the sweep start at 1; item 0 denotes the seed item.
   if (local < it0 || ndir == 1) {
     *d_out = 0;
     *item_out = local + 1;
@@ -91,45 +88,61 @@ __device__ __forceinline__ void decode_item(uint64_t w, uint64_t nseed, int ndir
   }
 }
 
+constexpr int kWindow = 4;  // window half-width of the bound pass
+
+// Pass 1 (mode 0) and pass 3 (mode 1) over items of 32 rows.
+//   mode 0: each row takes the minimum over a window of 2*kWindow+1 points
+//           of the other set around its relative position, an upper bound on
+//           its nearest-neighbour distance; the warp's largest bound (with its
+//           row) goes to ubound[problem-direction] by one atomicMax.
+//   mode 1: each row scans the other set circularly from the start of that
+//           window with early break against the running maximum.
 template <int D>
 __global__ void __launch_bounds__(kBatchThreads)
     k_batch(const float* __restrict__ A, const float* __restrict__ B,
             const hd_problem* __restrict__ probs, const uint32_t* __restrict__ order,
-            const uint64_t* __restrict__ rest_prefix, uint32_t nprob, int ndir, uint64_t begin,
-            uint64_t end, unsigned long long* __restrict__ keys) {
+            const uint64_t* __restrict__ rest_prefix, uint32_t nprob, int ndir, uint64_t total,
+            int mode, unsigned long long* __restrict__ keys,
+            unsigned long long* __restrict__ ubound) {
   const int lane = threadIdx.x & 31;
   const uint64_t warps = (uint64_t) gridDim.x * (kBatchThreads / 32);
-  const uint64_t nseed = (uint64_t) nprob * ndir;
-  for (uint64_t w = begin + (uint64_t) blockIdx.x * (kBatchThreads / 32) + (threadIdx.x >> 5);
-       w < end; w += warps) {
+  for (uint64_t w = (uint64_t) blockIdx.x * (kBatchThreads / 32) + (threadIdx.x >> 5); w < total;
+       w += warps) {
     uint32_t r;
     int d;
     uint64_t item;
-    decode_item(w, nseed, ndir, rest_prefix, nprob, probs, order, &r, &d, &item);
+    decode_item(w, ndir, rest_prefix, nprob, probs, order, &r, &d, &item);
     const uint32_t p = order[r];
     const hd_problem pr = probs[p];
     const float* X = d == 0 ? A + pr.offset_a * D : B + pr.offset_b * D;
     const float* Y = d == 0 ? B + pr.offset_b * D : A + pr.offset_a * D;
     const uint64_t nx = d == 0 ? pr.n_a : pr.n_b, ny = d == 0 ? pr.n_b : pr.n_a;
-    // The seed item takes 32 rows spread evenly over the set (a sample of the
-    // whole problem: its maximum is a good early threshold); sweep items
-    // 1, 2, ... take rows 32 (item - 1) onward, every row once.
-    uint64_t row;
-    if (item == 0) {
-      if (nx <= 32) {
-        if ((uint64_t) lane >= nx) continue;
-        row = lane;
-      } else {
-        row = ((uint64_t) lane * nx) / 32;
+    const uint64_t row = (item - 1) * 32 + lane;  // warp-uniform item
+    const bool valid = row < nx;
+    const uint64_t w0 = ny > 2 * kWindow + 1 ? (uint64_t) (2 * kWindow + 1) : ny;
+    uint64_t j = valid ? ((row * ny) / nx + ny - (w0 >> 1)) % ny : 0;
+    if (mode == 0) {
+      float u = -1.0f;
+      if (valid) {
+        u = INFINITY;
+        for (uint64_t k = 0; k < w0; ++k) {
+          u = fminf(u, pt_d2<D>(X, row, Y, j));
+          j = (j + 1 == ny) ? 0 : j + 1;
+        }
       }
-    } else {
-      row = (item - 1) * 32 + lane;
-      if (row >= nx) continue;
+      unsigned long long kk = valid ? pack_max(u, (uint32_t) row) : 0ull;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        const unsigned long long v = __shfl_xor_sync(0xFFFFFFFFu, kk, o);
+        kk = v > kk ? v : kk;
+      }
+      if (lane == 0 && kk) atomicMax(ubound + 2 * (uint64_t) p + d, kk);
+      continue;
     }
+    if (!valid) continue;
     unsigned long long* key = keys + 2 * (uint64_t) p + d;
     float thr = threshold_of(ld_relaxed_u64(key));
     float cmin = INFINITY;
-    uint64_t j = (row * ny) / nx;
     bool broke = false;
     for (uint64_t step = 0; step < ny;) {
       const uint64_t chunk = min((uint64_t) kCheckEvery, ny - step);
@@ -146,6 +159,34 @@ __global__ void __launch_bounds__(kBatchThreads)
     }
     if (!broke) atomicMax(key, pack_max(cmin, (uint32_t) row));
   }
+}
+
+// Pass 2: one warp per problem-direction computes the exact nearest-neighbour
+// distance of the row with the largest window bound (lanes split the other
+// set) and starts the running maximum with it.  That row is the most likely
+// maximiser, so the threshold is at or near its final value from the start.
+template <int D>
+__global__ void k_batch_seed(const float* __restrict__ A, const float* __restrict__ B,
+                             const hd_problem* __restrict__ probs, uint32_t nprob, int ndir,
+                             const unsigned long long* __restrict__ ubound,
+                             unsigned long long* __restrict__ keys) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t w = (uint64_t) blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (w >= (uint64_t) nprob * ndir) return;
+  const uint32_t p = (uint32_t) (w / ndir);
+  const int d = (int) (w % ndir);
+  const unsigned long long ub = ubound[2 * (uint64_t) p + d];
+  if (ub == 0) return;
+  const hd_problem pr = probs[p];
+  const float* X = d == 0 ? A + pr.offset_a * D : B + pr.offset_b * D;
+  const float* Y = d == 0 ? B + pr.offset_b * D : A + pr.offset_a * D;
+  const uint64_t ny = d == 0 ? pr.n_b : pr.n_a;
+  const uint32_t row = unpack_max_index(ub);
+  float m = INFINITY;
+  for (uint64_t j = lane; j < ny; j += 32) m = fminf(m, pt_d2<D>(X, row, Y, j));
+#pragma unroll
+  for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+  if (lane == 0) atomicMax(keys + 2 * (uint64_t) p + d, pack_max(m, row));
 }
 
 // Certification per problem-direction: one warp scans the other set for the
@@ -227,7 +268,7 @@ hd_status make_plan(const hd_problem* probs, uint64_t n, int ndir, BatchPlan* pl
     if (ndir == 2) acc += (p.n_b + 31) / 32;
   }
   plan->rest_prefix[n] = acc;
-  plan->total = (uint64_t) n * ndir + acc;
+  plan->total = acc;
   return HD_OK;
 }
 
@@ -264,10 +305,10 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   const size_t b_probs = n * sizeof(hd_problem);
   const size_t b_order = ((n * 4 + 255) / 256) * 256;
   const size_t b_prefix = ((n + 1) * 8 + 255) / 256 * 256;
-  const size_t b_keys = n * 2 * 8;
+  const size_t b_keys = n * 2 * 8;  // also the size of the window-bound words
   const size_t b_pd = n * 2 * sizeof(PD);
   const size_t b_out = ((n * sizeof(hd_batch_result) + 255) / 256) * 256;
-  const size_t total_bytes = b_probs + b_order + b_prefix + b_keys + b_pd + b_out + 256;
+  const size_t total_bytes = b_probs + b_order + b_prefix + 2 * b_keys + b_pd + b_out + 256;
   void* buf;
   if ((s = ensure(c, kBufBatch, total_bytes, &buf)) != HD_OK) return s;
   char* base = (char*) buf;
@@ -275,7 +316,8 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   uint32_t* d_order = (uint32_t*) (base + b_probs);
   uint64_t* d_prefix = (uint64_t*) (base + b_probs + b_order);
   unsigned long long* d_keys = (unsigned long long*) (base + b_probs + b_order + b_prefix);
-  PD* d_pd = (PD*) ((char*) d_keys + b_keys);
+  unsigned long long* d_ub = (unsigned long long*) ((char*) d_keys + b_keys);
+  PD* d_pd = (PD*) ((char*) d_ub + b_keys);
   hd_batch_result* d_out = (hd_batch_result*) ((char*) d_pd + b_pd);
   uint32_t* d_bad = (uint32_t*) ((char*) d_out + b_out);
 
@@ -311,20 +353,27 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   e = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cuda_fail(c, e, "begin capture");
   cudaMemsetAsync(d_keys, 0, b_keys, c.stream);
+  cudaMemsetAsync(d_ub, 0, b_keys, c.stream);
   cudaMemsetAsync(d_bad, 0, 4, c.stream);
-  // Seed items first, as their own launch: every problem has a running
-  // maximum before any of its sweep rows starts.
-  const uint64_t nseed = n * ndir;
-  for (int part = 0; part < 2; ++part) {
-    const uint64_t b = part == 0 ? 0 : nseed, e2 = part == 0 ? nseed : plan.total;
-    if (e2 <= b) continue;
-    const int g = (int) std::max<uint64_t>(1, std::min<uint64_t>((uint64_t) grid, (e2 - b + 7) / 8));
+  const uint64_t pdw = n * ndir;  // problem-directions, one warp each
+  for (int pass = 0; pass < 3; ++pass) {
+    if (pass == 1) {
+      const unsigned sb = (unsigned) ((pdw * 32 + 255) / 256);
+      if (dims == 2)
+        k_batch_seed<2><<<sb, 256, 0, c.stream>>>(dA, dB, d_probs, (uint32_t) n, ndir, d_ub, d_keys);
+      else
+        k_batch_seed<3><<<sb, 256, 0, c.stream>>>(dA, dB, d_probs, (uint32_t) n, ndir, d_ub, d_keys);
+      continue;
+    }
+    const int mode = pass == 0 ? 0 : 1;
     if (dims == 2)
-      k_batch<2><<<g, kBatchThreads, 0, c.stream>>>(dA, dB, d_probs, d_order, d_prefix,
-                                                    (uint32_t) n, ndir, b, e2, d_keys);
+      k_batch<2><<<grid, kBatchThreads, 0, c.stream>>>(dA, dB, d_probs, d_order, d_prefix,
+                                                       (uint32_t) n, ndir, plan.total, mode,
+                                                       d_keys, d_ub);
     else
-      k_batch<3><<<g, kBatchThreads, 0, c.stream>>>(dA, dB, d_probs, d_order, d_prefix,
-                                                    (uint32_t) n, ndir, b, e2, d_keys);
+      k_batch<3><<<grid, kBatchThreads, 0, c.stream>>>(dA, dB, d_probs, d_order, d_prefix,
+                                                       (uint32_t) n, ndir, plan.total, mode,
+                                                       d_keys, d_ub);
   }
   const uint64_t cw = n * ndir;
   const unsigned cblocks = (unsigned) ((cw * 32 + 255) / 256);
@@ -341,7 +390,7 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda_fail(c, e, "instantiate graph");
   e = cudaGraphLaunch(exec, c.stream);
-  c.launches += 4;
+  c.launches += 5;
   if (e != cudaSuccess) {
     cudaGraphExecDestroy(exec);
     return cuda_fail(c, e, "graph launch");
