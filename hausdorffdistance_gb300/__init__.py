@@ -130,13 +130,16 @@ class Engine:
         oa = np.asarray(offsets_a, np.int64)
         ob = np.asarray(offsets_b, np.int64)
         n = len(oa) - 1
-        probs = np.zeros(n, dtype=[("offset_a", "<u8"), ("n_a", "<u8"),
-                                   ("offset_b", "<u8"), ("n_b", "<u8")])
-        probs["offset_a"] = oa[:-1]
-        probs["n_a"] = np.diff(oa)
-        probs["offset_b"] = ob[:-1]
-        probs["n_b"] = np.diff(ob)
-        out = np.zeros(n, dtype=[("hd_f32", "<f4"), ("ia", "<u4"), ("ib", "<u4"),
+        if len(ob) - 1 != n:
+            raise ValueError("offsets_a and offsets_b must describe the same number of problems")
+        # hd_problem rows: offset_a, n_a, offset_b, n_b (uint64; negative
+        # counts wrap to huge values and are rejected by the library).
+        probs = np.empty((n, 4), np.int64)
+        probs[:, 0] = oa[:-1]
+        np.subtract(oa[1:], oa[:-1], out=probs[:, 1])
+        probs[:, 2] = ob[:-1]
+        np.subtract(ob[1:], ob[:-1], out=probs[:, 3])
+        out = np.empty(n, dtype=[("hd_f32", "<f4"), ("ia", "<u4"), ("ib", "<u4"),
                                  ("direction", "<i4")])
         flags = (HD_UNDIRECTED if undirected else 0) | (HD_DEVICE_PTRS if deva else 0)
         fn = self.lib.hd_solve_batch_plain if plain else self.lib.hd_solve_batch

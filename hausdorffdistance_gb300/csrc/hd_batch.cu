@@ -1,35 +1,49 @@
 // Batched Hausdorff distances: many independent 2-D / 3-D problems of uneven
-// sizes in one CUDA-graph launch of a persistent kernel.  No counterpart in
-// the reference, which solves one pair per hd_exec run; the per-problem
-// baseline (hd_solve_batch_plain) runs the plain early-break solve once per
-// problem with its own launches.
+// sizes in one CUDA-graph launch.  No counterpart in the reference, which
+// solves one pair per hd_exec run; the per-problem baseline
+// (hd_solve_batch_plain) runs the plain early-break solve once per problem
+// with its own launches.
 //
 // Work decomposition.  A problem-direction (problem p, A->B or B->A) is cut
 // into items of 32 query rows; one warp processes one item, one lane per
 // row.  Items are ordered largest problem first (longest-processing-time
-// order over |A|*|B|); warps take items in a grid-stride sweep over that
-// order, so there is no queue atomic per item.  Three passes, captured in one
-// graph:
-//   1. window bound: every row takes the minimum over a few points of the
-//      other set around its relative position, an upper bound on its
-//      nearest-neighbour distance; the largest bound per problem-direction
-//      (with its row) is kept;
-//   2. seed: one warp per problem-direction computes the exact nearest
-//      neighbour of that row and starts the running maximum with it;
-//   3. sweep: every row scans with early break against that maximum.
+// order over |A|*|B|, computed on the device by a radix sort inside the
+// graph).  Warps take chunks of consecutive items in grid-stride order and
+// walk from item to item, so the item -> problem lookup is one binary search
+// per chunk.  The graph runs:
+//   plan:   sort keys, radix sort, item counts, exclusive scan;
+//   window: every row takes the minimum over a few points of the other set
+//           around its relative position (row * |Y| / |X|), an upper bound on
+//           its nearest-neighbour distance, stored per row; per
+//           problem-direction the row with the largest bound in each residue
+//           class (row mod 8) is kept;
+//   seed:   the exact nearest-neighbour distances of those 8 rows, computed
+//           over stripes of the other set by all items of the
+//           problem-direction; between them the 8 rows nearly always contain
+//           the maximiser, so the sweep starts at or near the final
+//           threshold;
+//   fold:   the seed minima start each running maximum;
+//   sweep:  a row whose window bound is at or below the running maximum is
+//           settled by that one read; the others scan the other set
+//           circularly on from their window with early break; a row still
+//           open after kShortScan pairs is queued;
+//   long:   one warp per queued row finishes its scan (lanes split the other
+//           set, early break by warp vote);
+//   certify, finalize.
 //
-// Per row: a circular scan of the other set, starting at the row's relative
-// position (row * |Y| / |X|), so that sets stored in a spatially coherent
-// order (polylines, scans) meet their nearest points within a few steps; the
-// row stops as soon as its running minimum is at or below its problem's
-// running maximum, or completes and raises that maximum with one 64-bit
-// atomicMax (distance bits, ~row).  Squared distances use the reference
-// formula, so results are bit-identical to the single-problem solve.
+// A row that completes its scan raises its problem's running maximum with
+// one 64-bit atomicMax (distance bits, ~row).  Squared distances use the
+// reference formula, so results are bit-identical to the single-problem
+// solve.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstring>
 #include <numeric>
 #include <vector>
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include "hd_common.cuh"
 #include "hd_internal.h"
@@ -39,13 +53,30 @@ namespace hdg {
 namespace {
 
 constexpr int kBatchThreads = 256;
-constexpr int kCheckEvery = 8;     // pairs between early-break checks
-constexpr int kRefreshEvery = 64;  // pairs between reloads of the running maximum
+constexpr int kCheckEvery = 8;   // pairs between early-break checks of a row
+constexpr int kShortScan = 64;   // pairs a row scans alone before it is queued
+constexpr int kWindow = 4;       // window half-width of the bound pass
+constexpr int kSlots = 8;        // seed rows per problem-direction (row mod 8)
+constexpr int kChunk = 8;        // consecutive items per warp step
+constexpr int kLongIlp = 8;      // independent loads per lane per long-pass round
+constexpr int kSeedGroup = 8;    // items per seed stripe
+constexpr uint64_t kLongCap = 1ull << 21;  // queued long rows at most
+constexpr uint32_t kNoSeed = 0xFFFFFFFFu;  // empty seed minimum (above every float)
+
+enum Pass : int { kPassWindow = 0, kPassSeed = 1, kPassSweep = 2 };
 
 struct PD {
   float d2;
   uint32_t ia, ib;
   uint32_t valid;
+};
+
+// A row whose short scan did not settle it: problem, direction, row, the
+// circular position its scan reached and its running minimum.
+struct LongRow {
+  uint32_t p, d, row, j;
+  float cmin;
+  uint32_t pad[3];
 };
 
 template <int D>
@@ -60,133 +91,376 @@ __device__ __forceinline__ float pt_d2(const float* __restrict__ X, uint64_t i,
   }
 }
 
-// Decodes a global item index into (sorted problem rank, direction, item);
-// item numbers start at 1.
-__device__ __forceinline__ void decode_item(uint64_t w, int ndir,
-                                            const uint64_t* __restrict__ rest_prefix,
-                                            uint32_t nprob, const hd_problem* __restrict__ probs,
-                                            const uint32_t* __restrict__ order, uint32_t* r_out,
-                                            int* d_out, uint64_t* item_out) {
-  uint32_t lo = 0, hi = nprob;  // rest_prefix[lo] <= w < rest_prefix[hi]
-  while (hi - lo > 1) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if (rest_prefix[mid] <= w)
-      lo = mid;
-    else
-      hi = mid;
+__device__ __forceinline__ uint64_t items_of(uint64_t n) { return (n + 31) / 32; }
+
+// Walks the items in plan order: (sorted problem rank r, direction d, item
+// number within the direction).  init() is one binary search over the item
+// prefix; next() steps to the following item.
+struct Cursor {
+  const hd_problem* probs;
+  const uint32_t* order;
+  uint32_t nprob;
+  int ndir;
+  uint32_t r, p;
+  int d;
+  uint64_t item, nitems;
+  hd_problem pr;
+
+  __device__ void load(uint32_t rank) {
+    r = rank;
+    p = order[rank];
+    pr = probs[p];
   }
-  const uint64_t local = w - rest_prefix[lo];
-  const hd_problem pr = probs[order[lo]];
-  const uint64_t it0 = (pr.n_a + 31) / 32;  // items of direction 0
-  *r_out = lo;
-  if (local < it0 || ndir == 1) {
-    *d_out = 0;
-    *item_out = local + 1;
-  } else {
-    *d_out = 1;
-    *item_out = local - it0 + 1;
+  __device__ void init(uint64_t w, const uint64_t* __restrict__ prefix) {
+    uint32_t lo = 0, hi = nprob;  // prefix[lo] <= w < prefix[hi]
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (prefix[mid] <= w)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    load(lo);
+    const uint64_t local = w - prefix[lo];
+    const uint64_t it0 = items_of(pr.n_a);
+    if (local < it0 || ndir == 1) {
+      d = 0;
+      item = local;
+      nitems = it0;
+    } else {
+      d = 1;
+      item = local - it0;
+      nitems = items_of(pr.n_b);
+    }
+  }
+  __device__ void next() {
+    if (++item < nitems) return;
+    item = 0;
+    if (d == 0 && ndir == 2) {
+      d = 1;
+      nitems = items_of(pr.n_b);
+    } else if (r + 1 < nprob) {
+      load(r + 1);
+      d = 0;
+      nitems = items_of(pr.n_a);
+    }
+  }
+  __device__ uint64_t pd() const { return 2 * (uint64_t) p + d; }
+  __device__ uint64_t nx() const { return d == 0 ? pr.n_a : pr.n_b; }
+  __device__ uint64_t ny() const { return d == 0 ? pr.n_b : pr.n_a; }
+};
+
+struct BatchArgs {
+  const float* A;
+  const float* B;
+  const hd_problem* probs;
+  const uint32_t* order;
+  const uint64_t* prefix;  // item prefix over sorted ranks, nprob + 1 entries
+  uint32_t nprob;
+  int ndir;
+  uint64_t total;                  // items
+  unsigned long long* keys;        // running maximum per problem-direction
+  unsigned long long* ubound;      // window bound per problem-direction and class
+  uint32_t* smin;                  // seed minima (float bits) per problem-direction and class
+  float* wb_a;                     // window bound per row of A (direction A->B)
+  float* wb_b;                     // window bound per row of B (direction B->A)
+  LongRow* longq;
+  unsigned long long* long_count;
+  uint64_t long_cap;
+};
+
+// First position of a row's circular scan: the start of the window of w0
+// points centred on the row's relative position row * |Y| / |X| (computed in
+// float: the position is only a starting point, any value in [0, ny) is
+// correct).
+__device__ __forceinline__ uint32_t scan_start(uint32_t row, float ratio, uint32_t ny,
+                                               uint32_t half) {
+  uint32_t c = (uint32_t) ((float) row * ratio);
+  c = c < ny ? c : ny - 1;
+  return c >= half ? c - half : c + (ny - half);
+}
+
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  return v;
+}
+
+// Window pass, one item: each row's minimum over 2*kWindow+1 points of the
+// other set centred on its relative position, stored per row; the largest
+// bound (with its row) of each residue class goes to
+// ubound[problem-direction][class].
+template <int D>
+__device__ __forceinline__ void window_item(const BatchArgs& a, const Cursor& cu, int lane,
+                                            const float* X, const float* Y, uint32_t nx,
+                                            uint32_t ny) {
+  const uint32_t row = (uint32_t) cu.item * 32 + lane;
+  const bool valid = row < nx;
+  const uint32_t w0 = ny > 2 * kWindow + 1 ? (uint32_t) (2 * kWindow + 1) : ny;
+  float u = -1.0f;
+  if (valid) {
+    uint32_t j = scan_start(row, (float) ny / (float) nx, ny, w0 >> 1);
+    u = INFINITY;
+    for (uint32_t k = 0; k < w0; ++k) {
+      u = fminf(u, pt_d2<D>(X, row, Y, j));
+      j = (j + 1 == ny) ? 0 : j + 1;
+    }
+  }
+  if (valid) (cu.d == 0 ? a.wb_a + cu.pr.offset_a : a.wb_b + cu.pr.offset_b)[row] = u;
+  // Row r's class is r % kSlots = lane % kSlots (items start at multiples of
+  // 32): reduce over the lanes of a class, one atomicMax per class.
+  unsigned long long kk = valid ? pack_max(u, row) : 0ull;
+#pragma unroll
+  for (int o = 16; o >= kSlots; o >>= 1) {
+    const unsigned long long v = __shfl_xor_sync(0xFFFFFFFFu, kk, o);
+    kk = v > kk ? v : kk;
+  }
+  if (lane < kSlots && kk) atomicMax(a.ubound + cu.pd() * kSlots + lane, kk);
+}
+
+// Seed pass: the items of a problem-direction form groups of kSeedGroup;
+// the first item of group g of NG covers stripe [g*|Y|/NG, (g+1)*|Y|/NG) of
+// the other set and lowers the seed rows' minima over that stripe.  The
+// stripes partition the other set, so after the pass smin holds each seed
+// row's exact nearest-neighbour distance.
+template <int D>
+__device__ __forceinline__ void seed_item(const BatchArgs& a, const Cursor& cu, int lane,
+                                          const float* X, const float* Y, uint32_t nx,
+                                          uint32_t ny) {
+  if (cu.item % kSeedGroup) return;
+  const uint64_t NG = (items_of(nx) + kSeedGroup - 1) / kSeedGroup;
+  const uint64_t g = cu.item / kSeedGroup;
+  const uint32_t lo = (uint32_t) (g * ny / NG), hi = (uint32_t) ((g + 1) * ny / NG);
+  if (lo >= hi) return;
+  const unsigned long long* ub = a.ubound + cu.pd() * kSlots;
+  float x[kSlots][D];
+  bool has[kSlots];
+  float m[kSlots];
+#pragma unroll
+  for (int k = 0; k < kSlots; ++k) {
+    const unsigned long long u = ub[k];
+    has[k] = u != 0;
+    const uint64_t r = has[k] ? unpack_max_index(u) : 0;  // an empty class repeats row 0
+#pragma unroll
+    for (int t = 0; t < D; ++t) x[k][t] = X[r * D + t];
+    m[k] = INFINITY;
+  }
+  for (uint32_t j = lo + lane; j < hi; j += 32) {
+    float y[D];
+#pragma unroll
+    for (int t = 0; t < D; ++t) y[t] = Y[j * D + t];
+#pragma unroll
+    for (int k = 0; k < kSlots; ++k) {
+      if constexpr (D == 2)
+        m[k] = fminf(m[k], d2_2(x[k][0], x[k][1], y[0], y[1]));
+      else
+        m[k] = fminf(m[k], d2_3(x[k][0], x[k][1], x[k][2], y[0], y[1], y[2]));
+    }
+  }
+  uint32_t* sm = a.smin + cu.pd() * kSlots;
+#pragma unroll
+  for (int k = 0; k < kSlots; ++k) {
+    const float v = warp_min(m[k]);
+    if (lane == k && has[k]) {
+      const uint32_t bits = __float_as_uint(v);
+      if (bits < *(volatile uint32_t*) (sm + k)) atomicMin(sm + k, bits);
+    }
   }
 }
 
-constexpr int kWindow = 4;  // window half-width of the bound pass
+// Fold: one thread per problem-direction starts the running maximum with the
+// seed rows' exact minima.
+__global__ void k_batch_fold(const unsigned long long* __restrict__ ubound,
+                             const uint32_t* __restrict__ smin, uint64_t npd,
+                             unsigned long long* __restrict__ keys) {
+  const uint64_t t = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npd) return;
+  unsigned long long best = 0;
+  for (int k = 0; k < kSlots; ++k) {
+    const uint32_t bits = smin[t * kSlots + k];
+    if (bits == kNoSeed) continue;
+    const unsigned long long kk =
+        pack_max(__uint_as_float(bits), unpack_max_index(ubound[t * kSlots + k]));
+    best = kk > best ? kk : best;
+  }
+  keys[t] = best;
+}
 
-// Pass 1 (mode 0) and pass 3 (mode 1) over items of 32 rows.
-//   mode 0: each row takes the minimum over a window of 2*kWindow+1 points
-//           of the other set around its relative position, an upper bound on
-//           its nearest-neighbour distance; the warp's largest bound (with its
-//           row) goes to ubound[problem-direction] by one atomicMax.
-//   mode 1: each row scans the other set circularly from the start of that
-//           window with early break against the running maximum.
+// Sweep pass, one item: a row whose window bound is at or below the running
+// maximum is settled without a pair; the others continue their circular scan
+// after the window, up to kShortScan pairs in all; rows still open are queued
+// for the long pass (or, with the queue full, finish alone).
 template <int D>
-__global__ void __launch_bounds__(kBatchThreads)
-    k_batch(const float* __restrict__ A, const float* __restrict__ B,
-            const hd_problem* __restrict__ probs, const uint32_t* __restrict__ order,
-            const uint64_t* __restrict__ rest_prefix, uint32_t nprob, int ndir, uint64_t total,
-            int mode, unsigned long long* __restrict__ keys,
-            unsigned long long* __restrict__ ubound) {
+__device__ __forceinline__ void sweep_item(const BatchArgs& a, const Cursor& cu, int lane,
+                                           const float* X, const float* Y, uint32_t nx,
+                                           uint32_t ny) {
+  unsigned long long* key = a.keys + cu.pd();
+  float thr = threshold_of(ld_relaxed_u64(key));
+  const uint32_t row = (uint32_t) cu.item * 32 + lane;
+  const bool valid = row < nx;
+  float cmin = valid ? (cu.d == 0 ? a.wb_a + cu.pr.offset_a : a.wb_b + cu.pr.offset_b)[row]
+                     : 0.0f;
+  bool broke = !valid || cmin <= thr;
+  if (__all_sync(0xFFFFFFFFu, broke)) return;
+  const uint32_t w0 = ny > 2 * kWindow + 1 ? (uint32_t) (2 * kWindow + 1) : ny;
+  uint32_t j = 0;
+  if (!broke) {
+    j = scan_start(row, (float) ny / (float) nx, ny, w0 >> 1) + w0;
+    if (j >= ny) j -= ny;
+  }
+  uint32_t step = w0;
+  const uint32_t limit = ny < (uint32_t) kShortScan ? ny : (uint32_t) kShortScan;
+  while (!broke && step < limit) {
+    const uint32_t chunk = min((uint32_t) kCheckEvery, limit - step);
+    for (uint32_t u = 0; u < chunk; ++u) {
+      cmin = fminf(cmin, pt_d2<D>(X, row, Y, j));
+      j = (j + 1 == ny) ? 0 : j + 1;
+    }
+    step += chunk;
+    broke = cmin <= thr;
+  }
+  if (!broke && step < ny) broke = cmin <= threshold_of(ld_relaxed_u64(key));
+  const bool pending = !broke && step < ny;
+  if (!broke && !pending) atomicMax(key, pack_max(cmin, row));
+  const unsigned ballot = __ballot_sync(0xFFFFFFFFu, pending);
+  if (!ballot) return;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(a.long_count, (unsigned long long) __popc(ballot));
+  base = __shfl_sync(0xFFFFFFFFu, base, 0);
+  if (!pending) return;
+  const unsigned long long slot = base + __popc(ballot & ((1u << lane) - 1u));
+  if (slot < a.long_cap) {
+    a.longq[slot] = LongRow{cu.p, (uint32_t) cu.d, row, j, cmin, {0, 0, 0}};
+    return;
+  }
+  // Queue full: this lane finishes the row itself.
+  thr = threshold_of(ld_relaxed_u64(key));
+  while (step < ny) {
+    const uint32_t chunk = min((uint32_t) kCheckEvery, ny - step);
+    for (uint32_t u = 0; u < chunk; ++u) {
+      cmin = fminf(cmin, pt_d2<D>(X, row, Y, j));
+      j = (j + 1 == ny) ? 0 : j + 1;
+    }
+    step += chunk;
+    if (cmin <= thr) return;
+    if ((step % 64) == 0) thr = threshold_of(ld_relaxed_u64(key));
+  }
+  atomicMax(key, pack_max(cmin, row));
+}
+
+template <int D, int PASS>
+__global__ void __launch_bounds__(kBatchThreads, 4) k_batch_pass(BatchArgs a) {
   const int lane = threadIdx.x & 31;
-  const uint64_t warps = (uint64_t) gridDim.x * (kBatchThreads / 32);
-  for (uint64_t w = (uint64_t) blockIdx.x * (kBatchThreads / 32) + (threadIdx.x >> 5); w < total;
-       w += warps) {
-    uint32_t r;
-    int d;
-    uint64_t item;
-    decode_item(w, ndir, rest_prefix, nprob, probs, order, &r, &d, &item);
-    const uint32_t p = order[r];
-    const hd_problem pr = probs[p];
-    const float* X = d == 0 ? A + pr.offset_a * D : B + pr.offset_b * D;
-    const float* Y = d == 0 ? B + pr.offset_b * D : A + pr.offset_a * D;
-    const uint64_t nx = d == 0 ? pr.n_a : pr.n_b, ny = d == 0 ? pr.n_b : pr.n_a;
-    const uint64_t row = (item - 1) * 32 + lane;  // warp-uniform item
-    const bool valid = row < nx;
-    const uint64_t w0 = ny > 2 * kWindow + 1 ? (uint64_t) (2 * kWindow + 1) : ny;
-    uint64_t j = valid ? ((row * ny) / nx + ny - (w0 >> 1)) % ny : 0;
-    if (mode == 0) {
-      float u = -1.0f;
-      if (valid) {
-        u = INFINITY;
-        for (uint64_t k = 0; k < w0; ++k) {
-          u = fminf(u, pt_d2<D>(X, row, Y, j));
-          j = (j + 1 == ny) ? 0 : j + 1;
+  Cursor cu;
+  cu.probs = a.probs;
+  cu.order = a.order;
+  cu.nprob = a.nprob;
+  cu.ndir = a.ndir;
+  const uint64_t nw = (uint64_t) gridDim.x * (kBatchThreads / 32);
+  for (uint64_t chunk = (uint64_t) blockIdx.x * (kBatchThreads / 32) + (threadIdx.x >> 5);
+       chunk * kChunk < a.total; chunk += nw) {
+    const uint64_t base = chunk * kChunk;
+    const uint64_t end = min(base + kChunk, a.total);
+    cu.init(base, a.prefix);
+    for (uint64_t w = base; w < end; ++w, cu.next()) {
+      const float* X = cu.d == 0 ? a.A + cu.pr.offset_a * D : a.B + cu.pr.offset_b * D;
+      const float* Y = cu.d == 0 ? a.B + cu.pr.offset_b * D : a.A + cu.pr.offset_a * D;
+      const uint32_t nx = (uint32_t) cu.nx(), ny = (uint32_t) cu.ny();
+      if constexpr (PASS == kPassWindow)
+        window_item<D>(a, cu, lane, X, Y, nx, ny);
+      else if constexpr (PASS == kPassSeed)
+        seed_item<D>(a, cu, lane, X, Y, nx, ny);
+      else
+        sweep_item<D>(a, cu, lane, X, Y, nx, ny);
+    }
+  }
+}
+
+// Long pass: one warp per queued row finishes its circular scan from the
+// position the short scan reached, lanes splitting the remaining points,
+// with a warp-wide early-break vote every 4 rounds.
+template <int D>
+__global__ void __launch_bounds__(kBatchThreads) k_batch_long(BatchArgs a) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t nw = (uint64_t) gridDim.x * (kBatchThreads / 32);
+  const uint64_t cnt = min((uint64_t) *(volatile unsigned long long*) a.long_count, a.long_cap);
+  for (uint64_t e = (uint64_t) blockIdx.x * (kBatchThreads / 32) + (threadIdx.x >> 5); e < cnt;
+       e += nw) {
+    const LongRow L = a.longq[e];
+    const hd_problem pr = a.probs[L.p];
+    const float* X = L.d == 0 ? a.A + pr.offset_a * D : a.B + pr.offset_b * D;
+    const float* Y = L.d == 0 ? a.B + pr.offset_b * D : a.A + pr.offset_a * D;
+    const uint64_t ny = L.d == 0 ? pr.n_b : pr.n_a;
+    unsigned long long* key = a.keys + 2 * (uint64_t) L.p + L.d;
+    float thr = threshold_of(ld_relaxed_u64(key));
+    float cmin = lane == 0 ? L.cmin : INFINITY;
+    const uint64_t rem = ny - kShortScan;
+    float x[D];
+#pragma unroll
+    for (int t = 0; t < D; ++t) x[t] = X[(uint64_t) L.row * D + t];
+    // Rounds of kLongIlp independent loads per lane (32 * kLongIlp pairs per
+    // warp), then one warp-wide early-break vote.
+    bool broke = false;
+    int round = 0;
+    for (uint64_t t0 = 0; t0 < rem; t0 += 32 * kLongIlp) {
+      float y[kLongIlp][D];
+#pragma unroll
+      for (int u = 0; u < kLongIlp; ++u) {
+        const uint64_t t = t0 + (uint64_t) u * 32 + lane;
+        uint64_t jj = L.j + t;  // L.j < ny and t < ny: one subtraction wraps
+        if (jj >= ny) jj -= ny;
+        if (t < rem) {
+#pragma unroll
+          for (int k = 0; k < D; ++k) y[u][k] = Y[jj * D + k];
+        } else {
+#pragma unroll
+          for (int k = 0; k < D; ++k) y[u][k] = INFINITY;
         }
       }
-      unsigned long long kk = valid ? pack_max(u, (uint32_t) row) : 0ull;
 #pragma unroll
-      for (int o = 16; o; o >>= 1) {
-        const unsigned long long v = __shfl_xor_sync(0xFFFFFFFFu, kk, o);
-        kk = v > kk ? v : kk;
+      for (int u = 0; u < kLongIlp; ++u) {
+        const uint64_t t = t0 + (uint64_t) u * 32 + lane;
+        float d2;
+        if constexpr (D == 2)
+          d2 = d2_2(x[0], x[1], y[u][0], y[u][1]);
+        else
+          d2 = d2_3(x[0], x[1], x[2], y[u][0], y[u][1], y[u][2]);
+        if (t < rem) cmin = fminf(cmin, d2);
       }
-      if (lane == 0 && kk) atomicMax(ubound + 2 * (uint64_t) p + d, kk);
-      continue;
-    }
-    if (!valid) continue;
-    unsigned long long* key = keys + 2 * (uint64_t) p + d;
-    float thr = threshold_of(ld_relaxed_u64(key));
-    float cmin = INFINITY;
-    bool broke = false;
-    for (uint64_t step = 0; step < ny;) {
-      const uint64_t chunk = min((uint64_t) kCheckEvery, ny - step);
-      for (uint64_t u = 0; u < chunk; ++u) {
-        cmin = fminf(cmin, pt_d2<D>(X, row, Y, j));
-        j = (j + 1 == ny) ? 0 : j + 1;
-      }
-      step += chunk;
-      if (cmin <= thr) {
+      if (warp_min(cmin) <= thr) {
         broke = true;
         break;
       }
-      if ((step % kRefreshEvery) == 0) thr = threshold_of(ld_relaxed_u64(key));
+      if ((++round & 7) == 0) thr = threshold_of(ld_relaxed_u64(key));
     }
-    if (!broke) atomicMax(key, pack_max(cmin, (uint32_t) row));
+    if (broke) continue;
+    const float m = warp_min(cmin);
+    if (lane == 0 && m > threshold_of(ld_relaxed_u64(key))) atomicMax(key, pack_max(m, L.row));
   }
 }
 
-// Pass 2: one warp per problem-direction computes the exact nearest-neighbour
-// distance of the row with the largest window bound (lanes split the other
-// set) and starts the running maximum with it.  That row is the most likely
-// maximiser, so the threshold is at or near its final value from the start.
-template <int D>
-__global__ void k_batch_seed(const float* __restrict__ A, const float* __restrict__ B,
-                             const hd_problem* __restrict__ probs, uint32_t nprob, int ndir,
-                             const unsigned long long* __restrict__ ubound,
-                             unsigned long long* __restrict__ keys) {
-  const int lane = threadIdx.x & 31;
-  const uint64_t w = (uint64_t) blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-  if (w >= (uint64_t) nprob * ndir) return;
-  const uint32_t p = (uint32_t) (w / ndir);
-  const int d = (int) (w % ndir);
-  const unsigned long long ub = ubound[2 * (uint64_t) p + d];
-  if (ub == 0) return;
-  const hd_problem pr = probs[p];
-  const float* X = d == 0 ? A + pr.offset_a * D : B + pr.offset_b * D;
-  const float* Y = d == 0 ? B + pr.offset_b * D : A + pr.offset_a * D;
-  const uint64_t ny = d == 0 ? pr.n_b : pr.n_a;
-  const uint32_t row = unpack_max_index(ub);
-  float m = INFINITY;
-  for (uint64_t j = lane; j < ny; j += 32) m = fminf(m, pt_d2<D>(X, row, Y, j));
-#pragma unroll
-  for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
-  if (lane == 0) atomicMax(keys + 2 * (uint64_t) p + d, pack_max(m, row));
+// Plan: sort keys (largest |A|*|B| first, stable by problem index) and the
+// item count of each sorted rank (entry nprob is 0, so that an exclusive scan
+// over nprob + 1 entries gives the item prefix with the total at the end).
+__global__ void k_plan_keys(const hd_problem* __restrict__ probs, uint32_t n, uint64_t maxpairs,
+                            unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  keys[i] = maxpairs - probs[i].n_a * probs[i].n_b;
+  vals[i] = i;
+}
+
+__global__ void k_plan_counts(const hd_problem* __restrict__ probs,
+                              const uint32_t* __restrict__ order, uint32_t n, int ndir,
+                              uint64_t* __restrict__ cnt) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r > n) return;
+  if (r == n) {
+    cnt[n] = 0;
+    return;
+  }
+  const hd_problem pr = probs[order[r]];
+  cnt[r] = items_of(pr.n_a) + (ndir == 2 ? items_of(pr.n_b) : 0);
 }
 
 // Certification per problem-direction: one warp scans the other set for the
@@ -246,42 +520,95 @@ __global__ void k_batch_finalize(const PD* __restrict__ pd, uint32_t nprob, int 
   out[p] = hd_batch_result{__fsqrt_rn(w.d2), w.ia, w.ib, win};
 }
 
-struct BatchPlan {
-  std::vector<uint32_t> order;
-  std::vector<uint64_t> rest_prefix;
-  uint64_t total = 0;
-};
-
-hd_status make_plan(const hd_problem* probs, uint64_t n, int ndir, BatchPlan* plan) {
-  plan->order.resize(n);
-  std::iota(plan->order.begin(), plan->order.end(), 0u);
-  std::stable_sort(plan->order.begin(), plan->order.end(), [&](uint32_t x, uint32_t y) {
-    return (double) probs[x].n_a * (double) probs[x].n_b >
-           (double) probs[y].n_a * (double) probs[y].n_b;
-  });
-  plan->rest_prefix.resize(n + 1);
-  uint64_t acc = 0;
-  for (uint64_t r = 0; r < n; ++r) {
-    plan->rest_prefix[r] = acc;
-    const hd_problem& p = probs[plan->order[r]];
-    acc += (p.n_a + 31) / 32;
-    if (ndir == 2) acc += (p.n_b + 31) / 32;
-  }
-  plan->rest_prefix[n] = acc;
-  plan->total = acc;
-  return HD_OK;
-}
-
 hd_status check_problems(Ctx& c, const hd_problem* probs, uint64_t n, uint64_t ta, uint64_t tb) {
   for (uint64_t i = 0; i < n; ++i) {
     const hd_problem& p = probs[i];
     if (p.n_a == 0 || p.n_b == 0)
       return fail(c, HD_ERR_INVALID_ARG, "problem " + std::to_string(i) + " has an empty set");
-    if (p.offset_a + p.n_a > ta || p.offset_b + p.n_b > tb)
+    if (p.offset_a > ta || p.n_a > ta - p.offset_a || p.offset_b > tb || p.n_b > tb - p.offset_b)
       return fail(c, HD_ERR_INVALID_ARG, "problem " + std::to_string(i) + " is out of range");
     if (p.n_a >= 0xFFFFFFFFull || p.n_b >= 0xFFFFFFFFull)
       return fail(c, HD_ERR_INVALID_ARG, "problem sets are limited to 2^32-2 points");
   }
+  return HD_OK;
+}
+
+
+// Bump allocator over one device buffer, 256-byte aligned pieces.
+struct Layout {
+  size_t off = 0;
+  size_t take(size_t bytes) {
+    const size_t o = off;
+    off += (bytes + 255) / 256 * 256;
+    return o;
+  }
+};
+
+// Everything one batched-solve graph is captured from.
+struct BatchGraph {
+  BatchArgs args;
+  int dims, ndir, end_bit;
+  uint64_t n, maxpairs;
+  char* base;             // the batch buffer; reset region starts here
+  size_t zero_bytes;      // keys and window bounds per class (reset to 0)
+  unsigned long long* ctr;    // long-row count, certification mismatch count
+  size_t o_smin, smin_bytes;  // seed minima (reset to 0xFF bytes)
+  size_t o_pkeys, o_pkeys2, o_pvals, o_cnt, o_tmp, cub_tmp;
+  PD* pd;
+  hd_batch_result* out;
+  uint32_t* bad;
+  const void* fns[4];     // window, seed, sweep, long
+  int grids[4];
+};
+
+hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
+  auto at = [&](size_t o) { return (void*) (g.base + o); };
+  const BatchArgs& a = g.args;
+  const uint32_t n = (uint32_t) g.n;
+  const unsigned pblocks = (unsigned) ((g.n + 1 + 255) / 256);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_fail(c, e, "begin capture");
+  cudaMemsetAsync(g.base, 0, g.zero_bytes, c.stream);
+  cudaMemsetAsync(at(g.o_smin), 0xFF, g.smin_bytes, c.stream);
+  cudaMemsetAsync(g.ctr, 0, 2 * 8, c.stream);
+  k_plan_keys<<<pblocks, 256, 0, c.stream>>>(a.probs, n, g.maxpairs,
+                                            (unsigned long long*) at(g.o_pkeys),
+                                            (uint32_t*) at(g.o_pvals));
+  size_t tb = g.cub_tmp;
+  cub::DeviceRadixSort::SortPairs(at(g.o_tmp), tb, (const unsigned long long*) at(g.o_pkeys),
+                                  (unsigned long long*) at(g.o_pkeys2),
+                                  (const uint32_t*) at(g.o_pvals), const_cast<uint32_t*>(a.order),
+                                  (int64_t) n, 0, g.end_bit, c.stream);
+  k_plan_counts<<<pblocks, 256, 0, c.stream>>>(a.probs, a.order, n, g.ndir,
+                                              (uint64_t*) at(g.o_cnt));
+  tb = g.cub_tmp;
+  cub::DeviceScan::ExclusiveSum(at(g.o_tmp), tb, (const uint64_t*) at(g.o_cnt),
+                                const_cast<uint64_t*>(a.prefix), (int64_t) (g.n + 1), c.stream);
+  BatchArgs kernel_args = a;
+  void* kargs[] = {&kernel_args};
+  const uint64_t npd = g.n * g.ndir;
+  for (int k = 0; k < 4; ++k) {
+    if (k == 2)  // between seed and sweep
+      k_batch_fold<<<(unsigned) ((npd + 255) / 256), 256, 0, c.stream>>>(a.ubound, a.smin, npd,
+                                                                         a.keys);
+    cudaLaunchKernel(g.fns[k], dim3(g.grids[k]), dim3(kBatchThreads), kargs, 0, c.stream);
+  }
+  const unsigned cblocks = (unsigned) ((g.n * g.ndir * 32 + 255) / 256);
+  if (g.dims == 2)
+    k_batch_certify<2><<<cblocks, 256, 0, c.stream>>>(a.A, a.B, a.probs, n, g.ndir, a.keys, g.pd);
+  else
+    k_batch_certify<3><<<cblocks, 256, 0, c.stream>>>(a.A, a.B, a.probs, n, g.ndir, a.keys, g.pd);
+  k_batch_finalize<<<(unsigned) ((g.n + 255) / 256), 256, 0, c.stream>>>(g.pd, n, g.ndir, g.out,
+                                                                          g.bad);
+  e = cudaStreamEndCapture(c.stream, &graph);
+  if (e != cudaSuccess) return cuda_fail(c, e, "end capture");
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(c, e, "instantiate graph");
+  if (c.batch_graph) cudaGraphExecDestroy(c.batch_graph);
+  c.batch_graph = exec;
   return HD_OK;
 }
 
@@ -297,29 +624,62 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   hd_status s;
   if ((s = check_problems(c, probs, n, total_a, total_b)) != HD_OK) return s;
   const int ndir = (flags & HD_UNDIRECTED) ? 2 : 1;
-  BatchPlan plan;
-  make_plan(probs, n, ndir, &plan);
+  uint64_t total = 0, rows = 0, maxpairs = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    const hd_problem& p = probs[i];
+    total += (p.n_a + 31) / 32 + (ndir == 2 ? (p.n_b + 31) / 32 : 0);
+    rows += p.n_a + (ndir == 2 ? p.n_b : 0);
+    maxpairs = std::max<uint64_t>(maxpairs, p.n_a * p.n_b);
+  }
+  BatchGraph g{};
+  g.dims = dims;
+  g.ndir = ndir;
+  g.n = n;
+  g.maxpairs = maxpairs;
+  g.end_bit = 1;
+  while (g.end_bit < 64 && (maxpairs >> g.end_bit)) ++g.end_bit;
+  const uint64_t long_cap = std::min<uint64_t>(rows, kLongCap);
 
-  // Device layout in one buffer: problems | order | rest prefix | keys | PD |
-  // results | bad counter.
-  const size_t b_probs = n * sizeof(hd_problem);
-  const size_t b_order = ((n * 4 + 255) / 256) * 256;
-  const size_t b_prefix = ((n + 1) * 8 + 255) / 256 * 256;
-  const size_t b_keys = n * 2 * 8;  // also the size of the window-bound words
-  const size_t b_pd = n * 2 * sizeof(PD);
-  const size_t b_out = ((n * sizeof(hd_batch_result) + 255) / 256) * 256;
-  const size_t total_bytes = b_probs + b_order + b_prefix + 2 * b_keys + b_pd + b_out + 256;
+  // CUB temporary storage for the plan's sort and scan.
+  size_t sort_tmp = 0, scan_tmp = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, sort_tmp, (const unsigned long long*) nullptr,
+                                  (unsigned long long*) nullptr, (const uint32_t*) nullptr,
+                                  (uint32_t*) nullptr, (int64_t) n, 0, g.end_bit, c.stream);
+  cub::DeviceScan::ExclusiveSum(nullptr, scan_tmp, (const uint64_t*) nullptr, (uint64_t*) nullptr,
+                                (int64_t) (n + 1), c.stream);
+  g.cub_tmp = std::max(sort_tmp, scan_tmp);
+
+  // Device layout in one buffer; the words reset inside the graph come
+  // first: keys and window bounds (zero), seed minima (0xFF bytes).
+  Layout L;
+  const size_t o_keys = L.take(n * 2 * 8);
+  const size_t o_ub = L.take(n * 2 * kSlots * 8);
+  g.zero_bytes = L.off;
+  g.o_smin = L.take(n * 2 * kSlots * 4);
+  g.smin_bytes = L.off - g.o_smin;
+  const size_t o_ctr = L.take(2 * 8);  // long-row count, mismatch count
+  const size_t o_wb_a = L.take(total_a * 4);
+  const size_t o_wb_b = L.take(ndir == 2 ? total_b * 4 : 0);
+  const size_t o_probs = L.take(n * sizeof(hd_problem));
+  g.o_pkeys = L.take(n * 8);
+  g.o_pkeys2 = L.take(n * 8);
+  g.o_pvals = L.take(n * 4);
+  const size_t o_order = L.take(n * 4);
+  g.o_cnt = L.take((n + 1) * 8);
+  const size_t o_prefix = L.take((n + 1) * 8);
+  const size_t o_pd = L.take(n * 2 * sizeof(PD));
+  const size_t o_out = L.take(n * sizeof(hd_batch_result));
+  g.o_tmp = L.take(g.cub_tmp);
+  const size_t o_long = L.take(long_cap * sizeof(LongRow));
   void* buf;
-  if ((s = ensure(c, kBufBatch, total_bytes, &buf)) != HD_OK) return s;
-  char* base = (char*) buf;
-  hd_problem* d_probs = (hd_problem*) base;
-  uint32_t* d_order = (uint32_t*) (base + b_probs);
-  uint64_t* d_prefix = (uint64_t*) (base + b_probs + b_order);
-  unsigned long long* d_keys = (unsigned long long*) (base + b_probs + b_order + b_prefix);
-  unsigned long long* d_ub = (unsigned long long*) ((char*) d_keys + b_keys);
-  PD* d_pd = (PD*) ((char*) d_ub + b_keys);
-  hd_batch_result* d_out = (hd_batch_result*) ((char*) d_pd + b_pd);
-  uint32_t* d_bad = (uint32_t*) ((char*) d_out + b_out);
+  if ((s = ensure(c, kBufBatch, L.off, &buf)) != HD_OK) return s;
+  g.base = (char*) buf;
+  auto at = [&](size_t o) { return (void*) (g.base + o); };
+  unsigned long long* d_ctr = (unsigned long long*) at(o_ctr);
+  g.pd = (PD*) at(o_pd);
+  g.out = (hd_batch_result*) at(o_out);
+  g.ctr = d_ctr;
+  g.bad = (uint32_t*) (d_ctr + 1);
 
   const float* dA = A;
   const float* dB = B;
@@ -335,75 +695,72 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
     dA = (const float*) pa;
     dB = (const float*) pb;
   }
-  if ((e = cudaMemcpyAsync(d_probs, probs, b_probs, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess ||
-      (e = cudaMemcpyAsync(d_order, plan.order.data(), n * 4, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess ||
-      (e = cudaMemcpyAsync(d_prefix, plan.rest_prefix.data(), (n + 1) * 8, cudaMemcpyHostToDevice,
+  if ((e = cudaMemcpyAsync(at(o_probs), probs, n * sizeof(hd_problem), cudaMemcpyHostToDevice,
                            c.stream)) != cudaSuccess)
-    return cuda_fail(c, e, "copy batch plan");
+    return cuda_fail(c, e, "copy problems");
 
-  // One graph: reset, persistent solve, certification, finalisation.
-  int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dims == 2 ? k_batch<2> : k_batch<3>,
-                                                kBatchThreads, 0);
-  occ = std::max(occ, 1);
-  const uint64_t warps_needed = plan.total;
-  const int grid = (int) std::max<uint64_t>(
-      1, std::min<uint64_t>((uint64_t) c.num_sms * occ, (warps_needed + 7) / 8));
-  cudaGraph_t graph = nullptr;
-  e = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess) return cuda_fail(c, e, "begin capture");
-  cudaMemsetAsync(d_keys, 0, b_keys, c.stream);
-  cudaMemsetAsync(d_ub, 0, b_keys, c.stream);
-  cudaMemsetAsync(d_bad, 0, 4, c.stream);
-  const uint64_t pdw = n * ndir;  // problem-directions, one warp each
-  for (int pass = 0; pass < 3; ++pass) {
-    if (pass == 1) {
-      const unsigned sb = (unsigned) ((pdw * 32 + 255) / 256);
-      if (dims == 2)
-        k_batch_seed<2><<<sb, 256, 0, c.stream>>>(dA, dB, d_probs, (uint32_t) n, ndir, d_ub, d_keys);
-      else
-        k_batch_seed<3><<<sb, 256, 0, c.stream>>>(dA, dB, d_probs, (uint32_t) n, ndir, d_ub, d_keys);
-      continue;
-    }
-    const int mode = pass == 0 ? 0 : 1;
-    if (dims == 2)
-      k_batch<2><<<grid, kBatchThreads, 0, c.stream>>>(dA, dB, d_probs, d_order, d_prefix,
-                                                       (uint32_t) n, ndir, plan.total, mode,
-                                                       d_keys, d_ub);
-    else
-      k_batch<3><<<grid, kBatchThreads, 0, c.stream>>>(dA, dB, d_probs, d_order, d_prefix,
-                                                       (uint32_t) n, ndir, plan.total, mode,
-                                                       d_keys, d_ub);
+  BatchArgs& args = g.args;
+  args.A = dA;
+  args.B = dB;
+  args.probs = (const hd_problem*) at(o_probs);
+  args.order = (const uint32_t*) at(o_order);
+  args.prefix = (const uint64_t*) at(o_prefix);
+  args.nprob = (uint32_t) n;
+  args.ndir = ndir;
+  args.total = total;
+  args.keys = (unsigned long long*) at(o_keys);
+  args.ubound = (unsigned long long*) at(o_ub);
+  args.smin = (uint32_t*) at(g.o_smin);
+  args.wb_a = (float*) at(o_wb_a);
+  args.wb_b = (float*) at(o_wb_b);
+  args.longq = (LongRow*) at(o_long);
+  args.long_count = d_ctr;
+  args.long_cap = long_cap;
+
+  // Persistent grids: resident blocks of each kernel, at most one warp per
+  // chunk of items (or per queued row).
+  if (dims == 2) {
+    g.fns[0] = (const void*) k_batch_pass<2, kPassWindow>;
+    g.fns[1] = (const void*) k_batch_pass<2, kPassSeed>;
+    g.fns[2] = (const void*) k_batch_pass<2, kPassSweep>;
+    g.fns[3] = (const void*) k_batch_long<2>;
+  } else {
+    g.fns[0] = (const void*) k_batch_pass<3, kPassWindow>;
+    g.fns[1] = (const void*) k_batch_pass<3, kPassSeed>;
+    g.fns[2] = (const void*) k_batch_pass<3, kPassSweep>;
+    g.fns[3] = (const void*) k_batch_long<3>;
   }
-  const uint64_t cw = n * ndir;
-  const unsigned cblocks = (unsigned) ((cw * 32 + 255) / 256);
-  if (dims == 2)
-    k_batch_certify<2><<<cblocks, 256, 0, c.stream>>>(dA, dB, d_probs, (uint32_t) n, ndir, d_keys, d_pd);
-  else
-    k_batch_certify<3><<<cblocks, 256, 0, c.stream>>>(dA, dB, d_probs, (uint32_t) n, ndir, d_keys, d_pd);
-  k_batch_finalize<<<(unsigned) ((n + 255) / 256), 256, 0, c.stream>>>(d_pd, (uint32_t) n, ndir,
-                                                                        d_out, d_bad);
-  e = cudaStreamEndCapture(c.stream, &graph);
-  if (e != cudaSuccess) return cuda_fail(c, e, "end capture");
-  cudaGraphExec_t exec = nullptr;
-  e = cudaGraphInstantiate(&exec, graph, 0);
-  cudaGraphDestroy(graph);
-  if (e != cudaSuccess) return cuda_fail(c, e, "instantiate graph");
-  e = cudaGraphLaunch(exec, c.stream);
-  c.launches += 5;
-  if (e != cudaSuccess) {
-    cudaGraphExecDestroy(exec);
-    return cuda_fail(c, e, "graph launch");
+  const uint64_t chunks = (total + kChunk - 1) / kChunk;
+  for (int k = 0; k < 4; ++k) {
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, g.fns[k], kBatchThreads, 0);
+    const uint64_t warps = k < 3 ? chunks : long_cap;
+    g.grids[k] = (int) std::max<uint64_t>(
+        1, std::min<uint64_t>((uint64_t) c.num_sms * std::max(occ, 1), (warps + 7) / 8));
   }
+
+  // One graph: reset, plan, window, seed, sweep, long rows, certification,
+  // finalisation.  Captured once per launch shape; the per-call input (the
+  // problems) is read from device memory.
+  const uint64_t key[13] = {(uint64_t) dims, n,        (uint64_t) ndir, (uint64_t) dA,
+                            (uint64_t) dB,   total_a,  total_b,         (uint64_t) g.base,
+                            (uint64_t) L.off, total,   maxpairs,        long_cap,
+                            (uint64_t) c.stream};
+  static_assert(sizeof(key) == sizeof(c.batch_key), "batch key size");
+  if (!c.batch_graph || std::memcmp(key, c.batch_key, sizeof(key)) != 0) {
+    if ((s = capture_batch_graph(c, g)) != HD_OK) return s;
+    std::memcpy(c.batch_key, key, sizeof(key));
+  }
+  e = cudaGraphLaunch(c.batch_graph, c.stream);
+  c.launches += 9;  // own kernels: plan keys, plan counts, window, seed, fold, sweep, long,
+                    // certify, finalize
+  if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
   uint32_t bad = 0;
-  if ((e = cudaMemcpyAsync(out, d_out, n * sizeof(hd_batch_result), cudaMemcpyDeviceToHost,
+  if ((e = cudaMemcpyAsync(out, g.out, n * sizeof(hd_batch_result), cudaMemcpyDeviceToHost,
                            c.stream)) != cudaSuccess ||
-      (e = cudaMemcpyAsync(&bad, d_bad, 4, cudaMemcpyDeviceToHost, c.stream)) != cudaSuccess ||
-      (e = cudaStreamSynchronize(c.stream)) != cudaSuccess) {
-    cudaGraphExecDestroy(exec);
+      (e = cudaMemcpyAsync(&bad, g.bad, 4, cudaMemcpyDeviceToHost, c.stream)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(c.stream)) != cudaSuccess)
     return cuda_fail(c, e, "batch solve");
-  }
-  cudaGraphExecDestroy(exec);
   if (bad) return fail(c, HD_ERR_CUDA, "batch certification mismatch");
   return HD_OK;
 }

@@ -107,7 +107,10 @@ struct Ctx {
   cudaEvent_t ev[26] = {};
   bool timing = false;
   int ev_base = 0;
+  // Batched solve: the last instantiated graph and the launch shape it was
+  // captured for (reused while the shape, buffers and stream are unchanged).
   cudaGraphExec_t batch_graph = nullptr;
+  uint64_t batch_key[13] = {};
   // Per-solve cache: the Morton-sorted sets (slot 0 = call's A, 1 = call's B)
   // are shared by both directions of an undirected solve.
   SortedSet sorted[2];

@@ -62,3 +62,50 @@ def test_batch_rejects_empty_problem(engine):
     with pytest.raises(hd.HDError) as ei:
         engine.solve_batch(a, a, [0, 2, 2], [0, 2, 4])
     assert ei.value.status == 1
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_batch_incoherent_sets(engine, dims):
+    """Random (not spatially ordered) sets: most rows do not settle in their
+    short scan and go through the warp-per-row long pass."""
+    rng = np.random.default_rng(9 + dims)
+    na = [5000, 2000, 65, 64, 63, 1, 3000, 33]
+    nb = [4000, 2500, 64, 65, 1, 63, 3000, 97]
+    a = rng.random((sum(na), dims)).astype(np.float32)
+    b = rng.random((sum(nb), dims)).astype(np.float32)
+    oa = np.concatenate([[0], np.cumsum(na)])
+    ob = np.concatenate([[0], np.cumsum(nb)])
+    for undirected in (False, True):
+        out = engine.solve_batch(a, b, oa, ob, undirected=undirected)
+        for p in range(len(na)):
+            x, y = a[oa[p]:oa[p + 1]], b[ob[p]:ob[p + 1]]
+            want = hd_oracle.hd_f32(x, y, undirected=undirected)
+            assert out["hd_f32"][p] == want["hd_f32"], (p, undirected)
+
+
+def test_batch_rejects_out_of_range_offsets(engine):
+    import hausdorffdistance_gb300 as hd
+    a = np.ones((4, 2), np.float32)
+    # A huge offset whose sum with the count wraps around 2^64.
+    with pytest.raises(hd.HDError):
+        engine.solve_batch(a, a, np.array([2**63, 2**63 + 2], np.uint64).astype(np.int64),
+                           [0, 2])
+    with pytest.raises(ValueError):
+        engine.solve_batch(a, a, [0, 2, 4], [0, 4])
+
+
+def test_batch_reuses_graph_across_calls(engine):
+    """Same launch shape, different problems: the cached graph re-plans from
+    the problems on the device."""
+    rng = np.random.default_rng(21)
+    a = rng.random((3000, 2)).astype(np.float32)
+    b = rng.random((3000, 2)).astype(np.float32)
+    # Sizes (1000, 2000) then (2000, 1000): same item total and largest
+    # problem, so the second and third calls run the first call's graph.
+    for cut, shift in ((1000, 0.0), (2000, 0.0), (2000, 0.25)):
+        off = np.array([0, cut, 3000])
+        bb = b + np.float32(shift)
+        out = engine.solve_batch(a, bb, off, off, undirected=True)
+        for p in range(2):
+            want = hd_oracle.hd_f32(a[off[p]:off[p + 1]], bb[off[p]:off[p + 1]], undirected=True)
+            assert out["hd_f32"][p] == want["hd_f32"], (cut, shift, p)
