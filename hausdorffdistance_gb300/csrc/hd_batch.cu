@@ -59,6 +59,7 @@ constexpr int kWindow = 4;       // window half-width of the bound pass
 constexpr int kSlots = 8;        // seed rows per problem-direction (row mod 8)
 constexpr int kChunk = 8;        // consecutive items per warp step
 constexpr int kLongIlp = 8;      // independent loads per lane per long-pass round
+constexpr int kSmallRows = 1024; // directions up to this many query rows: one warp each
 constexpr int kSeedGroup = 8;    // items per seed stripe
 constexpr uint64_t kLongCap = 1ull << 21;  // queued long rows at most
 constexpr uint32_t kNoSeed = 0xFFFFFFFFu;  // empty seed minimum (above every float)
@@ -91,11 +92,19 @@ __device__ __forceinline__ float pt_d2(const float* __restrict__ X, uint64_t i,
   }
 }
 
-__device__ __forceinline__ uint64_t items_of(uint64_t n) { return (n + 31) / 32; }
+__device__ __host__ __forceinline__ uint64_t items_of(uint64_t n) { return (n + 31) / 32; }
 
-// Walks the items in plan order: (sorted problem rank r, direction d, item
-// number within the direction).  init() is one binary search over the item
-// prefix; next() steps to the following item.
+// Items of a direction whose query set has nx rows in the multi-pass
+// pipeline: directions of at most kSmallRows rows go to the one-warp path.
+__device__ __host__ __forceinline__ uint64_t large_items(uint64_t nx) {
+  return nx > (uint64_t) kSmallRows ? items_of(nx) : 0;
+}
+
+// Walks the items of the multi-pass pipeline in plan order: (sorted problem
+// rank r, direction d, item number within the direction), skipping the
+// directions of the one-warp path.  init() is one binary search over the
+// item prefix; next() steps to the following item.  Problems with an item
+// come first in plan order, so next() never has to skip a problem.
 struct Cursor {
   const hd_problem* probs;
   const uint32_t* order;
@@ -103,13 +112,15 @@ struct Cursor {
   int ndir;
   uint32_t r, p;
   int d;
-  uint64_t item, nitems;
+  uint64_t item, nitems, it0, it1;
   hd_problem pr;
 
   __device__ void load(uint32_t rank) {
     r = rank;
     p = order[rank];
     pr = probs[p];
+    it0 = large_items(pr.n_a);
+    it1 = ndir == 2 ? large_items(pr.n_b) : 0;
   }
   __device__ void init(uint64_t w, const uint64_t* __restrict__ prefix) {
     uint32_t lo = 0, hi = nprob;  // prefix[lo] <= w < prefix[hi]
@@ -122,27 +133,26 @@ struct Cursor {
     }
     load(lo);
     const uint64_t local = w - prefix[lo];
-    const uint64_t it0 = items_of(pr.n_a);
-    if (local < it0 || ndir == 1) {
+    if (local < it0) {
       d = 0;
       item = local;
       nitems = it0;
     } else {
       d = 1;
       item = local - it0;
-      nitems = items_of(pr.n_b);
+      nitems = it1;
     }
   }
   __device__ void next() {
     if (++item < nitems) return;
     item = 0;
-    if (d == 0 && ndir == 2) {
+    if (d == 0 && it1 > 0) {
       d = 1;
-      nitems = items_of(pr.n_b);
+      nitems = it1;
     } else if (r + 1 < nprob) {
       load(r + 1);
-      d = 0;
-      nitems = items_of(pr.n_a);
+      d = it0 > 0 ? 0 : 1;
+      nitems = it0 > 0 ? it0 : it1;
     }
   }
   __device__ uint64_t pd() const { return 2 * (uint64_t) p + d; }
@@ -180,6 +190,75 @@ __device__ __forceinline__ uint32_t scan_start(uint32_t row, float ratio, uint32
   return c >= half ? c - half : c + (ny - half);
 }
 
+template <int D>
+__device__ __forceinline__ void load_pt(const float* __restrict__ P, uint64_t i, float* v) {
+  if constexpr (D == 2) {
+    const float2 q = *reinterpret_cast<const float2*>(P + 2 * i);
+    v[0] = q.x;
+    v[1] = q.y;
+  } else {
+#pragma unroll
+    for (int t = 0; t < D; ++t) v[t] = P[D * i + t];
+  }
+}
+
+template <int D>
+__device__ __forceinline__ float d2_of(const float* a, const float* b) {
+  if constexpr (D == 2)
+    return d2_2(a[0], a[1], b[0], b[1]);
+  else
+    return d2_3(a[0], a[1], a[2], b[0], b[1], b[2]);
+}
+
+// Minimum over `count` consecutive points of Y from position j (circular),
+// starting from cmin; loads are issued in groups of 8 so that they overlap.
+// j advances past the points scanned.
+template <int D>
+__device__ __forceinline__ float scan_run(const float* __restrict__ X, uint32_t row,
+                                          const float* __restrict__ Y, uint32_t& j, uint32_t ny,
+                                          uint32_t count, float cmin) {
+  float x[D];
+  load_pt<D>(X, row, x);
+  if (j + (uint64_t) count <= ny) {
+    // No wrap: consecutive points at fixed offsets from one base pointer.
+    const float* yp = Y + (uint64_t) j * D;
+    uint32_t k = 0;
+    for (; k + 8 <= count; k += 8, yp += 8 * D) {
+      float y[8][D];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) load_pt<D>(yp, u, y[u]);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) cmin = fminf(cmin, d2_of<D>(x, y[u]));
+    }
+    for (; k < count; ++k, yp += D) {
+      float y[D];
+      load_pt<D>(yp, 0, y);
+      cmin = fminf(cmin, d2_of<D>(x, y));
+    }
+    j += count;
+    if (j == ny) j = 0;
+    return cmin;
+  }
+  uint32_t k = 0;
+  for (; k + 8 <= count; k += 8) {
+    float y[8][D];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      load_pt<D>(Y, j, y[u]);
+      j = (j + 1 == ny) ? 0 : j + 1;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) cmin = fminf(cmin, d2_of<D>(x, y[u]));
+  }
+  for (; k < count; ++k) {
+    float y[D];
+    load_pt<D>(Y, j, y);
+    cmin = fminf(cmin, d2_of<D>(x, y));
+    j = (j + 1 == ny) ? 0 : j + 1;
+  }
+  return cmin;
+}
+
 __device__ __forceinline__ float warp_min(float v) {
 #pragma unroll
   for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
@@ -200,11 +279,7 @@ __device__ __forceinline__ void window_item(const BatchArgs& a, const Cursor& cu
   float u = -1.0f;
   if (valid) {
     uint32_t j = scan_start(row, (float) ny / (float) nx, ny, w0 >> 1);
-    u = INFINITY;
-    for (uint32_t k = 0; k < w0; ++k) {
-      u = fminf(u, pt_d2<D>(X, row, Y, j));
-      j = (j + 1 == ny) ? 0 : j + 1;
-    }
+    u = scan_run<D>(X, row, Y, j, ny, w0, INFINITY);
   }
   if (valid) (cu.d == 0 ? a.wb_a + cu.pr.offset_a : a.wb_b + cu.pr.offset_b)[row] = u;
   // Row r's class is r % kSlots = lane % kSlots (items start at multiples of
@@ -245,6 +320,7 @@ __device__ __forceinline__ void seed_item(const BatchArgs& a, const Cursor& cu, 
     for (int t = 0; t < D; ++t) x[k][t] = X[r * D + t];
     m[k] = INFINITY;
   }
+#pragma unroll 4
   for (uint32_t j = lo + lane; j < hi; j += 32) {
     float y[D];
 #pragma unroll
@@ -283,7 +359,7 @@ __global__ void k_batch_fold(const unsigned long long* __restrict__ ubound,
         pack_max(__uint_as_float(bits), unpack_max_index(ubound[t * kSlots + k]));
     best = kk > best ? kk : best;
   }
-  keys[t] = best;
+  if (best) keys[t] = best;  // one-warp directions have no seeds and keep their own key
 }
 
 // Sweep pass, one item: a row whose window bound is at or below the running
@@ -312,10 +388,7 @@ __device__ __forceinline__ void sweep_item(const BatchArgs& a, const Cursor& cu,
   const uint32_t limit = ny < (uint32_t) kShortScan ? ny : (uint32_t) kShortScan;
   while (!broke && step < limit) {
     const uint32_t chunk = min((uint32_t) kCheckEvery, limit - step);
-    for (uint32_t u = 0; u < chunk; ++u) {
-      cmin = fminf(cmin, pt_d2<D>(X, row, Y, j));
-      j = (j + 1 == ny) ? 0 : j + 1;
-    }
+    cmin = scan_run<D>(X, row, Y, j, ny, chunk, cmin);
     step += chunk;
     broke = cmin <= thr;
   }
@@ -349,7 +422,8 @@ __device__ __forceinline__ void sweep_item(const BatchArgs& a, const Cursor& cu,
 }
 
 template <int D, int PASS>
-__global__ void __launch_bounds__(kBatchThreads, 4) k_batch_pass(BatchArgs a) {
+__global__ void __launch_bounds__(kBatchThreads, PASS == kPassSeed ? 3 : 4)
+    k_batch_pass(BatchArgs a) {
   const int lane = threadIdx.x & 31;
   Cursor cu;
   cu.probs = a.probs;
@@ -362,7 +436,8 @@ __global__ void __launch_bounds__(kBatchThreads, 4) k_batch_pass(BatchArgs a) {
     const uint64_t base = chunk * kChunk;
     const uint64_t end = min(base + kChunk, a.total);
     cu.init(base, a.prefix);
-    for (uint64_t w = base; w < end; ++w, cu.next()) {
+    for (uint64_t w = base; w < end; ++w) {
+      if (w > base) cu.next();
       const float* X = cu.d == 0 ? a.A + cu.pr.offset_a * D : a.B + cu.pr.offset_b * D;
       const float* Y = cu.d == 0 ? a.B + cu.pr.offset_b * D : a.A + cu.pr.offset_a * D;
       const uint32_t nx = (uint32_t) cu.nx(), ny = (uint32_t) cu.ny();
@@ -439,14 +514,194 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_long(BatchArgs a) {
   }
 }
 
-// Plan: sort keys (largest |A|*|B| first, stable by problem index) and the
-// item count of each sorted rank (entry nprob is 0, so that an exclusive scan
-// over nprob + 1 entries gives the item prefix with the total at the end).
-__global__ void k_plan_keys(const hd_problem* __restrict__ probs, uint32_t n, uint64_t maxpairs,
-                            unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals) {
+// One-warp path: a warp solves a whole problem-direction of at most
+// kSmallRows query rows with the same steps as the multi-pass pipeline —
+// window bounds (kept in shared memory), the 8 residue-class seeds, the
+// sweep with early break, queued rows scanned by the whole warp — and no
+// global intermediate state.  Warps take problem-directions in plan order.
+template <int D>
+__device__ __forceinline__ void small_direction(const BatchArgs& a, uint32_t p, int d,
+                                                const hd_problem& pr, float* wb, int lane) {
+  const float* X = d == 0 ? a.A + pr.offset_a * D : a.B + pr.offset_b * D;
+  const float* Y = d == 0 ? a.B + pr.offset_b * D : a.A + pr.offset_a * D;
+  const uint32_t nx = (uint32_t) (d == 0 ? pr.n_a : pr.n_b);
+  const uint32_t ny = (uint32_t) (d == 0 ? pr.n_b : pr.n_a);
+  const float ratio = (float) ny / (float) nx;
+  const uint32_t w0 = ny > 2 * kWindow + 1 ? (uint32_t) (2 * kWindow + 1) : ny;
+  const uint32_t half = w0 >> 1;
+
+  // Window bounds; each lane keeps the largest bound of its own rows (all in
+  // class lane % kSlots).
+  unsigned long long cls = 0;
+  for (uint32_t row = lane; row < nx; row += 32) {
+    uint32_t j = scan_start(row, ratio, ny, half);
+    const float u = scan_run<D>(X, row, Y, j, ny, w0, INFINITY);
+    wb[row] = u;
+    const unsigned long long kk = pack_max(u, row);
+    cls = kk > cls ? kk : cls;
+  }
+#pragma unroll
+  for (int o = 16; o >= kSlots; o >>= 1) {
+    const unsigned long long v = __shfl_xor_sync(0xFFFFFFFFu, cls, o);
+    cls = v > cls ? v : cls;
+  }
+
+  // Seeds: exact nearest-neighbour distances of the class maxima.
+  float x[kSlots][D];
+  uint32_t rows[kSlots];
+  float m[kSlots];
+#pragma unroll
+  for (int k = 0; k < kSlots; ++k) {
+    const unsigned long long u = __shfl_sync(0xFFFFFFFFu, cls, k);
+    rows[k] = u ? unpack_max_index(u) : 0xFFFFFFFFu;
+    const uint32_t r = u ? rows[k] : 0;
+#pragma unroll
+    for (int t = 0; t < D; ++t) x[k][t] = X[(uint64_t) r * D + t];
+    m[k] = INFINITY;
+  }
+#pragma unroll 4
+  for (uint32_t j = lane; j < ny; j += 32) {
+    float y[D];
+#pragma unroll
+    for (int t = 0; t < D; ++t) y[t] = Y[(uint64_t) j * D + t];
+#pragma unroll
+    for (int k = 0; k < kSlots; ++k) {
+      if constexpr (D == 2)
+        m[k] = fminf(m[k], d2_2(x[k][0], x[k][1], y[0], y[1]));
+      else
+        m[k] = fminf(m[k], d2_3(x[k][0], x[k][1], x[k][2], y[0], y[1], y[2]));
+    }
+  }
+  unsigned long long best = 0;
+#pragma unroll
+  for (int k = 0; k < kSlots; ++k) {
+    const float v = warp_min(m[k]);
+    if (rows[k] != 0xFFFFFFFFu) {
+      const unsigned long long kk = pack_max(v, rows[k]);
+      best = kk > best ? kk : best;
+    }
+  }
+  __syncwarp();
+  float thr = threshold_of(best);
+
+  // Sweep.
+  const uint32_t limit = ny < (uint32_t) kShortScan ? ny : (uint32_t) kShortScan;
+  for (uint32_t row0 = 0; row0 < nx; row0 += 32) {
+    const uint32_t row = row0 + lane;
+    const bool valid = row < nx;
+    float cmin = valid ? wb[row] : 0.0f;
+    bool broke = !valid || cmin <= thr;
+    if (__all_sync(0xFFFFFFFFu, broke)) continue;
+    uint32_t j = 0;
+    if (!broke) {
+      j = scan_start(row, ratio, ny, half) + w0;
+      if (j >= ny) j -= ny;
+    }
+    uint32_t step = w0;
+    while (!broke && step < limit) {
+      const uint32_t chunk = min((uint32_t) kCheckEvery, limit - step);
+      cmin = scan_run<D>(X, row, Y, j, ny, chunk, cmin);
+      step += chunk;
+      broke = cmin <= thr;
+    }
+    const bool pending = !broke && step < ny;
+    // Rows that completed their scan raise the maximum.
+    unsigned long long kk = (!broke && !pending) ? pack_max(cmin, row) : 0ull;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const unsigned long long v = __shfl_xor_sync(0xFFFFFFFFu, kk, o);
+      kk = v > kk ? v : kk;
+    }
+    if (kk > best) {
+      best = kk;
+      thr = threshold_of(best);
+    }
+    // Open rows: the whole warp finishes each in turn.
+    unsigned open = __ballot_sync(0xFFFFFFFFu, pending);
+    while (open) {
+      const int src = __ffs(open) - 1;
+      open &= open - 1;
+      const uint32_t r = __shfl_sync(0xFFFFFFFFu, row, src);
+      const uint32_t js = __shfl_sync(0xFFFFFFFFu, j, src);
+      float c = __shfl_sync(0xFFFFFFFFu, cmin, src);
+      if (c <= thr) continue;
+      float xr[D];
+#pragma unroll
+      for (int t = 0; t < D; ++t) xr[t] = X[(uint64_t) r * D + t];
+      const uint64_t rem = ny - kShortScan;
+      float cm = INFINITY;
+      bool done = false;
+      for (uint64_t t0 = 0; t0 < rem; t0 += 32 * kLongIlp) {
+        float y[kLongIlp][D];
+#pragma unroll
+        for (int u = 0; u < kLongIlp; ++u) {
+          const uint64_t t = t0 + (uint64_t) u * 32 + lane;
+          uint64_t jj = js + t;  // js < ny and t < ny: one subtraction wraps
+          if (jj >= ny) jj -= ny;
+#pragma unroll
+          for (int k = 0; k < D; ++k) y[u][k] = t < rem ? Y[(uint64_t) jj * D + k] : INFINITY;
+        }
+#pragma unroll
+        for (int u = 0; u < kLongIlp; ++u) {
+          const uint64_t t = t0 + (uint64_t) u * 32 + lane;
+          float d2;
+          if constexpr (D == 2)
+            d2 = d2_2(xr[0], xr[1], y[u][0], y[u][1]);
+          else
+            d2 = d2_3(xr[0], xr[1], xr[2], y[u][0], y[u][1], y[u][2]);
+          if (t < rem) cm = fminf(cm, d2);
+        }
+        if (fminf(c, warp_min(cm)) <= thr) {
+          done = true;
+          break;
+        }
+      }
+      if (done) continue;
+      c = fminf(c, warp_min(cm));
+      const unsigned long long kr = pack_max(c, r);
+      if (kr > best) {
+        best = kr;
+        thr = threshold_of(best);
+      }
+    }
+  }
+  if (lane == 0) a.keys[2 * (uint64_t) p + d] = best;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBatchThreads) k_batch_small(BatchArgs a) {
+  __shared__ float s_wb[kBatchThreads / 32][kSmallRows];
+  const int lane = threadIdx.x & 31;
+  float* wb = s_wb[threadIdx.x >> 5];
+  const uint64_t nw = (uint64_t) gridDim.x * (kBatchThreads / 32);
+  const uint64_t npd = (uint64_t) a.nprob * a.ndir;
+  for (uint64_t q = (uint64_t) blockIdx.x * (kBatchThreads / 32) + (threadIdx.x >> 5); q < npd;
+       q += nw) {
+    const uint32_t r = (uint32_t) (q / a.ndir);
+    const int d = (int) (q % a.ndir);
+    const uint32_t p = a.order[r];
+    const hd_problem pr = a.probs[p];
+    if ((d == 0 ? pr.n_a : pr.n_b) > (uint64_t) kSmallRows) continue;
+    small_direction<D>(a, p, d, pr, wb, lane);
+    __syncwarp();  // wb is reused by the next problem-direction
+  }
+}
+
+// Plan: sort keys and the item count of each sorted rank.  Problems with a
+// direction in the multi-pass pipeline come first, each group largest
+// |A|*|B| first (stable by problem index): key = maxpairs - pairs, plus
+// maxpairs + 1 for the problems whose directions all take the one-warp path.
+// Entry nprob of the counts is 0, so that an exclusive scan over nprob + 1
+// entries gives the item prefix with the total at the end.
+__global__ void k_plan_keys(const hd_problem* __restrict__ probs, uint32_t n, int ndir,
+                            uint64_t maxpairs, unsigned long long* __restrict__ keys,
+                            uint32_t* __restrict__ vals) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  keys[i] = maxpairs - probs[i].n_a * probs[i].n_b;
+  const hd_problem pr = probs[i];
+  const bool large = large_items(pr.n_a) > 0 || (ndir == 2 && large_items(pr.n_b) > 0);
+  const uint64_t pairs = min((uint64_t) (pr.n_a * pr.n_b), maxpairs);  // maxpairs < 2^62
+  keys[i] = maxpairs - pairs + (large ? 0 : maxpairs + 1);
   vals[i] = i;
 }
 
@@ -460,7 +715,7 @@ __global__ void k_plan_counts(const hd_problem* __restrict__ probs,
     return;
   }
   const hd_problem pr = probs[order[r]];
-  cnt[r] = items_of(pr.n_a) + (ndir == 2 ? items_of(pr.n_b) : 0);
+  cnt[r] = large_items(pr.n_a) + (ndir == 2 ? large_items(pr.n_b) : 0);
 }
 
 // Certification per problem-direction: one warp scans the other set for the
@@ -485,6 +740,7 @@ __global__ void k_batch_certify(const float* __restrict__ A, const float* __rest
   const uint64_t ny = d == 0 ? pr.n_b : pr.n_a;
   const uint32_t ia = unpack_max_index(key);
   unsigned long long best = ~0ull;
+#pragma unroll 4
   for (uint64_t j = lane; j < ny; j += 32) {
     const unsigned long long k = pack_min(pt_d2<D>(X, ia, Y, j), (uint32_t) j);
     best = k < best ? k : best;
@@ -557,8 +813,8 @@ struct BatchGraph {
   PD* pd;
   hd_batch_result* out;
   uint32_t* bad;
-  const void* fns[4];     // window, seed, sweep, long
-  int grids[4];
+  const void* fns[5];     // window, seed, sweep, long, one-warp path
+  int grids[5];
 };
 
 hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
@@ -572,7 +828,7 @@ hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
   cudaMemsetAsync(g.base, 0, g.zero_bytes, c.stream);
   cudaMemsetAsync(at(g.o_smin), 0xFF, g.smin_bytes, c.stream);
   cudaMemsetAsync(g.ctr, 0, 2 * 8, c.stream);
-  k_plan_keys<<<pblocks, 256, 0, c.stream>>>(a.probs, n, g.maxpairs,
+  k_plan_keys<<<pblocks, 256, 0, c.stream>>>(a.probs, n, g.ndir, g.maxpairs,
                                             (unsigned long long*) at(g.o_pkeys),
                                             (uint32_t*) at(g.o_pvals));
   size_t tb = g.cub_tmp;
@@ -587,6 +843,12 @@ hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
                                 const_cast<uint64_t*>(a.prefix), (int64_t) (g.n + 1), c.stream);
   BatchArgs kernel_args = a;
   void* kargs[] = {&kernel_args};
+  // Fork: the one-warp path runs on a side branch of the graph, beside the
+  // multi-pass pipeline; both join before certification.
+  cudaEventRecord(c.batch_fork, c.stream);
+  cudaStreamWaitEvent(c.batch_side, c.batch_fork, 0);
+  cudaLaunchKernel(g.fns[4], dim3(g.grids[4]), dim3(kBatchThreads), kargs, 0, c.batch_side);
+  cudaEventRecord(c.batch_join, c.batch_side);
   const uint64_t npd = g.n * g.ndir;
   for (int k = 0; k < 4; ++k) {
     if (k == 2)  // between seed and sweep
@@ -594,6 +856,7 @@ hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
                                                                          a.keys);
     cudaLaunchKernel(g.fns[k], dim3(g.grids[k]), dim3(kBatchThreads), kargs, 0, c.stream);
   }
+  cudaStreamWaitEvent(c.stream, c.batch_join, 0);
   const unsigned cblocks = (unsigned) ((g.n * g.ndir * 32 + 255) / 256);
   if (g.dims == 2)
     k_batch_certify<2><<<cblocks, 256, 0, c.stream>>>(a.A, a.B, a.probs, n, g.ndir, a.keys, g.pd);
@@ -627,7 +890,7 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   uint64_t total = 0, rows = 0, maxpairs = 0;
   for (uint64_t i = 0; i < n; ++i) {
     const hd_problem& p = probs[i];
-    total += (p.n_a + 31) / 32 + (ndir == 2 ? (p.n_b + 31) / 32 : 0);
+    total += large_items(p.n_a) + (ndir == 2 ? large_items(p.n_b) : 0);
     rows += p.n_a + (ndir == 2 ? p.n_b : 0);
     maxpairs = std::max<uint64_t>(maxpairs, p.n_a * p.n_b);
   }
@@ -635,9 +898,12 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   g.dims = dims;
   g.ndir = ndir;
   g.n = n;
+  // Plan keys stay below 2 * maxpairs + 2 (largest-first order among
+  // problems above 2^62 pairs is not needed).
+  maxpairs = std::min<uint64_t>(maxpairs, (1ull << 62) - 1);
   g.maxpairs = maxpairs;
   g.end_bit = 1;
-  while (g.end_bit < 64 && (maxpairs >> g.end_bit)) ++g.end_bit;
+  while (g.end_bit < 64 && ((2 * maxpairs + 1) >> g.end_bit)) ++g.end_bit;
   const uint64_t long_cap = std::min<uint64_t>(rows, kLongCap);
 
   // CUB temporary storage for the plan's sort and scan.
@@ -724,17 +990,19 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
     g.fns[1] = (const void*) k_batch_pass<2, kPassSeed>;
     g.fns[2] = (const void*) k_batch_pass<2, kPassSweep>;
     g.fns[3] = (const void*) k_batch_long<2>;
+    g.fns[4] = (const void*) k_batch_small<2>;
   } else {
     g.fns[0] = (const void*) k_batch_pass<3, kPassWindow>;
     g.fns[1] = (const void*) k_batch_pass<3, kPassSeed>;
     g.fns[2] = (const void*) k_batch_pass<3, kPassSweep>;
     g.fns[3] = (const void*) k_batch_long<3>;
+    g.fns[4] = (const void*) k_batch_small<3>;
   }
   const uint64_t chunks = (total + kChunk - 1) / kChunk;
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < 5; ++k) {
     int occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, g.fns[k], kBatchThreads, 0);
-    const uint64_t warps = k < 3 ? chunks : long_cap;
+    const uint64_t warps = k < 3 ? chunks : (k == 3 ? long_cap : n * ndir);
     g.grids[k] = (int) std::max<uint64_t>(
         1, std::min<uint64_t>((uint64_t) c.num_sms * std::max(occ, 1), (warps + 7) / 8));
   }
@@ -747,13 +1015,19 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
                             (uint64_t) L.off, total,   maxpairs,        long_cap,
                             (uint64_t) c.stream};
   static_assert(sizeof(key) == sizeof(c.batch_key), "batch key size");
+  if (!c.batch_side) {
+    if ((e = cudaStreamCreateWithFlags(&c.batch_side, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&c.batch_fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&c.batch_join, cudaEventDisableTiming)) != cudaSuccess)
+      return cuda_fail(c, e, "batch side stream");
+  }
   if (!c.batch_graph || std::memcmp(key, c.batch_key, sizeof(key)) != 0) {
     if ((s = capture_batch_graph(c, g)) != HD_OK) return s;
     std::memcpy(c.batch_key, key, sizeof(key));
   }
   e = cudaGraphLaunch(c.batch_graph, c.stream);
-  c.launches += 9;  // own kernels: plan keys, plan counts, window, seed, fold, sweep, long,
-                    // certify, finalize
+  c.launches += 10;  // own kernels: plan keys, plan counts, one-warp path, window, seed, fold,
+                     // sweep, long, certify, finalize
   if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
   uint32_t bad = 0;
   if ((e = cudaMemcpyAsync(out, g.out, n * sizeof(hd_batch_result), cudaMemcpyDeviceToHost,

@@ -392,6 +392,9 @@ hd_status hd_destroy(hd_ctx* c) {
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
+  if (c->batch_fork) cudaEventDestroy(c->batch_fork);
+  if (c->batch_join) cudaEventDestroy(c->batch_join);
+  if (c->batch_side) cudaStreamDestroy(c->batch_side);
   if (c->host_pinned) cudaFreeHost(c->host_pinned);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;

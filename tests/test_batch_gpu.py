@@ -69,8 +69,11 @@ def test_batch_incoherent_sets(engine, dims):
     """Random (not spatially ordered) sets: most rows do not settle in their
     short scan and go through the warp-per-row long pass."""
     rng = np.random.default_rng(9 + dims)
-    na = [5000, 2000, 65, 64, 63, 1, 3000, 33]
-    nb = [4000, 2500, 64, 65, 1, 63, 3000, 97]
+    # Directions of <= 1024 query rows take the one-warp path, larger ones the
+    # multi-pass pipeline; 1024/1025 straddle the boundary, 100 x 20000 sends
+    # open rows of a one-warp direction through its warp-wide scan.
+    na = [5000, 2000, 65, 64, 63, 1, 3000, 33, 1024, 1025, 100]
+    nb = [4000, 2500, 64, 65, 1, 63, 3000, 97, 1025, 1024, 20000]
     a = rng.random((sum(na), dims)).astype(np.float32)
     b = rng.random((sum(nb), dims)).astype(np.float32)
     oa = np.concatenate([[0], np.cumsum(na)])
