@@ -43,7 +43,8 @@ class Options(ctypes.Structure):
                 ("seed", ctypes.c_uint64), ("sample_rate", ctypes.c_double),
                 ("n_points_cell", ctypes.c_uint32), ("leaf_size", ctypes.c_uint32),
                 ("eb_only_threshold", ctypes.c_uint32), ("always_sample", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 7)]
+                ("batch_small_rows", ctypes.c_uint32), ("batch_chunk", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 5)]
 
 
 class Result(ctypes.Structure):

@@ -20,6 +20,10 @@ It then fits the selector's table:
   (each minimising the total time of the sweep's choices);
   prefer_grid  whether the grid beats the LBVH in total over the sweep.
 
+The batch sweep (skipped with --no-batch) times the batched solver on the
+lognormal polyline batch for each schedule (one-warp threshold
+batch_small_rows x items per warp step batch_chunk) and keeps the fastest.
+
 --write regenerates hausdorffdistance_gb300/csrc/hd_tuning_table.h and
 records the sweep in hausdorffdistance_gb300/tuning_sweep.json (or both in
 --out DIR).
@@ -125,6 +129,55 @@ def fit(rows):
             "total_ms_oracle_choice": sum(min(r["eb"], r["lbvh"], r["grid"]) for r in rows)}
 
 
+BATCH_SMALL_ROWS = (1024, 4096, 8192, 16384, 65536)
+BATCH_CHUNKS = (8, 16, 32)
+BATCH_DEFAULT = {"batch_small_rows": 8192, "batch_chunk": 8}
+
+
+def batch_sweep(quick: bool, reps: int = 3):
+    """Times every batch schedule on the polyline batch (device-resident
+    inputs, wall time around the synchronous call); all schedules must give
+    identical results."""
+    import time
+    import torch
+    n = 20_000 if quick else 100_000
+    a, b, off = synth.polylines(n_problems=n, seed=104)
+    ta, tb = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    rows, ref = [], None
+    for small in BATCH_SMALL_ROWS:
+        for chunk in BATCH_CHUNKS:
+            with hd.Engine(batch_small_rows=small, batch_chunk=chunk) as eng:
+                out = eng.solve_batch(ta, tb, off, off, undirected=True)
+                if ref is None:
+                    ref = out["hd_f32"].copy()
+                assert np.array_equal(out["hd_f32"], ref), (small, chunk)
+                best = float("inf")
+                for _ in range(reps):
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    eng.solve_batch(ta, tb, off, off, undirected=True)
+                    best = min(best, (time.perf_counter() - t0) * 1e3)
+            rec = {"batch_small_rows": small, "batch_chunk": chunk, "ms": best, "problems": n}
+            rows.append(rec)
+            print(json.dumps(rec), flush=True)
+    return rows
+
+
+def fit_batch(rows):
+    best = min(rows, key=lambda r: r["ms"])
+    return {"batch_small_rows": best["batch_small_rows"], "batch_chunk": best["batch_chunk"],
+            "batch_ms": best["ms"]}
+
+
+def read_table(path):
+    """The selector parameters of an existing table (for --batch-only)."""
+    import re
+    vals = dict(re.findall(r"#define HD_TUNED_(\w+) (\S+)", open(path).read()))
+    return {"eb_small_pairs": float(vals["EB_SMALL_PAIRS"]),
+            "index_min_pairs": float(vals["INDEX_MIN_PAIRS"]),
+            "eb_ratio": float(vals["EB_RATIO"]), "prefer_grid": vals["PREFER_GRID"] != "0"}
+
+
 def write_table(params, path):
     with open(path, "w") as f:
         f.write("// Generated by hausdorffdistance_gb300/autotune.py — do not edit by hand.\n")
@@ -135,7 +188,10 @@ def write_table(params, path):
         f.write("#define HD_TUNED_BF16_MIN_PAIRS 67108864.0\n")
         f.write(f"#define HD_TUNED_PREFER_GRID {1 if params['prefer_grid'] else 0}\n")
         f.write("#define HD_TUNED_LEAF_SIZE 16\n")
-        f.write("#define HD_TUNED_BATCH_SMALL 512\n")
+        f.write(f"#define HD_TUNED_BATCH_SMALL_ROWS "
+                f"{params.get('batch_small_rows', BATCH_DEFAULT['batch_small_rows'])}\n")
+        f.write(f"#define HD_TUNED_BATCH_CHUNK "
+                f"{params.get('batch_chunk', BATCH_DEFAULT['batch_chunk'])}\n")
 
 
 def main():
@@ -144,9 +200,22 @@ def main():
     ap.add_argument("--write", action="store_true")
     ap.add_argument("--out", default=None,
                     help="directory for the table and the sweep record (default: in place)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batch schedule sweep")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="only the batch sweep; the selector keeps the current table")
     args = ap.parse_args()
-    rows = sweep(args.quick)
-    params = fit(rows)
+    if args.batch_only:
+        # The selector keeps the committed table and sweep record.
+        params = read_table(os.path.join(HERE, "csrc", TABLE_NAME))
+        with open(os.path.join(HERE, SWEEP_NAME)) as f:
+            rows = json.load(f)["rows"]
+    else:
+        rows = sweep(args.quick)
+        params = fit(rows)
+    batch_rows = []
+    if not args.no_batch:
+        batch_rows = batch_sweep(args.quick)
+        params.update(fit_batch(batch_rows))
     print(json.dumps(params))
     if args.write:
         table_dir = args.out or os.path.join(HERE, "csrc")
@@ -154,7 +223,7 @@ def main():
         os.makedirs(table_dir, exist_ok=True)
         write_table(params, os.path.join(table_dir, TABLE_NAME))
         with open(os.path.join(sweep_dir, SWEEP_NAME), "w") as f:
-            json.dump({"rows": rows, "fit": params}, f, indent=1)
+            json.dump({"rows": rows, "batch_rows": batch_rows, "fit": params}, f, indent=1)
 
 
 if __name__ == "__main__":

@@ -57,9 +57,8 @@ constexpr int kCheckEvery = 8;   // pairs between early-break checks of a row
 constexpr int kShortScan = 64;   // pairs a row scans alone before it is queued
 constexpr int kWindow = 4;       // window half-width of the bound pass
 constexpr int kSlots = 8;        // seed rows per problem-direction (row mod 8)
-constexpr int kChunk = 8;        // consecutive items per warp step
 constexpr int kLongIlp = 8;      // independent loads per lane per long-pass round
-constexpr int kSmallRows = 1024; // directions up to this many query rows: one warp each
+constexpr int kSmallMax = 65536; // largest one-warp threshold accepted
 constexpr int kSeedGroup = 8;    // items per seed stripe
 constexpr uint64_t kLongCap = 1ull << 21;  // queued long rows at most
 constexpr uint32_t kNoSeed = 0xFFFFFFFFu;  // empty seed minimum (above every float)
@@ -95,9 +94,9 @@ __device__ __forceinline__ float pt_d2(const float* __restrict__ X, uint64_t i,
 __device__ __host__ __forceinline__ uint64_t items_of(uint64_t n) { return (n + 31) / 32; }
 
 // Items of a direction whose query set has nx rows in the multi-pass
-// pipeline: directions of at most kSmallRows rows go to the one-warp path.
-__device__ __host__ __forceinline__ uint64_t large_items(uint64_t nx) {
-  return nx > (uint64_t) kSmallRows ? items_of(nx) : 0;
+// pipeline: directions of at most small_rows rows go to the one-warp path.
+__device__ __host__ __forceinline__ uint64_t large_items(uint64_t nx, uint32_t small_rows) {
+  return nx > (uint64_t) small_rows ? items_of(nx) : 0;
 }
 
 // Walks the items of the multi-pass pipeline in plan order: (sorted problem
@@ -110,6 +109,7 @@ struct Cursor {
   const uint32_t* order;
   uint32_t nprob;
   int ndir;
+  uint32_t small_rows;
   uint32_t r, p;
   int d;
   uint64_t item, nitems, it0, it1;
@@ -119,8 +119,8 @@ struct Cursor {
     r = rank;
     p = order[rank];
     pr = probs[p];
-    it0 = large_items(pr.n_a);
-    it1 = ndir == 2 ? large_items(pr.n_b) : 0;
+    it0 = large_items(pr.n_a, small_rows);
+    it1 = ndir == 2 ? large_items(pr.n_b, small_rows) : 0;
   }
   __device__ void init(uint64_t w, const uint64_t* __restrict__ prefix) {
     uint32_t lo = 0, hi = nprob;  // prefix[lo] <= w < prefix[hi]
@@ -177,6 +177,8 @@ struct BatchArgs {
   LongRow* longq;
   unsigned long long* long_count;
   uint64_t long_cap;
+  uint32_t small_rows;             // one-warp path: directions up to this many rows
+  uint32_t chunk;                  // consecutive items per warp step
 };
 
 // First position of a row's circular scan: the start of the window of w0
@@ -430,11 +432,12 @@ __global__ void __launch_bounds__(kBatchThreads, PASS == kPassSeed ? 3 : 4)
   cu.order = a.order;
   cu.nprob = a.nprob;
   cu.ndir = a.ndir;
+  cu.small_rows = a.small_rows;
   const uint64_t nw = (uint64_t) gridDim.x * (kBatchThreads / 32);
   for (uint64_t chunk = (uint64_t) blockIdx.x * (kBatchThreads / 32) + (threadIdx.x >> 5);
-       chunk * kChunk < a.total; chunk += nw) {
-    const uint64_t base = chunk * kChunk;
-    const uint64_t end = min(base + kChunk, a.total);
+       chunk * a.chunk < a.total; chunk += nw) {
+    const uint64_t base = chunk * a.chunk;
+    const uint64_t end = min(base + a.chunk, a.total);
     cu.init(base, a.prefix);
     for (uint64_t w = base; w < end; ++w) {
       if (w > base) cu.next();
@@ -515,10 +518,11 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_long(BatchArgs a) {
 }
 
 // One-warp path: a warp solves a whole problem-direction of at most
-// kSmallRows query rows with the same steps as the multi-pass pipeline —
-// window bounds (kept in shared memory), the 8 residue-class seeds, the
-// sweep with early break, queued rows scanned by the whole warp — and no
-// global intermediate state.  Warps take problem-directions in plan order.
+// small_rows query rows with the same steps as the multi-pass pipeline —
+// window bounds (stored per row and read back by the lane that wrote them),
+// the 8 residue-class seeds, the sweep with early break, open rows scanned by
+// the whole warp — with no pass boundary in between.  Warps take
+// problem-directions in plan order.
 template <int D>
 __device__ __forceinline__ void small_direction(const BatchArgs& a, uint32_t p, int d,
                                                 const hd_problem& pr, float* wb, int lane) {
@@ -670,9 +674,7 @@ __device__ __forceinline__ void small_direction(const BatchArgs& a, uint32_t p, 
 
 template <int D>
 __global__ void __launch_bounds__(kBatchThreads) k_batch_small(BatchArgs a) {
-  __shared__ float s_wb[kBatchThreads / 32][kSmallRows];
   const int lane = threadIdx.x & 31;
-  float* wb = s_wb[threadIdx.x >> 5];
   const uint64_t nw = (uint64_t) gridDim.x * (kBatchThreads / 32);
   const uint64_t npd = (uint64_t) a.nprob * a.ndir;
   for (uint64_t q = (uint64_t) blockIdx.x * (kBatchThreads / 32) + (threadIdx.x >> 5); q < npd;
@@ -681,9 +683,8 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_small(BatchArgs a) {
     const int d = (int) (q % a.ndir);
     const uint32_t p = a.order[r];
     const hd_problem pr = a.probs[p];
-    if ((d == 0 ? pr.n_a : pr.n_b) > (uint64_t) kSmallRows) continue;
-    small_direction<D>(a, p, d, pr, wb, lane);
-    __syncwarp();  // wb is reused by the next problem-direction
+    if ((d == 0 ? pr.n_a : pr.n_b) > (uint64_t) a.small_rows) continue;
+    small_direction<D>(a, p, d, pr, d == 0 ? a.wb_a + pr.offset_a : a.wb_b + pr.offset_b, lane);
   }
 }
 
@@ -694,12 +695,14 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_small(BatchArgs a) {
 // Entry nprob of the counts is 0, so that an exclusive scan over nprob + 1
 // entries gives the item prefix with the total at the end.
 __global__ void k_plan_keys(const hd_problem* __restrict__ probs, uint32_t n, int ndir,
-                            uint64_t maxpairs, unsigned long long* __restrict__ keys,
+                            uint32_t small_rows, uint64_t maxpairs,
+                            unsigned long long* __restrict__ keys,
                             uint32_t* __restrict__ vals) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const hd_problem pr = probs[i];
-  const bool large = large_items(pr.n_a) > 0 || (ndir == 2 && large_items(pr.n_b) > 0);
+  const bool large = large_items(pr.n_a, small_rows) > 0 ||
+                     (ndir == 2 && large_items(pr.n_b, small_rows) > 0);
   const uint64_t pairs = min((uint64_t) (pr.n_a * pr.n_b), maxpairs);  // maxpairs < 2^62
   keys[i] = maxpairs - pairs + (large ? 0 : maxpairs + 1);
   vals[i] = i;
@@ -707,7 +710,7 @@ __global__ void k_plan_keys(const hd_problem* __restrict__ probs, uint32_t n, in
 
 __global__ void k_plan_counts(const hd_problem* __restrict__ probs,
                               const uint32_t* __restrict__ order, uint32_t n, int ndir,
-                              uint64_t* __restrict__ cnt) {
+                              uint32_t small_rows, uint64_t* __restrict__ cnt) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r > n) return;
   if (r == n) {
@@ -715,7 +718,7 @@ __global__ void k_plan_counts(const hd_problem* __restrict__ probs,
     return;
   }
   const hd_problem pr = probs[order[r]];
-  cnt[r] = large_items(pr.n_a) + (ndir == 2 ? large_items(pr.n_b) : 0);
+  cnt[r] = large_items(pr.n_a, small_rows) + (ndir == 2 ? large_items(pr.n_b, small_rows) : 0);
 }
 
 // Certification per problem-direction: one warp scans the other set for the
@@ -828,7 +831,7 @@ hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
   cudaMemsetAsync(g.base, 0, g.zero_bytes, c.stream);
   cudaMemsetAsync(at(g.o_smin), 0xFF, g.smin_bytes, c.stream);
   cudaMemsetAsync(g.ctr, 0, 2 * 8, c.stream);
-  k_plan_keys<<<pblocks, 256, 0, c.stream>>>(a.probs, n, g.ndir, g.maxpairs,
+  k_plan_keys<<<pblocks, 256, 0, c.stream>>>(a.probs, n, g.ndir, a.small_rows, g.maxpairs,
                                             (unsigned long long*) at(g.o_pkeys),
                                             (uint32_t*) at(g.o_pvals));
   size_t tb = g.cub_tmp;
@@ -836,7 +839,7 @@ hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
                                   (unsigned long long*) at(g.o_pkeys2),
                                   (const uint32_t*) at(g.o_pvals), const_cast<uint32_t*>(a.order),
                                   (int64_t) n, 0, g.end_bit, c.stream);
-  k_plan_counts<<<pblocks, 256, 0, c.stream>>>(a.probs, a.order, n, g.ndir,
+  k_plan_counts<<<pblocks, 256, 0, c.stream>>>(a.probs, a.order, n, g.ndir, a.small_rows,
                                               (uint64_t*) at(g.o_cnt));
   tb = g.cub_tmp;
   cub::DeviceScan::ExclusiveSum(at(g.o_tmp), tb, (const uint64_t*) at(g.o_cnt),
@@ -887,10 +890,12 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   hd_status s;
   if ((s = check_problems(c, probs, n, total_a, total_b)) != HD_OK) return s;
   const int ndir = (flags & HD_UNDIRECTED) ? 2 : 1;
+  const uint32_t small_rows = std::min<uint32_t>(c.opt.batch_small_rows, kSmallMax);
+  const uint32_t chunk = std::max<uint32_t>(1, c.opt.batch_chunk);
   uint64_t total = 0, rows = 0, maxpairs = 0;
   for (uint64_t i = 0; i < n; ++i) {
     const hd_problem& p = probs[i];
-    total += large_items(p.n_a) + (ndir == 2 ? large_items(p.n_b) : 0);
+    total += large_items(p.n_a, small_rows) + (ndir == 2 ? large_items(p.n_b, small_rows) : 0);
     rows += p.n_a + (ndir == 2 ? p.n_b : 0);
     maxpairs = std::max<uint64_t>(maxpairs, p.n_a * p.n_b);
   }
@@ -982,6 +987,8 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   args.longq = (LongRow*) at(o_long);
   args.long_count = d_ctr;
   args.long_cap = long_cap;
+  args.small_rows = small_rows;
+  args.chunk = chunk;
 
   // Persistent grids: resident blocks of each kernel, at most one warp per
   // chunk of items (or per queued row).
@@ -998,7 +1005,7 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
     g.fns[3] = (const void*) k_batch_long<3>;
     g.fns[4] = (const void*) k_batch_small<3>;
   }
-  const uint64_t chunks = (total + kChunk - 1) / kChunk;
+  const uint64_t chunks = (total + chunk - 1) / chunk;
   for (int k = 0; k < 5; ++k) {
     int occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, g.fns[k], kBatchThreads, 0);
@@ -1010,10 +1017,10 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   // One graph: reset, plan, window, seed, sweep, long rows, certification,
   // finalisation.  Captured once per launch shape; the per-call input (the
   // problems) is read from device memory.
-  const uint64_t key[13] = {(uint64_t) dims, n,        (uint64_t) ndir, (uint64_t) dA,
+  const uint64_t key[15] = {(uint64_t) dims, n,        (uint64_t) ndir, (uint64_t) dA,
                             (uint64_t) dB,   total_a,  total_b,         (uint64_t) g.base,
                             (uint64_t) L.off, total,   maxpairs,        long_cap,
-                            (uint64_t) c.stream};
+                            (uint64_t) c.stream, small_rows, chunk};
   static_assert(sizeof(key) == sizeof(c.batch_key), "batch key size");
   if (!c.batch_side) {
     if ((e = cudaStreamCreateWithFlags(&c.batch_side, cudaStreamNonBlocking)) != cudaSuccess ||

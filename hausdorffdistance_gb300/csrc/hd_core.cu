@@ -20,6 +20,7 @@
 
 #include "hd_common.cuh"
 #include "hd_internal.h"
+#include "hd_tuning.h"
 
 namespace hdg {
 
@@ -348,6 +349,10 @@ hd_status hd_create(hd_ctx** out, const hd_options* opt) {
   if (c->opt.leaf_size == 0 || c->opt.leaf_size > 32) c->opt.leaf_size = 16;
   if (c->opt.n_points_cell == 0) c->opt.n_points_cell = 8;
   if (!(c->opt.sample_rate > 0.0)) c->opt.sample_rate = 0.01;
+  if (c->opt.batch_small_rows == 0) c->opt.batch_small_rows = tuning().batch_small_rows;
+  c->opt.batch_small_rows = std::min<uint32_t>(c->opt.batch_small_rows, 65536);
+  if (c->opt.batch_chunk == 0) c->opt.batch_chunk = tuning().batch_chunk;
+  c->opt.batch_chunk = std::max<uint32_t>(1, std::min<uint32_t>(c->opt.batch_chunk, 64));
   int n = 0;
   cudaError_t e = cudaGetDeviceCount(&n);
   if (e != cudaSuccess || n == 0 || c->opt.device < 0 || c->opt.device >= n) {

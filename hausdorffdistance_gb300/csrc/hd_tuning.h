@@ -11,7 +11,8 @@ struct Tuning {
   double bf16_min_pairs;  // n_dims % 16 == 0: BF16 tiles from this |A|*|B| up
   bool prefer_grid;       // index-based choice: grid instead of LBVH
   unsigned leaf_size;     // LBVH points per leaf
-  unsigned batch_small;   // batched solver: problems up to this size per warp
+  unsigned batch_small_rows;  // batches: directions up to this many rows take one warp
+  unsigned batch_chunk;       // batches: consecutive items per warp step
 };
 
 const Tuning& tuning();

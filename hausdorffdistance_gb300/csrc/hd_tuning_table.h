@@ -6,4 +6,5 @@
 #define HD_TUNED_BF16_MIN_PAIRS 67108864.0
 #define HD_TUNED_PREFER_GRID 0
 #define HD_TUNED_LEAF_SIZE 16
-#define HD_TUNED_BATCH_SMALL 512
+#define HD_TUNED_BATCH_SMALL_ROWS 8192
+#define HD_TUNED_BATCH_CHUNK 8

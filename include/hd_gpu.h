@@ -82,7 +82,11 @@ typedef struct hd_options {
                               /* plain EB is chosen (hybrid.h:171); 0 = table */
   uint32_t always_sample;  /* selector: draw the sample statistic even where  */
                            /* the size bands decide alone (autotuning)        */
-  uint32_t reserved[7];
+  uint32_t batch_small_rows; /* batches: directions of at most this many query */
+                             /* rows take the one-warp path (1..65536); 0 = table */
+  uint32_t batch_chunk;    /* batches: consecutive items per warp step (1..64); */
+                           /* 0 = table                                        */
+  uint32_t reserved[5];
 } hd_options;
 
 typedef struct hd_result {

@@ -18,3 +18,25 @@ def test_fit_picks_cost_minimising_threshold(tmp_path):
     text = (tmp_path / "t.h").read_text()
     assert "HD_TUNED_EB_RATIO" in text and "HD_TUNED_PREFER_GRID 0" in text
     assert "HD_TUNED_INDEX_MIN_PAIRS" in text and "HD_TUNED_EB_SMALL_PAIRS" in text
+
+
+def test_batch_fit_and_table(tmp_path):
+    rows = [{"batch_small_rows": s, "batch_chunk": c, "ms": 10.0 + abs(s - autotune.BATCH_SMALL_ROWS[1]) / 100 + c / 10}
+            for s in autotune.BATCH_SMALL_ROWS for c in autotune.BATCH_CHUNKS]
+    p = autotune.fit_batch(rows)
+    assert p["batch_small_rows"] == autotune.BATCH_SMALL_ROWS[1]
+    assert p["batch_chunk"] == min(autotune.BATCH_CHUNKS)
+    sel = {"eb_ratio": 0, "eb_small_pairs": 0, "index_min_pairs": 0, "prefer_grid": False}
+    autotune.write_table({**sel, **p}, str(tmp_path / "t.h"))
+    text = (tmp_path / "t.h").read_text()
+    assert f"HD_TUNED_BATCH_SMALL_ROWS {autotune.BATCH_SMALL_ROWS[1]}" in text
+    assert f"HD_TUNED_BATCH_CHUNK {min(autotune.BATCH_CHUNKS)}" in text
+    # Without a batch sweep the table keeps the defaults.
+    autotune.write_table(sel, str(tmp_path / "u.h"))
+    assert "HD_TUNED_BATCH_SMALL_ROWS 8192" in (tmp_path / "u.h").read_text()
+
+
+def test_read_table_round_trip(tmp_path):
+    sel = {"eb_ratio": 0.5, "eb_small_pairs": 1e6, "index_min_pairs": 4e6, "prefer_grid": True}
+    autotune.write_table(sel, str(tmp_path / "t.h"))
+    assert autotune.read_table(str(tmp_path / "t.h")) == sel

@@ -65,13 +65,17 @@ def test_batch_rejects_empty_problem(engine):
 
 
 @pytest.mark.parametrize("dims", [2, 3])
-def test_batch_incoherent_sets(engine, dims):
+@pytest.mark.parametrize("small_rows", [0, 1024])
+def test_batch_incoherent_sets(dims, small_rows):
     """Random (not spatially ordered) sets: most rows do not settle in their
-    short scan and go through the warp-per-row long pass."""
+    short scan and go through the warp-wide scans."""
+    import hausdorffdistance_gb300 as hd
+    engine = hd.Engine(batch_small_rows=small_rows)  # 0: the tuned threshold
     rng = np.random.default_rng(9 + dims)
-    # Directions of <= 1024 query rows take the one-warp path, larger ones the
-    # multi-pass pipeline; 1024/1025 straddle the boundary, 100 x 20000 sends
-    # open rows of a one-warp direction through its warp-wide scan.
+    # With a threshold of 1024, directions of <= 1024 query rows take the
+    # one-warp path and larger ones the multi-pass pipeline; 1024/1025
+    # straddle the boundary, 100 x 20000 sends open rows of a one-warp
+    # direction through its warp-wide scan.
     na = [5000, 2000, 65, 64, 63, 1, 3000, 33, 1024, 1025, 100]
     nb = [4000, 2500, 64, 65, 1, 63, 3000, 97, 1025, 1024, 20000]
     a = rng.random((sum(na), dims)).astype(np.float32)
@@ -112,3 +116,16 @@ def test_batch_reuses_graph_across_calls(engine):
         for p in range(2):
             want = hd_oracle.hd_f32(a[off[p]:off[p + 1]], bb[off[p]:off[p + 1]], undirected=True)
             assert out["hd_f32"][p] == want["hd_f32"], (cut, shift, p)
+
+
+def test_batch_schedules_agree():
+    """Every schedule (one-warp threshold, items per warp step) gives the
+    oracle's distances: all directions one-warp, none, and mixed."""
+    import hausdorffdistance_gb300 as hd
+    a, b, off = small_batch(150, seed=46)
+    want = [hd_oracle.hd_f32(a[off[p]:off[p + 1]], b[off[p]:off[p + 1]], undirected=True)["hd_f32"]
+            for p in range(len(off) - 1)]
+    for small, chunk in ((1, 1), (64, 8), (8192, 3), (65536, 64)):
+        with hd.Engine(batch_small_rows=small, batch_chunk=chunk) as eng:
+            out = eng.solve_batch(a, b, off, off, undirected=True)
+        assert np.array_equal(out["hd_f32"], np.array(want, np.float32)), (small, chunk)
