@@ -31,6 +31,7 @@ records the sweep in hausdorffdistance_gb300/tuning_sweep.json (or both in
 from __future__ import annotations
 
 import argparse
+import itertools
 import json
 import os
 import sys
@@ -129,12 +130,13 @@ def fit(rows):
             "total_ms_oracle_choice": sum(min(r["eb"], r["lbvh"], r["grid"]) for r in rows)}
 
 
-BATCH_SMALL_ROWS = (1024, 4096, 8192, 16384, 65536)
-BATCH_CHUNKS = (8, 16, 32)
-BATCH_DEFAULT = {"batch_small_rows": 8192, "batch_chunk": 8}
+BATCH_SMALL_ROWS = (4096, 8192)
+BATCH_CHUNKS = (8, 16)
+BATCH_WINDOWS = (1, 2, 4)
+BATCH_DEFAULT = {"batch_small_rows": 8192, "batch_chunk": 8, "batch_window": 4}
 
 
-def batch_sweep(quick: bool, reps: int = 3):
+def batch_sweep(quick: bool, reps: int = 9):
     """Times every batch schedule on the polyline batch (device-resident
     inputs, wall time around the synchronous call); all schedules must give
     identical results."""
@@ -144,28 +146,29 @@ def batch_sweep(quick: bool, reps: int = 3):
     a, b, off = synth.polylines(n_problems=n, seed=104)
     ta, tb = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
     rows, ref = [], None
-    for small in BATCH_SMALL_ROWS:
-        for chunk in BATCH_CHUNKS:
-            with hd.Engine(batch_small_rows=small, batch_chunk=chunk) as eng:
-                out = eng.solve_batch(ta, tb, off, off, undirected=True)
-                if ref is None:
-                    ref = out["hd_f32"].copy()
-                assert np.array_equal(out["hd_f32"], ref), (small, chunk)
-                best = float("inf")
-                for _ in range(reps):
-                    torch.cuda.synchronize()
-                    t0 = time.perf_counter()
-                    eng.solve_batch(ta, tb, off, off, undirected=True)
-                    best = min(best, (time.perf_counter() - t0) * 1e3)
-            rec = {"batch_small_rows": small, "batch_chunk": chunk, "ms": best, "problems": n}
-            rows.append(rec)
-            print(json.dumps(rec), flush=True)
+    for small, chunk, window in itertools.product(BATCH_SMALL_ROWS, BATCH_CHUNKS, BATCH_WINDOWS):
+        with hd.Engine(batch_small_rows=small, batch_chunk=chunk, batch_window=window) as eng:
+            out = eng.solve_batch(ta, tb, off, off, undirected=True)
+            if ref is None:
+                ref = out["hd_f32"].copy()
+            assert np.array_equal(out["hd_f32"], ref), (small, chunk, window)
+            best = float("inf")
+            for _ in range(reps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                eng.solve_batch(ta, tb, off, off, undirected=True)
+                best = min(best, (time.perf_counter() - t0) * 1e3)
+        rec = {"batch_small_rows": small, "batch_chunk": chunk, "batch_window": window,
+               "ms": best, "problems": n}
+        rows.append(rec)
+        print(json.dumps(rec), flush=True)
     return rows
 
 
 def fit_batch(rows):
     best = min(rows, key=lambda r: r["ms"])
     return {"batch_small_rows": best["batch_small_rows"], "batch_chunk": best["batch_chunk"],
+            "batch_window": best.get("batch_window", BATCH_DEFAULT["batch_window"]),
             "batch_ms": best["ms"]}
 
 
@@ -192,6 +195,8 @@ def write_table(params, path):
                 f"{params.get('batch_small_rows', BATCH_DEFAULT['batch_small_rows'])}\n")
         f.write(f"#define HD_TUNED_BATCH_CHUNK "
                 f"{params.get('batch_chunk', BATCH_DEFAULT['batch_chunk'])}\n")
+        f.write(f"#define HD_TUNED_BATCH_WINDOW "
+                f"{params.get('batch_window', BATCH_DEFAULT['batch_window'])}\n")
 
 
 def main():

@@ -55,7 +55,6 @@ namespace {
 constexpr int kBatchThreads = 256;
 constexpr int kCheckEvery = 8;   // pairs between early-break checks of a row
 constexpr int kShortScan = 64;   // pairs a row scans alone before it is queued
-constexpr int kWindow = 4;       // window half-width of the bound pass
 constexpr int kSlots = 8;        // seed rows per problem-direction (row mod 8)
 constexpr int kLongIlp = 8;      // independent loads per lane per long-pass round
 constexpr int kSmallMax = 65536; // largest one-warp threshold accepted
@@ -179,6 +178,7 @@ struct BatchArgs {
   uint64_t long_cap;
   uint32_t small_rows;             // one-warp path: directions up to this many rows
   uint32_t chunk;                  // consecutive items per warp step
+  uint32_t window;                 // half-width of the bound window
 };
 
 // First position of a row's circular scan: the start of the window of w0
@@ -267,7 +267,7 @@ __device__ __forceinline__ float warp_min(float v) {
   return v;
 }
 
-// Window pass, one item: each row's minimum over 2*kWindow+1 points of the
+// Window pass, one item: each row's minimum over 2*window+1 points of the
 // other set centred on its relative position, stored per row; the largest
 // bound (with its row) of each residue class goes to
 // ubound[problem-direction][class].
@@ -277,7 +277,7 @@ __device__ __forceinline__ void window_item(const BatchArgs& a, const Cursor& cu
                                             uint32_t ny) {
   const uint32_t row = (uint32_t) cu.item * 32 + lane;
   const bool valid = row < nx;
-  const uint32_t w0 = ny > 2 * kWindow + 1 ? (uint32_t) (2 * kWindow + 1) : ny;
+  const uint32_t w0 = ny > 2 * a.window + 1 ? 2 * a.window + 1 : ny;
   float u = -1.0f;
   if (valid) {
     uint32_t j = scan_start(row, (float) ny / (float) nx, ny, w0 >> 1);
@@ -380,7 +380,7 @@ __device__ __forceinline__ void sweep_item(const BatchArgs& a, const Cursor& cu,
                      : 0.0f;
   bool broke = !valid || cmin <= thr;
   if (__all_sync(0xFFFFFFFFu, broke)) return;
-  const uint32_t w0 = ny > 2 * kWindow + 1 ? (uint32_t) (2 * kWindow + 1) : ny;
+  const uint32_t w0 = ny > 2 * a.window + 1 ? 2 * a.window + 1 : ny;
   uint32_t j = 0;
   if (!broke) {
     j = scan_start(row, (float) ny / (float) nx, ny, w0 >> 1) + w0;
@@ -531,7 +531,7 @@ __device__ __forceinline__ void small_direction(const BatchArgs& a, uint32_t p, 
   const uint32_t nx = (uint32_t) (d == 0 ? pr.n_a : pr.n_b);
   const uint32_t ny = (uint32_t) (d == 0 ? pr.n_b : pr.n_a);
   const float ratio = (float) ny / (float) nx;
-  const uint32_t w0 = ny > 2 * kWindow + 1 ? (uint32_t) (2 * kWindow + 1) : ny;
+  const uint32_t w0 = ny > 2 * a.window + 1 ? 2 * a.window + 1 : ny;
   const uint32_t half = w0 >> 1;
 
   // Window bounds; each lane keeps the largest bound of its own rows (all in
@@ -989,6 +989,7 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   args.long_cap = long_cap;
   args.small_rows = small_rows;
   args.chunk = chunk;
+  args.window = c.opt.batch_window;
 
   // Persistent grids: resident blocks of each kernel, at most one warp per
   // chunk of items (or per queued row).
@@ -1017,10 +1018,10 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   // One graph: reset, plan, window, seed, sweep, long rows, certification,
   // finalisation.  Captured once per launch shape; the per-call input (the
   // problems) is read from device memory.
-  const uint64_t key[15] = {(uint64_t) dims, n,        (uint64_t) ndir, (uint64_t) dA,
+  const uint64_t key[16] = {(uint64_t) dims, n,        (uint64_t) ndir, (uint64_t) dA,
                             (uint64_t) dB,   total_a,  total_b,         (uint64_t) g.base,
                             (uint64_t) L.off, total,   maxpairs,        long_cap,
-                            (uint64_t) c.stream, small_rows, chunk};
+                            (uint64_t) c.stream, small_rows, chunk, c.opt.batch_window};
   static_assert(sizeof(key) == sizeof(c.batch_key), "batch key size");
   if (!c.batch_side) {
     if ((e = cudaStreamCreateWithFlags(&c.batch_side, cudaStreamNonBlocking)) != cudaSuccess ||

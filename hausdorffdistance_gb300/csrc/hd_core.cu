@@ -353,6 +353,8 @@ hd_status hd_create(hd_ctx** out, const hd_options* opt) {
   c->opt.batch_small_rows = std::min<uint32_t>(c->opt.batch_small_rows, 65536);
   if (c->opt.batch_chunk == 0) c->opt.batch_chunk = tuning().batch_chunk;
   c->opt.batch_chunk = std::max<uint32_t>(1, std::min<uint32_t>(c->opt.batch_chunk, 64));
+  if (c->opt.batch_window == 0) c->opt.batch_window = tuning().batch_window;
+  c->opt.batch_window = std::max<uint32_t>(1, std::min<uint32_t>(c->opt.batch_window, 8));
   int n = 0;
   cudaError_t e = cudaGetDeviceCount(&n);
   if (e != cudaSuccess || n == 0 || c->opt.device < 0 || c->opt.device >= n) {

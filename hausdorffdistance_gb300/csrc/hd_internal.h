@@ -112,7 +112,7 @@ struct Ctx {
   cudaGraphExec_t batch_graph = nullptr;
   cudaStream_t batch_side = nullptr;  // side branch of the batch graph's capture
   cudaEvent_t batch_fork = nullptr, batch_join = nullptr;
-  uint64_t batch_key[15] = {};
+  uint64_t batch_key[16] = {};
   // Per-solve cache: the Morton-sorted sets (slot 0 = call's A, 1 = call's B)
   // are shared by both directions of an undirected solve.
   SortedSet sorted[2];

@@ -13,6 +13,7 @@ struct Tuning {
   unsigned leaf_size;     // LBVH points per leaf
   unsigned batch_small_rows;  // batches: directions up to this many rows take one warp
   unsigned batch_chunk;       // batches: consecutive items per warp step
+  unsigned batch_window;      // batches: half-width of the bound window
 };
 
 const Tuning& tuning();

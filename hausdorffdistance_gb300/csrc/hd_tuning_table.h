@@ -7,4 +7,5 @@
 #define HD_TUNED_PREFER_GRID 0
 #define HD_TUNED_LEAF_SIZE 16
 #define HD_TUNED_BATCH_SMALL_ROWS 8192
-#define HD_TUNED_BATCH_CHUNK 8
+#define HD_TUNED_BATCH_CHUNK 16
+#define HD_TUNED_BATCH_WINDOW 4

@@ -86,7 +86,9 @@ typedef struct hd_options {
                              /* rows take the one-warp path (1..65536); 0 = table */
   uint32_t batch_chunk;    /* batches: consecutive items per warp step (1..64); */
                            /* 0 = table                                        */
-  uint32_t reserved[5];
+  uint32_t batch_window;   /* batches: half-width of the bound window (1..8);  */
+                           /* 0 = table                                        */
+  uint32_t reserved[4];
 } hd_options;
 
 typedef struct hd_result {

@@ -125,7 +125,7 @@ def test_batch_schedules_agree():
     a, b, off = small_batch(150, seed=46)
     want = [hd_oracle.hd_f32(a[off[p]:off[p + 1]], b[off[p]:off[p + 1]], undirected=True)["hd_f32"]
             for p in range(len(off) - 1)]
-    for small, chunk in ((1, 1), (64, 8), (8192, 3), (65536, 64)):
-        with hd.Engine(batch_small_rows=small, batch_chunk=chunk) as eng:
+    for small, chunk, window in ((1, 1, 1), (64, 8, 4), (8192, 3, 8), (65536, 64, 2)):
+        with hd.Engine(batch_small_rows=small, batch_chunk=chunk, batch_window=window) as eng:
             out = eng.solve_batch(a, b, off, off, undirected=True)
-        assert np.array_equal(out["hd_f32"], np.array(want, np.float32)), (small, chunk)
+        assert np.array_equal(out["hd_f32"], np.array(want, np.float32)), (small, chunk, window)
