@@ -44,7 +44,8 @@ class Options(ctypes.Structure):
                 ("n_points_cell", ctypes.c_uint32), ("leaf_size", ctypes.c_uint32),
                 ("eb_only_threshold", ctypes.c_uint32), ("always_sample", ctypes.c_uint32),
                 ("batch_small_rows", ctypes.c_uint32), ("batch_chunk", ctypes.c_uint32),
-                ("batch_window", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 4)]
+                ("batch_window", ctypes.c_uint32), ("lbvh_budget", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 3)]
 
 
 class Result(ctypes.Structure):

@@ -22,7 +22,10 @@ It then fits the selector's table:
 
 The batch sweep (skipped with --no-batch) times the batched solver on the
 lognormal polyline batch for each schedule (one-warp threshold
-batch_small_rows x items per warp step batch_chunk) and keeps the fastest.
+batch_small_rows x items per warp step batch_chunk x bound-window half-width
+batch_window) and keeps the fastest.  The budget sweep (--no-budget) times
+undirected LBVH solves on clustered, planar and uniform sets for each
+per-packet traversal budget (lbvh_budget) and keeps the smallest total.
 
 --write regenerates hausdorffdistance_gb300/csrc/hd_tuning_table.h and
 records the sweep in hausdorffdistance_gb300/tuning_sweep.json (or both in
@@ -134,6 +137,8 @@ BATCH_SMALL_ROWS = (4096, 8192)
 BATCH_CHUNKS = (8, 16)
 BATCH_WINDOWS = (1, 2, 4)
 BATCH_DEFAULT = {"batch_small_rows": 8192, "batch_chunk": 8, "batch_window": 4}
+LBVH_BUDGET_DEFAULT = 256
+LBVH_BUDGETS = (128, 256, 512, 1024, 4096)
 
 
 def batch_sweep(quick: bool, reps: int = 9):
@@ -165,6 +170,44 @@ def batch_sweep(quick: bool, reps: int = 9):
     return rows
 
 
+def budget_sweep(quick: bool, reps: int = 7):
+    """Times undirected LBVH solves for each per-packet traversal budget on
+    the clustered, planar and uniform workloads (CUDA-event time reported by
+    the library); every budget must give the same distance."""
+    import torch
+    cases = [("clusters3d", synth.clusters3d(1_000_000 if quick else 10_000_000, seed=102)),
+             ("planes3d", synth.planes3d(1_000_000 if quick else 10_000_000, seed=103,
+                                         n_planes=100)),
+             ("uniform2d", synth.uniform2d(200_000, seed=101))]
+    rows = []
+    for name, (a, b) in cases:
+        ta, tb = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+        ref = None
+        for budget in LBVH_BUDGETS:
+            with hd.Engine(lbvh_budget=budget) as eng:
+                eng.solve(ta, tb, undirected=True, variant="lbvh")
+                best = float("inf")
+                for _ in range(reps):
+                    r = eng.solve(ta, tb, undirected=True, variant="lbvh", timing=True)
+                    best = min(best, r.ms)
+            if ref is None:
+                ref = r.hd_f32
+            assert r.hd_f32 == ref, (name, budget)
+            rec = {"case": name, "lbvh_budget": budget, "ms": best, "deferred": int(r.rechecked)}
+            rows.append(rec)
+            print(json.dumps(rec), flush=True)
+    return rows
+
+
+def fit_budget(rows):
+    """The budget with the smallest total time over the sweep's cases."""
+    totals = {}
+    for r in rows:
+        totals[r["lbvh_budget"]] = totals.get(r["lbvh_budget"], 0.0) + r["ms"]
+    best = min(totals, key=lambda k: (totals[k], k))
+    return {"lbvh_budget": best, "lbvh_budget_total_ms": totals[best]}
+
+
 def fit_batch(rows):
     best = min(rows, key=lambda r: r["ms"])
     return {"batch_small_rows": best["batch_small_rows"], "batch_chunk": best["batch_chunk"],
@@ -173,12 +216,17 @@ def fit_batch(rows):
 
 
 def read_table(path):
-    """The selector parameters of an existing table (for --batch-only)."""
+    """The parameters of an existing table (sweeps that are skipped keep them)."""
     import re
     vals = dict(re.findall(r"#define HD_TUNED_(\w+) (\S+)", open(path).read()))
-    return {"eb_small_pairs": float(vals["EB_SMALL_PAIRS"]),
-            "index_min_pairs": float(vals["INDEX_MIN_PAIRS"]),
-            "eb_ratio": float(vals["EB_RATIO"]), "prefer_grid": vals["PREFER_GRID"] != "0"}
+    out = {"eb_small_pairs": float(vals["EB_SMALL_PAIRS"]),
+           "index_min_pairs": float(vals["INDEX_MIN_PAIRS"]),
+           "eb_ratio": float(vals["EB_RATIO"]), "prefer_grid": vals["PREFER_GRID"] != "0"}
+    for key, name in (("batch_small_rows", "BATCH_SMALL_ROWS"), ("batch_chunk", "BATCH_CHUNK"),
+                      ("batch_window", "BATCH_WINDOW"), ("lbvh_budget", "LBVH_BUDGET")):
+        if name in vals:
+            out[key] = int(vals[name])
+    return out
 
 
 def write_table(params, path):
@@ -197,6 +245,7 @@ def write_table(params, path):
                 f"{params.get('batch_chunk', BATCH_DEFAULT['batch_chunk'])}\n")
         f.write(f"#define HD_TUNED_BATCH_WINDOW "
                 f"{params.get('batch_window', BATCH_DEFAULT['batch_window'])}\n")
+        f.write(f"#define HD_TUNED_LBVH_BUDGET {params.get('lbvh_budget', LBVH_BUDGET_DEFAULT)}\n")
 
 
 def main():
@@ -206,8 +255,10 @@ def main():
     ap.add_argument("--out", default=None,
                     help="directory for the table and the sweep record (default: in place)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batch schedule sweep")
+    ap.add_argument("--no-budget", action="store_true", help="skip the LBVH budget sweep")
     ap.add_argument("--batch-only", action="store_true",
-                    help="only the batch sweep; the selector keeps the current table")
+                    help="only the schedule sweeps (batch, LBVH budget); the selector keeps "
+                         "the current table")
     args = ap.parse_args()
     if args.batch_only:
         # The selector keeps the committed table and sweep record.
@@ -217,10 +268,13 @@ def main():
     else:
         rows = sweep(args.quick)
         params = fit(rows)
-    batch_rows = []
+    batch_rows, budget_rows = [], []
     if not args.no_batch:
         batch_rows = batch_sweep(args.quick)
         params.update(fit_batch(batch_rows))
+    if not args.no_budget:
+        budget_rows = budget_sweep(args.quick)
+        params.update(fit_budget(budget_rows))
     print(json.dumps(params))
     if args.write:
         table_dir = args.out or os.path.join(HERE, "csrc")
@@ -228,7 +282,8 @@ def main():
         os.makedirs(table_dir, exist_ok=True)
         write_table(params, os.path.join(table_dir, TABLE_NAME))
         with open(os.path.join(sweep_dir, SWEEP_NAME), "w") as f:
-            json.dump({"rows": rows, "batch_rows": batch_rows, "fit": params}, f, indent=1)
+            json.dump({"rows": rows, "batch_rows": batch_rows, "budget_rows": budget_rows,
+                       "fit": params}, f, indent=1)
 
 
 if __name__ == "__main__":

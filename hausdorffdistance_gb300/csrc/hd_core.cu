@@ -355,6 +355,7 @@ hd_status hd_create(hd_ctx** out, const hd_options* opt) {
   c->opt.batch_chunk = std::max<uint32_t>(1, std::min<uint32_t>(c->opt.batch_chunk, 64));
   if (c->opt.batch_window == 0) c->opt.batch_window = tuning().batch_window;
   c->opt.batch_window = std::max<uint32_t>(1, std::min<uint32_t>(c->opt.batch_window, 8));
+  if (c->opt.lbvh_budget == 0) c->opt.lbvh_budget = tuning().lbvh_budget;
   int n = 0;
   cudaError_t e = cudaGetDeviceCount(&n);
   if (e != cudaSuccess || n == 0 || c->opt.device < 0 || c->opt.device >= n) {
@@ -516,6 +517,9 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   out->sample_p80[1] = undirected ? c->last_p80[1] : 0.0;
   out->err_bound = std::max(ex[0].err_bound, ex[1].err_bound);
   out->rechecked = ex[0].rechecked + ex[1].rechecked;
+  // LBVH: queries whose packet ran over the traversal budget.
+  for (int d = 0; d < ndir; ++d)
+    if (used[d] == HD_VARIANT_LBVH) out->rechecked += h->s[d].heavy_count;
   if (c->timing) {
     float t = 0;
     if (cudaEventElapsedTime(&t, c->ev[24], c->ev[25]) == cudaSuccess) out->ms = t;

@@ -39,6 +39,19 @@ namespace {
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr int kQueryWarps = 4;
 constexpr int kStack = 64;
+// A packet that has visited `budget` nodes and leaves (an option, tuned)
+// queues its open queries for the deferred pass instead of finishing them
+// alone: a query whose nearest neighbour is far (an outlier) must prove that
+// a large empty ball is empty, and one warp walking that proof serially would
+// hold the whole launch.
+constexpr uint32_t kDeferCap = 1u << 16;  // queued queries per direction at most
+
+// A queued query: its position in the sorted query set and its running
+// minimum (float bits) when it was queued.
+struct Deferred {
+  uint32_t item;
+  uint32_t gmin;
+};
 
 __device__ __forceinline__ int delta(const uint32_t* __restrict__ codes, uint32_t L,
                                      int64_t nL, int64_t i, int64_t j) {
@@ -201,7 +214,7 @@ template <int D, bool COUNT>
 __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, uint64_t nItems, uint32_t pstride,
                  uint64_t rows, const uint32_t* __restrict__ ppos,
                  const float4* __restrict__ nodes, const float4* __restrict__ B, uint64_t nB,
-                 uint32_t L, DevScalars* sc) {
+                 uint32_t L, DevScalars* sc, Deferred* __restrict__ defer, uint32_t budget) {
   __shared__ uint32_t stk[kQueryWarps][kStack];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // Packets (32 consecutive Morton-sorted queries) are visited in a
@@ -226,6 +239,8 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
   float thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
   unsigned long long pairs = 0, visits = 0, leafv = 0;
+  uint32_t work = 0;  // nodes and leaves this packet has visited
+  bool may_defer = defer != nullptr;
 
   // Scans one leaf with every lane of the packet (points read as broadcast
   // loads, four at a time); stops as soon as no lane still needs a point,
@@ -253,6 +268,7 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
       }
     }
     if (active) cmin = m;
+    ++work;
     if (COUNT) {
       ++leafv;
       pairs += (unsigned long long) min(k, cnt) * __popc(__ballot_sync(0xFFFFFFFFu, active));
@@ -286,10 +302,26 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   bool have = true;
   for (;;) {
     if (!__any_sync(0xFFFFFFFFu, active)) break;
+    if (may_defer && work >= budget) {
+      // Over budget: queue the open queries (as many as the queue holds;
+      // lanes beyond it finish here, with no budget).
+      may_defer = false;
+      const unsigned open = __ballot_sync(0xFFFFFFFFu, active);
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(&sc->heavy_count, (uint32_t) __popc(open));
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      const uint32_t slot = base + __popc(open & ((1u << lane) - 1u));
+      if (active && slot < kDeferCap) {
+        defer[slot] = Deferred{(uint32_t) item, __float_as_uint(cmin)};
+        active = false;
+      }
+      continue;
+    }
     if (have && !(next & kLeafBit)) {
       // Internal node: test both children for every lane.
       const float4* nd = nodes + 4 * (uint64_t) next;
       const float4 n0 = nd[0], n1 = nd[1], n2 = nd[2], n3 = nd[3];
+      ++work;
       if (COUNT) ++visits;
       const float dL = box_min_d2<D>(q.x, q.y, q.z, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
       const float dR = box_min_d2<D>(q.x, q.y, q.z, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
@@ -403,6 +435,8 @@ __global__ void k_pack_nodes(BuildSets b) {
 }
 
 struct QuerySet {
+  Deferred* defer;   // queue of over-budget queries (kDeferCap entries)
+  uint32_t budget;   // visits per packet before its open queries are queued
   const float4* Q;
   uint64_t nQ;
   uint32_t pstride;
@@ -423,7 +457,127 @@ struct QuerySets {
 template <int D, bool COUNT>
 __global__ void __launch_bounds__(kQueryWarps * 32) k_lbvh_query(QuerySets qs) {
   const QuerySet& S = qs.d[blockIdx.y];
-  lbvh_query_body<D, COUNT>(S.Q, S.nQ, S.pstride, S.rows, S.ppos, S.nodes, S.B, S.nB, S.L, S.sc);
+  lbvh_query_body<D, COUNT>(S.Q, S.nQ, S.pstride, S.rows, S.ppos, S.nodes, S.B, S.nB, S.L, S.sc,
+                            S.defer, S.budget);
+}
+
+// Deferred pass: one warp per queued query walks the tree with 32 stack
+// entries popped per step (one per lane) instead of one, so the proof that a
+// large ball is empty takes 1/32 of the serial steps.  Subtrees whose box is
+// not nearer than the query's running minimum are pruned; the walk stops once
+// that minimum is at or below the running maximum.  The stack lives in
+// shared memory; a walk that would overflow it sets kErrInternal (the solve
+// then fails) rather than drop a subtree.
+constexpr int kDeferWarps = 4;
+constexpr int kDeferStack = 3072;
+
+template <int D, bool COUNT>
+__global__ void __launch_bounds__(kDeferWarps * 32) k_lbvh_defer(QuerySets qs) {
+  __shared__ uint32_t stk[kDeferWarps][kDeferStack];
+  const QuerySet& S = qs.d[blockIdx.y];
+  const uint32_t cnt = min(*(volatile uint32_t*) &S.sc->heavy_count, kDeferCap);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint32_t* st = stk[warp];
+  const uint32_t nw = gridDim.x * kDeferWarps;
+  unsigned long long pairs = 0, visits = 0, leafv = 0;
+  // The running maximum is read by lane 0 and broadcast: the walk below must
+  // see one value per warp.
+  auto read_thr = [&]() {
+    unsigned long long key = 0;
+    if (lane == 0) key = ld_relaxed_u64(&S.sc->max_key);
+    return threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
+  };
+  for (uint32_t e = blockIdx.x * kDeferWarps + warp; e < cnt; e += nw) {
+    const Deferred de = S.defer[e];
+    const float4 q = S.Q[de.item];
+    float m = __uint_as_float(de.gmin);
+    float thr = read_thr();
+    if (lane == 0) st[0] = 0;  // root: internal node 0
+    int sp = 1;
+    __syncwarp();
+    int round = 0;
+    while (sp > 0 && m > thr) {
+      const int k = min(sp, 32);
+      const bool has = lane < k;
+      const uint32_t node = has ? st[sp - k + lane] : 0;
+      sp -= k;
+      __syncwarp();
+      uint32_t push0 = 0, push1 = 0;
+      int npush = 0;
+      float lm = m;
+      if (has) {
+        if (node & kLeafBit) {
+          const uint64_t p0 = (uint64_t) (node & ~kLeafBit) * S.L;
+          const uint32_t c = (uint32_t) min((uint64_t) S.L, S.nB - p0);
+          for (uint32_t t = 0; t < c; ++t) {
+            const float4 b = S.B[p0 + t];
+            if constexpr (D == 2)
+              lm = fminf(lm, d2_2(q.x, q.y, b.x, b.y));
+            else
+              lm = fminf(lm, d2_3(q.x, q.y, q.z, b.x, b.y, b.z));
+          }
+          if (COUNT) {
+            pairs += c;
+            ++leafv;
+          }
+        } else {
+          const float4* nd = S.nodes + 4 * (uint64_t) node;
+          const float4 n0 = nd[0], n1 = nd[1], n2 = nd[2], n3 = nd[3];
+          const float dL = box_min_d2<D>(q.x, q.y, q.z, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
+          const float dR = box_min_d2<D>(q.x, q.y, q.z, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+          const uint32_t left = __float_as_uint(n3.x), right = __float_as_uint(n3.y);
+          // Nearer child pushed last, so that it is popped first.
+          const bool wL = dL < m, wR = dR < m;
+          if (wL && wR) {
+            push0 = dL <= dR ? right : left;
+            push1 = dL <= dR ? left : right;
+            npush = 2;
+          } else if (wL || wR) {
+            push0 = wL ? left : right;
+            npush = 1;
+          }
+          if (COUNT) ++visits;
+        }
+      }
+      m = fminf(m, lm);
+#pragma unroll
+      for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+      // Compact the pushes: lanes in order, two slots per lane at most.
+      int off = npush;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xFFFFFFFFu, off, o);
+        if (lane >= o) off += v;
+      }
+      const int total = __shfl_sync(0xFFFFFFFFu, off, 31);
+      off -= npush;  // exclusive prefix
+      if (sp + total > kDeferStack) {
+        if (lane == 0) atomicOr(&S.sc->status, kErrInternal);
+        break;
+      }
+      if (npush > 0) st[sp + off] = push0;
+      if (npush > 1) st[sp + off + 1] = push1;
+      sp += total;
+      __syncwarp();
+      if ((++round & 15) == 0) thr = read_thr();
+    }
+    if (lane == 0 && m > threshold_of(ld_relaxed_u64(&S.sc->max_key)))
+      atomicMax(&S.sc->max_key, pack_max(m, __float_as_uint(q.w)));
+    __syncwarp();
+  }
+  if (COUNT) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      pairs += __shfl_xor_sync(0xFFFFFFFFu, pairs, o);
+      visits += __shfl_xor_sync(0xFFFFFFFFu, visits, o);
+      leafv += __shfl_xor_sync(0xFFFFFFFFu, leafv, o);
+    }
+    if (lane == 0 && (pairs || leafv || visits)) {
+      atomicAdd(&S.sc->pairs, pairs);
+      atomicAdd(&S.sc->nodes, visits);
+      atomicAdd(&S.sc->leaves, leafv);
+    }
+  }
 }
 
 __global__ void k_packet_pos(QuerySets qs) {
@@ -513,6 +667,10 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
   }
   void* ppos;
   if ((s = ensure(c, kBufSample, maxppos * 4, &ppos)) != HD_OK) return s;
+  // Deferred-query queues, one per direction.
+  void* defer;
+  if ((s = ensure(c, kBufHeavy, (uint64_t) count * kDeferCap * sizeof(Deferred), &defer)) != HD_OK)
+    return s;
   uint64_t off = 0, max_warps = 0, max_pos_threads = 0;
   for (int k = 0; k < count; ++k) {
     QuerySet& d = qs.d[k];
@@ -529,6 +687,8 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
     d.sc = scalars(c, ins[k].dir);
     d.qcodes = q[k]->codes;
     d.bcodes = t[k]->codes;
+    d.defer = (Deferred*) defer + (uint64_t) k * kDeferCap;
+    d.budget = c.opt.lbvh_budget;
     off += 2 * packets[k];
     max_warps = std::max<uint64_t>(max_warps, d.rows * pstride);
     max_pos_threads = std::max<uint64_t>(max_pos_threads, 2 * packets[k]);
@@ -551,6 +711,21 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
       k_lbvh_query<3, false><<<grid, kQueryWarps * 32, 0, c.stream>>>(qs);
   }
   if ((s = after_launch(c, "lbvh_query")) != HD_OK) return s;
+  // Queries queued by over-budget packets (usually none: the launch then
+  // returns at once).
+  const dim3 dgrid((unsigned) (c.num_sms * 4), count);
+  if (dims == 2) {
+    if (cnt)
+      k_lbvh_defer<2, true><<<dgrid, kDeferWarps * 32, 0, c.stream>>>(qs);
+    else
+      k_lbvh_defer<2, false><<<dgrid, kDeferWarps * 32, 0, c.stream>>>(qs);
+  } else {
+    if (cnt)
+      k_lbvh_defer<3, true><<<dgrid, kDeferWarps * 32, 0, c.stream>>>(qs);
+    else
+      k_lbvh_defer<3, false><<<dgrid, kDeferWarps * 32, 0, c.stream>>>(qs);
+  }
+  if ((s = after_launch(c, "lbvh_defer")) != HD_OK) return s;
   mark(c, 4);
   for (int k = 0; k < count; ++k)
     if ((s = certify(c, ins[k])) != HD_OK) return s;

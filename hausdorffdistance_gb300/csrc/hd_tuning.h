@@ -14,6 +14,7 @@ struct Tuning {
   unsigned batch_small_rows;  // batches: directions up to this many rows take one warp
   unsigned batch_chunk;       // batches: consecutive items per warp step
   unsigned batch_window;      // batches: half-width of the bound window
+  unsigned lbvh_budget;       // LBVH: per-packet visits before queries are deferred
 };
 
 const Tuning& tuning();

@@ -9,3 +9,4 @@
 #define HD_TUNED_BATCH_SMALL_ROWS 8192
 #define HD_TUNED_BATCH_CHUNK 16
 #define HD_TUNED_BATCH_WINDOW 4
+#define HD_TUNED_LBVH_BUDGET 256

@@ -88,7 +88,9 @@ typedef struct hd_options {
                            /* 0 = table                                        */
   uint32_t batch_window;   /* batches: half-width of the bound window (1..8);  */
                            /* 0 = table                                        */
-  uint32_t reserved[4];
+  uint32_t lbvh_budget;    /* LBVH: nodes + leaves a packet visits before its  */
+                           /* open queries go to the deferred pass; 0 = table */
+  uint32_t reserved[3];
 } hd_options;
 
 typedef struct hd_result {
@@ -106,7 +108,9 @@ typedef struct hd_result {
   int32_t variant_used;    /* hd_variant actually run (direction A->B)         */
   int32_t variant_used_ba; /* and for B->A when undirected                     */
   double err_bound;        /* BF16: bound on |approx - exact| squared distance */
-  uint64_t rechecked;      /* BF16: rows rechecked exactly in FP32             */
+  uint64_t rechecked;      /* BF16: rows rechecked exactly in FP32; LBVH:      */
+                           /* queries over the traversal budget (finished by  */
+                           /* the deferred pass)                               */
   uint64_t visited_leaves; /* index leaves / cells scanned (HD_COUNT_PAIRS)    */
   double sample_p80[2];    /* AUTO: 80th percentile of the sampled early-break */
                            /* iteration counts per direction (0 = no sample)   */

@@ -39,4 +39,20 @@ def test_batch_fit_and_table(tmp_path):
 def test_read_table_round_trip(tmp_path):
     sel = {"eb_ratio": 0.5, "eb_small_pairs": 1e6, "index_min_pairs": 4e6, "prefer_grid": True}
     autotune.write_table(sel, str(tmp_path / "t.h"))
-    assert autotune.read_table(str(tmp_path / "t.h")) == sel
+    got = autotune.read_table(str(tmp_path / "t.h"))
+    assert {k: got[k] for k in sel} == sel
+    # Schedule values not swept keep what the table holds.
+    autotune.write_table({**sel, "batch_chunk": 16, "lbvh_budget": 512}, str(tmp_path / "u.h"))
+    got = autotune.read_table(str(tmp_path / "u.h"))
+    assert got["batch_chunk"] == 16 and got["lbvh_budget"] == 512
+
+
+def test_budget_fit_and_table(tmp_path):
+    rows = [{"case": c, "lbvh_budget": b, "ms": t}
+            for c, ts in (("x", {128: 3.0, 256: 2.0, 512: 2.5}), ("y", {128: 1.0, 256: 1.5, 512: 1.0}))
+            for b, t in ts.items()]
+    p = autotune.fit_budget(rows)
+    assert p["lbvh_budget"] == 256 and p["lbvh_budget_total_ms"] == 3.5
+    sel = {"eb_ratio": 0, "eb_small_pairs": 0, "index_min_pairs": 0, "prefer_grid": False}
+    autotune.write_table({**sel, **p}, str(tmp_path / "t.h"))
+    assert "HD_TUNED_LBVH_BUDGET 256" in (tmp_path / "t.h").read_text()

@@ -125,3 +125,32 @@ def test_invalid_arguments_raise(engine):
     with pytest.raises(hd.HDError) as ei:
         engine.solve(np.ones((5, 5), np.float32), np.ones((5, 5), np.float32), variant="lbvh")
     assert ei.value.status == 5
+
+
+def tilted_plane_with_far_points(n=1_000_000, n_far=300, seed=31):
+    """A: points on the tilted plane z = (x + y) / 2 over the unit square
+    (axis-aligned boxes of its patches are mostly empty); B: the same points
+    re-noised plus n_far points 0.5 to 1 above the plane."""
+    rng = np.random.default_rng(seed)
+    xy = rng.random((n, 2))
+    a = np.column_stack([xy, 0.5 * (xy[:, 0] + xy[:, 1])]) + rng.normal(0, 1e-4, (n, 3))
+    b = a + rng.normal(0, 1e-4, (n, 3))
+    far = rng.random((n_far, 2))
+    lift = 0.5 + 0.5 * rng.random(n_far)
+    b[:n_far] = np.column_stack([far, 0.5 * (far[:, 0] + far[:, 1]) + lift])
+    return a.astype(np.float32), b.astype(np.float32)
+
+
+@pytest.mark.parametrize("undirected", [False, True])
+def test_lbvh_over_budget_queries(engine, undirected):
+    """Points far above a tilted plane: proving their nearest neighbour means
+    showing that a large ball touching many plane-patch boxes is empty, which
+    runs over the per-packet traversal budget; those queries are finished by
+    the deferred pass and the result stays exact."""
+    a, b = tilted_plane_with_far_points()
+    want = hd_oracle.hd_f32(b, a, undirected=undirected)
+    for count in (False, True):
+        r = engine.solve(b, a, undirected=undirected, variant="lbvh", count_pairs=count)
+        assert r.hd_f32 == want["hd_f32"]
+        check_pair(b, a, r, want["d2"])
+        assert r.rechecked > 0, "no query went over the traversal budget"
