@@ -210,7 +210,9 @@ constexpr float kMaxDistMargin = 1.0f + 1.0f / 65536.0f;
 
 // Warp-packet traversal.  A packet is 32 consecutive Morton-sorted queries
 // (or 32 entries of a sample list).
-template <int D, bool COUNT>
+// LT: leaf size known at compile time (16, the tuned size), or 0 for a
+// runtime leaf size L.
+template <int D, bool COUNT, int LT>
 __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, uint64_t nItems, uint32_t pstride,
                  uint64_t rows, const uint32_t* __restrict__ ppos,
                  const float4* __restrict__ nodes, const float4* __restrict__ B, uint64_t nB,
@@ -246,11 +248,46 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   // loads, four at a time); stops as soon as no lane still needs a point,
   // and lets lanes that found a point within the running maximum stop.
   auto scan_leaf = [&](uint32_t leaf) {
-    const uint64_t s = (uint64_t) leaf * L;
-    const int cnt = (int) min((uint64_t) L, nB - s);
+    const uint64_t s = (uint64_t) leaf * (LT ? (uint32_t) LT : L);
     const float4* lp = B + s;
     float m = cmin;
     int k = 0;
+    if (LT && s + LT <= nB) {
+      // Full leaf of a compile-time size: fixed offsets, no clamping.
+      bool settled = false;  // every active lane is within the running maximum
+#pragma unroll
+      for (int k0 = 0; k0 < (LT ? LT : 4); k0 += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const float4 b = __ldg(lp + k0 + u);
+          if constexpr (D == 2) {
+            m = fminf(m, d2_2(q.x, q.y, b.x, b.y));
+          } else {
+            m = fminf(m, d2_3(q.x, q.y, q.z, b.x, b.y, b.z));
+          }
+        }
+        k = k0 + 4;
+        if (!__any_sync(0xFFFFFFFFu, active && m > thr)) {
+          settled = true;
+          break;
+        }
+      }
+      if (active) cmin = m;
+      ++work;
+      if (COUNT) {
+        ++leafv;
+        pairs += (unsigned long long) k * __popc(__ballot_sync(0xFFFFFFFFu, active));
+      }
+      // The running maximum is re-read only when some lane is still open.
+      if (!settled) {
+        if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
+        thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
+      }
+      if (active && cmin <= thr) active = false;
+      return;
+    }
+    const int cnt = (int) min((uint64_t) L, nB - s);
+    bool settled = false;
     for (; k < cnt; k += 4) {
       // Every lane reads the same point: one broadcast load per point.
 #pragma unroll
@@ -264,6 +301,7 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
       }
       if (!__any_sync(0xFFFFFFFFu, active && m > thr)) {
         k += 4;
+        settled = true;
         break;
       }
     }
@@ -273,8 +311,10 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
       ++leafv;
       pairs += (unsigned long long) min(k, cnt) * __popc(__ballot_sync(0xFFFFFFFFu, active));
     }
-    if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
-    thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
+    if (!settled) {
+      if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
+      thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
+    }
     if (active && cmin <= thr) active = false;
   };
 
@@ -454,10 +494,10 @@ struct QuerySets {
   QuerySet d[2];
 };
 
-template <int D, bool COUNT>
+template <int D, bool COUNT, int LT>
 __global__ void __launch_bounds__(kQueryWarps * 32) k_lbvh_query(QuerySets qs) {
   const QuerySet& S = qs.d[blockIdx.y];
-  lbvh_query_body<D, COUNT>(S.Q, S.nQ, S.pstride, S.rows, S.ppos, S.nodes, S.B, S.nB, S.L, S.sc,
+  lbvh_query_body<D, COUNT, LT>(S.Q, S.nQ, S.pstride, S.rows, S.ppos, S.nodes, S.B, S.nB, S.L, S.sc,
                             S.defer, S.budget);
 }
 
@@ -699,17 +739,17 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
   mark(c, 3);
   const dim3 grid((unsigned) ((max_warps + kQueryWarps - 1) / kQueryWarps), count);
   const bool cnt = ins[0].count;
-  if (dims == 2) {
-    if (cnt)
-      k_lbvh_query<2, true><<<grid, kQueryWarps * 32, 0, c.stream>>>(qs);
-    else
-      k_lbvh_query<2, false><<<grid, kQueryWarps * 32, 0, c.stream>>>(qs);
-  } else {
-    if (cnt)
-      k_lbvh_query<3, true><<<grid, kQueryWarps * 32, 0, c.stream>>>(qs);
-    else
-      k_lbvh_query<3, false><<<grid, kQueryWarps * 32, 0, c.stream>>>(qs);
-  }
+  // Kernel per (n_dims, counting, leaf size 16 or any).
+  const bool l16 = bs.s[0].L == 16;
+  const void* fn;
+  if (dims == 2)
+    fn = cnt ? (l16 ? (const void*) k_lbvh_query<2, true, 16> : (const void*) k_lbvh_query<2, true, 0>)
+             : (l16 ? (const void*) k_lbvh_query<2, false, 16> : (const void*) k_lbvh_query<2, false, 0>);
+  else
+    fn = cnt ? (l16 ? (const void*) k_lbvh_query<3, true, 16> : (const void*) k_lbvh_query<3, true, 0>)
+             : (l16 ? (const void*) k_lbvh_query<3, false, 16> : (const void*) k_lbvh_query<3, false, 0>);
+  void* qargs[] = {&qs};
+  cudaLaunchKernel(fn, grid, dim3(kQueryWarps * 32), qargs, 0, c.stream);
   if ((s = after_launch(c, "lbvh_query")) != HD_OK) return s;
   // Queries queued by over-budget packets (usually none: the launch then
   // returns at once).
