@@ -517,9 +517,10 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   out->sample_p80[1] = undirected ? c->last_p80[1] : 0.0;
   out->err_bound = std::max(ex[0].err_bound, ex[1].err_bound);
   out->rechecked = ex[0].rechecked + ex[1].rechecked;
-  // LBVH: queries whose packet ran over the traversal budget.
+  // LBVH: queries whose packet ran over the traversal budget; EB: points
+  // deferred past the per-point pair cap.
   for (int d = 0; d < ndir; ++d)
-    if (used[d] == HD_VARIANT_LBVH) out->rechecked += h->s[d].heavy_count;
+    if (used[d] == HD_VARIANT_LBVH || used[d] == HD_VARIANT_EB) out->rechecked += h->s[d].heavy_count;
   if (c->timing) {
     float t = 0;
     if (cudaEventElapsedTime(&t, c->ev[24], c->ev[25]) == cudaSuccess) out->ms = t;

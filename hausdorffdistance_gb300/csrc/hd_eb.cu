@@ -111,7 +111,9 @@ __device__ __forceinline__ float tile_d2(float ax, float ay, float az,
   }
 }
 
-template <int D>
+// S: A points carried per thread (4 for large sets; 2 or 1 when the set is
+// too small to give every SM a full complement of 4-slot CTAs).
+template <int D, int S = kEbSlots>
 __global__ void __launch_bounds__(kEbThreads)
     k_eb_main(const float* __restrict__ A, Perm permA, uint64_t a_begin,
               uint64_t a_end, const typename EbPt<D>::T* __restrict__ Bp,
@@ -124,13 +126,13 @@ __global__ void __launch_bounds__(kEbThreads)
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
-  float ax[kEbSlots], ay[kEbSlots], az[kEbSlots], cm[kEbSlots];
-  uint32_t ia[kEbSlots], vis[kEbSlots];
-  bool act[kEbSlots];
+  float ax[S], ay[S], az[S], cm[S];
+  uint32_t ia[S], vis[S];
+  bool act[S];
   unsigned long long pairs = 0;
   bool exhausted = false;
 #pragma unroll
-  for (int r = 0; r < kEbSlots; ++r) {
+  for (int r = 0; r < S; ++r) {
     act[r] = false;
     ax[r] = ay[r] = az[r] = 0.0f;
     cm[r] = FLT_MAX;
@@ -141,10 +143,10 @@ __global__ void __launch_bounds__(kEbThreads)
   // Warp-aggregated refill of every free slot from the visit queue.
   auto refill = [&]() {
     if (exhausted) return;
-    uint32_t masks[kEbSlots];
+    uint32_t masks[S];
     uint32_t total = 0;
 #pragma unroll
-    for (int r = 0; r < kEbSlots; ++r) {
+    for (int r = 0; r < S; ++r) {
       masks[r] = __ballot_sync(0xFFFFFFFFu, !act[r]);
       total += __popc(masks[r]);
     }
@@ -155,7 +157,7 @@ __global__ void __launch_bounds__(kEbThreads)
     const uint32_t lt = (1u << lane) - 1u;
     uint32_t before = 0;
 #pragma unroll
-    for (int r = 0; r < kEbSlots; ++r) {
+    for (int r = 0; r < S; ++r) {
       if (!act[r]) {
         uint64_t v = a_begin + base + before + __popc(masks[r] & lt);
         if (v < a_end) {
@@ -209,7 +211,7 @@ __global__ void __launch_bounds__(kEbThreads)
       for (int p = 0; p < kEbTile / 2; ++p) {
         float4 b = t4[p];
 #pragma unroll
-        for (int r = 0; r < kEbSlots; ++r) {
+        for (int r = 0; r < S; ++r) {
           cm[r] = fminf(cm[r], d2_2(ax[r], ay[r], b.x, b.y));
           cm[r] = fminf(cm[r], d2_2(ax[r], ay[r], b.z, b.w));
         }
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(kEbThreads)
       for (int p = 0; p < kEbTile; ++p) {
         float4 b = tile[buf][p];
 #pragma unroll
-        for (int r = 0; r < kEbSlots; ++r)
+        for (int r = 0; r < S; ++r)
           cm[r] = fminf(cm[r], d2_3(ax[r], ay[r], az[r], b.x, b.y, b.z));
       }
     }
@@ -230,7 +232,7 @@ __global__ void __launch_bounds__(kEbThreads)
     key = __shfl_sync(0xFFFFFFFFu, key, 0);
     const float thr = threshold_of(key);
 #pragma unroll
-    for (int r = 0; r < kEbSlots; ++r) {
+    for (int r = 0; r < S; ++r) {
       if (!act[r]) continue;
       pairs += kEbTile;
       vis[r] += 1;
@@ -252,7 +254,7 @@ __global__ void __launch_bounds__(kEbThreads)
     refill();
     bool any = false;
 #pragma unroll
-    for (int r = 0; r < kEbSlots; ++r) any |= act[r];
+    for (int r = 0; r < S; ++r) any |= act[r];
     tcur = tnext;
     if (!__syncthreads_or(any)) break;
   }
@@ -291,7 +293,25 @@ __global__ void __launch_bounds__(kEbThreads)
     bool broke = false;
     while (done < h.remaining) {
       uint32_t step = min((uint32_t) kHeavyStepTiles, h.remaining - done);
-      for (uint32_t s = 0; s < step; ++s) {
+      uint32_t s = 0;
+      // Groups of 8 tiles: the 8 loads are issued before any is used.
+      for (; s + 8 <= step; s += 8) {
+        typename EbPt<D>::T b[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          b[u] = Bp[(uint64_t) t * kEbTile + tid];
+          t = (t + 1 == nTiles) ? 0 : t + 1;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if constexpr (D == 2) {
+            m = fminf(m, d2_2(ax, ay, b[u].x, b[u].y));
+          } else {
+            m = fminf(m, d2_3(ax, ay, az, b[u].x, b[u].y, b[u].z));
+          }
+        }
+      }
+      for (; s < step; ++s) {
         const auto b = Bp[(uint64_t) t * kEbTile + tid];
         if constexpr (D == 2) {
           m = fminf(m, d2_2(ax, ay, b.x, b.y));
@@ -357,16 +377,36 @@ hd_status run_eb_dim(Ctx& c, const DirInput& in) {
   if ((s = after_launch(c, "eb_seed")) != HD_OK) return s;
   mark(c, 3);
   if (in.nA > n_seed) {
-    int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_eb_main<D>, kEbThreads, 0);
-    occ = std::max(1, occ);
-    uint64_t per_cta = (uint64_t) kEbThreads * kEbSlots;
-    uint64_t want = (in.nA - n_seed + per_cta - 1) / per_cta;
+    // Slots per thread: the most (4, 2, 1) that still fill every resident CTA
+    // of a full grid, so that a small set spreads over all SMs instead of
+    // leaving most of them idle (every slot of a thread is computed).
+    const void* fns[3] = {(const void*) k_eb_main<D, 4>, (const void*) k_eb_main<D, 2>,
+                          (const void*) k_eb_main<D, 1>};
+    const int slots[3] = {4, 2, 1};
+    const uint64_t rest = in.nA - n_seed;
+    int pick = 2, occ = 1;
+    for (int k = 0; k < 3; ++k) {
+      int o = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fns[k], kEbThreads, 0);
+      o = std::max(1, o);
+      if (rest >= (uint64_t) c.num_sms * o * kEbThreads * slots[k] || k == 2) {
+        pick = k;
+        occ = o;
+        break;
+      }
+    }
+    const uint64_t per_cta = (uint64_t) kEbThreads * slots[pick];
+    const uint64_t want = (rest + per_cta - 1) / per_cta;
     int grid = (int) std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t) c.num_sms * occ));
     uint32_t capTiles = std::max<uint32_t>(1, kCapPairs / kEbTile);
-    k_eb_main<D><<<grid, kEbThreads, 0, c.stream>>>(in.A, pA, n_seed, in.nA, (const PT*) pb,
-                                                    nTiles, capTiles, sc,
-                                                    (HeavyEntry*) ph, (uint32_t) in.nA);
+    const float* a_ptr = in.A;
+    const PT* b_ptr = (const PT*) pb;
+    HeavyEntry* h_ptr = (HeavyEntry*) ph;
+    uint32_t heavy_cap = (uint32_t) in.nA;
+    uint64_t a_begin = n_seed, a_end = in.nA;
+    void* args[] = {&a_ptr, &pA, &a_begin, &a_end, &b_ptr, (void*) &nTiles, &capTiles, &sc,
+                    &h_ptr, &heavy_cap};
+    cudaLaunchKernel(fns[pick], dim3(grid), dim3(kEbThreads), args, 0, c.stream);
     if ((s = after_launch(c, "eb_main")) != HD_OK) return s;
     mark(c, 4);
     k_eb_heavy<D><<<c.num_sms * 4, kEbThreads, 0, c.stream>>>(
@@ -455,13 +495,13 @@ cudaError_t noalloc_direction(cudaStream_t st, int num_sms, const float* A, uint
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (nA > n_seed) {
     int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_eb_main<D>, kEbThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_eb_main<D, kEbSlots>, kEbThreads, 0);
     occ = std::max(1, occ);
     const uint64_t per_cta = (uint64_t) kEbThreads * kEbSlots;
     const uint64_t want = (nA - n_seed + per_cta - 1) / per_cta;
     const int g = (int) std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t) num_sms * occ));
     const uint32_t capTiles = std::max<uint32_t>(1, kCapPairs / kEbTile);
-    k_eb_main<D><<<g, kEbThreads, 0, st>>>(A, pA, n_seed, nA, pb, nTiles, capTiles, sc, heavy,
+    k_eb_main<D, kEbSlots><<<g, kEbThreads, 0, st>>>(A, pA, n_seed, nA, pb, nTiles, capTiles, sc, heavy,
                                            (uint32_t) kNoAllocMaxPoints);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     k_eb_heavy<D><<<num_sms * 4, kEbThreads, 0, st>>>(A, pA, pb, nTiles, sc, heavy, 0,

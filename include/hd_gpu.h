@@ -110,7 +110,8 @@ typedef struct hd_result {
   double err_bound;        /* BF16: bound on |approx - exact| squared distance */
   uint64_t rechecked;      /* BF16: rows rechecked exactly in FP32; LBVH:      */
                            /* queries over the traversal budget (finished by  */
-                           /* the deferred pass)                               */
+                           /* the deferred pass); EB: points deferred past    */
+                           /* the per-point pair cap                           */
   uint64_t visited_leaves; /* index leaves / cells scanned (HD_COUNT_PAIRS)    */
   double sample_p80[2];    /* AUTO: 80th percentile of the sampled early-break */
                            /* iteration counts per direction (0 = no sample)   */
