@@ -16,7 +16,9 @@
 //    that stops — its running minimum at or below the running maximum (early
 //    break), a full cycle over B (completed: atomicMax), or more than the
 //    per-point cap of tiles (deferred) — is refilled at the next tile boundary
-//    from a global visit queue with one warp-aggregated atomicAdd.  Because
+//    from a global visit queue with one warp-aggregated atomicAdd; once the
+//    queue is drained and at most 1/8 of a CTA's threads still hold a point,
+//    those points are deferred too and the CTA retires.  Because
 //    B's visit order is a pseudo-random permutation, a slot may start at any
 //    tile and wrap around: no slot waits for a CTA-wide restart.
 //  * Deferred ("heavy") points — the ones whose nearest neighbour is farther
@@ -256,7 +258,25 @@ __global__ void __launch_bounds__(kEbThreads)
 #pragma unroll
     for (int r = 0; r < S; ++r) any |= act[r];
     tcur = tnext;
-    if (!__syncthreads_or(any)) break;
+    const int busy = __syncthreads_count(any);  // threads with an active slot
+    if (busy == 0) break;
+    if (busy * 8 <= kEbThreads && __syncthreads_and(exhausted)) {
+      // Nothing left to refill from and at most 1/8 of the threads busy:
+      // every thread would keep computing for a few stragglers, so hand
+      // them to the per-point kernel (all 256 threads on one point) instead.
+#pragma unroll
+      for (int r = 0; r < S; ++r) {
+        if (!act[r]) continue;
+        uint32_t s = atomicAdd(&sc->heavy_count, 1u);
+        if (s < heavy_cap) {
+          heavy[s] = HeavyEntry{ia[r], tcur, nTiles - vis[r], cm[r]};
+        } else {
+          atomicOr(&sc->status, kErrQueueOverflow);
+        }
+        act[r] = false;
+      }
+      break;
+    }
   }
   // One prefetch is still in flight (issued at the top of the last
   // iteration); wait for it so the CTA never exits with a copy pending.
