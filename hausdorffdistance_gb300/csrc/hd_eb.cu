@@ -47,7 +47,7 @@ constexpr int kEbThreads = 256;
 constexpr int kEbTile = 256;          // B points per tile (== kEbThreads)
 constexpr int kEbSlots = 4;           // A points carried per thread
 constexpr int kHeavyStepTiles = 32;   // tiles between CTA reductions (heavy)
-constexpr uint32_t kCapPairs = 32768; // per-point pairs before deferral
+constexpr uint32_t kCapPairs = 8192;  // per-point pairs before deferral
 constexpr uint32_t kWaitLimit = 1u << 26;
 
 template <int D>
