@@ -313,32 +313,35 @@ __global__ void __launch_bounds__(kEbThreads)
     bool broke = false;
     while (done < h.remaining) {
       uint32_t step = min((uint32_t) kHeavyStepTiles, h.remaining - done);
-      uint32_t s = 0;
-      // Groups of 8 tiles: the 8 loads are issued before any is used.
-      for (; s + 8 <= step; s += 8) {
-        typename EbPt<D>::T b[8];
+      // The round's tiles are t .. t+step-1 around the ring: at most two
+      // contiguous runs, each walked with one pointer (fixed load offsets,
+      // groups of 8 loads issued before any is used).
+      for (uint32_t k = 0; k < step;) {
+        const uint32_t run = min(step - k, nTiles - t);
+        const typename EbPt<D>::T* p = Bp + (uint64_t) t * kEbTile + tid;
+        uint32_t u = 0;
+        for (; u + 8 <= run; u += 8, p += 8 * kEbTile) {
+          typename EbPt<D>::T b[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          b[u] = Bp[(uint64_t) t * kEbTile + tid];
-          t = (t + 1 == nTiles) ? 0 : t + 1;
-        }
+          for (int v = 0; v < 8; ++v) b[v] = p[v * kEbTile];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          if constexpr (D == 2) {
-            m = fminf(m, d2_2(ax, ay, b[u].x, b[u].y));
-          } else {
-            m = fminf(m, d2_3(ax, ay, az, b[u].x, b[u].y, b[u].z));
+          for (int v = 0; v < 8; ++v) {
+            if constexpr (D == 2)
+              m = fminf(m, d2_2(ax, ay, b[v].x, b[v].y));
+            else
+              m = fminf(m, d2_3(ax, ay, az, b[v].x, b[v].y, b[v].z));
           }
         }
-      }
-      for (; s < step; ++s) {
-        const auto b = Bp[(uint64_t) t * kEbTile + tid];
-        if constexpr (D == 2) {
-          m = fminf(m, d2_2(ax, ay, b.x, b.y));
-        } else {
-          m = fminf(m, d2_3(ax, ay, az, b.x, b.y, b.z));
+        for (; u < run; ++u, p += kEbTile) {
+          const auto b = *p;
+          if constexpr (D == 2)
+            m = fminf(m, d2_2(ax, ay, b.x, b.y));
+          else
+            m = fminf(m, d2_3(ax, ay, az, b.x, b.y, b.z));
         }
-        t = (t + 1 == nTiles) ? 0 : t + 1;
+        k += run;
+        t += run;
+        if (t == nTiles) t = 0;
       }
       done += step;
       pairs += step;
