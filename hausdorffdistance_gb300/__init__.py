@@ -58,7 +58,7 @@ class Engine:
                  sample_rate: float = 0.01, n_points_cell: int = 8, leaf_size: int = 16,
                  eb_only_threshold: int = 0, always_sample: bool = False,
                  batch_small_rows: int = 0, batch_chunk: int = 0, batch_window: int = 0,
-                 lbvh_budget: int = 0):
+                 lbvh_budget: int = 0, eb_cap_pairs: int = 0):
         self.lib = _lib.load()
         opt = _lib.Options()
         self.lib.hd_default_options(ctypes.byref(opt))
@@ -74,6 +74,7 @@ class Engine:
         opt.batch_chunk = batch_chunk            # 0: tuned table value
         opt.batch_window = batch_window          # 0: tuned table value
         opt.lbvh_budget = lbvh_budget            # 0: tuned table value
+        opt.eb_cap_pairs = eb_cap_pairs          # 0: tuned table value
         h = ctypes.c_void_p()
         st = self.lib.hd_create(ctypes.byref(h), ctypes.byref(opt))
         if st != _lib.HD_OK:

@@ -45,7 +45,7 @@ class Options(ctypes.Structure):
                 ("eb_only_threshold", ctypes.c_uint32), ("always_sample", ctypes.c_uint32),
                 ("batch_small_rows", ctypes.c_uint32), ("batch_chunk", ctypes.c_uint32),
                 ("batch_window", ctypes.c_uint32), ("lbvh_budget", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 3)]
+                ("eb_cap_pairs", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
 
 
 class Result(ctypes.Structure):

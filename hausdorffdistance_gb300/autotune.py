@@ -138,6 +138,7 @@ BATCH_CHUNKS = (8, 16)
 BATCH_WINDOWS = (1, 2, 4)
 BATCH_DEFAULT = {"batch_small_rows": 8192, "batch_chunk": 8, "batch_window": 4}
 LBVH_BUDGET_DEFAULT = 256
+EB_CAP_DEFAULT = {"eb_cap_div": 512, "eb_cap_min": 4096, "eb_cap_max": 65536}
 LBVH_BUDGETS = (128, 256, 512, 1024, 4096)
 
 
@@ -223,7 +224,9 @@ def read_table(path):
            "index_min_pairs": float(vals["INDEX_MIN_PAIRS"]),
            "eb_ratio": float(vals["EB_RATIO"]), "prefer_grid": vals["PREFER_GRID"] != "0"}
     for key, name in (("batch_small_rows", "BATCH_SMALL_ROWS"), ("batch_chunk", "BATCH_CHUNK"),
-                      ("batch_window", "BATCH_WINDOW"), ("lbvh_budget", "LBVH_BUDGET")):
+                      ("batch_window", "BATCH_WINDOW"), ("lbvh_budget", "LBVH_BUDGET"),
+                      ("eb_cap_div", "EB_CAP_DIV"), ("eb_cap_min", "EB_CAP_MIN"),
+                      ("eb_cap_max", "EB_CAP_MAX")):
         if name in vals:
             out[key] = int(vals[name])
     return out
@@ -246,6 +249,9 @@ def write_table(params, path):
         f.write(f"#define HD_TUNED_BATCH_WINDOW "
                 f"{params.get('batch_window', BATCH_DEFAULT['batch_window'])}\n")
         f.write(f"#define HD_TUNED_LBVH_BUDGET {params.get('lbvh_budget', LBVH_BUDGET_DEFAULT)}\n")
+        for key, name in (("eb_cap_div", "EB_CAP_DIV"), ("eb_cap_min", "EB_CAP_MIN"),
+                          ("eb_cap_max", "EB_CAP_MAX")):
+            f.write(f"#define HD_TUNED_{name} {params.get(key, EB_CAP_DEFAULT[key])}\n")
 
 
 def main():

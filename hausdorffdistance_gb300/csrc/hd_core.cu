@@ -356,6 +356,7 @@ hd_status hd_create(hd_ctx** out, const hd_options* opt) {
   if (c->opt.batch_window == 0) c->opt.batch_window = tuning().batch_window;
   c->opt.batch_window = std::max<uint32_t>(1, std::min<uint32_t>(c->opt.batch_window, 8));
   if (c->opt.lbvh_budget == 0) c->opt.lbvh_budget = tuning().lbvh_budget;
+  // eb_cap_pairs 0: per solve, from |B| (see run_eb_dim).
   int n = 0;
   cudaError_t e = cudaGetDeviceCount(&n);
   if (e != cudaSuccess || n == 0 || c->opt.device < 0 || c->opt.device >= n) {

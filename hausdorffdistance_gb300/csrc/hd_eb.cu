@@ -39,6 +39,7 @@
 
 #include "hd_common.cuh"
 #include "hd_internal.h"
+#include "hd_tuning.h"
 
 namespace hdg {
 namespace {
@@ -47,7 +48,7 @@ constexpr int kEbThreads = 256;
 constexpr int kEbTile = 256;          // B points per tile (== kEbThreads)
 constexpr int kEbSlots = 4;           // A points carried per thread
 constexpr int kHeavyStepTiles = 32;   // tiles between CTA reductions (heavy)
-constexpr uint32_t kCapPairs = 8192;  // per-point pairs before deferral
+constexpr uint32_t kCapPairs = 8192;  // per-point pairs before deferral (no-alloc entry point)
 constexpr uint32_t kWaitLimit = 1u << 26;
 
 template <int D>
@@ -421,7 +422,14 @@ hd_status run_eb_dim(Ctx& c, const DirInput& in) {
     const uint64_t per_cta = (uint64_t) kEbThreads * slots[pick];
     const uint64_t want = (rest + per_cta - 1) / per_cta;
     int grid = (int) std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t) c.num_sms * occ));
-    uint32_t capTiles = std::max<uint32_t>(1, kCapPairs / kEbTile);
+    // Pairs a point scans before it is paused (deferred): an option, else
+    // clamp(|B| / div, min, max) from the tuning table.  Pausing is not only
+    // a tail guard: a paused point resumes under a higher running maximum.
+    uint64_t cap = c.opt.eb_cap_pairs;
+    if (cap == 0)
+      cap = std::min<uint64_t>(std::max<uint64_t>(in.nB / tuning().eb_cap_div, tuning().eb_cap_min),
+                               tuning().eb_cap_max);
+    uint32_t capTiles = (uint32_t) std::max<uint64_t>(1, cap / kEbTile);
     const float* a_ptr = in.A;
     const PT* b_ptr = (const PT*) pb;
     HeavyEntry* h_ptr = (HeavyEntry*) ph;

@@ -15,6 +15,7 @@ struct Tuning {
   unsigned batch_chunk;       // batches: consecutive items per warp step
   unsigned batch_window;      // batches: half-width of the bound window
   unsigned lbvh_budget;       // LBVH: per-packet visits before queries are deferred
+  unsigned eb_cap_div, eb_cap_min, eb_cap_max;  // EB deferral cap: clamp(|B| / div, min, max)
 };
 
 const Tuning& tuning();

@@ -90,7 +90,10 @@ typedef struct hd_options {
                            /* 0 = table                                        */
   uint32_t lbvh_budget;    /* LBVH: nodes + leaves a packet visits before its  */
                            /* open queries go to the deferred pass; 0 = table */
-  uint32_t reserved[3];
+  uint32_t eb_cap_pairs;   /* EB: pairs a point scans in the persistent kernel */
+                           /* before it is deferred (>= 256); 0 = from |B| by */
+                           /* the tuning table                                 */
+  uint32_t reserved[2];
 } hd_options;
 
 typedef struct hd_result {
