@@ -491,10 +491,12 @@ def main():
         t_ms = phase_avg[3]
         tag = "lbvh_query" if res.variant_used == hd._lib.VARIANT_LBVH else "grid_query"
         achieved = alg / (t_ms / 1e3) / 1e9
-        # One query launch per direction covers all of that direction's
-        # queries: per-launch figures.
-        nl = 2 if undirected else 1
-        tr = traffic_from_profiles(tag, float(n))
+        # An undirected LBVH solve answers both directions' queries in one
+        # launch (the fused pass); otherwise one launch per direction.
+        fused = (undirected and res.variant_used == hd._lib.VARIANT_LBVH
+                 and res.variant_used_ba == hd._lib.VARIANT_LBVH)
+        nl = 1 if (fused or not undirected) else 2
+        tr = traffic_from_profiles(tag, float(n) * (2 if fused else 1))
         roof = {"bound": "hbm", "kernel": tag, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "traffic": tr,
                 "algorithmic_bytes_per_launch": alg / nl, "kernel_ms_per_launch": t_ms / nl,
