@@ -154,3 +154,22 @@ def test_lbvh_over_budget_queries(engine, undirected):
         assert r.hd_f32 == want["hd_f32"]
         check_pair(b, a, r, want["d2"])
         assert r.rechecked > 0, "no query went over the traversal budget"
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_schedule_options_do_not_change_results(dims):
+    """The LBVH traversal budget and the EB deferral cap only move work
+    between kernels: every value, extreme ones included, gives the oracle's
+    result."""
+    import hausdorffdistance_gb300 as hd
+    rng = np.random.default_rng(60 + dims)
+    a = rng.random((30_000, dims)).astype(np.float32)
+    b = (a[rng.permutation(len(a))] + rng.normal(0, 1e-3, a.shape)).astype(np.float32)
+    b[:300] = rng.random((300, dims)).astype(np.float32) * 1.5
+    want = hd_oracle.hd_f32(a, b, undirected=True)["hd_f32"]
+    for budget in (1, 256, 1 << 30):
+        with hd.Engine(lbvh_budget=budget) as e:
+            assert e.solve(a, b, undirected=True, variant="lbvh").hd_f32 == want, budget
+    for cap in (256, 4096, 1 << 30):
+        with hd.Engine(eb_cap_pairs=cap) as e:
+            assert e.solve(a, b, undirected=True, variant="eb").hd_f32 == want, cap
