@@ -133,7 +133,7 @@ def fit(rows):
             "total_ms_oracle_choice": sum(min(r["eb"], r["lbvh"], r["grid"]) for r in rows)}
 
 
-BATCH_SMALL_ROWS = (4096, 8192)
+BATCH_SMALL_ROWS = (4096, 8192, 16384, 65536)
 BATCH_CHUNKS = (8, 16)
 BATCH_WINDOWS = (1, 2, 4)
 BATCH_DEFAULT = {"batch_small_rows": 8192, "batch_chunk": 8, "batch_window": 4}

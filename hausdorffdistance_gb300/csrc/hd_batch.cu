@@ -58,6 +58,7 @@ constexpr int kShortScan = 64;   // pairs a row scans alone before it is queued
 constexpr int kSlots = 8;        // seed rows per problem-direction (row mod 8)
 constexpr int kLongIlp = 8;      // independent loads per lane per long-pass round
 constexpr int kSmallMax = 65536; // largest one-warp threshold accepted
+constexpr int kBestFirst = 32;    // one-warp path: exact best-first scans before the sweep
 constexpr int kSeedGroup = 8;    // items per seed stripe
 constexpr uint64_t kLongCap = 1ull << 21;  // queued long rows at most
 constexpr uint32_t kNoSeed = 0xFFFFFFFFu;  // empty seed minimum (above every float)
@@ -534,63 +535,83 @@ __device__ __forceinline__ void small_direction(const BatchArgs& a, uint32_t p, 
   const uint32_t w0 = ny > 2 * a.window + 1 ? 2 * a.window + 1 : ny;
   const uint32_t half = w0 >> 1;
 
-  // Window bounds; each lane keeps the largest bound of its own rows (all in
-  // class lane % kSlots).
-  unsigned long long cls = 0;
+  // Window bounds, one per row (an upper bound on the row's nearest-neighbour
+  // distance); each row is read back only by the lane that wrote it.
   for (uint32_t row = lane; row < nx; row += 32) {
     uint32_t j = scan_start(row, ratio, ny, half);
-    const float u = scan_run<D>(X, row, Y, j, ny, w0, INFINITY);
-    wb[row] = u;
-    const unsigned long long kk = pack_max(u, row);
-    cls = kk > cls ? kk : cls;
-  }
-#pragma unroll
-  for (int o = 16; o >= kSlots; o >>= 1) {
-    const unsigned long long v = __shfl_xor_sync(0xFFFFFFFFu, cls, o);
-    cls = v > cls ? v : cls;
-  }
-
-  // Seeds: exact nearest-neighbour distances of the class maxima.
-  float x[kSlots][D];
-  uint32_t rows[kSlots];
-  float m[kSlots];
-#pragma unroll
-  for (int k = 0; k < kSlots; ++k) {
-    const unsigned long long u = __shfl_sync(0xFFFFFFFFu, cls, k);
-    rows[k] = u ? unpack_max_index(u) : 0xFFFFFFFFu;
-    const uint32_t r = u ? rows[k] : 0;
-#pragma unroll
-    for (int t = 0; t < D; ++t) x[k][t] = X[(uint64_t) r * D + t];
-    m[k] = INFINITY;
-  }
-#pragma unroll 4
-  for (uint32_t j = lane; j < ny; j += 32) {
-    float y[D];
-#pragma unroll
-    for (int t = 0; t < D; ++t) y[t] = Y[(uint64_t) j * D + t];
-#pragma unroll
-    for (int k = 0; k < kSlots; ++k) {
-      if constexpr (D == 2)
-        m[k] = fminf(m[k], d2_2(x[k][0], x[k][1], y[0], y[1]));
-      else
-        m[k] = fminf(m[k], d2_3(x[k][0], x[k][1], x[k][2], y[0], y[1], y[2]));
-    }
-  }
-  unsigned long long best = 0;
-#pragma unroll
-  for (int k = 0; k < kSlots; ++k) {
-    const float v = warp_min(m[k]);
-    if (rows[k] != 0xFFFFFFFFu) {
-      const unsigned long long kk = pack_max(v, rows[k]);
-      best = kk > best ? kk : best;
-    }
+    wb[row] = scan_run<D>(X, row, Y, j, ny, w0, INFINITY);
   }
   __syncwarp();
-  float thr = threshold_of(best);
+
+  // Best first: the row with the largest bound gets an exact scan (lanes
+  // split the other set, early break once the row cannot raise the maximum),
+  // then the next, until no bound exceeds the maximum — every other row is
+  // then settled by its bound alone.  A scanned row's bound is set to -1.
+  // After kBestFirst rows the sweep below settles the rest.
+  unsigned long long best = 0;
+  float thr = -1.0f;
+  bool all_settled = false;
+  for (int it = 0; it < kBestFirst; ++it) {
+    unsigned long long cand = 0;
+    for (uint32_t row = lane; row < nx; row += 32) {
+      const float u = wb[row];
+      if (u > thr) {
+        const unsigned long long kk = pack_max(u, row);
+        cand = kk > cand ? kk : cand;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const unsigned long long v = __shfl_xor_sync(0xFFFFFFFFu, cand, o);
+      cand = v > cand ? v : cand;
+    }
+    if (cand == 0) {
+      all_settled = true;
+      break;
+    }
+    const uint32_t r = unpack_max_index(cand);
+    float xr[D];
+#pragma unroll
+    for (int t = 0; t < D; ++t) xr[t] = X[(uint64_t) r * D + t];
+    float cm = __uint_as_float((uint32_t) (cand >> 32));  // its bound: a real distance
+    bool broke = false;
+    for (uint64_t t0 = 0; t0 < ny; t0 += 32 * kLongIlp) {
+      float y[kLongIlp][D];
+#pragma unroll
+      for (int u = 0; u < kLongIlp; ++u) {
+        const uint64_t jj = t0 + (uint64_t) u * 32 + lane;
+#pragma unroll
+        for (int k = 0; k < D; ++k) y[u][k] = jj < ny ? Y[jj * D + k] : INFINITY;
+      }
+#pragma unroll
+      for (int u = 0; u < kLongIlp; ++u) {
+        const uint64_t jj = t0 + (uint64_t) u * 32 + lane;
+        float d2;
+        if constexpr (D == 2)
+          d2 = d2_2(xr[0], xr[1], y[u][0], y[u][1]);
+        else
+          d2 = d2_3(xr[0], xr[1], xr[2], y[u][0], y[u][1], y[u][2]);
+        if (jj < ny) cm = fminf(cm, d2);
+      }
+      if (warp_min(cm) <= thr) {
+        broke = true;
+        break;
+      }
+    }
+    if (!broke) {
+      const unsigned long long kr = pack_max(warp_min(cm), r);
+      if (kr > best) {
+        best = kr;
+        thr = threshold_of(best);
+      }
+    }
+    if (lane == (int) (r & 31)) wb[r] = -1.0f;
+    __syncwarp();
+  }
 
   // Sweep.
   const uint32_t limit = ny < (uint32_t) kShortScan ? ny : (uint32_t) kShortScan;
-  for (uint32_t row0 = 0; row0 < nx; row0 += 32) {
+  for (uint32_t row0 = 0; !all_settled && row0 < nx; row0 += 32) {
     const uint32_t row = row0 + lane;
     const bool valid = row < nx;
     float cmin = valid ? wb[row] : 0.0f;
