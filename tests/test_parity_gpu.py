@@ -173,3 +173,17 @@ def test_schedule_options_do_not_change_results(dims):
     for cap in (256, 4096, 1 << 30):
         with hd.Engine(eb_cap_pairs=cap) as e:
             assert e.solve(a, b, undirected=True, variant="eb").hd_f32 == want, cap
+
+
+def test_lbvh_budget_one_defers_every_open_query():
+    """Budget 1: every packet with a query still open after its warm-start
+    leaves queues it for the deferred pass (up to the queue's 65,536 per
+    direction; any beyond finish in their own packets).  The result is
+    unchanged and the deferred count is reported."""
+    import hausdorffdistance_gb300 as hd
+    a, b = synth.uniform2d(150_000, seed=9)
+    want = hd_oracle.hd_f32(a, b, undirected=True)["hd_f32"]
+    with hd.Engine(lbvh_budget=1) as e:
+        r = e.solve(a, b, undirected=True, variant="lbvh")
+    assert r.hd_f32 == want
+    assert r.rechecked > 0
