@@ -52,6 +52,7 @@ hd_status ensure(Ctx& c, BufSlot slot, size_t bytes, void** out) {
     // Grow geometrically so that repeated solves of slightly larger inputs
     // do not reallocate every call.
     size_t want = std::max(bytes, b.bytes + b.bytes / 4);
+    ++c.buf_gen;
     cudaError_t e = cudaMalloc(&b.p, want);
     if (e != cudaSuccess) {
       (void) cudaGetLastError();
@@ -401,6 +402,7 @@ hd_status hd_destroy(hd_ctx* c) {
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
+  if (c->solve_graph) cudaGraphExecDestroy(c->solve_graph);
   if (c->batch_fork) cudaEventDestroy(c->batch_fork);
   if (c->batch_join) cudaEventDestroy(c->batch_join);
   if (c->batch_side) cudaStreamDestroy(c->batch_side);
@@ -470,19 +472,79 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
     }
   }
   const bool fused = undirected && used[0] == HD_VARIANT_LBVH && used[1] == HD_VARIANT_LBVH;
-  if (fused) {
-    // Fused undirected pass: one sort of both sets, both trees and both
-    // directions' queries in shared launches.
-    c->ev_base = 0;
-    mark(*c, 0);
-    if ((s = run_lbvh_pair(*c, ins[0], ins[1])) != HD_OK) return s;
-    mark(*c, 6);
-  } else {
-    for (int d = 0; d < ndir; ++d) {
-      c->ev_base = 12 * d;
+  auto run_all = [&]() -> hd_status {
+    hd_status r;
+    if (fused) {
+      // Fused undirected pass: one sort of both sets, both trees and both
+      // directions' queries in shared launches.
+      c->ev_base = 0;
       mark(*c, 0);
-      if ((s = run_direction(*c, ins[d], used[d], &used[d], &ex[d])) != HD_OK) return s;
+      if ((r = run_lbvh_pair(*c, ins[0], ins[1])) != HD_OK) return r;
       mark(*c, 6);
+    } else {
+      for (int d = 0; d < ndir; ++d) {
+        c->ev_base = 12 * d;
+        mark(*c, 0);
+        if ((r = run_direction(*c, ins[d], used[d], &used[d], &ex[d])) != HD_OK) return r;
+        mark(*c, 6);
+      }
+    }
+    return HD_OK;
+  };
+  // LBVH and EB solves launch a fixed kernel sequence with no host read-back
+  // before the result: the second identical solve in a row is captured into
+  // a CUDA graph and later ones replay it (no per-kernel launch cost).
+  // Timed solves (HD_TIMING) always launch directly.
+  auto graphable = [&](int v) { return v == HD_VARIANT_LBVH || v == HD_VARIANT_EB; };
+  const bool eligible = !c->timing && graphable(used[0]) && (!undirected || graphable(used[1]));
+  const uint64_t key[11] = {(uint64_t) dA, (uint64_t) dB, n_a, n_b, (uint64_t) n_dims, flags,
+                            (uint64_t) (int64_t) used[0], (uint64_t) (int64_t) used[1],
+                            (uint64_t) c->stream, c->buf_gen, 1};
+  static_assert(sizeof(key) == sizeof(c->solve_key), "solve key size");
+  const bool same = std::memcmp(key, c->solve_key, sizeof(key)) == 0;
+  cudaError_t ge;
+  if (eligible && same && c->solve_graph_valid) {
+    if ((ge = cudaGraphLaunch(c->solve_graph, c->stream)) != cudaSuccess)
+      return cuda_fail(*c, ge, "solve graph launch");
+    c->launches += c->solve_graph_launches;
+  } else if (eligible && same && c->solve_key_seen) {
+    // Second identical solve: capture it (buffers are already allocated by
+    // the first, so the sequence makes no allocation), then launch.
+    const uint64_t l0 = c->launches;
+    cudaGraph_t graph = nullptr;
+    if ((ge = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+      return cuda_fail(*c, ge, "begin solve capture");
+    s = run_all();
+    ge = cudaStreamEndCapture(c->stream, &graph);
+    cudaGraphExec_t exec = nullptr;
+    if (s == HD_OK && ge == cudaSuccess) ge = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (s != HD_OK || ge != cudaSuccess) {
+      // Something in the sequence cannot be captured (for example a buffer
+      // that has to grow): nothing ran, so run it directly and stop trying.
+      cudaGetLastError();
+      c->last_error.clear();
+      c->launches = l0;
+      c->solve_key_seen = false;
+      c->solve_graph_valid = false;
+      if ((s = run_all()) != HD_OK) return s;
+    } else {
+      if (c->solve_graph) cudaGraphExecDestroy(c->solve_graph);
+      c->solve_graph = exec;
+      c->solve_graph_valid = true;
+      c->solve_graph_launches = c->launches - l0;
+      if ((ge = cudaGraphLaunch(c->solve_graph, c->stream)) != cudaSuccess)
+        return cuda_fail(*c, ge, "solve graph launch");
+    }
+  } else {
+    if ((s = run_all()) != HD_OK) return s;
+    if (eligible) {
+      // The run may have (re)allocated buffers: key the graph on the
+      // generation they now have.
+      std::memcpy(c->solve_key, key, sizeof(key));
+      c->solve_key[9] = c->buf_gen;
+      c->solve_key_seen = true;
+      c->solve_graph_valid = false;
     }
   }
   HostScalars* h = reinterpret_cast<HostScalars*>(c->host_pinned);

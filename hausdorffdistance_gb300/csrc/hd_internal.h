@@ -111,6 +111,15 @@ struct Ctx {
   // captured for (reused while the shape, buffers and stream are unchanged).
   cudaGraphExec_t batch_graph = nullptr;
   cudaStream_t batch_side = nullptr;  // side branch of the batch graph's capture
+  // Single solves: the kernel sequence of an LBVH or EB solve is captured the
+  // second time the same shape runs back to back and replayed while it stays
+  // the same (pointers, sizes, flags, chosen variants, stream, buffers).
+  cudaGraphExec_t solve_graph = nullptr;
+  uint64_t solve_key[11] = {};
+  bool solve_key_seen = false;      // solve_key ran once uncaptured
+  bool solve_graph_valid = false;   // solve_graph replays solve_key
+  uint64_t solve_graph_launches = 0;
+  uint64_t buf_gen = 0;             // bumped by every (re)allocation
   cudaEvent_t batch_fork = nullptr, batch_join = nullptr;
   uint64_t batch_key[16] = {};
   // Per-solve cache: the Morton-sorted sets (slot 0 = call's A, 1 = call's B)

@@ -187,3 +187,30 @@ def test_lbvh_budget_one_defers_every_open_query():
         r = e.solve(a, b, undirected=True, variant="lbvh")
     assert r.hd_f32 == want
     assert r.rechecked > 0
+
+
+@pytest.mark.parametrize("variant", ["lbvh", "eb"])
+@pytest.mark.parametrize("undirected", [False, True])
+def test_repeated_solves_replay_a_graph(variant, undirected):
+    """The second identical solve in a row is captured into a CUDA graph and
+    later ones replay it: results stay exact when the same buffers are
+    refilled with new points, for device and host inputs."""
+    torch = pytest.importorskip("torch")
+    import hausdorffdistance_gb300 as hd
+    rng = np.random.default_rng(70)
+    n = 20_000
+    with hd.Engine() as e:
+        ta = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+        tb = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+        for rep in range(5):
+            a = rng.random((n, 3)).astype(np.float32)
+            b = (a + rng.normal(0, 1e-3, a.shape)).astype(np.float32)
+            b[rep * 7] += np.float32(0.3 + 0.1 * rep)  # a different maximiser each time
+            want = hd_oracle.hd_f32(a, b, undirected=undirected)["hd_f32"]
+            ta.copy_(torch.from_numpy(a))
+            tb.copy_(torch.from_numpy(b))
+            assert e.solve(ta, tb, undirected=undirected, variant=variant).hd_f32 == want, rep
+            assert e.solve(a, b, undirected=undirected, variant=variant).hd_f32 == want, rep
+            launches = e.kernel_launches
+            assert e.solve(ta, tb, undirected=undirected, variant=variant).hd_f32 == want, rep
+            assert e.kernel_launches > launches
