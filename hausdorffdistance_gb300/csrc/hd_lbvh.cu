@@ -101,7 +101,8 @@ __device__ __forceinline__ uint32_t node_id(uint32_t ref, uint32_t nI) {
 }
 
 // Bottom-up boxes: a thread per leaf climbs; the second child to arrive at a
-// parent computes its box (Karras 2012, section 4).
+// parent computes its box (Karras 2012, section 4) and writes the packed node
+// (4 float4: both children's boxes and refs).
 // Box of node `id`: leaves' boxes come from the sorted set's gather pass,
 // internal boxes from this build (written by other threads: read around L1).
 __device__ __forceinline__ void node_box(uint32_t id, uint32_t nI, const float4* boxes,
@@ -120,9 +121,20 @@ __device__ __forceinline__ void bottom_up_body(const uint2* __restrict__ child,
                                                const uint32_t* __restrict__ parent, uint32_t nL,
                                                uint32_t nI, float4* boxes,
                                                const float4* __restrict__ leaf_boxes,
-                                               uint32_t* flags) {
+                                               uint32_t* flags, float4* __restrict__ nodes) {
   uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
-  if (leaf >= nL || nI == 0) return;
+  if (nI == 0) {
+    // Single leaf: a root whose right child is an empty box (never visited).
+    if (leaf == 0) {
+      const float4 lo = leaf_boxes[0], hi = leaf_boxes[1];
+      nodes[0] = make_float4(lo.x, lo.y, lo.z, hi.x);
+      nodes[1] = make_float4(hi.y, hi.z, FLT_MAX, FLT_MAX);
+      nodes[2] = make_float4(FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX);
+      nodes[3] = make_float4(__uint_as_float(kLeafBit), __uint_as_float(kLeafBit), 0.f, 0.f);
+    }
+    return;
+  }
+  if (leaf >= nL) return;
   uint32_t node = nI + leaf;
   for (;;) {
     uint32_t p = parent[node];
@@ -138,39 +150,15 @@ __device__ __forceinline__ void bottom_up_body(const uint2* __restrict__ child,
     float4 hi = make_float4(fmaxf(ahi.x, bhi.x), fmaxf(ahi.y, bhi.y), fmaxf(ahi.z, bhi.z), 0.f);
     __stcg(&boxes[2 * (uint64_t) p], lo);
     __stcg(&boxes[2 * (uint64_t) p + 1], hi);
+    // The packed node the query reads: both children's boxes and refs.
+    float4* o = nodes + 4 * (uint64_t) p;
+    o[0] = make_float4(alo.x, alo.y, alo.z, ahi.x);
+    o[1] = make_float4(ahi.y, ahi.z, blo.x, blo.y);
+    o[2] = make_float4(blo.z, bhi.x, bhi.y, bhi.z);
+    o[3] = make_float4(__uint_as_float(ch.x), __uint_as_float(ch.y), 0.f, 0.f);
     if (p == 0) return;
     node = p;
   }
-}
-
-// Packs every internal node as 4 float4: both children's boxes and refs.
-__device__ __forceinline__ void pack_nodes_body(const uint2* __restrict__ child,
-                                                const float4* __restrict__ boxes,
-                                                const float4* __restrict__ leaf_boxes, uint32_t nI,
-                                                float4* __restrict__ nodes) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (nI == 0) {
-    // Single leaf: a root whose right child is an empty box (never visited).
-    if (i == 0) {
-      float4 lo = leaf_boxes[0], hi = leaf_boxes[1];
-      nodes[0] = make_float4(lo.x, lo.y, lo.z, hi.x);
-      nodes[1] = make_float4(hi.y, hi.z, FLT_MAX, FLT_MAX);
-      nodes[2] = make_float4(FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX);
-      nodes[3] = make_float4(__uint_as_float(kLeafBit), __uint_as_float(kLeafBit), 0.f, 0.f);
-    }
-    return;
-  }
-  if (i >= nI) return;
-  uint2 ch = child[i];
-  uint32_t a = node_id(ch.x, nI), b = node_id(ch.y, nI);
-  float4 alo, ahi, blo, bhi;
-  node_box(a, nI, boxes, leaf_boxes, &alo, &ahi);
-  node_box(b, nI, boxes, leaf_boxes, &blo, &bhi);
-  float4* o = nodes + 4 * (uint64_t) i;
-  o[0] = make_float4(alo.x, alo.y, alo.z, ahi.x);
-  o[1] = make_float4(ahi.y, ahi.z, blo.x, blo.y);
-  o[2] = make_float4(blo.z, bhi.x, bhi.y, bhi.z);
-  o[3] = make_float4(__uint_as_float(ch.x), __uint_as_float(ch.y), 0.f, 0.f);
 }
 
 // Squared distance from p to the box [lo, hi] (0 inside), rounded exactly
@@ -467,11 +455,7 @@ __global__ void k_karras(BuildSets b) {
 }
 __global__ void k_bottom_up(BuildSets b) {
   const BuildSet& S = b.s[blockIdx.y];
-  bottom_up_body(S.child, S.parent, S.nL, S.nI, S.boxes, S.leaf_boxes, S.flags);
-}
-__global__ void k_pack_nodes(BuildSets b) {
-  const BuildSet& S = b.s[blockIdx.y];
-  pack_nodes_body(S.child, S.boxes, S.leaf_boxes, S.nI, S.nodes);
+  bottom_up_body(S.child, S.parent, S.nL, S.nI, S.boxes, S.leaf_boxes, S.flags, S.nodes);
 }
 
 struct QuerySet {
@@ -681,9 +665,7 @@ static hd_status build_lbvhs(Ctx& c, const SortedSet* const* sets, int count, Bu
   cudaError_t e = cudaMemsetAsync(flags_base, 0, internal_total * 4, c.stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "memset flags");
   k_bottom_up<<<gl, 256, 0, c.stream>>>(*out);
-  if ((s = after_launch(c, "bottom_up")) != HD_OK) return s;
-  k_pack_nodes<<<gi, 256, 0, c.stream>>>(*out);
-  return after_launch(c, "pack_nodes");
+  return after_launch(c, "bottom_up");
 }
 
 // Directed LBVH solves of `count` directions (1, or 2 for an undirected solve)
