@@ -1044,12 +1044,7 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
                             (uint64_t) L.off, total,   maxpairs,        long_cap,
                             (uint64_t) c.stream, small_rows, chunk, c.opt.batch_window};
   static_assert(sizeof(key) == sizeof(c.batch_key), "batch key size");
-  if (!c.batch_side) {
-    if ((e = cudaStreamCreateWithFlags(&c.batch_side, cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaEventCreateWithFlags(&c.batch_fork, cudaEventDisableTiming)) != cudaSuccess ||
-        (e = cudaEventCreateWithFlags(&c.batch_join, cudaEventDisableTiming)) != cudaSuccess)
-      return cuda_fail(c, e, "batch side stream");
-  }
+  if ((s = ensure_side(c)) != HD_OK) return s;
   if (!c.batch_graph || std::memcmp(key, c.batch_key, sizeof(key)) != 0) {
     if ((s = capture_batch_graph(c, g)) != HD_OK) return s;
     std::memcpy(c.batch_key, key, sizeof(key));

@@ -78,6 +78,16 @@ hd_status after_launch(Ctx& c, const char* what) {
   return HD_OK;
 }
 
+hd_status ensure_side(Ctx& c) {
+  if (c.batch_side) return HD_OK;
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&c.batch_side, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&c.batch_fork, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&c.batch_join, cudaEventDisableTiming)) != cudaSuccess)
+    return cuda_fail(c, e, "side stream");
+  return HD_OK;
+}
+
 DevScalars* scalars(Ctx& c, int dir) {
   return reinterpret_cast<DevScalars*>(c.bufs[kBufScalars].p) + dir;
 }

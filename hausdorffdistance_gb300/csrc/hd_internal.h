@@ -110,7 +110,9 @@ struct Ctx {
   // Batched solve: the last instantiated graph and the launch shape it was
   // captured for (reused while the shape, buffers and stream are unchanged).
   cudaGraphExec_t batch_graph = nullptr;
-  cudaStream_t batch_side = nullptr;  // side branch of the batch graph's capture
+  // Side stream and fork/join events (created on first use): the batch
+  // graph's second branch and the LBVH packet positions beside the build.
+  cudaStream_t batch_side = nullptr;
   // Single solves: the kernel sequence of an LBVH or EB solve is captured the
   // second time the same shape runs back to back and replayed while it stays
   // the same (pointers, sizes, flags, chosen variants, stream, buffers).
@@ -162,6 +164,8 @@ hd_status ensure(Ctx& c, BufSlot slot, size_t bytes, void** out);
 
 // Counts a kernel launch and checks for launch errors.
 hd_status after_launch(Ctx& c, const char* what);
+// Creates the context's side stream and fork/join events on first use.
+hd_status ensure_side(Ctx& c);
 
 DevScalars* scalars(Ctx& c, int dir);
 

@@ -678,9 +678,6 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
   for (int k = 0; k < count; ++k)
     if ((s = spatial_prepare(c, ins[k], &q[k], &t[k])) != HD_OK) return s;
   mark(c, 1);
-  BuildSets bs;
-  if ((s = build_lbvhs(c, t, count, &bs)) != HD_OK) return s;
-  mark(c, 2);
   QuerySets qs;
   uint64_t packets[2], maxppos = 0;
   for (int k = 0; k < count; ++k) {
@@ -693,31 +690,46 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
   void* defer;
   if ((s = ensure(c, kBufHeavy, (uint64_t) count * kDeferCap * sizeof(Deferred), &defer)) != HD_OK)
     return s;
-  uint64_t off = 0, max_warps = 0, max_pos_threads = 0;
+  if ((s = ensure_side(c)) != HD_OK) return s;
+  uint64_t off = 0, max_pos_threads = 0;
   for (int k = 0; k < count; ++k) {
     QuerySet& d = qs.d[k];
-    const uint32_t pstride = packets[k] >= 4096 ? 64 : (packets[k] >= 256 ? 16 : 1);
     d.Q = q[k]->pts;
     d.nQ = q[k]->n;
-    d.pstride = pstride;
-    d.rows = (packets[k] + pstride - 1) / pstride;
     d.ppos = (const uint32_t*) ppos + off;
-    d.nodes = bs.s[k].nodes;
     d.B = t[k]->pts;
     d.nB = t[k]->n;
-    d.L = bs.s[k].L;
-    d.sc = scalars(c, ins[k].dir);
     d.qcodes = q[k]->codes;
     d.bcodes = t[k]->codes;
-    d.defer = (Deferred*) defer + (uint64_t) k * kDeferCap;
-    d.budget = c.opt.lbvh_budget;
     off += 2 * packets[k];
-    max_warps = std::max<uint64_t>(max_warps, d.rows * pstride);
     max_pos_threads = std::max<uint64_t>(max_pos_threads, 2 * packets[k]);
   }
   if (count == 1) qs.d[1] = qs.d[0];
-  k_packet_pos<<<dim3((unsigned) ((max_pos_threads + 255) / 256), count), 256, 0, c.stream>>>(qs);
+  // Packet positions need only the sorted codes: they run on the side
+  // stream while the (latency-bound) tree build runs on the main one.
+  cudaEventRecord(c.batch_fork, c.stream);
+  cudaStreamWaitEvent(c.batch_side, c.batch_fork, 0);
+  k_packet_pos<<<dim3((unsigned) ((max_pos_threads + 255) / 256), count), 256, 0, c.batch_side>>>(qs);
   if ((s = after_launch(c, "packet_pos")) != HD_OK) return s;
+  cudaEventRecord(c.batch_join, c.batch_side);
+  BuildSets bs;
+  if ((s = build_lbvhs(c, t, count, &bs)) != HD_OK) return s;
+  mark(c, 2);
+  cudaStreamWaitEvent(c.stream, c.batch_join, 0);
+  uint64_t max_warps = 0;
+  for (int k = 0; k < count; ++k) {
+    QuerySet& d = qs.d[k];
+    const uint32_t pstride = packets[k] >= 4096 ? 64 : (packets[k] >= 256 ? 16 : 1);
+    d.pstride = pstride;
+    d.rows = (packets[k] + pstride - 1) / pstride;
+    d.nodes = bs.s[k].nodes;
+    d.L = bs.s[k].L;
+    d.sc = scalars(c, ins[k].dir);
+    d.defer = (Deferred*) defer + (uint64_t) k * kDeferCap;
+    d.budget = c.opt.lbvh_budget;
+    max_warps = std::max<uint64_t>(max_warps, d.rows * pstride);
+  }
+  if (count == 1) qs.d[1] = qs.d[0];
   mark(c, 3);
   const dim3 grid((unsigned) ((max_warps + kQueryWarps - 1) / kQueryWarps), count);
   const bool cnt = ins[0].count;
