@@ -129,3 +129,17 @@ def test_batch_schedules_agree():
         with hd.Engine(batch_small_rows=small, batch_chunk=chunk, batch_window=window) as eng:
             out = eng.solve_batch(a, b, off, off, undirected=True)
         assert np.array_equal(out["hd_f32"], np.array(want, np.float32)), (small, chunk, window)
+
+
+def test_batch_threshold_boundary_and_many_tiny_problems(engine):
+    """Sizes straddling the tuned one-warp threshold (4096 rows) in the same
+    batch as 200,000 problems of 1 to 3 points."""
+    rng = np.random.default_rng(77)
+    sizes = [4095, 4096, 4097, 8191] + list(rng.integers(1, 4, size=200_000))
+    a, b, off = synth.polylines(sizes=sizes, seed=78)
+    out = engine.solve_batch(a, b, off, off, undirected=True)
+    check = list(range(4)) + list(rng.integers(4, len(sizes), size=300))
+    for p in check:
+        x, y = a[off[p]:off[p + 1]], b[off[p]:off[p + 1]]
+        want = hd_oracle.hd_f32(x, y, undirected=True)
+        assert out["hd_f32"][p] == want["hd_f32"], p
