@@ -625,7 +625,7 @@ hd_status hd_debug_bf16_rowmin(hd_ctx* c, const float* A, uint64_t n_a, const fl
   c->timing = false;
   c->sorted_valid = false;
   hd_status s;
-  const float *dA, *dB;
+  const float *dA = nullptr, *dB = nullptr;
   if ((s = copy_in(*c, A, n_a, n_dims, kBufA, &dA)) != HD_OK) return s;
   if ((s = copy_in(*c, B, n_b, n_dims, kBufB, &dB)) != HD_OK) return s;
   if ((s = init_scalars(*c)) != HD_OK) return s;
