@@ -134,25 +134,31 @@ class Engine:
         array with fields hd_f32, ia, ib, direction."""
         pa, na, da, deva, ka = _as_points(A, "A")
         pb, nb, db, devb, kb = _as_points(B, "B")
-        oa = np.asarray(offsets_a, np.int64)
-        ob = np.asarray(offsets_b, np.int64)
+        oa = np.ascontiguousarray(offsets_a, np.int64)
+        ob = np.ascontiguousarray(offsets_b, np.int64)
         n = len(oa) - 1
         if len(ob) - 1 != n:
             raise ValueError("offsets_a and offsets_b must describe the same number of problems")
-        # hd_problem rows: offset_a, n_a, offset_b, n_b (uint64; negative
-        # counts wrap to huge values and are rejected by the library).
-        probs = np.empty((n, 4), np.int64)
-        probs[:, 0] = oa[:-1]
-        np.subtract(oa[1:], oa[:-1], out=probs[:, 1])
-        probs[:, 2] = ob[:-1]
-        np.subtract(ob[1:], ob[:-1], out=probs[:, 3])
         out = np.empty(n, dtype=[("hd_f32", "<f4"), ("ia", "<u4"), ("ib", "<u4"),
                                  ("direction", "<i4")])
         flags = (HD_UNDIRECTED if undirected else 0) | (HD_DEVICE_PTRS if deva else 0)
-        fn = self.lib.hd_solve_batch_plain if plain else self.lib.hd_solve_batch
-        st = fn(self._h, ctypes.c_void_p(pa), na, ctypes.c_void_p(pb), nb, da,
-                probs.ctypes.data_as(ctypes.POINTER(_lib.Problem)), n, flags,
-                out.ctypes.data_as(ctypes.POINTER(_lib.BatchResult)))
+        res = out.ctypes.data_as(ctypes.POINTER(_lib.BatchResult))
+        if plain:
+            # hd_problem rows: offset_a, n_a, offset_b, n_b (uint64; negative
+            # counts wrap to huge values and are rejected by the library).
+            probs = np.empty((n, 4), np.int64)
+            probs[:, 0] = oa[:-1]
+            np.subtract(oa[1:], oa[:-1], out=probs[:, 1])
+            probs[:, 2] = ob[:-1]
+            np.subtract(ob[1:], ob[:-1], out=probs[:, 3])
+            st = self.lib.hd_solve_batch_plain(
+                self._h, ctypes.c_void_p(pa), na, ctypes.c_void_p(pb), nb, da,
+                probs.ctypes.data_as(ctypes.POINTER(_lib.Problem)), n, flags, res)
+        else:
+            # Offsets go to the library as they are (int64 viewed as uint64).
+            st = self.lib.hd_solve_batch_offsets(
+                self._h, ctypes.c_void_p(pa), na, ctypes.c_void_p(pb), nb, da,
+                ctypes.c_void_p(oa.ctypes.data), ctypes.c_void_p(ob.ctypes.data), n, flags, res)
         del ka, kb
         self._check(st)
         return out

@@ -33,7 +33,8 @@ HD_TIMING = 8
 
 # Every symbol include/hd_gpu.h declares.
 EXPORTED = ["hd_default_options", "hd_create", "hd_destroy", "hd_set_stream",
-            "hd_solve", "hd_solve_batch", "hd_solve_batch_plain", "hd_last_error",
+            "hd_solve", "hd_solve_batch", "hd_solve_batch_offsets", "hd_solve_batch_plain",
+            "hd_last_error",
             "hd_status_string", "hd_kernel_launches", "hd_version", "hd_solve_eb_noalloc",
             "hd_debug_bf16_rowmin"]
 
@@ -106,6 +107,10 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
                       ctypes.POINTER(Problem), ctypes.c_uint64, ctypes.c_uint32,
                       ctypes.POINTER(BatchResult)]
         f.restype = ctypes.c_int
+    lib.hd_solve_batch_offsets.argtypes = [P, P, ctypes.c_uint64, P, ctypes.c_uint64,
+                                           ctypes.c_int, P, P, ctypes.c_uint64, ctypes.c_uint32,
+                                           ctypes.POINTER(BatchResult)]
+    lib.hd_solve_batch_offsets.restype = ctypes.c_int
     lib.hd_last_error.argtypes = [P]
     lib.hd_last_error.restype = ctypes.c_char_p
     lib.hd_status_string.argtypes = [ctypes.c_int]

@@ -800,9 +800,31 @@ __global__ void k_batch_finalize(const PD* __restrict__ pd, uint32_t nprob, int 
   out[p] = hd_batch_result{__fsqrt_rn(w.d2), w.ia, w.ib, win};
 }
 
-hd_status check_problems(Ctx& c, const hd_problem* probs, uint64_t n, uint64_t ta, uint64_t tb) {
+// The problems of a batch, given either as an hd_problem array or as two
+// offset arrays (problem i owns rows oa[i]..oa[i+1] of A and ob[i]..ob[i+1]
+// of B; a decreasing pair gives a huge count, rejected as out of range).
+struct ProblemSource {
+  const hd_problem* probs = nullptr;
+  const uint64_t* oa = nullptr;
+  const uint64_t* ob = nullptr;
+  hd_problem get(uint64_t i) const {
+    if (probs) return probs[i];
+    return hd_problem{oa[i], oa[i + 1] - oa[i], ob[i], ob[i + 1] - ob[i]};
+  }
+};
+
+// Problems from offsets, on the device (one thread per problem).
+__global__ void k_probs_from_offsets(const uint64_t* __restrict__ oa,
+                                     const uint64_t* __restrict__ ob, uint64_t n,
+                                     hd_problem* __restrict__ probs) {
+  const uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  probs[i] = hd_problem{oa[i], oa[i + 1] - oa[i], ob[i], ob[i + 1] - ob[i]};
+}
+
+hd_status check_problems(Ctx& c, const ProblemSource& src, uint64_t n, uint64_t ta, uint64_t tb) {
   for (uint64_t i = 0; i < n; ++i) {
-    const hd_problem& p = probs[i];
+    const hd_problem p = src.get(i);
     if (p.n_a == 0 || p.n_b == 0)
       return fail(c, HD_ERR_INVALID_ARG, "problem " + std::to_string(i) + " has an empty set");
     if (p.offset_a > ta || p.n_a > ta - p.offset_a || p.offset_b > tb || p.n_b > tb - p.offset_b)
@@ -902,20 +924,21 @@ hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
 }  // namespace
 
 hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, uint64_t total_b,
-                      int dims, const hd_problem* probs, uint64_t n, uint32_t flags,
+                      int dims, const ProblemSource& src, uint64_t n, uint32_t flags,
                       hd_batch_result* out) {
-  if (!A || !B || !probs || !out || n == 0) return fail(c, HD_ERR_INVALID_ARG, "bad arguments");
+  if (!A || !B || !(src.probs || (src.oa && src.ob)) || !out || n == 0)
+    return fail(c, HD_ERR_INVALID_ARG, "bad arguments");
   if (dims != 2 && dims != 3) return fail(c, HD_ERR_UNSUPPORTED, "batches need n_dims 2 or 3");
   if (n >= 0xFFFFFFFFull) return fail(c, HD_ERR_INVALID_ARG, "too many problems");
   if (flags & ~(HD_UNDIRECTED | HD_DEVICE_PTRS)) return fail(c, HD_ERR_INVALID_ARG, "bad flags");
   hd_status s;
-  if ((s = check_problems(c, probs, n, total_a, total_b)) != HD_OK) return s;
+  if ((s = check_problems(c, src, n, total_a, total_b)) != HD_OK) return s;
   const int ndir = (flags & HD_UNDIRECTED) ? 2 : 1;
   const uint32_t small_rows = std::min<uint32_t>(c.opt.batch_small_rows, kSmallMax);
   const uint32_t chunk = std::max<uint32_t>(1, c.opt.batch_chunk);
   uint64_t total = 0, rows = 0, maxpairs = 0;
   for (uint64_t i = 0; i < n; ++i) {
-    const hd_problem& p = probs[i];
+    const hd_problem p = src.get(i);
     total += large_items(p.n_a, small_rows) + (ndir == 2 ? large_items(p.n_b, small_rows) : 0);
     rows += p.n_a + (ndir == 2 ? p.n_b : 0);
     maxpairs = std::max<uint64_t>(maxpairs, p.n_a * p.n_b);
@@ -953,6 +976,7 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   const size_t o_wb_a = L.take(total_a * 4);
   const size_t o_wb_b = L.take(ndir == 2 ? total_b * 4 : 0);
   const size_t o_probs = L.take(n * sizeof(hd_problem));
+  const size_t o_offs = L.take(src.probs ? 0 : 2 * (n + 1) * 8);
   g.o_pkeys = L.take(n * 8);
   g.o_pkeys2 = L.take(n * 8);
   g.o_pvals = L.take(n * 4);
@@ -987,9 +1011,22 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
     dA = (const float*) pa;
     dB = (const float*) pb;
   }
-  if ((e = cudaMemcpyAsync(at(o_probs), probs, n * sizeof(hd_problem), cudaMemcpyHostToDevice,
-                           c.stream)) != cudaSuccess)
-    return cuda_fail(c, e, "copy problems");
+  if (src.probs) {
+    if ((e = cudaMemcpyAsync(at(o_probs), src.probs, n * sizeof(hd_problem),
+                             cudaMemcpyHostToDevice, c.stream)) != cudaSuccess)
+      return cuda_fail(c, e, "copy problems");
+  } else {
+    uint64_t* d_oa = (uint64_t*) at(o_offs);
+    uint64_t* d_ob = d_oa + (n + 1);
+    if ((e = cudaMemcpyAsync(d_oa, src.oa, (n + 1) * 8, cudaMemcpyHostToDevice, c.stream)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(d_ob, src.ob, (n + 1) * 8, cudaMemcpyHostToDevice, c.stream)) !=
+            cudaSuccess)
+      return cuda_fail(c, e, "copy offsets");
+    k_probs_from_offsets<<<(unsigned) ((n + 255) / 256), 256, 0, c.stream>>>(
+        d_oa, d_ob, n, (hd_problem*) at(o_probs));
+    if ((s = after_launch(c, "problems from offsets")) != HD_OK) return s;
+  }
 
   BatchArgs& args = g.args;
   args.A = dA;
@@ -1070,7 +1107,7 @@ hd_status batch_solve_plain(Ctx& c, const float* A, uint64_t total_a, const floa
   if (dims != 2 && dims != 3) return fail(c, HD_ERR_UNSUPPORTED, "batches need n_dims 2 or 3");
   if (flags & ~(HD_UNDIRECTED | HD_DEVICE_PTRS)) return fail(c, HD_ERR_INVALID_ARG, "bad flags");
   hd_status s;
-  if ((s = check_problems(c, probs, n, total_a, total_b)) != HD_OK) return s;
+  if ((s = check_problems(c, ProblemSource{probs}, n, total_a, total_b)) != HD_OK) return s;
   const uint32_t solve_flags = (flags & HD_UNDIRECTED) | HD_DEVICE_PTRS;
   const float* dA = A;
   const float* dB = B;
@@ -1108,7 +1145,21 @@ hd_status hd_solve_batch(hd_ctx* c, const float* A, uint64_t total_a, const floa
   if (!c) return HD_ERR_INVALID_ARG;
   c->last_error.clear();
   cudaSetDevice(c->device);
-  return batch_solve(*c, A, total_a, B, total_b, n_dims, probs, n_problems, flags, out);
+  return batch_solve(*c, A, total_a, B, total_b, n_dims, ProblemSource{probs}, n_problems, flags,
+                     out);
+}
+
+hd_status hd_solve_batch_offsets(hd_ctx* c, const float* A, uint64_t total_a, const float* B,
+                                 uint64_t total_b, int n_dims, const uint64_t* offsets_a,
+                                 const uint64_t* offsets_b, uint64_t n_problems, uint32_t flags,
+                                 hd_batch_result* out) {
+  if (!c) return HD_ERR_INVALID_ARG;
+  c->last_error.clear();
+  cudaSetDevice(c->device);
+  ProblemSource src;
+  src.oa = offsets_a;
+  src.ob = offsets_b;
+  return batch_solve(*c, A, total_a, B, total_b, n_dims, src, n_problems, flags, out);
 }
 
 hd_status hd_solve_batch_plain(hd_ctx* c, const float* A, uint64_t total_a, const float* B,

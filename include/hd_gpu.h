@@ -170,6 +170,17 @@ HD_API hd_status hd_solve_batch(hd_ctx* ctx, const float* A, uint64_t total_a,
                          const hd_problem* probs, uint64_t n_problems,
                          uint32_t flags, hd_batch_result* out);
 
+/* The same batched solve with the problems given as offsets: problem i owns
+ * rows offsets_a[i] .. offsets_a[i+1]-1 of A and offsets_b[i] ..
+ * offsets_b[i+1]-1 of B (n_problems + 1 entries each, host memory).  Saves
+ * building an hd_problem array; the problems are expanded on the device.
+ * Decreasing offsets or empty problems are rejected (HD_ERR_INVALID_ARG).
+ * No counterpart in the reference. */
+HD_API hd_status hd_solve_batch_offsets(hd_ctx* ctx, const float* A, uint64_t total_a,
+                                 const float* B, uint64_t total_b, int n_dims,
+                                 const uint64_t* offsets_a, const uint64_t* offsets_b,
+                                 uint64_t n_problems, uint32_t flags, hd_batch_result* out);
+
 /* Same batch computed with one plain early-break launch per problem and
  * direction (the per-pair baseline the batched form is compared against). */
 HD_API hd_status hd_solve_batch_plain(hd_ctx* ctx, const float* A, uint64_t total_a,

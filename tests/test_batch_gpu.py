@@ -143,3 +143,27 @@ def test_batch_threshold_boundary_and_many_tiny_problems(engine):
         x, y = a[off[p]:off[p + 1]], b[off[p]:off[p + 1]]
         want = hd_oracle.hd_f32(x, y, undirected=True)
         assert out["hd_f32"][p] == want["hd_f32"], p
+
+
+def test_batch_problem_array_abi_matches_offsets(engine):
+    """hd_solve_batch (an hd_problem array) and hd_solve_batch_offsets (two
+    offset arrays, what Engine.solve_batch calls) give the same results."""
+    import ctypes
+    from hausdorffdistance_gb300 import _lib
+    a, b, off = small_batch(200, seed=47)
+    offb = np.concatenate([[0], np.cumsum(np.maximum(np.diff(off) - 3, 1))])
+    bb = np.concatenate([b[off[p]:off[p] + (offb[p + 1] - offb[p])] for p in range(len(off) - 1)])
+    via_offsets = engine.solve_batch(a, bb, off, offb, undirected=True)
+    n = len(off) - 1
+    probs = (_lib.Problem * n)()
+    for i in range(n):
+        probs[i].offset_a, probs[i].n_a = int(off[i]), int(off[i + 1] - off[i])
+        probs[i].offset_b, probs[i].n_b = int(offb[i]), int(offb[i + 1] - offb[i])
+    out = np.empty(n, dtype=via_offsets.dtype)
+    st = engine.lib.hd_solve_batch(engine._h, ctypes.c_void_p(a.ctypes.data), len(a),
+                                   ctypes.c_void_p(bb.ctypes.data), len(bb), 2, probs, n,
+                                   _lib.HD_UNDIRECTED,
+                                   out.ctypes.data_as(ctypes.POINTER(_lib.BatchResult)))
+    assert st == _lib.HD_OK
+    assert np.array_equal(out["hd_f32"], via_offsets["hd_f32"])
+    assert np.array_equal(out["direction"], via_offsets["direction"])
