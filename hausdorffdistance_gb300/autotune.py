@@ -133,8 +133,8 @@ def fit(rows):
             "total_ms_oracle_choice": sum(min(r["eb"], r["lbvh"], r["grid"]) for r in rows)}
 
 
-BATCH_SMALL_ROWS = (4096, 8192, 16384, 65536)
-BATCH_CHUNKS = (8, 16)
+BATCH_SMALL_ROWS = (512, 1024, 2048, 4096, 8192)
+BATCH_CHUNKS = (8,)
 BATCH_WINDOWS = (1, 2, 4)
 BATCH_DEFAULT = {"batch_small_rows": 8192, "batch_chunk": 8, "batch_window": 4}
 LBVH_BUDGET_DEFAULT = 256

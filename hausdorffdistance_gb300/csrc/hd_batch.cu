@@ -59,6 +59,7 @@ constexpr int kSlots = 8;        // seed rows per problem-direction (row mod 8)
 constexpr int kLongIlp = 8;      // independent loads per lane per long-pass round
 constexpr int kSmallMax = 65536; // largest one-warp threshold accepted
 constexpr int kBestFirst = 32;    // one-warp path: exact best-first scans before the sweep
+constexpr uint32_t kPipeRows = 65536;  // directions above this many rows use the multi-pass pipeline
 constexpr int kSeedGroup = 8;    // items per seed stripe
 constexpr uint64_t kLongCap = 1ull << 21;  // queued long rows at most
 constexpr uint32_t kNoSeed = 0xFFFFFFFFu;  // empty seed minimum (above every float)
@@ -94,9 +95,10 @@ __device__ __forceinline__ float pt_d2(const float* __restrict__ X, uint64_t i,
 __device__ __host__ __forceinline__ uint64_t items_of(uint64_t n) { return (n + 31) / 32; }
 
 // Items of a direction whose query set has nx rows in the multi-pass
-// pipeline: directions of at most small_rows rows go to the one-warp path.
-__device__ __host__ __forceinline__ uint64_t large_items(uint64_t nx, uint32_t small_rows) {
-  return nx > (uint64_t) small_rows ? items_of(nx) : 0;
+// pipeline: directions of at most pipe_rows rows go to the CTA or one-warp
+// path.
+__device__ __host__ __forceinline__ uint64_t large_items(uint64_t nx, uint32_t pipe_rows) {
+  return nx > (uint64_t) pipe_rows ? items_of(nx) : 0;
 }
 
 // Walks the items of the multi-pass pipeline in plan order: (sorted problem
@@ -109,7 +111,7 @@ struct Cursor {
   const uint32_t* order;
   uint32_t nprob;
   int ndir;
-  uint32_t small_rows;
+  uint32_t pipe_rows;  // directions above this many rows are the pipeline's items
   uint32_t r, p;
   int d;
   uint64_t item, nitems, it0, it1;
@@ -119,8 +121,8 @@ struct Cursor {
     r = rank;
     p = order[rank];
     pr = probs[p];
-    it0 = large_items(pr.n_a, small_rows);
-    it1 = ndir == 2 ? large_items(pr.n_b, small_rows) : 0;
+    it0 = large_items(pr.n_a, pipe_rows);
+    it1 = ndir == 2 ? large_items(pr.n_b, pipe_rows) : 0;
   }
   __device__ void init(uint64_t w, const uint64_t* __restrict__ prefix) {
     uint32_t lo = 0, hi = nprob;  // prefix[lo] <= w < prefix[hi]
@@ -178,6 +180,8 @@ struct BatchArgs {
   unsigned long long* long_count;
   uint64_t long_cap;
   uint32_t small_rows;             // one-warp path: directions up to this many rows
+  uint32_t pipe_rows;              // CTA path up to this many rows; multi-pass pipeline above
+  uint32_t n_big;                  // problems (first in plan order) with a direction above small_rows
   uint32_t chunk;                  // consecutive items per warp step
   uint32_t window;                 // half-width of the bound window
 };
@@ -433,7 +437,7 @@ __global__ void __launch_bounds__(kBatchThreads, PASS == kPassSeed ? 3 : 4)
   cu.order = a.order;
   cu.nprob = a.nprob;
   cu.ndir = a.ndir;
-  cu.small_rows = a.small_rows;
+  cu.pipe_rows = a.pipe_rows;
   const uint64_t nw = (uint64_t) gridDim.x * (kBatchThreads / 32);
   for (uint64_t chunk = (uint64_t) blockIdx.x * (kBatchThreads / 32) + (threadIdx.x >> 5);
        chunk * a.chunk < a.total; chunk += nw) {
@@ -693,9 +697,170 @@ __device__ __forceinline__ void small_direction(const BatchArgs& a, uint32_t p, 
   if (lane == 0) a.keys[2 * (uint64_t) p + d] = best;
 }
 
+// Block-wide reductions over the kBatchThreads threads (result in every
+// thread).  `red` is shared scratch of one word per warp.
+__device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v,
+                                                            unsigned long long* red) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    v = w > v ? w : v;
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  v = red[0];
+#pragma unroll
+  for (int k = 1; k < kBatchThreads / 32; ++k) v = red[k] > v ? red[k] : v;
+  __syncthreads();
+  return v;
+}
+
+__device__ __forceinline__ float block_min_f(float v, float* red) {
+  v = warp_min(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  v = red[0];
+#pragma unroll
+  for (int k = 1; k < kBatchThreads / 32; ++k) v = fminf(v, red[k]);
+  __syncthreads();
+  return v;
+}
+
+// CTA path: the whole block solves one problem-direction of small_rows+1 ..
+// pipe_rows query rows with the one-warp path's algorithm — window bounds
+// (per row), best-first exact scans (all threads over the other set, an
+// early-break vote every 2048 pairs), and after kBestFirst rows a sweep of
+// the rows still above the maximum, one warp per row.
+template <int D>
+__device__ __forceinline__ void cta_direction(const BatchArgs& a, uint32_t p, int d,
+                                              const hd_problem& pr, float* wb) {
+  __shared__ unsigned long long s_red[kBatchThreads / 32];
+  __shared__ float s_redf[kBatchThreads / 32];
+  __shared__ unsigned long long s_best;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const float* X = d == 0 ? a.A + pr.offset_a * D : a.B + pr.offset_b * D;
+  const float* Y = d == 0 ? a.B + pr.offset_b * D : a.A + pr.offset_a * D;
+  const uint32_t nx = (uint32_t) (d == 0 ? pr.n_a : pr.n_b);
+  const uint32_t ny = (uint32_t) (d == 0 ? pr.n_b : pr.n_a);
+  const float ratio = (float) ny / (float) nx;
+  const uint32_t w0 = ny > 2 * a.window + 1 ? 2 * a.window + 1 : ny;
+  const uint32_t half = w0 >> 1;
+  for (uint32_t row = tid; row < nx; row += kBatchThreads) {
+    uint32_t j = scan_start(row, ratio, ny, half);
+    wb[row] = scan_run<D>(X, row, Y, j, ny, w0, INFINITY);
+  }
+  __syncthreads();
+
+  unsigned long long best = 0;
+  float thr = -1.0f;
+  bool settled = false;
+  for (int it = 0; it < kBestFirst; ++it) {
+    unsigned long long cand = 0;
+    for (uint32_t row = tid; row < nx; row += kBatchThreads) {
+      const float u = wb[row];
+      if (u > thr) {
+        const unsigned long long kk = pack_max(u, row);
+        cand = kk > cand ? kk : cand;
+      }
+    }
+    cand = block_max_u64(cand, s_red);
+    if (cand == 0) {
+      settled = true;
+      break;
+    }
+    const uint32_t r = unpack_max_index(cand);
+    float xr[D];
+    load_pt<D>(X, r, xr);
+    float cm = __uint_as_float((uint32_t) (cand >> 32));  // its bound: a real distance
+    bool broke = false;
+    for (uint64_t t0 = 0; t0 < ny; t0 += (uint64_t) kBatchThreads * kLongIlp) {
+      float y[kLongIlp][D];
+#pragma unroll
+      for (int u = 0; u < kLongIlp; ++u) {
+        const uint64_t jj = t0 + (uint64_t) u * kBatchThreads + tid;
+#pragma unroll
+        for (int k = 0; k < D; ++k) y[u][k] = jj < ny ? Y[jj * D + k] : INFINITY;
+      }
+#pragma unroll
+      for (int u = 0; u < kLongIlp; ++u) {
+        const uint64_t jj = t0 + (uint64_t) u * kBatchThreads + tid;
+        const float d2 = d2_of<D>(xr, y[u]);
+        if (jj < ny) cm = fminf(cm, d2);
+      }
+      if (__syncthreads_or(cm <= thr)) {
+        broke = true;
+        break;
+      }
+    }
+    if (!broke) {
+      const unsigned long long kr = pack_max(block_min_f(cm, s_redf), r);
+      if (kr > best) {
+        best = kr;
+        thr = threshold_of(best);
+      }
+    }
+    if (tid == 0) wb[r] = -1.0f;
+    __syncthreads();
+  }
+  if (!settled) {
+    // Rows still above the maximum: one warp per row, lanes over the other
+    // set; the block's maximum is shared through s_best.
+    if (tid == 0) s_best = best;
+    __syncthreads();
+    for (uint32_t row = warp; row < nx; row += kBatchThreads / 32) {
+      const float u = wb[row];
+      const float t = threshold_of(*(volatile unsigned long long*) &s_best);
+      if (!(u > t)) continue;
+      float xr[D];
+      load_pt<D>(X, row, xr);
+      float cm = u;
+      bool broke = false;
+      for (uint64_t t0 = 0; t0 < ny; t0 += 32 * kLongIlp) {
+        float y[kLongIlp][D];
+#pragma unroll
+        for (int v = 0; v < kLongIlp; ++v) {
+          const uint64_t jj = t0 + (uint64_t) v * 32 + lane;
+#pragma unroll
+          for (int k = 0; k < D; ++k) y[v][k] = jj < ny ? Y[jj * D + k] : INFINITY;
+        }
+#pragma unroll
+        for (int v = 0; v < kLongIlp; ++v) {
+          const uint64_t jj = t0 + (uint64_t) v * 32 + lane;
+          const float d2 = d2_of<D>(xr, y[v]);
+          if (jj < ny) cm = fminf(cm, d2);
+        }
+        if (warp_min(cm) <= threshold_of(*(volatile unsigned long long*) &s_best)) {
+          broke = true;
+          break;
+        }
+      }
+      if (broke) continue;
+      const float m = warp_min(cm);  // all lanes: full-warp shuffles
+      if (lane == 0) atomicMax(&s_best, pack_max(m, row));
+      __syncwarp();
+    }
+    __syncthreads();
+    best = s_best;
+    __syncthreads();
+  }
+  if (tid == 0) a.keys[2 * (uint64_t) p + d] = best;
+}
+
 template <int D>
 __global__ void __launch_bounds__(kBatchThreads) k_batch_small(BatchArgs a) {
   const int lane = threadIdx.x & 31;
+  // First the CTA-path directions, one per block: they sit among the first
+  // n_big ranks of the plan, largest first.
+  for (uint64_t q = blockIdx.x; q < (uint64_t) a.n_big * a.ndir; q += gridDim.x) {
+    const uint32_t r = (uint32_t) (q / a.ndir);
+    const int d = (int) (q % a.ndir);
+    const uint32_t p = a.order[r];
+    const hd_problem pr = a.probs[p];
+    const uint64_t nx = d == 0 ? pr.n_a : pr.n_b;
+    if (nx <= (uint64_t) a.small_rows || nx > (uint64_t) a.pipe_rows) continue;
+    cta_direction<D>(a, p, d, pr, d == 0 ? a.wb_a + pr.offset_a : a.wb_b + pr.offset_b);
+  }
+  // Then the one-warp directions, one per warp.
   const uint64_t nw = (uint64_t) gridDim.x * (kBatchThreads / 32);
   const uint64_t npd = (uint64_t) a.nprob * a.ndir;
   for (uint64_t q = (uint64_t) blockIdx.x * (kBatchThreads / 32) + (threadIdx.x >> 5); q < npd;
@@ -709,29 +874,29 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_small(BatchArgs a) {
   }
 }
 
-// Plan: sort keys and the item count of each sorted rank.  Problems with a
-// direction in the multi-pass pipeline come first, each group largest
-// |A|*|B| first (stable by problem index): key = maxpairs - pairs, plus
-// maxpairs + 1 for the problems whose directions all take the one-warp path.
+// Plan: sort keys and the item count of each sorted rank.  Three groups, each
+// largest |A|*|B| first (stable by problem index): problems with a direction
+// in the multi-pass pipeline, then problems with a CTA-path direction, then
+// the rest (key = maxpairs - pairs + group * (maxpairs + 1)).
 // Entry nprob of the counts is 0, so that an exclusive scan over nprob + 1
 // entries gives the item prefix with the total at the end.
 __global__ void k_plan_keys(const hd_problem* __restrict__ probs, uint32_t n, int ndir,
-                            uint32_t small_rows, uint64_t maxpairs,
+                            uint32_t small_rows, uint32_t pipe_rows, uint64_t maxpairs,
                             unsigned long long* __restrict__ keys,
                             uint32_t* __restrict__ vals) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const hd_problem pr = probs[i];
-  const bool large = large_items(pr.n_a, small_rows) > 0 ||
-                     (ndir == 2 && large_items(pr.n_b, small_rows) > 0);
+  const uint64_t big = ndir == 2 ? max(pr.n_a, pr.n_b) : pr.n_a;
+  const uint64_t group = big > pipe_rows ? 0 : (big > small_rows ? 1 : 2);
   const uint64_t pairs = min((uint64_t) (pr.n_a * pr.n_b), maxpairs);  // maxpairs < 2^62
-  keys[i] = maxpairs - pairs + (large ? 0 : maxpairs + 1);
+  keys[i] = maxpairs - pairs + group * (maxpairs + 1);
   vals[i] = i;
 }
 
 __global__ void k_plan_counts(const hd_problem* __restrict__ probs,
                               const uint32_t* __restrict__ order, uint32_t n, int ndir,
-                              uint32_t small_rows, uint64_t* __restrict__ cnt) {
+                              uint32_t pipe_rows, uint64_t* __restrict__ cnt) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r > n) return;
   if (r == n) {
@@ -739,7 +904,7 @@ __global__ void k_plan_counts(const hd_problem* __restrict__ probs,
     return;
   }
   const hd_problem pr = probs[order[r]];
-  cnt[r] = large_items(pr.n_a, small_rows) + (ndir == 2 ? large_items(pr.n_b, small_rows) : 0);
+  cnt[r] = large_items(pr.n_a, pipe_rows) + (ndir == 2 ? large_items(pr.n_b, pipe_rows) : 0);
 }
 
 // Certification per problem-direction: one warp scans the other set for the
@@ -874,7 +1039,8 @@ hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
   cudaMemsetAsync(g.base, 0, g.zero_bytes, c.stream);
   cudaMemsetAsync(at(g.o_smin), 0xFF, g.smin_bytes, c.stream);
   cudaMemsetAsync(g.ctr, 0, 2 * 8, c.stream);
-  k_plan_keys<<<pblocks, 256, 0, c.stream>>>(a.probs, n, g.ndir, a.small_rows, g.maxpairs,
+  k_plan_keys<<<pblocks, 256, 0, c.stream>>>(a.probs, n, g.ndir, a.small_rows, a.pipe_rows,
+                                            g.maxpairs,
                                             (unsigned long long*) at(g.o_pkeys),
                                             (uint32_t*) at(g.o_pvals));
   size_t tb = g.cub_tmp;
@@ -882,7 +1048,7 @@ hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
                                   (unsigned long long*) at(g.o_pkeys2),
                                   (const uint32_t*) at(g.o_pvals), const_cast<uint32_t*>(a.order),
                                   (int64_t) n, 0, g.end_bit, c.stream);
-  k_plan_counts<<<pblocks, 256, 0, c.stream>>>(a.probs, a.order, n, g.ndir, a.small_rows,
+  k_plan_counts<<<pblocks, 256, 0, c.stream>>>(a.probs, a.order, n, g.ndir, a.pipe_rows,
                                               (uint64_t*) at(g.o_cnt));
   tb = g.cub_tmp;
   cub::DeviceScan::ExclusiveSum(at(g.o_tmp), tb, (const uint64_t*) at(g.o_cnt),
@@ -935,24 +1101,26 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   if ((s = check_problems(c, src, n, total_a, total_b)) != HD_OK) return s;
   const int ndir = (flags & HD_UNDIRECTED) ? 2 : 1;
   const uint32_t small_rows = std::min<uint32_t>(c.opt.batch_small_rows, kSmallMax);
+  const uint32_t pipe_rows = std::max<uint32_t>(small_rows, kPipeRows);
   const uint32_t chunk = std::max<uint32_t>(1, c.opt.batch_chunk);
-  uint64_t total = 0, rows = 0, maxpairs = 0;
+  uint64_t total = 0, rows = 0, maxpairs = 0, n_big = 0;
   for (uint64_t i = 0; i < n; ++i) {
     const hd_problem p = src.get(i);
-    total += large_items(p.n_a, small_rows) + (ndir == 2 ? large_items(p.n_b, small_rows) : 0);
+    total += large_items(p.n_a, pipe_rows) + (ndir == 2 ? large_items(p.n_b, pipe_rows) : 0);
     rows += p.n_a + (ndir == 2 ? p.n_b : 0);
     maxpairs = std::max<uint64_t>(maxpairs, p.n_a * p.n_b);
+    n_big += (p.n_a > small_rows || (ndir == 2 && p.n_b > small_rows)) ? 1 : 0;
   }
   BatchGraph g{};
   g.dims = dims;
   g.ndir = ndir;
   g.n = n;
-  // Plan keys stay below 2 * maxpairs + 2 (largest-first order among
+  // Plan keys stay below 3 * maxpairs + 3 (largest-first order among
   // problems above 2^62 pairs is not needed).
   maxpairs = std::min<uint64_t>(maxpairs, (1ull << 62) - 1);
   g.maxpairs = maxpairs;
   g.end_bit = 1;
-  while (g.end_bit < 64 && ((2 * maxpairs + 1) >> g.end_bit)) ++g.end_bit;
+  while (g.end_bit < 64 && ((3 * maxpairs + 2) >> g.end_bit)) ++g.end_bit;
   const uint64_t long_cap = std::min<uint64_t>(rows, kLongCap);
 
   // CUB temporary storage for the plan's sort and scan.
@@ -1046,6 +1214,8 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   args.long_count = d_ctr;
   args.long_cap = long_cap;
   args.small_rows = small_rows;
+  args.pipe_rows = pipe_rows;
+  args.n_big = (uint32_t) n_big;
   args.chunk = chunk;
   args.window = c.opt.batch_window;
 
@@ -1076,10 +1246,10 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   // One graph: reset, plan, window, seed, sweep, long rows, certification,
   // finalisation.  Captured once per launch shape; the per-call input (the
   // problems) is read from device memory.
-  const uint64_t key[16] = {(uint64_t) dims, n,        (uint64_t) ndir, (uint64_t) dA,
+  const uint64_t key[17] = {(uint64_t) dims, n,        (uint64_t) ndir, (uint64_t) dA,
                             (uint64_t) dB,   total_a,  total_b,         (uint64_t) g.base,
                             (uint64_t) L.off, total,   maxpairs,        long_cap,
-                            (uint64_t) c.stream, small_rows, chunk, c.opt.batch_window};
+                            (uint64_t) c.stream, small_rows, chunk, c.opt.batch_window, n_big};
   static_assert(sizeof(key) == sizeof(c.batch_key), "batch key size");
   if ((s = ensure_side(c)) != HD_OK) return s;
   if (!c.batch_graph || std::memcmp(key, c.batch_key, sizeof(key)) != 0) {

@@ -123,7 +123,7 @@ struct Ctx {
   uint64_t solve_graph_launches = 0;
   uint64_t buf_gen = 0;             // bumped by every (re)allocation
   cudaEvent_t batch_fork = nullptr, batch_join = nullptr;
-  uint64_t batch_key[16] = {};
+  uint64_t batch_key[17] = {};
   // Per-solve cache: the Morton-sorted sets (slot 0 = call's A, 1 = call's B)
   // are shared by both directions of an undirected solve.
   SortedSet sorted[2];
