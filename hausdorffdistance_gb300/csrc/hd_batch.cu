@@ -184,6 +184,7 @@ struct BatchArgs {
   uint32_t n_big;                  // problems (first in plan order) with a direction above small_rows
   uint32_t chunk;                  // consecutive items per warp step
   uint32_t window;                 // half-width of the bound window
+  PD* pd;                          // certified result per problem-direction
 };
 
 // First position of a row's circular scan: the start of the window of w0
@@ -694,7 +695,31 @@ __device__ __forceinline__ void small_direction(const BatchArgs& a, uint32_t p, 
       }
     }
   }
-  if (lane == 0) a.keys[2 * (uint64_t) p + d] = best;
+  // Certification here, where the rows are at hand: the argmin of the
+  // certifying row (lowest index among ties), as k_batch_certify does for
+  // the pipeline's directions.
+  const uint32_t rc = unpack_max_index(best);
+  float xc[D];
+  load_pt<D>(X, rc, xc);
+  unsigned long long am = ~0ull;
+#pragma unroll 4
+  for (uint32_t j = lane; j < ny; j += 32) {
+    float y[D];
+    load_pt<D>(Y, j, y);
+    const unsigned long long k = pack_min(d2_of<D>(xc, y), j);
+    am = k < am ? k : am;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const unsigned long long v = __shfl_xor_sync(0xFFFFFFFFu, am, o);
+    am = v < am ? v : am;
+  }
+  if (lane == 0) {
+    a.keys[2 * (uint64_t) p + d] = best;
+    const bool ok = (uint32_t) (am >> 32) == (uint32_t) (best >> 32);
+    a.pd[2 * (uint64_t) p + d] = PD{__uint_as_float((uint32_t) (best >> 32)), rc,
+                                    (uint32_t) (am & 0xFFFFFFFFull), ok ? 1u : 2u};
+  }
 }
 
 // Block-wide reductions over the kBatchThreads threads (result in every
@@ -843,7 +868,25 @@ __device__ __forceinline__ void cta_direction(const BatchArgs& a, uint32_t p, in
     best = s_best;
     __syncthreads();
   }
-  if (tid == 0) a.keys[2 * (uint64_t) p + d] = best;
+  // Certification (block-wide argmin of the certifying row).
+  const uint32_t rc = unpack_max_index(best);
+  float xc[D];
+  load_pt<D>(X, rc, xc);
+  unsigned long long am = ~0ull;
+#pragma unroll 4
+  for (uint32_t j = tid; j < ny; j += kBatchThreads) {
+    float y[D];
+    load_pt<D>(Y, j, y);
+    const unsigned long long k = pack_min(d2_of<D>(xc, y), j);
+    am = k < am ? k : am;
+  }
+  am = ~block_max_u64(~am, s_red);  // min via the complement
+  if (tid == 0) {
+    a.keys[2 * (uint64_t) p + d] = best;
+    const bool ok = (uint32_t) (am >> 32) == (uint32_t) (best >> 32);
+    a.pd[2 * (uint64_t) p + d] = PD{__uint_as_float((uint32_t) (best >> 32)), rc,
+                                    (uint32_t) (am & 0xFFFFFFFFull), ok ? 1u : 2u};
+  }
 }
 
 template <int D>
@@ -912,13 +955,16 @@ __global__ void k_plan_counts(const hd_problem* __restrict__ probs,
 template <int D>
 __global__ void k_batch_certify(const float* __restrict__ A, const float* __restrict__ B,
                                 const hd_problem* __restrict__ probs, uint32_t nprob, int ndir,
-                                const unsigned long long* __restrict__ keys, PD* __restrict__ pd) {
+                                const unsigned long long* __restrict__ keys, PD* __restrict__ pd,
+                                uint32_t pipe_rows) {
   const int lane = threadIdx.x & 31;
   const uint64_t w = (uint64_t) blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
   if (w >= (uint64_t) nprob * ndir) return;
   const uint32_t p = (uint32_t) (w / ndir);
   const int d = (int) (w % ndir);
   const hd_problem pr = probs[p];
+  // The one-warp and CTA paths certify their own directions.
+  if ((d == 0 ? pr.n_a : pr.n_b) <= pipe_rows) return;
   const unsigned long long key = keys[2 * (uint64_t) p + d];
   if (key == 0) {
     if (lane == 0) pd[2 * (uint64_t) p + d] = PD{0.0f, 0, 0, 0};
@@ -1071,9 +1117,11 @@ hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
   cudaStreamWaitEvent(c.stream, c.batch_join, 0);
   const unsigned cblocks = (unsigned) ((g.n * g.ndir * 32 + 255) / 256);
   if (g.dims == 2)
-    k_batch_certify<2><<<cblocks, 256, 0, c.stream>>>(a.A, a.B, a.probs, n, g.ndir, a.keys, g.pd);
+    k_batch_certify<2><<<cblocks, 256, 0, c.stream>>>(a.A, a.B, a.probs, n, g.ndir, a.keys, g.pd,
+                                                      a.pipe_rows);
   else
-    k_batch_certify<3><<<cblocks, 256, 0, c.stream>>>(a.A, a.B, a.probs, n, g.ndir, a.keys, g.pd);
+    k_batch_certify<3><<<cblocks, 256, 0, c.stream>>>(a.A, a.B, a.probs, n, g.ndir, a.keys, g.pd,
+                                                      a.pipe_rows);
   k_batch_finalize<<<(unsigned) ((g.n + 255) / 256), 256, 0, c.stream>>>(g.pd, n, g.ndir, g.out,
                                                                           g.bad);
   e = cudaStreamEndCapture(c.stream, &graph);
@@ -1218,6 +1266,7 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   args.n_big = (uint32_t) n_big;
   args.chunk = chunk;
   args.window = c.opt.batch_window;
+  args.pd = g.pd;
 
   // Persistent grids: resident blocks of each kernel, at most one warp per
   // chunk of items (or per queued row).
