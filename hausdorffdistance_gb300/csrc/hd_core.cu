@@ -3,7 +3,7 @@
 //
 // The C ABI replaces the reference's algorithm seam
 // HausdorffDistance<COORD_T,N_DIMS>::CalculateDistance
-// (src/hausdorff_distance.h:21-32) and the driver's variant factory and
+// (src/hausdorff_distance.h:21-32) and hd_exec's variant factory and
 // repeat loop (src/run_hausdorff_distance.cu:220-357).  Errors never escape
 // as exceptions (the reference aborts through glog CHECK or throws
 // hd::Exception from CUDA_CHECK, utils/exception.h:151-160); every call

@@ -104,7 +104,8 @@ __device__ __forceinline__ uint32_t node_id(uint32_t ref, uint32_t nI) {
 // parent computes its box (Karras 2012, section 4) and writes the packed node
 // (4 float4: both children's boxes and refs).
 // Box of node `id`: leaves' boxes come from the sorted set's gather pass,
-// internal boxes from this build (written by other threads: read around L1).
+// internal boxes from this bottom-up pass (written by other threads: read
+// around L1).
 __device__ __forceinline__ void node_box(uint32_t id, uint32_t nI, const float4* boxes,
                                          const float4* __restrict__ leaf_boxes, float4* lo,
                                          float4* hi) {

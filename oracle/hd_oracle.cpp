@@ -2,8 +2,8 @@
 //
 // CPU restatement of the reference's Hausdorff-distance path, used only by
 // tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py, and
-// only as the checker (or the timed CPU baseline), never as the thing being
-// measured.  Parity is pinned: tests/test_oracle.py checks this restatement
+// only to check results (or as the timed CPU baseline), never as the thing
+// being measured.  Parity is pinned: tests/test_oracle.py checks this restatement
 // against outputs of the reference's own CPU early-break code compiled from
 // its sources (oracle/build_ref.sh -> oracle/_ref/ref_eb), committed as
 // tests/golden/*.json by tests/golden/make_golden.py.

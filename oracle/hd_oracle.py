@@ -3,7 +3,7 @@
 ctypes wrapper of oracle/hd_oracle.cpp (the CPU restatement of the reference's
 early-break path plus an exact max-min with the certifying pair).  Only
 tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, and
-only as the checker or as the timed CPU baseline.  Parity is pinned against
+only to check results or as the timed CPU baseline.  Parity is pinned against
 the reference's own compiled CPU code through tests/golden/ (see
 tests/test_oracle.py).
 """
