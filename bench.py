@@ -341,7 +341,7 @@ def main_batch(args):
     alg = float((2 if undirected else 1) * (2 * sizes).sum() * 8)  # both sets, both directions
     achieved = alg / (ms / 1e3) / 1e9
     roof = {"bound": "hbm", "kernel": "batch_graph", "achieved": achieved, "peak": peak,
-            "unit": "GB/s", "frac": achieved / peak, "traffic": traffic_from_profiles("batch", 1),
+            "unit": "GB/s", "frac": achieved / peak, "traffic": traffic_from_profiles("batch", float(sizes.sum())),
             "algorithmic_bytes": alg, "kernel_ms": ms, "peak_source": peak_kind + " hbm_gbs"}
     base = None if (args.no_cpu or world > 1) else cpu_baseline_batch(a, b, off, undirected)
     if rank == 0:
