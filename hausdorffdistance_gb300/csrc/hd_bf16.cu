@@ -15,15 +15,20 @@
 // Hausdorff distance — bit-identical to the FP32 scans.  The certifying
 // pair's distance is then recomputed in FP64 (certify()).
 //
-// Kernel shape (one CTA per 128 A rows, 6 warps, 1 CTA per SM):
+// Kernel shape (one CTA per 256 A rows = two 128-row regions, 6 warps, 1 CTA
+// per SM):
 //   warp 0      producer: TMA bulk copies (cp.async.bulk) of the A block once
-//               and of B tiles (256 rows, hi+lo) into a 2-stage ring
+//               and of B tiles (128 rows, hi+lo) into a 4-stage ring
 //   warp 1      allocates 512 TMEM columns; one lane issues the MMAs:
-//               per B tile and 128-row half, 3 products x (Kp/16) MMAs of
+//               per B tile and A region, 3 products x (Kp/16) MMAs of
 //               M=128, N=128, K=16 into one of two 256-column FP32
-//               accumulators
+//               accumulators (region r at columns r*128)
 //   warps 2-5   epilogue: tcgen05.ld of the accumulator (one TMEM lane per
-//               A row), min over the tile of ||b||^2 - 2 acc
+//               pair of A rows, one per region), min over the tile of
+//               ||b||^2 - 2 acc
+// Both A regions read every B tile from shared memory, so each B tile is
+// streamed from L2 once per 256 A rows: half the L2 -> SM traffic per MMA of
+// a 128-row CTA.
 // Operands are pre-packed in global memory in the no-swizzle K-major
 // core-matrix layout (8 rows x 16 bytes per core matrix), so every tile is
 // one contiguous bulk copy.  No TMA multicast.
@@ -38,13 +43,14 @@
 namespace hdg {
 namespace {
 
-constexpr int kBM = 128;   // A rows per CTA (UMMA M)
-constexpr int kBN = 256;   // B rows per tile: two 128-row halves (UMMA N = 128 each)
-constexpr int kBH = 128;   // rows of one B half / one packed sub-tile
+constexpr int kBM = 128;   // rows of one A region (UMMA M)
+constexpr int kAM = 256;   // A rows per CTA: two 128-row regions sharing every B tile
+constexpr int kBH = 128;   // B rows per tile / one packed sub-tile (UMMA N)
+constexpr int kStages = 4; // B tiles in flight (ring of shared-memory stages)
 constexpr int kThreads = 192;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kWaitLimit = 1u << 24;
-// Dynamic shared memory reserved per CTA.  The operands use 160 KB; the rest
+// Dynamic shared memory reserved per CTA.  The operands use up to 192 KB; the rest
 // keeps every address a descriptor could form (even with its two strides
 // read the other way round) inside this CTA's own window.
 constexpr uint32_t kSmemBytes = 220 * 1024;
@@ -214,25 +220,30 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_bf16_rowmin(const unsigned char* __restrict__ Apack, const unsigned char* __restrict__ Bpack,
                   const float* __restrict__ anorm, const float* __restrict__ bnorm, uint64_t nA,
                   uint32_t nTilesB, float* __restrict__ rowmin, Bf16Scalars* bs) {
-  constexpr uint32_t kAReg = kBM * Kp * 2;   // bytes of one A region (hi or lo)
-  constexpr uint32_t kBHReg = kBH * Kp * 2;  // bytes of one B half region (hi or lo)
-  constexpr uint32_t kATile = 2 * kAReg;     // A block: hi, lo
-  constexpr uint32_t kBTile = 4 * kBHReg;    // B tile: (hi, lo) of half 0, then of half 1
-  static_assert(kATile + 2 * kBTile <= kSmemBytes, "operands exceed shared memory");
+  constexpr uint32_t kAReg = kBM * Kp * 2;   // bytes of one A region's hi (or lo) operand
+  constexpr uint32_t kBReg = kBH * Kp * 2;   // bytes of one B tile's hi (or lo) operand
+  constexpr uint32_t kABlock = 4 * kAReg;    // A block: (hi, lo) of region 0, then of region 1
+  constexpr uint32_t kBTile = 2 * kBReg;     // B tile: hi, lo
+  constexpr uint32_t kAccCols = 2 * kBH;     // one accumulator: region 0, then region 1
+  static_assert(kABlock + kStages * kBTile <= kSmemBytes, "operands exceed shared memory");
+  static_assert(2 * kAccCols <= kTmemCols, "accumulators exceed the TMEM allocation");
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t a_full, b_full[2], b_empty[2], acc_full[2], acc_empty[2];
+  __shared__ __align__(8) uint64_t a_full, b_full[kStages], b_empty[kStages], acc_full[2],
+      acc_empty[2];
   __shared__ uint32_t tmem_base;
-  __shared__ __align__(16) float s_bn[2][kBN];
+  __shared__ __align__(16) float s_bn[2][kBH];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned char* sA = smem;
-  unsigned char* sB = smem + kATile;
+  unsigned char* sB = smem + kABlock;
 
   if (threadIdx.x == 0) {
     mbar_init(&a_full, 1);
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < kStages; ++i) {
       mbar_init(&b_full[i], 1);
       mbar_init(&b_empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
       mbar_init(&acc_full[i], 1);
       mbar_init(&acc_empty[i], 128);
     }
@@ -254,43 +265,45 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (warp == 0) {
     if (lane == 0) {
-      mbar_expect_tx(&a_full, kATile);
-      tma_load_1d(sA, Apack + (uint64_t) blockIdx.x * kATile, kATile, &a_full);
+      mbar_expect_tx(&a_full, kABlock);
+      tma_load_1d(sA, Apack + (uint64_t) blockIdx.x * kABlock, kABlock, &a_full);
       for (uint32_t t = 0; t < nTilesB && ok; ++t) {
-        const int buf = t & 1;
-        if (t >= 2) ok = mbar_wait(&b_empty[buf], ((t >> 1) - 1) & 1, status, kWaitLimit);
+        const uint32_t st = t % kStages;
+        if (t >= kStages) ok = mbar_wait(&b_empty[st], ((t / kStages) - 1) & 1, status, kWaitLimit);
         if (!ok) break;
-        mbar_expect_tx(&b_full[buf], kBTile);
-        tma_load_1d(sB + buf * kBTile, Bpack + (uint64_t) t * kBTile, kBTile, &b_full[buf]);
+        mbar_expect_tx(&b_full[st], kBTile);
+        tma_load_1d(sB + st * kBTile, Bpack + (uint64_t) t * kBTile, kBTile, &b_full[st]);
       }
-      // Every issued copy must land before the CTA may exit.
-      if (ok && nTilesB >= 1) ok = mbar_wait(&b_empty[(nTilesB - 1) & 1], ((nTilesB - 1) >> 1) & 1,
-                                            status, kWaitLimit);
-      if (ok && nTilesB >= 2) ok = mbar_wait(&b_empty[(nTilesB - 2) & 1], ((nTilesB - 2) >> 1) & 1,
-                                            status, kWaitLimit);
+      // Every issued copy must land before the CTA may exit: wait for the
+      // MMAs of the last tile of every stage.
+      const uint32_t first = nTilesB > (uint32_t) kStages ? nTilesB - kStages : 0;
+      for (uint32_t t = first; t < nTilesB && ok; ++t)
+        ok = mbar_wait(&b_empty[t % kStages], (t / kStages) & 1, status, kWaitLimit);
     }
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = make_idesc();
+      // K-major, no swizzle: LBO = next 8-element chunk along K (16 core
+      // matrices further in a 128-row operand), SBO = next 8-row group (one
+      // core matrix further).  Every operand holds 128 rows, so even a
+      // descriptor read with the two strides exchanged stays inside this
+      // CTA's shared-memory window.
+      constexpr uint32_t kLbo = (kBM / 8) * 128u, kSbo = 128u;
+      static_assert(kBM == kBH, "A and B operands share one descriptor layout");
       ok = mbar_wait(&a_full, 0, status, kWaitLimit);
-      const uint32_t a_hi = smem_u32(sA), a_lo = a_hi + kAReg;
+      const uint32_t a0 = smem_u32(sA);
       for (uint32_t t = 0; t < nTilesB && ok; ++t) {
+        const uint32_t st = t % kStages;
         const int buf = t & 1;
-        ok = mbar_wait(&b_full[buf], (t >> 1) & 1, status, kWaitLimit);
+        ok = mbar_wait(&b_full[st], (t / kStages) & 1, status, kWaitLimit);
         if (ok && t >= 2) ok = mbar_wait(&acc_empty[buf], ((t >> 1) - 1) & 1, status, kWaitLimit);
         if (!ok) break;
         tc_fence_after();
-        // K-major, no swizzle: LBO = next 8-element chunk along K (16 core
-        // matrices further in a 128-row region), SBO = next 8-row group (one
-        // core matrix further).  Every region holds 128 rows, so even a
-        // descriptor read with the two strides exchanged stays inside this
-        // CTA's shared-memory window.
-        constexpr uint32_t kLbo = (kBM / 8) * 128u, kSbo = 128u;
+        const uint32_t b_hi = smem_u32(sB + st * kBTile), b_lo = b_hi + kBReg;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const uint32_t b_hi = smem_u32(sB + buf * kBTile + h * 2 * kBHReg);
-          const uint32_t b_lo = b_hi + kBHReg;
-          const uint32_t d = tmem + (uint32_t) buf * kBN + (uint32_t) h * kBH;
+        for (int r = 0; r < 2; ++r) {
+          const uint32_t a_hi = a0 + (uint32_t) r * 2u * kAReg, a_lo = a_hi + kAReg;
+          const uint32_t d = tmem + (uint32_t) buf * kAccCols + (uint32_t) r * kBH;
           uint32_t acc = 0;
 #pragma unroll
           for (int prod = 0; prod < 3; ++prod) {
@@ -305,26 +318,30 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
           }
         }
-        mma_commit(&b_empty[buf]);
+        mma_commit(&b_empty[st]);
         mma_commit(&acc_full[buf]);
       }
     }
   } else {
-    // Epilogue: warp w reads TMEM lanes [32 (w % 4), +32): one A row per
-    // thread.  ||b||^2 of the current tile is staged in shared memory by the
-    // 128 epilogue threads (two floats each) ahead of the accumulator wait;
-    // eight independent partial minima keep the FP32 pipes busy.
+    // Epilogue: warp w reads TMEM lanes [32 (w % 4), +32): one row of each A
+    // region per thread.  ||b||^2 of a tile is fetched one tile ahead into a
+    // register (its load latency hides behind the current tile) and staged
+    // in shared memory ahead of the accumulator wait; eight independent
+    // partial minima per row keep the FP32 pipes busy.
     const int quad = warp & 3;
     const int etid = (warp - 2) * 32 + lane;  // 0..127
-    const uint32_t row_in_block = (uint32_t) (quad * 32 + lane);
-    const uint64_t row = (uint64_t) blockIdx.x * kBM + row_in_block;
-    float m8[8];
+    const uint64_t row0 = (uint64_t) blockIdx.x * kAM + (uint32_t) (quad * 32 + lane);
+    const uint32_t tlane = (uint32_t) (quad * 32) << 16;
+    float m8[2][8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) m8[q] = INFINITY;
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int q = 0; q < 8; ++q) m8[r][q] = INFINITY;
+    float bn_next = nTilesB ? __ldg(bnorm + etid) : 0.0f;
     for (uint32_t t = 0; t < nTilesB; ++t) {
       const int buf = t & 1;
-      const float2 bnv = __ldg(reinterpret_cast<const float2*>(bnorm + (uint64_t) t * kBN) + etid);
-      reinterpret_cast<float2*>(s_bn[buf])[etid] = bnv;
+      s_bn[buf][etid] = bn_next;
+      if (t + 1 < nTilesB) bn_next = __ldg(bnorm + (uint64_t) (t + 1) * kBH + etid);
       // All epilogue threads have written this tile's norms, and all have
       // finished reading the buffer's previous contents (tile t - 2).
       asm volatile("bar.sync 1, 128;" ::: "memory");
@@ -335,32 +352,42 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       tc_fence_after();
       const float4* bn4 = reinterpret_cast<const float4*>(s_bn[buf]);
-#pragma unroll 1
-      for (int cc = 0; cc < kBN / 64; ++cc) {
-        float v[64];
-        tmem_ld32x2(tmem + ((uint32_t) (quad * 32) << 16) + (uint32_t) buf * kBN + cc * 64, v);
 #pragma unroll
-        for (int j4 = 0; j4 < 16; ++j4) {
-          const float4 bn = bn4[cc * 16 + j4];
-          const int q = (j4 & 1) * 4;
-          m8[q + 0] = fminf(m8[q + 0], fmaf(-2.0f, v[4 * j4 + 0], bn.x));
-          m8[q + 1] = fminf(m8[q + 1], fmaf(-2.0f, v[4 * j4 + 1], bn.y));
-          m8[q + 2] = fminf(m8[q + 2], fmaf(-2.0f, v[4 * j4 + 2], bn.z));
-          m8[q + 3] = fminf(m8[q + 3], fmaf(-2.0f, v[4 * j4 + 3], bn.w));
+      for (int r = 0; r < 2; ++r) {
+#pragma unroll 1
+        for (int cc = 0; cc < kBH / 64; ++cc) {
+          float v[64];
+          tmem_ld32x2(tmem + tlane + (uint32_t) buf * kAccCols + (uint32_t) r * kBH + cc * 64, v);
+#pragma unroll
+          for (int j4 = 0; j4 < 16; ++j4) {
+            const float4 bn = bn4[cc * 16 + j4];
+            const int q = (j4 & 1) * 4;
+            m8[r][q + 0] = fminf(m8[r][q + 0], fmaf(-2.0f, v[4 * j4 + 0], bn.x));
+            m8[r][q + 1] = fminf(m8[r][q + 1], fmaf(-2.0f, v[4 * j4 + 1], bn.y));
+            m8[r][q + 2] = fminf(m8[r][q + 2], fmaf(-2.0f, v[4 * j4 + 2], bn.z));
+            m8[r][q + 3] = fminf(m8[r][q + 3], fmaf(-2.0f, v[4 * j4 + 3], bn.w));
+          }
         }
       }
       tc_fence_before();
       mbar_arrive(&acc_empty[buf]);
     }
-    float m = m8[0];
+    if (ok) {
+      const double bmax = (double) ord2f(bs->bmax_ord);
 #pragma unroll
-    for (int q = 1; q < 8; ++q) m = fminf(m, m8[q]);
-    if (ok && row < nA) {
-      const float an = anorm[row];
-      const float mi = an + m;
-      rowmin[row] = mi;
-      const double E = row_bound(sqrt((double) an), (double) ord2f(bs->bmax_ord), Kp);
-      atomicMax(&bs->lo_ord, f2ord((float) ((double) mi - E)));
+      for (int r = 0; r < 2; ++r) {
+        float m = m8[r][0];
+#pragma unroll
+        for (int q = 1; q < 8; ++q) m = fminf(m, m8[r][q]);
+        const uint64_t row = row0 + (uint64_t) r * kBM;
+        if (row < nA) {
+          const float an = anorm[row];
+          const float mi = an + m;
+          rowmin[row] = mi;
+          const double E = row_bound(sqrt((double) an), bmax, Kp);
+          atomicMax(&bs->lo_ord, f2ord((float) ((double) mi - E)));
+        }
+      }
     }
   }
   // Every MMA of this CTA has completed once the epilogue consumed the last
@@ -450,9 +477,9 @@ __global__ void k_bf16_recheck_final(const uint32_t* __restrict__ list, const Bf
 template <int Kp>
 hd_status run_bf16_k(Ctx& c, const DirInput& in, DirResult* extra, float* rowmin_host) {
   hd_status s;
-  const uint64_t nTA = (in.nA + kBM - 1) / kBM, nTB = (in.nB + kBN - 1) / kBN;
-  if (nTA >= (1u << 31) || nTB >= 0xFFFFFFFFull) return fail(c, HD_ERR_INVALID_ARG, "too large");
-  const uint64_t padA = nTA * kBM, padB = nTB * kBN;
+  const uint64_t nCta = (in.nA + kAM - 1) / kAM, nTB = (in.nB + kBH - 1) / kBH;
+  if (nCta >= (1u << 31) || nTB >= 0xFFFFFFFFull) return fail(c, HD_ERR_INVALID_ARG, "too large");
+  const uint64_t padA = nCta * kAM, padB = nTB * kBH;
   void *pa, *pb, *na, *nb, *rm, *cand, *bsv;
   if ((s = ensure(c, kBufBf16A, padA * Kp * 4, &pa)) != HD_OK) return s;
   if ((s = ensure(c, kBufBf16B, padB * Kp * 4, &pb)) != HD_OK) return s;
@@ -482,7 +509,7 @@ hd_status run_bf16_k(Ctx& c, const DirInput& in, DirResult* extra, float* rowmin
   mark(c, 3);
   auto kern = k_bf16_rowmin<Kp>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kSmemBytes);
-  kern<<<(unsigned) nTA, kThreads, kSmemBytes, c.stream>>>(
+  kern<<<(unsigned) nCta, kThreads, kSmemBytes, c.stream>>>(
       (const unsigned char*) pa, (const unsigned char*) pb, (const float*) na, (const float*) nb,
       in.nA, (uint32_t) nTB, (float*) rm, bs);
   if ((s = after_launch(c, "bf16_rowmin")) != HD_OK) return s;
