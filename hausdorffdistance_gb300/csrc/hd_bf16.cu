@@ -18,17 +18,19 @@
 // Kernel shape (one CTA per 256 A rows = two 128-row regions, 6 warps, 1 CTA
 // per SM):
 //   warp 0      producer: TMA bulk copies (cp.async.bulk) of the A block once
-//               and of B tiles (128 rows, hi+lo) into a 4-stage ring
+//               and of B tiles (256 rows, hi+lo) into a 2-stage ring
 //   warp 1      allocates 512 TMEM columns; one lane issues the MMAs:
 //               per B tile and A region, 3 products x (Kp/16) MMAs of
-//               M=128, N=128, K=16 into one of two 256-column FP32
-//               accumulators (region r at columns r*128)
+//               M=128, N=256, K=16 into the region's 256-column FP32
+//               accumulator (region r at columns r*256); the two regions
+//               alternate, so one is computed while the other is read out
 //   warps 2-5   epilogue: tcgen05.ld of the accumulator (one TMEM lane per
 //               pair of A rows, one per region), min over the tile of
 //               ||b||^2 - 2 acc
-// Both A regions read every B tile from shared memory, so each B tile is
-// streamed from L2 once per 256 A rows: half the L2 -> SM traffic per MMA of
-// a 128-row CTA.
+// N = 256 keeps the MMA's shared-memory operand reads (A 4 KB + B 8 KB per
+// 128 x 256 x 16 step) below the SM's shared-memory bandwidth, which an
+// N = 128 step (8 KB per half as many cycles) saturates; both A regions
+// read every B tile, so each B tile is streamed from L2 once per 256 A rows.
 // Operands are pre-packed in global memory in the no-swizzle K-major
 // core-matrix layout (8 rows x 16 bytes per core matrix), so every tile is
 // one contiguous bulk copy.  No TMA multicast.
@@ -45,15 +47,14 @@ namespace {
 
 constexpr int kBM = 128;   // rows of one A region (UMMA M)
 constexpr int kAM = 256;   // A rows per CTA: two 128-row regions sharing every B tile
-constexpr int kBH = 128;   // B rows per tile / one packed sub-tile (UMMA N)
-constexpr int kStages = 4; // B tiles in flight (ring of shared-memory stages)
+constexpr int kBN = 256;   // B rows per tile (UMMA N)
+constexpr int kStages = 2; // B tiles in flight (ring of shared-memory stages)
 constexpr int kThreads = 192;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kWaitLimit = 1u << 24;
-// Dynamic shared memory reserved per CTA.  The operands use up to 192 KB; the rest
-// keeps every address a descriptor could form (even with its two strides
-// read the other way round) inside this CTA's own window.
-constexpr uint32_t kSmemBytes = 220 * 1024;
+// Dynamic shared memory per CTA: the A block (64 KB) and two B stages (64 KB
+// each) at Kp = 64; smaller Kp use a prefix.
+constexpr uint32_t kSmemBytes = 192 * 1024;
 
 // Byte offset of element (row, k) inside one packed operand region of R rows:
 // core matrix (chunk c = k/8, group g = row/8) at (c * R/8 + g) * 128 bytes,
@@ -138,12 +139,12 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint
 }
 
 // Instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major,
-// M = 128, N = 128.
+// M = 128, N = 256.
 __host__ __device__ constexpr uint32_t make_idesc() {
   return (1u << 4)                        // D format F32
          | (1u << 7)                      // A format BF16
          | (1u << 10)                     // B format BF16
-         | ((uint32_t) (kBH >> 3) << 17)  // N >> 3
+         | ((uint32_t) (kBN >> 3) << 17)  // N >> 3
          | ((uint32_t) (kBM >> 4) << 24);  // M >> 4
 }
 
@@ -161,6 +162,21 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(bar))
                : "memory");
+}
+
+// Named barrier over n threads that also returns whether any of them passed
+// v = true (the same answer in every participating thread).
+__device__ __forceinline__ bool bar_any(uint32_t id, uint32_t n, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n"
+      " setp.ne.u32 q, %1, 0;\n"
+      " bar.red.or.pred p, %2, %3, q;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t) v), "r"(id), "r"(n)
+      : "memory");
+  return r != 0;
 }
 
 __device__ __forceinline__ void tc_fence_before() {
@@ -221,17 +237,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                   const float* __restrict__ anorm, const float* __restrict__ bnorm, uint64_t nA,
                   uint32_t nTilesB, float* __restrict__ rowmin, Bf16Scalars* bs) {
   constexpr uint32_t kAReg = kBM * Kp * 2;   // bytes of one A region's hi (or lo) operand
-  constexpr uint32_t kBReg = kBH * Kp * 2;   // bytes of one B tile's hi (or lo) operand
+  constexpr uint32_t kBReg = kBN * Kp * 2;   // bytes of one B tile's hi (or lo) operand
   constexpr uint32_t kABlock = 4 * kAReg;    // A block: (hi, lo) of region 0, then of region 1
   constexpr uint32_t kBTile = 2 * kBReg;     // B tile: hi, lo
-  constexpr uint32_t kAccCols = 2 * kBH;     // one accumulator: region 0, then region 1
   static_assert(kABlock + kStages * kBTile <= kSmemBytes, "operands exceed shared memory");
-  static_assert(2 * kAccCols <= kTmemCols, "accumulators exceed the TMEM allocation");
+  static_assert(2 * kBN <= kTmemCols, "accumulators exceed the TMEM allocation");
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t a_full, b_full[kStages], b_empty[kStages], acc_full[2],
       acc_empty[2];
   __shared__ uint32_t tmem_base;
-  __shared__ __align__(16) float s_bn[2][kBH];
+  __shared__ __align__(16) float s_bn[2][kBN];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned char* sA = smem;
@@ -283,27 +298,27 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = make_idesc();
-      // K-major, no swizzle: LBO = next 8-element chunk along K (16 core
-      // matrices further in a 128-row operand), SBO = next 8-row group (one
-      // core matrix further).  Every operand holds 128 rows, so even a
-      // descriptor read with the two strides exchanged stays inside this
-      // CTA's shared-memory window.
-      constexpr uint32_t kLbo = (kBM / 8) * 128u, kSbo = 128u;
-      static_assert(kBM == kBH, "A and B operands share one descriptor layout");
+      // K-major, no swizzle: LBO = next 8-element chunk along K (one column
+      // of core matrices further: 16 of them in a 128-row A region, 32 in a
+      // 256-row B tile), SBO = next 8-row group (one core matrix further).
+      constexpr uint32_t kLboA = (kBM / 8) * 128u, kLboB = (kBN / 8) * 128u, kSbo = 128u;
       ok = mbar_wait(&a_full, 0, status, kWaitLimit);
       const uint32_t a0 = smem_u32(sA);
       for (uint32_t t = 0; t < nTilesB && ok; ++t) {
         const uint32_t st = t % kStages;
-        const int buf = t & 1;
         ok = mbar_wait(&b_full[st], (t / kStages) & 1, status, kWaitLimit);
-        if (ok && t >= 2) ok = mbar_wait(&acc_empty[buf], ((t >> 1) - 1) & 1, status, kWaitLimit);
         if (!ok) break;
-        tc_fence_after();
         const uint32_t b_hi = smem_u32(sB + st * kBTile), b_lo = b_hi + kBReg;
+        // Region r's accumulator is free once the epilogue has read it for
+        // tile t - 1; region 0's MMAs of tile t run while the epilogue still
+        // reads region 1 of tile t - 1.
 #pragma unroll
-        for (int r = 0; r < 2; ++r) {
+        for (int r = 0; r < 2 && ok; ++r) {
+          if (t >= 1) ok = mbar_wait(&acc_empty[r], (t - 1) & 1, status, kWaitLimit);
+          if (!ok) break;
+          tc_fence_after();
           const uint32_t a_hi = a0 + (uint32_t) r * 2u * kAReg, a_lo = a_hi + kAReg;
-          const uint32_t d = tmem + (uint32_t) buf * kAccCols + (uint32_t) r * kBH;
+          const uint32_t d = tmem + (uint32_t) r * kBN;
           uint32_t acc = 0;
 #pragma unroll
           for (int prod = 0; prod < 3; ++prod) {
@@ -311,53 +326,55 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint32_t br = prod == 1 ? b_lo : b_hi;
 #pragma unroll
             for (int s = 0; s < Kp / 16; ++s) {
-              const uint64_t da = make_desc(ar + (uint32_t) s * 2u * kLbo, kLbo, kSbo);
-              const uint64_t db = make_desc(br + (uint32_t) s * 2u * kLbo, kLbo, kSbo);
+              const uint64_t da = make_desc(ar + (uint32_t) s * 2u * kLboA, kLboA, kSbo);
+              const uint64_t db = make_desc(br + (uint32_t) s * 2u * kLboB, kLboB, kSbo);
               mma_bf16(d, da, db, idesc, acc);
               acc = 1;
             }
           }
+          mma_commit(&acc_full[r]);
         }
-        mma_commit(&b_empty[st]);
-        mma_commit(&acc_full[buf]);
+        if (ok) mma_commit(&b_empty[st]);
       }
     }
   } else {
-    // Epilogue: warp w reads TMEM lanes [32 (w % 4), +32): one row of each A
-    // region per thread.  ||b||^2 of a tile is fetched one tile ahead into a
-    // register (its load latency hides behind the current tile) and staged
-    // in shared memory ahead of the accumulator wait; eight independent
-    // partial minima per row keep the FP32 pipes busy.
+    // Epilogue: warp w reads TMEM lanes [32 (w % 4), +32), one row of each A
+    // region per thread.  ||b||^2 of a tile is fetched one tile ahead into
+    // registers (its load latency hides behind the current tile) and staged
+    // in shared memory; eight independent partial minima per row keep the
+    // FP32 pipes busy.  A failed wait in any epilogue thread ends the loop in
+    // all of them (bar_any).
     const int quad = warp & 3;
     const int etid = (warp - 2) * 32 + lane;  // 0..127
-    const uint64_t row0 = (uint64_t) blockIdx.x * kAM + (uint32_t) (quad * 32 + lane);
+    const uint32_t lrow = (uint32_t) (quad * 32 + lane);
     const uint32_t tlane = (uint32_t) (quad * 32) << 16;
     float m8[2][8];
 #pragma unroll
     for (int r = 0; r < 2; ++r)
 #pragma unroll
       for (int q = 0; q < 8; ++q) m8[r][q] = INFINITY;
-    float bn_next = nTilesB ? __ldg(bnorm + etid) : 0.0f;
-    for (uint32_t t = 0; t < nTilesB; ++t) {
+    const float2* bn2 = reinterpret_cast<const float2*>(bnorm);
+    float2 bn_next = nTilesB ? __ldg(bn2 + etid) : make_float2(0.0f, 0.0f);
+    for (uint32_t t = 0; t < nTilesB && ok; ++t) {
       const int buf = t & 1;
-      s_bn[buf][etid] = bn_next;
-      if (t + 1 < nTilesB) bn_next = __ldg(bnorm + (uint64_t) (t + 1) * kBH + etid);
-      // All epilogue threads have written this tile's norms, and all have
-      // finished reading the buffer's previous contents (tile t - 2).
-      asm volatile("bar.sync 1, 128;" ::: "memory");
-      ok = mbar_wait(&acc_full[buf], (t >> 1) & 1, status, kWaitLimit);
-      if (__any_sync(0xFFFFFFFFu, !ok)) {
-        ok = false;
-        break;
-      }
-      tc_fence_after();
+      reinterpret_cast<float2*>(s_bn[buf])[etid] = bn_next;
+      if (t + 1 < nTilesB) bn_next = __ldg(bn2 + (uint64_t) (t + 1) * (kBN / 2) + etid);
       const float4* bn4 = reinterpret_cast<const float4*>(s_bn[buf]);
 #pragma unroll
       for (int r = 0; r < 2; ++r) {
+        const bool got = mbar_wait(&acc_full[r], t & 1, status, kWaitLimit);
+        // Also a barrier over the epilogue threads: this tile's norms are
+        // written, and the reads of the buffer's previous contents (tile
+        // t - 2) are done.
+        if (bar_any(1, 128, !got)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
 #pragma unroll 1
-        for (int cc = 0; cc < kBH / 64; ++cc) {
+        for (int cc = 0; cc < kBN / 64; ++cc) {
           float v[64];
-          tmem_ld32x2(tmem + tlane + (uint32_t) buf * kAccCols + (uint32_t) r * kBH + cc * 64, v);
+          tmem_ld32x2(tmem + tlane + (uint32_t) r * kBN + cc * 64, v);
 #pragma unroll
           for (int j4 = 0; j4 < 16; ++j4) {
             const float4 bn = bn4[cc * 16 + j4];
@@ -368,9 +385,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             m8[r][q + 3] = fminf(m8[r][q + 3], fmaf(-2.0f, v[4 * j4 + 3], bn.w));
           }
         }
+        tc_fence_before();
+        mbar_arrive(&acc_empty[r]);
       }
-      tc_fence_before();
-      mbar_arrive(&acc_empty[buf]);
     }
     if (ok) {
       const double bmax = (double) ord2f(bs->bmax_ord);
@@ -379,7 +396,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         float m = m8[r][0];
 #pragma unroll
         for (int q = 1; q < 8; ++q) m = fminf(m, m8[r][q]);
-        const uint64_t row = row0 + (uint64_t) r * kBM;
+        const uint64_t row = (uint64_t) blockIdx.x * kAM + (uint64_t) r * kBM + lrow;
         if (row < nA) {
           const float an = anorm[row];
           const float mi = an + m;
@@ -477,9 +494,9 @@ __global__ void k_bf16_recheck_final(const uint32_t* __restrict__ list, const Bf
 template <int Kp>
 hd_status run_bf16_k(Ctx& c, const DirInput& in, DirResult* extra, float* rowmin_host) {
   hd_status s;
-  const uint64_t nCta = (in.nA + kAM - 1) / kAM, nTB = (in.nB + kBH - 1) / kBH;
+  const uint64_t nCta = (in.nA + kAM - 1) / kAM, nTB = (in.nB + kBN - 1) / kBN;
   if (nCta >= (1u << 31) || nTB >= 0xFFFFFFFFull) return fail(c, HD_ERR_INVALID_ARG, "too large");
-  const uint64_t padA = nCta * kAM, padB = nTB * kBH;
+  const uint64_t padA = nCta * kAM, padB = nTB * kBN;
   void *pa, *pb, *na, *nb, *rm, *cand, *bsv;
   if ((s = ensure(c, kBufBf16A, padA * Kp * 4, &pa)) != HD_OK) return s;
   if ((s = ensure(c, kBufBf16B, padB * Kp * 4, &pb)) != HD_OK) return s;
@@ -498,7 +515,7 @@ hd_status run_bf16_k(Ctx& c, const DirInput& in, DirResult* extra, float* rowmin
   k_bf16_pack<<<g, 256, 0, c.stream>>>(in.A, in.nA, in.dims, Kp, kBM, padA, (unsigned char*) pa,
                                        (float*) na, nullptr, 0);
   if ((s = after_launch(c, "bf16_pack_a")) != HD_OK) return s;
-  k_bf16_pack<<<g, 256, 0, c.stream>>>(in.B, in.nB, in.dims, Kp, kBH, padB, (unsigned char*) pb,
+  k_bf16_pack<<<g, 256, 0, c.stream>>>(in.B, in.nB, in.dims, Kp, kBN, padB, (unsigned char*) pb,
                                        (float*) nb, nullptr, 0);
   if ((s = after_launch(c, "bf16_pack_b")) != HD_OK) return s;
   // A's norm maximum is not needed; B's gives the bound.
