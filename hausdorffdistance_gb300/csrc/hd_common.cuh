@@ -28,6 +28,30 @@ __device__ __forceinline__ float d2_3(float ax, float ay, float az, float bx,
                    __fmul_rn(dz, dz));
 }
 
+// Two FP32 differences a - b in one packed instruction: fma(b, -1, a) has an
+// exact product, so its single rounding gives exactly __fsub_rn(a, b) per
+// component (signed zeros included); __ffma2_rn / __fmul2_rn round each
+// component like __fmaf_rn / __fmul_rn.
+__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+}
+
+// The same squared distance of two float4 points, bit for bit, with x and y
+// through the packed pair forms: fewer issue slots where both points already
+// sit in registers as float4 (the LBVH leaf scans); with scattered scalar
+// operands the packing moves cost more than they save.
+template <int D>
+__device__ __forceinline__ float d2_pt_packed(const float4& a, const float4& b) {
+  const float2 d = sub2_rn(make_float2(a.x, a.y), make_float2(b.x, b.y));
+  const float2 p = __fmul2_rn(d, d);
+  if constexpr (D == 2) {
+    return __fadd_rn(p.x, p.y);
+  } else {
+    const float dz = __fsub_rn(a.z, b.z);
+    return __fadd_rn(__fadd_rn(p.x, p.y), __fmul_rn(dz, dz));
+  }
+}
+
 template <int D>
 __device__ __forceinline__ float d2_pt(const float4& a, const float4& b) {
   if constexpr (D == 2) {

@@ -24,10 +24,14 @@
 // Layout in HBM:
 //   sorted points  float4 (x, y, z, caller index)       16 B / point
 //   leaves         implicit: leaf i = points [i*L, i*L+L), L <= 32
-//   nodes          4 x float4 per internal node: the boxes of both children
-//                  and the two child references (bit 31 set = leaf)   64 B
-// A traversal step loads one 64-byte node (all lanes the same address:
-// one broadcast) and tests both children for every lane of the packet.
+//   nodes          4 x float4 per internal node: (lo.x, lo.y, hi.x, hi.y) of
+//                  the left child, the same of the right child, (lo.z, hi.z)
+//                  of both, and the two child references (bit 31 set =
+//                  leaf)                                               64 B
+// A traversal step loads one node (all lanes the same address: one
+// broadcast; 2-D trees skip the z quarter) and tests both children for
+// every lane of the packet.  x and y of a box sit in aligned register pairs,
+// so the box distances use the packed pair instructions.
 #include <cfloat>
 
 #include "hd_common.cuh"
@@ -128,9 +132,9 @@ __device__ __forceinline__ void bottom_up_body(const uint2* __restrict__ child,
     // Single leaf: a root whose right child is an empty box (never visited).
     if (leaf == 0) {
       const float4 lo = leaf_boxes[0], hi = leaf_boxes[1];
-      nodes[0] = make_float4(lo.x, lo.y, lo.z, hi.x);
-      nodes[1] = make_float4(hi.y, hi.z, FLT_MAX, FLT_MAX);
-      nodes[2] = make_float4(FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX);
+      nodes[0] = make_float4(lo.x, lo.y, hi.x, hi.y);
+      nodes[1] = make_float4(FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX);
+      nodes[2] = make_float4(lo.z, hi.z, FLT_MAX, -FLT_MAX);
       nodes[3] = make_float4(__uint_as_float(kLeafBit), __uint_as_float(kLeafBit), 0.f, 0.f);
     }
     return;
@@ -153,41 +157,46 @@ __device__ __forceinline__ void bottom_up_body(const uint2* __restrict__ child,
     __stcg(&boxes[2 * (uint64_t) p + 1], hi);
     // The packed node the query reads: both children's boxes and refs.
     float4* o = nodes + 4 * (uint64_t) p;
-    o[0] = make_float4(alo.x, alo.y, alo.z, ahi.x);
-    o[1] = make_float4(ahi.y, ahi.z, blo.x, blo.y);
-    o[2] = make_float4(blo.z, bhi.x, bhi.y, bhi.z);
+    o[0] = make_float4(alo.x, alo.y, ahi.x, ahi.y);
+    o[1] = make_float4(blo.x, blo.y, bhi.x, bhi.y);
+    o[2] = make_float4(alo.z, ahi.z, blo.z, bhi.z);
     o[3] = make_float4(__uint_as_float(ch.x), __uint_as_float(ch.y), 0.f, 0.f);
     if (p == 0) return;
     node = p;
   }
 }
 
-// Squared distance from p to the box [lo, hi] (0 inside), rounded exactly
-// like the pair formula (same non-fused operations in the same order).
+// Squared distance from q to the box [lo, hi] (0 inside), with xy = (lo.x,
+// lo.y, hi.x, hi.y), rounded exactly like the pair formula (same non-fused
+// operations in the same order).
 // Rounding is monotone, so for every point b in the box this value is <= the
 // FP32 squared distance of (p, b): pruning a box whose value is >= the current
 // minimum can never skip a strictly smaller pair distance.
 template <int D>
-__device__ __forceinline__ float box_min_d2(float px, float py, float pz, float lx, float ly,
-                                            float lz, float hx, float hy, float hz) {
-  float dx = fmaxf(fmaxf(__fsub_rn(lx, px), __fsub_rn(px, hx)), 0.0f);
-  float dy = fmaxf(fmaxf(__fsub_rn(ly, py), __fsub_rn(py, hy)), 0.0f);
-  float s = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+__device__ __forceinline__ float box_min_d2(const float4& q, const float4& xy, float lz, float hz) {
+  const float2 p = make_float2(q.x, q.y);
+  const float2 below = sub2_rn(make_float2(xy.x, xy.y), p);
+  const float2 above = sub2_rn(p, make_float2(xy.z, xy.w));
+  const float dx = fmaxf(fmaxf(below.x, above.x), 0.0f);
+  const float dy = fmaxf(fmaxf(below.y, above.y), 0.0f);
+  const float2 sq = __fmul2_rn(make_float2(dx, dy), make_float2(dx, dy));
+  float s = __fadd_rn(sq.x, sq.y);
   if constexpr (D == 3) {
-    float dz = fmaxf(fmaxf(__fsub_rn(lz, pz), __fsub_rn(pz, hz)), 0.0f);
+    const float dz = fmaxf(fmaxf(__fsub_rn(lz, q.z), __fsub_rn(q.z, hz)), 0.0f);
     s = __fadd_rn(s, __fmul_rn(dz, dz));
   }
   return s;
 }
 
+// Largest squared distance from p to the box (an estimate; callers compare
+// it with a safety margin).
 template <int D>
-__device__ __forceinline__ float box_max_d2(float px, float py, float pz, float lx, float ly,
-                                            float lz, float hx, float hy, float hz) {
-  float dx = fmaxf(fabsf(px - lx), fabsf(hx - px));
-  float dy = fmaxf(fabsf(py - ly), fabsf(hy - py));
+__device__ __forceinline__ float box_max_d2(const float4& q, const float4& xy, float lz, float hz) {
+  float dx = fmaxf(fabsf(q.x - xy.x), fabsf(xy.z - q.x));
+  float dy = fmaxf(fabsf(q.y - xy.y), fabsf(xy.w - q.y));
   float s = dx * dx + dy * dy;
   if constexpr (D == 3) {
-    float dz = fmaxf(fabsf(pz - lz), fabsf(hz - pz));
+    float dz = fmaxf(fabsf(q.z - lz), fabsf(hz - q.z));
     s += dz * dz;
   }
   return s;
@@ -249,11 +258,7 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const float4 b = __ldg(lp + k0 + u);
-          if constexpr (D == 2) {
-            m = fminf(m, d2_2(q.x, q.y, b.x, b.y));
-          } else {
-            m = fminf(m, d2_3(q.x, q.y, q.z, b.x, b.y, b.z));
-          }
+          m = fminf(m, d2_pt_packed<D>(q, b));
         }
         k = k0 + 4;
         if (!__any_sync(0xFFFFFFFFu, active && m > thr)) {
@@ -282,11 +287,7 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const float4 b = __ldg(lp + min(k + u, cnt - 1));
-        if constexpr (D == 2) {
-          m = fminf(m, d2_2(q.x, q.y, b.x, b.y));
-        } else {
-          m = fminf(m, d2_3(q.x, q.y, q.z, b.x, b.y, b.z));
-        }
+        m = fminf(m, d2_pt_packed<D>(q, b));
       }
       if (!__any_sync(0xFFFFFFFFu, active && m > thr)) {
         k += 4;
@@ -349,14 +350,15 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
     if (have && !(next & kLeafBit)) {
       // Internal node: test both children for every lane.
       const float4* nd = nodes + 4 * (uint64_t) next;
-      const float4 n0 = nd[0], n1 = nd[1], n2 = nd[2], n3 = nd[3];
+      const float4 n0 = nd[0], n1 = nd[1], n3 = nd[3];
+      const float4 n2 = D == 3 ? nd[2] : make_float4(0.f, 0.f, 0.f, 0.f);
       ++work;
       if (COUNT) ++visits;
-      const float dL = box_min_d2<D>(q.x, q.y, q.z, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
-      const float dR = box_min_d2<D>(q.x, q.y, q.z, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+      const float dL = box_min_d2<D>(q, n0, n2.x, n2.y);
+      const float dR = box_min_d2<D>(q, n1, n2.z, n2.w);
       if (active && thr >= 0.0f) {
-        const float mL = box_max_d2<D>(q.x, q.y, q.z, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
-        const float mR = box_max_d2<D>(q.x, q.y, q.z, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+        const float mL = box_max_d2<D>(q, n0, n2.x, n2.y);
+        const float mR = box_max_d2<D>(q, n1, n2.z, n2.w);
         if (fminf(mL, mR) * kMaxDistMargin <= thr) active = false;
       }
       const bool wL = active && dL < cmin;
@@ -454,7 +456,9 @@ __global__ void k_karras(BuildSets b) {
   const BuildSet& S = b.s[blockIdx.y];
   karras_body(S.codes, S.L, S.nL, S.child, S.parent);
 }
-__global__ void k_bottom_up(BuildSets b) {
+// Latency-bound chains of atomics: full occupancy (8 blocks of 256 threads
+// per SM, at most 32 registers) matters more than a few spilled values.
+__global__ void __launch_bounds__(256, 8) k_bottom_up(BuildSets b) {
   const BuildSet& S = b.s[blockIdx.y];
   bottom_up_body(S.child, S.parent, S.nL, S.nI, S.boxes, S.leaf_boxes, S.flags, S.nodes);
 }
@@ -536,10 +540,7 @@ __global__ void __launch_bounds__(kDeferWarps * 32) k_lbvh_defer(QuerySets qs) {
           const uint32_t c = (uint32_t) min((uint64_t) S.L, S.nB - p0);
           for (uint32_t t = 0; t < c; ++t) {
             const float4 b = S.B[p0 + t];
-            if constexpr (D == 2)
-              lm = fminf(lm, d2_2(q.x, q.y, b.x, b.y));
-            else
-              lm = fminf(lm, d2_3(q.x, q.y, q.z, b.x, b.y, b.z));
+            lm = fminf(lm, d2_pt_packed<D>(q, b));
           }
           if (COUNT) {
             pairs += c;
@@ -547,9 +548,10 @@ __global__ void __launch_bounds__(kDeferWarps * 32) k_lbvh_defer(QuerySets qs) {
           }
         } else {
           const float4* nd = S.nodes + 4 * (uint64_t) node;
-          const float4 n0 = nd[0], n1 = nd[1], n2 = nd[2], n3 = nd[3];
-          const float dL = box_min_d2<D>(q.x, q.y, q.z, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
-          const float dR = box_min_d2<D>(q.x, q.y, q.z, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+          const float4 n0 = nd[0], n1 = nd[1], n3 = nd[3];
+          const float4 n2 = D == 3 ? nd[2] : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float dL = box_min_d2<D>(q, n0, n2.x, n2.y);
+          const float dR = box_min_d2<D>(q, n1, n2.z, n2.w);
           const uint32_t left = __float_as_uint(n3.x), right = __float_as_uint(n3.y);
           // Nearer child pushed last, so that it is popped first.
           const bool wL = dL < m, wR = dR < m;
