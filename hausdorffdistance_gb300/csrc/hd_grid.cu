@@ -237,23 +237,53 @@ __global__ void __launch_bounds__(128)
 }
 
 // Deferred points: one CTA each, all threads over the sorted B, early break.
+// The scan starts at the query's own position in B's Morton order (binary
+// search of its code) and grows outward in alternating forward and backward
+// chunks, so the spatially nearest B points, which decide the early break,
+// come first; a point that does not break still visits every B point.
 __global__ void __launch_bounds__(256)
-    k_grid_deferred(const float4* __restrict__ Q, const float4* __restrict__ B, uint64_t nB,
+    k_grid_deferred(const float4* __restrict__ Q, const uint32_t* __restrict__ qcodes,
+                    const float4* __restrict__ B, const uint32_t* __restrict__ bcodes, uint64_t nB,
                     int dims, const Deferred* __restrict__ list, const uint32_t* count,
                     DevScalars* sc) {
   __shared__ float red[8];
   __shared__ float s_thr;
+  constexpr uint64_t kChunk = 256 * 64;
   const uint32_t n = *count;
   for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
     const Deferred dfr = list[e];
     const float4 q = Q[dfr.qpos];
+    const uint32_t code = qcodes[dfr.qpos] & kCodeMask;
+    // First B position whose code is >= the query's (every thread finds the
+    // same one).
+    uint64_t lo = 0, hi = nB;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if ((bcodes[mid] & kCodeMask) < code) lo = mid + 1;
+      else hi = mid;
+    }
+    const uint64_t p0 = lo;
     float cmin = dfr.cmin;
     bool broke = false;
-    const uint64_t chunk = 256 * 64;
-    for (uint64_t base = 0; base < nB; base += chunk) {
+    // Chunk k: forward block k/2 = [p0 + (k/2) kChunk, +kChunk) for even k,
+    // backward block k/2 = [p0 - (k/2 + 1) kChunk, p0 - (k/2) kChunk) for
+    // odd k, clipped to [0, nB); together they cover [0, nB) once.
+    for (uint64_t k = 0;; ++k) {
+      const uint64_t f = k >> 1;
+      uint64_t b0, b1;
+      if ((k & 1) == 0) {
+        b0 = p0 + f * kChunk;
+        b1 = min(nB, b0 + kChunk);
+      } else {
+        const uint64_t back = f * kChunk;
+        b1 = p0 > back ? p0 - back : 0;
+        b0 = b1 > kChunk ? b1 - kChunk : 0;
+      }
+      const bool fwd_left = p0 + f * kChunk < nB;
+      const bool bwd_left = p0 > f * kChunk;
+      if (!fwd_left && !bwd_left) break;
       float m = INFINITY;
-      const uint64_t end = min(nB, base + chunk);
-      for (uint64_t j = base + threadIdx.x; j < end; j += 256) {
+      for (uint64_t j = b0 + threadIdx.x; j < b1; j += 256) {
         const float4 b = B[j];
         m = fminf(m, dims == 2 ? d2_2(q.x, q.y, b.x, b.y) : d2_3(q.x, q.y, q.z, b.x, b.y, b.z));
       }
@@ -262,7 +292,7 @@ __global__ void __launch_bounds__(256)
       if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
       if (threadIdx.x == 0) s_thr = threshold_of(ld_relaxed_u64(&sc->max_key));
       __syncthreads();
-      for (int k = 0; k < 8; ++k) cmin = fminf(cmin, red[k]);
+      for (int w = 0; w < 8; ++w) cmin = fminf(cmin, red[w]);
       const float thr = s_thr;
       __syncthreads();
       if (cmin <= thr) {
@@ -341,8 +371,9 @@ hd_status run_grid(Ctx& c, const DirInput& in) {
     if (phase == 0) mark(c, 3);
   }
   mark(c, 4);
-  k_grid_deferred<<<c.num_sms * 2, 256, 0, c.stream>>>(q->pts, t->pts, t->n, in.dims,
-                                                      (const Deferred*) defl, defer_count, sc);
+  k_grid_deferred<<<c.num_sms * 2, 256, 0, c.stream>>>(q->pts, q->codes, t->pts, t->codes, t->n,
+                                                      in.dims, (const Deferred*) defl, defer_count,
+                                                      sc);
   if ((s = after_launch(c, "grid_deferred")) != HD_OK) return s;
   return certify(c, in);
 }
