@@ -461,12 +461,24 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   const float* dA = A;
   const float* dB = B;
   mark_abs(*c, 24);  // start of the whole call (copies included)
-  if (!(flags & HD_DEVICE_PTRS)) {
-    if ((s = copy_in(*c, A, n_a, n_dims, kBufA, &dA)) != HD_OK) return s;
-    if ((s = copy_in(*c, B, n_b, n_dims, kBufB, &dB)) != HD_OK) return s;
-  }
-  if ((s = init_scalars(*c)) != HD_OK) return s;
   const bool undirected = (flags & HD_UNDIRECTED) != 0;
+  if ((s = init_scalars(*c)) != HD_OK) return s;
+  if (!(flags & HD_DEVICE_PTRS)) {
+    // An undirected solve known (from the sizes alone) to take the LBVH in
+    // both directions sorts A while B is still being copied.
+    int v0 = variant, v1 = variant;
+    bool known = variant != HD_VARIANT_AUTO;
+    if (!known)
+      known = select_variant_by_size(*c, n_a, n_b, n_dims, &v0) &&
+              select_variant_by_size(*c, n_b, n_a, n_dims, &v1);
+    if (undirected && known && v0 == HD_VARIANT_LBVH && v1 == HD_VARIANT_LBVH &&
+        n_a + n_b >= kSplitMinPoints) {
+      if ((s = spatial_upload_sort(*c, A, n_a, B, n_b, n_dims, &dA, &dB)) != HD_OK) return s;
+    } else {
+      if ((s = copy_in(*c, A, n_a, n_dims, kBufA, &dA)) != HD_OK) return s;
+      if ((s = copy_in(*c, B, n_b, n_dims, kBufB, &dB)) != HD_OK) return s;
+    }
+  }
   const bool count = (flags & HD_COUNT_PAIRS) != 0;
   const int ndir = undirected ? 2 : 1;
   DirResult ex[2];

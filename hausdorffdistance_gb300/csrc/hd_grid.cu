@@ -5,7 +5,7 @@
 // resolution, :343-484 insert, :542-589 tight cell boxes) and its use as the
 // RT search's primitive set (hausdorff_distance_hybrid.h:203-227).
 //
-// Build: in the common cubic Morton frame, grid level g groups 2^g x 2^g
+// Build: in B's cubic Morton frame, grid level g groups 2^g x 2^g
 // (x 2^g) finest Morton cells into one grid cell, so a grid cell is a
 // contiguous run of the Morton-sorted points — no counting, scan or scatter.
 // The level follows the reference's resolution rule (cell side s =
@@ -139,7 +139,7 @@ struct Deferred {
 
 template <int D, bool COUNT>
 __global__ void __launch_bounds__(128)
-    k_grid_query(const float4* __restrict__ Q, const uint32_t* __restrict__ qcodes, uint64_t nQ,
+    k_grid_query(const float4* __restrict__ Q, const Frame* __restrict__ tframe, uint64_t nQ,
                  const float4* __restrict__ B, const uint2* __restrict__ table,
                  const GridParams* __restrict__ gpp, int ring_cap, uint32_t pstride, int phase,
                  DevScalars* sc, Deferred* __restrict__ deferred, uint32_t* defer_count) {
@@ -153,17 +153,14 @@ __global__ void __launch_bounds__(128)
   if (i >= nQ) return;
   const float4 q4 = Q[i];
   const float p[3] = {q4.x, q4.y, q4.z};
-  const uint32_t cc = (qcodes[i] & kCodeMask) >> gp.shift;
+  // Home cell: the point's cell in the target set's frame at the grid level
+  // (points outside that frame start from its border cells).
+  const Frame tf = *tframe;
+  const uint32_t maxq = (1u << tf.bits) - 1u;
   int home[3];
-  if (D == 2) {
-    home[0] = (int) compact2(cc);
-    home[1] = (int) compact2(cc >> 1);
-    home[2] = 0;
-  } else {
-    home[0] = (int) compact3(cc);
-    home[1] = (int) compact3(cc >> 1);
-    home[2] = (int) compact3(cc >> 2);
-  }
+  home[0] = (int) (frame_quant(p[0], tf.lo[0], tf.scale, maxq) >> gp.g);
+  home[1] = (int) (frame_quant(p[1], tf.lo[1], tf.scale, maxq) >> gp.g);
+  home[2] = D == 3 ? (int) (frame_quant(p[2], tf.lo[2], tf.scale, maxq) >> gp.g) : 0;
   const int cpa = (int) gp.cpa;
   float cmin = INFINITY;
   float thr = threshold_of(ld_relaxed_u64(&sc->max_key));
@@ -238,11 +235,11 @@ __global__ void __launch_bounds__(128)
 
 // Deferred points: one CTA each, all threads over the sorted B, early break.
 // The scan starts at the query's own position in B's Morton order (binary
-// search of its code) and grows outward in alternating forward and backward
+// search of its code in B's frame) and grows outward in alternating forward and backward
 // chunks, so the spatially nearest B points, which decide the early break,
 // come first; a point that does not break still visits every B point.
 __global__ void __launch_bounds__(256)
-    k_grid_deferred(const float4* __restrict__ Q, const uint32_t* __restrict__ qcodes,
+    k_grid_deferred(const float4* __restrict__ Q, const Frame* __restrict__ tframe,
                     const float4* __restrict__ B, const uint32_t* __restrict__ bcodes, uint64_t nB,
                     int dims, const Deferred* __restrict__ list, const uint32_t* count,
                     DevScalars* sc) {
@@ -253,7 +250,7 @@ __global__ void __launch_bounds__(256)
   for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
     const Deferred dfr = list[e];
     const float4 q = Q[dfr.qpos];
-    const uint32_t code = qcodes[dfr.qpos] & kCodeMask;
+    const uint32_t code = frame_code(*tframe, q.x, q.y, q.z);
     // First B position whose code is >= the query's (every thread finds the
     // same one).
     uint64_t lo = 0, hi = nB;
@@ -324,7 +321,7 @@ hd_status run_grid(Ctx& c, const DirInput& in) {
   // The set this grid indexes is the call's A for direction 1, B otherwise.
   const uint32_t* ordT = &scalars(c, 0)->mbr_ord[t == &c.sorted[0] ? 0 : 1][0][0];
   const uint32_t k = c.opt.n_points_cell ? c.opt.n_points_cell : 8;
-  k_grid_params<<<1, 32, 0, c.stream>>>(frame(c), ordT, t->n, in.dims, k, gp);
+  k_grid_params<<<1, 32, 0, c.stream>>>(t->frame, ordT, t->n, in.dims, k, gp);
   if ((s = after_launch(c, "grid_params")) != HD_OK) return s;
   cudaError_t e = cudaMemsetAsync(defer_count, 0, 4, c.stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "memset");
@@ -351,27 +348,27 @@ hd_status run_grid(Ctx& c, const DirInput& in) {
     if (in.dims == 2) {
       if (in.count)
         k_grid_query<2, true><<<blocks, 128, 0, c.stream>>>(
-            q->pts, q->codes, q->n, t->pts, (const uint2*) table, gp, ring_cap, pstride, phase, sc,
+            q->pts, t->frame, q->n, t->pts, (const uint2*) table, gp, ring_cap, pstride, phase, sc,
             (Deferred*) defl, defer_count);
       else
         k_grid_query<2, false><<<blocks, 128, 0, c.stream>>>(
-            q->pts, q->codes, q->n, t->pts, (const uint2*) table, gp, ring_cap, pstride, phase, sc,
+            q->pts, t->frame, q->n, t->pts, (const uint2*) table, gp, ring_cap, pstride, phase, sc,
             (Deferred*) defl, defer_count);
     } else {
       if (in.count)
         k_grid_query<3, true><<<blocks, 128, 0, c.stream>>>(
-            q->pts, q->codes, q->n, t->pts, (const uint2*) table, gp, ring_cap, pstride, phase, sc,
+            q->pts, t->frame, q->n, t->pts, (const uint2*) table, gp, ring_cap, pstride, phase, sc,
             (Deferred*) defl, defer_count);
       else
         k_grid_query<3, false><<<blocks, 128, 0, c.stream>>>(
-            q->pts, q->codes, q->n, t->pts, (const uint2*) table, gp, ring_cap, pstride, phase, sc,
+            q->pts, t->frame, q->n, t->pts, (const uint2*) table, gp, ring_cap, pstride, phase, sc,
             (Deferred*) defl, defer_count);
     }
     if ((s = after_launch(c, "grid_query")) != HD_OK) return s;
     if (phase == 0) mark(c, 3);
   }
   mark(c, 4);
-  k_grid_deferred<<<c.num_sms * 2, 256, 0, c.stream>>>(q->pts, q->codes, t->pts, t->codes, t->n,
+  k_grid_deferred<<<c.num_sms * 2, 256, 0, c.stream>>>(q->pts, t->frame, t->pts, t->codes, t->n,
                                                       in.dims, (const Deferred*) defl, defer_count,
                                                       sc);
   if ((s = after_launch(c, "grid_deferred")) != HD_OK) return s;

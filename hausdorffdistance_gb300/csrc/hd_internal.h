@@ -10,8 +10,14 @@
 
 namespace hdg {
 
-// Bits of a sorted key that hold the Morton code (bit 30 marks the set).
+// Bits of a sorted key that hold the Morton code (bit 30 marks the set in
+// the fused sort of small sets).
 constexpr uint32_t kCodeMask = (1u << 30) - 1u;
+// From this many points (|A| + |B|) the two sets are sorted as independent
+// chains, each in its own frame (and, for host inputs, A's sort overlaps
+// B's copy); below it one fused chain in a common frame has fewer launches
+// and aligned Morton orders.
+constexpr uint64_t kSplitMinPoints = 4000000;
 
 // Device scalars of one directed solve, zeroed with one memset per solve.
 struct DevScalars {
@@ -72,18 +78,57 @@ enum BufSlot {
   kNumBufs
 };
 
-// Common cubic frame of both point sets (device resident, after the two
-// DevScalars in the scalars buffer).
+// Cubic Morton frame of a sorted point set (device resident, two of them
+// after the two DevScalars in the scalars buffer; frame k belongs to
+// c.sorted[k], or frame 0 to both sets when they share a common frame).  A
+// query set's points are coded in the target set's frame (frame_code)
+// wherever they meet the target's sorted codes.
 struct Frame {
   float lo[3], hi[3];
   float scale, extent;  // quantisation scale (cells per unit), max extent
   int bits, dims;       // Morton bits per axis, dimensionality
 };
 
+#ifdef __CUDACC__
+__device__ __forceinline__ uint32_t morton_spread2(uint32_t x) {  // 16 bits -> even bits
+  x &= 0xFFFFu;
+  x = (x | (x << 8)) & 0x00FF00FFu;
+  x = (x | (x << 4)) & 0x0F0F0F0Fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+__device__ __forceinline__ uint32_t morton_spread3(uint32_t x) {  // 10 bits -> every 3rd bit
+  x &= 0x3FFu;
+  x = (x | (x << 16)) & 0x030000FFu;
+  x = (x | (x << 8)) & 0x0300F00Fu;
+  x = (x | (x << 4)) & 0x030C30C3u;
+  x = (x | (x << 2)) & 0x09249249u;
+  return x;
+}
+// Cell index of coordinate v along one axis, clamped to the frame.
+__device__ __forceinline__ uint32_t frame_quant(float v, float lo, float scale, uint32_t maxq) {
+  float q = (v - lo) * scale;
+  q = fminf(fmaxf(q, 0.0f), (float) maxq);
+  return (uint32_t) q;
+}
+// Morton code of a point in frame f (points outside the frame clamp to its
+// border cells).
+__device__ __forceinline__ uint32_t frame_code(const Frame& f, float x, float y, float z) {
+  const uint32_t maxq = (1u << f.bits) - 1u;
+  const uint32_t qx = frame_quant(x, f.lo[0], f.scale, maxq);
+  const uint32_t qy = frame_quant(y, f.lo[1], f.scale, maxq);
+  if (f.dims == 2) return morton_spread2(qx) | (morton_spread2(qy) << 1);
+  const uint32_t qz = frame_quant(z, f.lo[2], f.scale, maxq);
+  return morton_spread3(qx) | (morton_spread3(qy) << 1) | (morton_spread3(qz) << 2);
+}
+#endif
+
 // A point set in Morton order: float4 (x, y, z|0, caller index as bits).
 struct SortedSet {
   float4* pts = nullptr;
-  uint32_t* codes = nullptr;   // sorted keys: Morton code in bits 0-29 (mask kCodeMask)
+  uint32_t* codes = nullptr;   // sorted Morton codes (30 bits) in this set's frame
+  const Frame* frame = nullptr;  // that frame (device)
   float4* leaf_boxes = nullptr;  // per leaf of leaf_size points: lo, hi
   uint32_t leaf_size = 16;
   uint64_t n = 0;
@@ -181,6 +226,9 @@ hd_status run_bf16(Ctx& c, const DirInput& in, DirResult* extra);
 // Test hook: the BF16 kernel's approximate row minima (no certification).
 hd_status bf16_rowmin_debug(Ctx& c, const DirInput& in, float* rowmin_host);
 hd_status select_variant(Ctx& c, const DirInput& in, int* variant);
+// The selector's choice when the sizes alone decide it (no sampling of the
+// data); false when it needs the sample pass.
+bool select_variant_by_size(const Ctx& c, uint64_t nA, uint64_t nB, int dims, int* variant);
 
 // Common tail: exact argmin of A[ia] over B, FP64 recomputation, written to
 // DevScalars[dir].  Used by every variant.
@@ -197,12 +245,16 @@ void mark(Ctx& c, int phase_event);
 uint64_t pick_multiplier(uint64_t n, uint64_t seed);
 
 // Spatial preparation (hd_spatial.cu).
-Frame* frame(Ctx& c);
+Frame* frame(Ctx& c, int set);
 size_t scalars_bytes();
 // Morton-sorts the call's two point sets (both, once per hd_solve) and
 // returns the ones matching a directed input: *q = in.A, *t = in.B.
 hd_status spatial_prepare(Ctx& c, const DirInput& in, const SortedSet** q,
                           const SortedSet** t);
+// Host inputs: copies A, sorts it while B is copied on the side stream,
+// then sorts B (sets c.sorted, c.sorted_valid); *dA, *dB = device copies.
+hd_status spatial_upload_sort(Ctx& c, const float* hA, uint64_t nA, const float* hB, uint64_t nB,
+                              int dims, const float** dA, const float** dB);
 // k random positions in [0, n) (with replacement), k from opt.sample_rate.
 hd_status make_sample(Ctx& c, uint64_t n, uint64_t seed, uint32_t* k, uint32_t** list);
 

@@ -309,9 +309,9 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   };
 
   {
-    // Warm start: queries and B share one Morton frame, so the B leaves at
-    // the packet's position in B's sorted codes (precomputed per packet) are
-    // spatially close.  Scanning that leaf and its neighbours lets most lanes
+    // Warm start: a query's Morton code in B's frame locates it in B's
+    // sorted codes, so the B leaves at the packet's position (precomputed
+    // per packet) are spatially close.  Scanning that leaf and its neighbours lets most lanes
     // stop before any traversal, and gives the others a small running
     // minimum that prunes the traversal.
     const uint32_t lshift = __ffs(L) - 1;  // L is a power of two
@@ -410,18 +410,19 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   }
 }
 
-// Position of every packet's first query in B's sorted codes (lower bound),
-// one binary search per packet.
 // Positions of every packet's first and last query in B's sorted codes
 // (lower bounds), one thread per packet end.
-__device__ __forceinline__ void packet_pos_body(const uint32_t* __restrict__ qcodes, uint64_t nQ,
+__device__ __forceinline__ void packet_pos_body(const float4* __restrict__ Q, uint64_t nQ,
+                                                const Frame* __restrict__ tframe,
                                                 const uint32_t* __restrict__ bcodes, uint64_t nB,
                                                 uint32_t* __restrict__ pos) {
   const uint64_t t = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
   const uint64_t p = t >> 1;
   if (p * 32 >= nQ) return;
   const uint64_t q = (t & 1) ? min(p * 32 + 31, nQ - 1) : p * 32;
-  const uint32_t target = qcodes[q] & kCodeMask;
+  // The query's code in the target set's frame.
+  const float4 qp = Q[q];
+  const uint32_t target = frame_code(*tframe, qp.x, qp.y, qp.z);
   uint64_t lo = 0, hi = nB;
   while (lo < hi) {
     const uint64_t mid = (lo + hi) >> 1;
@@ -476,7 +477,7 @@ struct QuerySet {
   uint64_t nB;
   uint32_t L;
   DevScalars* sc;
-  const uint32_t* qcodes;
+  const Frame* tframe;  // frame of the target set's codes
   const uint32_t* bcodes;
 };
 struct QuerySets {
@@ -609,7 +610,7 @@ __global__ void __launch_bounds__(kDeferWarps * 32) k_lbvh_defer(QuerySets qs) {
 
 __global__ void k_packet_pos(QuerySets qs) {
   const QuerySet& S = qs.d[blockIdx.y];
-  packet_pos_body(S.qcodes, S.nQ, S.bcodes, S.nB, const_cast<uint32_t*>(S.ppos));
+  packet_pos_body(S.Q, S.nQ, S.tframe, S.bcodes, S.nB, const_cast<uint32_t*>(S.ppos));
 }
 
 }  // namespace
@@ -702,13 +703,13 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
     d.ppos = (const uint32_t*) ppos + off;
     d.B = t[k]->pts;
     d.nB = t[k]->n;
-    d.qcodes = q[k]->codes;
+    d.tframe = t[k]->frame;
     d.bcodes = t[k]->codes;
     off += 2 * packets[k];
     max_pos_threads = std::max<uint64_t>(max_pos_threads, 2 * packets[k]);
   }
   if (count == 1) qs.d[1] = qs.d[0];
-  // Packet positions need only the sorted codes: they run on the side
+  // Packet positions need only the sorted sets: they run on the side
   // stream while the (latency-bound) tree build runs on the main one.
   cudaEventRecord(c.batch_fork, c.stream);
   cudaStreamWaitEvent(c.batch_side, c.batch_fork, 0);

@@ -122,23 +122,28 @@ __global__ void k_seed_finish(Perm pA, uint32_t offset, const uint32_t* __restri
 
 }  // namespace
 
-hd_status select_variant(Ctx& c, const DirInput& in, int* v) {
+bool select_variant_by_size(const Ctx& c, uint64_t nA, uint64_t nB, int dims, int* v) {
   const Tuning& tu = tuning();
-  if (in.dims != 2 && in.dims != 3) {
-    const double pairs = (double) in.nA * (double) in.nB;
-    *v = (in.dims % 16 == 0 && pairs >= tu.bf16_min_pairs) ? HD_VARIANT_BF16 : HD_VARIANT_EB;
-    return HD_OK;
+  const double pairs = (double) nA * (double) nB;
+  if (dims != 2 && dims != 3) {
+    *v = (dims % 16 == 0 && pairs >= tu.bf16_min_pairs) ? HD_VARIANT_BF16 : HD_VARIANT_EB;
+    return true;
   }
-  const double pairs = (double) in.nA * (double) in.nB;
   const bool sample = c.opt.always_sample != 0;
   if (!sample && pairs <= tu.eb_small_pairs) {
     *v = HD_VARIANT_EB;
-    return HD_OK;
+    return true;
   }
   if (!sample && pairs >= tu.index_min_pairs) {
     *v = tu.prefer_grid ? HD_VARIANT_GRID : HD_VARIANT_LBVH;
-    return HD_OK;
+    return true;
   }
+  return false;
+}
+
+hd_status select_variant(Ctx& c, const DirInput& in, int* v) {
+  const Tuning& tu = tuning();
+  if (select_variant_by_size(c, in.nA, in.nB, in.dims, v)) return HD_OK;
   const double rate = c.opt.sample_rate > 0 ? c.opt.sample_rate : 0.01;
   uint32_t k = (uint32_t) std::min<double>(std::max<double>(rate * (double) in.nA, 64.0), 256.0);
   k = (uint32_t) std::min<uint64_t>(k, in.nA);

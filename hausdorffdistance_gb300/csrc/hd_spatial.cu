@@ -1,6 +1,9 @@
-// Spatial preparation shared by the LBVH and grid variants: one fused pass
-// for both bounding boxes, Morton codes in a common cubic frame, a radix sort
-// per set, and a gather into Morton order as float4 (x, y, z, caller index).
+// Spatial preparation shared by the LBVH and grid variants: bounding boxes,
+// Morton codes in a cubic frame, a radix sort, and a gather into Morton
+// order as float4 (x, y, z, caller index).  Large sets run as two
+// independent chains, each set in its own frame (main stream and side
+// stream), so for host inputs A is sorted while B is still being copied;
+// small sets run one fused chain in a common frame.
 //
 // Replaces the reference's MBR reduction (src/geoms/mbr.h:307-321: thrust
 // for_each with CAS float atomics per point) and the first half of the grid
@@ -18,7 +21,7 @@
 namespace hdg {
 namespace {
 
-// Bounding boxes of both sets in one launch (blockIdx.y = set): per-thread
+// Bounding boxes of one or two sets in one launch (blockIdx.y = set): per-thread
 // min/max, a warp reduction, one shared atomic per warp and one global
 // atomic per CTA and dimension on the order-preserving integer image of the
 // float.  When the array is 16-byte aligned, 4 points (3-D) or 2 points (2-D)
@@ -110,8 +113,7 @@ __global__ void k_frame(const uint32_t* __restrict__ ordA, const uint32_t* __res
     fr->hi[k] = hi;
     ext = fmaxf(ext, hi - lo);
   }
-  // 30-bit codes in both cases, leaving bit 30 for the set when both sets
-  // are sorted together.
+  // 30-bit codes in both cases.
   const int bits = dims == 2 ? 15 : 10;
   fr->bits = bits;
   fr->dims = dims;
@@ -120,27 +122,58 @@ __global__ void k_frame(const uint32_t* __restrict__ ordA, const uint32_t* __res
   fr->scale = ext > 0.0f ? (float) ((1u << bits) - 1) / ext : 0.0f;
 }
 
-__device__ __forceinline__ uint32_t spread2(uint32_t x) {  // 16 bits -> even bits
-  x &= 0xFFFFu;
-  x = (x | (x << 8)) & 0x00FF00FFu;
-  x = (x | (x << 4)) & 0x0F0F0F0Fu;
-  x = (x | (x << 2)) & 0x33333333u;
-  x = (x | (x << 1)) & 0x55555555u;
-  return x;
-}
-__device__ __forceinline__ uint32_t spread3(uint32_t x) {  // 10 bits -> every 3rd bit
-  x &= 0x3FFu;
-  x = (x | (x << 16)) & 0x030000FFu;
-  x = (x | (x << 8)) & 0x0300F00Fu;
-  x = (x | (x << 4)) & 0x030C30C3u;
-  x = (x | (x << 2)) & 0x09249249u;
-  return x;
+// Morton codes of one set in its frame: key = code, value = row.
+__global__ void k_morton1(const float* __restrict__ P, uint64_t n, int dims,
+                          const Frame* __restrict__ fr, uint32_t* __restrict__ keys,
+                          uint32_t* __restrict__ vals) {
+  const Frame f = *fr;
+  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t) gridDim.x * blockDim.x) {
+    const float x = P[i * dims], y = P[i * dims + 1];
+    const float z = dims == 3 ? P[i * dims + 2] : 0.0f;
+    keys[i] = frame_code(f, x, y, z);
+    vals[i] = (uint32_t) i;
+  }
 }
 
-__device__ __forceinline__ uint32_t quant(float v, float lo, float scale, uint32_t maxq) {
-  float q = (v - lo) * scale;
-  q = fminf(fmaxf(q, 0.0f), (float) maxq);
-  return (uint32_t) q;
+// Gathers one sorted set into float4 (x, y, z, caller index) and, in the
+// same pass, the bounding box of every leaf of L consecutive sorted points
+// (L a power of two <= 32; lanes of a warp cover whole leaves, reduced with
+// shuffles).
+__global__ void k_gather1(const float* __restrict__ P, uint64_t n, int dims,
+                          const uint32_t* __restrict__ order, float4* __restrict__ out, uint32_t L,
+                          float4* __restrict__ lb) {
+  const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+  for (uint64_t j0 = blockIdx.x * (uint64_t) blockDim.x + (threadIdx.x & ~31u); j0 < n; j0 += stride) {
+    const uint64_t j = j0 + (threadIdx.x & 31u);
+    const bool valid = j < n;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    float lx = FLT_MAX, ly = FLT_MAX, lz = FLT_MAX, hx = -FLT_MAX, hy = -FLT_MAX, hz = -FLT_MAX;
+    if (valid) {
+      const uint64_t r = order[j];
+      p.x = P[r * dims];
+      p.y = P[r * dims + 1];
+      p.z = dims == 3 ? P[r * dims + 2] : 0.0f;
+      p.w = __uint_as_float((uint32_t) r);
+      out[j] = p;
+      lx = hx = p.x;
+      ly = hy = p.y;
+      lz = hz = p.z;
+    }
+    for (uint32_t o = 1; o < L; o <<= 1) {
+      lx = fminf(lx, __shfl_xor_sync(0xFFFFFFFFu, lx, o));
+      ly = fminf(ly, __shfl_xor_sync(0xFFFFFFFFu, ly, o));
+      lz = fminf(lz, __shfl_xor_sync(0xFFFFFFFFu, lz, o));
+      hx = fmaxf(hx, __shfl_xor_sync(0xFFFFFFFFu, hx, o));
+      hy = fmaxf(hy, __shfl_xor_sync(0xFFFFFFFFu, hy, o));
+      hz = fmaxf(hz, __shfl_xor_sync(0xFFFFFFFFu, hz, o));
+    }
+    if (valid && (j & (L - 1)) == 0) {
+      const uint64_t leaf = j / L;
+      lb[2 * leaf] = make_float4(lx, ly, lz, 0.f);
+      lb[2 * leaf + 1] = make_float4(hx, hy, hz, 0.f);
+    }
+  }
 }
 
 // Morton codes of both sets in one launch (blockIdx.y = set); the key carries
@@ -158,12 +191,12 @@ __global__ void k_morton2(const float* __restrict__ A, uint64_t nA, const float*
        i += (uint64_t) gridDim.x * blockDim.x) {
     uint32_t code;
     if (dims == 2) {
-      code = spread2(quant(P[2 * i], lo0, s, maxq)) |
-             (spread2(quant(P[2 * i + 1], lo1, s, maxq)) << 1);
+      code = morton_spread2(frame_quant(P[2 * i], lo0, s, maxq)) |
+             (morton_spread2(frame_quant(P[2 * i + 1], lo1, s, maxq)) << 1);
     } else {
-      code = spread3(quant(P[3 * i], lo0, s, maxq)) |
-             (spread3(quant(P[3 * i + 1], lo1, s, maxq)) << 1) |
-             (spread3(quant(P[3 * i + 2], lo2, s, maxq)) << 2);
+      code = morton_spread3(frame_quant(P[3 * i], lo0, s, maxq)) |
+             (morton_spread3(frame_quant(P[3 * i + 1], lo1, s, maxq)) << 1) |
+             (morton_spread3(frame_quant(P[3 * i + 2], lo2, s, maxq)) << 2);
     }
     keys[base + i] = code | setbit;
     vals[base + i] = (uint32_t) (base + i);
@@ -243,31 +276,30 @@ int grid_for(Ctx& c, uint64_t n, int per = 256) {
 
 }  // namespace
 
-Frame* frame(Ctx& c) {
-  return reinterpret_cast<Frame*>(reinterpret_cast<DevScalars*>(c.bufs[kBufScalars].p) + 2);
+Frame* frame(Ctx& c, int set) {
+  return reinterpret_cast<Frame*>(reinterpret_cast<DevScalars*>(c.bufs[kBufScalars].p) + 2) + set;
 }
 
-static hd_status spatial_sort(Ctx& c, const float* A, uint64_t nA, const float* B,
-                              uint64_t nB, int dims, SortedSet* sa, SortedSet* sb) {
-  const bool need_a = true, need_b = true;
-  hd_status s;
-  DevScalars* sc = scalars(c, 0);
-  // One bounding box per set (both boxes feed the common frame).
-  {
-    const int gx = grid_for(c, (std::max(nA, nB) + 3) / 4, 256);
-    k_mbr2<<<dim3(gx, 2), 256, 0, c.stream>>>(A, nA, B, nB, dims, &sc->mbr_ord[0][0][0],
-                                              &sc->mbr_ord[1][0][0]);
-    if ((s = after_launch(c, "mbr")) != HD_OK) return s;
-  }
-  k_frame<<<1, 32, 0, c.stream>>>(&sc->mbr_ord[0][0][0], &sc->mbr_ord[1][0][0], dims, 1, 1,
-                                  frame(c));
-  if ((s = after_launch(c, "frame")) != HD_OK) return s;
+namespace {
 
-  // One sort of both sets: key = 30-bit code | set << 30, value = global row.
+// Scratch of both sets' sorts, allocated before either chain launches (an
+// allocation may synchronise the device).  Set 1 uses the upper halves.
+struct SortScratch {
+  uint32_t *keys, *keys2, *vals, *vals2;
+  unsigned char* tmp;
+  size_t tmp_bytes, tmp_stride;
+  float4* pts;
+  float4* lboxes;
+  uint64_t nA, leaves_a;
+  uint32_t L;
+};
+
+hd_status sort_scratch(Ctx& c, uint64_t nA, uint64_t nB, bool fused, SortScratch* x) {
   const uint64_t n = nA + nB;
   uint32_t L = c.opt.leaf_size ? std::min<uint32_t>(c.opt.leaf_size, 32) : 16;
   while (L & (L - 1)) L &= L - 1;
   const uint64_t leaves_a = (nA + L - 1) / L, leaves_b = (nB + L - 1) / L;
+  hd_status s;
   void *keys, *keys2, *vals, *vals2, *tmp, *pts, *lboxes;
   if ((s = ensure(c, kBufKeys, n * 4, &keys)) != HD_OK) return s;
   if ((s = ensure(c, kBufKeysAlt, n * 4, &keys2)) != HD_OK) return s;
@@ -276,34 +308,152 @@ static hd_status spatial_sort(Ctx& c, const float* A, uint64_t nA, const float* 
   if ((s = ensure(c, kBufSorted0, n * sizeof(float4), &pts)) != HD_OK) return s;
   if ((s = ensure(c, kBufCodes0, (leaves_a + leaves_b) * 2 * sizeof(float4), &lboxes)) != HD_OK)
     return s;
+  // Fused: one sort of both sets (set in bit 30); else one sort per set,
+  // each with its own temporary region.
   size_t tmp_bytes = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, (const uint32_t*) keys, (uint32_t*) keys2,
-                                  (const uint32_t*) vals, (uint32_t*) vals2, (int64_t) n, 0, 31,
+                                  (const uint32_t*) vals, (uint32_t*) vals2,
+                                  (int64_t) (fused ? n : std::max(nA, nB)), 0, fused ? 31 : 30,
                                   c.stream);
-  if ((s = ensure(c, kBufCubTemp, tmp_bytes, &tmp)) != HD_OK) return s;
-  {
-    const int gx = grid_for(c, std::max(nA, nB));
-    k_morton2<<<dim3(gx, 2), 256, 0, c.stream>>>(A, nA, B, nB, dims, frame(c), (uint32_t*) keys,
-                                                (uint32_t*) vals);
-    if ((s = after_launch(c, "morton")) != HD_OK) return s;
-  }
-  size_t tb = tmp_bytes;
-  cudaError_t e = cub::DeviceRadixSort::SortPairs(tmp, tb, (const uint32_t*) keys,
-                                                  (uint32_t*) keys2, (const uint32_t*) vals,
-                                                  (uint32_t*) vals2, (int64_t) n, 0, 31, c.stream);
-  if (e != cudaSuccess) return cuda_fail(c, e, "radix sort");
-  k_gather2<<<dim3(grid_for(c, std::max(nA, nB)), 2), 256, 0, c.stream>>>(
-      A, nA, B, nB, dims, (const uint32_t*) vals2, (float4*) pts, L, (float4*) lboxes, leaves_a);
-  if ((s = after_launch(c, "gather")) != HD_OK) return s;
-  *sa = SortedSet{(float4*) pts, (uint32_t*) keys2, (float4*) lboxes, L, nA, dims, A};
-  *sb = SortedSet{(float4*) pts + nA, (uint32_t*) keys2 + nA, (float4*) lboxes + 2 * leaves_a, L,
-                  nB, dims, B};
-  (void) need_a;
-  (void) need_b;
+  const size_t stride = (tmp_bytes + 255) & ~(size_t) 255;
+  if ((s = ensure(c, kBufCubTemp, (fused ? 1 : 2) * stride, &tmp)) != HD_OK) return s;
+  *x = SortScratch{(uint32_t*) keys, (uint32_t*) keys2, (uint32_t*) vals, (uint32_t*) vals2,
+                   (unsigned char*) tmp, tmp_bytes, stride, (float4*) pts, (float4*) lboxes,
+                   nA, leaves_a, L};
   return HD_OK;
 }
 
-size_t scalars_bytes() { return 2 * sizeof(DevScalars) + sizeof(Frame); }
+// Sorts set k (0 = the call's A, 1 = its B) on stream st: bounding box, its
+// frame, Morton codes, radix sort, gather with leaf boxes.
+hd_status sort_set(Ctx& c, int k, const float* P, uint64_t n, int dims, const SortScratch& x,
+                   cudaStream_t st, SortedSet* out) {
+  hd_status s;
+  const uint64_t base = k ? x.nA : 0;
+  uint32_t* ord = &scalars(c, 0)->mbr_ord[k][0][0];
+  Frame* fr = frame(c, k);
+  {
+    const int gx = grid_for(c, (n + 3) / 4, 256);
+    k_mbr2<<<dim3(gx, 1), 256, 0, st>>>(P, n, P, n, dims, ord, ord);
+    if ((s = after_launch(c, "mbr")) != HD_OK) return s;
+  }
+  k_frame<<<1, 32, 0, st>>>(ord, ord, dims, 1, 0, fr);
+  if ((s = after_launch(c, "frame")) != HD_OK) return s;
+  k_morton1<<<grid_for(c, n), 256, 0, st>>>(P, n, dims, fr, x.keys + base, x.vals + base);
+  if ((s = after_launch(c, "morton")) != HD_OK) return s;
+  size_t tb = x.tmp_bytes;
+  cudaError_t e = cub::DeviceRadixSort::SortPairs(
+      x.tmp + (size_t) k * x.tmp_stride, tb, (const uint32_t*) x.keys + base, x.keys2 + base,
+      (const uint32_t*) x.vals + base, x.vals2 + base, (int64_t) n, 0, 30, st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "radix sort");
+  float4* lb = x.lboxes + (k ? 2 * x.leaves_a : 0);
+  k_gather1<<<grid_for(c, n), 256, 0, st>>>(P, n, dims, x.vals2 + base, x.pts + base, x.L, lb);
+  if ((s = after_launch(c, "gather")) != HD_OK) return s;
+  SortedSet& o = *out;
+  o.pts = x.pts + base;
+  o.codes = x.keys2 + base;
+  o.frame = fr;
+  o.leaf_boxes = lb;
+  o.leaf_size = x.L;
+  o.n = n;
+  o.dims = dims;
+  o.src = P;
+  return HD_OK;
+}
+
+}  // namespace
+
+// Small sets: one fused chain (both boxes, one common frame, both sets'
+// codes, one sort with the set in bit 30, both gathers), so a query set's
+// Morton order matches the target's exactly and the launches are few.
+static hd_status spatial_sort_fused(Ctx& c, const float* A, uint64_t nA, const float* B,
+                                    uint64_t nB, int dims, SortedSet* sa, SortedSet* sb) {
+  hd_status s;
+  SortScratch x;
+  if ((s = sort_scratch(c, nA, nB, true, &x)) != HD_OK) return s;
+  DevScalars* sc = scalars(c, 0);
+  {
+    const int gx = grid_for(c, (std::max(nA, nB) + 3) / 4, 256);
+    k_mbr2<<<dim3(gx, 2), 256, 0, c.stream>>>(A, nA, B, nB, dims, &sc->mbr_ord[0][0][0],
+                                              &sc->mbr_ord[1][0][0]);
+    if ((s = after_launch(c, "mbr")) != HD_OK) return s;
+  }
+  Frame* fr = frame(c, 0);
+  k_frame<<<1, 32, 0, c.stream>>>(&sc->mbr_ord[0][0][0], &sc->mbr_ord[1][0][0], dims, 1, 1, fr);
+  if ((s = after_launch(c, "frame")) != HD_OK) return s;
+  {
+    const int gx = grid_for(c, std::max(nA, nB));
+    k_morton2<<<dim3(gx, 2), 256, 0, c.stream>>>(A, nA, B, nB, dims, fr, x.keys, x.vals);
+    if ((s = after_launch(c, "morton")) != HD_OK) return s;
+  }
+  size_t tb = x.tmp_bytes;
+  cudaError_t e = cub::DeviceRadixSort::SortPairs(x.tmp, tb, (const uint32_t*) x.keys, x.keys2,
+                                                  (const uint32_t*) x.vals, x.vals2,
+                                                  (int64_t) (nA + nB), 0, 31, c.stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "radix sort");
+  k_gather2<<<dim3(grid_for(c, std::max(nA, nB)), 2), 256, 0, c.stream>>>(
+      A, nA, B, nB, dims, x.vals2, x.pts, x.L, x.lboxes, x.leaves_a);
+  if ((s = after_launch(c, "gather")) != HD_OK) return s;
+  *sa = SortedSet{x.pts, x.keys2, fr, x.lboxes, x.L, nA, dims, A};
+  *sb = SortedSet{x.pts + nA, x.keys2 + nA, fr, x.lboxes + 2 * x.leaves_a, x.L, nB, dims, B};
+  return HD_OK;
+}
+
+// Large sets: A's chain (own frame) on the main stream, B's on the side
+// stream, joined before anything reads the sorted sets.
+static hd_status spatial_sort(Ctx& c, const float* A, uint64_t nA, const float* B,
+                              uint64_t nB, int dims, SortedSet* sa, SortedSet* sb) {
+  if (nA + nB < kSplitMinPoints) return spatial_sort_fused(c, A, nA, B, nB, dims, sa, sb);
+  hd_status s;
+  SortScratch x;
+  if ((s = sort_scratch(c, nA, nB, false, &x)) != HD_OK) return s;
+  if ((s = ensure_side(c)) != HD_OK) return s;
+  cudaError_t e;
+  if ((e = cudaEventRecord(c.batch_fork, c.stream)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(c.batch_side, c.batch_fork, 0)) != cudaSuccess)
+    return cuda_fail(c, e, "fork");
+  if ((s = sort_set(c, 0, A, nA, dims, x, c.stream, sa)) != HD_OK) return s;
+  if ((s = sort_set(c, 1, B, nB, dims, x, c.batch_side, sb)) != HD_OK) return s;
+  if ((e = cudaEventRecord(c.batch_join, c.batch_side)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(c.stream, c.batch_join, 0)) != cudaSuccess)
+    return cuda_fail(c, e, "join");
+  return HD_OK;
+}
+
+hd_status spatial_upload_sort(Ctx& c, const float* hA, uint64_t nA, const float* hB, uint64_t nB,
+                              int dims, const float** dA, const float** dB) {
+  hd_status s;
+  void *pa, *pb;
+  if ((s = ensure(c, kBufA, (size_t) nA * dims * sizeof(float), &pa)) != HD_OK) return s;
+  if ((s = ensure(c, kBufB, (size_t) nB * dims * sizeof(float), &pb)) != HD_OK) return s;
+  SortScratch x;
+  if ((s = sort_scratch(c, nA, nB, false, &x)) != HD_OK) return s;
+  if ((s = ensure_side(c)) != HD_OK) return s;
+  cudaError_t e;
+  // A's copy first, alone on the link; B's copy starts when it is done and
+  // runs beside A's sort.
+  if ((e = cudaMemcpyAsync(pa, hA, (size_t) nA * dims * sizeof(float), cudaMemcpyHostToDevice,
+                           c.stream)) != cudaSuccess)
+    return cuda_fail(c, e, "copy inputs to device");
+  if ((e = cudaEventRecord(c.batch_fork, c.stream)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(c.batch_side, c.batch_fork, 0)) != cudaSuccess)
+    return cuda_fail(c, e, "fork");
+  if ((s = sort_set(c, 0, (const float*) pa, nA, dims, x, c.stream, &c.sorted[0])) != HD_OK)
+    return s;
+  if ((e = cudaMemcpyAsync(pb, hB, (size_t) nB * dims * sizeof(float), cudaMemcpyHostToDevice,
+                           c.batch_side)) != cudaSuccess)
+    return cuda_fail(c, e, "copy inputs to device");
+  if ((s = sort_set(c, 1, (const float*) pb, nB, dims, x, c.batch_side, &c.sorted[1])) != HD_OK)
+    return s;
+  if ((e = cudaEventRecord(c.batch_join, c.batch_side)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(c.stream, c.batch_join, 0)) != cudaSuccess)
+    return cuda_fail(c, e, "join");
+  c.sorted_valid = true;
+  *dA = (const float*) pa;
+  *dB = (const float*) pb;
+  return HD_OK;
+}
+
+size_t scalars_bytes() { return 2 * sizeof(DevScalars) + 2 * sizeof(Frame); }
 
 hd_status spatial_prepare(Ctx& c, const DirInput& in, const SortedSet** q,
                           const SortedSet** t) {

@@ -142,18 +142,21 @@ def tilted_plane_with_far_points(n=1_000_000, n_far=300, seed=31):
 
 
 @pytest.mark.parametrize("undirected", [False, True])
-def test_lbvh_over_budget_queries(engine, undirected):
+def test_lbvh_over_budget_queries(undirected):
     """Points far above a tilted plane: proving their nearest neighbour means
     showing that a large ball touching many plane-patch boxes is empty, which
-    runs over the per-packet traversal budget; those queries are finished by
-    the deferred pass and the result stays exact."""
+    runs over a per-packet traversal budget of 32 visits (the tree alone is
+    16 levels deep); those queries are finished by the deferred pass and the
+    result stays exact."""
+    import hausdorffdistance_gb300 as hd
     a, b = tilted_plane_with_far_points()
     want = hd_oracle.hd_f32(b, a, undirected=undirected)
-    for count in (False, True):
-        r = engine.solve(b, a, undirected=undirected, variant="lbvh", count_pairs=count)
-        assert r.hd_f32 == want["hd_f32"]
-        check_pair(b, a, r, want["d2"])
-        assert r.rechecked > 0, "no query went over the traversal budget"
+    with hd.Engine(lbvh_budget=32) as engine:
+        for count in (False, True):
+            r = engine.solve(b, a, undirected=undirected, variant="lbvh", count_pairs=count)
+            assert r.hd_f32 == want["hd_f32"]
+            check_pair(b, a, r, want["d2"])
+            assert r.rechecked > 0, "no query went over the traversal budget"
 
 
 @pytest.mark.parametrize("dims", [2, 3])
@@ -214,3 +217,30 @@ def test_repeated_solves_replay_a_graph(variant, undirected):
             launches = e.kernel_launches
             assert e.solve(ta, tb, undirected=undirected, variant=variant).hd_f32 == want, rep
             assert e.kernel_launches > launches
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_large_sets_sorted_per_set(dims):
+    """From 4,000,000 points (|A| + |B|) the two sets are Morton-sorted as
+    independent chains, each in its own frame, and host inputs overlap A's
+    sort with B's copy; B's points beyond A's box clamp to the border cells
+    of A's frame.  LBVH and grid, on host and on device inputs, directed and
+    undirected, give the exact EB result and a valid certifying pair."""
+    import torch
+    import hausdorffdistance_gb300 as hd
+    rng = np.random.default_rng(70 + dims)
+    n = 2_100_000
+    a = rng.random((n, dims)).astype(np.float32)
+    b = (a[rng.permutation(n)] + rng.normal(0, 1e-3, a.shape)).astype(np.float32)
+    b[:2000] = (rng.random((2000, dims)) * 1.4 - 0.2).astype(np.float32)
+    ta, tb = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    with hd.Engine() as e:
+        for undirected in (True, False):
+            ref = e.solve(a, b, undirected=undirected, variant="eb")
+            src, dst = (a, b) if ref.direction == 0 else (b, a)
+            d2 = hd_oracle.dist2_f32(src[int(ref.ia)], dst[int(ref.ib)])
+            for v in ("lbvh", "grid", None):
+                for pa, pb in ((a, b), (ta, tb)):
+                    r = e.solve(pa, pb, undirected=undirected, variant=v)
+                    assert r.hd_f32 == ref.hd_f32, (v, undirected)
+                    check_pair(a, b, r, d2)
