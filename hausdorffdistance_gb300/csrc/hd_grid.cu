@@ -238,11 +238,11 @@ __global__ void __launch_bounds__(128)
 // search of its code in B's frame) and grows outward in alternating forward and backward
 // chunks, so the spatially nearest B points, which decide the early break,
 // come first; a point that does not break still visits every B point.
+template <int D>
 __global__ void __launch_bounds__(256)
     k_grid_deferred(const float4* __restrict__ Q, const Frame* __restrict__ tframe,
                     const float4* __restrict__ B, const uint32_t* __restrict__ bcodes, uint64_t nB,
-                    int dims, const Deferred* __restrict__ list, const uint32_t* count,
-                    DevScalars* sc) {
+                    const Deferred* __restrict__ list, const uint32_t* count, DevScalars* sc) {
   __shared__ float red[8];
   __shared__ float s_thr;
   constexpr uint64_t kChunk = 256 * 64;
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(256)
   for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
     const Deferred dfr = list[e];
     const float4 q = Q[dfr.qpos];
-    const uint32_t code = frame_code(*tframe, q.x, q.y, q.z);
+    const uint32_t code = frame_code<D>(*tframe, q.x, q.y, q.z);
     // First B position whose code is >= the query's (every thread finds the
     // same one).
     uint64_t lo = 0, hi = nB;
@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(256)
       float m = INFINITY;
       for (uint64_t j = b0 + threadIdx.x; j < b1; j += 256) {
         const float4 b = B[j];
-        m = fminf(m, dims == 2 ? d2_2(q.x, q.y, b.x, b.y) : d2_3(q.x, q.y, q.z, b.x, b.y, b.z));
+        m = fminf(m, D == 2 ? d2_2(q.x, q.y, b.x, b.y) : d2_3(q.x, q.y, q.z, b.x, b.y, b.z));
       }
 #pragma unroll
       for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
@@ -368,9 +368,12 @@ hd_status run_grid(Ctx& c, const DirInput& in) {
     if (phase == 0) mark(c, 3);
   }
   mark(c, 4);
-  k_grid_deferred<<<c.num_sms * 2, 256, 0, c.stream>>>(q->pts, t->frame, t->pts, t->codes, t->n,
-                                                      in.dims, (const Deferred*) defl, defer_count,
-                                                      sc);
+  if (in.dims == 2)
+    k_grid_deferred<2><<<c.num_sms * 2, 256, 0, c.stream>>>(q->pts, t->frame, t->pts, t->codes, t->n,
+                                                           (const Deferred*) defl, defer_count, sc);
+  else
+    k_grid_deferred<3><<<c.num_sms * 2, 256, 0, c.stream>>>(q->pts, t->frame, t->pts, t->codes, t->n,
+                                                           (const Deferred*) defl, defer_count, sc);
   if ((s = after_launch(c, "grid_deferred")) != HD_OK) return s;
   return certify(c, in);
 }

@@ -113,14 +113,23 @@ __device__ __forceinline__ uint32_t frame_quant(float v, float lo, float scale, 
   return (uint32_t) q;
 }
 // Morton code of a point in frame f (points outside the frame clamp to its
-// border cells).
+// border cells), D = f.dims.  D is a template parameter on purpose: one
+// body that chose between the 2-D and 3-D interleave at run time produced
+// wrong y bits inside one kernel on sm_103a (nvcc 13.0) while the same
+// arithmetic written without the run-time branch was right, so every caller
+// is instantiated per dimensionality.
+template <int D>
 __device__ __forceinline__ uint32_t frame_code(const Frame& f, float x, float y, float z) {
   const uint32_t maxq = (1u << f.bits) - 1u;
   const uint32_t qx = frame_quant(x, f.lo[0], f.scale, maxq);
   const uint32_t qy = frame_quant(y, f.lo[1], f.scale, maxq);
-  if (f.dims == 2) return morton_spread2(qx) | (morton_spread2(qy) << 1);
-  const uint32_t qz = frame_quant(z, f.lo[2], f.scale, maxq);
-  return morton_spread3(qx) | (morton_spread3(qy) << 1) | (morton_spread3(qz) << 2);
+  if constexpr (D == 2) {
+    (void) z;
+    return morton_spread2(qx) | (morton_spread2(qy) << 1);
+  } else {
+    const uint32_t qz = frame_quant(z, f.lo[2], f.scale, maxq);
+    return morton_spread3(qx) | (morton_spread3(qy) << 1) | (morton_spread3(qz) << 2);
+  }
 }
 #endif
 

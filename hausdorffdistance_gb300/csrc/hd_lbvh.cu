@@ -412,7 +412,11 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
 
 // Positions of every packet's first and last query in B's sorted codes
 // (lower bounds), one thread per packet end.
-__device__ __forceinline__ void packet_pos_body(const float4* __restrict__ Q, uint64_t nQ,
+// The query's code in the target set's frame: its own sorted code when both
+// sets share one frame (qcodes != null), else computed from the point.
+template <int D>
+__device__ __forceinline__ void packet_pos_body(const float4* __restrict__ Q,
+                                                const uint32_t* __restrict__ qcodes, uint64_t nQ,
                                                 const Frame* __restrict__ tframe,
                                                 const uint32_t* __restrict__ bcodes, uint64_t nB,
                                                 uint32_t* __restrict__ pos) {
@@ -420,9 +424,13 @@ __device__ __forceinline__ void packet_pos_body(const float4* __restrict__ Q, ui
   const uint64_t p = t >> 1;
   if (p * 32 >= nQ) return;
   const uint64_t q = (t & 1) ? min(p * 32 + 31, nQ - 1) : p * 32;
-  // The query's code in the target set's frame.
-  const float4 qp = Q[q];
-  const uint32_t target = frame_code(*tframe, qp.x, qp.y, qp.z);
+  uint32_t target;
+  if (qcodes) {
+    target = qcodes[q] & kCodeMask;
+  } else {
+    const float4 qp = Q[q];
+    target = frame_code<D>(*tframe, qp.x, qp.y, qp.z);
+  }
   uint64_t lo = 0, hi = nB;
   while (lo < hi) {
     const uint64_t mid = (lo + hi) >> 1;
@@ -477,7 +485,8 @@ struct QuerySet {
   uint64_t nB;
   uint32_t L;
   DevScalars* sc;
-  const Frame* tframe;  // frame of the target set's codes
+  const Frame* tframe;      // frame of the target set's codes
+  const uint32_t* qcodes;   // the query set's sorted codes when in that frame, else null
   const uint32_t* bcodes;
 };
 struct QuerySets {
@@ -608,9 +617,10 @@ __global__ void __launch_bounds__(kDeferWarps * 32) k_lbvh_defer(QuerySets qs) {
   }
 }
 
+template <int D>
 __global__ void k_packet_pos(QuerySets qs) {
   const QuerySet& S = qs.d[blockIdx.y];
-  packet_pos_body(S.Q, S.nQ, S.tframe, S.bcodes, S.nB, const_cast<uint32_t*>(S.ppos));
+  packet_pos_body<D>(S.Q, S.qcodes, S.nQ, S.tframe, S.bcodes, S.nB, const_cast<uint32_t*>(S.ppos));
 }
 
 }  // namespace
@@ -704,6 +714,7 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
     d.B = t[k]->pts;
     d.nB = t[k]->n;
     d.tframe = t[k]->frame;
+    d.qcodes = q[k]->frame == t[k]->frame ? q[k]->codes : nullptr;
     d.bcodes = t[k]->codes;
     off += 2 * packets[k];
     max_pos_threads = std::max<uint64_t>(max_pos_threads, 2 * packets[k]);
@@ -713,7 +724,11 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
   // stream while the (latency-bound) tree build runs on the main one.
   cudaEventRecord(c.batch_fork, c.stream);
   cudaStreamWaitEvent(c.batch_side, c.batch_fork, 0);
-  k_packet_pos<<<dim3((unsigned) ((max_pos_threads + 255) / 256), count), 256, 0, c.batch_side>>>(qs);
+  const dim3 pgrid((unsigned) ((max_pos_threads + 255) / 256), count);
+  if (dims == 2)
+    k_packet_pos<2><<<pgrid, 256, 0, c.batch_side>>>(qs);
+  else
+    k_packet_pos<3><<<pgrid, 256, 0, c.batch_side>>>(qs);
   if ((s = after_launch(c, "packet_pos")) != HD_OK) return s;
   cudaEventRecord(c.batch_join, c.batch_side);
   BuildSets bs;

@@ -123,15 +123,15 @@ __global__ void k_frame(const uint32_t* __restrict__ ordA, const uint32_t* __res
 }
 
 // Morton codes of one set in its frame: key = code, value = row.
-__global__ void k_morton1(const float* __restrict__ P, uint64_t n, int dims,
-                          const Frame* __restrict__ fr, uint32_t* __restrict__ keys,
-                          uint32_t* __restrict__ vals) {
+template <int D>
+__global__ void k_morton1(const float* __restrict__ P, uint64_t n, const Frame* __restrict__ fr,
+                          uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
   const Frame f = *fr;
   for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
        i += (uint64_t) gridDim.x * blockDim.x) {
-    const float x = P[i * dims], y = P[i * dims + 1];
-    const float z = dims == 3 ? P[i * dims + 2] : 0.0f;
-    keys[i] = frame_code(f, x, y, z);
+    const float x = P[i * D], y = P[i * D + 1];
+    const float z = D == 3 ? P[i * D + 2] : 0.0f;
+    keys[i] = frame_code<D>(f, x, y, z);
     vals[i] = (uint32_t) i;
   }
 }
@@ -338,7 +338,10 @@ hd_status sort_set(Ctx& c, int k, const float* P, uint64_t n, int dims, const So
   }
   k_frame<<<1, 32, 0, st>>>(ord, ord, dims, 1, 0, fr);
   if ((s = after_launch(c, "frame")) != HD_OK) return s;
-  k_morton1<<<grid_for(c, n), 256, 0, st>>>(P, n, dims, fr, x.keys + base, x.vals + base);
+  if (dims == 2)
+    k_morton1<2><<<grid_for(c, n), 256, 0, st>>>(P, n, fr, x.keys + base, x.vals + base);
+  else
+    k_morton1<3><<<grid_for(c, n), 256, 0, st>>>(P, n, fr, x.keys + base, x.vals + base);
   if ((s = after_launch(c, "morton")) != HD_OK) return s;
   size_t tb = x.tmp_bytes;
   cudaError_t e = cub::DeviceRadixSort::SortPairs(
