@@ -1018,6 +1018,9 @@ struct ProblemSource {
   const hd_problem* probs = nullptr;
   const uint64_t* oa = nullptr;
   const uint64_t* ob = nullptr;
+  // Device copies of oa / ob when already uploaded (grouped batches).
+  const uint64_t* doa = nullptr;
+  const uint64_t* dob = nullptr;
   hd_problem get(uint64_t i) const {
     if (probs) return probs[i];
     return hd_problem{oa[i], oa[i + 1] - oa[i], ob[i], ob[i + 1] - ob[i]};
@@ -1074,7 +1077,19 @@ struct BatchGraph {
   int grids[5];
 };
 
-hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
+// Resets the graph's per-call words with a kernel (no memset node that could
+// queue behind copies): keys and window bounds to 0, seed minima to all ones,
+// the two counters to 0.
+__global__ void k_batch_reset(uint4* __restrict__ zero, size_t zero16, uint4* __restrict__ ones,
+                              size_t ones16, unsigned long long* __restrict__ ctr) {
+  const size_t stride = (size_t) gridDim.x * blockDim.x;
+  const size_t t = blockIdx.x * (size_t) blockDim.x + threadIdx.x;
+  for (size_t i = t; i < zero16; i += stride) zero[i] = make_uint4(0u, 0u, 0u, 0u);
+  for (size_t i = t; i < ones16; i += stride) ones[i] = make_uint4(~0u, ~0u, ~0u, ~0u);
+  if (t < 2) ctr[t] = 0ull;
+}
+
+hd_status capture_batch_graph(Ctx& c, const BatchGraph& g, cudaGraphExec_t* out) {
   auto at = [&](size_t o) { return (void*) (g.base + o); };
   const BatchArgs& a = g.args;
   const uint32_t n = (uint32_t) g.n;
@@ -1082,9 +1097,14 @@ hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cuda_fail(c, e, "begin capture");
-  cudaMemsetAsync(g.base, 0, g.zero_bytes, c.stream);
-  cudaMemsetAsync(at(g.o_smin), 0xFF, g.smin_bytes, c.stream);
-  cudaMemsetAsync(g.ctr, 0, 2 * 8, c.stream);
+  {
+    // Both regions are whole multiples of 256 bytes (Layout pieces).
+    const size_t z16 = g.zero_bytes / 16, o16 = g.smin_bytes / 16;
+    const size_t work = std::max<size_t>(std::max(z16, o16), 2);
+    const unsigned rb = (unsigned) std::min<size_t>((work + 255) / 256, (size_t) c.num_sms * 8);
+    k_batch_reset<<<rb, 256, 0, c.stream>>>((uint4*) g.base, z16, (uint4*) at(g.o_smin), o16,
+                                            g.ctr);
+  }
   k_plan_keys<<<pblocks, 256, 0, c.stream>>>(a.probs, n, g.ndir, a.small_rows, a.pipe_rows,
                                             g.maxpairs,
                                             (unsigned long long*) at(g.o_pkeys),
@@ -1130,23 +1150,52 @@ hd_status capture_batch_graph(Ctx& c, const BatchGraph& g) {
   e = cudaGraphInstantiate(&exec, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda_fail(c, e, "instantiate graph");
-  if (c.batch_graph) cudaGraphExecDestroy(c.batch_graph);
-  c.batch_graph = exec;
+  *out = exec;
+  return HD_OK;
+}
+
+// The cached graph for a launch shape: a hit, or a capture into the least
+// recently used slot.
+hd_status batch_graph_for(Ctx& c, const BatchGraph& g, const uint64_t* key,
+                          cudaGraphExec_t* out) {
+  int slot = -1, lru = 0;
+  for (int i = 0; i < Ctx::kBatchGraphs; ++i) {
+    if (c.batch_graphs[i] && std::memcmp(key, c.batch_keys[i], sizeof(c.batch_keys[i])) == 0) {
+      slot = i;
+      break;
+    }
+    if (c.batch_stamp[i] < c.batch_stamp[lru]) lru = i;
+  }
+  if (slot < 0) {
+    slot = lru;
+    cudaGraphExec_t exec = nullptr;
+    hd_status s = capture_batch_graph(c, g, &exec);
+    if (s != HD_OK) return s;
+    if (c.batch_graphs[slot]) cudaGraphExecDestroy(c.batch_graphs[slot]);
+    c.batch_graphs[slot] = exec;
+    std::memcpy(c.batch_keys[slot], key, sizeof(c.batch_keys[slot]));
+  }
+  c.batch_stamp[slot] = ++c.batch_clock;
+  *out = c.batch_graphs[slot];
   return HD_OK;
 }
 
 }  // namespace
 
+// stage_bad != null: the results and the mismatch word are only queued (to
+// out and *stage_bad, both pinned host memory) and the call returns without
+// waiting; the caller synchronises and checks *stage_bad.
 hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, uint64_t total_b,
                       int dims, const ProblemSource& src, uint64_t n, uint32_t flags,
-                      hd_batch_result* out) {
+                      hd_batch_result* out, uint32_t* stage_bad = nullptr) {
   if (!A || !B || !(src.probs || (src.oa && src.ob)) || !out || n == 0)
     return fail(c, HD_ERR_INVALID_ARG, "bad arguments");
   if (dims != 2 && dims != 3) return fail(c, HD_ERR_UNSUPPORTED, "batches need n_dims 2 or 3");
   if (n >= 0xFFFFFFFFull) return fail(c, HD_ERR_INVALID_ARG, "too many problems");
   if (flags & ~(HD_UNDIRECTED | HD_DEVICE_PTRS)) return fail(c, HD_ERR_INVALID_ARG, "bad flags");
   hd_status s;
-  if ((s = check_problems(c, src, n, total_a, total_b)) != HD_OK) return s;
+  // A group of a grouped batch was validated with the whole batch.
+  if (!src.doa && (s = check_problems(c, src, n, total_a, total_b)) != HD_OK) return s;
   const int ndir = (flags & HD_UNDIRECTED) ? 2 : 1;
   const uint32_t small_rows = std::min<uint32_t>(c.opt.batch_small_rows, kSmallMax);
   const uint32_t pipe_rows = std::max<uint32_t>(small_rows, kPipeRows);
@@ -1192,7 +1241,7 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
   const size_t o_wb_a = L.take(total_a * 4);
   const size_t o_wb_b = L.take(ndir == 2 ? total_b * 4 : 0);
   const size_t o_probs = L.take(n * sizeof(hd_problem));
-  const size_t o_offs = L.take(src.probs ? 0 : 2 * (n + 1) * 8);
+  const size_t o_offs = L.take(src.probs || src.doa ? 0 : 2 * (n + 1) * 8);
   g.o_pkeys = L.take(n * 8);
   g.o_pkeys2 = L.take(n * 8);
   g.o_pvals = L.take(n * 4);
@@ -1232,13 +1281,19 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
                              cudaMemcpyHostToDevice, c.stream)) != cudaSuccess)
       return cuda_fail(c, e, "copy problems");
   } else {
-    uint64_t* d_oa = (uint64_t*) at(o_offs);
-    uint64_t* d_ob = d_oa + (n + 1);
-    if ((e = cudaMemcpyAsync(d_oa, src.oa, (n + 1) * 8, cudaMemcpyHostToDevice, c.stream)) !=
-            cudaSuccess ||
-        (e = cudaMemcpyAsync(d_ob, src.ob, (n + 1) * 8, cudaMemcpyHostToDevice, c.stream)) !=
-            cudaSuccess)
-      return cuda_fail(c, e, "copy offsets");
+    const uint64_t* d_oa = src.doa;
+    const uint64_t* d_ob = src.dob;
+    if (!d_oa) {
+      uint64_t* oa_up = (uint64_t*) at(o_offs);
+      uint64_t* ob_up = oa_up + (n + 1);
+      if ((e = cudaMemcpyAsync(oa_up, src.oa, (n + 1) * 8, cudaMemcpyHostToDevice, c.stream)) !=
+              cudaSuccess ||
+          (e = cudaMemcpyAsync(ob_up, src.ob, (n + 1) * 8, cudaMemcpyHostToDevice, c.stream)) !=
+              cudaSuccess)
+        return cuda_fail(c, e, "copy offsets");
+      d_oa = oa_up;
+      d_ob = ob_up;
+    }
     k_probs_from_offsets<<<(unsigned) ((n + 255) / 256), 256, 0, c.stream>>>(
         d_oa, d_ob, n, (hd_problem*) at(o_probs));
     if ((s = after_launch(c, "problems from offsets")) != HD_OK) return s;
@@ -1299,16 +1354,21 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
                             (uint64_t) dB,   total_a,  total_b,         (uint64_t) g.base,
                             (uint64_t) L.off, total,   maxpairs,        long_cap,
                             (uint64_t) c.stream, small_rows, chunk, c.opt.batch_window, n_big};
-  static_assert(sizeof(key) == sizeof(c.batch_key), "batch key size");
+  static_assert(sizeof(key) == sizeof(c.batch_keys[0]), "batch key size");
   if ((s = ensure_side(c)) != HD_OK) return s;
-  if (!c.batch_graph || std::memcmp(key, c.batch_key, sizeof(key)) != 0) {
-    if ((s = capture_batch_graph(c, g)) != HD_OK) return s;
-    std::memcpy(c.batch_key, key, sizeof(key));
-  }
-  e = cudaGraphLaunch(c.batch_graph, c.stream);
-  c.launches += 10;  // own kernels: plan keys, plan counts, one-warp path, window, seed, fold,
-                     // sweep, long, certify, finalize
+  cudaGraphExec_t exec = nullptr;
+  if ((s = batch_graph_for(c, g, key, &exec)) != HD_OK) return s;
+  e = cudaGraphLaunch(exec, c.stream);
+  c.launches += 11;  // own kernels: reset, plan keys, plan counts, one-warp path, window, seed,
+                     // fold, sweep, long, certify, finalize
   if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
+  if (stage_bad) {
+    if ((e = cudaMemcpyAsync(out, g.out, n * sizeof(hd_batch_result), cudaMemcpyDeviceToHost,
+                             c.stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(stage_bad, g.bad, 4, cudaMemcpyDeviceToHost, c.stream)) != cudaSuccess)
+      return cuda_fail(c, e, "batch solve");
+    return HD_OK;
+  }
   uint32_t bad = 0;
   if ((e = cudaMemcpyAsync(out, g.out, n * sizeof(hd_batch_result), cudaMemcpyDeviceToHost,
                            c.stream)) != cudaSuccess ||
@@ -1316,6 +1376,125 @@ hd_status batch_solve(Ctx& c, const float* A, uint64_t total_a, const float* B, 
       (e = cudaStreamSynchronize(c.stream)) != cudaSuccess)
     return cuda_fail(c, e, "batch solve");
   if (bad) return fail(c, HD_ERR_CUDA, "batch certification mismatch");
+  return HD_OK;
+}
+
+// Host points given by offsets: the problems run as a few groups of
+// consecutive problems (about kGroupBytes of points each).  Every group's
+// point ranges are copied on the copy stream up front, and group j is solved
+// as soon as its own copies have landed, so the host link keeps streaming
+// later groups while the GPU solves earlier ones.  Offsets are validated on
+// the whole batch first (non-empty problems inside the sets, which makes
+// them increasing), so every copied range lies inside A and B.
+constexpr uint64_t kGroupBytes = 96ull << 20;
+
+hd_status batch_solve_grouped(Ctx& c, const float* A, uint64_t total_a, const float* B,
+                              uint64_t total_b, int dims, const uint64_t* oa, const uint64_t* ob,
+                              uint64_t n, uint32_t flags, hd_batch_result* out) {
+  ProblemSource all;
+  all.oa = oa;
+  all.ob = ob;
+  const uint64_t bytes = (total_a + total_b) * (uint64_t) (dims > 0 ? dims : 0) * 4;
+  const int K = (int) std::min<uint64_t>(Ctx::kBatchGroups, bytes / kGroupBytes);
+  if ((flags & HD_DEVICE_PTRS) || K < 2 || n < 64 * (uint64_t) K || !A || !B || !out ||
+      (dims != 2 && dims != 3))
+    return batch_solve(c, A, total_a, B, total_b, dims, all, n, flags, out);
+  if (flags & ~(HD_UNDIRECTED | HD_DEVICE_PTRS)) return fail(c, HD_ERR_INVALID_ARG, "bad flags");
+  hd_status s;
+  if ((s = check_problems(c, all, n, total_a, total_b)) != HD_OK) return s;
+  // Group boundaries: equal shares of the points of both sets.
+  uint64_t cut[Ctx::kBatchGroups + 1];
+  int ng = 0;
+  cut[0] = 0;
+  const uint64_t span = (oa[n] - oa[0]) + (ob[n] - ob[0]);
+  for (uint64_t i = 1; i < n && ng + 1 < K; ++i) {
+    const uint64_t done = (oa[i] - oa[0]) + (ob[i] - ob[0]);
+    if (done * (uint64_t) K >= span * (uint64_t) (ng + 1)) cut[++ng] = i;
+  }
+  cut[++ng] = n;
+  void *pa, *pb, *po;
+  if ((s = ensure(c, kBufA, total_a * dims * 4, &pa)) != HD_OK) return s;
+  if ((s = ensure(c, kBufB, total_b * dims * 4, &pb)) != HD_OK) return s;
+  if ((s = ensure(c, kBufGroupOffs, 2 * (n + 1) * 8, &po)) != HD_OK) return s;
+  if ((s = ensure_side(c)) != HD_OK) return s;
+  cudaError_t e;
+  if (!c.copy_stream) {
+    if ((e = cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking)) != cudaSuccess)
+      return cuda_fail(c, e, "copy stream");
+    for (auto& ev : c.copy_ev)
+      if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
+        return cuda_fail(c, e, "copy events");
+  }
+  // The copies start after everything already queued on the call's stream.
+  if ((e = cudaEventRecord(c.batch_fork, c.stream)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(c.copy_stream, c.batch_fork, 0)) != cudaSuccess)
+    return cuda_fail(c, e, "fork");
+  // The offsets go first, so no group's solve waits behind the point copies
+  // for them (copies to the device share one queue).
+  uint64_t* d_oa = (uint64_t*) po;
+  uint64_t* d_ob = d_oa + (n + 1);
+  if ((e = cudaMemcpyAsync(d_oa, oa, (n + 1) * 8, cudaMemcpyHostToDevice, c.copy_stream)) !=
+          cudaSuccess ||
+      (e = cudaMemcpyAsync(d_ob, ob, (n + 1) * 8, cudaMemcpyHostToDevice, c.copy_stream)) !=
+          cudaSuccess) {
+    cudaStreamSynchronize(c.copy_stream);
+    return cuda_fail(c, e, "copy offsets");
+  }
+  const size_t row = (size_t) dims * sizeof(float);
+  for (int j = 0; j < ng; ++j) {
+    const uint64_t a0 = oa[cut[j]], a1 = oa[cut[j + 1]], b0 = ob[cut[j]], b1 = ob[cut[j + 1]];
+    e = cudaMemcpyAsync((char*) pa + a0 * row, (const char*) A + a0 * row, (a1 - a0) * row,
+                        cudaMemcpyHostToDevice, c.copy_stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync((char*) pb + b0 * row, (const char*) B + b0 * row, (b1 - b0) * row,
+                          cudaMemcpyHostToDevice, c.copy_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c.copy_ev[j], c.copy_stream);
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(c.copy_stream);
+      return cuda_fail(c, e, "copy points");
+    }
+  }
+  // Results of all groups are staged in pinned memory and the host waits
+  // once, at the end (the groups share the batch buffer, in stream order).
+  const size_t stage = n * sizeof(hd_batch_result) + 16 * sizeof(uint32_t);
+  if (c.batch_pinned_bytes < stage) {
+    if (c.batch_pinned) cudaFreeHost(c.batch_pinned);
+    c.batch_pinned = nullptr;
+    c.batch_pinned_bytes = 0;
+    if ((e = cudaMallocHost(&c.batch_pinned, stage)) != cudaSuccess) {
+      c.batch_pinned = nullptr;
+      cudaStreamSynchronize(c.copy_stream);
+      return fail(c, HD_ERR_OOM, "pinned staging of batch results");
+    }
+    c.batch_pinned_bytes = stage;
+  }
+  hd_batch_result* staged = (hd_batch_result*) c.batch_pinned;
+  uint32_t* bad = (uint32_t*) (staged + n);
+  s = HD_OK;
+  for (int j = 0; j < ng && s == HD_OK; ++j) {
+    if ((e = cudaStreamWaitEvent(c.stream, c.copy_ev[j], 0)) != cudaSuccess) {
+      s = cuda_fail(c, e, "wait for copies");
+      break;
+    }
+    ProblemSource grp;
+    grp.oa = oa + cut[j];
+    grp.ob = ob + cut[j];
+    grp.doa = d_oa + cut[j];
+    grp.dob = d_ob + cut[j];
+    s = batch_solve(c, (const float*) pa, total_a, (const float*) pb, total_b, dims, grp,
+                    cut[j + 1] - cut[j], (flags & HD_UNDIRECTED) | HD_DEVICE_PTRS,
+                    staged + cut[j], bad + j);
+  }
+  // No copy may still read the caller's buffers when the call returns, and
+  // no staged result may still be in flight.
+  e = cudaStreamSynchronize(c.stream);
+  const cudaError_t e2 = cudaStreamSynchronize(c.copy_stream);
+  if (s != HD_OK) return s;
+  if (e != cudaSuccess) return cuda_fail(c, e, "batch solve");
+  if (e2 != cudaSuccess) return cuda_fail(c, e2, "copy points");
+  for (int j = 0; j < ng; ++j)
+    if (bad[j]) return fail(c, HD_ERR_CUDA, "batch certification mismatch");
+  std::memcpy(out, staged, n * sizeof(hd_batch_result));
   return HD_OK;
 }
 
@@ -1375,10 +1554,10 @@ hd_status hd_solve_batch_offsets(hd_ctx* c, const float* A, uint64_t total_a, co
   if (!c) return HD_ERR_INVALID_ARG;
   c->last_error.clear();
   cudaSetDevice(c->device);
-  ProblemSource src;
-  src.oa = offsets_a;
-  src.ob = offsets_b;
-  return batch_solve(*c, A, total_a, B, total_b, n_dims, src, n_problems, flags, out);
+  if (!offsets_a || !offsets_b || n_problems == 0)
+    return fail(*c, HD_ERR_INVALID_ARG, "bad arguments");
+  return batch_solve_grouped(*c, A, total_a, B, total_b, n_dims, offsets_a, offsets_b, n_problems,
+                             flags, out);
 }
 
 hd_status hd_solve_batch_plain(hd_ctx* c, const float* A, uint64_t total_a, const float* B,

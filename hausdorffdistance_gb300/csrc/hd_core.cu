@@ -411,12 +411,17 @@ hd_status hd_destroy(hd_ctx* c) {
     if (b.p) cudaFree(b.p);
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
-  if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
+  for (auto& gx : c->batch_graphs)
+    if (gx) cudaGraphExecDestroy(gx);
+  for (auto& ev : c->copy_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->solve_graph) cudaGraphExecDestroy(c->solve_graph);
   if (c->batch_fork) cudaEventDestroy(c->batch_fork);
   if (c->batch_join) cudaEventDestroy(c->batch_join);
   if (c->batch_side) cudaStreamDestroy(c->batch_side);
   if (c->host_pinned) cudaFreeHost(c->host_pinned);
+  if (c->batch_pinned) cudaFreeHost(c->batch_pinned);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return HD_OK;

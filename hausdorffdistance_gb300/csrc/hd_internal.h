@@ -75,6 +75,7 @@ enum BufSlot {
   kBufCand,
   kBufBatch,
   kBufBatch2,
+  kBufGroupOffs,  // offsets of a grouped host-input batch (device copy)
   kNumBufs
 };
 
@@ -154,6 +155,8 @@ struct Ctx {
   DevBuf bufs[kNumBufs];
   void* host_pinned = nullptr;   // pinned result staging
   size_t host_pinned_bytes = 0;
+  void* batch_pinned = nullptr;  // pinned staging of grouped batch results
+  size_t batch_pinned_bytes = 0;
   std::string last_error;
   uint64_t launches = 0;
   // Timing events (HD_TIMING): [12*dir + phase] per direction, 24/25 = the
@@ -161,9 +164,19 @@ struct Ctx {
   cudaEvent_t ev[26] = {};
   bool timing = false;
   int ev_base = 0;
-  // Batched solve: the last instantiated graph and the launch shape it was
-  // captured for (reused while the shape, buffers and stream are unchanged).
-  cudaGraphExec_t batch_graph = nullptr;
+  // Batched solve: instantiated graphs and the launch shapes they were
+  // captured for (reused while the shape, buffers and stream are unchanged);
+  // several, because a host-input batch runs as a few groups of problems.
+  static constexpr int kBatchGraphs = 16;
+  cudaGraphExec_t batch_graphs[kBatchGraphs] = {};
+  uint64_t batch_keys[kBatchGraphs][17] = {};
+  uint64_t batch_stamp[kBatchGraphs] = {};
+  uint64_t batch_clock = 0;
+  // Host-input batches: group copies run on their own stream, one event per
+  // group.
+  static constexpr int kBatchGroups = 16;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ev[kBatchGroups] = {};
   // Side stream and fork/join events (created on first use): the batch
   // graph's second branch and the LBVH packet positions beside the build.
   cudaStream_t batch_side = nullptr;
@@ -177,7 +190,6 @@ struct Ctx {
   uint64_t solve_graph_launches = 0;
   uint64_t buf_gen = 0;             // bumped by every (re)allocation
   cudaEvent_t batch_fork = nullptr, batch_join = nullptr;
-  uint64_t batch_key[17] = {};
   // Per-solve cache: the Morton-sorted sets (slot 0 = call's A, 1 = call's B)
   // are shared by both directions of an undirected solve.
   SortedSet sorted[2];

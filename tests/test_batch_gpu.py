@@ -167,3 +167,31 @@ def test_batch_problem_array_abi_matches_offsets(engine):
     assert st == _lib.HD_OK
     assert np.array_equal(out["hd_f32"], via_offsets["hd_f32"])
     assert np.array_equal(out["direction"], via_offsets["direction"])
+
+
+@pytest.mark.parametrize("undirected", [True, False])
+def test_host_batch_runs_in_groups(engine, undirected):
+    """Host points of at least 2 x 96 MB, given by offsets, run as groups of
+    consecutive problems whose copies overlap the solves of earlier groups
+    (here about 290 MB: three groups).  Every problem's result equals the
+    device-input solve of the whole batch at once; a sample is checked
+    against the oracle."""
+    import torch
+    rng = np.random.default_rng(91)
+    n = 3000
+    sizes = rng.integers(3000, 9000, n)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    total = int(off[-1])
+    a = rng.random((total, 2), dtype=np.float32)
+    b = (a + rng.normal(0, 1e-3, a.shape)).astype(np.float32)
+    far = rng.choice(total, 500, replace=False)
+    b[far] = rng.random((500, 2), dtype=np.float32) * 1.5
+    host = engine.solve_batch(a, b, off, off, undirected=undirected)
+    dev = engine.solve_batch(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(), off, off,
+                             undirected=undirected)
+    for f in ("hd_f32", "ia", "ib", "direction"):
+        assert np.array_equal(host[f], dev[f]), f
+    for i in (0, 1234, n - 1):
+        sa, sb = a[off[i]:off[i + 1]], b[off[i]:off[i + 1]]
+        want = hd_oracle.hd_f32(sa, sb, undirected=undirected)["hd_f32"]
+        assert host["hd_f32"][i] == want, i
