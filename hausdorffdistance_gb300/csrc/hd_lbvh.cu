@@ -122,6 +122,16 @@ __device__ __forceinline__ void node_box(uint32_t id, uint32_t nI, const float4*
   }
 }
 
+// Arrival count at a parent with release and acquire semantics (GPU scope):
+// it publishes this thread's box writes to whichever thread arrives second,
+// and the second arriver sees the first one's box (the RMW chain on the
+// flag carries the synchronisation), without full fences.
+__device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t* p) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  return old;
+}
+
 __device__ __forceinline__ void bottom_up_body(const uint2* __restrict__ child,
                                                const uint32_t* __restrict__ parent, uint32_t nL,
                                                uint32_t nI, float4* boxes,
@@ -143,9 +153,7 @@ __device__ __forceinline__ void bottom_up_body(const uint2* __restrict__ child,
   uint32_t node = nI + leaf;
   for (;;) {
     uint32_t p = parent[node];
-    __threadfence();
-    if (atomicAdd(&flags[p], 1u) == 0) return;
-    __threadfence();
+    if (arrive_acq_rel(&flags[p]) == 0) return;
     uint2 ch = child[p];
     uint32_t a = node_id(ch.x, nI), b = node_id(ch.y, nI);
     float4 alo, ahi, blo, bhi;
