@@ -193,13 +193,17 @@ __global__ void __launch_bounds__(128)
           const uint2 run = table[lin];
           if (COUNT) ++cells;
           if (run.x == 0xFFFFFFFFu) continue;
-          for (uint32_t j = run.x; j < run.y; ++j) {
-            const float4 b = B[j];
+          // The early break is tested after every point: a cell can hold a
+          // very long run (many copies of one point, dense cluster cores).
+          uint32_t j = run.x;
+          while (j < run.y) {
+            const float4 b = B[j++];
             const float d = D == 2 ? d2_2(p[0], p[1], b.x, b.y)
                                    : d2_3(p[0], p[1], p[2], b.x, b.y, b.z);
             cmin = fminf(cmin, d);
+            if (cmin <= thr) break;
           }
-          if (COUNT) pairs += run.y - run.x;
+          if (COUNT) pairs += j - run.x;
           if (cmin <= thr) {
             done = true;  // early break: cannot raise the maximum
             break;

@@ -244,3 +244,24 @@ def test_large_sets_sorted_per_set(dims):
                     r = e.solve(pa, pb, undirected=undirected, variant=v)
                     assert r.hd_f32 == ref.hd_f32, (v, undirected)
                     check_pair(a, b, r, d2)
+
+
+def test_large_set_of_one_repeated_point():
+    """A set of 2,050,000 copies of one point beside 2,050,000 random points:
+    on the per-set path the repeated set's frame has zero extent (every code
+    0), and queries from the other set all clamp to its single cell (for the
+    grid, one cell holding the whole set, scanned with the early break
+    tested after every point).  LBVH and grid give the EB result in both
+    directions."""
+    import hausdorffdistance_gb300 as hd
+    rng = np.random.default_rng(83)
+    n = 2_050_000
+    a = np.tile(np.array([[0.25, 0.5, 0.75]], np.float32), (n, 1))
+    b = rng.random((n, 3), dtype=np.float32)
+    with hd.Engine() as e:
+        ref = e.solve(a, b, undirected=True, variant="eb")
+        for v in ("lbvh", "grid", None):
+            r = e.solve(a, b, undirected=True, variant=v)
+            assert r.hd_f32 == ref.hd_f32, v
+            rs, rd = (a, b) if ref.direction == 0 else (b, a)
+            check_pair(a, b, r, hd_oracle.dist2_f32(rs[int(ref.ia)], rd[int(ref.ib)]))
