@@ -1,27 +1,45 @@
 """Benchmark: Hausdorff solves/s (and Gpairs/s) on one GB300 per rank.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload clusters3d|uniform2d|planes3d] [--n POINTS]
-                    [--variant auto|eb|lbvh|grid] [--directed]
+                    [--workload all|clusters3d|uniform2d|planes3d|unit64|polylines]
+                    [--n POINTS] [--variant auto|eb|lbvh|grid|bf16] [--directed]
 
-A step is one undirected Hausdorff solve H(A,B) = max(h(A,B), h(B,A)) of the
-workload through libhdgpu.so's C ABI.  The default workload is the 3-D
-Gaussian mixture: |A| = |B| = 10,000,000 points, 64 clusters, sigma 0.01, B
-shifted by (0.05, 0, 0) (seeded synthetic data standing in for the
-reference's real datasets).  Inputs are larger than L2 (2 x 120 MB), so no
-flush is needed between steps.
+A step is one undirected Hausdorff solve H(A,B) = max(h(A,B), h(B,A)) of a
+workload through libhdgpu.so's C ABI (for the polyline workload: one batched
+solve of all its problems).  Workloads (seeded synthetic data with the shapes,
+sizes and distributions of the benchmark configurations; the reference's real
+datasets are not available):
 
-value   solves/s with A and B already resident in HBM (device pointers),
-        CUDA events on the library's stream, max over ranks, x N ranks.
-e2e     the same solve through the C ABI from pinned host buffers: the H2D
-        copies of A and B and the D2H read of the result are inside the
-        timed region.
+  clusters3d  3-D Gaussian mixture, |A| = |B| = 10,000,000, 64 clusters,
+              sigma 0.01, B shifted (0.05, 0, 0)          (the headline)
+  uniform2d   2-D, |A| = |B| = 200,000, B a jittered permutation of A plus
+              5% outliers
+  unit64      64-D unit rows, |A| = |B| = 1,000,000, 1% of B replaced
+  polylines   100,000 2-D polyline-pair problems, lognormal sizes
+  planes3d    3-D LiDAR-like planes, |A| = |B| = 50,000,000, B rotated
+              1 degree plus 0.1% outliers
+
+The default (--workload all) measures the headline at the top level of the
+JSON line and the other four under "workloads", each with the same keys.
+Inputs are larger than L2 (or the step's working set is), so no flush runs
+between steps; "config.l2" says so per workload.
+
+value     solves/s with A and B resident in HBM (device pointers), CUDA
+          events on the library's stream around K steps, the same call a user
+          makes (no timing instrumentation), max over ranks, x N ranks.
+e2e       the same solve through the C ABI from pinned host buffers: the H2D
+          copies of A and B and the D2H read of the result are inside the
+          timed region.
+phase_ms  per-phase device times from a separate instrumented run (HD_TIMING).
+rel_err_vs_oracle  |hd - H64| / H64 where H64 is the oracle's independent FP64
+          max-min (k-d tree, computed outside the timed region).
 Multi-GPU: each rank solves its own replica (the solve does not shard); the
 whole-job value is the number of solves all ranks completed / max time.
 
---impl reference times the reference's CPU early-break (the oracle's
-restatement of src/hd_impl/hausdorff_distance_early_break.h:44-115) on the
-host cores, on a bounded sample of the same workload.
+--impl reference runs the reference's CPU early-break (the oracle's
+restatement of src/hd_impl/hausdorff_distance_early_break.h:44-115) on all host
+cores: each step is one whole undirected solve of the headline workload when
+it fits the step budget, else a bounded estimate (see cpu_eb_baseline).
 """
 from __future__ import annotations
 
@@ -39,8 +57,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
-FALLBACK_HBM_GBS = 6800.0
+FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
 METRIC = "Hausdorff solves/s & Gpairs/s at rel err<=1e-6, chosen vs plain FP32, 1 GB300"
+ALL = ["clusters3d", "uniform2d", "unit64", "polylines", "planes3d"]
+WORKLOAD_SIZES = {"clusters3d": 10_000_000, "uniform2d": 200_000, "planes3d": 50_000_000,
+                  "unit64": 1_000_000, "polylines": 100_000}
+SEEDS = {"clusters3d": 2, "uniform2d": 1, "planes3d": 5, "unit64": 3, "polylines": 4}
 
 
 def parse():
@@ -49,26 +71,23 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="clusters3d",
-                   choices=["clusters3d", "uniform2d", "planes3d", "unit64", "polylines"])
+    p.add_argument("--workload", default="all", choices=["all"] + ALL)
     p.add_argument("--n", type=int, default=0, help="points per set (default: workload size)")
     p.add_argument("--variant", default="auto")
     p.add_argument("--directed", action="store_true")
     p.add_argument("--no-compare", action="store_true", help="skip the plain-EB comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--no-oracle", action="store_true", help="skip the FP64 oracle check")
     p.add_argument("--profile", action="store_true",
-                   help="one solve and exit (the command profiled under ncu)")
+                   help="one solve of one workload and exit (the command profiled under ncu)")
     return p.parse_args()
-
-
-WORKLOAD_SIZES = {"clusters3d": 10_000_000, "uniform2d": 200_000, "planes3d": 50_000_000,
-                  "unit64": 1_000_000, "polylines": 100_000}
 
 
 def make_data(name, n):
     from hausdorffdistance_gb300 import synth
-    seed = {"clusters3d": 2, "uniform2d": 1, "planes3d": 5, "unit64": 3}[name]
-    return getattr(synth, name)(n, seed=seed)
+    if name == "polylines":
+        return synth.polylines(n_problems=n, seed=SEEDS[name])
+    return getattr(synth, name)(n, seed=SEEDS[name])
 
 
 def workload_desc(name, n):
@@ -77,12 +96,14 @@ def workload_desc(name, n):
         "uniform2d": f"2-D uniform, |A|=|B|={n}, B = jittered permutation of A + 5% outliers",
         "planes3d": f"3-D LiDAR-like planes, |A|=|B|={n}, B = A rotated 1 deg + 0.1% outliers",
         "unit64": f"64-D unit rows, |A|=|B|={n}, B = A with 1% of rows replaced",
-        "polylines": f"{n} 2-D polyline-pair problems, lognormal sizes (median 200, sigma 1.2)",
+        "polylines": (f"{n} 2-D polyline-pair problems, sizes round(LogNormal(ln 200, 1.2)) "
+                      "clipped to [8, 50000]"),
     }[name]
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+    """nvidia-smi clock / throttle-reason sampling during the timed region
+    (a read-only query)."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -102,6 +123,7 @@ class ClockSampler:
             self.t.start()
         except Exception:
             self.proc = None
+        return self
 
     def _read(self):
         for ln in self.proc.stdout:
@@ -139,191 +161,409 @@ def load_peaks():
     try:
         with open(PEAKS_PATH) as f:
             pk = json.load(f)
-        return float(pk["hbm_gbs"]), "measured"
+        return {k: float(pk[k]) for k in FALLBACK}, "measured"
     except Exception:
-        return FALLBACK_HBM_GBS, "fallback"
+        return dict(FALLBACK), "fallback"
 
 
-def traffic_from_profiles(kernel_tag, units):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
-    summary (profiles/<kernel>.txt, a line 'dram_bytes_per_unit: X'),
-    scaled to this launch's units; None if no summary exists."""
-    path = os.path.join(ROOT, "profiles", f"{kernel_tag}.txt")
+def profile_figures(tag):
+    """'key: value' lines of the committed ncu summary profiles/<tag>.txt
+    (dram_bytes_per_unit, issue_active, ...)."""
+    out = {}
     try:
-        for ln in open(path):
-            if ln.startswith("dram_bytes_per_unit:"):
-                return float(ln.split(":", 1)[1]) * units
+        for ln in open(os.path.join(ROOT, "profiles", f"{tag}.txt")):
+            if ":" in ln and not ln.startswith((" ", "\t")):
+                k, v = ln.split(":", 1)
+                try:
+                    out[k.strip()] = float(v.split()[0])
+                except (ValueError, IndexError):
+                    pass
     except OSError:
         pass
-    return None
+    return out
 
 
-def cpu_baseline(a, b, undirected, max_seconds=25.0):
-    """The reference's CPU early-break (oracle restatement) on all host cores
-    over bounded samples of A (first k points of the seeded shuffle), per
-    direction, extrapolated to the full set from the marginal cost between two
-    sample sizes.  Returns the baseline dict (solves/s)."""
+def traffic_from_profiles(tag, units):
+    """Per-launch DRAM bytes of a kernel from its committed ncu summary
+    (dram_bytes_per_unit) scaled to this launch's units; None without one."""
+    v = profile_figures(tag).get("dram_bytes_per_unit")
+    return None if v is None else v * units
+
+
+def host_cpu():
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    return int(cores or 1), model
+
+
+# ---------------------------------------------------------------------------
+# Oracle and CPU baseline (test infrastructure; never part of a timed GPU step)
+
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import hd_oracle
-    cores = os.cpu_count() or 1
-    dirs = [(a, b), (b, a)] if undirected else [(a, b)]
+    return hd_oracle
+
+
+def oracle_hd64(a, b, undirected):
+    """The oracle's independent FP64 max-min (k-d tree with early break, all
+    host threads): (H64, seconds)."""
+    o = _oracle()
+    t0 = time.perf_counter()
+    h2 = o.exact(a, b, 64)[0]
+    if undirected:
+        h2 = max(h2, o.exact(b, a, 64)[0])
+    return float(np.sqrt(h2)), time.perf_counter() - t0
+
+
+def oracle_batch_hd64(a, b, off, undirected):
+    o = _oracle()
+    t0 = time.perf_counter()
+    h2 = o.exact_batch(a, b, off, off, 64, undirected=undirected)[0]
+    return np.sqrt(h2), time.perf_counter() - t0
+
+
+def _eb_direction(o, x, y, d2_final, cores, budget_s):
+    """One direction of the reference CPU early-break (oracle restatement) on
+    all host cores.  The whole scan runs when a probe says it fits budget_s;
+    otherwise its time is estimated as (measured time of the first k points
+    of the seeded shuffle) + (n - k) x (mean per-point time of a window of
+    later points scanned from the final running maximum).  A point's scan can
+    only get shorter as the running maximum rises, so the window's per-point
+    time is at most the same points' time in the whole run: the estimate is
+    biased low (the CPU figure is, if anything, too fast)."""
+    n = len(x)
+    k = min(n, 4096)
+    r1 = o.eb_window(x, y, 0, k, 0.0, n_threads=cores)
+    if k >= n:
+        return {"ms": r1["compute_ms"], "shuffle_ms": r1["shuffle_ms"], "full": True,
+                "pairs": r1["compared_pairs"]}
+    c2 = np.float32(d2_final) * np.float32(1.0 + 1e-6)
+    m = min(n - k, 16384)
+    while True:
+        r2 = o.eb_window(x, y, k, k + m, c2, n_threads=cores)
+        if r2["compute_ms"] > 300.0 or k + m >= n or m >= 4_000_000:
+            break
+        m = min(n - k, m * 4)
+    per_point = r2["compute_ms"] / m
+    est = r1["compute_ms"] + per_point * (n - k)
+    if est <= budget_s * 1e3:
+        r = o.eb(x, y, seed=0, n_threads=cores)
+        return {"ms": r["compute_ms"], "shuffle_ms": r["shuffle_ms"], "full": True,
+                "pairs": r["compared_pairs"]}
+    return {"ms": est, "shuffle_ms": r1["shuffle_ms"], "full": False,
+            "first_k": k, "first_k_ms": r1["compute_ms"], "window": m,
+            "window_ms": r2["compute_ms"]}
+
+
+def cpu_eb_baseline(a, b, undirected, d2_final, budget_s=20.0):
+    """The reference's CPU early-break (restated in oracle/hd_oracle.cpp; for
+    n_dims other than 2 and 3, which the reference does not support, the same
+    algorithm applied to rows, not reference code) on all host cores, per
+    direction, whole runs where they fit budget_s, else the bounded estimate
+    of _eb_direction.  d2_final: the final squared maxima per direction
+    (from the GPU result).  Times are compute times, the reference's own
+    ReportedTime (early_break.h:106); the shuffle is listed beside them."""
+    o = _oracle()
+    cores, model = host_cpu()
+    dirs = [(a, b, d2_final[0]), (b, a, d2_final[1])] if undirected else [(a, b, d2_final[0])]
+    parts = [_eb_direction(o, x, y, d2, cores, budget_s) for x, y, d2 in dirs]
+    total = sum(p["ms"] for p in parts)
+    full = all(p["full"] for p in parts)
+    ref = "reference CPU early-break restated (oracle/hd_oracle.cpp)"
     if a.shape[1] not in (2, 3):
-        # The reference has no path for n_dims other than 2 and 3: time the
-        # oracle's exact FP32 max-min (not reference code) on the first k rows
-        # of A against all of B and extrapolate linearly (no early break).
-        total_ms = 0.0
-        detail = []
-        for x, y in dirs:
-            k = max(16, min(len(x), 64))
-            t0 = time.perf_counter()
-            hd_oracle.exact(x[:k], y, 32, n_threads=cores)
-            ms = (time.perf_counter() - t0) * 1e3
-            est = ms * len(x) / k
-            total_ms += est
-            detail.append({"sample_rows": k, "sample_ms": ms, "extrapolated_ms": est})
-        return {"value": 1000.0 / total_ms, "unit": "solves/s", "cores": cores, "kind": "port",
-                "sample": ("oracle exact FP32 max-min restatement (not reference code: the "
-                           "reference supports n_dims 2 and 3 only), all host threads, first k "
-                           "rows of A against all of B, extrapolated linearly: "
-                           + json.dumps(detail))}
-    total_ms = 0.0
-    detail = []
-    budget = max_seconds / len(dirs)
-    for x, y in dirs:
-        k1 = max(64, min(len(x), 2048))
-        r1 = hd_oracle.eb(x, y, seed=0, n_threads=cores, limit_a=k1)
-        # Grow the second sample while it stays well inside the budget.
-        k2 = min(len(x), k1 * 4)
-        if r1["compute_ms"] * 4 > budget * 1e3:
-            k2 = k1
-        r2 = hd_oracle.eb(x, y, seed=0, n_threads=cores, limit_a=k2) if k2 > k1 else r1
-        if k2 >= len(x):
-            est = r2["compute_ms"]
-        else:
-            marginal = max(0.0, (r2["compute_ms"] - r1["compute_ms"]) / max(1, k2 - k1))
-            est = r2["compute_ms"] + marginal * (len(x) - k2)
-        total_ms += est
-        detail.append({"sample_points": [k1, k2], "sample_ms": [r1["compute_ms"], r2["compute_ms"]],
-                       "extrapolated_ms": est})
-    return {"value": 1000.0 / total_ms, "unit": "solves/s", "cores": cores, "kind": "port",
-            "sample": ("reference CPU early-break restated (oracle/hd_oracle.cpp), all host "
-                       "threads, per direction the first k of the seeded shuffle of A against all "
-                       "of B for two k, extrapolated linearly from the marginal cost: "
-                       + json.dumps(detail))}
+        ref = ("the reference's early-break algorithm applied to 64-D rows (oracle/hd_oracle.cpp; "
+               "not reference code: the reference supports n_dims 2 and 3 only)")
+    how = ("whole solve measured" if full else
+           "estimated per direction: measured first k points of the seeded shuffle + remaining "
+           "points at the per-point time of a window scanned from the final running maximum "
+           "(a lower bound on the reference's time)")
+    return {"value": 1000.0 / total, "unit": "solves/s", "cores": cores, "cpu_model": model,
+            "kind": "port", "ms_per_solve": total, "measured_whole_solve": full,
+            "sample": f"{ref}, {cores} host threads, {how}: " + json.dumps(parts)}
 
 
-def run_reference(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
-    n = args.n or WORKLOAD_SIZES[args.workload]
-    undirected = not args.directed
-    if args.workload == "polylines":
-        from hausdorffdistance_gb300 import synth
-        a, b, off = synth.polylines(n_problems=n, seed=4)
-        measure = lambda: cpu_baseline_batch(a, b, off, undirected, max_seconds=8.0)  # noqa: E731
-    else:
-        a, b = make_data(args.workload, n)
-        measure = lambda: cpu_baseline(a, b, undirected, max_seconds=8.0)  # noqa: E731
-    vals = []
-    base = None
-    for i in range(args.warmup + args.steps):
-        base = measure()
-        if i >= args.warmup:
-            vals.append(base["value"])
-    v = float(np.median(vals))
-    base["value"] = v
-    line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "impl": "reference",
-            "config": {"workload": workload_desc(args.workload, n),
-                       "undirected": undirected, "l2": "inputs larger than L2"},
-            "cpu_baseline": base,
-            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
-
-
-def cpu_baseline_batch(a, b, off, undirected, max_seconds=20.0):
-    """Reference CPU early-break (oracle restatement), one thread per problem,
-    problems spread over all host cores, on the first k problems of the
-    (randomly ordered) batch; extrapolated to the whole batch by pair count."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+def cpu_batch_baseline(a, b, off, undirected, budget_s=20.0):
+    """Reference CPU early-break (oracle restatement), n_threads = 1 per
+    problem, problems spread over all host cores: the whole batch when the
+    first problems' rate says it fits budget_s, else those first problems
+    extrapolated by pair count."""
     import concurrent.futures as cf
-    import hd_oracle
-    cores = os.cpu_count() or 1
+    o = _oracle()
+    cores, model = host_cpu()
     sizes = np.diff(off)
     pairs = sizes.astype(np.float64) ** 2
-    k = 0
-    acc = 0.0
-    budget_pairs = 4e9 * max_seconds / 20.0  # ~ what the cores finish in the budget
-    while k < len(sizes) and acc < budget_pairs:
-        acc += pairs[k]
-        k += 1
 
     def one(p):
         x, y = a[off[p]:off[p + 1]], b[off[p]:off[p + 1]]
-        hd_oracle.eb(x, y, n_threads=1)
+        o.eb(x, y, n_threads=1)
         if undirected:
-            hd_oracle.eb(y, x, n_threads=1)
+            o.eb(y, x, n_threads=1)
 
-    t0 = time.perf_counter()
-    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
-        list(ex.map(one, range(k)))
-    t = time.perf_counter() - t0
+    def run(k):
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+            list(ex.map(one, range(k)))
+        return time.perf_counter() - t0
+
+    k = min(len(sizes), 4000)
+    t = run(k)
     est = t * pairs.sum() / pairs[:k].sum()
-    return {"value": len(sizes) / est, "unit": "solves/s", "cores": cores, "kind": "port",
+    full = False
+    if est <= budget_s:
+        t, k, full = run(len(sizes)), len(sizes), True
+        est = t
+    return {"value": len(sizes) / est, "unit": "solves/s", "cores": cores, "cpu_model": model,
+            "kind": "port", "ms_per_step": est * 1e3, "measured_whole_batch": full,
             "sample": (f"reference CPU early-break restated (oracle/hd_oracle.cpp), n_threads=1 "
-                       f"per problem, problems spread over {cores} host threads; first {k} of "
-                       f"{len(sizes)} problems ({t:.2f} s), extrapolated by pair count")}
+                       f"per problem, problems spread over {cores} host threads; "
+                       + ("the whole batch measured" if full else
+                          f"first {k} of {len(sizes)} problems ({t:.2f} s), extrapolated by "
+                          "pair count"))}
 
 
-def main_batch(args):
+# ---------------------------------------------------------------------------
+# GPU workloads
+
+def _events_ms(stream, fn, steps):
+    """Average device time per call of fn() over `steps` calls: CUDA events on
+    the library's stream, synchronised on both sides."""
     import torch
-
-    import hausdorffdistance_gb300 as hd
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    n = args.n or WORKLOAD_SIZES["polylines"]
-    from hausdorffdistance_gb300 import synth
-    a, b, off = synth.polylines(n_problems=n, seed=4)
-    undirected = not args.directed
-    stream = torch.cuda.current_stream()
-    eng = hd.Engine(device=local)
-    eng.set_stream(stream.cuda_stream)
-    ta = torch.from_numpy(a).cuda()
-    tb = torch.from_numpy(b).cuda()
-    if args.profile:
-        eng.solve_batch(ta, tb, off, off, undirected=undirected)
-        torch.cuda.synchronize()
-        print(json.dumps({"profile_solve": True}), flush=True)
-        return
-    for _ in range(args.warmup):
-        ref = eng.solve_batch(ta, tb, off, off, undirected=undirected)
-    clocks = ClockSampler(local)
-    clocks.start()
-    l0 = eng.kernel_launches
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
-        res = eng.solve_batch(ta, tb, off, off, undirected=undirected)
+    r = None
+    for _ in range(steps):
+        r = fn()
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+    return e0.elapsed_time(e1) / steps, r
+
+
+def _fp32_issue_peak(local, sm_mhz):
+    """Non-fused FP32 operations per second: SMs x 128 FP32 lanes x SM clock
+    (the sampled clock; nominal maximum 2070 MHz when unsampled)."""
+    import torch
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    return sms * 128 * (sm_mhz or 2070.0) * 1e6
+
+
+def _lbvh_phases(n_a, n_b, dims, undirected, rc, phase):
+    """Roofline entries of the LBVH path's three phases, algorithmic bytes as
+    the measurement plan defines them: sort (per set: read the points twice,
+    two 8-byte key/index passes read and written, write the sorted points),
+    tree build ((2 n/16) nodes x 32 B per set), query (queries x n_dims x 4 +
+    visited nodes x 32 + visited leaf points x n_dims x 4)."""
+    sets = [n_a, n_b]
+    sort_b = sum(n * (dims * 4 * 2 + 2 * 16 + dims * 4) for n in sets)
+    build_b = sum((2 * ((n + 15) // 16)) * 32 for n in sets)
+    queries = (n_a + n_b) if undirected else n_a
+    query_b = queries * dims * 4 + rc.visited_nodes * 32 + rc.visited_leaves * 16 * dims * 4
+    return [("morton_sort", sort_b, phase[0]), ("lbvh_build", build_b, phase[1]),
+            ("lbvh_query", query_b, phase[3])]
+
+
+def bench_single(eng, name, n, steps, warmup, args, ctx):
+    import torch
+    import hausdorffdistance_gb300 as hd
+    stream, local, world, barrier = ctx["stream"], ctx["local"], ctx["world"], ctx["barrier"]
+    t_gen = time.perf_counter()
+    a, b = make_data(name, n)
+    t_gen = time.perf_counter() - t_gen
+    undirected = not args.directed
+    dims = a.shape[1]
+    ta = torch.from_numpy(a).cuda()
+    tb = torch.from_numpy(b).cuda()
+    variant = args.variant
+
+    def solve():
+        return eng.solve(ta, tb, undirected=undirected, variant=variant)
+
+    # Instrumented runs (outside the timed region): visited pairs / nodes for
+    # the algorithmic byte counts, per-phase event times.
+    rc = eng.solve(ta, tb, undirected=undirected, variant=variant, count_pairs=True)
+    phase = np.zeros(8)
+    n_inst = 3
+    for _ in range(n_inst):
+        ri = eng.solve(ta, tb, undirected=undirected, variant=variant, timing=True)
+        phase += np.array(ri.phase_ms[:8])
+    phase /= n_inst
+    for _ in range(warmup):
+        solve()
+    clocks = ClockSampler(local).start()
+    launches0 = eng.kernel_launches
+    barrier()
+    ms, res = _events_ms(stream, solve, steps)
+    barrier()
+    launches = eng.kernel_launches - launches0
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1e3 / ms
+
+    # End to end from pinned host buffers (copies and result read inside).
+    pa = torch.from_numpy(a).pin_memory()
+    pb = torch.from_numpy(b).pin_memory()
+    na, nb = pa.numpy(), pb.numpy()
+    for _ in range(2):
+        eng.solve(na, nb, undirected=undirected, variant=variant)
+    e2e_steps = max(3, steps // 2)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        re2e = eng.solve(na, nb, undirected=undirected, variant=variant)
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    assert re2e.hd_f32 == res.hd_f32
+
+    # Plain FP32 early-break on the same inputs ("chosen vs plain FP32").
+    plain = None
+    if not args.no_compare and res.variant_used != hd._lib.VARIANT_EB:
+        eng.solve(ta, tb, undirected=undirected, variant="eb")
+        ksteps = 2 if dims <= 3 else 1
+        pms, rp = _events_ms(stream, lambda: eng.solve(ta, tb, undirected=undirected,
+                                                       variant="eb"), ksteps)
+        assert rp.hd_f32 == res.hd_f32, "plain EB and chosen variant disagree"
+        plain = {"variant": "eb", "ms_per_step": pms, "solves_per_s": 1e3 / pms,
+                 "speedup_chosen_vs_plain": pms / ms}
+
+    peaks, pkind = load_peaks()
+    used = (hd._lib.VARIANT_NAMES.get(res.variant_used),
+            hd._lib.VARIANT_NAMES.get(res.variant_used_ba) if undirected else None)
+    roof, phases = None, []
+    if res.variant_used == hd._lib.VARIANT_LBVH:
+        for tag, alg, t_ms in _lbvh_phases(n, n, dims, undirected, rc, phase):
+            if t_ms <= 0:
+                continue
+            ach = alg / (t_ms / 1e3) / 1e9
+            fig = profile_figures(tag)
+            units = 2.0 * n if undirected else float(n)
+            phases.append({"bound": "hbm", "kernel": tag, "achieved": ach,
+                           "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                           "frac": ach / peaks["hbm_gbs"],
+                           "traffic": (fig["dram_bytes_per_unit"] * units
+                                       if "dram_bytes_per_unit" in fig else None),
+                           "algorithmic_bytes": alg, "ms": t_ms,
+                           "issue_active_ncu": fig.get("issue_active"),
+                           "peak_source": pkind + " hbm_gbs"})
+        if phases:
+            roof = max(phases, key=lambda p: p["ms"])
+    elif res.variant_used in (hd._lib.VARIANT_EB, hd._lib.VARIANT_GRID):
+        # FP32-issue bound: 3 n_dims - 1 non-fused FLOP per visited pair.
+        t_ms = phase[3] + phase[4]
+        flops = rc.visited_pairs * (3 * dims - 1)
+        pk = _fp32_issue_peak(local, clk.get("sm_mhz"))
+        ach = flops / (t_ms / 1e3) / 1e12
+        roof = {"bound": "fp32_issue", "kernel": "eb_main+eb_heavy", "achieved": ach,
+                "peak": pk / 1e12, "unit": "TFLOP/s", "frac": ach / (pk / 1e12),
+                "traffic": None, "ms": t_ms, "visited_pairs": int(rc.visited_pairs),
+                "issue_active_ncu": profile_figures("eb_main").get("issue_active"),
+                "peak_source": "SMs x 128 FP32 lanes x sampled SM clock (non-fused ops)"}
+    elif res.variant_used == hd._lib.VARIANT_BF16:
+        # Split-BF16 contraction: 3 products x 2 K FLOP per pair and direction.
+        K = ((dims + 15) // 16) * 16
+        dirs = 2 if undirected else 1
+        flops = dirs * 3.0 * 2.0 * K * float(n) * float(n)
+        t_ms = phase[3]
+        ach = flops / (t_ms / 1e3) / 1e12
+        fig = profile_figures("bf16_rowmin")
+        roof = {"bound": "tensor", "kernel": "bf16_rowmin", "achieved": ach,
+                "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": ach / peaks["bf16_tflops"],
+                "frac_of_sustained": ach / peaks["bf16_tflops_sustained"],
+                "traffic": traffic_from_profiles("bf16_rowmin", float(n) * float(n)),
+                "algorithmic_flops_per_launch": flops / dirs, "ms": t_ms,
+                "tensor_pipe_active_ncu": fig.get("tensor_pipe_active"),
+                "peak_source": pkind + " bf16_tflops (burst); frac_of_sustained against "
+                               "bf16_tflops_sustained",
+                "rechecked_rows": int(res.rechecked), "err_bound": res.err_bound}
+
+    # Relative error against the oracle's independent FP64 max-min.
+    oracle = None
+    if not args.no_oracle and ctx["rank"] == 0:
+        h64, t_or = oracle_hd64(a, b, undirected)
+        oracle = {"hd64": h64, "rel_err_vs_oracle": abs(res.hd - h64) / h64,
+                  "hd_f32_rel_err_vs_oracle": abs(float(res.hd_f32) - h64) / h64,
+                  "oracle_s": t_or}
+
+    base = None
+    if ctx["rank"] == 0 and world == 1 and not args.no_cpu:
+        d2f = [np.float32(res.hd_ab) ** 2, np.float32(max(res.hd_ba, 0.0)) ** 2]
+        base = cpu_eb_baseline(a, b, undirected, d2f)
+
+    pairs_eff = (2 if undirected else 1) * float(n) * float(n)
+    return {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": steps, "warmup": warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": workload_desc(name, n), "n_a": n, "n_b": n, "n_dims": dims,
+                   "undirected": undirected, "l2": l2_note(a.nbytes + b.nbytes),
+                   "parallelism": f"replicas x{world}"},
+        "variant": variant, "variant_used": list(used),
+        "gpairs_per_s_effective": value * pairs_eff / 1e9,
+        "gpairs_per_s_visited": (rc.visited_pairs * value / 1e9) if rc.visited_pairs else None,
+        "hd_f32": float(res.hd_f32), "hd64_certified": res.hd,
+        "certifying_pair": [int(res.ia), int(res.ib), int(res.direction)],
+        "rel_err_vs_oracle": None if not oracle or "hd64" not in oracle
+        else oracle["rel_err_vs_oracle"],
+        "oracle": oracle,
+        "phase_ms": {nm: float(phase[i]) for i, nm in
+                     enumerate(["prep", "build", "sample", "main_pass", "tail", "certify"])},
+        "instrumented_ms": float(ri.ms),
+        "plain_fp32_eb": plain,
+        "e2e": {"value": world / t_e2e, "unit": "solves/s",
+                # D2H: the two per-direction result records.
+                "h2d_bytes_per_step": int(a.nbytes + b.nbytes), "d2h_bytes_per_step": 2 * 152},
+        "gpu_launches": int(launches),
+        "roofline": roof, "phases_roofline": phases or None,
+        "cpu_baseline": base, "clocks": clk, "data_gen_s": t_gen,
+    }
+
+
+def bench_batch(eng, n, steps, warmup, args, ctx):
+    import torch
+    stream, local, world, barrier = ctx["stream"], ctx["local"], ctx["world"], ctx["barrier"]
+    t_gen = time.perf_counter()
+    a, b, off = make_data("polylines", n)
+    t_gen = time.perf_counter() - t_gen
+    undirected = not args.directed
+    ta = torch.from_numpy(a).cuda()
+    tb = torch.from_numpy(b).cuda()
+
+    def solve():
+        return eng.solve_batch(ta, tb, off, off, undirected=undirected)
+
+    for _ in range(warmup):
+        ref = solve()
+    clocks = ClockSampler(local).start()
+    l0 = eng.kernel_launches
+    barrier()
+    ms, res = _events_ms(stream, solve, steps)
+    barrier()
     clk = clocks.stop()
     launches = eng.kernel_launches - l0
     assert np.array_equal(res["hd_f32"], ref["hd_f32"])
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
     value = world * n / (ms / 1e3)
     pa = torch.from_numpy(a).pin_memory().numpy()
     pb = torch.from_numpy(b).pin_memory().numpy()
     eng.solve_batch(pa, pb, off, off, undirected=undirected)
+    ke = max(3, steps // 2)
     t0 = time.perf_counter()
-    ke = max(3, args.steps // 2)
     for _ in range(ke):
         eng.solve_batch(pa, pb, off, off, undirected=undirected)
     t_e2e = (time.perf_counter() - t0) / ke
@@ -336,42 +576,67 @@ def main_batch(args):
         assert np.array_equal(rp["hd_f32"], res["hd_f32"]), "plain and batched disagree"
         plain = {"variant": "per-problem plain EB launches", "ms_per_step": tp * 1e3,
                  "solves_per_s": n / tp, "speedup_batched_vs_plain": tp * 1e3 / ms}
-    peak, peak_kind = load_peaks()
+    peaks, pkind = load_peaks()
     sizes = np.diff(off)
     alg = float((2 if undirected else 1) * (2 * sizes).sum() * 8)  # both sets, both directions
     achieved = alg / (ms / 1e3) / 1e9
-    roof = {"bound": "hbm", "kernel": "batch_graph", "achieved": achieved, "peak": peak,
-            "unit": "GB/s", "frac": achieved / peak, "traffic": traffic_from_profiles("batch", float(sizes.sum())),
-            "algorithmic_bytes": alg, "kernel_ms": ms, "peak_source": peak_kind + " hbm_gbs"}
-    base = None if (args.no_cpu or world > 1) else cpu_baseline_batch(a, b, off, undirected)
-    if rank == 0:
-        print(json.dumps({
-            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded numpy PCG64)",
-            "config": {"workload": (f"{n} 2-D polyline-pair problems, sizes round(LogNormal(ln 200,"
-                                    f" 1.2)) clipped to [8, 50000], {int(sizes.sum())} points "
-                                    "per side"), "undirected": undirected,
-                       "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
-            "gpairs_per_s_effective": float((sizes.astype(np.float64) ** 2).sum()
-                                            * (2 if undirected else 1) / (ms / 1e3) / 1e9),
-            "plain_per_problem": plain,
-            "e2e": {"value": world * n / t_e2e, "unit": "solves/s",
-                    "h2d_bytes_per_step": int(a.nbytes + b.nbytes + n * 32),
-                    "d2h_bytes_per_step": int(n * 16)},
-            "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": base, "clocks": clk,
-        }), flush=True)
-    eng.close()
+    fig = profile_figures("batch")
+    roof = {"bound": "hbm", "kernel": "batch_graph", "achieved": achieved,
+            "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+            "traffic": traffic_from_profiles("batch", float(sizes.sum())),
+            "algorithmic_bytes": alg, "ms": ms, "issue_active_ncu": fig.get("issue_active"),
+            "peak_source": pkind + " hbm_gbs"}
+    oracle = None
+    if not args.no_oracle and ctx["rank"] == 0:
+        h64, t_or = oracle_batch_hd64(a, b, off, undirected)
+        rel = np.abs(res["hd_f32"].astype(np.float64) - h64) / np.maximum(h64, 1e-30)
+        oracle = {"max_rel_err_vs_oracle": float(rel.max()), "oracle_s": t_or,
+                  "what": "per problem |hd_f32 - H64| / H64, maximum over the batch"}
+    base = None
+    if ctx["rank"] == 0 and world == 1 and not args.no_cpu:
+        base = cpu_batch_baseline(a, b, off, undirected)
+    return {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": steps, "warmup": warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": workload_desc("polylines", n) + f", {int(sizes.sum())} points per side",
+                   "undirected": undirected, "l2": "inputs larger than L2 (no flush)",
+                   "parallelism": f"replicas x{world}"},
+        "variant_used": ["batch", "batch"],
+        "gpairs_per_s_effective": float((sizes.astype(np.float64) ** 2).sum()
+                                        * (2 if undirected else 1) / (ms / 1e3) / 1e9),
+        "rel_err_vs_oracle": oracle["max_rel_err_vs_oracle"] if oracle else None,
+        "oracle": oracle,
+        "plain_per_problem": plain,
+        "e2e": {"value": world * n / t_e2e, "unit": "solves/s",
+                "h2d_bytes_per_step": int(a.nbytes + b.nbytes + n * 32),
+                "d2h_bytes_per_step": int(n * 16)},
+        "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": base, "clocks": clk,
+        "data_gen_s": t_gen,
+    }
+
+
+def l2_note(nbytes):
+    if nbytes > 130e6:
+        return "inputs larger than L2 (no flush)"
+    return ("inputs smaller than L2, no flush: every step re-sorts or re-packs both sets, so "
+            "the solve rebuilds its own working set each step")
+
+
+def sub_steps(name, steps, warmup):
+    """Steps for a workload measured beside the headline: K and W as given,
+    except that the long 64-D solves (~0.4 s each) keep their timed region to
+    a few seconds."""
+    if name == "unit64":
+        return max(3, min(steps, 8)), max(3, min(warmup, 3))
+    return steps, warmup
 
 
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
-        return
-    if args.workload == "polylines":
-        main_batch(args)
         return
     import torch
     import torch.distributed as dist
@@ -389,183 +654,96 @@ def main():
         if world > 1:
             dist.barrier()
 
-    n = args.n or WORKLOAD_SIZES[args.workload]
-    a, b = make_data(args.workload, n)
-    undirected = not args.directed
-    dims = a.shape[1]
     stream = torch.cuda.current_stream()
     eng = hd.Engine(device=local, variant=args.variant)
     eng.set_stream(stream.cuda_stream)
-    ta = torch.from_numpy(a).cuda()
-    tb = torch.from_numpy(b).cuda()
+    ctx = {"stream": stream, "local": local, "world": world, "rank": rank, "barrier": barrier}
+    names = ALL if args.workload == "all" else [args.workload]
+
     if args.profile:
-        r = eng.solve(ta, tb, undirected=undirected)
+        name = names[0]
+        n = args.n or WORKLOAD_SIZES[name]
+        if name == "polylines":
+            a, b, off = make_data(name, n)
+            eng.solve_batch(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(), off, off,
+                            undirected=not args.directed)
+            out = {"profile_solve": True, "workload": name}
+        else:
+            a, b = make_data(name, n)
+            r = eng.solve(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(),
+                          undirected=not args.directed)
+            out = {"profile_solve": True, "workload": name, "hd_f32": float(r.hd_f32),
+                   "variant_used": int(r.variant_used)}
         torch.cuda.synchronize()
-        print(json.dumps({"profile_solve": True, "hd_f32": float(r.hd_f32),
-                          "variant_used": int(r.variant_used)}), flush=True)
+        print(json.dumps(out), flush=True)
         eng.close()
         return
 
-    # Instrumented run (outside the timed region): visited pairs / nodes for
-    # the algorithmic byte counts of the roofline.
-    rc = eng.solve(ta, tb, undirected=undirected, count_pairs=True, timing=True)
-    for _ in range(args.warmup):
-        eng.solve(ta, tb, undirected=undirected)
-    torch.cuda.synchronize()
-
-    clocks = ClockSampler(local)
-    clocks.start()
-    launches0 = eng.kernel_launches
-    phase = np.zeros(8)
-    barrier()
-    torch.cuda.synchronize()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    res = None
-    for _ in range(args.steps):
-        res = eng.solve(ta, tb, undirected=undirected, timing=True)
-        phase += np.array(res.phase_ms[:8])
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    elapsed_ms = ev0.elapsed_time(ev1)
-    launches = eng.kernel_launches - launches0
-    clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-    ms_step = elapsed_ms / args.steps
-    value = world * args.steps / (elapsed_ms / 1e3)
-    pairs_eff = (2 if undirected else 1) * float(n) * float(n)
-
-    # End to end through the C ABI from pinned host buffers.
-    pa = torch.from_numpy(a).pin_memory()
-    pb = torch.from_numpy(b).pin_memory()
-    na, nb = pa.numpy(), pb.numpy()
-    for _ in range(2):
-        eng.solve(na, nb, undirected=undirected)
-    barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    e2e_steps = max(3, args.steps // 2)
-    for _ in range(e2e_steps):
-        re2e = eng.solve(na, nb, undirected=undirected)
-    t_e2e = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([t_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
-    assert re2e.hd_f32 == res.hd_f32
-
-    # Plain FP32 early-break on the same inputs ("chosen vs plain FP32").
-    plain = None
-    if not args.no_compare and args.variant != "eb":
-        eng.solve(ta, tb, undirected=undirected, variant="eb")
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        ksteps = 2
-        e0.record(stream)
-        for _ in range(ksteps):
-            rp = eng.solve(ta, tb, undirected=undirected, variant="eb")
-        e1.record(stream)
-        torch.cuda.synchronize()
-        pms = e0.elapsed_time(e1) / ksteps
-        assert rp.hd_f32 == res.hd_f32, "plain EB and chosen variant disagree"
-        plain = {"variant": "eb", "ms_per_step": pms, "solves_per_s": 1e3 / pms,
-                 "speedup_chosen_vs_plain": pms / ms_step}
-
-    # Roofline of the dominant kernel of the chosen variant.
-    peak, peak_kind = load_peaks()
-    phase_avg = phase / args.steps
-    names = ["prep", "build", "sample", "main_pass", "tail", "certify"]
-    roof = None
-    if res.variant_used in (hd._lib.VARIANT_LBVH, hd._lib.VARIANT_GRID):
-        # Query pass (phase 3): algorithmic bytes = query points (16 B each)
-        # + internal nodes visited (64 B) + leaf points scanned (16 B each).
-        leaf = 16 if res.variant_used == hd._lib.VARIANT_LBVH else 0
-        lf = rc.visited_leaves
-        alg = (2 if undirected else 1) * n * 16 + rc.visited_nodes * 64 + lf * 16 * 16
-        t_ms = phase_avg[3]
-        tag = "lbvh_query" if res.variant_used == hd._lib.VARIANT_LBVH else "grid_query"
-        achieved = alg / (t_ms / 1e3) / 1e9
-        # An undirected LBVH solve answers both directions' queries in one
-        # launch (the fused pass); otherwise one launch per direction.
-        fused = (undirected and res.variant_used == hd._lib.VARIANT_LBVH
-                 and res.variant_used_ba == hd._lib.VARIANT_LBVH)
-        nl = 1 if (fused or not undirected) else 2
-        tr = traffic_from_profiles(tag, float(n) * (2 if fused else 1))
-        roof = {"bound": "hbm", "kernel": tag, "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "traffic": tr,
-                "algorithmic_bytes_per_launch": alg / nl, "kernel_ms_per_launch": t_ms / nl,
-                "launches": nl, "peak_source": peak_kind + " hbm_gbs"}
-    elif res.variant_used == hd._lib.VARIANT_EB:
-        # The EB scan is FP32-issue bound; its HBM view counts the B tiles each
-        # CTA streams (16 B per point, one 256-point tile per 256 x 4 x 256
-        # slot-pairs), reported with the pair rate beside it.
-        t_ms = phase_avg[3]
-        alg = rc.visited_pairs * 16.0 / (256 * 4)
-        achieved = alg / (t_ms / 1e3) / 1e9
-        roof = {"bound": "hbm", "kernel": "eb_main", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                "kernel_ms": t_ms, "peak_source": peak_kind + " hbm_gbs",
-                "pairs_per_s": rc.visited_pairs / (t_ms / 1e3)}
-
-    if res.variant_used == hd._lib.VARIANT_BF16:
-        # Split-BF16 contraction: 3 products x 2 K FLOP per (a, b) pair per
-        # direction, against the sustained dense BF16 rate (a long kernel).
-        K = ((dims + 15) // 16) * 16
-        flops = (2 if undirected else 1) * 3.0 * 2.0 * K * float(n) * float(n)
-        t_ms = phase_avg[3]
-        try:
-            with open(PEAKS_PATH) as f:
-                pk = json.load(f)
-            tpeak, tkind = float(pk["bf16_tflops_sustained"]), "measured bf16_tflops_sustained"
-        except Exception:
-            tpeak, tkind = 1700.0, "fallback sustained bf16"
-        achieved = flops / (t_ms / 1e3) / 1e12
-        roof = {"bound": "tensor", "kernel": "bf16_rowmin", "achieved": achieved, "peak": tpeak,
-                "unit": "TFLOP/s", "frac": achieved / tpeak,
-                "traffic": traffic_from_profiles("bf16_rowmin", float(n) * float(n)),
-                "algorithmic_flops_per_launch": flops / (2 if undirected else 1),
-                "kernel_ms_per_launch": t_ms / (2 if undirected else 1), "peak_source": tkind,
-                "rechecked_rows": int(res.rechecked), "err_bound": res.err_bound}
-    base = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        base = cpu_baseline(a, b, undirected)
-
+    records = {}
+    for i, name in enumerate(names):
+        n = args.n or WORKLOAD_SIZES[name]
+        steps, warmup = (args.steps, args.warmup) if i == 0 else sub_steps(name, args.steps,
+                                                                           args.warmup)
+        if name == "polylines":
+            records[name] = bench_batch(eng, n, steps, warmup, args, ctx)
+        else:
+            records[name] = bench_single(eng, name, n, steps, warmup, args, ctx)
+        torch.cuda.empty_cache()
     if rank == 0:
-        line = {
-            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded numpy PCG64)",
-            "config": {"workload": workload_desc(args.workload, n), "n_a": n, "n_b": n,
-                       "n_dims": dims, "undirected": undirected, "variant": args.variant,
-                       "variant_used": [hd._lib.VARIANT_NAMES.get(res.variant_used),
-                                        hd._lib.VARIANT_NAMES.get(res.variant_used_ba)],
-                       "l2": "inputs larger than L2 (no flush)",
-                       "parallelism": f"replicas x{world}"},
-            "gpairs_per_s_effective": value * pairs_eff / 1e9,
-            "gpairs_per_s_visited": (rc.visited_pairs * value / 1e9) if rc.visited_pairs else None,
-            "hd_f32": float(res.hd_f32), "hd64_certified": res.hd,
-            "certifying_pair": [int(res.ia), int(res.ib), int(res.direction)],
-            "phase_ms": {nm: float(phase_avg[i]) for i, nm in enumerate(names)},
-            "plain_fp32_eb": plain,
-            "e2e": {"value": world * e2e_steps / t_e2e, "unit": "solves/s",
-                    "h2d_bytes_per_step": int(a.nbytes + b.nbytes),
-                    "d2h_bytes_per_step": 2 * 160},
-            "gpu_launches": int(launches),
-            "roofline": roof,
-            "cpu_baseline": base,
-            "clocks": clk,
-        }
+        line = dict(records[names[0]])
+        if len(names) > 1:
+            line["workloads"] = {nm: records[nm] for nm in names[1:]}
         print(json.dumps(line), flush=True)
     eng.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_reference(args):
+    """The reference arm: the reference's CPU early-break on all host cores
+    (oracle restatement; the reference's own x86 build cannot run on an Arm
+    host), for the headline workload, one undirected solve per step."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    name = ALL[0] if args.workload == "all" else args.workload
+    n = args.n or WORKLOAD_SIZES[name]
+    undirected = not args.directed
+    o = _oracle()
+    if name == "polylines":
+        a, b, off = make_data(name, n)
+
+        def measure():
+            return cpu_batch_baseline(a, b, off, undirected)
+    else:
+        a, b = make_data(name, n)
+        # Final squared maxima per direction (only used when a whole solve does
+        # not fit the step budget and the bounded estimate runs instead).
+        d2f = [np.float32(o.exact(a, b, 32)[0])]
+        if undirected:
+            d2f.append(np.float32(o.exact(b, a, 32)[0]))
+
+        def measure():
+            return cpu_eb_baseline(a, b, undirected, d2f, budget_s=8.0)
+    vals, base = [], None
+    for i in range(args.warmup + args.steps):
+        base = measure()
+        if i >= args.warmup:
+            vals.append(base["value"])
+    v = float(np.median(vals))
+    base["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded numpy PCG64)", "impl": "reference",
+            "config": {"workload": workload_desc(name, n), "n_a": n, "n_b": n,
+                       "n_dims": int(a.shape[1]), "undirected": undirected,
+                       "l2": l2_note(a.nbytes + b.nbytes), "parallelism": "replicas x1"},
+            "variant": "reference CPU early-break (host cores)",
+            "cpu_baseline": base,
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -103,14 +103,19 @@ def build_oracle() -> str:
     return ORACLE_LIB
 
 
+# Where the reference checkout lies in the build container (read-only); a
+# different location can be given with HD_REFERENCE_SRC.
+REFERENCE_SRC = os.environ.get("HD_REFERENCE_SRC", "/root/reference/src")
+
+
 def build_reference() -> None:
     """Builds the reference's own CPU early-break path into oracle/_ref when the
     reference sources are present (test infrastructure only)."""
     script = os.path.join(ORACLE, "build_ref.sh")
     target = os.path.join(ORACLE, "_ref", "ref_eb")
-    if os.path.exists(target):
+    if os.path.exists(target) or not os.path.isdir(REFERENCE_SRC):
         return
-    subprocess.run(["bash", script], check=False, capture_output=True)
+    subprocess.run(["bash", script, REFERENCE_SRC], check=False, capture_output=True)
 
 
 def build_all(exec_=True, oracle=True) -> None:

@@ -35,7 +35,6 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
-#include <mutex>
 
 #include "hd_common.cuh"
 #include "hd_internal.h"
@@ -488,21 +487,16 @@ static_assert(2 * sizeof(DevScalars) <= kNoAllocScalarBytes, "scalar area too sm
 // device address comes from cudaGetSymbolAddress (see noalloc_scratch).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-std::mutex g_noalloc_mu;
-void* g_noalloc_addr[256] = {};
-
-// Device address of the scratch array on the current device, looked up once
-// per device (with that device current) and cached.
-cudaError_t noalloc_scratch(int dev, unsigned char** out) {
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
-  if (!g_noalloc_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_noalloc_addr[dev] = p;
-  }
-  *out = (unsigned char*) g_noalloc_addr[dev];
+// Device address of the scratch array in the current context.  It is looked
+// up on every call rather than cached: the address belongs to the context
+// the library's module is loaded in, so it changes after a device reset or
+// under another context on the same device.  The lookup is a host-side table
+// read and allocates nothing.
+cudaError_t noalloc_scratch(unsigned char** out) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return e;
+  *out = (unsigned char*) p;
   return cudaSuccess;
 }
 
@@ -525,16 +519,35 @@ cudaError_t noalloc_direction(cudaStream_t st, int num_sms, const float* A, uint
   k_eb_heavy<D><<<n_seed, kEbThreads, 0, st>>>(A, pA, pb, nTiles, sc, nullptr, n_seed, nullptr);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (nA > n_seed) {
-    int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_eb_main<D, kEbSlots>, kEbThreads, 0);
-    occ = std::max(1, occ);
-    const uint64_t per_cta = (uint64_t) kEbThreads * kEbSlots;
-    const uint64_t want = (nA - n_seed + per_cta - 1) / per_cta;
+    // Slots per thread chosen as hd_solve's EB variant chooses them: the most
+    // (4, 2, 1) that still fill every resident CTA of a full grid.
+    const void* fns[3] = {(const void*) k_eb_main<D, 4>, (const void*) k_eb_main<D, 2>,
+                          (const void*) k_eb_main<D, 1>};
+    const int slots[3] = {4, 2, 1};
+    const uint64_t rest = nA - n_seed;
+    int pick = 2, occ = 1;
+    for (int k = 0; k < 3; ++k) {
+      int o = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fns[k], kEbThreads, 0);
+      o = std::max(1, o);
+      if (rest >= (uint64_t) num_sms * o * kEbThreads * slots[k] || k == 2) {
+        pick = k;
+        occ = o;
+        break;
+      }
+    }
+    const uint64_t per_cta = (uint64_t) kEbThreads * slots[pick];
+    const uint64_t want = (rest + per_cta - 1) / per_cta;
     const int g = (int) std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t) num_sms * occ));
-    const uint32_t capTiles = std::max<uint32_t>(1, kCapPairs / kEbTile);
-    k_eb_main<D, kEbSlots><<<g, kEbThreads, 0, st>>>(A, pA, n_seed, nA, pb, nTiles, capTiles, sc, heavy,
-                                           (uint32_t) kNoAllocMaxPoints);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    uint32_t capTiles = std::max<uint32_t>(1, kCapPairs / kEbTile);
+    const float* a_ptr = A;
+    const PT* b_ptr = pb;
+    uint32_t heavy_cap = (uint32_t) kNoAllocMaxPoints;
+    uint64_t a_begin = n_seed, a_end = nA;
+    void* args[] = {&a_ptr, &pA, &a_begin, &a_end, &b_ptr, (void*) &nTiles, &capTiles, &sc,
+                    &heavy, &heavy_cap};
+    if ((e = cudaLaunchKernel(fns[pick], dim3(g), dim3(kEbThreads), args, 0, st)) != cudaSuccess)
+      return e;
     k_eb_heavy<D><<<num_sms * 4, kEbThreads, 0, st>>>(A, pA, pb, nTiles, sc, heavy, 0,
                                                       &sc->heavy_count);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -563,19 +576,26 @@ extern "C" HD_API hd_status hd_solve_eb_noalloc(const float* A, uint64_t n_a, co
   e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess || num_sms <= 0) return HD_ERR_NO_DEVICE;
   unsigned char* base = nullptr;
-  if ((e = noalloc_scratch(dev, &base)) != cudaSuccess) return HD_ERR_CUDA;
+  if ((e = noalloc_scratch(&base)) != cudaSuccess) return HD_ERR_CUDA;
   DevScalars* sc = (DevScalars*) base;
   const bool undirected = (flags & HD_UNDIRECTED) != 0;
   const int ndir = undirected ? 2 : 1;
   // The scratch keeps the previous call's contents: reset the result words.
-  if ((e = init_scalars_on_stream(st, sc, 2)) != cudaSuccess) return HD_ERR_CUDA;
-  for (int d = 0; d < ndir; ++d) {
+  e = init_scalars_on_stream(st, sc, 2);
+  for (int d = 0; d < ndir && e == cudaSuccess; ++d) {
     const float* x = d == 0 ? A : B;
     const float* y = d == 0 ? B : A;
     const uint64_t nx = d == 0 ? n_a : n_b, ny = d == 0 ? n_b : n_a;
     e = n_dims == 2 ? noalloc_direction<2>(st, num_sms, x, nx, y, ny, base, sc + d)
                     : noalloc_direction<3>(st, num_sms, x, nx, y, ny, base, sc + d);
-    if (e != cudaSuccess) return e == cudaErrorNoKernelImageForDevice ? HD_ERR_NO_DEVICE : HD_ERR_CUDA;
+  }
+  if (e != cudaSuccess) {
+    // Kernels queued before the failing launch still write the shared
+    // array: let them finish so that a retry (on any stream) does not race
+    // with them.
+    (void) cudaStreamSynchronize(st);
+    (void) cudaGetLastError();
+    return e == cudaErrorNoKernelImageForDevice ? HD_ERR_NO_DEVICE : HD_ERR_CUDA;
   }
   DevScalars h[2];
   e = cudaMemcpyAsync(h, sc, sizeof(h), cudaMemcpyDeviceToHost, st);

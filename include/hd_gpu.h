@@ -205,12 +205,16 @@ HD_API hd_status hd_solve_batch_plain(hd_ctx* ctx, const float* A, uint64_t tota
  * call returns after the result is in *out (same fields and FP32 bit-exact
  * result as hd_solve with HD_VARIANT_EB; no timing).  n_a and n_b are limited
  * to 1,048,576 points each: larger inputs return HD_ERR_INVALID_ARG before any
- * device work.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture.  Every call shares the one array, which
- * keeps the last call's contents (each call resets what must start at zero):
- * calls that overlap on the GPU — from two host threads, or on two streams —
- * race on it and must be serialised by the caller. */
+ * device work.  Every call looks up the array's device address in the current
+ * context (cudaGetSymbolAddress, which allocates nothing), so the address
+ * stays right after a device reset or under another context.  The call waits
+ * for its stream to finish its own work before it returns (it reads the result
+ * back and synchronises the stream); if a launch fails part-way, it also waits
+ * for the kernels it already queued before returning the error.  Every call
+ * shares the one array, which keeps the last call's contents (each call resets
+ * what must start at zero): calls that overlap on the GPU — from two host
+ * threads, or on two streams — race on it and must be serialised by the
+ * caller. */
 HD_API hd_status hd_solve_eb_noalloc(const float* A, uint64_t n_a, const float* B,
                                      uint64_t n_b, int n_dims, uint32_t flags,
                                      void* stream, hd_result* out);

@@ -5,9 +5,15 @@
 # reference header mixes host code with thrust/CUDA device lambdas).  The
 # shims in oracle/shim/ stand in for glog, nlohmann::json, HdrHistogram and
 # OptiX, none of which the CPU path calls at run time.
+#
+# Usage: build_ref.sh <reference src directory>   (or HD_REFERENCE_SRC=<dir>)
 set -euo pipefail
 here="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-ref="${HD_REFERENCE_SRC:-/root/reference/src}"
+ref="${1:-${HD_REFERENCE_SRC:-}}"
+if [ -z "$ref" ]; then
+  echo "usage: $0 <reference src directory> (or set HD_REFERENCE_SRC)" >&2
+  exit 2
+fi
 if [ ! -f "$ref/hd_impl/hausdorff_distance_early_break.h" ]; then
   echo "reference sources not found at $ref; skipping oracle/_ref" >&2
   exit 0

@@ -34,9 +34,18 @@ def _load():
         lib.hd_oracle_eb.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint64, ctypes.c_int,
                                      ctypes.c_int, ctypes.c_int, ctypes.c_uint64, P, P, P, P]
         lib.hd_oracle_eb.restype = ctypes.c_int
+        lib.hd_oracle_eb_window.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint64,
+                                            ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_uint64, ctypes.c_uint64, ctypes.c_float,
+                                            P, P, P, P]
+        lib.hd_oracle_eb_window.restype = ctypes.c_int
         lib.hd_oracle_exact.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint64, ctypes.c_int,
                                         ctypes.c_int, ctypes.c_int, P, P, P]
         lib.hd_oracle_exact.restype = ctypes.c_int
+        lib.hd_oracle_exact_batch.argtypes = [P, P, P, P, ctypes.c_uint64, ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P,
+                                              P]
+        lib.hd_oracle_exact_batch.restype = ctypes.c_int
         lib.hd_oracle_dist2_f32.argtypes = [P, P, ctypes.c_int]
         lib.hd_oracle_dist2_f32.restype = ctypes.c_float
         _lib = lib
@@ -66,6 +75,27 @@ def eb(A, B, seed=0, n_threads=1, limit_a=0):
             "compute_ms": cm.value, "shuffle_ms": sm.value}
 
 
+def eb_window(A, B, begin, end, cmax2_init, seed=0, n_threads=1):
+    """The reference CPU early-break restated, over the window [begin, end)
+    of the seeded shuffle of A, starting from the running maximum cmax2_init
+    (a squared distance).  Returns the same dict as eb()."""
+    lib = _load()
+    A = _f32(A)
+    B = _f32(B)
+    hd = ctypes.c_float()
+    pairs = ctypes.c_uint64()
+    cm = ctypes.c_double()
+    sm = ctypes.c_double()
+    st = lib.hd_oracle_eb_window(A.ctypes.data, A.shape[0], B.ctypes.data, B.shape[0],
+                                 A.shape[1], seed, n_threads, begin, end, float(cmax2_init),
+                                 ctypes.byref(hd), ctypes.byref(pairs), ctypes.byref(cm),
+                                 ctypes.byref(sm))
+    if st != 0:
+        raise ValueError("oracle eb_window: unsupported input")
+    return {"hd": np.float32(hd.value), "compared_pairs": int(pairs.value),
+            "compute_ms": cm.value, "shuffle_ms": sm.value}
+
+
 def exact(A, B, precision=32, n_threads=None):
     """Exact directed max-min: returns (hd2, ia, ib) with hd2 the squared
     distance (FP32 formula for precision=32, FP64 for 64) and the certifying
@@ -84,6 +114,31 @@ def exact(A, B, precision=32, n_threads=None):
     if st != 0:
         raise ValueError("oracle exact: unsupported input")
     return h2.value, int(ia.value), int(ib.value)
+
+
+def exact_batch(A, B, offsets_a, offsets_b, precision=32, undirected=True, n_threads=None):
+    """Exact max-min of many independent problems (problem p owns rows
+    offsets_a[p]..offsets_a[p+1]-1 of A and the same of B).  Returns arrays
+    (hd2, ia, ib, direction); ia/ib are relative to the problem's start and
+    index the direction's own source/target set."""
+    lib = _load()
+    A = _f32(A)
+    B = _f32(B)
+    oa = np.ascontiguousarray(offsets_a, dtype=np.uint64)
+    ob = np.ascontiguousarray(offsets_b, dtype=np.uint64)
+    n = len(oa) - 1
+    if n_threads is None:
+        n_threads = os.cpu_count() or 1
+    h2 = np.zeros(n, np.float64)
+    ia = np.zeros(n, np.uint64)
+    ib = np.zeros(n, np.uint64)
+    dr = np.zeros(n, np.int32)
+    st = lib.hd_oracle_exact_batch(A.ctypes.data, B.ctypes.data, oa.ctypes.data, ob.ctypes.data,
+                                   n, A.shape[1], precision, int(undirected), n_threads,
+                                   h2.ctypes.data, ia.ctypes.data, ib.ctypes.data, dr.ctypes.data)
+    if st != 0:
+        raise ValueError("oracle exact_batch: unsupported input")
+    return h2, ia, ib, dr
 
 
 def dist2_f32(a, b):

@@ -10,7 +10,7 @@ count for n_threads=1 (deterministic: it depends only on the seeded shuffle),
 and the distance for n_threads=4.
 
 Run from the repository root, in a container that has the reference sources:
-    oracle/build_ref.sh && python tests/golden/make_golden.py
+    oracle/build_ref.sh <reference src directory> && python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -85,7 +85,7 @@ def run_ref(a_path, b_path, dims, seed, threads):
 
 def main():
     if not os.path.exists(REF):
-        sys.exit("oracle/_ref/ref_eb is missing: run oracle/build_ref.sh first")
+        sys.exit("oracle/_ref/ref_eb is missing: run oracle/build_ref.sh <reference src directory> first")
     inp = os.path.join(HERE, "inputs")
     os.makedirs(inp, exist_ok=True)
     records = []
