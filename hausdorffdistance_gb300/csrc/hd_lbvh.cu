@@ -33,7 +33,6 @@
 // every lane of the packet.  x and y of a box sit in aligned register pairs,
 // so the box distances use the packed pair instructions.
 #include <cfloat>
-#include <cstdlib>
 
 #include "hd_common.cuh"
 #include "hd_internal.h"
@@ -626,97 +625,6 @@ __global__ void __launch_bounds__(kDeferWarps * 32) k_lbvh_defer(QuerySets qs) {
   }
 }
 
-// Heap-ordered tree over the Morton-sorted leaves.  The leaf count is padded
-// to a power of two P; internal node h (0 = root) has children 2h+1 and 2h+2,
-// so internal nodes are heap positions [0, P-1) and leaf j sits at heap
-// position P-1+j.  Leaves j >= nL are empty (inverted boxes: every box
-// distance to them is +inf, so no query ever enters them).  Each node covers
-// a contiguous, count-balanced range of the Morton order, so boxes need no
-// pointer-chasing to build: one CTA reduces up to 1024 consecutive boxes of a
-// level through up to 10 levels in shared memory and writes the packed nodes
-// of those levels; the next launch continues from the boxes it leaves.
-constexpr int kTreeSpan = 1024;
-
-struct LevelSet {
-  const float4* in;     // boxes of this level (lo, hi pairs); leaf boxes at t0 = 0
-  float4* out;          // boxes of the level kTreeSpan times smaller (may be unused)
-  float4* nodes;        // packed nodes
-  uint32_t count;       // boxes at this level (P >> t0)
-  uint32_t valid;       // boxes of this level that exist (nL at t0 = 0; else count)
-  uint32_t P;           // padded leaf count
-  uint32_t t0;          // level of the input boxes (0 = leaves)
-};
-struct LevelSets {
-  LevelSet s[2];
-};
-
-__global__ void __launch_bounds__(kTreeSpan / 2) k_tree_levels(LevelSets ls) {
-  const LevelSet& S = ls.s[blockIdx.y];
-  __shared__ float4 slo[kTreeSpan], shi[kTreeSpan];
-  const uint32_t span = min((uint32_t) kTreeSpan, S.count);
-  const uint32_t base = blockIdx.x * span;
-  if (base >= S.count) return;
-  const float4 empty_lo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f);
-  const float4 empty_hi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
-  for (uint32_t i = threadIdx.x; i < span; i += blockDim.x) {
-    const uint32_t j = base + i;
-    if (j < S.valid) {
-      slo[i] = S.in[2 * (uint64_t) j];
-      shi[i] = S.in[2 * (uint64_t) j + 1];
-    } else {
-      slo[i] = empty_lo;
-      shi[i] = empty_hi;
-    }
-  }
-  __syncthreads();
-  uint32_t m = span;  // boxes at the current level in shared memory
-  uint32_t t = S.t0;  // their level
-  while (m > 1) {
-    const uint32_t half = m >> 1;
-    // Parents of this level: level t+1 holds P >> (t+1) nodes, starting at
-    // heap position (P >> (t+1)) - 1.
-    const uint32_t first = (S.P >> (t + 1)) - 1u;
-    const uint32_t lvl_base = base >> (t + 1 - S.t0);  // this CTA's first parent in its level
-    float4 plo = empty_lo, phi = empty_hi;
-    const uint32_t i = threadIdx.x;
-    if (i < half) {
-      const float4 alo = slo[2 * i], ahi = shi[2 * i];
-      const float4 blo = slo[2 * i + 1], bhi = shi[2 * i + 1];
-      plo = make_float4(fminf(alo.x, blo.x), fminf(alo.y, blo.y), fminf(alo.z, blo.z), 0.f);
-      phi = make_float4(fmaxf(ahi.x, bhi.x), fmaxf(ahi.y, bhi.y), fmaxf(ahi.z, bhi.z), 0.f);
-      const uint32_t h = first + lvl_base + i;  // heap position of the parent
-      uint32_t left, right;
-      if (t == 0) {
-        // Children are leaves: refs carry the leaf index.
-        const uint32_t j = 2u * (lvl_base + i);
-        left = j | kLeafBit;
-        right = (j + 1u) | kLeafBit;
-      } else {
-        left = 2u * h + 1u;
-        right = 2u * h + 2u;
-      }
-      float4* o = S.nodes + 4 * (uint64_t) h;
-      o[0] = make_float4(alo.x, alo.y, ahi.x, ahi.y);
-      o[1] = make_float4(blo.x, blo.y, bhi.x, bhi.y);
-      o[2] = make_float4(alo.z, ahi.z, blo.z, bhi.z);
-      o[3] = make_float4(__uint_as_float(left), __uint_as_float(right), 0.f, 0.f);
-    }
-    __syncthreads();
-    if (i < half) {
-      slo[i] = plo;
-      shi[i] = phi;
-    }
-    __syncthreads();
-    m = half;
-    ++t;
-  }
-  // This CTA's top box feeds the next launch.
-  if (threadIdx.x == 0 && S.count > span) {
-    S.out[2 * (uint64_t) blockIdx.x] = slo[0];
-    S.out[2 * (uint64_t) blockIdx.x + 1] = shi[0];
-  }
-}
-
 template <int D>
 __global__ void k_packet_pos(QuerySets qs) {
   const QuerySet& S = qs.d[blockIdx.y];
@@ -782,83 +690,6 @@ static hd_status build_lbvhs(Ctx& c, const SortedSet* const* sets, int count, Bu
   return after_launch(c, "bottom_up");
 }
 
-// Builds the heap-ordered trees of `count` sorted sets (tree k into node
-// slot k): a few launches of k_tree_levels, each reducing up to 10 levels.
-static hd_status build_heap_trees(Ctx& c, const SortedSet* const* sets, int count,
-                                  BuildSets* out) {
-  const uint32_t L = sets[0]->leaf_size;
-  hd_status s;
-  uint32_t nL[2] = {1, 1}, P[2] = {2, 2};
-  uint64_t tmp_boxes = 0;
-  for (int k = 0; k < count; ++k) {
-    if (sets[k]->leaf_size != L) return fail(c, HD_ERR_CUDA, "leaf sizes differ");
-    nL[k] = (uint32_t) ((sets[k]->n + L - 1) / L);
-    while (P[k] < nL[k]) P[k] <<= 1;
-    tmp_boxes = std::max<uint64_t>(tmp_boxes, 2 * (uint64_t) (P[k] / kTreeSpan + 1));
-  }
-  void* tmp;
-  if ((s = ensure(c, kBufBoxes, (uint64_t) count * 2 * tmp_boxes * 2 * sizeof(float4), &tmp)) != HD_OK)
-    return s;
-  LevelSets ls;
-  uint32_t t0[2] = {0, 0}, cnt[2] = {0, 0};
-  for (int k = 0; k < count; ++k) {
-    void* nodes;
-    if ((s = ensure(c, k == 0 ? kBufNodes0 : kBufNodes1, (uint64_t) (P[k] - 1) * 4 * sizeof(float4),
-                    &nodes)) != HD_OK)
-      return s;
-    BuildSet& b = out->s[k];
-    b = BuildSet{};
-    b.pts = sets[k]->pts;
-    b.codes = sets[k]->codes;
-    b.n = sets[k]->n;
-    b.L = L;
-    b.nL = nL[k];
-    b.nI = P[k] - 1;
-    b.leaf_boxes = sets[k]->leaf_boxes;
-    b.nodes = (float4*) nodes;
-    ls.s[k] = LevelSet{sets[k]->leaf_boxes, nullptr, (float4*) nodes, P[k], nL[k], P[k], 0};
-    cnt[k] = P[k];
-  }
-  if (count == 1) {
-    out->s[1] = out->s[0];
-    ls.s[1] = ls.s[0];
-    ls.s[1].count = 0;
-    cnt[1] = 1;
-  }
-  float4* bufs[2][2];
-  for (int k = 0; k < 2; ++k)
-    for (int h = 0; h < 2; ++h)
-      bufs[k][h] = (float4*) tmp + (uint64_t) (2 * k + h) * 2 * tmp_boxes;
-  for (int round = 0; cnt[0] > 1 || cnt[1] > 1; ++round) {
-    uint32_t gx = 1;
-    for (int k = 0; k < 2; ++k) {
-      LevelSet& l = ls.s[k];
-      if (cnt[k] <= 1) {
-        l.count = 0;  // this set's tree is complete: its CTAs return at once
-        continue;
-      }
-      const uint32_t span = std::min<uint32_t>(kTreeSpan, cnt[k]);
-      l.count = cnt[k];
-      l.t0 = t0[k];
-      l.out = bufs[k][round & 1];
-      gx = std::max(gx, cnt[k] / span);
-    }
-    k_tree_levels<<<dim3(gx, 2), kTreeSpan / 2, 0, c.stream>>>(ls);
-    if ((s = after_launch(c, "tree_levels")) != HD_OK) return s;
-    for (int k = 0; k < 2; ++k) {
-      if (cnt[k] <= 1) continue;
-      const uint32_t span = std::min<uint32_t>(kTreeSpan, cnt[k]);
-      uint32_t lv = 0;
-      while ((1u << lv) < span) ++lv;
-      t0[k] += lv;
-      cnt[k] /= span;
-      ls.s[k].in = ls.s[k].out;
-      ls.s[k].valid = cnt[k];
-    }
-  }
-  return HD_OK;
-}
-
 // Directed LBVH solves of `count` directions (1, or 2 for an undirected solve)
 // with shared launches.
 static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
@@ -909,11 +740,7 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
   if ((s = after_launch(c, "packet_pos")) != HD_OK) return s;
   cudaEventRecord(c.batch_join, c.batch_side);
   BuildSets bs;
-  if (getenv("HDG_TREE_KARRAS")) {
-    if ((s = build_lbvhs(c, t, count, &bs)) != HD_OK) return s;
-  } else {
-    if ((s = build_heap_trees(c, t, count, &bs)) != HD_OK) return s;
-  }
+  if ((s = build_lbvhs(c, t, count, &bs)) != HD_OK) return s;
   mark(c, 2);
   cudaStreamWaitEvent(c.stream, c.batch_join, 0);
   uint64_t max_warps = 0;
