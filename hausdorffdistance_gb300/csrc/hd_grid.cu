@@ -105,9 +105,9 @@ __global__ void k_grid_runs(const uint32_t* __restrict__ codes, uint64_t n, int 
   const uint32_t shift = gp->shift, cpa = gp->cpa;
   for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
        i += (uint64_t) gridDim.x * blockDim.x) {
-    const uint32_t c = (codes[i] & kCodeMask) >> shift;
-    const bool first = i == 0 || ((codes[i - 1] & kCodeMask) >> shift) != c;
-    const bool last = i + 1 == n || ((codes[i + 1] & kCodeMask) >> shift) != c;
+    const uint32_t c = (codes[i] & kSortedMask) >> shift;
+    const bool first = i == 0 || ((codes[i - 1] & kSortedMask) >> shift) != c;
+    const bool last = i + 1 == n || ((codes[i + 1] & kSortedMask) >> shift) != c;
     if (first || last) {
       const uint32_t lin = cell_linear(c, dims, cpa);
       if (first) table[lin].x = (uint32_t) i;
@@ -254,13 +254,13 @@ __global__ void __launch_bounds__(256)
   for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
     const Deferred dfr = list[e];
     const float4 q = Q[dfr.qpos];
-    const uint32_t code = frame_code<D>(*tframe, q.x, q.y, q.z);
+    const uint32_t code = frame_code<D>(*tframe, q.x, q.y, q.z) & kSortedMask;
     // First B position whose code is >= the query's (every thread finds the
     // same one).
     uint64_t lo = 0, hi = nB;
     while (lo < hi) {
       const uint64_t mid = (lo + hi) >> 1;
-      if ((bcodes[mid] & kCodeMask) < code) lo = mid + 1;
+      if ((bcodes[mid] & kSortedMask) < code) lo = mid + 1;
       else hi = mid;
     }
     const uint64_t p0 = lo;

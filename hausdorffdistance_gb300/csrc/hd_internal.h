@@ -13,6 +13,12 @@ namespace hdg {
 // Bits of a sorted key that hold the Morton code (bit 30 marks the set in
 // the fused sort of small sets).
 constexpr uint32_t kCodeMask = (1u << 30) - 1u;
+// Code bits below kSortLowBits are left out of the sort of large sets (one
+// radix pass fewer): the sorted order is exact only above them, so every
+// consumer compares codes through kSortedMask (cells of 2^-8 of the frame per
+// axis in 3-D, 2^-12 in 2-D; grid levels never go finer).
+constexpr int kSortLowBits = 6;
+constexpr uint32_t kSortedMask = kCodeMask & ~((1u << kSortLowBits) - 1u);
 // From this many points (|A| + |B|) the two sets are sorted as independent
 // chains, each in its own frame (and, for host inputs, A's sort overlaps
 // B's copy); below it one fused chain in a common frame has fewer launches

@@ -1,7 +1,8 @@
-// LBVH variant: a linear BVH over Morton-sorted B, built with Karras' radix
-// tree construction (T. Karras, "Maximizing Parallelism in the Construction
-// of BVHs, Octrees, and k-d Trees", HPG 2012) and bottom-up box fitting, and
-// a warp-packet nearest-neighbour traversal with early break.
+// LBVH variant: a linear BVH over Morton-sorted B — the binary radix tree of
+// Karras ("Maximizing Parallelism in the Construction of BVHs, Octrees, and
+// k-d Trees", HPG 2012), built together with its boxes in one agglomerative
+// bottom-up pass (Apetrei, CGVC 2014) — and a warp-packet nearest-neighbour
+// traversal with early break.
 //
 // It replaces the reference's OptiX/RT-core search
 // (src/hd_impl/hausdorff_distance_ray_tracing.h:63-236 with the programs of
@@ -57,88 +58,46 @@ struct Deferred {
   uint32_t gmin;
 };
 
-__device__ __forceinline__ int delta(const uint32_t* __restrict__ codes, uint32_t L,
-                                     int64_t nL, int64_t i, int64_t j) {
-  if (j < 0 || j >= nL) return -1;
-  uint64_t ki = ((uint64_t) (codes[(uint64_t) i * L] & kCodeMask) << 32) | (uint64_t) i;
-  uint64_t kj = ((uint64_t) (codes[(uint64_t) j * L] & kCodeMask) << 32) | (uint64_t) j;
+// Common-prefix length of the keys of leaves i and i+1 (i + 1 < nL).  A
+// leaf's key is its first point's sorted Morton code with the leaf index
+// appended, which makes every key distinct.
+__device__ __forceinline__ int leaf_delta(const uint32_t* __restrict__ codes, uint32_t L,
+                                          uint32_t i) {
+  const uint64_t ki = ((uint64_t) (codes[(uint64_t) i * L] & kSortedMask) << 32) | (uint64_t) i;
+  const uint64_t kj =
+      ((uint64_t) (codes[(uint64_t) (i + 1) * L] & kSortedMask) << 32) | (uint64_t) (i + 1);
   return __clzll(ki ^ kj);
 }
 
-// Karras 2012, one thread per internal node.  Node ids: internal [0, nI),
-// leaves nI + [0, nL).  Keys are the leaves' first Morton codes augmented
-// with the leaf index, which makes them distinct.
-__device__ __forceinline__ void karras_body(const uint32_t* __restrict__ codes, uint32_t L,
-                                            uint32_t nL, uint2* __restrict__ child,
-                                            uint32_t* __restrict__ parent) {
-  const int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x;
-  const int64_t nI = (int64_t) nL - 1;
-  if (i >= nI) return;
-  const int d = (delta(codes, L, nL, i, i + 1) - delta(codes, L, nL, i, i - 1)) >= 0 ? 1 : -1;
-  const int dmin = delta(codes, L, nL, i, i - d);
-  int64_t lmax = 2;
-  while (delta(codes, L, nL, i, i + lmax * d) > dmin) lmax <<= 1;
-  int64_t l = 0;
-  for (int64_t t = lmax >> 1; t >= 1; t >>= 1)
-    if (delta(codes, L, nL, i, i + (l + t) * d) > dmin) l += t;
-  const int64_t j = i + l * d;
-  const int dnode = delta(codes, L, nL, i, j);
-  int64_t s = 0;
-  int64_t div = 2;
-  for (;;) {
-    int64_t t = (l + div - 1) / div;
-    if (delta(codes, L, nL, i, i + (s + t) * d) > dnode) s += t;
-    if (t <= 1) break;
-    div <<= 1;
-  }
-  const int64_t gamma = i + s * d + min(d, 0);
-  const int64_t lo = min(i, j), hi = max(i, j);
-  uint32_t left = (lo == gamma) ? ((uint32_t) gamma | kLeafBit) : (uint32_t) gamma;
-  uint32_t right = (hi == gamma + 1) ? ((uint32_t) (gamma + 1) | kLeafBit) : (uint32_t) (gamma + 1);
-  child[i] = make_uint2(left, right);
-  parent[(left & kLeafBit) ? nI + (left & ~kLeafBit) : left] = (uint32_t) i;
-  parent[(right & kLeafBit) ? nI + (right & ~kLeafBit) : right] = (uint32_t) i;
-}
-
-__device__ __forceinline__ uint32_t node_id(uint32_t ref, uint32_t nI) {
-  return (ref & kLeafBit) ? nI + (ref & ~kLeafBit) : ref;
-}
-
-// Bottom-up boxes: a thread per leaf climbs; the second child to arrive at a
-// parent computes its box (Karras 2012, section 4) and writes the packed node
-// (4 float4: both children's boxes and refs).
-// Box of node `id`: leaves' boxes come from the sorted set's gather pass,
-// internal boxes from this bottom-up pass (written by other threads: read
-// around L1).
-__device__ __forceinline__ void node_box(uint32_t id, uint32_t nI, const float4* boxes,
-                                         const float4* __restrict__ leaf_boxes, float4* lo,
-                                         float4* hi) {
-  if (id >= nI) {
-    *lo = leaf_boxes[2 * (uint64_t) (id - nI)];
-    *hi = leaf_boxes[2 * (uint64_t) (id - nI) + 1];
-  } else {
-    *lo = __ldcg(&boxes[2 * (uint64_t) id]);
-    *hi = __ldcg(&boxes[2 * (uint64_t) id + 1]);
-  }
-}
-
 // Arrival count at a parent with release and acquire semantics (GPU scope):
-// it publishes this thread's box writes to whichever thread arrives second,
-// and the second arriver sees the first one's box (the RMW chain on the
-// flag carries the synchronisation), without full fences.
+// it publishes this thread's writes to whichever thread arrives second, and
+// the second arriver sees the first one's (the RMW chain on the flag carries
+// the synchronisation), without full fences.
 __device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t* p) {
   uint32_t old;
   asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
   return old;
 }
 
-__device__ __forceinline__ void bottom_up_body(const uint2* __restrict__ child,
-                                               const uint32_t* __restrict__ parent, uint32_t nL,
-                                               uint32_t nI, float4* boxes,
-                                               const float4* __restrict__ leaf_boxes,
-                                               uint32_t* flags, float4* __restrict__ nodes) {
-  uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
-  if (nI == 0) {
+// Agglomerative build of the binary radix tree over the leaves' keys, with
+// boxes, in one bottom-up pass (after Apetrei, "Fast and Simple Agglomerative
+// LBVH Construction", CGVC 2014): it yields the tree of Karras' construction
+// (HPG 2012) without its per-node searches.  A thread starts at a leaf with
+// the range [l, r] = [i, i].  The node's parent is internal node r (the node
+// is its left child) when the key pair (r, r+1) shares a longer prefix than
+// (l-1, l), else internal node l-1 (right child); the ends of the array
+// decide alone.  Each arriver writes its half of the parent's packed node
+// (its box and reference) and its outer range bound, then arrives; the first
+// to arrive stops, the second reads its sibling's half, forms the union box
+// and climbs with the merged range.  The thread that completes [0, nL-1]
+// records the root.
+__device__ __forceinline__ void agglomerate_body(const uint32_t* __restrict__ codes, uint32_t L,
+                                                 uint32_t nL,
+                                                 const float4* __restrict__ leaf_boxes,
+                                                 uint32_t* flags, uint32_t* bound, uint32_t* root,
+                                                 float4* nodes) {
+  const uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nL == 1) {
     // Single leaf: a root whose right child is an empty box (never visited).
     if (leaf == 0) {
       const float4 lo = leaf_boxes[0], hi = leaf_boxes[1];
@@ -146,31 +105,38 @@ __device__ __forceinline__ void bottom_up_body(const uint2* __restrict__ child,
       nodes[1] = make_float4(FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX);
       nodes[2] = make_float4(lo.z, hi.z, FLT_MAX, -FLT_MAX);
       nodes[3] = make_float4(__uint_as_float(kLeafBit), __uint_as_float(kLeafBit), 0.f, 0.f);
+      *root = 0;
     }
     return;
   }
   if (leaf >= nL) return;
-  uint32_t node = nI + leaf;
+  float4 lo = leaf_boxes[2 * (uint64_t) leaf], hi = leaf_boxes[2 * (uint64_t) leaf + 1];
+  uint32_t l = leaf, r = leaf, me = leaf | kLeafBit;
   for (;;) {
-    uint32_t p = parent[node];
-    if (arrive_acq_rel(&flags[p]) == 0) return;
-    uint2 ch = child[p];
-    uint32_t a = node_id(ch.x, nI), b = node_id(ch.y, nI);
-    float4 alo, ahi, blo, bhi;
-    node_box(a, nI, boxes, leaf_boxes, &alo, &ahi);
-    node_box(b, nI, boxes, leaf_boxes, &blo, &bhi);
-    float4 lo = make_float4(fminf(alo.x, blo.x), fminf(alo.y, blo.y), fminf(alo.z, blo.z), 0.f);
-    float4 hi = make_float4(fmaxf(ahi.x, bhi.x), fmaxf(ahi.y, bhi.y), fmaxf(ahi.z, bhi.z), 0.f);
-    __stcg(&boxes[2 * (uint64_t) p], lo);
-    __stcg(&boxes[2 * (uint64_t) p + 1], hi);
-    // The packed node the query reads: both children's boxes and refs.
+    const bool left_child = l == 0 || (r != nL - 1 && leaf_delta(codes, L, r) >
+                                                           leaf_delta(codes, L, l - 1));
+    const uint32_t p = left_child ? r : l - 1;
+    const int side = left_child ? 0 : 1;
     float4* o = nodes + 4 * (uint64_t) p;
-    o[0] = make_float4(alo.x, alo.y, ahi.x, ahi.y);
-    o[1] = make_float4(blo.x, blo.y, bhi.x, bhi.y);
-    o[2] = make_float4(alo.z, ahi.z, blo.z, bhi.z);
-    o[3] = make_float4(__uint_as_float(ch.x), __uint_as_float(ch.y), 0.f, 0.f);
-    if (p == 0) return;
-    node = p;
+    o[side] = make_float4(lo.x, lo.y, hi.x, hi.y);
+    reinterpret_cast<float2*>(o + 2)[side] = make_float2(lo.z, hi.z);
+    reinterpret_cast<uint32_t*>(o + 3)[side] = me;
+    bound[2 * (uint64_t) p + side] = left_child ? l : r;
+    if (arrive_acq_rel(&flags[p]) == 0) return;
+    const float4 sxy = __ldcg(o + (1 - side));
+    const float2 sz = __ldcg(reinterpret_cast<const float2*>(o + 2) + (1 - side));
+    const uint32_t other = __ldcg(&bound[2 * (uint64_t) p + (1 - side)]);
+    lo = make_float4(fminf(lo.x, sxy.x), fminf(lo.y, sxy.y), fminf(lo.z, sz.x), 0.f);
+    hi = make_float4(fmaxf(hi.x, sxy.z), fmaxf(hi.y, sxy.w), fmaxf(hi.z, sz.y), 0.f);
+    if (left_child)
+      r = other;
+    else
+      l = other;
+    me = p;
+    if (l == 0 && r == nL - 1) {
+      *root = p;
+      return;
+    }
   }
 }
 
@@ -222,7 +188,8 @@ template <int D, bool COUNT, int LT>
 __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, uint64_t nItems, uint32_t pstride,
                  uint64_t rows, const uint32_t* __restrict__ ppos,
                  const float4* __restrict__ nodes, const float4* __restrict__ B, uint64_t nB,
-                 uint32_t L, DevScalars* sc, Deferred* __restrict__ defer, uint32_t budget) {
+                 uint32_t L, DevScalars* sc, Deferred* __restrict__ defer, uint32_t budget,
+                 uint32_t root) {
   __shared__ uint32_t stk[kQueryWarps][kStack];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // Packets (32 consecutive Morton-sorted queries) are visited in a
@@ -336,7 +303,7 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   }
 
   int sp = 0;
-  uint32_t next = 0;  // root (internal node 0)
+  uint32_t next = root;
   bool have = true;
   for (;;) {
     if (!__any_sync(0xFFFFFFFFu, active)) break;
@@ -434,15 +401,15 @@ __device__ __forceinline__ void packet_pos_body(const float4* __restrict__ Q,
   const uint64_t q = (t & 1) ? min(p * 32 + 31, nQ - 1) : p * 32;
   uint32_t target;
   if (qcodes) {
-    target = qcodes[q] & kCodeMask;
+    target = qcodes[q] & kSortedMask;
   } else {
     const float4 qp = Q[q];
-    target = frame_code<D>(*tframe, qp.x, qp.y, qp.z);
+    target = frame_code<D>(*tframe, qp.x, qp.y, qp.z) & kSortedMask;
   }
   uint64_t lo = 0, hi = nB;
   while (lo < hi) {
     const uint64_t mid = (lo + hi) >> 1;
-    if ((bcodes[mid] & kCodeMask) < target)
+    if ((bcodes[mid] & kSortedMask) < target)
       lo = mid + 1;
     else
       hi = mid;
@@ -458,29 +425,25 @@ struct BuildSet {
   const uint32_t* codes;
   uint64_t n;
   uint32_t L, nL, nI;
-  float4* boxes;  // internal nodes only
   const float4* leaf_boxes;
-  uint2* child;
-  uint32_t* parent;
-  uint32_t* flags;
+  uint32_t* flags;   // arrivals per internal node (zeroed before the build)
+  uint32_t* bound;   // two range bounds per internal node
+  uint32_t* root;    // the root's internal node index
   float4* nodes;
 };
 struct BuildSets {
   BuildSet s[2];
 };
 
-__global__ void k_karras(BuildSets b) {
+// Chains of dependent atomics: full occupancy (8 blocks of 256 threads per
+// SM) matters more than a few spilled values.
+__global__ void __launch_bounds__(256, 8) k_agglomerate(BuildSets b) {
   const BuildSet& S = b.s[blockIdx.y];
-  karras_body(S.codes, S.L, S.nL, S.child, S.parent);
-}
-// Latency-bound chains of atomics: full occupancy (8 blocks of 256 threads
-// per SM, at most 32 registers) matters more than a few spilled values.
-__global__ void __launch_bounds__(256, 8) k_bottom_up(BuildSets b) {
-  const BuildSet& S = b.s[blockIdx.y];
-  bottom_up_body(S.child, S.parent, S.nL, S.nI, S.boxes, S.leaf_boxes, S.flags, S.nodes);
+  agglomerate_body(S.codes, S.L, S.nL, S.leaf_boxes, S.flags, S.bound, S.root, S.nodes);
 }
 
 struct QuerySet {
+  const uint32_t* root;  // root of the target tree (internal node index)
   Deferred* defer;   // queue of over-budget queries (kDeferCap entries)
   uint32_t budget;   // visits per packet before its open queries are queued
   const float4* Q;
@@ -505,7 +468,7 @@ template <int D, bool COUNT, int LT>
 __global__ void __launch_bounds__(kQueryWarps * 32) k_lbvh_query(QuerySets qs) {
   const QuerySet& S = qs.d[blockIdx.y];
   lbvh_query_body<D, COUNT, LT>(S.Q, S.nQ, S.pstride, S.rows, S.ppos, S.nodes, S.B, S.nB, S.L, S.sc,
-                            S.defer, S.budget);
+                            S.defer, S.budget, *S.root);
 }
 
 // Deferred pass: one warp per queued query walks the tree with 32 stack
@@ -539,7 +502,7 @@ __global__ void __launch_bounds__(kDeferWarps * 32) k_lbvh_defer(QuerySets qs) {
     const float4 q = S.Q[de.item];
     float m = __uint_as_float(de.gmin);
     float thr = read_thr();
-    if (lane == 0) st[0] = 0;  // root: internal node 0
+    if (lane == 0) st[0] = *S.root;
     int sp = 1;
     __syncwarp();
     int round = 0;
@@ -639,28 +602,26 @@ static hd_status build_lbvhs(Ctx& c, const SortedSet* const* sets, int count, Bu
   // turns positions into leaf indices with a shift.
   const uint32_t L = sets[0]->leaf_size;  // fixed by the gather's leaf boxes
   hd_status s;
-  uint64_t nodes_total = 0, internal_total = 0;
+  uint64_t internal_total = 0;
   uint64_t nL[2], nI[2];
   for (int k = 0; k < count; ++k) {
     nL[k] = (sets[k]->n + L - 1) / L;
-    nI[k] = nL[k] - 1;
-    nodes_total += nI[k] + nL[k];
-    internal_total += std::max<uint64_t>(nI[k], 1);
+    nI[k] = std::max<uint64_t>(nL[k] - 1, 1);
+    internal_total += nI[k];
     if (sets[k]->leaf_size != L) return fail(c, HD_ERR_CUDA, "leaf sizes differ");
   }
-  void *boxes, *aux, *aux2;
-  if ((s = ensure(c, kBufBoxes, internal_total * 2 * sizeof(float4), &boxes)) != HD_OK) return s;
-  if ((s = ensure(c, kBufAux, internal_total * sizeof(uint2), &aux)) != HD_OK) return s;
-  if ((s = ensure(c, kBufAux2, (nodes_total + internal_total) * 4, &aux2)) != HD_OK) return s;
-  // Flags of all sets are contiguous (first in aux2) so one memset clears them.
+  // Flags of all sets first (one memset clears them), then the bounds, then
+  // one root word per set.
+  void* aux2;
+  if ((s = ensure(c, kBufAux2, (internal_total * 3 + 2) * 4, &aux2)) != HD_OK) return s;
   uint32_t* flags_base = (uint32_t*) aux2;
-  uint32_t* parent_base = flags_base + internal_total;
-  uint64_t off_nodes = 0, off_int = 0;
-  uint64_t maxL = 0, maxI = 1;
+  uint32_t* bound_base = flags_base + internal_total;
+  uint32_t* roots = bound_base + 2 * internal_total;
+  uint64_t off_int = 0, maxL = 0;
   for (int k = 0; k < count; ++k) {
     void* nodes;
-    if ((s = ensure(c, k == 0 ? kBufNodes0 : kBufNodes1,
-                    std::max<uint64_t>(nI[k], 1) * 4 * sizeof(float4), &nodes)) != HD_OK)
+    if ((s = ensure(c, k == 0 ? kBufNodes0 : kBufNodes1, nI[k] * 4 * sizeof(float4), &nodes)) !=
+        HD_OK)
       return s;
     BuildSet& b = out->s[k];
     b.pts = sets[k]->pts;
@@ -669,25 +630,20 @@ static hd_status build_lbvhs(Ctx& c, const SortedSet* const* sets, int count, Bu
     b.L = L;
     b.nL = (uint32_t) nL[k];
     b.nI = (uint32_t) nI[k];
-    b.boxes = (float4*) boxes + 2 * off_int;
     b.leaf_boxes = sets[k]->leaf_boxes;
-    b.child = (uint2*) aux + off_int;
     b.flags = flags_base + off_int;
-    b.parent = parent_base + off_nodes;
+    b.bound = bound_base + 2 * off_int;
+    b.root = roots + k;
     b.nodes = (float4*) nodes;
-    off_nodes += nI[k] + nL[k];
-    off_int += std::max<uint64_t>(nI[k], 1);
+    off_int += nI[k];
     maxL = std::max(maxL, nL[k]);
-    maxI = std::max(maxI, nI[k]);
   }
   if (count == 1) out->s[1] = out->s[0];
-  const dim3 gl((unsigned) ((maxL + 255) / 256), count), gi((unsigned) ((maxI + 255) / 256), count);
-  k_karras<<<gi, 256, 0, c.stream>>>(*out);
-  if ((s = after_launch(c, "karras")) != HD_OK) return s;
   cudaError_t e = cudaMemsetAsync(flags_base, 0, internal_total * 4, c.stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "memset flags");
-  k_bottom_up<<<gl, 256, 0, c.stream>>>(*out);
-  return after_launch(c, "bottom_up");
+  const dim3 gl((unsigned) ((maxL + 255) / 256), count);
+  k_agglomerate<<<gl, 256, 0, c.stream>>>(*out);
+  return after_launch(c, "agglomerate");
 }
 
 // Directed LBVH solves of `count` directions (1, or 2 for an undirected solve)
@@ -750,6 +706,7 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
     d.pstride = pstride;
     d.rows = (packets[k] + pstride - 1) / pstride;
     d.nodes = bs.s[k].nodes;
+    d.root = bs.s[k].root;
     d.L = bs.s[k].L;
     d.sc = scalars(c, ins[k].dir);
     d.defer = (Deferred*) defer + (uint64_t) k * kDeferCap;

@@ -1,9 +1,9 @@
 // Spatial preparation shared by the LBVH and grid variants: bounding boxes,
-// cubic Morton frames, and the Morton sort of both sets into float4 (x, y, z,
-// caller index) with leaf boxes (hd_msort.cu).  Both sets are sorted in
-// shared launches; below kSplitMinPoints points they share one frame, above
-// it each set has its own.  For host inputs A is copied and sorted while B is
-// still being copied (two streams).
+// Morton codes in a cubic frame, a radix sort, and a gather into Morton
+// order as float4 (x, y, z, caller index).  Large sets run as two
+// independent chains, each set in its own frame (main stream and side
+// stream), so for host inputs A is sorted while B is still being copied;
+// small sets run one fused chain in a common frame.
 //
 // Replaces the reference's MBR reduction (src/geoms/mbr.h:307-321: thrust
 // for_each with CAS float atomics per point) and the first half of the grid
@@ -11,9 +11,12 @@
 // binary-search counting, atomic scatter): here the sort itself produces the
 // cell order, because a cubic Morton frame makes every grid level a prefix of
 // the code.
+#include <cub/device/device_radix_sort.cuh>
+
+#include <cfloat>
+
 #include "hd_common.cuh"
 #include "hd_internal.h"
-#include "hd_msort.h"
 
 namespace hdg {
 namespace {
@@ -119,6 +122,134 @@ __global__ void k_frame(const uint32_t* __restrict__ ordA, const uint32_t* __res
   fr->scale = ext > 0.0f ? (float) ((1u << bits) - 1) / ext : 0.0f;
 }
 
+// Morton codes of one set in its frame: key = code, value = row.
+template <int D>
+__global__ void k_morton1(const float* __restrict__ P, uint64_t n, const Frame* __restrict__ fr,
+                          uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const Frame f = *fr;
+  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t) gridDim.x * blockDim.x) {
+    const float x = P[i * D], y = P[i * D + 1];
+    const float z = D == 3 ? P[i * D + 2] : 0.0f;
+    keys[i] = frame_code<D>(f, x, y, z);
+    vals[i] = (uint32_t) i;
+  }
+}
+
+// Gathers one sorted set into float4 (x, y, z, caller index) and, in the
+// same pass, the bounding box of every leaf of L consecutive sorted points
+// (L a power of two <= 32; lanes of a warp cover whole leaves, reduced with
+// shuffles).
+__global__ void k_gather1(const float* __restrict__ P, uint64_t n, int dims,
+                          const uint32_t* __restrict__ order, float4* __restrict__ out, uint32_t L,
+                          float4* __restrict__ lb) {
+  const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+  for (uint64_t j0 = blockIdx.x * (uint64_t) blockDim.x + (threadIdx.x & ~31u); j0 < n; j0 += stride) {
+    const uint64_t j = j0 + (threadIdx.x & 31u);
+    const bool valid = j < n;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    float lx = FLT_MAX, ly = FLT_MAX, lz = FLT_MAX, hx = -FLT_MAX, hy = -FLT_MAX, hz = -FLT_MAX;
+    if (valid) {
+      const uint64_t r = order[j];
+      p.x = P[r * dims];
+      p.y = P[r * dims + 1];
+      p.z = dims == 3 ? P[r * dims + 2] : 0.0f;
+      p.w = __uint_as_float((uint32_t) r);
+      out[j] = p;
+      lx = hx = p.x;
+      ly = hy = p.y;
+      lz = hz = p.z;
+    }
+    for (uint32_t o = 1; o < L; o <<= 1) {
+      lx = fminf(lx, __shfl_xor_sync(0xFFFFFFFFu, lx, o));
+      ly = fminf(ly, __shfl_xor_sync(0xFFFFFFFFu, ly, o));
+      lz = fminf(lz, __shfl_xor_sync(0xFFFFFFFFu, lz, o));
+      hx = fmaxf(hx, __shfl_xor_sync(0xFFFFFFFFu, hx, o));
+      hy = fmaxf(hy, __shfl_xor_sync(0xFFFFFFFFu, hy, o));
+      hz = fmaxf(hz, __shfl_xor_sync(0xFFFFFFFFu, hz, o));
+    }
+    if (valid && (j & (L - 1)) == 0) {
+      const uint64_t leaf = j / L;
+      lb[2 * leaf] = make_float4(lx, ly, lz, 0.f);
+      lb[2 * leaf + 1] = make_float4(hx, hy, hz, 0.f);
+    }
+  }
+}
+
+// Morton codes of both sets in one launch (blockIdx.y = set); the key carries
+// the set in bit 30 so one radix sort orders A's points and then B's.
+__global__ void k_morton2(const float* __restrict__ A, uint64_t nA, const float* __restrict__ B,
+                          uint64_t nB, int dims, const Frame* __restrict__ fr,
+                          uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const float* P = blockIdx.y ? B : A;
+  const uint64_t n = blockIdx.y ? nB : nA;
+  const uint64_t base = blockIdx.y ? nA : 0;
+  const uint32_t setbit = blockIdx.y ? (1u << 30) : 0u;
+  const float lo0 = fr->lo[0], lo1 = fr->lo[1], lo2 = fr->lo[2], s = fr->scale;
+  const uint32_t maxq = (1u << fr->bits) - 1u;
+  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t) gridDim.x * blockDim.x) {
+    uint32_t code;
+    if (dims == 2) {
+      code = morton_spread2(frame_quant(P[2 * i], lo0, s, maxq)) |
+             (morton_spread2(frame_quant(P[2 * i + 1], lo1, s, maxq)) << 1);
+    } else {
+      code = morton_spread3(frame_quant(P[3 * i], lo0, s, maxq)) |
+             (morton_spread3(frame_quant(P[3 * i + 1], lo1, s, maxq)) << 1) |
+             (morton_spread3(frame_quant(P[3 * i + 2], lo2, s, maxq)) << 2);
+    }
+    keys[base + i] = code | setbit;
+    vals[base + i] = (uint32_t) (base + i);
+  }
+}
+
+// Gathers the sorted sets (blockIdx.y = set) into float4 (x, y, z, index
+// within its own set) and, in the same pass, the bounding box of every leaf
+// of L consecutive sorted points (L a power of two <= 32; lanes of a warp
+// cover whole leaves, reduced with shuffles).
+__global__ void k_gather2(const float* __restrict__ A, uint64_t nA, const float* __restrict__ B,
+                          uint64_t nB, int dims, const uint32_t* __restrict__ order,
+                          float4* __restrict__ out, uint32_t L, float4* __restrict__ leaf_boxes,
+                          uint64_t leaf_off_b) {
+  const bool setb = blockIdx.y != 0;
+  const float* P = setb ? B : A;
+  const uint64_t n = setb ? nB : nA;
+  const uint64_t base = setb ? nA : 0;
+  float4* lb = leaf_boxes + (setb ? 2 * leaf_off_b : 0);
+  const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+  for (uint64_t j0 = blockIdx.x * (uint64_t) blockDim.x + (threadIdx.x & ~31u); j0 < n; j0 += stride) {
+    const uint64_t j = j0 + (threadIdx.x & 31u);
+    const bool valid = j < n;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    float lx = FLT_MAX, ly = FLT_MAX, lz = FLT_MAX, hx = -FLT_MAX, hy = -FLT_MAX, hz = -FLT_MAX;
+    if (valid) {
+      const uint64_t v = order[base + j];
+      const uint64_t r = setb ? v - nA : v;
+      p.x = P[r * dims];
+      p.y = P[r * dims + 1];
+      p.z = dims == 3 ? P[r * dims + 2] : 0.0f;
+      p.w = __uint_as_float((uint32_t) r);
+      out[base + j] = p;
+      lx = hx = p.x;
+      ly = hy = p.y;
+      lz = hz = p.z;
+    }
+    for (uint32_t o = 1; o < L; o <<= 1) {
+      lx = fminf(lx, __shfl_xor_sync(0xFFFFFFFFu, lx, o));
+      ly = fminf(ly, __shfl_xor_sync(0xFFFFFFFFu, ly, o));
+      lz = fminf(lz, __shfl_xor_sync(0xFFFFFFFFu, lz, o));
+      hx = fmaxf(hx, __shfl_xor_sync(0xFFFFFFFFu, hx, o));
+      hy = fmaxf(hy, __shfl_xor_sync(0xFFFFFFFFu, hy, o));
+      hz = fmaxf(hz, __shfl_xor_sync(0xFFFFFFFFu, hz, o));
+    }
+    if (valid && (j & (L - 1)) == 0) {
+      const uint64_t leaf = j / L;
+      lb[2 * leaf] = make_float4(lx, ly, lz, 0.f);
+      lb[2 * leaf + 1] = make_float4(hx, hy, hz, 0.f);
+    }
+  }
+}
+
 // Stratified sample of k positions in [0, n): position i lies in stratum
 // [i*n/k, (i+1)*n/k) at an offset drawn from a counter-based hash
 // (splitmix64).  It stands in for the reference's per-sample curand draws
@@ -151,103 +282,97 @@ Frame* frame(Ctx& c, int set) {
 
 namespace {
 
-// Buffers of both sets' sorts (set 1 after set 0 in every array), allocated
-// before anything launches (an allocation may synchronise the device).
-hd_status sort_buffers(Ctx& c, const float* A, uint64_t nA, const float* B, uint64_t nB,
-                       MsortSets* ss) {
+// Scratch of both sets' sorts, allocated before either chain launches (an
+// allocation may synchronise the device).  Set 1 uses the upper halves.
+struct SortScratch {
+  uint32_t *keys, *keys2, *vals, *vals2;
+  unsigned char* tmp;
+  size_t tmp_bytes, tmp_stride;
+  float4* pts;
+  float4* lboxes;
+  uint64_t nA, leaves_a;
+  uint32_t L;
+};
+
+hd_status sort_scratch(Ctx& c, uint64_t nA, uint64_t nB, bool fused, SortScratch* x) {
   const uint64_t n = nA + nB;
   uint32_t L = c.opt.leaf_size ? std::min<uint32_t>(c.opt.leaf_size, 32) : 16;
   while (L & (L - 1)) L &= L - 1;
-  const uint64_t ns[2] = {nA, nB};
-  uint32_t shift[2], nbins[2], caps[2];
-  uint64_t leaves[2];
-  for (int k = 0; k < 2; ++k) {
-    shift[k] = msort_shift(ns[k]);
-    nbins[k] = 1u << (30 - shift[k]);
-    caps[k] = (uint32_t) (ns[k] / 33 + 2);
-    leaves[k] = (ns[k] + L - 1) / L;
-  }
+  const uint64_t leaves_a = (nA + L - 1) / L, leaves_b = (nB + L - 1) / L;
   hd_status s;
-  void *pts, *codes, *tpts, *tcodes, *bins, *aux, *lboxes;
+  void *keys, *keys2, *vals, *vals2, *tmp, *pts, *lboxes;
+  if ((s = ensure(c, kBufKeys, n * 4, &keys)) != HD_OK) return s;
+  if ((s = ensure(c, kBufKeysAlt, n * 4, &keys2)) != HD_OK) return s;
+  if ((s = ensure(c, kBufVals, n * 4, &vals)) != HD_OK) return s;
+  if ((s = ensure(c, kBufValsAlt, n * 4, &vals2)) != HD_OK) return s;
   if ((s = ensure(c, kBufSorted0, n * sizeof(float4), &pts)) != HD_OK) return s;
-  if ((s = ensure(c, kBufKeys, n * 4, &codes)) != HD_OK) return s;
-  if ((s = ensure(c, kBufSorted1, n * sizeof(float4), &tpts)) != HD_OK) return s;
-  if ((s = ensure(c, kBufKeysAlt, n * 4, &tcodes)) != HD_OK) return s;
-  if ((s = ensure(c, kBufVals, ((uint64_t) nbins[0] + nbins[1]) * 4, &bins)) != HD_OK) return s;
-  const uint64_t tiles = 1024 + 1;
-  const uint64_t aux_words = 2 * tiles + 2 * ((uint64_t) caps[0] + caps[1]) + 8;
-  if ((s = ensure(c, kBufValsAlt, aux_words * 4, &aux)) != HD_OK) return s;
-  if ((s = ensure(c, kBufCodes0, (leaves[0] + leaves[1]) * 2 * sizeof(float4), &lboxes)) != HD_OK)
+  if ((s = ensure(c, kBufCodes0, (leaves_a + leaves_b) * 2 * sizeof(float4), &lboxes)) != HD_OK)
     return s;
-  uint32_t* w = (uint32_t*) aux;
-  uint32_t* counters = w;  // 4 words per set
-  w += 8;
-  uint64_t off = 0, boff = 0, loff = 0;
-  const float* P[2] = {A, B};
-  for (int k = 0; k < 2; ++k) {
-    MsortSet& m = ss->s[k];
-    m.P = P[k];
-    m.n = ns[k];
-    m.fr = frame(c, k);
-    m.shift = shift[k];
-    m.nbins = nbins[k];
-    m.bins = (uint32_t*) bins + boff;
-    m.tile_sums = w;
-    w += tiles;
-    m.pts = (float4*) pts + off;
-    m.codes = (uint32_t*) codes + off;
-    m.tpts = (float4*) tpts + off;
-    m.tcodes = (uint32_t*) tcodes + off;
-    m.mid_list = w;
-    w += caps[k];
-    m.big_list = w;
-    w += caps[k];
-    m.counters = counters + 4 * k;
-    m.status = &scalars(c, 0)->status;
-    m.list_cap = caps[k];
-    m.L = L;
-    m.leaf_boxes = (float4*) lboxes + 2 * loff;
-    off += ns[k];
-    boff += nbins[k];
-    loff += leaves[k];
-  }
+  // Fused: one sort of both sets (set in bit 30); else one sort per set,
+  // each with its own temporary region.
+  size_t tmp_bytes = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, (const uint32_t*) keys, (uint32_t*) keys2,
+                                  (const uint32_t*) vals, (uint32_t*) vals2,
+                                  (int64_t) (fused ? n : std::max(nA, nB)),
+                                  fused ? 0 : kSortLowBits, fused ? 31 : 30, c.stream);
+  const size_t stride = (tmp_bytes + 255) & ~(size_t) 255;
+  if ((s = ensure(c, kBufCubTemp, (fused ? 1 : 2) * stride, &tmp)) != HD_OK) return s;
+  *x = SortScratch{(uint32_t*) keys, (uint32_t*) keys2, (uint32_t*) vals, (uint32_t*) vals2,
+                   (unsigned char*) tmp, tmp_bytes, stride, (float4*) pts, (float4*) lboxes,
+                   nA, leaves_a, L};
   return HD_OK;
 }
 
-SortedSet sorted_of(const MsortSet& m, int dims) {
-  SortedSet o;
-  o.pts = m.pts;
-  o.codes = m.codes;
-  o.frame = m.fr;
-  o.leaf_boxes = m.leaf_boxes;
-  o.leaf_size = m.L;
-  o.n = m.n;
-  o.dims = dims;
-  o.src = m.P;
-  return o;
-}
-
-// Bounding box and frame of set k on stream st (its own frame).
-hd_status frame_one(Ctx& c, int k, const float* P, uint64_t n, int dims, cudaStream_t st) {
+// Sorts set k (0 = the call's A, 1 = its B) on stream st: bounding box, its
+// frame, Morton codes, radix sort, gather with leaf boxes.
+hd_status sort_set(Ctx& c, int k, const float* P, uint64_t n, int dims, const SortScratch& x,
+                   cudaStream_t st, SortedSet* out) {
   hd_status s;
+  const uint64_t base = k ? x.nA : 0;
   uint32_t* ord = &scalars(c, 0)->mbr_ord[k][0][0];
-  const int gx = grid_for(c, (n + 3) / 4, 256);
-  k_mbr2<<<dim3(gx, 1), 256, 0, st>>>(P, n, P, n, dims, ord, ord);
-  if ((s = after_launch(c, "mbr")) != HD_OK) return s;
-  k_frame<<<1, 32, 0, st>>>(ord, ord, dims, 1, 0, frame(c, k));
-  return after_launch(c, "frame");
+  Frame* fr = frame(c, k);
+  {
+    const int gx = grid_for(c, (n + 3) / 4, 256);
+    k_mbr2<<<dim3(gx, 1), 256, 0, st>>>(P, n, P, n, dims, ord, ord);
+    if ((s = after_launch(c, "mbr")) != HD_OK) return s;
+  }
+  k_frame<<<1, 32, 0, st>>>(ord, ord, dims, 1, 0, fr);
+  if ((s = after_launch(c, "frame")) != HD_OK) return s;
+  if (dims == 2)
+    k_morton1<2><<<grid_for(c, n), 256, 0, st>>>(P, n, fr, x.keys + base, x.vals + base);
+  else
+    k_morton1<3><<<grid_for(c, n), 256, 0, st>>>(P, n, fr, x.keys + base, x.vals + base);
+  if ((s = after_launch(c, "morton")) != HD_OK) return s;
+  size_t tb = x.tmp_bytes;
+  cudaError_t e = cub::DeviceRadixSort::SortPairs(
+      x.tmp + (size_t) k * x.tmp_stride, tb, (const uint32_t*) x.keys + base, x.keys2 + base,
+      (const uint32_t*) x.vals + base, x.vals2 + base, (int64_t) n, kSortLowBits, 30, st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "radix sort");
+  float4* lb = x.lboxes + (k ? 2 * x.leaves_a : 0);
+  k_gather1<<<grid_for(c, n), 256, 0, st>>>(P, n, dims, x.vals2 + base, x.pts + base, x.L, lb);
+  if ((s = after_launch(c, "gather")) != HD_OK) return s;
+  SortedSet& o = *out;
+  o.pts = x.pts + base;
+  o.codes = x.keys2 + base;
+  o.frame = fr;
+  o.leaf_boxes = lb;
+  o.leaf_size = x.L;
+  o.n = n;
+  o.dims = dims;
+  o.src = P;
+  return HD_OK;
 }
 
 }  // namespace
 
-// Sorts both sets in shared launches.  Below kSplitMinPoints points the two
-// sets share one cubic frame (a query set's Morton order then matches the
-// target's exactly); from there on each set has its own frame.
-static hd_status spatial_sort(Ctx& c, const float* A, uint64_t nA, const float* B, uint64_t nB,
-                              int dims, SortedSet* sa, SortedSet* sb) {
+// Small sets: one fused chain (both boxes, one common frame, both sets'
+// codes, one sort with the set in bit 30, both gathers), so a query set's
+// Morton order matches the target's exactly and the launches are few.
+static hd_status spatial_sort_fused(Ctx& c, const float* A, uint64_t nA, const float* B,
+                                    uint64_t nB, int dims, SortedSet* sa, SortedSet* sb) {
   hd_status s;
-  MsortSets ss;
-  if ((s = sort_buffers(c, A, nA, B, nB, &ss)) != HD_OK) return s;
+  SortScratch x;
+  if ((s = sort_scratch(c, nA, nB, true, &x)) != HD_OK) return s;
   DevScalars* sc = scalars(c, 0);
   {
     const int gx = grid_for(c, (std::max(nA, nB) + 3) / 4, 256);
@@ -255,21 +380,45 @@ static hd_status spatial_sort(Ctx& c, const float* A, uint64_t nA, const float* 
                                               &sc->mbr_ord[1][0][0]);
     if ((s = after_launch(c, "mbr")) != HD_OK) return s;
   }
-  if (nA + nB < kSplitMinPoints) {
-    k_frame<<<1, 32, 0, c.stream>>>(&sc->mbr_ord[0][0][0], &sc->mbr_ord[1][0][0], dims, 1, 1,
-                                    frame(c, 0));
-    if ((s = after_launch(c, "frame")) != HD_OK) return s;
-    ss.s[1].fr = frame(c, 0);
-  } else {
-    for (int k = 0; k < 2; ++k) {
-      k_frame<<<1, 32, 0, c.stream>>>(&sc->mbr_ord[k][0][0], &sc->mbr_ord[k][0][0], dims, 1, 0,
-                                      frame(c, k));
-      if ((s = after_launch(c, "frame")) != HD_OK) return s;
-    }
+  Frame* fr = frame(c, 0);
+  k_frame<<<1, 32, 0, c.stream>>>(&sc->mbr_ord[0][0][0], &sc->mbr_ord[1][0][0], dims, 1, 1, fr);
+  if ((s = after_launch(c, "frame")) != HD_OK) return s;
+  {
+    const int gx = grid_for(c, std::max(nA, nB));
+    k_morton2<<<dim3(gx, 2), 256, 0, c.stream>>>(A, nA, B, nB, dims, fr, x.keys, x.vals);
+    if ((s = after_launch(c, "morton")) != HD_OK) return s;
   }
-  if ((s = msort_run(c, ss, 2, dims, c.stream)) != HD_OK) return s;
-  *sa = sorted_of(ss.s[0], dims);
-  *sb = sorted_of(ss.s[1], dims);
+  size_t tb = x.tmp_bytes;
+  cudaError_t e = cub::DeviceRadixSort::SortPairs(x.tmp, tb, (const uint32_t*) x.keys, x.keys2,
+                                                  (const uint32_t*) x.vals, x.vals2,
+                                                  (int64_t) (nA + nB), 0, 31, c.stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "radix sort");
+  k_gather2<<<dim3(grid_for(c, std::max(nA, nB)), 2), 256, 0, c.stream>>>(
+      A, nA, B, nB, dims, x.vals2, x.pts, x.L, x.lboxes, x.leaves_a);
+  if ((s = after_launch(c, "gather")) != HD_OK) return s;
+  *sa = SortedSet{x.pts, x.keys2, fr, x.lboxes, x.L, nA, dims, A};
+  *sb = SortedSet{x.pts + nA, x.keys2 + nA, fr, x.lboxes + 2 * x.leaves_a, x.L, nB, dims, B};
+  return HD_OK;
+}
+
+// Large sets: A's chain (own frame) on the main stream, B's on the side
+// stream, joined before anything reads the sorted sets.
+static hd_status spatial_sort(Ctx& c, const float* A, uint64_t nA, const float* B,
+                              uint64_t nB, int dims, SortedSet* sa, SortedSet* sb) {
+  if (nA + nB < kSplitMinPoints) return spatial_sort_fused(c, A, nA, B, nB, dims, sa, sb);
+  hd_status s;
+  SortScratch x;
+  if ((s = sort_scratch(c, nA, nB, false, &x)) != HD_OK) return s;
+  if ((s = ensure_side(c)) != HD_OK) return s;
+  cudaError_t e;
+  if ((e = cudaEventRecord(c.batch_fork, c.stream)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(c.batch_side, c.batch_fork, 0)) != cudaSuccess)
+    return cuda_fail(c, e, "fork");
+  if ((s = sort_set(c, 0, A, nA, dims, x, c.stream, sa)) != HD_OK) return s;
+  if ((s = sort_set(c, 1, B, nB, dims, x, c.batch_side, sb)) != HD_OK) return s;
+  if ((e = cudaEventRecord(c.batch_join, c.batch_side)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(c.stream, c.batch_join, 0)) != cudaSuccess)
+    return cuda_fail(c, e, "join");
   return HD_OK;
 }
 
@@ -279,33 +428,28 @@ hd_status spatial_upload_sort(Ctx& c, const float* hA, uint64_t nA, const float*
   void *pa, *pb;
   if ((s = ensure(c, kBufA, (size_t) nA * dims * sizeof(float), &pa)) != HD_OK) return s;
   if ((s = ensure(c, kBufB, (size_t) nB * dims * sizeof(float), &pb)) != HD_OK) return s;
-  MsortSets ss;
-  if ((s = sort_buffers(c, (const float*) pa, nA, (const float*) pb, nB, &ss)) != HD_OK) return s;
+  SortScratch x;
+  if ((s = sort_scratch(c, nA, nB, false, &x)) != HD_OK) return s;
   if ((s = ensure_side(c)) != HD_OK) return s;
   cudaError_t e;
   // A's copy first, alone on the link; B's copy starts when it is done and
-  // runs beside A's sort (each set in its own frame).
+  // runs beside A's sort.
   if ((e = cudaMemcpyAsync(pa, hA, (size_t) nA * dims * sizeof(float), cudaMemcpyHostToDevice,
                            c.stream)) != cudaSuccess)
     return cuda_fail(c, e, "copy inputs to device");
   if ((e = cudaEventRecord(c.batch_fork, c.stream)) != cudaSuccess ||
       (e = cudaStreamWaitEvent(c.batch_side, c.batch_fork, 0)) != cudaSuccess)
     return cuda_fail(c, e, "fork");
-  MsortSets one;
-  one.s[0] = ss.s[0];
-  if ((s = frame_one(c, 0, (const float*) pa, nA, dims, c.stream)) != HD_OK) return s;
-  if ((s = msort_run(c, one, 1, dims, c.stream)) != HD_OK) return s;
+  if ((s = sort_set(c, 0, (const float*) pa, nA, dims, x, c.stream, &c.sorted[0])) != HD_OK)
+    return s;
   if ((e = cudaMemcpyAsync(pb, hB, (size_t) nB * dims * sizeof(float), cudaMemcpyHostToDevice,
                            c.batch_side)) != cudaSuccess)
     return cuda_fail(c, e, "copy inputs to device");
-  one.s[0] = ss.s[1];
-  if ((s = frame_one(c, 1, (const float*) pb, nB, dims, c.batch_side)) != HD_OK) return s;
-  if ((s = msort_run(c, one, 1, dims, c.batch_side)) != HD_OK) return s;
+  if ((s = sort_set(c, 1, (const float*) pb, nB, dims, x, c.batch_side, &c.sorted[1])) != HD_OK)
+    return s;
   if ((e = cudaEventRecord(c.batch_join, c.batch_side)) != cudaSuccess ||
       (e = cudaStreamWaitEvent(c.stream, c.batch_join, 0)) != cudaSuccess)
     return cuda_fail(c, e, "join");
-  c.sorted[0] = sorted_of(ss.s[0], dims);
-  c.sorted[1] = sorted_of(ss.s[1], dims);
   c.sorted_valid = true;
   *dA = (const float*) pa;
   *dB = (const float*) pb;
