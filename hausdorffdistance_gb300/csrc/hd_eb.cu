@@ -21,14 +21,14 @@
 //    those points are deferred too and the CTA retires.  Because
 //    B's visit order is a pseudo-random permutation, a slot may start at any
 //    tile and wrap around: no slot waits for a CTA-wide restart.
-//  * Deferred ("heavy") points — the ones whose nearest neighbour is farther
-//    than the running maximum — are finished by k_eb_heavy, one point per CTA
-//    with all 256 threads over B, the block-per-point shape of the reference
-//    but with a CTA reduction only every 32 tiles.  The same kernel seeds the
-//    running maximum with the first 152 visited points before the main pass,
-//    which keeps the main pass from starting with a zero threshold (the
-//    reference's hybrid seeds it with an MBR lower bound and a sample,
-//    hybrid.h:111-142).
+//  * Deferred points — the ones whose nearest neighbour is farther than the
+//    running maximum — and the seeds that start the maximum (the first 152
+//    visited points, before the main pass, so that it never starts from a
+//    zero threshold; the reference's hybrid seeds it with an MBR lower bound
+//    and a sample, hybrid.h:111-142) are finished by the tile-wise list
+//    scan k_eb_list: groups of up to 256 points against chunks of B's tiles
+//    staged in shared memory; a group raises the running maximum as soon as
+//    its last chunk is done, so later groups break early.
 //  * The running maximum is one 64-bit word (squared-distance bits, ~index):
 //    a single atomicMax on the bit pattern — no CAS loop — which also keeps
 //    the certifying A index.
@@ -46,9 +46,9 @@ namespace {
 constexpr int kEbThreads = 256;
 constexpr int kEbTile = 256;          // B points per tile (== kEbThreads)
 constexpr int kEbSlots = 4;           // A points carried per thread
-constexpr int kHeavyStepTiles = 32;   // tiles between CTA reductions (heavy)
 constexpr uint32_t kCapPairs = 8192;  // per-point pairs before deferral (no-alloc entry point)
 constexpr uint32_t kWaitLimit = 1u << 26;
+constexpr uint32_t kListChunks = 64;  // B chunks per group in the list scan, at least
 
 template <int D>
 struct EbPt;
@@ -284,96 +284,158 @@ __global__ void __launch_bounds__(kEbThreads)
   if (pairs) atomicAdd(&sc->pairs, pairs);
 }
 
-// One A point per CTA, all threads over B.  list == nullptr: seed mode, the
-// entries are the first n visit positions.  Every point scans the whole ring
-// of B's tiles (a deferred point keeps the running minimum of its main-pass
-// tiles, and scanning those few tiles again costs next to nothing), starting
-// where the CTA's previous point stopped: all CTAs sweep B from tile 0 in the
-// same direction at about the same pace, so the tiles they read are shared
-// through L2 instead of each point streaming B from its own offset in HBM.
+// Points finished outside the persistent pass — the seeds that start the
+// running maximum, and the points deferred past the pair cap (the far ones
+// that decide the distance) — are scanned tile-wise: a work item is a group
+// of up to 256 listed points (one per thread) against one chunk of B's
+// tiles, streamed through a shared-memory double buffer with the TMA bulk
+// copy as in k_eb_main, so every B point loaded serves 256 pairs.  A point's
+// minimum over its chunks is combined with an atomicMin on the float's bits
+// (non-negative floats order as their bit patterns).  Items are taken group
+// by group, and the CTA that completes a group's last chunk raises the
+// running maximum with that group's points at once: the maximum climbs while
+// later groups are still scanning, so their points stop early, as the
+// reference's early break does (early_break.h:76).  An item stops once every
+// point of its group is at or below the running maximum: such a point cannot
+// raise it, and the partial minimum it records is at or below it too.
 template <int D>
 __global__ void __launch_bounds__(kEbThreads)
-    k_eb_heavy(const float* __restrict__ A, Perm permA,
-               const typename EbPt<D>::T* __restrict__ Bp, uint32_t nTiles,
-               DevScalars* sc, const HeavyEntry* __restrict__ list,
-               uint32_t n_host, const uint32_t* n_dev) {
-  __shared__ float red[kEbThreads / 32];
-  __shared__ float s_thr;
+    k_eb_list(const float* __restrict__ A, const typename EbPt<D>::T* __restrict__ Bp,
+              uint32_t nTiles, HeavyEntry* list, uint32_t* group_done, uint32_t n_host,
+              const uint32_t* n_dev, uint32_t cap, DevScalars* sc) {
+  using PT = typename EbPt<D>::T;
+  constexpr uint32_t kTileBytes = kEbTile * sizeof(PT);
+  __shared__ __align__(128) PT tile[2][kEbTile];
+  __shared__ __align__(8) uint64_t full[2];
+  __shared__ bool s_last;
   const int tid = threadIdx.x;
-  const uint32_t n = n_dev ? *n_dev : n_host;
-  unsigned long long pairs = 0;
-  uint32_t sweep = 0;  // this CTA's position in B's tile ring
-  for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
-    HeavyEntry h;
-    if (list) {
-      h = list[e];
-    } else {
-      h = HeavyEntry{(uint32_t) permA(e), 0u, nTiles, FLT_MAX};
-    }
-    float ax, ay, az;
-    load_a<D>(A, h.ia, ax, ay, az);
-    float m = FLT_MAX;
-    float cmin = h.cmin;
-    uint32_t done = 0;
-    uint32_t t = sweep;
-    bool broke = false;
-    while (done < nTiles) {
-      uint32_t step = min((uint32_t) kHeavyStepTiles, nTiles - done);
-      // The round's tiles are t .. t+step-1 around the ring: at most two
-      // contiguous runs, each walked with one pointer (fixed load offsets,
-      // groups of 8 loads issued before any is used).
-      for (uint32_t k = 0; k < step;) {
-        const uint32_t run = min(step - k, nTiles - t);
-        const typename EbPt<D>::T* p = Bp + (uint64_t) t * kEbTile + tid;
-        uint32_t u = 0;
-        for (; u + 8 <= run; u += 8, p += 8 * kEbTile) {
-          typename EbPt<D>::T b[8];
-#pragma unroll
-          for (int v = 0; v < 8; ++v) b[v] = p[v * kEbTile];
-#pragma unroll
-          for (int v = 0; v < 8; ++v) {
-            if constexpr (D == 2)
-              m = fminf(m, d2_2(ax, ay, b[v].x, b[v].y));
-            else
-              m = fminf(m, d2_3(ax, ay, az, b[v].x, b[v].y, b[v].z));
-          }
-        }
-        for (; u < run; ++u, p += kEbTile) {
-          const auto b = *p;
-          if constexpr (D == 2)
-            m = fminf(m, d2_2(ax, ay, b.x, b.y));
-          else
-            m = fminf(m, d2_3(ax, ay, az, b.x, b.y, b.z));
-        }
-        k += run;
-        t += run;
-        if (t == nTiles) t = 0;
-      }
-      done += step;
-      pairs += step;
-      float w = m;
-#pragma unroll
-      for (int o = 16; o; o >>= 1) w = fminf(w, __shfl_xor_sync(0xFFFFFFFFu, w, o));
-      if ((tid & 31) == 0) red[tid >> 5] = w;
-      // One thread reads the shared maximum so that every thread of the CTA
-      // takes the same break decision.
-      if (tid == 0) s_thr = threshold_of(ld_relaxed_u64(&sc->max_key));
-      __syncthreads();
-      float bm = red[0];
-#pragma unroll
-      for (int k = 1; k < kEbThreads / 32; ++k) bm = fminf(bm, red[k]);
-      cmin = fminf(cmin, bm);
-      const float thr = s_thr;
-      __syncthreads();
-      if (cmin <= thr) {
-        broke = true;
-        break;
-      }
-    }
-    if (!broke && tid == 0) atomicMax(&sc->max_key, pack_max(cmin, h.ia));
-    sweep = t;
+  const uint32_t n = n_dev ? min(*n_dev, cap) : n_host;
+  if (n == 0) return;
+  const uint32_t groups = (n + kEbThreads - 1) / kEbThreads;
+  // At least kListChunks chunks per group, so that the CTAs running at one
+  // time share a few groups (B chunks reused through L2, groups completing
+  // one after another); more when there are few groups.
+  const uint32_t chunks =
+      max(1u, min(nTiles, max(kListChunks, (2 * gridDim.x + groups - 1) / groups)));
+  const uint32_t items = groups * chunks;
+  if (tid == 0) {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    fence_barrier_init();
   }
-  if (tid == 0 && pairs) atomicAdd(&sc->pairs, pairs * kEbTile);
+  __syncthreads();
+  uint32_t it = 0;  // tiles this CTA has consumed (buffer it & 1, parity (it >> 1) & 1)
+  unsigned long long pairs = 0;
+  for (uint32_t w = blockIdx.x; w < items; w += gridDim.x) {
+    const uint32_t group = w / chunks, chunk = w - group * chunks;
+    const uint32_t t0 = (uint32_t) (((uint64_t) chunk * nTiles) / chunks);
+    const uint32_t t1 = (uint32_t) (((uint64_t) (chunk + 1) * nTiles) / chunks);
+    const uint32_t e = group * kEbThreads + tid;
+    float ax = 0.f, ay = 0.f, az = 0.f, m = FLT_MAX;
+    uint32_t ia = 0;
+    if (e < n) {
+      const HeavyEntry h = list[e];
+      load_a<D>(A, h.ia, ax, ay, az);
+      m = h.cmin;
+      ia = h.ia;
+    }
+    unsigned long long key = 0;
+    if ((tid & 31) == 0) key = ld_relaxed_u64(&sc->max_key);
+    key = __shfl_sync(0xFFFFFFFFu, key, 0);
+    bool act = e < n && m > threshold_of(key);
+    if (__syncthreads_or(act)) {
+      if (tid == 0) {
+        mbar_expect_tx(&full[it & 1], kTileBytes);
+        tma_load_1d(&tile[it & 1][0], Bp + (uint64_t) t0 * kEbTile, kTileBytes, &full[it & 1]);
+      }
+      for (uint32_t t = t0;;) {
+        const int buf = it & 1;
+        const bool more = t + 1 < t1;
+        if (tid == 0 && more) {
+          // Buffer buf^1 was released by every thread at the end of the
+          // last tile (the barrier below).
+          mbar_expect_tx(&full[buf ^ 1], kTileBytes);
+          tma_load_1d(&tile[buf ^ 1][0], Bp + (uint64_t) (t + 1) * kEbTile, kTileBytes,
+                      &full[buf ^ 1]);
+        }
+        const bool ok = mbar_wait(&full[buf], (it >> 1) & 1, &sc->status, kWaitLimit);
+        if (__syncthreads_or(!ok)) {
+          // A copy did not arrive in time: the status bit fails the solve.
+          if (pairs) atomicAdd(&sc->pairs, pairs);
+          return;
+        }
+        if (act) {
+          if constexpr (D == 2) {
+            const float4* t4 = reinterpret_cast<const float4*>(&tile[buf][0]);
+#pragma unroll 8
+            for (int p = 0; p < kEbTile / 2; ++p) {
+              const float4 b = t4[p];
+              m = fminf(m, d2_2(ax, ay, b.x, b.y));
+              m = fminf(m, d2_2(ax, ay, b.z, b.w));
+            }
+          } else {
+#pragma unroll 8
+            for (int p = 0; p < kEbTile; ++p) {
+              const float4 b = tile[buf][p];
+              m = fminf(m, d2_3(ax, ay, az, b.x, b.y, b.z));
+            }
+          }
+          pairs += kEbTile;
+        }
+        ++it;
+        ++t;
+        if ((tid & 31) == 0) key = ld_relaxed_u64(&sc->max_key);
+        key = __shfl_sync(0xFFFFFFFFu, key, 0);
+        if (act && m <= threshold_of(key)) act = false;
+        const bool any = __syncthreads_or(act);
+        if (!more) break;
+        if (!any) {
+          // Early break of the whole group: drain the prefetch in flight.
+          if (tid == 0) mbar_wait(&full[it & 1], (it >> 1) & 1, &sc->status, kWaitLimit);
+          ++it;
+          __syncthreads();
+          break;
+        }
+      }
+    }
+    if (e < n) atomicMin(reinterpret_cast<unsigned int*>(&list[e].cmin), __float_as_uint(m));
+    // The CTA completing the group's last chunk raises the maximum with the
+    // group's points whose minimum over all of B stayed above it.
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&group_done[group], 1u) == chunks - 1;
+    __syncthreads();
+    if (s_last && e < n) {
+      __threadfence();
+      const float gm = __uint_as_float(__ldcg(reinterpret_cast<const unsigned int*>(&list[e].cmin)));
+      if (gm > threshold_of(ld_relaxed_u64(&sc->max_key)))
+        atomicMax(&sc->max_key, pack_max(gm, ia));
+    }
+  }
+  if (pairs) atomicAdd(&sc->pairs, pairs);
+}
+
+// The seed list: the first n visit positions of A, nothing scanned yet.
+__global__ void k_eb_seed_list(Perm permA, uint32_t n, uint32_t nTiles, HeavyEntry* list) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) list[e] = HeavyEntry{(uint32_t) permA(e), 0u, nTiles, FLT_MAX};
+}
+
+// Seeds, or the deferred points, through the tile-wise list scan
+// (stream-level, shared by the context path and the allocation-free entry
+// point).  n_dev: device count of listed points (deferred points), or null
+// with n_host (seeds).  group_done: one zeroed counter per group of 256 list
+// entries (cap / 256 + 1 words).
+template <int D>
+cudaError_t eb_list_pass(cudaStream_t st, int num_sms, const float* A,
+                         const typename EbPt<D>::T* Bp, uint32_t nTiles, HeavyEntry* list,
+                         uint32_t* group_done, uint32_t n_host, const uint32_t* n_dev,
+                         uint32_t cap, DevScalars* sc) {
+  cudaError_t e = cudaMemsetAsync(group_done, 0, ((size_t) cap / kEbThreads + 1) * 4, st);
+  if (e != cudaSuccess) return e;
+  k_eb_list<D><<<num_sms * 4, kEbThreads, 0, st>>>(A, Bp, nTiles, list, group_done, n_host, n_dev,
+                                                   cap, sc);
+  return cudaGetLastError();
 }
 
 template <int D>
@@ -386,7 +448,11 @@ hd_status run_eb_dim(Ctx& c, const DirInput& in) {
   void *pb = nullptr, *ph = nullptr;
   hd_status s;
   if ((s = ensure(c, kBufPackB, nPad * sizeof(PT), &pb)) != HD_OK) return s;
-  if ((s = ensure(c, kBufHeavy, in.nA * sizeof(HeavyEntry), &ph)) != HD_OK) return s;
+  // The point list, then one completion counter per group of 256 entries.
+  if ((s = ensure(c, kBufHeavy, in.nA * sizeof(HeavyEntry) + (in.nA / kEbThreads + 1) * 4, &ph)) !=
+      HD_OK)
+    return s;
+  uint32_t* group_done = (uint32_t*) ((HeavyEntry*) ph + in.nA);
   DevScalars* sc = scalars(c, in.dir);
   const uint64_t seed = c.opt.seed;
   Perm pB{in.nB, pick_multiplier(in.nB, seed + 1), (seed * 7919u) % in.nB};
@@ -399,12 +465,19 @@ hd_status run_eb_dim(Ctx& c, const DirInput& in) {
   }
   mark(c, 1);
   mark(c, 2);
-  // Seeds: the first visited A points, one CTA each, no early break until a
-  // first point completes.
+  // Seeds: the first visited A points, scanned in full (the running maximum
+  // is still zero) by the tile-wise list pass.  Their list entries sit at the
+  // end of the deferred-point list, which the main pass fills from the start.
   const uint32_t n_seed = (uint32_t) std::min<uint64_t>(in.nA, (uint64_t) c.num_sms);
-  k_eb_heavy<D><<<n_seed, kEbThreads, 0, c.stream>>>(in.A, pA, (const PT*) pb, nTiles,
-                                                     sc, nullptr, n_seed, nullptr);
-  if ((s = after_launch(c, "eb_seed")) != HD_OK) return s;
+  HeavyEntry* seeds = (HeavyEntry*) ph + (in.nA - n_seed);
+  k_eb_seed_list<<<(n_seed + 255) / 256, 256, 0, c.stream>>>(pA, n_seed, nTiles, seeds);
+  if ((s = after_launch(c, "eb_seed_list")) != HD_OK) return s;
+  {
+    cudaError_t e = eb_list_pass<D>(c.stream, c.num_sms, in.A, (const PT*) pb, nTiles, seeds,
+                                    group_done, n_seed, nullptr, n_seed, sc);
+    c.launches += 1;
+    if (e != cudaSuccess) return cuda_fail(c, e, "eb_seed");
+  }
   mark(c, 3);
   if (in.nA > n_seed) {
     // Slots per thread: the most (4, 2, 1) that still fill every resident CTA
@@ -439,16 +512,18 @@ hd_status run_eb_dim(Ctx& c, const DirInput& in) {
     const float* a_ptr = in.A;
     const PT* b_ptr = (const PT*) pb;
     HeavyEntry* h_ptr = (HeavyEntry*) ph;
-    uint32_t heavy_cap = (uint32_t) in.nA;
+    uint32_t heavy_cap = (uint32_t) (in.nA - n_seed);
     uint64_t a_begin = n_seed, a_end = in.nA;
     void* args[] = {&a_ptr, &pA, &a_begin, &a_end, &b_ptr, (void*) &nTiles, &capTiles, &sc,
                     &h_ptr, &heavy_cap};
     cudaLaunchKernel(fns[pick], dim3(grid), dim3(kEbThreads), args, 0, c.stream);
     if ((s = after_launch(c, "eb_main")) != HD_OK) return s;
     mark(c, 4);
-    k_eb_heavy<D><<<c.num_sms * 4, kEbThreads, 0, c.stream>>>(
-        in.A, pA, (const PT*) pb, nTiles, sc, (const HeavyEntry*) ph, 0, &sc->heavy_count);
-    if ((s = after_launch(c, "eb_heavy")) != HD_OK) return s;
+    cudaError_t e = eb_list_pass<D>(c.stream, c.num_sms, in.A, (const PT*) pb, nTiles,
+                                    (HeavyEntry*) ph, group_done, 0, &sc->heavy_count, heavy_cap,
+                                    sc);
+    c.launches += 1;
+    if (e != cudaSuccess) return cuda_fail(c, e, "eb_deferred");
   } else {
     mark(c, 4);
   }
@@ -487,7 +562,9 @@ constexpr uint64_t kNoAllocMaxPoints = 1ull << 20;
 constexpr size_t kNoAllocScalarBytes = 1024;  // two DevScalars, padded
 constexpr size_t kNoAllocHeavyBytes = kNoAllocMaxPoints * sizeof(HeavyEntry);
 constexpr size_t kNoAllocPackBytes = kNoAllocMaxPoints * sizeof(float4);
-constexpr size_t kNoAllocBytes = kNoAllocScalarBytes + kNoAllocHeavyBytes + kNoAllocPackBytes;
+constexpr size_t kNoAllocGroupBytes = (kNoAllocMaxPoints / kEbThreads + 1) * 4;  // list groups
+constexpr size_t kNoAllocBytes =
+    kNoAllocScalarBytes + kNoAllocHeavyBytes + kNoAllocPackBytes + kNoAllocGroupBytes;
 static_assert(2 * sizeof(DevScalars) <= kNoAllocScalarBytes, "scalar area too small");
 
 // In host code this name is only a host-side stand-in for the symbol: its
@@ -516,6 +593,8 @@ cudaError_t noalloc_direction(cudaStream_t st, int num_sms, const float* A, uint
   const uint64_t nPad = (uint64_t) nTiles * kEbTile;
   HeavyEntry* heavy = (HeavyEntry*) (base + kNoAllocScalarBytes);
   PT* pb = (PT*) (base + kNoAllocScalarBytes + kNoAllocHeavyBytes);
+  uint32_t* group_done =
+      (uint32_t*) (base + kNoAllocScalarBytes + kNoAllocHeavyBytes + kNoAllocPackBytes);
   Perm pB{nB, pick_multiplier(nB, 1), 0};
   Perm pA{nA, pick_multiplier(nA, 2), 0};
   int grid = (int) std::min<uint64_t>((nPad + 255) / 256, (uint64_t) num_sms * 16);
@@ -523,8 +602,12 @@ cudaError_t noalloc_direction(cudaStream_t st, int num_sms, const float* A, uint
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const uint32_t n_seed = (uint32_t) std::min<uint64_t>(nA, (uint64_t) num_sms);
-  k_eb_heavy<D><<<n_seed, kEbThreads, 0, st>>>(A, pA, pb, nTiles, sc, nullptr, n_seed, nullptr);
+  HeavyEntry* seeds = heavy + (nA - n_seed);
+  k_eb_seed_list<<<(n_seed + 255) / 256, 256, 0, st>>>(pA, n_seed, nTiles, seeds);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = eb_list_pass<D>(st, num_sms, A, pb, nTiles, seeds, group_done, n_seed, nullptr, n_seed,
+                           sc)) != cudaSuccess)
+    return e;
   if (nA > n_seed) {
     // Slots per thread chosen as hd_solve's EB variant chooses them: the most
     // (4, 2, 1) that still fill every resident CTA of a full grid.
@@ -549,15 +632,15 @@ cudaError_t noalloc_direction(cudaStream_t st, int num_sms, const float* A, uint
     uint32_t capTiles = std::max<uint32_t>(1, kCapPairs / kEbTile);
     const float* a_ptr = A;
     const PT* b_ptr = pb;
-    uint32_t heavy_cap = (uint32_t) kNoAllocMaxPoints;
+    uint32_t heavy_cap = (uint32_t) (nA - n_seed);
     uint64_t a_begin = n_seed, a_end = nA;
     void* args[] = {&a_ptr, &pA, &a_begin, &a_end, &b_ptr, (void*) &nTiles, &capTiles, &sc,
                     &heavy, &heavy_cap};
     if ((e = cudaLaunchKernel(fns[pick], dim3(g), dim3(kEbThreads), args, 0, st)) != cudaSuccess)
       return e;
-    k_eb_heavy<D><<<num_sms * 4, kEbThreads, 0, st>>>(A, pA, pb, nTiles, sc, heavy, 0,
-                                                      &sc->heavy_count);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = eb_list_pass<D>(st, num_sms, A, pb, nTiles, heavy, group_done, 0, &sc->heavy_count,
+                             heavy_cap, sc)) != cudaSuccess)
+      return e;
   }
   return certify_on_stream(st, num_sms, A, B, nB, D, sc);
 }
