@@ -49,6 +49,8 @@ constexpr int kEbSlots = 4;           // A points carried per thread
 constexpr uint32_t kCapPairs = 8192;  // per-point pairs before deferral (no-alloc entry point)
 constexpr uint32_t kWaitLimit = 1u << 26;
 constexpr uint32_t kListChunks = 64;  // B chunks per group in the list scan, at least
+constexpr int kHeavySlots = 4;        // deferred points a CTA carries at once
+constexpr uint32_t kHeavyStepTiles = 32;  // tiles between a CTA's reductions
 
 template <int D>
 struct EbPt;
@@ -415,6 +417,132 @@ __global__ void __launch_bounds__(kEbThreads)
   if (pairs) atomicAdd(&sc->pairs, pairs);
 }
 
+// Deferred points: the CTA's threads all stride over B (every thread loads
+// one point of each tile), carrying kHeavySlots listed points at once, so
+// that every B point loaded serves kHeavySlots pairs.  Every kHeavyStepTiles
+// tiles the CTA reduces each slot's minimum and re-reads the running
+// maximum: a slot whose minimum is at or below it is freed (early break), a
+// slot that has covered B's whole tile ring raises the maximum and is freed,
+// and free slots take the CTA's next list entries (entries blockIdx.x,
+// blockIdx.x + gridDim.x, ...).  Points thus finish one after another and
+// the maximum climbs while the rest of the list is still open, as in the
+// reference's early break (early_break.h:63-85).  A point keeps the running
+// minimum of its main-pass tiles and scans the whole ring from the CTA's
+// current position (the few tiles it already saw cost next to nothing); all
+// CTAs start at tile 0 and move at about the same pace, so they read B's
+// tiles through L2.
+template <int D>
+__global__ void __launch_bounds__(kEbThreads)
+    k_eb_heavy(const float* __restrict__ A, const typename EbPt<D>::T* __restrict__ Bp,
+               uint32_t nTiles, DevScalars* sc, const HeavyEntry* __restrict__ list,
+               const uint32_t* n_dev, uint32_t cap) {
+  constexpr int P = kHeavySlots;
+  __shared__ float red[kEbThreads / 32][P];
+  __shared__ float s_thr;
+  const int tid = threadIdx.x;
+  const uint32_t n = min(*n_dev, cap);
+  float ax[P], ay[P], az[P], cmin[P];
+  uint32_t ia[P], done[P];
+  bool act[P];
+  uint32_t next = blockIdx.x;  // next list entry of this CTA
+  auto take = [&](int s) {
+    act[s] = next < n;
+    if (act[s]) {
+      const HeavyEntry h = list[next];
+      ia[s] = h.ia;
+      load_a<D>(A, h.ia, ax[s], ay[s], az[s]);
+      cmin[s] = h.cmin;
+      done[s] = 0;
+      next += gridDim.x;
+    } else {
+      ax[s] = ay[s] = az[s] = 0.0f;
+      cmin[s] = FLT_MAX;
+    }
+  };
+#pragma unroll
+  for (int s = 0; s < P; ++s) take(s);
+  unsigned long long pairs = 0;
+  uint32_t t = 0;  // this CTA's position in B's tile ring
+  for (;;) {
+    bool any = false;
+#pragma unroll
+    for (int s = 0; s < P; ++s) any |= act[s];
+    if (!any) break;
+    const uint32_t step = min((uint32_t) kHeavyStepTiles, nTiles);
+    float m[P];
+#pragma unroll
+    for (int s = 0; s < P; ++s) m[s] = FLT_MAX;
+    // The step's tiles t .. t+step-1 around the ring: at most two contiguous
+    // runs, each walked with one pointer (groups of 8 loads issued before any
+    // is used).
+    for (uint32_t k = 0; k < step;) {
+      const uint32_t run = min(step - k, nTiles - t);
+      const typename EbPt<D>::T* p = Bp + (uint64_t) t * kEbTile + tid;
+      uint32_t u = 0;
+      for (; u + 8 <= run; u += 8, p += 8 * kEbTile) {
+        typename EbPt<D>::T b[8];
+#pragma unroll
+        for (int v = 0; v < 8; ++v) b[v] = p[v * kEbTile];
+#pragma unroll
+        for (int v = 0; v < 8; ++v)
+#pragma unroll
+          for (int s = 0; s < P; ++s) {
+            if (!act[s]) continue;
+            if constexpr (D == 2)
+              m[s] = fminf(m[s], d2_2(ax[s], ay[s], b[v].x, b[v].y));
+            else
+              m[s] = fminf(m[s], d2_3(ax[s], ay[s], az[s], b[v].x, b[v].y, b[v].z));
+          }
+      }
+      for (; u < run; ++u, p += kEbTile) {
+        const auto b = *p;
+#pragma unroll
+        for (int s = 0; s < P; ++s) {
+          if (!act[s]) continue;
+          if constexpr (D == 2)
+            m[s] = fminf(m[s], d2_2(ax[s], ay[s], b.x, b.y));
+          else
+            m[s] = fminf(m[s], d2_3(ax[s], ay[s], az[s], b.x, b.y, b.z));
+        }
+      }
+      k += run;
+      t += run;
+      if (t == nTiles) t = 0;
+    }
+#pragma unroll
+    for (int s = 0; s < P; ++s) {
+      if (!act[s]) continue;
+      pairs += step;
+      float w = m[s];
+#pragma unroll
+      for (int o = 16; o; o >>= 1) w = fminf(w, __shfl_xor_sync(0xFFFFFFFFu, w, o));
+      if ((tid & 31) == 0) red[tid >> 5][s] = w;
+    }
+    // One thread reads the shared maximum so that every thread of the CTA
+    // takes the same decisions.
+    if (tid == 0) s_thr = threshold_of(ld_relaxed_u64(&sc->max_key));
+    __syncthreads();
+    const float thr = s_thr;
+#pragma unroll
+    for (int s = 0; s < P; ++s) {
+      if (!act[s]) continue;
+      float bm = red[0][s];
+#pragma unroll
+      for (int k = 1; k < kEbThreads / 32; ++k) bm = fminf(bm, red[k][s]);
+      cmin[s] = fminf(cmin[s], bm);
+      done[s] += step;
+      if (cmin[s] <= thr) {
+        take(s);  // early break: this point cannot raise the maximum
+      } else if (done[s] >= nTiles) {
+        if (tid == 0) atomicMax(&sc->max_key, pack_max(cmin[s], ia[s]));
+        take(s);  // whole ring scanned: exact minimum
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0 && pairs) atomicAdd(&sc->pairs, pairs * kEbTile);
+}
+
 // The seed list: the first n visit positions of A, nothing scanned yet.
 __global__ void k_eb_seed_list(Perm permA, uint32_t n, uint32_t nTiles, HeavyEntry* list) {
   const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -519,11 +647,10 @@ hd_status run_eb_dim(Ctx& c, const DirInput& in) {
     cudaLaunchKernel(fns[pick], dim3(grid), dim3(kEbThreads), args, 0, c.stream);
     if ((s = after_launch(c, "eb_main")) != HD_OK) return s;
     mark(c, 4);
-    cudaError_t e = eb_list_pass<D>(c.stream, c.num_sms, in.A, (const PT*) pb, nTiles,
-                                    (HeavyEntry*) ph, group_done, 0, &sc->heavy_count, heavy_cap,
-                                    sc);
-    c.launches += 1;
-    if (e != cudaSuccess) return cuda_fail(c, e, "eb_deferred");
+    k_eb_heavy<D><<<c.num_sms * 4, kEbThreads, 0, c.stream>>>(in.A, (const PT*) pb, nTiles, sc,
+                                                               (const HeavyEntry*) ph,
+                                                               &sc->heavy_count, heavy_cap);
+    if ((s = after_launch(c, "eb_deferred")) != HD_OK) return s;
   } else {
     mark(c, 4);
   }
@@ -638,9 +765,9 @@ cudaError_t noalloc_direction(cudaStream_t st, int num_sms, const float* A, uint
                     &heavy, &heavy_cap};
     if ((e = cudaLaunchKernel(fns[pick], dim3(g), dim3(kEbThreads), args, 0, st)) != cudaSuccess)
       return e;
-    if ((e = eb_list_pass<D>(st, num_sms, A, pb, nTiles, heavy, group_done, 0, &sc->heavy_count,
-                             heavy_cap, sc)) != cudaSuccess)
-      return e;
+    k_eb_heavy<D><<<num_sms * 4, kEbThreads, 0, st>>>(A, pb, nTiles, sc, heavy, &sc->heavy_count,
+                                                      heavy_cap);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return certify_on_stream(st, num_sms, A, B, nB, D, sc);
 }
