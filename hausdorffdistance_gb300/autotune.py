@@ -8,17 +8,20 @@ For a sweep of synthetic workloads (uniform 2-D, Gaussian clusters 3-D,
 LiDAR-like planes 3-D, coherent polylines 2-D; several sizes; both
 directions) it times every index-free and index-based variant on the GPU
 (device-resident inputs, CUDA-event time reported by the library) and records
-the sampler statistic the selector sees: the 80th percentile of sampled
-early-break iteration counts, p80, and ratio = |A| * p80 / (|A| + |B|).
-It then fits the selector's table:
+the statistics the selector sees: the 80th percentile of sampled early-break
+iteration counts, p80, and ratio = |A| * p80 / (|A| + |B|); the fraction of
+sampled queries outside the target's box (outside) and the target's cell
+occupancy skew (skew).  It then fits the selector's table:
 
-  eb_small_pairs / index_min_pairs
-               size bands (|A| * |B|) below / above which EB / the index is
-               chosen without sampling;
-  eb_ratio     between the bands, the threshold on ratio below which EB is
-               chosen;
-  (each minimising the total time of the sweep's choices);
-  prefer_grid  whether the grid beats the LBVH in total over the sweep.
+  eb_small_pairs
+               size band (|A| * |B|) below which EB is chosen without
+               sampling (index_min_pairs, above which the LBVH is chosen
+               without sampling, and eb_sample_max_pairs, the largest problem
+               the EB sample runs on, are fixed by design);
+  eb_ratio     the threshold on ratio below which EB is chosen;
+  grid_max_outside, grid_max_skew
+               the grid is chosen when both statistics are at or below them;
+  (each minimising the total time of the sweep's choices).
 
 The batch sweep (skipped with --no-batch) times the batched solver on the
 lognormal polyline batch for each schedule (one-warp threshold
@@ -67,6 +70,18 @@ def workloads(quick: bool):
         yield f"planes3d_{n}", a, b
     a, b, _ = synth.polylines(sizes=[50_000], seed=104)
     yield "polyline_50000", a, b
+    for n in ([100_000] if quick else [100_000, 1_000_000]):
+        a, b = duplicated3d(n, seed=105)
+        yield f"duplicated3d_{n}", a, b
+
+
+def duplicated3d(n, seed=105, sites=16):
+    """Heavily duplicated 3-D data: every point is one of `sites` locations
+    (both sets), the case where the early break stops after a few pairs."""
+    rng = np.random.default_rng(seed)
+    c = rng.random((sites, 3)).astype(np.float32)
+    return (np.ascontiguousarray(c[rng.integers(0, sites, n)]),
+            np.ascontiguousarray(c[rng.integers(0, sites, n)]))
 
 
 def time_variant(eng, ta, tb, variant, reps=3):
@@ -89,6 +104,8 @@ def sweep(quick: bool):
                 r = eng.solve(tx, ty, variant="auto")
                 rec["p80"] = r.sample_p80[0]
                 rec["ratio"] = len(x) * r.sample_p80[0] / (len(x) + len(y))
+                rec["outside"] = r.grid_outside[0]
+                rec["skew"] = r.grid_skew[0]
                 for v in ("eb", "lbvh", "grid"):
                     ms, rv = time_variant(eng, tx, ty, v)
                     rec[v] = ms
@@ -98,38 +115,44 @@ def sweep(quick: bool):
     return rows
 
 
+INDEX_MIN_PAIRS = 1e13
+EB_SAMPLE_MAX_PAIRS = 1e10
+
+
+def choose(r, small, eb_ratio, max_outside, max_skew):
+    """The selector's choice for a sweep row under a table."""
+    if r["pairs"] <= small:
+        return "eb"
+    if r["pairs"] >= INDEX_MIN_PAIRS:
+        return "lbvh"
+    if r["pairs"] <= EB_SAMPLE_MAX_PAIRS and r["ratio"] < eb_ratio:
+        return "eb"
+    if r.get("outside", 1.0) <= max_outside and r.get("skew", 1e30) <= max_skew:
+        return "grid"
+    return "lbvh"
+
+
 def fit(rows):
-    """Fits the selector table.  Choice for a row, given the table:
-    EB if pairs <= eb_small; index if pairs >= index_min; else EB iff
-    ratio < eb_ratio.  Each parameter is chosen from the sweep's own values
-    to minimise the sweep's total time (coordinate search, two rounds)."""
-    grid_total = sum(r["grid"] for r in rows)
-    lbvh_total = sum(r["lbvh"] for r in rows)
-    prefer_grid = grid_total < lbvh_total
-    idx = "grid" if prefer_grid else "lbvh"
+    """Fits the selector table: each parameter is chosen from the sweep's own
+    values to minimise the sweep's total time (coordinate search, three
+    rounds)."""
     for r in rows:
         r.setdefault("pairs", float(r.get("n_a", 1)) * float(r.get("n_b", 1)))
 
-    def cost(small, big, t):
-        total = 0.0
-        for r in rows:
-            if r["pairs"] <= small:
-                total += r["eb"]
-            elif r["pairs"] >= big:
-                total += r[idx]
-            else:
-                total += r["eb"] if r["ratio"] < t else r[idx]
-        return total
+    def cost(*p):
+        return sum(r[choose(r, *p)] for r in rows)
 
-    pair_cands = sorted({0.0, 1e30} | {r["pairs"] for r in rows})
-    ratio_cands = sorted({0.0, 1e30} | {r["ratio"] * 1.0001 for r in rows})
-    small, big, t = 0.0, 1e30, 0.0
-    for _ in range(2):
-        t = min(ratio_cands, key=lambda x: (cost(small, big, x), x))
-        small = min(pair_cands, key=lambda x: (cost(x, big, t), -x))
-        big = min([b for b in pair_cands if b > small] or [1e30], key=lambda x: (cost(small, x, t), x))
-    return {"eb_ratio": t, "eb_small_pairs": small, "index_min_pairs": big,
-            "prefer_grid": prefer_grid, "total_ms_chosen": cost(small, big, t),
+    pair_c = sorted({0.0} | {r["pairs"] for r in rows})
+    ratio_c = sorted({0.0} | {r["ratio"] * 1.0001 for r in rows})
+    out_c = sorted({0.0} | {r.get("outside", 0.0) * 1.0001 for r in rows})
+    skew_c = sorted({0.0} | {r.get("skew", 0.0) * 1.0001 for r in rows})
+    p = [0.0, 0.0, 0.0, 0.0]
+    for _ in range(3):
+        for i, cands in enumerate((pair_c, ratio_c, out_c, skew_c)):
+            p[i] = min(cands, key=lambda x: (cost(*(p[:i] + [x] + p[i + 1:])), x))
+    return {"eb_small_pairs": p[0], "index_min_pairs": INDEX_MIN_PAIRS, "eb_ratio": p[1],
+            "eb_sample_max_pairs": EB_SAMPLE_MAX_PAIRS, "grid_max_outside": p[2],
+            "grid_max_skew": p[3], "total_ms_chosen": cost(*p),
             "total_ms_oracle_choice": sum(min(r["eb"], r["lbvh"], r["grid"]) for r in rows)}
 
 
@@ -222,7 +245,10 @@ def read_table(path):
     vals = dict(re.findall(r"#define HD_TUNED_(\w+) (\S+)", open(path).read()))
     out = {"eb_small_pairs": float(vals["EB_SMALL_PAIRS"]),
            "index_min_pairs": float(vals["INDEX_MIN_PAIRS"]),
-           "eb_ratio": float(vals["EB_RATIO"]), "prefer_grid": vals["PREFER_GRID"] != "0"}
+           "eb_ratio": float(vals["EB_RATIO"]),
+           "eb_sample_max_pairs": float(vals["EB_SAMPLE_MAX_PAIRS"]),
+           "grid_max_outside": float(vals["GRID_MAX_OUTSIDE"]),
+           "grid_max_skew": float(vals["GRID_MAX_SKEW"])}
     for key, name in (("batch_small_rows", "BATCH_SMALL_ROWS"), ("batch_chunk", "BATCH_CHUNK"),
                       ("batch_window", "BATCH_WINDOW"), ("lbvh_budget", "LBVH_BUDGET"),
                       ("eb_cap_div", "EB_CAP_DIV"), ("eb_cap_min", "EB_CAP_MIN"),
@@ -240,7 +266,9 @@ def write_table(params, path):
         f.write(f"#define HD_TUNED_INDEX_MIN_PAIRS {params['index_min_pairs']:.6g}\n")
         f.write(f"#define HD_TUNED_EB_RATIO {params['eb_ratio']:.6g}\n")
         f.write("#define HD_TUNED_BF16_MIN_PAIRS 67108864.0\n")
-        f.write(f"#define HD_TUNED_PREFER_GRID {1 if params['prefer_grid'] else 0}\n")
+        f.write(f"#define HD_TUNED_EB_SAMPLE_MAX_PAIRS {params['eb_sample_max_pairs']:.6g}\n")
+        f.write(f"#define HD_TUNED_GRID_MAX_OUTSIDE {params['grid_max_outside']:.6g}\n")
+        f.write(f"#define HD_TUNED_GRID_MAX_SKEW {params['grid_max_skew']:.6g}\n")
         f.write("#define HD_TUNED_LEAF_SIZE 16\n")
         f.write(f"#define HD_TUNED_BATCH_SMALL_ROWS "
                 f"{params.get('batch_small_rows', BATCH_DEFAULT['batch_small_rows'])}\n")

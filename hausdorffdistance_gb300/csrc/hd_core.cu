@@ -461,6 +461,8 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   c->sorted_valid = false;
   c->ev_base = 0;
   c->last_p80[0] = c->last_p80[1] = 0.0;
+  c->last_outside[0] = c->last_outside[1] = 0.0;
+  c->last_skew[0] = c->last_skew[1] = 0.0;
 
   hd_status s;
   const float* dA = A;
@@ -497,6 +499,13 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
       c->ev_base = 12 * d;
       if ((s = select_variant(*c, ins[d], &used[d])) != HD_OK) return s;
     }
+  }
+  if (variant == HD_VARIANT_AUTO && undirected) {
+    // The grid only when both directions qualify; otherwise both directions
+    // share the fused LBVH launches.
+    auto index = [](int v) { return v == HD_VARIANT_GRID || v == HD_VARIANT_LBVH; };
+    if (index(used[0]) && index(used[1]) && used[0] != used[1])
+      used[0] = used[1] = HD_VARIANT_LBVH;
   }
   const bool fused = undirected && used[0] == HD_VARIANT_LBVH && used[1] == HD_VARIANT_LBVH;
   auto run_all = [&]() -> hd_status {
@@ -605,6 +614,10 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   out->variant_used_ba = undirected ? used[1] : -1;
   out->sample_p80[0] = c->last_p80[0];
   out->sample_p80[1] = undirected ? c->last_p80[1] : 0.0;
+  for (int d = 0; d < 2; ++d) {
+    out->grid_outside[d] = d < ndir ? c->last_outside[d] : 0.0;
+    out->grid_skew[d] = d < ndir ? c->last_skew[d] : 0.0;
+  }
   out->err_bound = std::max(ex[0].err_bound, ex[1].err_bound);
   out->rechecked = ex[0].rechecked + ex[1].rechecked;
   // LBVH: queries whose packet ran over the traversal budget; EB: points

@@ -9,24 +9,47 @@
 //   1. Eight points of A get their exact nearest-neighbour distance (one
 //      grid-wide scan of B) and seed the running maximum.  Then k further
 //      points of A (k = sample_rate * |A|, clamped to [64, 256]) run the
-//      early-break scan against B, one CTA each, B visited in a pseudo-random
-//      order, counting the B points each visited before it stopped (capped at
-//      16,384).  Seeds and completed samples also seed the running maximum
+//      early-break scan against B, one warp each, B visited in a
+//      pseudo-random order, counting the B points each visited before it
+//      stopped (in rounds of 64, capped at 16,384).  Seeds and completed samples also seed the running maximum
 //      that the chosen variant starts from.
 //   2. The EB cost of the full set is ~ |A| * p80 pairs; the index-based cost
 //      is ~ |A| + |B| point operations.  EB is chosen when
-//          ratio = |A| * p80 / (|A| + |B|)  <  eb_only_threshold,
-//      otherwise the LBVH (the grid when the table says so).  The threshold
-//      comes from the autotuner's table (hausdorffdistance_gb300/autotune.py
-//      fits it over a sweep of workloads) unless hd_options overrides it.
-//   3. Size bands from the same table: problems with |A| * |B| up to
+//          ratio = |A| * p80 / (|A| + |B|)  <  eb_ratio
+//      (points that break after a few pairs: heavily duplicated data, or a
+//      running maximum far above the typical nearest-neighbour distance).
+//      The sample runs up to eb_sample_max_pairs.
+//   3. Otherwise an index: the uniform grid or the LBVH, from two statistics
+//      of small strided samples of both sets (2,048 points each), computed
+//      on the host:
+//        outside  the fraction of query samples outside the target sample's
+//                 box (padded by 1%): queries far from every target point
+//                 make the grid's ring search grow without bound;
+//        skew     the target's cell-occupancy skew at the grid's resolution
+//                 (the reference's rule: |B| / n_points_cell cells over B's
+//                 box): the number of target-sample pairs that share a cell
+//                 divided by the number a uniform set would give (birthday
+//                 statistic, ~1 for uniform data; clustered or planar data,
+//                 whose cells are mostly empty and partly crowded, give many
+//                 times more).  It plays the role of the reference's grid
+//                 histogram Gini feature (src/models/features.h).
+//      The grid is chosen when outside <= grid_max_outside and skew <=
+//      grid_max_skew, else the LBVH.  An undirected solve takes the grid only
+//      when both directions qualify (otherwise both directions share the
+//      fused LBVH launches).
+//   4. Size bands from the same table: problems with |A| * |B| up to
 //      eb_small_pairs take EB and problems from index_min_pairs up take the
-//      index, both without sampling (the sweep shows the choice there does
-//      not depend on the data); inputs with n_dims other than 2 or 3 take the
-//      split-BF16 tiles when n_dims is a multiple of 16 and the pair count is
-//      large, else the FP32 scan.
+//      LBVH, both without sampling (at the largest sizes the grid's worst
+//      cases cost tens of times the LBVH while its best cases save ~20%);
+//      inputs with n_dims other than 2 or 3 take the split-BF16 tiles when
+//      n_dims is a multiple of 16 and the pair count is large, else the FP32
+//      scan.
+//   All thresholds come from the autotuner's table
+//   (hausdorffdistance_gb300/autotune.py fits them over a sweep of
+//   workloads); hd_options.eb_only_threshold overrides eb_ratio.
 #include <algorithm>
 #include <cfloat>
+#include <cmath>
 #include <vector>
 
 #include "hd_common.cuh"
@@ -38,44 +61,49 @@ namespace {
 
 constexpr uint32_t kSampleCap = 16384;
 
+// Sampled early-break scans: one warp per sampled point of A, B visited in
+// a pseudo-random order, 64 B points per round (two per lane), a warp vote
+// after every round; the count of B points visited before the point stopped
+// (or the cap) is its statistic.
 __global__ void __launch_bounds__(256)
-    k_sample_eb(const float* __restrict__ A, Perm pA, const float* __restrict__ B, Perm pB,
-                uint64_t nB, int dims, uint32_t cap, DevScalars* sc, uint32_t* __restrict__ iters) {
-  __shared__ float red[8];
-  __shared__ float s_thr;
-  const uint32_t e = blockIdx.x;
+    k_sample_eb(const float* __restrict__ A, Perm pA, uint32_t k, const float* __restrict__ B,
+                Perm pB, uint64_t nB, int dims, uint32_t cap, DevScalars* sc,
+                uint32_t* __restrict__ iters) {
+  const uint32_t e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (e >= k) return;
   const uint32_t ia = (uint32_t) pA(e);
-  float a[3] = {A[(uint64_t) ia * dims], A[(uint64_t) ia * dims + 1],
-                dims == 3 ? A[(uint64_t) ia * dims + 2] : 0.0f};
+  const float a0 = A[(uint64_t) ia * dims], a1 = A[(uint64_t) ia * dims + 1];
+  const float a2 = dims == 3 ? A[(uint64_t) ia * dims + 2] : 0.0f;
   float cmin = INFINITY;
   const uint64_t limit = min((uint64_t) cap, nB);
   uint64_t done = 0;
   bool broke = false;
-  const uint64_t step = 256 * 8;
+  unsigned long long key = 0;
   while (done < limit) {
-    float m = INFINITY;
-    const uint64_t end = min(limit, done + step);
-    for (uint64_t j = done + threadIdx.x; j < end; j += 256) {
-      const uint64_t b = pB(j);
-      const float d = dims == 2 ? d2_2(a[0], a[1], B[2 * b], B[2 * b + 1])
-                                : d2_3(a[0], a[1], a[2], B[3 * b], B[3 * b + 1], B[3 * b + 2]);
-      m = fminf(m, d);
+    const uint64_t end = min(limit, done + 64);
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const uint64_t j = done + lane + 32 * u;
+      if (j < end) {
+        const uint64_t b = pB(j);
+        const float d = dims == 2 ? d2_2(a0, a1, B[2 * b], B[2 * b + 1])
+                                  : d2_3(a0, a1, a2, B[3 * b], B[3 * b + 1], B[3 * b + 2]);
+        cmin = fminf(cmin, d);
+      }
     }
     done = end;
+    float m = cmin;
 #pragma unroll
     for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-    if (threadIdx.x == 0) s_thr = threshold_of(ld_relaxed_u64(&sc->max_key));
-    __syncthreads();
-    for (int k = 0; k < 8; ++k) cmin = fminf(cmin, red[k]);
-    const float thr = s_thr;
-    __syncthreads();
-    if (cmin <= thr) {
+    cmin = m;
+    if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
+    if (cmin <= threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0))) {
       broke = true;
       break;
     }
   }
-  if (threadIdx.x == 0) {
+  if (lane == 0) {
     iters[e] = (uint32_t) done;
     // A sample that scanned all of B without stopping has its exact minimum.
     if (!broke && done == nB) atomicMax(&sc->max_key, pack_max(cmin, ia));
@@ -120,6 +148,70 @@ __global__ void k_seed_finish(Perm pA, uint32_t offset, const uint32_t* __restri
     atomicMax(&sc->max_key, pack_max(__uint_as_float(seed_min[e]), (uint32_t) pA(offset + e)));
 }
 
+// Strided sample of m points of P (point i*n/m), rows of dims floats.
+__global__ void k_gather_sample(const float* __restrict__ P, uint64_t n, int dims, uint32_t m,
+                                float* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const uint64_t src = (uint64_t) i * n / m;
+  for (int d = 0; d < dims; ++d) out[(uint64_t) i * dims + d] = P[src * dims + d];
+}
+
+constexpr uint32_t kStatSamples = 2048;
+
+// Grid statistics of a query sample q (mq points) against a target sample t
+// (mt points) of a target set of nT points (see the rule above).
+void grid_stats(const float* q, uint32_t mq, const float* t, uint32_t mt, int dims, uint64_t nT,
+                uint32_t npc, double* outside, double* skew) {
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  for (int d = 0; d < dims; ++d) {
+    lo[d] = INFINITY;
+    hi[d] = -INFINITY;
+    for (uint32_t i = 0; i < mt; ++i) {
+      lo[d] = std::min(lo[d], (double) t[(size_t) i * dims + d]);
+      hi[d] = std::max(hi[d], (double) t[(size_t) i * dims + d]);
+    }
+    const double pad = 0.01 * (hi[d] - lo[d]);
+    lo[d] -= pad;
+    hi[d] += pad;
+  }
+  uint32_t out = 0;
+  for (uint32_t i = 0; i < mq; ++i)
+    for (int d = 0; d < dims; ++d) {
+      const double v = q[(size_t) i * dims + d];
+      if (v < lo[d] || v > hi[d]) {
+        ++out;
+        break;
+      }
+    }
+  *outside = mq ? (double) out / mq : 0.0;
+  // The reference's cell size: |B| / n_points_cell cells over the box (zero
+  // extents count as 1e-5, as uniform_grid.h does).
+  double vol = 1.0;
+  for (int d = 0; d < dims; ++d) vol *= hi[d] > lo[d] ? hi[d] - lo[d] : 1e-5;
+  const double cells = std::max(1.0, (double) nT / std::max<uint32_t>(npc, 1));
+  const double side = std::pow(vol / cells, 1.0 / dims);
+  std::vector<uint64_t> keys(mt);
+  for (uint32_t i = 0; i < mt; ++i) {
+    uint64_t k = 0;
+    for (int d = 0; d < dims; ++d) {
+      const double c = std::floor((t[(size_t) i * dims + d] - lo[d]) / side);
+      k = k * 2097152u + (uint64_t) std::min(std::max(c, 0.0), 2097151.0);
+    }
+    keys[i] = k;
+  }
+  std::sort(keys.begin(), keys.end());
+  double same = 0.0;
+  for (uint32_t i = 0, j; i < mt; i = j) {
+    for (j = i + 1; j < mt && keys[j] == keys[i]; ++j) {
+    }
+    const double c = j - i;
+    same += c * (c - 1.0) / 2.0;
+  }
+  const double expect = (double) mt * (mt - 1.0) / 2.0 / cells;
+  *skew = same / std::max(expect, 1e-9);
+}
+
 }  // namespace
 
 bool select_variant_by_size(const Ctx& c, uint64_t nA, uint64_t nB, int dims, int* v) {
@@ -135,7 +227,7 @@ bool select_variant_by_size(const Ctx& c, uint64_t nA, uint64_t nB, int dims, in
     return true;
   }
   if (!sample && pairs >= tu.index_min_pairs) {
-    *v = tu.prefer_grid ? HD_VARIANT_GRID : HD_VARIANT_LBVH;
+    *v = HD_VARIANT_LBVH;
     return true;
   }
   return false;
@@ -144,18 +236,33 @@ bool select_variant_by_size(const Ctx& c, uint64_t nA, uint64_t nB, int dims, in
 hd_status select_variant(Ctx& c, const DirInput& in, int* v) {
   const Tuning& tu = tuning();
   if (select_variant_by_size(c, in.nA, in.nB, in.dims, v)) return HD_OK;
+  const double pairs = (double) in.nA * (double) in.nB;
+  const bool sample_eb = c.opt.always_sample != 0 || pairs <= tu.eb_sample_max_pairs;
   const double rate = c.opt.sample_rate > 0 ? c.opt.sample_rate : 0.01;
   uint32_t k = (uint32_t) std::min<double>(std::max<double>(rate * (double) in.nA, 64.0), 256.0);
-  k = (uint32_t) std::min<uint64_t>(k, in.nA);
+  k = sample_eb ? (uint32_t) std::min<uint64_t>(k, in.nA) : 0u;
+  const uint32_t mq = (uint32_t) std::min<uint64_t>(in.nA, kStatSamples);
+  const uint32_t mt = (uint32_t) std::min<uint64_t>(in.nB, kStatSamples);
+  // One buffer, read back with one copy: sampled iteration counts, seed
+  // minima, query sample, target sample.
+  const size_t o_seed = k, o_q = o_seed + kSeeds, o_t = o_q + (size_t) mq * in.dims;
+  const size_t words = o_t + (size_t) mt * in.dims;
   void* buf;
-  hd_status s = ensure(c, kBufCand, (size_t) (k + kSeeds) * 4, &buf);
+  hd_status s = ensure(c, kBufCand, words * 4, &buf);
   if (s != HD_OK) return s;
+  uint32_t* w = (uint32_t*) buf;
+  k_gather_sample<<<(mq + 255) / 256, 256, 0, c.stream>>>(in.A, in.nA, in.dims, mq,
+                                                          (float*) (w + o_q));
+  if ((s = after_launch(c, "gather_sample")) != HD_OK) return s;
+  k_gather_sample<<<(mt + 255) / 256, 256, 0, c.stream>>>(in.B, in.nB, in.dims, mt,
+                                                          (float*) (w + o_t));
+  if ((s = after_launch(c, "gather_sample")) != HD_OK) return s;
   DevScalars* sc = scalars(c, in.dir);
   const uint64_t seed = c.opt.seed;
   Perm pA{in.nA, pick_multiplier(in.nA, seed + 11), (seed * 1299709u) % in.nA};
   Perm pB{in.nB, pick_multiplier(in.nB, seed + 13), (seed * 15485863u) % in.nB};
-  if (in.nA > k) {
-    uint32_t* seed_min = (uint32_t*) buf + k;
+  if (k > 0 && in.nA > k) {
+    uint32_t* seed_min = w + o_seed;
     cudaError_t e0 = cudaMemsetAsync(seed_min, 0xFF, kSeeds * 4, c.stream);
     if (e0 != cudaSuccess) return cuda_fail(c, e0, "memset");
     const unsigned gx = (unsigned) std::max<uint64_t>(
@@ -166,23 +273,36 @@ hd_status select_variant(Ctx& c, const DirInput& in, int* v) {
     k_seed_finish<<<1, 32, 0, c.stream>>>(pA, k, seed_min, sc);
     if ((s = after_launch(c, "seed_finish")) != HD_OK) return s;
   }
-  k_sample_eb<<<k, 256, 0, c.stream>>>(in.A, pA, in.B, pB, in.nB, in.dims, kSampleCap, sc,
-                                       (uint32_t*) buf);
-  if ((s = after_launch(c, "sample_eb")) != HD_OK) return s;
-  std::vector<uint32_t> it(k);
-  cudaError_t e = cudaMemcpyAsync(it.data(), buf, (size_t) k * 4, cudaMemcpyDeviceToHost, c.stream);
+  if (k > 0) {
+    k_sample_eb<<<(k * 32 + 255) / 256, 256, 0, c.stream>>>(in.A, pA, k, in.B, pB, in.nB, in.dims,
+                                                             kSampleCap, sc, w);
+    if ((s = after_launch(c, "sample_eb")) != HD_OK) return s;
+  }
+  std::vector<uint32_t> h(words);
+  cudaError_t e = cudaMemcpyAsync(h.data(), buf, words * 4, cudaMemcpyDeviceToHost, c.stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "sample statistics");
-  std::sort(it.begin(), it.end());
-  const double p80 = it[(size_t) (0.8 * (k - 1))];
+  double outside = 0.0, skew = 0.0;
+  grid_stats(reinterpret_cast<const float*>(h.data() + o_q), mq,
+             reinterpret_cast<const float*>(h.data() + o_t), mt, in.dims, in.nB,
+             c.opt.n_points_cell, &outside, &skew);
+  c.last_outside[in.dir] = outside;
+  c.last_skew[in.dir] = skew;
+  double p80 = 0.0;
+  if (k > 0) {
+    std::vector<uint32_t> it(h.begin(), h.begin() + k);
+    std::sort(it.begin(), it.end());
+    p80 = it[(size_t) (0.8 * (k - 1))];
+  }
+  c.last_p80[in.dir] = p80;
   const double ratio = (double) in.nA * p80 / (double) (in.nA + in.nB);
   const double thr = c.opt.eb_only_threshold ? (double) c.opt.eb_only_threshold : tu.eb_ratio;
-  c.last_p80[in.dir] = p80;
-  if (ratio < thr) {
+  if (k > 0 && ratio < thr)
     *v = HD_VARIANT_EB;
-  } else {
-    *v = tu.prefer_grid ? HD_VARIANT_GRID : HD_VARIANT_LBVH;
-  }
+  else if (outside <= tu.grid_max_outside && skew <= tu.grid_max_skew)
+    *v = HD_VARIANT_GRID;
+  else
+    *v = HD_VARIANT_LBVH;
   return HD_OK;
 }
 

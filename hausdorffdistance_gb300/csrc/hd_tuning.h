@@ -9,7 +9,9 @@ struct Tuning {
   double index_min_pairs; // |A|*|B| from which AUTO takes the index unsampled
   double eb_ratio;        // EB when |A| * p80 / (|A| + |B|) is below this
   double bf16_min_pairs;  // n_dims % 16 == 0: BF16 tiles from this |A|*|B| up
-  bool prefer_grid;       // index-based choice: grid instead of LBVH
+  double eb_sample_max_pairs;  // the EB sample runs up to this |A|*|B|
+  double grid_max_outside;     // grid only when at most this query fraction is outside
+  double grid_max_skew;        // grid only when the target's occupancy skew is at most this
   unsigned leaf_size;     // LBVH points per leaf
   unsigned batch_small_rows;  // batches: directions up to this many rows take one warp
   unsigned batch_chunk;       // batches: consecutive items per warp step

@@ -118,6 +118,10 @@ typedef struct hd_result {
   uint64_t visited_leaves; /* index leaves / cells scanned (HD_COUNT_PAIRS)    */
   double sample_p80[2];    /* AUTO: 80th percentile of the sampled early-break */
                            /* iteration counts per direction (0 = no sample)   */
+  double grid_outside[2];  /* AUTO: fraction of sampled query points outside   */
+                           /* the target's box, per direction (0 = not drawn)  */
+  double grid_skew[2];     /* AUTO: target cell-occupancy skew at the grid's   */
+                           /* resolution, ~1 for uniform data (0 = not drawn)  */
 } hd_result;
 
 /* One problem of a batch: A[offset_a .. offset_a+n_a), B[offset_b ..).
