@@ -462,6 +462,7 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   c->ev_base = 0;
   c->last_p80[0] = c->last_p80[1] = 0.0;
   c->last_outside[0] = c->last_outside[1] = 0.0;
+  c->seeded[0] = c->seeded[1] = false;
   c->last_skew[0] = c->last_skew[1] = 0.0;
 
   hd_status s;

@@ -192,6 +192,13 @@ __global__ void __launch_bounds__(kEbThreads)
     tma_load_1d(&tile[0][0], Bp + (uint64_t) tcur * kEbTile, kTileBytes, &full[0]);
   }
 
+  // Running maximum as of the last tile boundary (mid-tile early stop).
+  float thr_prev;
+  {
+    unsigned long long k0 = 0;
+    if (lane == 0) k0 = ld_relaxed_u64(&sc->max_key);
+    thr_prev = threshold_of(__shfl_sync(0xFFFFFFFFu, k0, 0));
+  }
   uint32_t i = 0;
   bool failed = false;
   for (;; ++i) {
@@ -209,25 +216,36 @@ __global__ void __launch_bounds__(kEbThreads)
       break;
     }
 
-    if constexpr (D == 2) {
-      const float4* t4 = reinterpret_cast<const float4*>(&tile[buf][0]);
+    // The tile in chunks of 32 points: a warp whose open slots are all at or
+    // below the maximum read at the last boundary stops early (they would
+    // break at the boundary anyway), which matters for data where points
+    // break after a few pairs.
+#pragma unroll 1
+    for (int c0 = 0; c0 < kEbTile; c0 += 32) {
+      if constexpr (D == 2) {
+        const float4* t4 = reinterpret_cast<const float4*>(&tile[buf][0]) + c0 / 2;
 #pragma unroll 4
-      for (int p = 0; p < kEbTile / 2; ++p) {
-        float4 b = t4[p];
+        for (int p = 0; p < 16; ++p) {
+          float4 b = t4[p];
 #pragma unroll
-        for (int r = 0; r < S; ++r) {
-          cm[r] = fminf(cm[r], d2_2(ax[r], ay[r], b.x, b.y));
-          cm[r] = fminf(cm[r], d2_2(ax[r], ay[r], b.z, b.w));
+          for (int r = 0; r < S; ++r) {
+            cm[r] = fminf(cm[r], d2_2(ax[r], ay[r], b.x, b.y));
+            cm[r] = fminf(cm[r], d2_2(ax[r], ay[r], b.z, b.w));
+          }
+        }
+      } else {
+#pragma unroll 4
+        for (int p = 0; p < 32; ++p) {
+          float4 b = tile[buf][c0 + p];
+#pragma unroll
+          for (int r = 0; r < S; ++r)
+            cm[r] = fminf(cm[r], d2_3(ax[r], ay[r], az[r], b.x, b.y, b.z));
         }
       }
-    } else {
-#pragma unroll 4
-      for (int p = 0; p < kEbTile; ++p) {
-        float4 b = tile[buf][p];
+      bool open = false;
 #pragma unroll
-        for (int r = 0; r < S; ++r)
-          cm[r] = fminf(cm[r], d2_3(ax[r], ay[r], az[r], b.x, b.y, b.z));
-      }
+      for (int r = 0; r < S; ++r) open |= act[r] && cm[r] > thr_prev;
+      if (!__any_sync(0xFFFFFFFFu, open)) break;
     }
 
     // Slot bookkeeping at the tile boundary.
@@ -235,6 +253,7 @@ __global__ void __launch_bounds__(kEbThreads)
     if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
     key = __shfl_sync(0xFFFFFFFFu, key, 0);
     const float thr = threshold_of(key);
+    thr_prev = thr;
 #pragma unroll
     for (int r = 0; r < S; ++r) {
       if (!act[r]) continue;
@@ -596,11 +615,14 @@ hd_status run_eb_dim(Ctx& c, const DirInput& in) {
   // Seeds: the first visited A points, scanned in full (the running maximum
   // is still zero) by the tile-wise list pass.  Their list entries sit at the
   // end of the deferred-point list, which the main pass fills from the start.
-  const uint32_t n_seed = (uint32_t) std::min<uint64_t>(in.nA, (uint64_t) c.num_sms);
+  // An AUTO solve whose selector already scanned seeds and a sample of A
+  // against B starts from the maximum they set instead.
+  const uint32_t n_seed =
+      c.seeded[in.dir] ? 0u : (uint32_t) std::min<uint64_t>(in.nA, (uint64_t) c.num_sms);
   HeavyEntry* seeds = (HeavyEntry*) ph + (in.nA - n_seed);
-  k_eb_seed_list<<<(n_seed + 255) / 256, 256, 0, c.stream>>>(pA, n_seed, nTiles, seeds);
-  if ((s = after_launch(c, "eb_seed_list")) != HD_OK) return s;
-  {
+  if (n_seed > 0) {
+    k_eb_seed_list<<<(n_seed + 255) / 256, 256, 0, c.stream>>>(pA, n_seed, nTiles, seeds);
+    if ((s = after_launch(c, "eb_seed_list")) != HD_OK) return s;
     cudaError_t e = eb_list_pass<D>(c.stream, c.num_sms, in.A, (const PT*) pb, nTiles, seeds,
                                     group_done, n_seed, nullptr, n_seed, sc);
     c.launches += 1;

@@ -206,6 +206,9 @@ struct Ctx {
   // Grid statistics of the last AUTO decision per direction (query fraction
   // outside the target's box, target occupancy skew; 0 when not drawn).
   double last_outside[2] = {0.0, 0.0};
+  // The selector's sampled scans already raised this direction's running
+  // maximum (the EB variant then skips its own seed pass).
+  bool seeded[2] = {false, false};
   double last_skew[2] = {0.0, 0.0};
 };
 

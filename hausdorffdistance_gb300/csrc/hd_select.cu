@@ -277,6 +277,7 @@ hd_status select_variant(Ctx& c, const DirInput& in, int* v) {
     k_sample_eb<<<(k * 32 + 255) / 256, 256, 0, c.stream>>>(in.A, pA, k, in.B, pB, in.nB, in.dims,
                                                              kSampleCap, sc, w);
     if ((s = after_launch(c, "sample_eb")) != HD_OK) return s;
+    c.seeded[in.dir] = in.nA > k;
   }
   std::vector<uint32_t> h(words);
   cudaError_t e = cudaMemcpyAsync(h.data(), buf, words * 4, cudaMemcpyDeviceToHost, c.stream);
