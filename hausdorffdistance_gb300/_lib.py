@@ -59,7 +59,7 @@ class Result(ctypes.Structure):
                 ("variant_used_ba", ctypes.c_int32), ("err_bound", ctypes.c_double),
                 ("rechecked", ctypes.c_uint64), ("visited_leaves", ctypes.c_uint64),
                 ("sample_p80", ctypes.c_double * 2), ("grid_outside", ctypes.c_double * 2),
-                ("grid_skew", ctypes.c_double * 2)]
+                ("grid_skew", ctypes.c_double * 2), ("sample_mean", ctypes.c_double * 2)]
 
 
 class Problem(ctypes.Structure):

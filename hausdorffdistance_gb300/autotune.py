@@ -8,8 +8,9 @@ For a sweep of synthetic workloads (uniform 2-D, Gaussian clusters 3-D,
 LiDAR-like planes 3-D, coherent polylines 2-D; several sizes; both
 directions) it times every index-free and index-based variant on the GPU
 (device-resident inputs, CUDA-event time reported by the library) and records
-the statistics the selector sees: the 80th percentile of sampled early-break
-iteration counts, p80, and ratio = |A| * p80 / (|A| + |B|); the fraction of
+the statistics the selector sees: the mean (and the 80th percentile, p80) of
+sampled early-break iteration counts and ratio = |A| * mean / (|A| + |B|); the
+fraction of
 sampled queries outside the target's box (outside) and the target's cell
 occupancy skew (skew).  It then fits the selector's table:
 
@@ -103,7 +104,8 @@ def sweep(quick: bool):
                 rec = {"case": name, "direction": direction, "n_a": len(x), "n_b": len(y)}
                 r = eng.solve(tx, ty, variant="auto")
                 rec["p80"] = r.sample_p80[0]
-                rec["ratio"] = len(x) * r.sample_p80[0] / (len(x) + len(y))
+                rec["mean"] = r.sample_mean[0]
+                rec["ratio"] = len(x) * r.sample_mean[0] / (len(x) + len(y))
                 rec["outside"] = r.grid_outside[0]
                 rec["skew"] = r.grid_skew[0]
                 for v in ("eb", "lbvh", "grid"):

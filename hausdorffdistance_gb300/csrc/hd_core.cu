@@ -461,6 +461,7 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   c->sorted_valid = false;
   c->ev_base = 0;
   c->last_p80[0] = c->last_p80[1] = 0.0;
+  c->last_mean[0] = c->last_mean[1] = 0.0;
   c->last_outside[0] = c->last_outside[1] = 0.0;
   c->seeded[0] = c->seeded[1] = false;
   c->last_skew[0] = c->last_skew[1] = 0.0;
@@ -618,6 +619,7 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   for (int d = 0; d < 2; ++d) {
     out->grid_outside[d] = d < ndir ? c->last_outside[d] : 0.0;
     out->grid_skew[d] = d < ndir ? c->last_skew[d] : 0.0;
+    out->sample_mean[d] = d < ndir ? c->last_mean[d] : 0.0;
   }
   out->err_bound = std::max(ex[0].err_bound, ex[1].err_bound);
   out->rechecked = ex[0].rechecked + ex[1].rechecked;

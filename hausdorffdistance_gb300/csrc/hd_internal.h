@@ -203,6 +203,7 @@ struct Ctx {
   // Sampler statistic of the last AUTO decision per direction (p80 of the
   // sampled early-break iteration counts; 0 when no sample was drawn).
   double last_p80[2] = {0.0, 0.0};
+  double last_mean[2] = {0.0, 0.0};
   // Grid statistics of the last AUTO decision per direction (query fraction
   // outside the target's box, target occupancy skew; 0 when not drawn).
   double last_outside[2] = {0.0, 0.0};

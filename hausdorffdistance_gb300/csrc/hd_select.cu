@@ -13,12 +13,16 @@
 //      pseudo-random order, counting the B points each visited before it
 //      stopped (in rounds of 64, capped at 16,384).  Seeds and completed samples also seed the running maximum
 //      that the chosen variant starts from.
-//   2. The EB cost of the full set is ~ |A| * p80 pairs; the index-based cost
-//      is ~ |A| + |B| point operations.  EB is chosen when
-//          ratio = |A| * p80 / (|A| + |B|)  <  eb_ratio
+//   2. The EB cost of the full set is ~ |A| * mean pairs, mean being the
+//      average of the sampled counts; the index-based cost is ~ |A| + |B|
+//      point operations.  EB is chosen when
+//          ratio = |A| * mean / (|A| + |B|)  <  eb_ratio
 //      (points that break after a few pairs: heavily duplicated data, or a
 //      running maximum far above the typical nearest-neighbour distance).
-//      The sample runs up to eb_sample_max_pairs.
+//      The reference thresholds the 80th percentile instead; the mean keeps
+//      the slow tail (say 5% of points that scan all of B), which is most of
+//      the EB's work and which an 80th percentile does not see.  The p80 is
+//      still reported.  The sample runs up to eb_sample_max_pairs.
 //   3. Otherwise an index: the uniform grid or the LBVH, from two statistics
 //      of small strided samples of both sets (2,048 points each), computed
 //      on the host:
@@ -289,14 +293,17 @@ hd_status select_variant(Ctx& c, const DirInput& in, int* v) {
              c.opt.n_points_cell, &outside, &skew);
   c.last_outside[in.dir] = outside;
   c.last_skew[in.dir] = skew;
-  double p80 = 0.0;
+  double p80 = 0.0, mean = 0.0;
   if (k > 0) {
     std::vector<uint32_t> it(h.begin(), h.begin() + k);
     std::sort(it.begin(), it.end());
     p80 = it[(size_t) (0.8 * (k - 1))];
+    for (uint32_t x : it) mean += x;
+    mean /= k;
   }
   c.last_p80[in.dir] = p80;
-  const double ratio = (double) in.nA * p80 / (double) (in.nA + in.nB);
+  c.last_mean[in.dir] = mean;
+  const double ratio = (double) in.nA * mean / (double) (in.nA + in.nB);
   const double thr = c.opt.eb_only_threshold ? (double) c.opt.eb_only_threshold : tu.eb_ratio;
   if (k > 0 && ratio < thr)
     *v = HD_VARIANT_EB;

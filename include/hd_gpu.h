@@ -122,6 +122,8 @@ typedef struct hd_result {
                            /* the target's box, per direction (0 = not drawn)  */
   double grid_skew[2];     /* AUTO: target cell-occupancy skew at the grid's   */
                            /* resolution, ~1 for uniform data (0 = not drawn)  */
+  double sample_mean[2];   /* AUTO: mean of the sampled early-break iteration  */
+                           /* counts (capped), per direction (0 = no sample)   */
 } hd_result;
 
 /* One problem of a batch: A[offset_a .. offset_a+n_a), B[offset_b ..).
