@@ -304,6 +304,12 @@ def main():
     else:
         rows = sweep(args.quick)
         params = fit(rows)
+        # Schedule values whose sweeps are skipped keep what the table holds.
+        kept = read_table(os.path.join(HERE, "csrc", TABLE_NAME))
+        for key in ("batch_small_rows", "batch_chunk", "batch_window", "lbvh_budget",
+                    "eb_cap_div", "eb_cap_min", "eb_cap_max"):
+            if key in kept:
+                params.setdefault(key, kept[key])
     batch_rows, budget_rows = [], []
     if not args.no_batch:
         batch_rows = batch_sweep(args.quick)

@@ -1,16 +1,20 @@
 """AUTO chooses the variant from sampled statistics, not from sizes alone.
 
 Three inputs of the same size (100,000 x 100,000 points, inside the band
-where the selector samples) lead to three different variants:
+where the selector samples) lead to three different variants when the
+early-break threshold is set, as the reference's -eb_only_threshold sets it:
 
   duplicated 3-D points  the sampled early-break scans stop after a few
-                         pairs (small p80)               -> early break
+                         pairs (small mean count)        -> early break
   uniform 2-D points     no query outside the target's box, occupancy skew
                          ~1                              -> uniform grid
   clustered 3-D points   occupancy skew far above 1      -> LBVH
 
-Every result is checked against the oracle as in the parity suite.  This is
-the role of the reference's hybrid decision (src/hd_impl/
+With the tuned table's own threshold (0: on this GPU the early break lost to
+the LBVH above the small-size band on every swept input, duplicated data
+included) the statistics still pick between the grid and the LBVH.  Every
+result is checked against the oracle as in the parity suite.  This is the
+role of the reference's hybrid decision (src/hd_impl/
 hausdorff_distance_hybrid.h:143-199), which picks EB-only or the index from
 sampled iteration counts.
 """
@@ -32,25 +36,33 @@ def check(a, b, r, undirected=False):
     assert hd_oracle.dist2_f32(src[int(r.ia)], dst[int(r.ib)]) == want["d2"]
 
 
-def test_auto_picks_three_variants_from_statistics(engine):
-    import hausdorffdistance_gb300 as hd
+def inputs():
     dup = autotune.duplicated3d(N, seed=5)
     rng = np.random.default_rng(6)
     uni = (rng.random((N, 2)).astype(np.float32), rng.random((N, 2)).astype(np.float32))
     clu = synth.clusters3d(N, seed=7)
+    return (("dup", dup), ("uniform", uni), ("clusters", clu))
+
+
+@pytest.mark.parametrize("eb_threshold", [64, 0])
+def test_auto_picks_variants_from_statistics(eb_threshold):
+    import hausdorffdistance_gb300 as hd
     got = {}
-    for name, (a, b) in (("dup", dup), ("uniform", uni), ("clusters", clu)):
-        r = engine.solve(a, b, variant="auto")
-        got[name] = hd._lib.VARIANT_NAMES[r.variant_used]
-        check(a, b, r)
-        assert r.sample_p80[0] > 0 and r.grid_skew[0] > 0
-        if name == "dup":
-            assert r.sample_p80[0] <= 128
-        if name == "uniform":
-            assert r.grid_outside[0] == 0.0 and r.grid_skew[0] < 2.0
-        if name == "clusters":
-            assert r.grid_skew[0] > 10.0
-    assert got == {"dup": "eb", "uniform": "grid", "clusters": "lbvh"}
+    with hd.Engine(device=0, eb_only_threshold=eb_threshold) as eng:
+        for name, (a, b) in inputs():
+            r = eng.solve(a, b, variant="auto")
+            got[name] = hd._lib.VARIANT_NAMES[r.variant_used]
+            check(a, b, r)
+            assert r.sample_mean[0] > 0 and r.grid_skew[0] > 0
+            if name == "dup":
+                assert r.sample_mean[0] <= 128
+            if name == "uniform":
+                assert r.grid_outside[0] == 0.0 and r.grid_skew[0] < 1.5
+                assert r.sample_mean[0] > 1000
+            if name == "clusters":
+                assert r.grid_skew[0] > 10.0
+    want_dup = "eb" if eb_threshold else "lbvh"
+    assert got == {"dup": want_dup, "uniform": "grid", "clusters": "lbvh"}
 
 
 def test_auto_undirected_shares_the_lbvh_unless_both_directions_qualify(engine):
