@@ -421,6 +421,7 @@ hd_status hd_destroy(hd_ctx* c) {
   if (c->batch_join) cudaEventDestroy(c->batch_join);
   if (c->batch_side) cudaStreamDestroy(c->batch_side);
   if (c->host_pinned) cudaFreeHost(c->host_pinned);
+  if (c->sel_pinned) cudaFreeHost(c->sel_pinned);
   if (c->batch_pinned) cudaFreeHost(c->batch_pinned);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
@@ -497,10 +498,10 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
     ins[d] = DirInput{d == 0 ? dA : dB, d == 0 ? n_a : n_b, d == 0 ? dB : dA,
                       d == 0 ? n_b : n_a, n_dims, d, count};
     used[d] = variant;
-    if (variant == HD_VARIANT_AUTO) {
-      c->ev_base = 12 * d;
-      if ((s = select_variant(*c, ins[d], &used[d])) != HD_OK) return s;
-    }
+  }
+  if (variant == HD_VARIANT_AUTO) {
+    c->ev_base = 0;
+    if ((s = select_variants(*c, ins, ndir, used)) != HD_OK) return s;
   }
   if (variant == HD_VARIANT_AUTO && undirected) {
     // The grid only when both directions qualify; otherwise both directions

@@ -161,6 +161,8 @@ struct Ctx {
   DevBuf bufs[kNumBufs];
   void* host_pinned = nullptr;   // pinned result staging
   size_t host_pinned_bytes = 0;
+  void* sel_pinned = nullptr;    // pinned staging of the selector's samples
+  size_t sel_pinned_bytes = 0;
   void* batch_pinned = nullptr;  // pinned staging of grouped batch results
   size_t batch_pinned_bytes = 0;
   std::string last_error;
@@ -261,6 +263,10 @@ hd_status run_bf16(Ctx& c, const DirInput& in, DirResult* extra);
 // Test hook: the BF16 kernel's approximate row minima (no certification).
 hd_status bf16_rowmin_debug(Ctx& c, const DirInput& in, float* rowmin_host);
 hd_status select_variant(Ctx& c, const DirInput& in, int* variant);
+// AUTO for the ndir directions of one call at once (ins[d].dir == d; the
+// directions query and target the same two sets): one sample of each set, one
+// read-back.  v[d] receives each direction's variant.
+hd_status select_variants(Ctx& c, const DirInput* ins, int ndir, int* v);
 // The selector's choice when the sizes alone decide it (no sampling of the
 // data); false when it needs the sample pass.
 bool select_variant_by_size(const Ctx& c, uint64_t nA, uint64_t nB, int dims, int* variant);

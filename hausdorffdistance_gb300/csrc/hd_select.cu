@@ -24,8 +24,9 @@
 //      the EB's work and which an 80th percentile does not see.  The p80 is
 //      still reported.  The sample runs up to eb_sample_max_pairs.
 //   3. Otherwise an index: the uniform grid or the LBVH, from two statistics
-//      of small strided samples of both sets (2,048 points each), computed
-//      on the host:
+//      of small strided samples of both sets (1,024 points each; the same
+//      two samples serve both directions of an undirected solve, read back
+//      with the early-break counts in one copy), computed on the host:
 //        outside  the fraction of query samples outside the target sample's
 //                 box (padded by 1%): queries far from every target point
 //                 make the grid's ring search grow without bound;
@@ -161,7 +162,7 @@ __global__ void k_gather_sample(const float* __restrict__ P, uint64_t n, int dim
   for (int d = 0; d < dims; ++d) out[(uint64_t) i * dims + d] = P[src * dims + d];
 }
 
-constexpr uint32_t kStatSamples = 2048;
+constexpr uint32_t kStatSamples = 1024;
 
 // Grid statistics of a query sample q (mq points) against a target sample t
 // (mt points) of a target set of nT points (see the rule above).
@@ -237,81 +238,120 @@ bool select_variant_by_size(const Ctx& c, uint64_t nA, uint64_t nB, int dims, in
   return false;
 }
 
-hd_status select_variant(Ctx& c, const DirInput& in, int* v) {
+hd_status select_variants(Ctx& c, const DirInput* ins, int ndir, int* v) {
   const Tuning& tu = tuning();
-  if (select_variant_by_size(c, in.nA, in.nB, in.dims, v)) return HD_OK;
-  const double pairs = (double) in.nA * (double) in.nB;
-  const bool sample_eb = c.opt.always_sample != 0 || pairs <= tu.eb_sample_max_pairs;
+  bool need = false, decided[2] = {false, false};
+  for (int d = 0; d < ndir; ++d) {
+    decided[d] = select_variant_by_size(c, ins[d].nA, ins[d].nB, ins[d].dims, &v[d]);
+    need |= !decided[d];
+  }
+  if (!need) return HD_OK;
+  // One sample of each set serves both directions (query in one, target in
+  // the other); the early-break samples run per direction.  Everything comes
+  // back in one copy, with one synchronisation.
+  const int dims = ins[0].dims;
+  const float* P[2] = {ins[0].A, ins[0].B};
+  const uint64_t nP[2] = {ins[0].nA, ins[0].nB};
+  const uint32_t m[2] = {(uint32_t) std::min<uint64_t>(nP[0], kStatSamples),
+                         (uint32_t) std::min<uint64_t>(nP[1], kStatSamples)};
+  uint32_t k[2] = {0, 0};
   const double rate = c.opt.sample_rate > 0 ? c.opt.sample_rate : 0.01;
-  uint32_t k = (uint32_t) std::min<double>(std::max<double>(rate * (double) in.nA, 64.0), 256.0);
-  k = sample_eb ? (uint32_t) std::min<uint64_t>(k, in.nA) : 0u;
-  const uint32_t mq = (uint32_t) std::min<uint64_t>(in.nA, kStatSamples);
-  const uint32_t mt = (uint32_t) std::min<uint64_t>(in.nB, kStatSamples);
-  // One buffer, read back with one copy: sampled iteration counts, seed
-  // minima, query sample, target sample.
-  const size_t o_seed = k, o_q = o_seed + kSeeds, o_t = o_q + (size_t) mq * in.dims;
-  const size_t words = o_t + (size_t) mt * in.dims;
+  for (int d = 0; d < ndir; ++d) {
+    if (decided[d]) continue;
+    const double pairs = (double) ins[d].nA * (double) ins[d].nB;
+    if (c.opt.always_sample == 0 && pairs > tu.eb_sample_max_pairs) continue;
+    uint32_t kk = (uint32_t) std::min<double>(std::max<double>(rate * (double) ins[d].nA, 64.0),
+                                              256.0);
+    k[d] = (uint32_t) std::min<uint64_t>(kk, ins[d].nA);
+  }
+  // Layout (32-bit words): iteration counts of direction 0 and 1, seed
+  // minima of both, sample of set 0 (the call's A), sample of set 1.
+  const size_t o_it[2] = {0, k[0]};
+  const size_t o_seed = (size_t) k[0] + k[1];
+  const size_t o_smp[2] = {o_seed + 2 * kSeeds, o_seed + 2 * kSeeds + (size_t) m[0] * dims};
+  const size_t words = o_smp[1] + (size_t) m[1] * dims;
   void* buf;
   hd_status s = ensure(c, kBufCand, words * 4, &buf);
   if (s != HD_OK) return s;
+  if (c.sel_pinned_bytes < words * 4) {
+    if (c.sel_pinned) cudaFreeHost(c.sel_pinned);
+    c.sel_pinned = nullptr;
+    c.sel_pinned_bytes = 0;
+    if (cudaMallocHost(&c.sel_pinned, words * 4) != cudaSuccess) {
+      (void) cudaGetLastError();
+      return fail(c, HD_ERR_OOM, "pinned staging for the selector");
+    }
+    c.sel_pinned_bytes = words * 4;
+  }
   uint32_t* w = (uint32_t*) buf;
-  k_gather_sample<<<(mq + 255) / 256, 256, 0, c.stream>>>(in.A, in.nA, in.dims, mq,
-                                                          (float*) (w + o_q));
-  if ((s = after_launch(c, "gather_sample")) != HD_OK) return s;
-  k_gather_sample<<<(mt + 255) / 256, 256, 0, c.stream>>>(in.B, in.nB, in.dims, mt,
-                                                          (float*) (w + o_t));
-  if ((s = after_launch(c, "gather_sample")) != HD_OK) return s;
-  DevScalars* sc = scalars(c, in.dir);
+  for (int t = 0; t < 2; ++t) {
+    k_gather_sample<<<(m[t] + 255) / 256, 256, 0, c.stream>>>(P[t], nP[t], dims, m[t],
+                                                              (float*) (w + o_smp[t]));
+    if ((s = after_launch(c, "gather_sample")) != HD_OK) return s;
+  }
   const uint64_t seed = c.opt.seed;
-  Perm pA{in.nA, pick_multiplier(in.nA, seed + 11), (seed * 1299709u) % in.nA};
-  Perm pB{in.nB, pick_multiplier(in.nB, seed + 13), (seed * 15485863u) % in.nB};
-  if (k > 0 && in.nA > k) {
-    uint32_t* seed_min = w + o_seed;
-    cudaError_t e0 = cudaMemsetAsync(seed_min, 0xFF, kSeeds * 4, c.stream);
-    if (e0 != cudaSuccess) return cuda_fail(c, e0, "memset");
-    const unsigned gx = (unsigned) std::max<uint64_t>(
-        1, std::min<uint64_t>((in.nB + 255) / 256, (uint64_t) c.num_sms * 2));
-    k_seed_scan<<<dim3(gx, kSeeds), 256, 0, c.stream>>>(in.A, pA, k, in.B, in.nB, in.dims,
-                                                        seed_min);
-    if ((s = after_launch(c, "seed_scan")) != HD_OK) return s;
-    k_seed_finish<<<1, 32, 0, c.stream>>>(pA, k, seed_min, sc);
-    if ((s = after_launch(c, "seed_finish")) != HD_OK) return s;
-  }
-  if (k > 0) {
-    k_sample_eb<<<(k * 32 + 255) / 256, 256, 0, c.stream>>>(in.A, pA, k, in.B, pB, in.nB, in.dims,
-                                                             kSampleCap, sc, w);
+  for (int d = 0; d < ndir; ++d) {
+    if (k[d] == 0) continue;
+    const DirInput& in = ins[d];
+    DevScalars* sc = scalars(c, in.dir);
+    Perm pA{in.nA, pick_multiplier(in.nA, seed + 11), (seed * 1299709u) % in.nA};
+    Perm pB{in.nB, pick_multiplier(in.nB, seed + 13), (seed * 15485863u) % in.nB};
+    if (in.nA > k[d]) {
+      uint32_t* seed_min = w + o_seed + (size_t) d * kSeeds;
+      cudaError_t e0 = cudaMemsetAsync(seed_min, 0xFF, kSeeds * 4, c.stream);
+      if (e0 != cudaSuccess) return cuda_fail(c, e0, "memset");
+      const unsigned gx = (unsigned) std::max<uint64_t>(
+          1, std::min<uint64_t>((in.nB + 255) / 256, (uint64_t) c.num_sms * 2));
+      k_seed_scan<<<dim3(gx, kSeeds), 256, 0, c.stream>>>(in.A, pA, k[d], in.B, in.nB, in.dims,
+                                                          seed_min);
+      if ((s = after_launch(c, "seed_scan")) != HD_OK) return s;
+      k_seed_finish<<<1, 32, 0, c.stream>>>(pA, k[d], seed_min, sc);
+      if ((s = after_launch(c, "seed_finish")) != HD_OK) return s;
+    }
+    k_sample_eb<<<(k[d] * 32 + 255) / 256, 256, 0, c.stream>>>(
+        in.A, pA, k[d], in.B, pB, in.nB, in.dims, kSampleCap, sc, w + o_it[d]);
     if ((s = after_launch(c, "sample_eb")) != HD_OK) return s;
-    c.seeded[in.dir] = in.nA > k;
+    c.seeded[in.dir] = in.nA > k[d];
   }
-  std::vector<uint32_t> h(words);
-  cudaError_t e = cudaMemcpyAsync(h.data(), buf, words * 4, cudaMemcpyDeviceToHost, c.stream);
+  uint32_t* h = (uint32_t*) c.sel_pinned;
+  cudaError_t e = cudaMemcpyAsync(h, buf, words * 4, cudaMemcpyDeviceToHost, c.stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "sample statistics");
-  double outside = 0.0, skew = 0.0;
-  grid_stats(reinterpret_cast<const float*>(h.data() + o_q), mq,
-             reinterpret_cast<const float*>(h.data() + o_t), mt, in.dims, in.nB,
-             c.opt.n_points_cell, &outside, &skew);
-  c.last_outside[in.dir] = outside;
-  c.last_skew[in.dir] = skew;
-  double p80 = 0.0, mean = 0.0;
-  if (k > 0) {
-    std::vector<uint32_t> it(h.begin(), h.begin() + k);
-    std::sort(it.begin(), it.end());
-    p80 = it[(size_t) (0.8 * (k - 1))];
-    for (uint32_t x : it) mean += x;
-    mean /= k;
+  for (int d = 0; d < ndir; ++d) {
+    if (decided[d]) continue;
+    const DirInput& in = ins[d];
+    // Direction d queries set q against set t (set 0 is the call's A).
+    const int q = in.A == P[0] && in.nA == nP[0] ? 0 : 1, t = 1 - q;
+    double outside = 0.0, skew = 0.0;
+    grid_stats(reinterpret_cast<const float*>(h + o_smp[q]), m[q],
+               reinterpret_cast<const float*>(h + o_smp[t]), m[t], dims, nP[t],
+               c.opt.n_points_cell, &outside, &skew);
+    c.last_outside[in.dir] = outside;
+    c.last_skew[in.dir] = skew;
+    double p80 = 0.0, mean = 0.0;
+    if (k[d] > 0) {
+      std::vector<uint32_t> it(h + o_it[d], h + o_it[d] + k[d]);
+      std::sort(it.begin(), it.end());
+      p80 = it[(size_t) (0.8 * (k[d] - 1))];
+      for (uint32_t x : it) mean += x;
+      mean /= k[d];
+    }
+    c.last_p80[in.dir] = p80;
+    c.last_mean[in.dir] = mean;
+    const double ratio = (double) in.nA * mean / (double) (in.nA + in.nB);
+    const double thr = c.opt.eb_only_threshold ? (double) c.opt.eb_only_threshold : tu.eb_ratio;
+    if (k[d] > 0 && ratio < thr)
+      v[d] = HD_VARIANT_EB;
+    else if (outside <= tu.grid_max_outside && skew <= tu.grid_max_skew)
+      v[d] = HD_VARIANT_GRID;
+    else
+      v[d] = HD_VARIANT_LBVH;
   }
-  c.last_p80[in.dir] = p80;
-  c.last_mean[in.dir] = mean;
-  const double ratio = (double) in.nA * mean / (double) (in.nA + in.nB);
-  const double thr = c.opt.eb_only_threshold ? (double) c.opt.eb_only_threshold : tu.eb_ratio;
-  if (k > 0 && ratio < thr)
-    *v = HD_VARIANT_EB;
-  else if (outside <= tu.grid_max_outside && skew <= tu.grid_max_skew)
-    *v = HD_VARIANT_GRID;
-  else
-    *v = HD_VARIANT_LBVH;
   return HD_OK;
+}
+
+hd_status select_variant(Ctx& c, const DirInput& in, int* v) {
+  return select_variants(c, &in, 1, v);
 }
 
 }  // namespace hdg
