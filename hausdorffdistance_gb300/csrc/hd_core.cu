@@ -465,7 +465,6 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
   c->last_mean[0] = c->last_mean[1] = 0.0;
   c->last_outside[0] = c->last_outside[1] = 0.0;
   c->seeded[0] = c->seeded[1] = false;
-  c->presorted = false;
   c->last_skew[0] = c->last_skew[1] = 0.0;
 
   hd_status s;
@@ -518,13 +517,13 @@ hd_status hd_solve(hd_ctx* c, const float* A, uint64_t n_a, const float* B,
       // Fused undirected pass: one sort of both sets, both trees and both
       // directions' queries in shared launches.
       c->ev_base = 0;
-      if (!c->presorted) mark(*c, 0);
+      mark(*c, 0);
       if ((r = run_lbvh_pair(*c, ins[0], ins[1])) != HD_OK) return r;
       mark(*c, 6);
     } else {
       for (int d = 0; d < ndir; ++d) {
         c->ev_base = 12 * d;
-        if (!(c->presorted && d == 0)) mark(*c, 0);
+        mark(*c, 0);
         if ((r = run_direction(*c, ins[d], used[d], &used[d], &ex[d])) != HD_OK) return r;
         mark(*c, 6);
       }

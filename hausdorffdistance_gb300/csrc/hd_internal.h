@@ -202,9 +202,6 @@ struct Ctx {
   // are shared by both directions of an undirected solve.
   SortedSet sorted[2];
   bool sorted_valid = false;
-  // The selector sorted the sets (and recorded the prep phase's start) while
-  // it waited for its samples.
-  bool presorted = false;
   // Sampler statistic of the last AUTO decision per direction (p80 of the
   // sampled early-break iteration counts; 0 when no sample was drawn).
   double last_p80[2] = {0.0, 0.0};

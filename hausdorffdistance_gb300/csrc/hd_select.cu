@@ -315,19 +315,7 @@ hd_status select_variants(Ctx& c, const DirInput* ins, int ndir, int* v) {
   }
   uint32_t* h = (uint32_t*) c.sel_pinned;
   cudaError_t e = cudaMemcpyAsync(h, buf, words * 4, cudaMemcpyDeviceToHost, c.stream);
-  if (e != cudaSuccess) return cuda_fail(c, e, "sample statistics");
-  // When no direction can take the early break, every choice left is an
-  // index over the Morton-sorted sets: sort them now, while the host waits
-  // for the samples (the variant's launches then find the sets sorted).
-  bool index_only = dims == 2 || dims == 3;
-  for (int d = 0; d < ndir; ++d) index_only &= !decided[d] && k[d] == 0;
-  if (index_only) {
-    mark(c, 0);
-    const SortedSet *sq, *st;
-    if ((s = spatial_prepare(c, ins[0], &sq, &st)) != HD_OK) return s;
-    c.presorted = true;
-  }
-  e = cudaStreamSynchronize(c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "sample statistics");
   for (int d = 0; d < ndir; ++d) {
     if (decided[d]) continue;
