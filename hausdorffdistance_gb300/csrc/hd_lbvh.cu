@@ -185,8 +185,26 @@ constexpr float kMaxDistMargin = 1.0f + 1.0f / 65536.0f;
 // LT: leaf size known at compile time (16, the tuned size), or 0 for a
 // runtime leaf size L.
 template <int D, bool COUNT, int LT>
+// Division of a 32-bit value by a run-time constant d, with the multiplier
+// m and shifts s1, s2 prepared on the host (Granlund and Montgomery,
+// "Division by Invariant Integers using Multiplication", PLDI 1994):
+// q = (t + ((n - t) >> s1)) >> s2 with t = umulhi(m, n).
+struct FastDiv {
+  uint32_t m, s1, s2;
+};
+static FastDiv make_fastdiv(uint32_t d) {
+  uint32_t l = 0;
+  while (l < 32 && (1ull << l) < d) ++l;
+  const uint64_t m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
+  return FastDiv{(uint32_t) m, l < 1 ? l : 1u, l > 0 ? l - 1 : 0u};
+}
+__device__ __forceinline__ uint32_t fastdiv(uint32_t n, FastDiv f) {
+  const uint32_t t = __umulhi(f.m, n);
+  return (t + ((n - t) >> f.s1)) >> f.s2;
+}
+
 __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, uint64_t nItems, uint32_t pstride,
-                 uint64_t rows, const uint32_t* __restrict__ ppos,
+                 uint64_t rows, FastDiv rows_div, const uint32_t* __restrict__ ppos,
                  const float4* __restrict__ nodes, const float4* __restrict__ B, uint64_t nB,
                  uint32_t L, DevScalars* sc, Deferred* __restrict__ defer, uint32_t budget,
                  uint32_t root) {
@@ -201,7 +219,7 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   // 32-bit arithmetic: packet counts stay below 2^27 (point sets < 2^32).
   const uint32_t w = blockIdx.x * kQueryWarps + warp;
   const uint32_t r32 = (uint32_t) rows;
-  const uint32_t wq = w / r32;
+  const uint32_t wq = fastdiv(w, rows_div);
   const uint64_t packet = (uint64_t) (w - wq * r32) * pstride + wq;
   if (packet * 32 >= nItems) return;
   const uint64_t item = packet * 32 + lane;
@@ -450,6 +468,7 @@ struct QuerySet {
   uint64_t nQ;
   uint32_t pstride;
   uint64_t rows;
+  FastDiv rows_div;  // division by rows
   const uint32_t* ppos;
   const float4* nodes;
   const float4* B;
@@ -467,7 +486,8 @@ struct QuerySets {
 template <int D, bool COUNT, int LT>
 __global__ void __launch_bounds__(kQueryWarps * 32) k_lbvh_query(QuerySets qs) {
   const QuerySet& S = qs.d[blockIdx.y];
-  lbvh_query_body<D, COUNT, LT>(S.Q, S.nQ, S.pstride, S.rows, S.ppos, S.nodes, S.B, S.nB, S.L, S.sc,
+  lbvh_query_body<D, COUNT, LT>(S.Q, S.nQ, S.pstride, S.rows, S.rows_div, S.ppos, S.nodes, S.B,
+                                S.nB, S.L, S.sc,
                             S.defer, S.budget, *S.root);
 }
 
@@ -705,6 +725,7 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
     const uint32_t pstride = packets[k] >= 4096 ? 64 : (packets[k] >= 256 ? 16 : 1);
     d.pstride = pstride;
     d.rows = (packets[k] + pstride - 1) / pstride;
+    d.rows_div = make_fastdiv((uint32_t) d.rows);
     d.nodes = bs.s[k].nodes;
     d.root = bs.s[k].root;
     d.L = bs.s[k].L;
