@@ -184,7 +184,6 @@ constexpr float kMaxDistMargin = 1.0f + 1.0f / 65536.0f;
 // (or 32 entries of a sample list).
 // LT: leaf size known at compile time (16, the tuned size), or 0 for a
 // runtime leaf size L.
-template <int D, bool COUNT, int LT>
 // Division of a 32-bit value by a run-time constant d, with the multiplier
 // m and shifts s1, s2 prepared on the host (Granlund and Montgomery,
 // "Division by Invariant Integers using Multiplication", PLDI 1994):
@@ -203,6 +202,7 @@ __device__ __forceinline__ uint32_t fastdiv(uint32_t n, FastDiv f) {
   return (t + ((n - t) >> f.s1)) >> f.s2;
 }
 
+template <int D, bool COUNT, int LT>
 __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, uint64_t nItems, uint32_t pstride,
                  uint64_t rows, FastDiv rows_div, const uint32_t* __restrict__ ppos,
                  const float4* __restrict__ nodes, const float4* __restrict__ B, uint64_t nB,
