@@ -128,6 +128,18 @@ class Engine:
         self._check(st)
         return res
 
+    def point_stats(self, P, n_points_cell: int = 10) -> _lib.PointStats:
+        """Bounding box, density and statistics-grid occupancy of one 2-D or
+        3-D point set (hd_compute_stats; the reference's per-file "Grid",
+        "MBR" and "Density" log entries)."""
+        pp, n, d, dev, keep = _as_points(P, "P")
+        out = _lib.PointStats()
+        st = self.lib.hd_compute_stats(self._h, ctypes.c_void_p(pp), n, d, n_points_cell,
+                                       HD_DEVICE_PTRS if dev else 0, ctypes.byref(out))
+        del keep
+        self._check(st)
+        return out
+
     def solve_batch(self, A, B, offsets_a, offsets_b, undirected=False, plain=False):
         """Many independent problems: problem i owns rows offsets_a[i]:offsets_a[i+1]
         of A and offsets_b[i]:offsets_b[i+1] of B.  Returns a structured numpy

@@ -36,7 +36,9 @@ EXPORTED = ["hd_default_options", "hd_create", "hd_destroy", "hd_set_stream",
             "hd_solve", "hd_solve_batch", "hd_solve_batch_offsets", "hd_solve_batch_plain",
             "hd_last_error",
             "hd_status_string", "hd_kernel_launches", "hd_version", "hd_solve_eb_noalloc",
-            "hd_debug_bf16_rowmin"]
+            "hd_debug_bf16_rowmin", "hd_compute_stats"]
+
+HD_STATS_HIST_ROWS = 96
 
 
 class Options(ctypes.Structure):
@@ -47,6 +49,20 @@ class Options(ctypes.Structure):
                 ("batch_small_rows", ctypes.c_uint32), ("batch_chunk", ctypes.c_uint32),
                 ("batch_window", ctypes.c_uint32), ("lbvh_budget", ctypes.c_uint32),
                 ("eb_cap_pairs", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
+
+
+class PointStats(ctypes.Structure):
+    _fields_ = [("n_dims", ctypes.c_int32), ("n_points_cell", ctypes.c_uint32),
+                ("n_points", ctypes.c_uint64), ("lower", ctypes.c_double * 3),
+                ("upper", ctypes.c_double * 3), ("density", ctypes.c_double),
+                ("grid_size", ctypes.c_uint32 * 3), ("max_points", ctypes.c_uint32),
+                ("total_cells", ctypes.c_uint64), ("nonempty_cells", ctypes.c_uint64),
+                ("median_points", ctypes.c_uint32), ("n_hist", ctypes.c_uint32),
+                ("gini_index", ctypes.c_double), ("cell_diagonal", ctypes.c_double),
+                ("build_ms", ctypes.c_double),
+                ("hist_value", ctypes.c_double * HD_STATS_HIST_ROWS),
+                ("hist_percentile", ctypes.c_double * HD_STATS_HIST_ROWS),
+                ("hist_count", ctypes.c_uint64 * HD_STATS_HIST_ROWS)]
 
 
 class Result(ctypes.Structure):
@@ -123,6 +139,9 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.hd_solve_eb_noalloc.restype = ctypes.c_int
     lib.hd_debug_bf16_rowmin.argtypes = [P, P, ctypes.c_uint64, P, ctypes.c_uint64, ctypes.c_int, P]
     lib.hd_debug_bf16_rowmin.restype = ctypes.c_int
+    lib.hd_compute_stats.argtypes = [P, P, ctypes.c_uint64, ctypes.c_int, ctypes.c_uint32,
+                                     ctypes.c_uint32, ctypes.POINTER(PointStats)]
+    lib.hd_compute_stats.restype = ctypes.c_int
     lib.hd_version.argtypes = []
     lib.hd_version.restype = ctypes.c_char_p
     _lib = lib

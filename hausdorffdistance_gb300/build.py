@@ -86,7 +86,9 @@ def build_exec() -> str:
     cuda = os.path.dirname(os.path.dirname(os.path.realpath(_nvcc())))
     libdir = next((d for d in (os.path.join(cuda, "lib64"), os.path.join(cuda, "lib"))
                    if os.path.isdir(d)), os.path.join(cuda, "lib64"))
-    _run(["g++", "-std=c++17", "-O2", "-pthread", f"-I{INCLUDE}", f"-I{HOST}",
+    # -ffp-contract=off: the CPU early-break forms squared distances without
+    # fused multiply-adds, as the reference does.
+    _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-pthread", f"-I{INCLUDE}", f"-I{HOST}",
           f"-I{os.path.join(cuda, 'include')}"] + srcs
          + ["-o", EXE, f"-L{OUT}", "-lhdgpu", f"-L{libdir}", "-lcudart",
             "-Wl,-rpath,$ORIGIN", f"-Wl,-rpath,{libdir}"])

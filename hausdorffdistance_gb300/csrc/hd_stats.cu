@@ -1,0 +1,279 @@
+// Point-set statistics for hd_exec's JSON log (hd_compute_stats in
+// include/hd_gpu.h): bounding box, density, and the occupancy of the
+// reference's statistics grid — the per-file "Grid", "MBR" and "Density"
+// entries of src/run_hausdorff_distance.cu:150-185, whose grid is
+// src/index/uniform_grid.h (CalculateGridResolution :222-244, Insert
+// :343-484, ComputeHistogram :673-693) and whose Gini index is
+// src/running_stats.h:33-62.
+//
+// The counting runs on the device: the box (one atomic per CTA and dimension
+// on order-preserving integers), one counter per grid cell (atomic
+// increments into a dense array), the largest count and the number of
+// non-empty cells, then a histogram of the per-cell counts.  The host turns
+// that histogram into the Gini index, the median and the percentile table:
+// the counts' sorted order is the histogram's order, so nothing is sorted.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "hd_common.cuh"
+#include "hd_internal.h"
+
+namespace hdg {
+namespace {
+
+constexpr uint64_t kStatsMaxCells = 1ull << 28;  // dense counters: at most 1 GiB
+constexpr uint32_t kStatsMaxHist = 1u << 24;     // per-cell counts histogrammed exactly
+
+template <int D>
+__global__ void k_stats_mbr(const float* __restrict__ P, uint64_t n, uint32_t* __restrict__ ord) {
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t) gridDim.x * blockDim.x)
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      const float v = P[i * D + k];
+      lo[k] = fminf(lo[k], v);
+      hi[k] = fmaxf(hi[k], v);
+    }
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    float a = lo[k], b = hi[k];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      a = fminf(a, __shfl_xor_sync(0xFFFFFFFFu, a, o));
+      b = fmaxf(b, __shfl_xor_sync(0xFFFFFFFFu, b, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&ord[k], f2ord(a));
+      atomicMax(&ord[4 + k], f2ord(b));
+    }
+  }
+}
+
+struct StatsGrid {
+  float lo[3], scale[3];  // cell = floor((p - lo) * scale), clamped
+  uint32_t size[3];
+};
+
+template <int D>
+__global__ void k_stats_count(const float* __restrict__ P, uint64_t n, StatsGrid g,
+                              uint32_t* __restrict__ counts) {
+  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t) gridDim.x * blockDim.x) {
+    uint64_t cell = 0;
+#pragma unroll
+    for (int k = D - 1; k >= 0; --k) {
+      float c = floorf((P[i * D + k] - g.lo[k]) * g.scale[k]);
+      c = fminf(fmaxf(c, 0.0f), (float) (g.size[k] - 1));
+      cell = cell * g.size[k] + (uint64_t) c;
+    }
+    atomicAdd(&counts[cell], 1u);
+  }
+}
+
+// Largest count and number of non-empty cells.
+__global__ void k_stats_reduce(const uint32_t* __restrict__ counts, uint64_t cells,
+                               uint32_t* __restrict__ out) {
+  uint32_t mx = 0, ne = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < cells;
+       i += (uint64_t) gridDim.x * blockDim.x) {
+    const uint32_t c = counts[i];
+    mx = max(mx, c);
+    ne += c ? 1u : 0u;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+    ne += __shfl_xor_sync(0xFFFFFFFFu, ne, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&out[0], mx);
+    atomicAdd(&out[1], ne);
+  }
+}
+
+__global__ void k_stats_hist(const uint32_t* __restrict__ counts, uint64_t cells, uint32_t nbins,
+                             uint32_t* __restrict__ hist) {
+  for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < cells;
+       i += (uint64_t) gridDim.x * blockDim.x) {
+    const uint32_t c = counts[i];
+    if (c) atomicAdd(&hist[min(c, nbins - 1)], 1u);
+  }
+}
+
+// Percentile table in the shape HdrHistogram's percentile iteration prints
+// (ticks_per_half_distance ticks in each half of the remaining distance to
+// 100 %), from the histogram of per-cell counts: the value at each
+// percentile, the percentile as a fraction, and the cumulative count there.
+void percentile_table(const std::vector<uint32_t>& hist, uint64_t total, int ticks,
+                      hd_point_stats* out) {
+  out->n_hist = 0;
+  if (total == 0) return;
+  std::vector<uint64_t> cum(hist.size());
+  uint64_t run = 0;
+  for (size_t v = 0; v < hist.size(); ++v) cum[v] = run += hist[v];
+  double p = 0.0;
+  for (int row = 0; row < HD_STATS_HIST_ROWS; ++row) {
+    // The smallest value whose cumulative count reaches p of the total.
+    const uint64_t need = std::max<uint64_t>(1, (uint64_t) std::ceil(p / 100.0 * (double) total));
+    const size_t v = (size_t) (std::lower_bound(cum.begin(), cum.end(), need) - cum.begin());
+    out->hist_value[row] = (double) v;
+    out->hist_percentile[row] = (double) cum[v] / (double) total;
+    out->hist_count[row] = cum[v];
+    out->n_hist = (uint32_t) row + 1;
+    if (cum[v] >= total) break;
+    // Next percentile: the distance to 100 % halves every `ticks` rows.
+    p = 100.0 * (double) cum[v] / (double) total;
+    const double half = std::pow(2.0, std::floor(std::log2(100.0 / std::max(100.0 - p, 1e-12))) + 1);
+    p += 100.0 / (ticks * half);
+    p = std::min(p, 100.0);
+  }
+}
+
+}  // namespace
+}  // namespace hdg
+
+using namespace hdg;
+
+extern "C" hd_status hd_compute_stats(hd_ctx* c, const float* P, uint64_t n, int n_dims,
+                                    uint32_t n_points_cell, uint32_t flags, hd_point_stats* out) {
+  if (!c) return HD_ERR_INVALID_ARG;
+  c->last_error.clear();
+  if (!P || !out || n == 0) return fail(*c, HD_ERR_INVALID_ARG, "null pointer or empty set");
+  if (n_dims != 2 && n_dims != 3)
+    return fail(*c, HD_ERR_UNSUPPORTED, "point statistics need n_dims 2 or 3");
+  if (n_points_cell == 0) return fail(*c, HD_ERR_INVALID_ARG, "n_points_cell must be positive");
+  if (flags & ~HD_DEVICE_PTRS) return fail(*c, HD_ERR_INVALID_ARG, "unknown flag bits");
+  cudaSetDevice(c->device);
+  memset(out, 0, sizeof(*out));
+  out->n_dims = n_dims;
+  out->n_points_cell = n_points_cell;
+  out->n_points = n;
+  hd_status s;
+  cudaError_t e;
+  const float* dP = P;
+  if (!(flags & HD_DEVICE_PTRS)) {
+    void* p;
+    if ((s = ensure(*c, kBufA, (size_t) n * n_dims * 4, &p)) != HD_OK) return s;
+    if ((e = cudaMemcpyAsync(p, P, (size_t) n * n_dims * 4, cudaMemcpyHostToDevice, c->stream)) !=
+        cudaSuccess)
+      return cuda_fail(*c, e, "copy points");
+    dP = (const float*) p;
+  }
+  void* sv;
+  if ((s = ensure(*c, kBufSample, 64, &sv)) != HD_OK) return s;
+  uint32_t* small = (uint32_t*) sv;
+  uint32_t init[16];
+  for (int k = 0; k < 4; ++k) {
+    init[k] = 0xFFFFFFFFu;
+    init[4 + k] = 0u;
+  }
+  for (int k = 8; k < 16; ++k) init[k] = 0u;
+  if ((e = cudaMemcpyAsync(small, init, sizeof(init), cudaMemcpyHostToDevice, c->stream)) !=
+      cudaSuccess)
+    return cuda_fail(*c, e, "stats init");
+  const unsigned g = (unsigned) std::max<uint64_t>(
+      1, std::min<uint64_t>((n + 255) / 256, (uint64_t) c->num_sms * 8));
+  cudaEvent_t t0 = c->ev[24], t1 = c->ev[25];
+  cudaEventRecord(t0, c->stream);
+  if (n_dims == 2)
+    k_stats_mbr<2><<<g, 256, 0, c->stream>>>(dP, n, small);
+  else
+    k_stats_mbr<3><<<g, 256, 0, c->stream>>>(dP, n, small);
+  if ((s = after_launch(*c, "stats_mbr")) != HD_OK) return s;
+  uint32_t ord[8];
+  if ((e = cudaMemcpyAsync(ord, small, sizeof(ord), cudaMemcpyDeviceToHost, c->stream)) !=
+          cudaSuccess ||
+      (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
+    return cuda_fail(*c, e, "stats box");
+  // The reference's resolution rule on the non-empty box (a zero extent
+  // becomes 1e-5): s = (volume * n_points_cell / n)^(1/d), ceil(extent / s)
+  // cells per axis.
+  StatsGrid grid{};
+  double volume = 1.0, ext[3] = {0, 0, 0};
+  for (int k = 0; k < n_dims; ++k) {
+    const double lo = ord2f(ord[k]), hi = ord2f(ord[4 + k]);
+    ext[k] = hi > lo ? hi - lo : 1e-5;
+    out->lower[k] = lo;
+    out->upper[k] = lo + ext[k];
+    volume *= ext[k];
+  }
+  out->density = (double) n / volume;
+  const double side = std::pow(volume * n_points_cell / (double) n, 1.0 / n_dims);
+  uint64_t cells = 1;
+  double diag2 = 0.0;
+  for (int k = 0; k < n_dims; ++k) {
+    const double sz = std::max(1.0, std::ceil(ext[k] / side));
+    if (sz > 4294967295.0) return fail(*c, HD_ERR_UNSUPPORTED, "statistics grid too large");
+    grid.size[k] = (uint32_t) sz;
+    grid.lo[k] = (float) out->lower[k];
+    grid.scale[k] = (float) (sz / ext[k]);
+    out->grid_size[k] = grid.size[k];
+    cells *= grid.size[k];
+    const double unit = ext[k] / sz;
+    diag2 += unit * unit;
+    if (cells > kStatsMaxCells) return fail(*c, HD_ERR_UNSUPPORTED, "statistics grid too large");
+  }
+  out->total_cells = cells;
+  out->cell_diagonal = std::sqrt(diag2);
+  void* cv;
+  if ((s = ensure(*c, kBufKeys, cells * 4, &cv)) != HD_OK) return s;
+  uint32_t* counts = (uint32_t*) cv;
+  if ((e = cudaMemsetAsync(counts, 0, cells * 4, c->stream)) != cudaSuccess)
+    return cuda_fail(*c, e, "stats counts");
+  if (n_dims == 2)
+    k_stats_count<2><<<g, 256, 0, c->stream>>>(dP, n, grid, counts);
+  else
+    k_stats_count<3><<<g, 256, 0, c->stream>>>(dP, n, grid, counts);
+  if ((s = after_launch(*c, "stats_count")) != HD_OK) return s;
+  const unsigned gc = (unsigned) std::max<uint64_t>(
+      1, std::min<uint64_t>((cells + 255) / 256, (uint64_t) c->num_sms * 8));
+  k_stats_reduce<<<gc, 256, 0, c->stream>>>(counts, cells, small + 8);
+  if ((s = after_launch(*c, "stats_reduce")) != HD_OK) return s;
+  cudaEventRecord(t1, c->stream);
+  uint32_t red[2];
+  if ((e = cudaMemcpyAsync(red, small + 8, sizeof(red), cudaMemcpyDeviceToHost, c->stream)) !=
+          cudaSuccess ||
+      (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
+    return cuda_fail(*c, e, "stats reduce");
+  float ms = 0.0f;
+  if (cudaEventElapsedTime(&ms, t0, t1) == cudaSuccess) out->build_ms = ms;
+  out->max_points = red[0];
+  out->nonempty_cells = red[1];
+  const uint32_t nbins = (uint32_t) std::min<uint64_t>((uint64_t) red[0] + 1, kStatsMaxHist);
+  void* hv;
+  if ((s = ensure(*c, kBufVals, (size_t) nbins * 4, &hv)) != HD_OK) return s;
+  if ((e = cudaMemsetAsync(hv, 0, (size_t) nbins * 4, c->stream)) != cudaSuccess)
+    return cuda_fail(*c, e, "stats histogram");
+  k_stats_hist<<<gc, 256, 0, c->stream>>>(counts, cells, nbins, (uint32_t*) hv);
+  if ((s = after_launch(*c, "stats_hist")) != HD_OK) return s;
+  std::vector<uint32_t> hist(nbins);
+  if ((e = cudaMemcpyAsync(hist.data(), hv, (size_t) nbins * 4, cudaMemcpyDeviceToHost,
+                           c->stream)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
+    return cuda_fail(*c, e, "stats histogram");
+  // Gini index over the non-empty cells' counts in ascending order
+  // (sum_i (2i - m + 1) v_i / (m * total), running_stats.h:33-62); values of
+  // equal count occupy consecutive ranks, so each histogram bin adds its
+  // value times the sum of its ranks' weights.
+  const double m = (double) out->nonempty_cells;
+  double total = 0.0, weighted = 0.0, rank = 0.0;
+  uint32_t median = 0;
+  const uint64_t median_rank = out->nonempty_cells / 2;
+  for (uint32_t v = 1; v < nbins; ++v) {
+    const double cnt = hist[v];
+    if (cnt == 0) continue;
+    const double w = cnt * (2.0 * rank + cnt - 1.0) - cnt * (m - 1.0);
+    weighted += w * v;
+    total += cnt * v;
+    if ((uint64_t) rank <= median_rank && median_rank < (uint64_t) (rank + cnt)) median = v;
+    rank += cnt;
+  }
+  out->gini_index = (m > 0 && total > 0) ? weighted / (m * total) : 0.0;
+  out->median_points = median;
+  percentile_table(hist, out->nonempty_cells, 3, out);
+  return HD_OK;
+}

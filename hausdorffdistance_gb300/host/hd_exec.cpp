@@ -3,13 +3,17 @@
 // over libhdgpu.so.  Prints "Time: <avg> ms" and
 // "HausdorffDistance: distance is <d>" and writes the reference's JSON keys.
 //
-// Differences: -execution cpu is not offered (this is the GPU engine; the
-// reference's own build provides its CPU path); -check verifies the result
-// against the engine's plain early-break variant (same exact FP32
-// semantics) instead of the CPU early-break; -undirected computes
-// max(h(A,B), h(B,A)) in one call; -input_type also accepts "bin" (the
-// reference's point-cache layout); -variant accepts eb | hybrid | auto | rt |
-// lbvh | grid | bf16 | brute.
+// -execution cpu runs the CPU early-break of cpu_early_break.h (the
+// reference's CPU path, on -parallelism threads, every host thread when it is
+// not positive), and -check re-runs it on all host threads and compares, as the
+// reference does (run_hausdorff_distance.cu:366-389).  Each file, and both
+// together, get the reference's "Grid", "MBR" and "Density" statistics
+// (run_hausdorff_distance.cu:150-185) from hd_compute_stats on the GPU.
+// Differences: -undirected computes max(h(A,B), h(B,A)) in one call;
+// -input_type also accepts "bin" (the reference's point-cache layout);
+// -variant accepts eb | hybrid | auto | rt | lbvh | grid | bf16 | brute; the
+// grid statistics' "NonEmptyCells" is the non-empty fraction as a real number
+// (the reference divides two integers there, which truncates it to 0).
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -22,8 +26,10 @@
 #include <map>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
+#include "cpu_early_break.h"
 #include "hausdorff_distance.h"
 #include "hd_gpu.h"
 #include "json.h"
@@ -109,10 +115,10 @@ std::string now_string() {
 void usage(const char* argv0) {
   std::fprintf(stderr,
                "Usage: %s -input1 A -input2 B -input_type wkt|off|ply|bin -n_dims 2|3|<d> "
-               "[-variant eb|hybrid|rt|lbvh|grid|bf16|brute] [-execution gpu] [-repeat 5] "
+               "[-variant eb|hybrid|rt|lbvh|grid|bf16|brute] [-execution gpu|cpu] [-repeat 5] "
                "[-seed 0] [-check] [-json out.json] [-serialize dir] [-limit n] [-normalize] "
                "[-translate r] [-undirected] [-sample_rate 0.01] [-n_points_cell 8] "
-               "[-eb_only_threshold 0] [-device 0]\n",
+               "[-eb_only_threshold 0] [-device 0] [-parallelism n] [-stats_n_points_cell 10]\n",
                argv0);
 }
 
@@ -152,10 +158,9 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "double inputs are not supported (the engine computes in float32)\n");
     return 1;
   }
-  if (lower(fl.get("execution", "gpu")) != "gpu") {
-    std::fprintf(stderr,
-                 "-execution cpu: this driver runs the GPU engine only; the reference's own "
-                 "build provides the CPU early-break path\n");
+  const std::string execution = lower(fl.get("execution", "gpu"));
+  if (execution != "gpu" && execution != "cpu") {
+    std::fprintf(stderr, "Unknown execution: %s\n", execution.c_str());
     return 1;
   }
   const std::string vname = lower(fl.get("variant", "eb"));
@@ -214,12 +219,17 @@ int main(int argc, char** argv) {
   hd::Json stats = hd::Json::Object();
   int dev = opt.device;
   cudaDeviceProp prop;
-  if (cudaSetDevice(dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+  // -execution cpu runs without a GPU too (then without the GPU statistics).
+  const bool have_gpu =
+      cudaSetDevice(dev) == cudaSuccess && cudaGetDeviceProperties(&prop, dev) == cudaSuccess;
+  if (!have_gpu && execution == "gpu") {
     std::fprintf(stderr, "no CUDA device %d\n", dev);
     return 1;
   }
-  stats["GPU"]["Device"] = dev;
-  stats["GPU"]["name"] = prop.name;
+  if (have_gpu) {
+    stats["GPU"]["Device"] = dev;
+    stats["GPU"]["name"] = prop.name;
+  }
   stats["DateTime"] = now_string();
   hd::Json& input = stats["Input"];
   hd::Json files = hd::Json::Array();
@@ -238,13 +248,73 @@ int main(int argc, char** argv) {
   input["NumDims"] = dims;
   input["Type"] = "Float";
 
+  // Per-file and combined point statistics on the GPU (the reference's
+  // write_points_stats).
+  const uint32_t stats_npc = (uint32_t) std::max<long long>(1, fl.geti("stats_n_points_cell", 10));
+  if (have_gpu && (dims == 2 || dims == 3)) {
+    hd_ctx* sctx = nullptr;
+    if (hd_create(&sctx, &opt) != HD_OK) {
+      std::fprintf(stderr, "hd_create failed\n");
+      return 1;
+    }
+    auto write_stats = [&](hd::Json& j, const std::vector<float>& xyz) -> bool {
+      hd_point_stats ps;
+      const hd_status st = hd_compute_stats(sctx, xyz.data(), xyz.size() / dims, dims, stats_npc,
+                                            0u, &ps);
+      if (st != HD_OK) {
+        std::fprintf(stderr, "hd_compute_stats: %s: %s\n", hd_status_string(st),
+                     hd_last_error(sctx));
+        return false;
+      }
+      hd::Json grid = hd::Json::Object();
+      grid["TotalCells"] = (unsigned long long) ps.total_cells;
+      grid["NonEmptyCells"] = (double) ps.nonempty_cells / (double) ps.total_cells;
+      grid["MaxPoints"] = (unsigned long long) ps.max_points;
+      grid["GiniIndex"] = ps.gini_index;
+      grid["BuildTime"] = ps.build_ms;
+      hd::Json gsize = hd::Json::Array();
+      for (int k = 0; k < dims; ++k) gsize.push_back((unsigned long long) ps.grid_size[k]);
+      grid["GridSize"] = gsize;
+      grid["CellDiagonalLength"] = ps.cell_diagonal;
+      grid["MedianPointsPerCell"] = (unsigned long long) ps.median_points;
+      hd::Json hist = hd::Json::Array();
+      for (uint32_t r = 0; r < ps.n_hist; ++r) {
+        hd::Json row = hd::Json::Object();
+        row["value"] = ps.hist_value[r];
+        row["percentile"] = ps.hist_percentile[r];
+        row["count"] = (unsigned long long) ps.hist_count[r];
+        hist.push_back(row);
+      }
+      grid["Histogram"] = hist;
+      j["Grid"] = grid;
+      j["StatsGridNumPointsPerCell"] = (unsigned long long) stats_npc;
+      hd::Json mbr = hd::Json::Array();
+      for (int k = 0; k < dims; ++k) {
+        hd::Json e = hd::Json::Object();
+        e["Lower"] = ps.lower[k];
+        e["Upper"] = ps.upper[k];
+        mbr.push_back(e);
+      }
+      j["MBR"] = mbr;
+      j["Density"] = ps.density;
+      return true;
+    };
+    hd::Json& jf = input["Files"];
+    std::vector<float> both = pa.xyz;
+    both.insert(both.end(), pb.xyz.begin(), pb.xyz.end());
+    const bool ok = write_stats(jf.element(0), pa.xyz) && write_stats(jf.element(1), pb.xyz) &&
+                    write_stats(input, both);
+    hd_destroy(sctx);
+    if (!ok) return 1;
+  }
+
   // Inputs go to the device once, before the repeat loop, as in the
   // reference (run_hausdorff_distance.cu:148); ReportedTime excludes them.
   float *dA = nullptr, *dB = nullptr;
-  if (cudaMalloc(&dA, pa.xyz.size() * 4) != cudaSuccess ||
+  if (have_gpu && (cudaMalloc(&dA, pa.xyz.size() * 4) != cudaSuccess ||
       cudaMalloc(&dB, pb.xyz.size() * 4) != cudaSuccess ||
       cudaMemcpy(dA, pa.xyz.data(), pa.xyz.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(dB, pb.xyz.data(), pb.xyz.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaMemcpy(dB, pb.xyz.data(), pb.xyz.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)) {
     std::fprintf(stderr, "device allocation or copy failed\n");
     return 1;
   }
@@ -298,7 +368,64 @@ int main(int argc, char** argv) {
     return 0;
   };
 
+  // The CPU early-break on all host threads (or -parallelism of them); both
+  // directions for -undirected.
+  auto cpu_distance = [&](unsigned threads, double* compute_ms, unsigned long long* pairs) {
+    hd::CpuEarlyBreakResult ab = hd::CpuEarlyBreak(pa.xyz.data(), pa.size(), pb.xyz.data(),
+                                                   pb.size(), dims, (uint32_t) opt.seed, threads);
+    float d = ab.distance;
+    *compute_ms = ab.compute_ms;
+    *pairs = ab.compared_pairs;
+    if (undirected) {
+      hd::CpuEarlyBreakResult ba = hd::CpuEarlyBreak(pb.xyz.data(), pb.size(), pa.xyz.data(),
+                                                     pa.size(), dims, (uint32_t) opt.seed, threads);
+      d = std::max(d, ba.distance);
+      *compute_ms += ba.compute_ms;
+      *pairs += ba.compared_pairs;
+    }
+    return d;
+  };
+  const long long parallelism = fl.geti("parallelism", -1);
+  const unsigned all_threads = std::max(1u, std::thread::hardware_concurrency());
+  const unsigned cpu_threads = parallelism > 0 ? (unsigned) parallelism : all_threads;
+
   const std::string json_path = fl.get("json", "");
+  if (execution == "cpu") {
+    hd::Json& run_json = stats["Running"];
+    hd::Json repeats = hd::Json::Array();
+    double total = 0.0;
+    float dist = 0.0f;
+    for (int i = 0; i < repeat; ++i) {
+      double ms = 0.0;
+      unsigned long long pairs = 0;
+      dist = cpu_distance(cpu_threads, &ms, &pairs);
+      hd::Json rep = hd::Json::Object();
+      rep["Repeat"] = i + 1;
+      rep["Algorithm"] = "Early Break";
+      rep["Execution"] = "CPU";
+      rep["Threads"] = (unsigned long long) cpu_threads;
+      rep["ComparedPairs"] = pairs;
+      rep["ReportedTime"] = ms;
+      total += ms;
+      repeats.push_back(rep);
+    }
+    run_json["Seed"] = (unsigned long long) opt.seed;
+    run_json["Undirected"] = undirected;
+    run_json["Repeats"] = repeats;
+    run_json["AvgTime"] = total / repeat;
+    stats["HDResult"] = dist;
+    std::printf("Time: %f ms\n", total / repeat);
+    std::printf("HausdorffDistance: distance is %.9g\n", dist);
+    if (!json_path.empty()) {
+      const bool exists = access(json_path.c_str(), R_OK) == 0;
+      if (!exists || fl.getb("overwrite", false)) std::ofstream(json_path) << stats.dump(4);
+    }
+    if (have_gpu) {
+      cudaFree(dA);
+      cudaFree(dB);
+    }
+    return 0;
+  }
   if (fl.getb("vary_params", false)) {
     // Parameter sweep over the selector's knobs (the reference's
     // autotune_hausdorff_distance.cu:208-299), one JSON file per combination.
@@ -331,24 +458,17 @@ int main(int argc, char** argv) {
   std::printf("HausdorffDistance: distance is %.9g\n", dist);
 
   if (check) {
-    // Same exact FP32 semantics through the plain early-break kernel.
-    hd_ctx* ctx = nullptr;
-    hd_options o = opt;
-    o.variant = HD_VARIANT_EB;
-    hd_result r{};
-    if (hd_create(&ctx, &o) != HD_OK ||
-        hd_solve(ctx, dA, pa.size(), dB, pb.size(), dims,
-                 HD_DEVICE_PTRS | (undirected ? HD_UNDIRECTED : 0u), HD_VARIANT_EB, &r) != HD_OK) {
-      std::fprintf(stderr, "check solve failed\n");
-      return 1;
-    }
-    hd_destroy(ctx);
+    // The reference re-runs its CPU early-break on every host thread.
+    double ms = 0.0;
+    unsigned long long pairs = 0;
+    const float answer = cpu_distance(all_threads, &ms, &pairs);
     hd::Json& ck = stats["Check"];
-    ck["HDAnswer"] = r.hd_f32;
-    ck["Diff"] = (double) r.hd_f32 - (double) dist;
-    ck["Pass"] = r.hd_f32 == dist;
-    if (r.hd_f32 != dist) {
-      std::fprintf(stderr, "Wrong HausdorffDistance. Result: %.8f Answer: %.8f\n", dist, r.hd_f32);
+    ck["HDAnswer"] = answer;
+    ck["Diff"] = (double) answer - (double) dist;
+    ck["Pass"] = answer == dist;
+    if (answer != dist) {
+      std::fprintf(stderr, "Wrong HausdorffDistance. Result: %.8f Answer: %.8f Diff: %.8f\n", dist,
+                   answer, (double) answer - (double) dist);
     } else {
       std::printf("HausdorffDistance is checked\n");
     }

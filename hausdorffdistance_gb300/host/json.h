@@ -65,6 +65,8 @@ class Json {
     arr_.push_back(v);
   }
   Json& back() { return arr_.back(); }
+  // Element i of an array (which must hold more than i elements).
+  Json& element(size_t i) { return arr_.at(i); }
   void update(const Json& other) {
     for (auto& kv : other.obj_) (*this)[kv.first] = kv.second;
   }

@@ -139,6 +139,31 @@ typedef struct hd_batch_result {
   int32_t direction;
 } hd_batch_result;
 
+/* Statistics of one point set (hd_compute_stats): the per-file "Grid", "MBR"
+ * and "Density" entries the reference writes to its JSON log
+ * (src/run_hausdorff_distance.cu:150-185). */
+#define HD_STATS_HIST_ROWS 96
+typedef struct hd_point_stats {
+  int32_t n_dims;              /* 2 or 3                                        */
+  uint32_t n_points_cell;      /* target points per cell of the statistics grid */
+  uint64_t n_points;
+  double lower[3], upper[3];   /* bounding box (a zero extent widened to 1e-5)  */
+  double density;              /* n_points / box volume                         */
+  uint32_t grid_size[3];       /* cells per axis: ceil(extent / s),             */
+                               /* s = (volume * n_points_cell / n)^(1/d)        */
+  uint32_t max_points;         /* most points in one cell                      */
+  uint64_t total_cells;
+  uint64_t nonempty_cells;
+  uint32_t median_points;      /* median count over the non-empty cells        */
+  uint32_t n_hist;             /* rows of the percentile table below           */
+  double gini_index;           /* Gini index of the non-empty cells' counts    */
+  double cell_diagonal;        /* length of a cell's diagonal                  */
+  double build_ms;             /* device time of the box and cell counts       */
+  double hist_value[HD_STATS_HIST_ROWS];      /* points per cell at ...         */
+  double hist_percentile[HD_STATS_HIST_ROWS]; /* ... this fraction of the cells */
+  uint64_t hist_count[HD_STATS_HIST_ROWS];    /* cells at or below the value    */
+} hd_point_stats;
+
 typedef struct hd_ctx hd_ctx;
 
 /* Fills *opt with defaults (device 0, AUTO, seed 0, sample_rate 0.01,
@@ -232,6 +257,16 @@ HD_API hd_status hd_solve_eb_noalloc(const float* A, uint64_t n_a, const float* 
 HD_API hd_status hd_debug_bf16_rowmin(hd_ctx* ctx, const float* A, uint64_t n_a,
                                       const float* B, uint64_t n_b, int n_dims,
                                       float* rowmin_out);
+
+/* Bounding box, density and the occupancy of the reference's statistics
+ * grid (n_points_cell points per cell on average) of one 2-D or 3-D point set,
+ * host or device pointer (HD_DEVICE_PTRS), computed on the device.  Replaces
+ * the per-file statistics pass of src/run_hausdorff_distance.cu:150-185
+ * (UniformGrid::Insert and ComputeHistogram, src/index/uniform_grid.h:343-484,
+ * 673-693, and gini_index_thrust, src/running_stats.h:33-62).  Grids of more
+ * than 2^28 cells return HD_ERR_UNSUPPORTED. */
+HD_API hd_status hd_compute_stats(hd_ctx* ctx, const float* points, uint64_t n, int n_dims,
+                                uint32_t n_points_cell, uint32_t flags, hd_point_stats* out);
 
 /* Message for the last failing call on this context (never NULL). */
 HD_API const char* hd_last_error(hd_ctx* ctx);

@@ -55,3 +55,36 @@ def test_no_device_is_reported_loudly(built_lib):
     with pytest.raises(hd.HDError) as ei:
         hd.Engine()
     assert ei.value.status == 6
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of hd_result, hd_options and hd_point_stats have the
+    sizes and field offsets the C compiler gives the header's structs."""
+    import shutil
+    import subprocess
+    from hausdorffdistance_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    include = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    checks = [("hd_result", _lib.Result), ("hd_options", _lib.Options),
+              ("hd_point_stats", _lib.PointStats)]
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "hd_gpu.h"', 'int main(void) {']
+    for cname, ct in checks:
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in ct._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", include, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    got = {}
+    for ln in out.splitlines():
+        c, f, v = ln.split()
+        got[(c, f)] = int(v)
+    for cname, ct in checks:
+        assert got[(cname, "size")] == ctypes.sizeof(ct), cname
+        for fname, _ in ct._fields_:
+            assert got[(cname, fname)] == getattr(ct, fname).offset, (cname, fname)

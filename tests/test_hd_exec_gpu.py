@@ -26,12 +26,33 @@ def bits(x):
     return int(np.float32(x).view(np.uint32))
 
 
-def test_cpu_execution_and_bad_flags_rejected(exe):
+@pytest.mark.parametrize("case", GOLDEN, ids=[c["name"] for c in GOLDEN])
+def test_cpu_execution_matches_reference_golden(exe, case, tmp_path):
+    """-execution cpu (the driver's CPU early-break, product code written
+    apart from the oracle) gives the reference's own CPU result bit for bit
+    and, on one thread, its compared-pair count (which pins the seeded
+    shuffle and the break rule).  Needs no GPU."""
+    out = tmp_path / "run.json"
+    r = subprocess.run([exe, "-input1", os.path.join(HERE, "golden", case["a"]), "-input2",
+                        os.path.join(HERE, "golden", case["b"]), "-input_type", "bin",
+                        "-n_dims", str(case["dims"]), "-execution", "cpu", "-repeat", "1",
+                        "-parallelism", "1", "-seed", str(case["seed"]), "-json", str(out)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    st = json.load(open(out))
+    assert bits(st["HDResult"]) == case["hd_bits"]
+    rep = st["Running"]["Repeats"][0]
+    assert rep["Execution"] == "CPU" and rep["Algorithm"] == "Early Break"
+    assert rep["ComparedPairs"] == case["compared_pairs_t1"]
+
+
+def test_bad_flags_rejected(exe):
     c = GOLDEN[0]
     base = [exe, "-input1", os.path.join(HERE, "golden", c["a"]), "-input2",
             os.path.join(HERE, "golden", c["b"]), "-n_dims", str(c["dims"])]
-    r = subprocess.run(base + ["-input_type", "bin", "-execution", "cpu"], capture_output=True, text=True)
-    assert r.returncode == 1 and "GPU engine only" in r.stderr
+    r = subprocess.run(base + ["-input_type", "bin", "-execution", "tpu"], capture_output=True,
+                       text=True)
+    assert r.returncode == 1 and "Unknown execution" in r.stderr
     r = subprocess.run(base + ["-input_type", "shp"], capture_output=True, text=True)
     assert r.returncode == 1 and "Unsupported input type" in r.stderr
     r = subprocess.run(base + ["-input_type", "bin", "-variant", "itk"], capture_output=True, text=True)
