@@ -33,18 +33,18 @@ __all__ = ["Engine", "HDError", "HausdorffDistance", "HausdorffDistanceEarlyBrea
            "HausdorffDistanceBrute", "solve"]
 
 
-def _as_points(x, name):
+def _as_points(x, name, dtype="float32"):
     """Returns (pointer, n, dims, is_device, keepalive) for a numpy array or a
-    CUDA torch tensor of shape (n, dims)."""
+    CUDA torch tensor of shape (n, dims) (dtype float32, or float64)."""
     mod = type(x).__module__
     if mod.startswith("torch"):
-        if x.dtype.is_floating_point is False or str(x.dtype) != "torch.float32":
-            raise TypeError(f"{name} must be float32")
+        if str(x.dtype) != "torch." + dtype:
+            raise TypeError(f"{name} must be {dtype}")
         if x.dim() != 2:
             raise ValueError(f"{name} must have shape (n, n_dims)")
         x = x.contiguous()
         return x.data_ptr(), x.shape[0], x.shape[1], x.is_cuda, x
-    a = np.ascontiguousarray(x, dtype=np.float32)
+    a = np.ascontiguousarray(x, dtype=np.float32 if dtype == "float32" else np.float64)
     if a.ndim != 2:
         raise ValueError(f"{name} must have shape (n, n_dims)")
     return a.ctypes.data, a.shape[0], a.shape[1], False, a
@@ -128,6 +128,28 @@ class Engine:
         self._check(st)
         return res
 
+    def solve_f64(self, A, B, undirected: bool = False, variant: str | int | None = None,
+                  count_pairs: bool = False, timing: bool = False) -> _lib.Result:
+        """Exact FP64 Hausdorff distance of float64 point sets (hd_solve_f64:
+        the reference's double instantiations behind its disabled -is_double
+        switch).  variant: auto, lbvh, eb or brute."""
+        pa, na, da, deva, ka = _as_points(A, "A", "float64")
+        pb, nb, db, devb, kb = _as_points(B, "B", "float64")
+        if da != db:
+            raise ValueError("A and B must have the same n_dims")
+        if deva != devb:
+            raise ValueError("A and B must both be host arrays or both device tensors")
+        flags = (HD_UNDIRECTED if undirected else 0) | (HD_DEVICE_PTRS if deva else 0)
+        flags |= (HD_COUNT_PAIRS if count_pairs else 0) | (HD_TIMING if timing else 0)
+        v = -1 if variant is None else (VARIANTS[variant] if isinstance(variant, str)
+                                        else int(variant))
+        res = _lib.Result()
+        st = self.lib.hd_solve_f64(self._h, ctypes.c_void_p(pa), na, ctypes.c_void_p(pb), nb,
+                                   da, flags, v, ctypes.byref(res))
+        del ka, kb
+        self._check(st)
+        return res
+
     def point_stats(self, P, n_points_cell: int = 10) -> _lib.PointStats:
         """Bounding box, density and statistics-grid occupancy of one 2-D or
         3-D point set (hd_compute_stats; the reference's per-file "Grid",
@@ -188,21 +210,26 @@ class HausdorffDistance:
     h(A,B) as float32 (bit-identical to the reference's -execution=cpu
     result); the inputs may be numpy arrays (host, copied to the device
     inside the call) or CUDA float32 torch tensors (the reference's
-    device_vector overload).  ``get_stats()`` returns the per-call stats with
+    device_vector overload).  ``coord_type="float64"`` is the COORD_T =
+    double instantiation: float64 inputs, the exact FP64 distance as
+    float64 (hd_solve_f64).  ``get_stats()`` returns the per-call stats with
     the keys the reference requires."""
 
     algorithm = "?"
     variant = "auto"
 
-    def __init__(self, seed: int = 0, device: int = 0, **kw):
+    def __init__(self, seed: int = 0, device: int = 0, coord_type: str = "float32", **kw):
+        if coord_type not in ("float32", "float64"):
+            raise ValueError("coord_type is float32 or float64")
+        self.coord_type = coord_type
         self._engine = Engine(device=device, variant=self.variant, seed=seed, **kw)
         self.stats_: dict = {}
         self.last_result: _lib.Result | None = None
 
     def CalculateDistance(self, points_a, points_b, undirected: bool = False):
         t0 = time.perf_counter()
-        res = self._engine.solve(points_a, points_b, undirected=undirected,
-                                 count_pairs=True, timing=True)
+        solve = self._engine.solve_f64 if self.coord_type == "float64" else self._engine.solve
+        res = solve(points_a, points_b, undirected=undirected, count_pairs=True, timing=True)
         wall_ms = (time.perf_counter() - t0) * 1e3
         self.last_result = res
         on_device = type(points_a).__module__.startswith("torch") and points_a.is_cuda
@@ -219,7 +246,7 @@ class HausdorffDistance:
             "CertifyingPair": [int(res.ia), int(res.ib)],
             "Direction": int(res.direction),
         }
-        return np.float32(res.hd_f32)
+        return np.float64(res.hd) if self.coord_type == "float64" else np.float32(res.hd_f32)
 
     def get_stats(self) -> dict:
         for k in ("Algorithm", "Execution", "ReportedTime"):

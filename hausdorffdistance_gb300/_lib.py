@@ -33,7 +33,7 @@ HD_TIMING = 8
 
 # Every symbol include/hd_gpu.h declares.
 EXPORTED = ["hd_default_options", "hd_create", "hd_destroy", "hd_set_stream",
-            "hd_solve", "hd_solve_batch", "hd_solve_batch_offsets", "hd_solve_batch_plain",
+            "hd_solve", "hd_solve_f64", "hd_solve_batch", "hd_solve_batch_offsets", "hd_solve_batch_plain",
             "hd_last_error",
             "hd_status_string", "hd_kernel_launches", "hd_version", "hd_solve_eb_noalloc",
             "hd_debug_bf16_rowmin", "hd_compute_stats"]
@@ -118,6 +118,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.hd_solve.argtypes = [P, P, ctypes.c_uint64, P, ctypes.c_uint64, ctypes.c_int,
                              ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(Result)]
     lib.hd_solve.restype = ctypes.c_int
+    lib.hd_solve_f64.argtypes = lib.hd_solve.argtypes
+    lib.hd_solve_f64.restype = ctypes.c_int
     for name in ("hd_solve_batch", "hd_solve_batch_plain"):
         f = getattr(lib, name)
         f.argtypes = [P, P, ctypes.c_uint64, P, ctypes.c_uint64, ctypes.c_int,

@@ -82,6 +82,10 @@ enum BufSlot {
   kBufBatch,
   kBufBatch2,
   kBufGroupOffs,  // offsets of a grouped host-input batch (device copy)
+  kBufF64A,       // FP64 input path: caller's double A / B on the device
+  kBufF64B,
+  kBufF64Aux,     // FP64 scalars, frozen-pass scalars, candidate lists
+  kBufF64Rows,    // FP64 nearest distance and column of every walked row
   kNumBufs
 };
 
@@ -271,9 +275,45 @@ hd_status select_variants(Ctx& c, const DirInput* ins, int ndir, int* v);
 // data); false when it needs the sample pass.
 bool select_variant_by_size(const Ctx& c, uint64_t nA, uint64_t nB, int dims, int* variant);
 
+// FP64 input path (hd_f64.cu) and its hooks into the LBVH solve.
+// A row of a list: the caller's row index and its FP32 nearest squared
+// distance over the rounded sets (float bits).
+struct RowEntry {
+  uint32_t row;
+  uint32_t min32;
+};
+// A built tree of one direction's target set: packed nodes, the root's
+// index (device), the Morton-sorted points (float4 x, y, z, caller index)
+// in leaves of `leaf` points.
+struct LbvhTree {
+  const float4* nodes;
+  const uint32_t* root;
+  const float4* pts;
+  uint64_t n;
+  uint32_t leaf;
+};
+// run_lbvh_f64 solves the rounded sets in FP32, records each direction's
+// tree, calls f64_seed (which leaves frozen[k]->max_key at direction k's
+// frozen threshold), then re-runs the query pass with those scalars: rows
+// that stay open are listed in cand[k] (count in *cand_count[k], at most
+// cand_cap stored).
+struct F64Plan {
+  LbvhTree tree[2];
+  DevScalars* frozen[2];
+  RowEntry* cand[2];
+  uint32_t* cand_count[2];
+  uint32_t cand_cap;
+  void* state;  // the FP64 solve's own data (hd_f64.cu)
+};
+hd_status run_lbvh_f64(Ctx& c, const DirInput* ins, int count, F64Plan* plan);
+hd_status f64_seed(Ctx& c, F64Plan& plan, int count);
+
 // Common tail: exact argmin of A[ia] over B, FP64 recomputation, written to
 // DevScalars[dir].  Used by every variant.
 hd_status certify(Ctx& c, const DirInput& in);
+
+// Resets both directions' DevScalars (allocating the scalars buffer).
+hd_status init_scalars(Ctx& c);
 
 // Context-free forms used by hd_solve_eb_noalloc.
 cudaError_t certify_on_stream(cudaStream_t st, int num_sms, const float* A, const float* B,

@@ -207,7 +207,8 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
                  uint64_t rows, FastDiv rows_div, const uint32_t* __restrict__ ppos,
                  const float4* __restrict__ nodes, const float4* __restrict__ B, uint64_t nB,
                  uint32_t L, DevScalars* sc, Deferred* __restrict__ defer, uint32_t budget,
-                 uint32_t root) {
+                 uint32_t root, RowEntry* __restrict__ cand, uint32_t* cand_count,
+                 uint32_t cand_cap) {
   __shared__ uint32_t stk[kQueryWarps][kStack];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // Packets (32 consecutive Morton-sorted queries) are visited in a
@@ -395,7 +396,21 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
     const bool want = active && dstk[sp] < cmin;
     have = __any_sync(0xFFFFFFFFu, want);
   }
-  if (active) atomicMax(&sc->max_key, pack_max(cmin, __float_as_uint(q.w)));
+  if (cand) {
+    // Frozen-threshold pass (FP64 refinement): the running maximum is never
+    // raised; the rows still open are listed with their FP32 minima.
+    const unsigned open = __ballot_sync(0xFFFFFFFFu, active);
+    if (open) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(cand_count, (uint32_t) __popc(open));
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      const uint32_t slot = base + __popc(open & ((1u << lane) - 1u));
+      if (active && slot < cand_cap)
+        cand[slot] = RowEntry{__float_as_uint(q.w), __float_as_uint(cmin)};
+    }
+  } else if (active) {
+    atomicMax(&sc->max_key, pack_max(cmin, __float_as_uint(q.w)));
+  }
   if (COUNT && lane == 0) {
     atomicAdd(&sc->pairs, pairs);
     atomicAdd(&sc->nodes, visits);
@@ -478,6 +493,11 @@ struct QuerySet {
   const Frame* tframe;      // frame of the target set's codes
   const uint32_t* qcodes;   // the query set's sorted codes when in that frame, else null
   const uint32_t* bcodes;
+  // Frozen-threshold pass only (else null): open rows are listed here
+  // instead of raising the maximum.
+  RowEntry* cand;
+  uint32_t* cand_count;
+  uint32_t cand_cap;
 };
 struct QuerySets {
   QuerySet d[2];
@@ -487,8 +507,8 @@ template <int D, bool COUNT, int LT>
 __global__ void __launch_bounds__(kQueryWarps * 32) k_lbvh_query(QuerySets qs) {
   const QuerySet& S = qs.d[blockIdx.y];
   lbvh_query_body<D, COUNT, LT>(S.Q, S.nQ, S.pstride, S.rows, S.rows_div, S.ppos, S.nodes, S.B,
-                                S.nB, S.L, S.sc,
-                            S.defer, S.budget, *S.root);
+                                S.nB, S.L, S.sc, S.defer, S.budget, *S.root, S.cand,
+                                S.cand_count, S.cand_cap);
 }
 
 // Deferred pass: one warp per queued query walks the tree with 32 stack
@@ -589,8 +609,14 @@ __global__ void __launch_bounds__(kDeferWarps * 32) k_lbvh_defer(QuerySets qs) {
       __syncwarp();
       if ((++round & 15) == 0) thr = read_thr();
     }
-    if (lane == 0 && m > threshold_of(ld_relaxed_u64(&S.sc->max_key)))
-      atomicMax(&S.sc->max_key, pack_max(m, __float_as_uint(q.w)));
+    if (lane == 0 && m > threshold_of(ld_relaxed_u64(&S.sc->max_key))) {
+      if (S.cand) {
+        const uint32_t slot = atomicAdd(S.cand_count, 1u);
+        if (slot < S.cand_cap) S.cand[slot] = RowEntry{__float_as_uint(q.w), __float_as_uint(m)};
+      } else {
+        atomicMax(&S.sc->max_key, pack_max(m, __float_as_uint(q.w)));
+      }
+    }
     __syncwarp();
   }
   if (COUNT) {
@@ -667,8 +693,11 @@ static hd_status build_lbvhs(Ctx& c, const SortedSet* const* sets, int count, Bu
 }
 
 // Directed LBVH solves of `count` directions (1, or 2 for an undirected solve)
-// with shared launches.
-static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
+// with shared launches.  With a plan (the FP64 input path), the certified
+// FP32 solve is followed by f64_seed and a second query pass over the same
+// trees with the plan's frozen thresholds, which lists the rows that stay
+// open.
+static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count, F64Plan* plan) {
   const int dims = ins[0].dims;
   if (dims != 2 && dims != 3) return fail(c, HD_ERR_UNSUPPORTED, "LBVH needs n_dims 2 or 3");
   hd_status s;
@@ -700,6 +729,9 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
     d.tframe = t[k]->frame;
     d.qcodes = q[k]->frame == t[k]->frame ? q[k]->codes : nullptr;
     d.bcodes = t[k]->codes;
+    d.cand = nullptr;
+    d.cand_count = nullptr;
+    d.cand_cap = 0;
     off += 2 * packets[k];
     max_pos_threads = std::max<uint64_t>(max_pos_threads, 2 * packets[k]);
   }
@@ -737,45 +769,66 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count) {
   if (count == 1) qs.d[1] = qs.d[0];
   mark(c, 3);
   const dim3 grid((unsigned) ((max_warps + kQueryWarps - 1) / kQueryWarps), count);
-  const bool cnt = ins[0].count;
   // Kernel per (n_dims, counting, leaf size 16 or any).
   const bool l16 = bs.s[0].L == 16;
-  const void* fn;
-  if (dims == 2)
-    fn = cnt ? (l16 ? (const void*) k_lbvh_query<2, true, 16> : (const void*) k_lbvh_query<2, true, 0>)
-             : (l16 ? (const void*) k_lbvh_query<2, false, 16> : (const void*) k_lbvh_query<2, false, 0>);
-  else
-    fn = cnt ? (l16 ? (const void*) k_lbvh_query<3, true, 16> : (const void*) k_lbvh_query<3, true, 0>)
-             : (l16 ? (const void*) k_lbvh_query<3, false, 16> : (const void*) k_lbvh_query<3, false, 0>);
-  void* qargs[] = {&qs};
-  cudaLaunchKernel(fn, grid, dim3(kQueryWarps * 32), qargs, 0, c.stream);
-  if ((s = after_launch(c, "lbvh_query")) != HD_OK) return s;
-  // Queries queued by over-budget packets (usually none: the launch then
-  // returns at once).
-  const dim3 dgrid((unsigned) (c.num_sms * 4), count);
-  if (dims == 2) {
-    if (cnt)
-      k_lbvh_defer<2, true><<<dgrid, kDeferWarps * 32, 0, c.stream>>>(qs);
+  auto launch_queries = [&](bool cnt) -> hd_status {
+    const void* fn;
+    if (dims == 2)
+      fn = cnt ? (l16 ? (const void*) k_lbvh_query<2, true, 16> : (const void*) k_lbvh_query<2, true, 0>)
+               : (l16 ? (const void*) k_lbvh_query<2, false, 16> : (const void*) k_lbvh_query<2, false, 0>);
     else
-      k_lbvh_defer<2, false><<<dgrid, kDeferWarps * 32, 0, c.stream>>>(qs);
-  } else {
-    if (cnt)
-      k_lbvh_defer<3, true><<<dgrid, kDeferWarps * 32, 0, c.stream>>>(qs);
-    else
-      k_lbvh_defer<3, false><<<dgrid, kDeferWarps * 32, 0, c.stream>>>(qs);
-  }
-  if ((s = after_launch(c, "lbvh_defer")) != HD_OK) return s;
+      fn = cnt ? (l16 ? (const void*) k_lbvh_query<3, true, 16> : (const void*) k_lbvh_query<3, true, 0>)
+               : (l16 ? (const void*) k_lbvh_query<3, false, 16> : (const void*) k_lbvh_query<3, false, 0>);
+    void* qargs[] = {&qs};
+    cudaLaunchKernel(fn, grid, dim3(kQueryWarps * 32), qargs, 0, c.stream);
+    hd_status r;
+    if ((r = after_launch(c, "lbvh_query")) != HD_OK) return r;
+    // Queries queued by over-budget packets (usually none: the launch then
+    // returns at once).
+    const dim3 dgrid((unsigned) (c.num_sms * 4), count);
+    if (dims == 2) {
+      if (cnt)
+        k_lbvh_defer<2, true><<<dgrid, kDeferWarps * 32, 0, c.stream>>>(qs);
+      else
+        k_lbvh_defer<2, false><<<dgrid, kDeferWarps * 32, 0, c.stream>>>(qs);
+    } else {
+      if (cnt)
+        k_lbvh_defer<3, true><<<dgrid, kDeferWarps * 32, 0, c.stream>>>(qs);
+      else
+        k_lbvh_defer<3, false><<<dgrid, kDeferWarps * 32, 0, c.stream>>>(qs);
+    }
+    return after_launch(c, "lbvh_defer");
+  };
+  if ((s = launch_queries(ins[0].count)) != HD_OK) return s;
   mark(c, 4);
   for (int k = 0; k < count; ++k)
     if ((s = certify(c, ins[k])) != HD_OK) return s;
+  if (plan) {
+    for (int k = 0; k < count; ++k)
+      plan->tree[k] = LbvhTree{bs.s[k].nodes, bs.s[k].root, t[k]->pts, t[k]->n, bs.s[k].L};
+    if ((s = f64_seed(c, *plan, count)) != HD_OK) return s;
+    for (int k = 0; k < count; ++k) {
+      QuerySet& d = qs.d[k];
+      d.sc = plan->frozen[k];
+      d.cand = plan->cand[k];
+      d.cand_count = plan->cand_count[k];
+      d.cand_cap = plan->cand_cap;
+    }
+    if (count == 1) qs.d[1] = qs.d[0];
+    if ((s = launch_queries(false)) != HD_OK) return s;
+  }
   return HD_OK;
 }
 
-hd_status run_lbvh(Ctx& c, const DirInput& in) { return run_lbvh_dirs(c, &in, 1); }
+hd_status run_lbvh(Ctx& c, const DirInput& in) { return run_lbvh_dirs(c, &in, 1, nullptr); }
 
 hd_status run_lbvh_pair(Ctx& c, const DirInput& ab, const DirInput& ba) {
   const DirInput ins[2] = {ab, ba};
-  return run_lbvh_dirs(c, ins, 2);
+  return run_lbvh_dirs(c, ins, 2, nullptr);
+}
+
+hd_status run_lbvh_f64(Ctx& c, const DirInput* ins, int count, F64Plan* plan) {
+  return run_lbvh_dirs(c, ins, count, plan);
 }
 
 }  // namespace hdg

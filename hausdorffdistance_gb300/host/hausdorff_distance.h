@@ -3,12 +3,16 @@
 // libhdgpu.so's C ABI (include/hd_gpu.h).  Same class names for the variants
 // the engine provides, same CalculateDistance(points_a, points_b) call and
 // the same required stats keys ("Algorithm", "Execution", "ReportedTime").
-// Differences: the inputs are never permuted, errors throw hd::Error with
-// the library's status instead of aborting, and every class runs on the GPU.
+// COORD_T float solves through hd_solve; COORD_T double through hd_solve_f64
+// (the reference's double instantiation, which its driver leaves disabled,
+// src/run_hausdorff_distance.cu:56-62).  Differences: the inputs are never
+// permuted, errors throw hd::Error with the library's status instead of
+// aborting, and every class runs on the GPU.
 #pragma once
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "hd_gpu.h"
@@ -16,9 +20,9 @@
 
 namespace hd {
 
-template <int N>
+template <int N, typename T = float>
 struct Point {
-  float c[N];
+  T c[N];
 };
 
 class Error : public std::runtime_error {
@@ -31,8 +35,9 @@ class Error : public std::runtime_error {
 template <typename COORD_T, int N_DIMS>
 class HausdorffDistance {
  public:
-  static_assert(sizeof(COORD_T) == 4, "the engine computes in float32");
-  using point_t = Point<N_DIMS>;
+  static_assert(std::is_same<COORD_T, float>::value || std::is_same<COORD_T, double>::value,
+                "coordinates are float or double");
+  using point_t = Point<N_DIMS, COORD_T>;
 
   HausdorffDistance(int variant, const hd_options* opt, const char* algorithm)
       : algorithm_(algorithm) {
@@ -54,13 +59,13 @@ class HausdorffDistance {
   // Directed h(A,B) (undirected = false) or H(A,B), host vectors.
   COORD_T CalculateDistance(std::vector<point_t>& points_a, std::vector<point_t>& points_b,
                             bool undirected = false) {
-    return Solve(reinterpret_cast<const float*>(points_a.data()), points_a.size(),
-                 reinterpret_cast<const float*>(points_b.data()), points_b.size(),
+    return Solve(reinterpret_cast<const COORD_T*>(points_a.data()), points_a.size(),
+                 reinterpret_cast<const COORD_T*>(points_b.data()), points_b.size(),
                  undirected ? HD_UNDIRECTED : 0u);
   }
 
-  // Same on row-major float arrays (host or, with on_device, device memory).
-  COORD_T CalculateDistance(const float* a, uint64_t n_a, const float* b, uint64_t n_b,
+  // Same on row-major arrays (host or, with on_device, device memory).
+  COORD_T CalculateDistance(const COORD_T* a, uint64_t n_a, const COORD_T* b, uint64_t n_b,
                             bool undirected, bool on_device) {
     return Solve(a, n_a, b, n_b, (undirected ? HD_UNDIRECTED : 0u) | (on_device ? HD_DEVICE_PTRS : 0u));
   }
@@ -75,9 +80,13 @@ class HausdorffDistance {
   hd_ctx* context() { return ctx_; }
 
  protected:
-  COORD_T Solve(const float* a, uint64_t na, const float* b, uint64_t nb, uint32_t flags) {
-    hd_status s = hd_solve(ctx_, a, na, b, nb, N_DIMS, flags | HD_TIMING | HD_COUNT_PAIRS, -1,
-                           &result_);
+  COORD_T Solve(const COORD_T* a, uint64_t na, const COORD_T* b, uint64_t nb, uint32_t flags) {
+    flags |= HD_TIMING | HD_COUNT_PAIRS;
+    hd_status s;
+    if constexpr (std::is_same<COORD_T, double>::value)
+      s = hd_solve_f64(ctx_, a, na, b, nb, N_DIMS, flags, -1, &result_);
+    else
+      s = hd_solve(ctx_, a, na, b, nb, N_DIMS, flags, -1, &result_);
     if (s != HD_OK) throw Error(s, hd_last_error(ctx_));
     static const char* names[] = {"auto", "eb", "grid", "lbvh", "bf16", "brute"};
     stats_ = Json::Object();
@@ -99,7 +108,10 @@ class HausdorffDistance {
     const char* pn[] = {"Prep", "Build", "Sample", "Main", "Tail", "Certify"};
     for (int i = 0; i < 6; ++i) phases[pn[i]] = result_.phase_ms[i];
     stats_["PhaseTimes"] = phases;
-    return (COORD_T) result_.hd_f32;
+    if constexpr (std::is_same<COORD_T, double>::value)
+      return result_.hd;
+    else
+      return result_.hd_f32;
   }
 
   hd_ctx* ctx_ = nullptr;

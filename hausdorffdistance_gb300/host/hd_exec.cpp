@@ -154,10 +154,9 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "%s inputs have 2 or 3 dimensions\n", input_type.c_str());
     return 1;
   }
-  if (fl.getb("is_double", false)) {
-    std::fprintf(stderr, "double inputs are not supported (the engine computes in float32)\n");
-    return 1;
-  }
+  // -is_double: coordinates parsed and solved in FP64 (hd_solve_f64; the
+  // reference's disabled double dispatch, run_hausdorff_distance.cu:56-62).
+  const bool is_double = fl.getb("is_double", false);
   const std::string execution = lower(fl.get("execution", "gpu"));
   if (execution != "gpu" && execution != "cpu") {
     std::fprintf(stderr, "Unknown execution: %s\n", execution.c_str());
@@ -182,8 +181,8 @@ int main(int argc, char** argv) {
 
   hd::PointSet pa, pb;
   try {
-    pa = hd::LoadPoints(input1, input_type, dims, limit, fl.get("serialize", ""));
-    pb = hd::LoadPoints(input2, input_type, dims, limit, fl.get("serialize", ""));
+    pa = hd::LoadPoints(input1, input_type, dims, limit, fl.get("serialize", ""), is_double);
+    pb = hd::LoadPoints(input2, input_type, dims, limit, fl.get("serialize", ""), is_double);
   } catch (const std::exception& e) {
     std::fprintf(stderr, "%s\n", e.what());
     return 1;
@@ -310,16 +309,27 @@ int main(int argc, char** argv) {
 
   // Inputs go to the device once, before the repeat loop, as in the
   // reference (run_hausdorff_distance.cu:148); ReportedTime excludes them.
-  float *dA = nullptr, *dB = nullptr;
-  if (have_gpu && (cudaMalloc(&dA, pa.xyz.size() * 4) != cudaSuccess ||
-      cudaMalloc(&dB, pb.xyz.size() * 4) != cudaSuccess ||
-      cudaMemcpy(dA, pa.xyz.data(), pa.xyz.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(dB, pb.xyz.data(), pb.xyz.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)) {
+  // With -is_double the device copies hold the doubles.
+  void *dA = nullptr, *dB = nullptr;
+  const size_t esz = is_double ? sizeof(double) : sizeof(float);
+  const void* hA = is_double ? (const void*) pa.xyz64.data() : (const void*) pa.xyz.data();
+  const void* hB = is_double ? (const void*) pb.xyz64.data() : (const void*) pb.xyz.data();
+  if (have_gpu && (cudaMalloc(&dA, pa.xyz.size() * esz) != cudaSuccess ||
+      cudaMalloc(&dB, pb.xyz.size() * esz) != cudaSuccess ||
+      cudaMemcpy(dA, hA, pa.xyz.size() * esz, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(dB, hB, pb.xyz.size() * esz, cudaMemcpyHostToDevice) != cudaSuccess)) {
     std::fprintf(stderr, "device allocation or copy failed\n");
     return 1;
   }
+  // Distances are printed with the digits their type needs.
+  auto print_dist = [&](double d) {
+    if (is_double)
+      std::printf("HausdorffDistance: distance is %.17g\n", d);
+    else
+      std::printf("HausdorffDistance: distance is %.9g\n", d);
+  };
 
-  auto run = [&](const hd_options& o, hd::Json& run_json, float* out_dist) -> int {
+  auto run = [&](const hd_options& o, hd::Json& run_json, double* out_dist) -> int {
     hd_ctx* ctx = nullptr;
     hd_status s = hd_create(&ctx, &o);
     if (s != HD_OK) {
@@ -331,11 +341,15 @@ int main(int argc, char** argv) {
     hd_result r{};
     const auto t0 = std::chrono::steady_clock::now();
     for (int i = 0; i < repeat; ++i) {
-      s = hd_solve(ctx, dA, pa.size(), dB, pb.size(), dims,
-                   HD_DEVICE_PTRS | HD_TIMING | HD_COUNT_PAIRS | (undirected ? HD_UNDIRECTED : 0u),
-                   variant, &r);
+      const uint32_t sflags =
+          HD_DEVICE_PTRS | HD_TIMING | HD_COUNT_PAIRS | (undirected ? HD_UNDIRECTED : 0u);
+      s = is_double ? hd_solve_f64(ctx, (const double*) dA, pa.size(), (const double*) dB,
+                                   pb.size(), dims, sflags, variant, &r)
+                    : hd_solve(ctx, (const float*) dA, pa.size(), (const float*) dB, pb.size(),
+                               dims, sflags, variant, &r);
       if (s != HD_OK) {
-        std::fprintf(stderr, "hd_solve: %s: %s\n", hd_status_string(s), hd_last_error(ctx));
+        std::fprintf(stderr, "%s: %s: %s\n", is_double ? "hd_solve_f64" : "hd_solve",
+                     hd_status_string(s), hd_last_error(ctx));
         hd_destroy(ctx);
         return 1;
       }
@@ -363,22 +377,26 @@ int main(int argc, char** argv) {
     run_json["AvgTime"] = total / repeat;
     run_json["AvgWallTime"] = wall / repeat;
     std::printf("Time: %f ms\n", total / repeat);
-    *out_dist = r.hd_f32;
+    *out_dist = is_double ? r.hd : (double) r.hd_f32;
     hd_destroy(ctx);
     return 0;
   };
 
   // The CPU early-break on all host threads (or -parallelism of them); both
   // directions for -undirected.
+  auto cpu_eb = [&](const hd::PointSet& x, const hd::PointSet& y, unsigned threads) {
+    return is_double ? hd::CpuEarlyBreak(x.xyz64.data(), x.size(), y.xyz64.data(), y.size(), dims,
+                                         (uint32_t) opt.seed, threads)
+                     : hd::CpuEarlyBreak(x.xyz.data(), x.size(), y.xyz.data(), y.size(), dims,
+                                         (uint32_t) opt.seed, threads);
+  };
   auto cpu_distance = [&](unsigned threads, double* compute_ms, unsigned long long* pairs) {
-    hd::CpuEarlyBreakResult ab = hd::CpuEarlyBreak(pa.xyz.data(), pa.size(), pb.xyz.data(),
-                                                   pb.size(), dims, (uint32_t) opt.seed, threads);
-    float d = ab.distance;
+    hd::CpuEarlyBreakResult ab = cpu_eb(pa, pb, threads);
+    double d = ab.distance;
     *compute_ms = ab.compute_ms;
     *pairs = ab.compared_pairs;
     if (undirected) {
-      hd::CpuEarlyBreakResult ba = hd::CpuEarlyBreak(pb.xyz.data(), pb.size(), pa.xyz.data(),
-                                                     pa.size(), dims, (uint32_t) opt.seed, threads);
+      hd::CpuEarlyBreakResult ba = cpu_eb(pb, pa, threads);
       d = std::max(d, ba.distance);
       *compute_ms += ba.compute_ms;
       *pairs += ba.compared_pairs;
@@ -394,7 +412,7 @@ int main(int argc, char** argv) {
     hd::Json& run_json = stats["Running"];
     hd::Json repeats = hd::Json::Array();
     double total = 0.0;
-    float dist = 0.0f;
+    double dist = 0.0;
     for (int i = 0; i < repeat; ++i) {
       double ms = 0.0;
       unsigned long long pairs = 0;
@@ -415,7 +433,7 @@ int main(int argc, char** argv) {
     run_json["AvgTime"] = total / repeat;
     stats["HDResult"] = dist;
     std::printf("Time: %f ms\n", total / repeat);
-    std::printf("HausdorffDistance: distance is %.9g\n", dist);
+    print_dist(dist);
     if (!json_path.empty()) {
       const bool exists = access(json_path.c_str(), R_OK) == 0;
       if (!exists || fl.getb("overwrite", false)) std::ofstream(json_path) << stats.dump(4);
@@ -440,7 +458,7 @@ int main(int argc, char** argv) {
           o.eb_only_threshold = (uint32_t) th;
           o.n_points_cell = (uint32_t) np;
           hd::Json st = stats;
-          float dist = 0.0f;
+          double dist = 0.0;
           if (run(o, st["Running"], &dist)) return 1;
           st["HDResult"] = dist;
           if (!json_path.empty()) {
@@ -452,23 +470,23 @@ int main(int argc, char** argv) {
     return 0;
   }
 
-  float dist = 0.0f;
+  double dist = 0.0;
   if (run(opt, stats["Running"], &dist)) return 1;
   stats["HDResult"] = dist;
-  std::printf("HausdorffDistance: distance is %.9g\n", dist);
+  print_dist(dist);
 
   if (check) {
     // The reference re-runs its CPU early-break on every host thread.
     double ms = 0.0;
     unsigned long long pairs = 0;
-    const float answer = cpu_distance(all_threads, &ms, &pairs);
+    const double answer = cpu_distance(all_threads, &ms, &pairs);
     hd::Json& ck = stats["Check"];
     ck["HDAnswer"] = answer;
-    ck["Diff"] = (double) answer - (double) dist;
+    ck["Diff"] = answer - dist;
     ck["Pass"] = answer == dist;
     if (answer != dist) {
       std::fprintf(stderr, "Wrong HausdorffDistance. Result: %.8f Answer: %.8f Diff: %.8f\n", dist,
-                   answer, (double) answer - (double) dist);
+                   answer, answer - dist);
     } else {
       std::printf("HausdorffDistance is checked\n");
     }

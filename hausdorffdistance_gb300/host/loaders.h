@@ -1,7 +1,9 @@
 // Point-set loaders and preprocessing for hd_exec, written for this engine
 // without boost, rply or ITK.  Each follows the reference loader it stands in
 // for (file:line given per function).  Points are returned as a flat
-// row-major float array (n x dims), the layout the C ABI takes.
+// row-major float array (n x dims), the layout the C ABI takes, and for
+// -is_double also as doubles parsed from the same text (the reference's
+// double instantiation of its loaders).
 #pragma once
 #include <dirent.h>
 #include <sys/stat.h>
@@ -24,8 +26,14 @@ namespace hd {
 
 struct PointSet {
   int dims = 0;
-  std::vector<float> xyz;  // n * dims
+  std::vector<float> xyz;     // n * dims
+  bool keep64 = false;        // also keep the coordinates as doubles
+  std::vector<double> xyz64;  // n * dims when keep64
   size_t size() const { return dims ? xyz.size() / dims : 0; }
+  void push(double v) {
+    xyz.push_back((float) v);
+    if (keep64) xyz64.push_back(v);
+  }
 };
 
 inline void load_fail(const std::string& msg) { throw std::runtime_error(msg); }
@@ -35,11 +43,12 @@ inline void load_fail(const std::string& msg) { throw std::runtime_error(msg); }
 // vertices (polygons only their outer ring); GEOMETRYCOLLECTION lines are
 // skipped; any other geometry is an error.  The first `dims` coordinates of
 // each vertex are used.
-inline PointSet LoadWKT(const std::string& path, int dims, size_t limit) {
+inline PointSet LoadWKT(const std::string& path, int dims, size_t limit, bool keep64 = false) {
   std::ifstream ifs(path);
   if (!ifs) load_fail("cannot open " + path);
   PointSet ps;
   ps.dims = dims;
+  ps.keep64 = keep64;
   std::string line;
   auto starts = [](const std::string& s, const char* p) { return s.rfind(p, 0) == 0; };
   while (std::getline(ifs, line) && ps.size() < limit) {
@@ -72,7 +81,7 @@ inline PointSet LoadWKT(const std::string& path, int dims, size_t limit) {
       if (tuple.empty()) return;
       if ((int) tuple.size() < dims) load_fail("WKT vertex with too few coordinates in " + path);
       if (ps.size() < limit)
-        for (int k = 0; k < dims; ++k) ps.xyz.push_back((float) tuple[k]);
+        for (int k = 0; k < dims; ++k) ps.push(tuple[k]);
       tuple.clear();
     };
     const char* p = line.c_str();
@@ -115,7 +124,7 @@ inline PointSet LoadWKT(const std::string& path, int dims, size_t limit) {
 // OFF (src/loaders/loader.h:99-147): "OFF" header, counts on the same or the
 // next line, then the vertices.  Like the reference, `dims` consecutive
 // numbers are read per vertex.
-inline PointSet LoadOFF(const std::string& path, int dims, size_t limit) {
+inline PointSet LoadOFF(const std::string& path, int dims, size_t limit, bool keep64 = false) {
   std::ifstream ifs(path);
   if (!ifs) load_fail("cannot open " + path);
   std::string line;
@@ -129,11 +138,24 @@ inline PointSet LoadOFF(const std::string& path, int dims, size_t limit) {
   if (nv == 0) load_fail("OFF vertex count is zero or missing: " + path);
   PointSet ps;
   ps.dims = dims;
+  ps.keep64 = keep64;
   for (size_t i = 0; i < nv && i < limit; ++i) {
     for (int k = 0; k < dims; ++k) {
-      float v;
-      if (!(ifs >> v)) load_fail("truncated OFF vertex list: " + path);
-      ps.xyz.push_back(v);
+      if (keep64) {
+        // Each number parsed twice: directly to float (as the float
+        // loader does) and to double.
+        std::string tok;
+        if (!(ifs >> tok)) load_fail("truncated OFF vertex list: " + path);
+        char* end = nullptr;
+        const float f = std::strtof(tok.c_str(), &end);
+        if (end == tok.c_str()) load_fail("bad OFF coordinate in " + path);
+        ps.xyz.push_back(f);
+        ps.xyz64.push_back(std::strtod(tok.c_str(), nullptr));
+      } else {
+        float v;
+        if (!(ifs >> v)) load_fail("truncated OFF vertex list: " + path);
+        ps.xyz.push_back(v);
+      }
     }
   }
   return ps;
@@ -142,7 +164,7 @@ inline PointSet LoadOFF(const std::string& path, int dims, size_t limit) {
 // PLY (src/loaders/ply_loader.h:37-101): the x, y (, z) properties of the
 // "vertex" element, ASCII or binary (either byte order), read as doubles,
 // shifted so that the minimum of every axis is 0, then stored as float.
-inline PointSet LoadPLY(const std::string& path, int dims, size_t limit) {
+inline PointSet LoadPLY(const std::string& path, int dims, size_t limit, bool keep64 = false) {
   std::ifstream ifs(path, std::ios::binary);
   if (!ifs) load_fail("cannot open " + path);
   std::string line;
@@ -266,19 +288,26 @@ inline PointSet LoadPLY(const std::string& path, int dims, size_t limit) {
   }
   PointSet ps;
   ps.dims = dims;
+  ps.keep64 = keep64;
   const size_t n = verts.size() / dims;
   std::vector<double> lo(dims, std::numeric_limits<double>::max());
   for (size_t i = 0; i < n; ++i)
     for (int k = 0; k < dims; ++k) lo[k] = std::min(lo[k], verts[i * dims + k]);
   ps.xyz.resize(verts.size());
+  if (keep64) ps.xyz64.resize(verts.size());
   for (size_t i = 0; i < n; ++i)
-    for (int k = 0; k < dims; ++k) ps.xyz[i * dims + k] = (float) (verts[i * dims + k] - lo[k]);
+    for (int k = 0; k < dims; ++k) {
+      const double v = verts[i * dims + k] - lo[k];
+      ps.xyz[i * dims + k] = (float) v;
+      if (keep64) ps.xyz64[i * dims + k] = v;
+    }
   return ps;
 }
 
 // Point cache (src/loaders/loader.h:150-185): a 64-bit count followed by the
-// packed float points.
-inline PointSet LoadBin(const std::string& path, int dims, size_t limit) {
+// packed points, floats, or doubles when keep64 (the reference's cache of
+// its double instantiation).
+inline PointSet LoadBin(const std::string& path, int dims, size_t limit, bool keep64 = false) {
   std::ifstream ifs(path, std::ios::binary);
   if (!ifs) load_fail("cannot open " + path);
   uint64_t n = 0;
@@ -286,8 +315,15 @@ inline PointSet LoadBin(const std::string& path, int dims, size_t limit) {
   n = std::min<uint64_t>(n, limit);
   PointSet ps;
   ps.dims = dims;
+  ps.keep64 = keep64;
   ps.xyz.resize(n * dims);
-  ifs.read((char*) ps.xyz.data(), (std::streamsize) (n * dims * sizeof(float)));
+  if (keep64) {
+    ps.xyz64.resize(n * dims);
+    ifs.read((char*) ps.xyz64.data(), (std::streamsize) (n * dims * sizeof(double)));
+    for (size_t i = 0; i < ps.xyz64.size(); ++i) ps.xyz[i] = (float) ps.xyz64[i];
+  } else {
+    ifs.read((char*) ps.xyz.data(), (std::streamsize) (n * dims * sizeof(float)));
+  }
   if (!ifs) load_fail("truncated point file: " + path);
   return ps;
 }
@@ -297,14 +333,19 @@ inline void SaveBin(const std::string& path, const PointSet& ps) {
   if (!ofs) load_fail("cannot write " + path);
   const uint64_t n = ps.size();
   ofs.write((const char*) &n, sizeof(n));
-  ofs.write((const char*) ps.xyz.data(), (std::streamsize) (ps.xyz.size() * sizeof(float)));
+  if (ps.keep64)
+    ofs.write((const char*) ps.xyz64.data(), (std::streamsize) (ps.xyz64.size() * sizeof(double)));
+  else
+    ofs.write((const char*) ps.xyz.data(), (std::streamsize) (ps.xyz.size() * sizeof(float)));
 }
 
 // Loads with the reference's -serialize cache (loader.h:188-234): the cache
 // file <folder>/points_<path with '/' as '_'>_limit_<limit>.bin is read when
-// present, else written after loading.  type: wkt | off | ply | bin.
+// present, else written after loading (a separate "_f64" cache holds
+// doubles).  type: wkt | off | ply | bin.
 inline PointSet LoadPoints(const std::string& path, const std::string& type, int dims,
-                           long long limit, const std::string& cache_folder) {
+                           long long limit, const std::string& cache_folder,
+                           bool keep64 = false) {
   const size_t lim = limit > 0 ? (size_t) limit : std::numeric_limits<size_t>::max();
   std::string cache;
   if (!cache_folder.empty() && type != "bin") {
@@ -312,47 +353,70 @@ inline PointSet LoadPoints(const std::string& path, const std::string& type, int
     std::replace(esc.begin(), esc.end(), '/', '_');
     if (mkdir(cache_folder.c_str(), 0755) != 0 && errno != EEXIST)
       load_fail("cannot create " + cache_folder);
-    cache = cache_folder + "/points_" + esc + "_limit_" + std::to_string(limit) + ".bin";
-    if (access(cache.c_str(), R_OK) == 0) return LoadBin(cache, dims, lim);
+    cache = cache_folder + "/points_" + esc + "_limit_" + std::to_string(limit) +
+            (keep64 ? "_f64" : "") + ".bin";
+    if (access(cache.c_str(), R_OK) == 0) return LoadBin(cache, dims, lim, keep64);
   }
   PointSet ps;
   if (type == "wkt")
-    ps = LoadWKT(path, dims, lim);
+    ps = LoadWKT(path, dims, lim, keep64);
   else if (type == "off")
-    ps = LoadOFF(path, dims, lim);
+    ps = LoadOFF(path, dims, lim, keep64);
   else if (type == "ply")
-    ps = LoadPLY(path, dims, lim);
+    ps = LoadPLY(path, dims, lim, keep64);
   else if (type == "bin")
-    ps = LoadBin(path, dims, lim);
+    ps = LoadBin(path, dims, lim, keep64);
   else
     load_fail("Unsupported input type: " + type);
   if (!cache.empty() && ps.size() > 0) SaveBin(cache, ps);
   return ps;
 }
 
+// The same preprocessing in double (keep64), the float copy re-rounded.
+template <typename T>
+inline void NormalizeRows(std::vector<T>& xyz, size_t n, int dims) {
+  std::vector<T> lo(dims, std::numeric_limits<T>::max()), hi(dims, std::numeric_limits<T>::lowest());
+  for (size_t i = 0; i < n; ++i)
+    for (int k = 0; k < dims; ++k) {
+      lo[k] = std::min(lo[k], xyz[i * dims + k]);
+      hi[k] = std::max(hi[k], xyz[i * dims + k]);
+    }
+  T ext = 0;
+  for (int k = 0; k < dims; ++k) ext = std::max(ext, hi[k] - lo[k]);
+  if (ext == T(0)) ext = T(1);
+  for (size_t i = 0; i < n; ++i)
+    for (int k = 0; k < dims; ++k) xyz[i * dims + k] = (xyz[i * dims + k] - lo[k]) / ext;
+}
+
 // -normalize (translate_points.h:42-66): (x - min) / max extent per axis.
 inline void NormalizePoints(PointSet& ps) {
   const size_t n = ps.size();
   if (n == 0) return;
-  std::vector<float> lo(ps.dims, std::numeric_limits<float>::max()),
-      hi(ps.dims, std::numeric_limits<float>::lowest());
-  for (size_t i = 0; i < n; ++i)
-    for (int k = 0; k < ps.dims; ++k) {
-      lo[k] = std::min(lo[k], ps.xyz[i * ps.dims + k]);
-      hi[k] = std::max(hi[k], ps.xyz[i * ps.dims + k]);
-    }
-  float ext = 0.0f;
-  for (int k = 0; k < ps.dims; ++k) ext = std::max(ext, hi[k] - lo[k]);
-  if (ext == 0.0f) ext = 1.0f;
-  for (size_t i = 0; i < n; ++i)
-    for (int k = 0; k < ps.dims; ++k)
-      ps.xyz[i * ps.dims + k] = (ps.xyz[i * ps.dims + k] - lo[k]) / ext;
+  if (ps.keep64) {
+    NormalizeRows(ps.xyz64, n, ps.dims);
+    for (size_t i = 0; i < ps.xyz64.size(); ++i) ps.xyz[i] = (float) ps.xyz64[i];
+    return;
+  }
+  NormalizeRows(ps.xyz, n, ps.dims);
 }
 
 // -translate (translate_points.h:68-79): shift axis `dim` by ratio x extent.
 inline void TranslatePoints(PointSet& ps, int dim, double ratio) {
   const size_t n = ps.size();
   if (n == 0) return;
+  if (ps.keep64) {
+    double lo = std::numeric_limits<double>::max(), hi = std::numeric_limits<double>::lowest();
+    for (size_t i = 0; i < n; ++i) {
+      lo = std::min(lo, ps.xyz64[i * ps.dims + dim]);
+      hi = std::max(hi, ps.xyz64[i * ps.dims + dim]);
+    }
+    const double shift = (hi - lo) * ratio;
+    for (size_t i = 0; i < n; ++i) {
+      ps.xyz64[i * ps.dims + dim] += shift;
+      ps.xyz[i * ps.dims + dim] = (float) ps.xyz64[i * ps.dims + dim];
+    }
+    return;
+  }
   float lo = std::numeric_limits<float>::max(), hi = std::numeric_limits<float>::lowest();
   for (size_t i = 0; i < n; ++i) {
     lo = std::min(lo, ps.xyz[i * ps.dims + dim]);

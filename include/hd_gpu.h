@@ -191,6 +191,32 @@ HD_API hd_status hd_solve(hd_ctx* ctx, const float* A, uint64_t n_a, const float
                    uint64_t n_b, int n_dims, uint32_t flags, int variant,
                    hd_result* out);
 
+/* FP64 input path: the Hausdorff distance of double-precision point sets,
+ * exact in FP64 (squared distances formed in double by the same formula:
+ * per-dimension difference, squared, summed left to right, no FMA).
+ * Replaces the reference's double instantiations behind its disabled
+ * -is_double dispatch (run_hausdorff_distance.cu:56-62, the
+ * RunHausdorffDistanceImpl<double, 2|3> cases).
+ *
+ * A is n_a x n_dims doubles, B n_b x n_dims (row-major; host pointers, or
+ * device pointers with HD_DEVICE_PTRS).  variant: HD_VARIANT_AUTO or
+ * HD_VARIANT_LBVH (n_dims 2 or 3: FP32 tree search on the sets rounded to
+ * float, FP64 only for the rows the FP32 values cannot settle), or
+ * HD_VARIANT_EB / HD_VARIANT_BRUTE (an FP64 scan, n_dims in [1, 256]);
+ * the grid and BF16 variants return HD_ERR_UNSUPPORTED.  AUTO takes the
+ * scan for other n_dims and for coordinates beyond +-1e18.  NaN or infinite
+ * coordinates return HD_ERR_INVALID_ARG.
+ *
+ * Results in *out: hd, hd_ab, hd_ba are the FP64 distances; ia, ib,
+ * direction the certifying pair (lowest row, then lowest column among
+ * ties; direction 1 only when B->A is strictly larger); hd_f32 = hd
+ * rounded to float; variant_used the path taken; rechecked the rows whose
+ * nearest neighbour was searched in FP64; flags HD_COUNT_PAIRS (the FP32
+ * search's counts) and HD_TIMING (ms only) as for hd_solve. */
+HD_API hd_status hd_solve_f64(hd_ctx* ctx, const double* A, uint64_t n_a, const double* B,
+                              uint64_t n_b, int n_dims, uint32_t flags, int variant,
+                              hd_result* out);
+
 /* Solves many independent problems (2-D or 3-D) in one graph-captured
  * persistent launch.  A/B hold all problems' points back to back; probs[i]
  * gives each problem's ranges; out[i] receives its result.  flags as for

@@ -20,6 +20,7 @@
 //                     conservative pruning and the early-break rule keeps
 //                     large inputs tractable.
 //   hd_oracle_exact_batch  the same for many independent problems.
+//   hd_oracle_exact_f64    exact directed max-min of FP64 coordinates in FP64.
 //
 // Build: g++ -O2 -std=c++17 -ffp-contract=off -pthread -shared -fPIC.
 // -ffp-contract=off matters: the reference builds with fmad off
@@ -50,13 +51,26 @@ inline float dist2_f32(const float* a, const float* b, int dims) {
   return s;
 }
 
-inline double dist2_f64(const float* a, const float* b, int dims) {
+// The same formula in FP64, from float or double coordinates.
+template <typename T>
+inline double dist2_f64(const T* a, const T* b, int dims) {
   double s = 0.0;
   for (int k = 0; k < dims; ++k) {
     double d = (double) a[k] - (double) b[k];
-    s += d * d;
+    double sq = d * d;
+    s = (k == 0) ? sq : s + sq;
   }
   return s;
+}
+
+// Metric M over coordinates T: 0 = the FP32 formula (float coordinates
+// only), 1 = FP64.
+template <int M, typename T>
+inline double dist2_m(const T* a, const T* b, int dims) {
+  if constexpr (M == 0)
+    return (double) dist2_f32(a, b, dims);
+  else
+    return dist2_f64(a, b, dims);
 }
 
 template <int N>
@@ -208,24 +222,26 @@ void eb_impl_dims(const float* A, uint64_t nA, const float* B, uint64_t nB, int 
 // Such a query cannot reach the maximum, and every query whose nearest
 // neighbour is at or above the final maximum runs to completion, so the
 // maximum and its lowest-index certifying pair are exact.
+template <typename T>
 struct KdNode {
   int32_t left, right;  // children, or -1 for a leaf
   int32_t dim;
-  float split;
+  T split;
   uint64_t begin, end;  // range in perm for leaves
 };
 
+template <typename T>
 struct KdTree {
   int dims = 0;
-  const float* pts = nullptr;
+  const T* pts = nullptr;
   std::vector<uint64_t> perm;
-  std::vector<float> tp;  // coordinates in tree order (perm applied)
-  std::vector<KdNode> nodes;
+  std::vector<T> tp;  // coordinates in tree order (perm applied)
+  std::vector<KdNode<T>> nodes;
   std::atomic<int32_t> used{0};
 
   int32_t alloc_node(uint64_t b, uint64_t e) {
     int32_t id = used.fetch_add(1);
-    nodes[id] = KdNode{-1, -1, 0, 0.0f, b, e};
+    nodes[id] = KdNode<T>{-1, -1, 0, T(0), b, e};
     return id;
   }
 
@@ -235,11 +251,11 @@ struct KdTree {
     int32_t id = alloc_node(b, e);
     if (e - b <= 16) return id;
     int best_dim = 0;
-    float best_ext = -1.0f;
+    T best_ext = T(-1);
     for (int k = 0; k < dims; ++k) {
-      float lo = std::numeric_limits<float>::infinity(), hi = -lo;
+      T lo = std::numeric_limits<T>::infinity(), hi = -lo;
       for (uint64_t i = b; i < e; ++i) {
-        float v = pts[perm[i] * dims + k];
+        T v = pts[perm[i] * dims + k];
         lo = std::min(lo, v);
         hi = std::max(hi, v);
       }
@@ -248,13 +264,13 @@ struct KdTree {
         best_dim = k;
       }
     }
-    if (best_ext <= 0.0f) return id;  // all points identical: keep a leaf
+    if (best_ext <= T(0)) return id;  // all points identical: keep a leaf
     uint64_t mid = b + (e - b) / 2;
     std::nth_element(perm.begin() + b, perm.begin() + mid, perm.begin() + e,
                      [&](uint64_t x, uint64_t y) {
                        return pts[x * dims + best_dim] < pts[y * dims + best_dim];
                      });
-    float split = pts[perm[mid] * dims + best_dim];
+    T split = pts[perm[mid] * dims + best_dim];
     int32_t l, r;
     if (depth < par_depth && e - b > 65536) {
       int32_t lr = -1;
@@ -273,14 +289,14 @@ struct KdTree {
     return id;
   }
 
-  void init(const float* p, uint64_t n, int d, int n_threads) {
+  void init(const T* p, uint64_t n, int d, int n_threads) {
     pts = p;
     dims = d;
     perm.resize(n);
     std::iota(perm.begin(), perm.end(), 0);
     // Every split leaves at least 8 points on each side, so there are at
     // most n/8 + 1 leaves.
-    nodes.assign(2 * (n / 8 + 2), KdNode{});
+    nodes.assign(2 * (n / 8 + 2), KdNode<T>{});
     used = 0;
     int par_depth = 0;
     while ((1 << par_depth) < std::max(1, n_threads)) ++par_depth;
@@ -288,12 +304,12 @@ struct KdTree {
     // Leaves scan contiguous coordinates instead of following perm into the
     // caller's array.
     tp.resize(n * (uint64_t) d);
-    const uint64_t T = (uint64_t) std::max(1, n_threads);
+    const uint64_t nt = (uint64_t) std::max(1, n_threads);
     std::vector<std::thread> ts;
-    for (uint64_t t = 0; t < T; ++t)
+    for (uint64_t t = 0; t < nt; ++t)
       ts.emplace_back([&, t] {
-        for (uint64_t i = t * n / T; i < (t + 1) * n / T; ++i)
-          std::memcpy(&tp[i * d], pts + perm[i] * d, sizeof(float) * d);
+        for (uint64_t i = t * n / nt; i < (t + 1) * n / nt; ++i)
+          std::memcpy(&tp[i * d], pts + perm[i] * d, sizeof(T) * d);
       });
     for (auto& t : ts) t.join();
   }
@@ -301,12 +317,12 @@ struct KdTree {
   // Nearest neighbour of q under metric M (0 = FP32 formula, 1 = FP64),
   // abandoned (returns true) once best < stop.
   template <int M>
-  bool query(int32_t id, const float* q, double& best, uint64_t& best_idx, double stop) const {
-    const KdNode& n = nodes[id];
+  bool query(int32_t id, const T* q, double& best, uint64_t& best_idx, double stop) const {
+    const KdNode<T>& n = nodes[id];
     if (n.left < 0) {
-      const float* p = &tp[n.begin * dims];
+      const T* p = &tp[n.begin * dims];
       for (uint64_t i = n.begin; i < n.end; ++i, p += dims) {
-        double d = M == 0 ? (double) dist2_f32(q, p, dims) : dist2_f64(q, p, dims);
+        double d = dist2_m<M>(q, p, dims);
         if (d <= best) {
           const uint64_t j = perm[i];
           if (d < best || j < best_idx) {
@@ -333,12 +349,12 @@ void atomic_max(std::atomic<double>& a, double v) {
   }
 }
 
-template <int M>
-void exact_tree(const KdTree& tree, const float* A, uint64_t nA, int dims, int n_threads,
+template <int M, typename T>
+void exact_tree(const KdTree<T>& tree, const T* A, uint64_t nA, int dims, int n_threads,
                 double* hd2, uint64_t* ia, uint64_t* ib) {
-  int T = std::max(1, n_threads);
-  std::vector<double> tbest(T, -1.0);
-  std::vector<uint64_t> ta(T, 0), tb(T, 0);
+  const int nt = std::max(1, n_threads);
+  std::vector<double> tbest(nt, -1.0);
+  std::vector<uint64_t> ta(nt, 0), tb(nt, 0);
   std::atomic<uint64_t> next{0};
   std::atomic<double> gbest{-1.0};
   // Queries are visited in a pseudo-random order (j -> j*mul mod nA) so that
@@ -359,7 +375,7 @@ void exact_tree(const KdTree& tree, const float* A, uint64_t nA, int dims, int n
         const uint64_t i = (uint64_t) (((unsigned __int128) v * mul) % nA);
         double best = std::numeric_limits<double>::infinity();
         uint64_t bi = 0;
-        if (tree.query<M>(0, A + i * dims, best, bi, stop)) continue;
+        if (tree.template query<M>(0, A + i * dims, best, bi, stop)) continue;
         if (best > tbest[t] || (best == tbest[t] && i < ta[t])) {
           tbest[t] = best;
           ta[t] = i;
@@ -371,11 +387,11 @@ void exact_tree(const KdTree& tree, const float* A, uint64_t nA, int dims, int n
     }
   };
   std::vector<std::thread> ts;
-  for (int t = 0; t < T; ++t) ts.emplace_back(work, t);
+  for (int t = 0; t < nt; ++t) ts.emplace_back(work, t);
   for (auto& t : ts) t.join();
   double best = -1.0;
   uint64_t ba = 0, bb = 0;
-  for (int t = 0; t < T; ++t) {
+  for (int t = 0; t < nt; ++t) {
     if (tbest[t] > best || (tbest[t] == best && ta[t] < ba)) {
       best = tbest[t];
       ba = ta[t];
@@ -387,19 +403,19 @@ void exact_tree(const KdTree& tree, const float* A, uint64_t nA, int dims, int n
   *ib = bb;
 }
 
-template <int M>
-void exact_impl(const float* A, uint64_t nA, const float* B, uint64_t nB,
+template <int M, typename T>
+void exact_impl(const T* A, uint64_t nA, const T* B, uint64_t nB,
                 int dims, int n_threads, double* hd2, uint64_t* ia,
                 uint64_t* ib) {
-  KdTree tree;
+  KdTree<T> tree;
   tree.init(B, nB, dims, n_threads);
   exact_tree<M>(tree, A, nA, dims, n_threads, hd2, ia, ib);
 }
 
 // One small problem, single-threaded: brute force with early break against
 // the running maximum (the same exactness argument as exact_tree).
-template <int M>
-void exact_small(const float* A, uint64_t nA, const float* B, uint64_t nB, int dims,
+template <int M, typename T>
+void exact_small(const T* A, uint64_t nA, const T* B, uint64_t nB, int dims,
                  double* hd2, uint64_t* ia, uint64_t* ib) {
   double gbest = -1.0;
   uint64_t ba = 0, bb = 0;
@@ -408,8 +424,7 @@ void exact_small(const float* A, uint64_t nA, const float* B, uint64_t nB, int d
     uint64_t bi = 0;
     bool broke = false;
     for (uint64_t j = 0; j < nB; ++j) {
-      double d = M == 0 ? (double) dist2_f32(A + i * dims, B + j * dims, dims)
-                        : dist2_f64(A + i * dims, B + j * dims, dims);
+      double d = dist2_m<M>(A + i * dims, B + j * dims, dims);
       if (d < best) {
         best = d;
         bi = j;
@@ -555,6 +570,21 @@ int hd_oracle_exact_batch(const float* A, const float* B, const uint64_t* offset
   std::vector<std::thread> ts;
   for (int t = 0; t < T; ++t) ts.emplace_back(work);
   for (auto& t : ts) t.join();
+  return 0;
+}
+
+// Exact directed max-min of FP64 coordinates with FP64 squared distances
+// formed by the same formula in double (the reference's distance template
+// instantiated for double points, src/geoms/distance.h:17-24, as its disabled
+// -is_double dispatch would, src/run_hausdorff_distance.cu:56-62), with the
+// certifying pair (lowest indices on ties).
+int hd_oracle_exact_f64(const double* A, uint64_t nA, const double* B, uint64_t nB, int dims,
+                        int n_threads, double* hd2, uint64_t* ia, uint64_t* ib) {
+  if (nA == 0 || nB == 0 || dims < 1) return -1;
+  if (nA * nB <= (uint64_t) 1 << 22)
+    exact_small<1>(A, nA, B, nB, dims, hd2, ia, ib);
+  else
+    exact_impl<1>(A, nA, B, nB, dims, n_threads, hd2, ia, ib);
   return 0;
 }
 

@@ -24,7 +24,8 @@ _lib = None
 def _load():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB):
+        src = os.path.join(_HERE, "hd_oracle.cpp")
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
             os.makedirs(os.path.dirname(LIB), exist_ok=True)
             subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-pthread",
                             "-shared", "-fPIC", os.path.join(_HERE, "hd_oracle.cpp"),
@@ -46,6 +47,9 @@ def _load():
                                               ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P,
                                               P]
         lib.hd_oracle_exact_batch.restype = ctypes.c_int
+        lib.hd_oracle_exact_f64.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint64, ctypes.c_int,
+                                            ctypes.c_int, P, P, P]
+        lib.hd_oracle_exact_f64.restype = ctypes.c_int
         lib.hd_oracle_dist2_f32.argtypes = [P, P, ctypes.c_int]
         lib.hd_oracle_dist2_f32.restype = ctypes.c_float
         _lib = lib
@@ -113,6 +117,26 @@ def exact(A, B, precision=32, n_threads=None):
                              ctypes.byref(ia), ctypes.byref(ib))
     if st != 0:
         raise ValueError("oracle exact: unsupported input")
+    return h2.value, int(ia.value), int(ib.value)
+
+
+def exact_f64(A, B, n_threads=None):
+    """Exact directed max-min of FP64 points with FP64 squared distances:
+    returns (hd2, ia, ib), the certifying pair with the lowest indices on
+    ties."""
+    lib = _load()
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    if n_threads is None:
+        n_threads = os.cpu_count() or 1
+    h2 = ctypes.c_double()
+    ia = ctypes.c_uint64()
+    ib = ctypes.c_uint64()
+    st = lib.hd_oracle_exact_f64(A.ctypes.data, A.shape[0], B.ctypes.data, B.shape[0],
+                                 A.shape[1], n_threads, ctypes.byref(h2), ctypes.byref(ia),
+                                 ctypes.byref(ib))
+    if st != 0:
+        raise ValueError("oracle exact_f64: unsupported input")
     return h2.value, int(ia.value), int(ib.value)
 
 

@@ -46,6 +46,63 @@ def test_cpu_execution_matches_reference_golden(exe, case, tmp_path):
     assert rep["ComparedPairs"] == case["compared_pairs_t1"]
 
 
+def write_wkt(path, pts):
+    with open(path, "w") as f:
+        for p in pts:
+            f.write("POINT (" + " ".join("%.17g" % v for v in p) + ")\n")
+
+
+@pytest.fixture(scope="module")
+def double_inputs(tmp_path_factory):
+    """Two 3-D WKT files whose coordinates need double precision (17
+    significant digits), and the oracle's exact FP64 directed/undirected
+    distances of the parsed doubles."""
+    import hd_oracle
+    d = tmp_path_factory.mktemp("f64")
+    rng = np.random.default_rng(4)
+    a = rng.random((3000, 3))
+    b = rng.random((2500, 3)) * 1.1
+    pa, pb = str(d / "a.wkt"), str(d / "b.wkt")
+    write_wkt(pa, a)
+    write_wkt(pb, b)
+    h_ab = np.sqrt(hd_oracle.exact_f64(a, b)[0])
+    h_ba = np.sqrt(hd_oracle.exact_f64(b, a)[0])
+    return pa, pb, float(h_ab), float(max(h_ab, h_ba))
+
+
+@pytest.mark.parametrize("undirected", [False, True])
+def test_cpu_execution_is_double(exe, double_inputs, undirected, tmp_path):
+    """-is_double -execution cpu: the CPU early-break over the parsed doubles
+    gives the oracle's exact FP64 distance (printed with 17 digits)."""
+    pa, pb, h_ab, h_und = double_inputs
+    out = tmp_path / "run.json"
+    r = subprocess.run([exe, "-input1", pa, "-input2", pb, "-input_type", "wkt", "-n_dims", "3",
+                        "-execution", "cpu", "-is_double", "-repeat", "1", "-json", str(out)]
+                       + (["-undirected"] if undirected else []), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    want = h_und if undirected else h_ab
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("HausdorffDistance")][0]
+    assert float(line.split()[-1]) == want
+    assert json.loads(out.read_text())["HDResult"] == want
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", ["hybrid", "rt", "eb"])
+def test_hd_exec_is_double(exe, double_inputs, variant, tmp_path):
+    """-is_double on the GPU (hd_solve_f64): the oracle's exact FP64 value, and
+    the driver's own -check (the CPU early-break in double) agrees."""
+    pa, pb, _, h_und = double_inputs
+    out = tmp_path / "run.json"
+    r = subprocess.run([exe, "-input1", pa, "-input2", pb, "-input_type", "wkt", "-n_dims", "3",
+                        "-variant", variant, "-is_double", "-undirected", "-repeat", "2",
+                        "-json", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("HausdorffDistance: distance")][0]
+    assert float(line.split()[-1]) == h_und
+    js = json.loads(out.read_text())
+    assert js["HDResult"] == h_und and js["Check"]["Pass"] is True
+
+
 def test_bad_flags_rejected(exe):
     c = GOLDEN[0]
     base = [exe, "-input1", os.path.join(HERE, "golden", c["a"]), "-input2",
@@ -93,15 +150,27 @@ def test_hd_exec_undirected(exe):
     assert bits(float(line.split()[-1])) == max(c["hd_bits"], d["hd_bits"])
 
 
-@pytest.mark.gpu
-def test_cpp_seam_mirror(tmp_path):
+def build_seam_probe(tmp_path):
     from hausdorffdistance_gb300 import build
     build.build_lib()
     probe = str(tmp_path / "seam_probe")
-    subprocess.run(["g++", "-std=c++17", "-O1", f"-I{os.path.join(ROOT, 'include')}",
-                    f"-I{os.path.join(ROOT, 'hausdorffdistance_gb300', 'host')}",
-                    os.path.join(HERE, "seam_probe.cpp"), "-o", probe, f"-L{BUILD}", "-lhdgpu",
-                    f"-Wl,-rpath,{BUILD}"], check=True)
+    r = subprocess.run(["g++", "-std=c++17", "-O1", f"-I{os.path.join(ROOT, 'include')}",
+                        f"-I{os.path.join(ROOT, 'hausdorffdistance_gb300', 'host')}",
+                        os.path.join(HERE, "seam_probe.cpp"), "-o", probe, f"-L{BUILD}",
+                        "-lhdgpu", f"-Wl,-rpath,{BUILD}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return probe
+
+
+def test_cpp_seam_mirror_compiles(tmp_path):
+    """The C++ seam mirror and the driver's loaders compile and link against
+    libhdgpu.so (no GPU needed)."""
+    assert os.path.exists(build_seam_probe(tmp_path))
+
+
+@pytest.mark.gpu
+def test_cpp_seam_mirror(tmp_path):
+    probe = build_seam_probe(tmp_path)
     c = [g for g in GOLDEN if g["name"] == "clusters3d_4k_ab"][0]
     r = subprocess.run([probe, os.path.join(HERE, "golden", c["a"]),
                         os.path.join(HERE, "golden", c["b"])], capture_output=True, text=True)
@@ -111,3 +180,9 @@ def test_cpp_seam_mirror(tmp_path):
     stats = json.loads(lines[1])
     assert stats["Execution"] == "GPU" and stats["Algorithm"] == "LBVH" and stats["ReportedTime"] > 0
     assert lines[2] == "error 1"
+    # The double instantiation: the oracle's exact FP64 max-min.
+    import hd_oracle
+    a = np.fromfile(os.path.join(HERE, "golden", c["a"]), dtype=np.float32, offset=8).reshape(-1, 3)
+    b = np.fromfile(os.path.join(HERE, "golden", c["b"]), dtype=np.float32, offset=8).reshape(-1, 3)
+    assert float(lines[3]) == float(np.sqrt(hd_oracle.exact_f64(a.astype(np.float64),
+                                                                b.astype(np.float64))[0]))

@@ -65,6 +65,37 @@ def test_exact_fp64_against_numpy(dims, na, nb, seed):
     assert ia == wia
 
 
+def brute_f64_rows(a, b):
+    """Exact FP64 max-min of double rows by numpy (the same left-to-right
+    formula: difference, square, sum over dims in order), with the lowest
+    row among equal maxima and its lowest column."""
+    best = np.full(len(a), np.inf)
+    col = np.zeros(len(a), np.int64)
+    for s in range(0, len(b), 2048):
+        diff = a[:, None, :] - b[None, s:s + 2048, :]
+        d = diff[..., 0] * diff[..., 0]
+        for k in range(1, a.shape[1]):
+            d = d + diff[..., k] * diff[..., k]
+        m = d.min(1)
+        better = m < best
+        col[better] = s + d.argmin(1)[better]
+        best = np.minimum(best, m)
+    i = int(np.flatnonzero(best == best.max())[0])
+    return best[i], i, int(col[i])
+
+
+@pytest.mark.parametrize("dims,na,nb,seed", [(2, 900, 700, 5), (3, 600, 800, 6), (5, 300, 400, 7)])
+def test_exact_f64_inputs_against_numpy(dims, na, nb, seed):
+    """The FP64-input oracle (double coordinates) against numpy, including a
+    set whose points differ only below float precision."""
+    rng = np.random.default_rng(seed)
+    a = rng.random((na, dims))
+    b = rng.random((nb, dims)) * 1.1
+    assert hd_oracle.exact_f64(a, b) == brute_f64_rows(a, b)
+    b2 = a[: nb // 2] + rng.normal(0.0, 1e-12, (nb // 2, dims))
+    assert hd_oracle.exact_f64(a[: nb // 2 + 7], b2) == brute_f64_rows(a[: nb // 2 + 7], b2)
+
+
 def test_exact_clustered_kdtree_vs_brute():
     a, b = synth.clusters3d(20000, seed=9)
     h2, ia, ib = hd_oracle.exact(a, b, 32)
