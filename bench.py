@@ -1,7 +1,8 @@
 """Benchmark: Hausdorff solves/s (and Gpairs/s) on one GB300 per rank.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload all|clusters3d|uniform2d|planes3d|unit64|polylines]
+                    [--workload all|clusters3d|uniform2d|planes3d|unit64|polylines|
+                                clusters3d_f64]
                     [--n POINTS] [--variant auto|eb|lbvh|grid|bf16] [--directed]
 
 A step is one undirected Hausdorff solve H(A,B) = max(h(A,B), h(B,A)) of a
@@ -18,9 +19,11 @@ datasets are not available):
   polylines   100,000 2-D polyline-pair problems, lognormal sizes
   planes3d    3-D LiDAR-like planes, |A| = |B| = 50,000,000, B rotated
               1 degree plus 0.1% outliers
+  clusters3d_f64  the clusters3d sets in float64 with N(0, 1e-7) jitter (true
+              double coordinates), solved exactly in FP64 (hd_solve_f64)
 
 The default (--workload all) measures the headline at the top level of the
-JSON line and the other four under "workloads", each with the same keys.
+JSON line and the other five under "workloads", each with the same keys.
 Inputs are larger than L2 (or the step's working set is), so no flush runs
 between steps; "config.l2" says so per workload.
 
@@ -59,10 +62,11 @@ sys.path.insert(0, ROOT)
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
 METRIC = "Hausdorff solves/s & Gpairs/s at rel err<=1e-6, chosen vs plain FP32, 1 GB300"
-ALL = ["clusters3d", "uniform2d", "unit64", "polylines", "planes3d"]
+ALL = ["clusters3d", "uniform2d", "unit64", "polylines", "planes3d", "clusters3d_f64"]
 WORKLOAD_SIZES = {"clusters3d": 10_000_000, "uniform2d": 200_000, "planes3d": 50_000_000,
-                  "unit64": 1_000_000, "polylines": 100_000}
-SEEDS = {"clusters3d": 2, "uniform2d": 1, "planes3d": 5, "unit64": 3, "polylines": 4}
+                  "unit64": 1_000_000, "polylines": 100_000, "clusters3d_f64": 10_000_000}
+SEEDS = {"clusters3d": 2, "uniform2d": 1, "planes3d": 5, "unit64": 3, "polylines": 4,
+         "clusters3d_f64": 2}
 
 
 def parse():
@@ -87,6 +91,13 @@ def make_data(name, n):
     from hausdorffdistance_gb300 import synth
     if name == "polylines":
         return synth.polylines(n_problems=n, seed=SEEDS[name])
+    if name == "clusters3d_f64":
+        # The mixture in double precision: jitter below float resolution
+        # makes every coordinate a true double.
+        a, b = synth.clusters3d(n, seed=SEEDS[name])
+        rng = np.random.default_rng(SEEDS[name] + 100)
+        return (a.astype(np.float64) + rng.normal(0.0, 1e-7, a.shape),
+                b.astype(np.float64) + rng.normal(0.0, 1e-7, b.shape))
     return getattr(synth, name)(n, seed=SEEDS[name])
 
 
@@ -98,6 +109,8 @@ def workload_desc(name, n):
         "unit64": f"64-D unit rows, |A|=|B|={n}, B = A with 1% of rows replaced",
         "polylines": (f"{n} 2-D polyline-pair problems, sizes round(LogNormal(ln 200, 1.2)) "
                       "clipped to [8, 50000]"),
+        "clusters3d_f64": (f"clusters3d in float64 (+N(0, 1e-7) jitter), |A|=|B|={n}, exact "
+                           "FP64 distance (hd_solve_f64)"),
     }[name]
 
 
@@ -617,6 +630,89 @@ def bench_batch(eng, n, steps, warmup, args, ctx):
     }
 
 
+def bench_f64(eng, name, n, steps, warmup, args, ctx):
+    """FP64 input path (hd_solve_f64) on double-precision sets: device-resident
+    solves/s, end to end from pinned float64 host buffers, the oracle's exact
+    FP64 value (must match bit for bit), and the FP32 solve of the same sets
+    rounded to float for comparison."""
+    import torch
+    stream, local, world, barrier = ctx["stream"], ctx["local"], ctx["world"], ctx["barrier"]
+    a, b = make_data(name, n)
+    undirected = not args.directed
+    ta = torch.from_numpy(a).cuda()
+    tb = torch.from_numpy(b).cuda()
+
+    def solve():
+        return eng.solve_f64(ta, tb, undirected=undirected)
+
+    ri = eng.solve_f64(ta, tb, undirected=undirected, timing=True)
+    for _ in range(warmup):
+        solve()
+    clocks = ClockSampler(local).start()
+    launches0 = eng.kernel_launches
+    barrier()
+    ms, res = _events_ms(stream, solve, steps)
+    barrier()
+    launches = eng.kernel_launches - launches0
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1e3 / ms
+    pa = torch.from_numpy(a).pin_memory()
+    pb = torch.from_numpy(b).pin_memory()
+    na, nb = pa.numpy(), pb.numpy()
+    eng.solve_f64(na, nb, undirected=undirected)
+    e2e_steps = max(3, steps // 2)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        re2e = eng.solve_f64(na, nb, undirected=undirected)
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    assert re2e.hd == res.hd
+    # The FP32 solve of the same sets rounded to float.
+    fa, fb = ta.float(), tb.float()
+    eng.solve(fa, fb, undirected=undirected)
+    ms32, _ = _events_ms(stream, lambda: eng.solve(fa, fb, undirected=undirected), 3)
+    oracle = None
+    if not args.no_oracle and ctx["rank"] == 0:
+        o = _oracle()
+        t_or = time.perf_counter()
+        h2 = o.exact_f64(a, b)[0]
+        if undirected:
+            h2 = max(h2, o.exact_f64(b, a)[0])
+        h64 = float(np.sqrt(h2))
+        oracle = {"hd64": h64, "rel_err_vs_oracle": abs(res.hd - h64) / h64,
+                  "bit_identical": res.hd == h64, "oracle_s": time.perf_counter() - t_or}
+    return {
+        "metric": "exact FP64 Hausdorff solves/s, 1 GB300", "value": value, "unit": "solves/s",
+        "n_gpus": world, "steps": steps, "warmup": warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": workload_desc(name, n), "n_a": n, "n_b": n, "n_dims": 3,
+                   "undirected": undirected, "l2": l2_note(a.nbytes + b.nbytes),
+                   "parallelism": f"replicas x{world}"},
+        "variant_used": int(res.variant_used),
+        "hd64": res.hd, "certifying_pair": [int(res.ia), int(res.ib), int(res.direction)],
+        "rows_walked_in_fp64": int(res.rechecked),
+        "rel_err_vs_oracle": None if not oracle else oracle["rel_err_vs_oracle"],
+        "oracle": oracle,
+        "fp32_solve_of_rounded_sets_ms": ms32,
+        "fp64_over_fp32_time": ms / ms32,
+        "instrumented_ms": float(ri.ms),
+        "e2e": {"value": 1.0 / t_e2e, "unit": "solves/s",
+                "h2d_bytes_per_step": int(a.nbytes + b.nbytes),
+                # three read-backs of the FP64 scalars (456 B) and one of the
+                # FP32 stage's two DevScalars (152 B each)
+                "d2h_bytes_per_step": 3 * 456 + 2 * 152, "ms_per_step": t_e2e * 1e3},
+        "cpu_baseline": None,
+        "cpu_baseline_note": "not measured: the reference has no double build of its CPU "
+                             "path (its -is_double dispatch is disabled)",
+        "clocks": clk, "gpu_launches": launches,
+    }
+
+
 def l2_note(nbytes):
     if nbytes > 130e6:
         return "inputs larger than L2 (no flush)"
@@ -668,6 +764,12 @@ def main():
             eng.solve_batch(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(), off, off,
                             undirected=not args.directed)
             out = {"profile_solve": True, "workload": name}
+        elif name == "clusters3d_f64":
+            a, b = make_data(name, n)
+            r = eng.solve_f64(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(),
+                              undirected=not args.directed)
+            out = {"profile_solve": True, "workload": name, "hd64": r.hd,
+                   "rows_walked_in_fp64": int(r.rechecked)}
         else:
             a, b = make_data(name, n)
             r = eng.solve(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(),
@@ -686,6 +788,8 @@ def main():
                                                                            args.warmup)
         if name == "polylines":
             records[name] = bench_batch(eng, n, steps, warmup, args, ctx)
+        elif name == "clusters3d_f64":
+            records[name] = bench_f64(eng, name, n, steps, warmup, args, ctx)
         else:
             records[name] = bench_single(eng, name, n, steps, warmup, args, ctx)
         torch.cuda.empty_cache()

@@ -4,40 +4,45 @@
 // instantiate its algorithms with double coordinates and double squared
 // distances (the template of src/geoms/distance.h:17-24).
 //
-// GB300 runs FP64 at a small fraction of its FP32 rate, so the search stays
-// in FP32 and FP64 arithmetic is spent only where FP32 values cannot decide.
-// Directed h(X, Y), n_dims 2 or 3 (the LBVH route):
-//  1. X and Y are rounded to float; dX = max |x_k - fl(x_k)| over X's
-//     coordinates (likewise dY).  A point moves by at most sqrt(D)·dX when
-//     rounded, so the exact distances of a rounded pair and of the original
-//     pair differ by at most r = sqrt(D)·(dX + dY).
-//  2. The FP32 LBVH solve of the rounded sets certifies a row i* and its
-//     FP32 nearest squared distance.
+// GB300 runs FP64 arithmetic at a small fraction of its FP32 rate, so the
+// search stays in FP32 and integer arithmetic, and FP64 is spent only on the
+// pair distances FP32 values cannot decide.  Directed h(X, Y), n_dims 2 or 3
+// (the LBVH route):
+//  1. X and Y are cut to float by dropping mantissa bits (integer
+//     operations); a coordinate then moves by less than one float ulp of its
+//     magnitude, so with dX = that ulp at the largest exponent of X, a point
+//     moves by at most rX = sqrt(D)·dX, and the exact distances of a cut pair
+//     and of the original pair differ by at most r = rX + rY.
+//  2. The FP32 LBVH solve of the cut sets certifies a row i* and its FP32
+//     nearest squared distance.
 //  3. Seed: the exact FP64 nearest neighbour of x_{i*} (the walk below)
 //     gives L = min_j d64(x_{i*}, y_j)^2 <= h64^2.
-//  4. A float threshold T is derived from L so that every rounded pair with
-//     FP32 squared distance <= T has FP64 squared distance < L.  A second
-//     query pass over the same trees, with the running maximum frozen at T,
-//     stops each row that has such a pair and lists the others with their
-//     FP32 minima; every row whose FP64 nearest distance is >= L is listed.
+//  4. A float threshold T is derived from L so that every cut pair with FP32
+//     squared distance <= T has FP64 squared distance < L.  A second query
+//     pass over the same trees, with the running maximum frozen at T, stops
+//     each row that has such a pair and lists the others with their FP32
+//     minima; every row whose FP64 nearest distance is >= L is listed.
 //  5. Each listed row's FP64 nearest neighbour is found by a walk of the
-//     same tree (FP64 box bounds and FP64 pair distances); a walk stops once
-//     an upper bound of its distance is strictly below the running FP64
-//     maximum (seeded with L).  The answer is the largest completed
-//     distance, the lowest row among equal ones, and that row's lowest
-//     column.
+//     same tree, one warp per row: boxes and points are tested in FP32
+//     against a float threshold P derived from the row's best FP64 distance
+//     (anything above P is provably farther in FP64), and only points within
+//     P get an FP64 distance.  A walk stops once its best (an upper bound of
+//     its distance) is strictly below the running FP64 maximum (seeded with
+//     L).  The answer is the largest completed distance, the lowest row
+//     among equal ones, and that row's lowest column.
 // When the list overflows (rows that nearly all tie: a lattice and its
 // translate) step 5 walks every row.  Other n_dims, coordinates beyond
 // +-1e18 and the eb / brute variants use an FP64 scan instead.
 //
 // Rounding bounds, with u = 2^-24, v = 2^-53 and D + 2 rounded operations
-// per squared distance over non-negative terms: the FP32 formula gives
-// d32^2 >= e^2 (1 - u)^(D+2) - (D+2) 2^-126 for the exact distance e of the
-// rounded pair (the absolute term covers underflow, even with flush to
-// zero); the FP64 formula gives d64^2 <= d^2 (1 + v)^(D+2) + (D+2) 2^-1074
-// for the exact distance d of the original pair; and |d - e| <= r.  The code
-// applies them with a further relative margin of 2^-40, which covers the
-// rounding of its own double arithmetic.
+// per squared distance over non-negative terms: an FP32 squared distance
+// lies within e^2 (1 -+ u)^(D+2) -+ (D+2) 2^-126 of the exact squared
+// distance e^2 of the cut pair (the absolute term covers underflow, even
+// with flush to zero), and the same holds for the FP32 squared distance to a
+// box; the FP64 formula lies within d^2 (1 -+ v)^(D+2) -+ (D+2) 2^-1074 of
+// the exact d^2 of the original pair; and |d - e| <= r.  The code applies
+// these with a further relative margin of 2^-40, which covers the rounding
+// of its own double arithmetic.
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -50,17 +55,18 @@ namespace {
 
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr uint32_t kListCap = 1u << 20;  // listed rows per direction
-constexpr double kRangeLimit = 1e18;     // |coordinate| the LBVH route accepts
-constexpr uint32_t kF64NonFinite = 1u, kF64Range = 2u;
-constexpr int kWalkStack = 64;           // one entry per tree level at most
+// |coordinate| the LBVH route accepts (1e18: FP32 squared distances of cut
+// points stay finite for n_dims <= 3).
+constexpr unsigned long long kRangeBits = 0x43ABC16D674EC800ull;
+constexpr uint32_t kF64NonFinite = 1u, kF64Range = 2u, kF64Tiny = 4u;
 constexpr double kMargin = 0x1p-40;
-constexpr int kWalkThreads = 128;
 constexpr int kScanThreads = 128;
+constexpr int kWalkWarps = 4;
+constexpr int kWalkStack = 2048;  // stack entries per warp (shared memory)
 
 struct RoundStats {
-  unsigned long long dmax;  // max |x - fl(x)| over the set's coordinates (double bits)
-  uint32_t flags;           // kF64NonFinite | kF64Range
-  uint32_t pad;
+  uint32_t emax;   // largest biased double exponent of a coordinate cut to a normal float
+  uint32_t flags;  // kF64NonFinite | kF64Range | kF64Tiny (a nonzero |x| < 2^-126)
 };
 
 struct F64Dir {
@@ -90,6 +96,22 @@ __device__ __forceinline__ double bits_d(unsigned long long b) {
   return __longlong_as_double((long long) b);
 }
 
+// x cut to float by integer operations: the sign, the exponent rebiased,
+// the top 23 mantissa bits (truncation, |x - cut| < one float ulp of |x|).
+// Magnitudes below 2^-126 become a signed zero (displacement < 2^-126);
+// magnitudes of 2^128 and above (never on the LBVH route) become infinity.
+__device__ __forceinline__ float cut_to_float(double x) {
+  const unsigned long long u = dbits(x);
+  const uint32_t hi = (uint32_t) (u >> 32);
+  const uint32_t ex = (hi >> 20) & 0x7FFu;
+  uint32_t f = hi & 0x80000000u;
+  if (ex >= 1023u + 128u)
+    f |= 0x7F800000u;
+  else if (ex >= 1023u - 126u)
+    f |= ((ex - 1023u + 127u) << 23) | (uint32_t) ((u >> 29) & 0x7FFFFFu);
+  return __uint_as_float(f);
+}
+
 // The reference formula in FP64: per-dimension difference, squared, summed
 // left to right, no FMA.
 template <int D>
@@ -104,8 +126,33 @@ __device__ __forceinline__ double d2_64(const double* x, const double* y) {
   return s;
 }
 
+// FP32 squared distance of cut points (any correctly rounded order).
+template <int D>
+__device__ __forceinline__ float d2_32(const float* q, const float4& b) {
+  const float dx = __fsub_rn(q[0], b.x), dy = __fsub_rn(q[1], b.y);
+  float s = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+  if (D == 3) {
+    const float dz = __fsub_rn(q[2], b.z);
+    s = __fadd_rn(s, __fmul_rn(dz, dz));
+  }
+  return s;
+}
+
+// FP32 squared distance from a cut point to a box (0 inside).
+template <int D>
+__device__ __forceinline__ float box_d2_32(const float* q, const float4& xy, float lz, float hz) {
+  const float gx = fmaxf(fmaxf(__fsub_rn(xy.x, q[0]), __fsub_rn(q[0], xy.z)), 0.0f);
+  const float gy = fmaxf(fmaxf(__fsub_rn(xy.y, q[1]), __fsub_rn(q[1], xy.w)), 0.0f);
+  float s = __fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy));
+  if (D == 3) {
+    const float gz = fmaxf(fmaxf(__fsub_rn(lz, q[2]), __fsub_rn(q[2], hz)), 0.0f);
+    s = __fadd_rn(s, __fmul_rn(gz, gz));
+  }
+  return s;
+}
+
 // An upper bound of the FP64 nearest squared distance of a row whose FP32
-// nearest squared distance over the rounded sets is m32 (+inf: none known).
+// nearest squared distance over the cut sets is m32 (+inf: none known).
 template <int D>
 __device__ __forceinline__ double upper_from32(float m32, double rxy) {
   if (!(m32 < INFINITY)) return INFINITY;
@@ -114,51 +161,47 @@ __device__ __forceinline__ double upper_from32(float m32, double rxy) {
   return d * d * (1.0 + kMargin) + 0x1p-1000;
 }
 
-// A lower bound of the FP64 squared distance from x to every original point
-// whose rounded point lies in the box (float bounds), ry = how far a
-// target point moves when rounded.
+// The float threshold P of a row whose best FP64 squared distance so far is
+// best: a cut point (or box) whose FP32 squared distance from the cut row
+// exceeds P is at FP64 squared distance > best from the row (every original
+// point behind it).  +inf while best is unknown.
 template <int D>
-__device__ __forceinline__ double box_lb64(const double* x, const float4& xy, float lz, float hz,
-                                           double ry) {
-  const double g0 = fmax(fmax((double) xy.x - x[0], x[0] - (double) xy.z), 0.0);
-  const double g1 = fmax(fmax((double) xy.y - x[1], x[1] - (double) xy.w), 0.0);
-  double s = g0 * g0 + g1 * g1;
-  if (D == 3) {
-    const double g2 = fmax(fmax((double) lz - x[2], x[2] - (double) hz), 0.0);
-    s += g2 * g2;
-  }
-  const double d = sqrt(s) * (1.0 - kMargin) - ry;
-  if (d <= 0.0) return 0.0;
-  return d * d * (1.0 - kMargin) - 0x1p-1000;
+__device__ __forceinline__ float prune32(double best, double rxy) {
+  if (!(best < INFINITY)) return INFINITY;
+  const double d = sqrt((best + 0x1p-1000) / (1.0 - kMargin)) * (1.0 + kMargin) + rxy;
+  const double p =
+      (d * d * (1.0 + (D + 2) * 0x1p-24 * 1.01) + (D + 2) * 0x1p-126) * (1.0 + kMargin);
+  return p >= (double) FLT_MAX ? INFINITY : __double2float_ru(p);
 }
 
-// Rounds a set to float (Xf may be null: check only) and records the
-// largest rounding displacement of a coordinate and the range flags.
+// Cuts a set to float (Xf may be null: check only); records the largest
+// exponent, non-finite and out-of-range values, and tiny magnitudes.
+// Integer operations only.
 __global__ void k_f64_round(const double* __restrict__ X, uint64_t total, float* __restrict__ Xf,
                             RoundStats* st) {
-  double dm = 0.0;
-  uint32_t fl = 0;
+  uint32_t emax = 0, fl = 0;
   for (uint64_t t = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; t < total;
        t += (uint64_t) gridDim.x * blockDim.x) {
     const double x = X[t];
-    const float f = __double2float_rn(x);
-    if (!isfinite(x))
+    const unsigned long long a = dbits(x) & 0x7FFFFFFFFFFFFFFFull;
+    const uint32_t ex = (uint32_t) (a >> 52);
+    if (ex == 0x7FFu)
       fl |= kF64NonFinite;
-    else if (fabs(x) > kRangeLimit)
+    else if (a > kRangeBits)
       fl |= kF64Range;
-    if (Xf) Xf[t] = f;
-    // Exact: f is x rounded to float, so x and f are within a factor of two
-    // (or f = 0 and the difference is x).
-    const double d = fabs(x - (double) f);
-    if (d > dm) dm = d;
+    if (ex >= 1023u - 126u)
+      emax = max(emax, ex);
+    else if (a != 0ull)
+      fl |= kF64Tiny;
+    if (Xf) Xf[t] = cut_to_float(x);
   }
 #pragma unroll
   for (int o = 16; o; o >>= 1) {
-    dm = fmax(dm, __shfl_xor_sync(0xFFFFFFFFu, dm, o));
+    emax = max(emax, __shfl_xor_sync(0xFFFFFFFFu, emax, o));
     fl |= __shfl_xor_sync(0xFFFFFFFFu, fl, o);
   }
   if ((threadIdx.x & 31) == 0) {
-    if (dm > 0.0) atomicMax(&st->dmax, dbits(dm));
+    if (emax) atomicMax(&st->emax, emax);
     if (fl) atomicOr(&st->flags, fl);
   }
 }
@@ -174,7 +217,7 @@ __global__ void k_f64_init(F64Aux* aux) {
     z.cand_count = 0u;
     z.thr = -1.0f;
     aux->dir[k] = z;
-    aux->round[k].dmax = 0ull;
+    aux->round[k].emax = 0u;
     aux->round[k].flags = 0u;
   }
 }
@@ -189,11 +232,10 @@ __global__ void k_f64_seed_entries(const DevScalars* sc, F64Aux* aux, int count)
 struct WalkArgs {
   const double* X;        // query set, caller's rows
   const double* Y;        // target set, caller's rows
-  LbvhTree t;             // the target's tree over its rounded points
+  LbvhTree t;             // the target's tree over its cut points
   const RowEntry* list;   // rows to walk, or null: every row of X
   uint64_t n_rows;
-  double ry;              // bound on a target point's displacement by rounding
-  double rxy;             // the same for a pair
+  double rxy;             // bound on |d(x, y) - d(cut x, cut y)|
   F64Dir* f;
   double* row_min;        // per walked row: FP64 nearest squared distance, -1 if stopped
   uint32_t* row_col;      // and its lowest nearest column
@@ -203,18 +245,37 @@ struct WalkSets {
   WalkArgs d[2];
 };
 
-// Exact FP64 nearest neighbour of each walked row: thread per row,
-// depth-first with the nearer child first and the farther one stacked with
-// its bound (one entry per level: the tree is at most 64 levels deep).
-// A subtree is skipped when its bound exceeds the best distance so far
-// (never when equal, so that the lowest column among ties is found); the
-// walk stops once its best (an upper bound of the row's distance) is
-// strictly below the running maximum.
+// The lexicographically smaller of (d, j) over the warp.
+__device__ __forceinline__ void warp_min_pair(double& d, uint32_t& j) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const double od = __shfl_xor_sync(0xFFFFFFFFu, d, o);
+    const uint32_t oj = __shfl_xor_sync(0xFFFFFFFFu, j, o);
+    if (od < d || (od == d && oj < j)) {
+      d = od;
+      j = oj;
+    }
+  }
+}
+
+// Exact FP64 nearest neighbour of each walked row, one warp per row.  Up to
+// 32 stacked subtrees are expanded per step (one per lane; the stack lives in
+// shared memory); a subtree or point is skipped when its FP32 squared
+// distance from the cut row exceeds the row's threshold P (never when its
+// FP64 distance could equal the best, so that the lowest column among ties
+// is found); points within P get their FP64 distance.  A row without a
+// starting bound first descends to the nearest leaf along one path.  The
+// walk stops once the best (an upper bound of the row's distance) is
+// strictly below the running maximum.  A walk that would overflow the stack
+// sets kErrInternal (the solve fails) rather than drop a subtree.
 template <int D>
-__global__ void __launch_bounds__(kWalkThreads) k_f64_walk(WalkSets ws) {
+__global__ void __launch_bounds__(kWalkWarps * 32) k_f64_walk(WalkSets ws) {
+  __shared__ uint32_t stk[kWalkWarps][kWalkStack];
   const WalkArgs& w = ws.d[blockIdx.y];
-  const uint64_t k = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint64_t k = blockIdx.x * (uint64_t) kWalkWarps + warp;
   if (k >= w.n_rows) return;
+  uint32_t* st = stk[warp];
   uint32_t row;
   double best = INFINITY;
   if (w.list) {
@@ -225,67 +286,129 @@ __global__ void __launch_bounds__(kWalkThreads) k_f64_walk(WalkSets ws) {
     row = (uint32_t) k;
   }
   double x[D];
+  float q[D];
 #pragma unroll
-  for (int i = 0; i < D; ++i) x[i] = w.X[(uint64_t) row * D + i];
+  for (int i = 0; i < D; ++i) {
+    x[i] = w.X[(uint64_t) row * D + i];
+    q[i] = cut_to_float(x[i]);
+  }
   uint32_t col = 0xFFFFFFFFu;
-  uint32_t stk[kWalkStack];
-  double slb[kWalkStack];
-  int sp = 0;
-  uint32_t node = *w.t.root;
-  bool have = true;
-  bool stopped = best < bits_d(ld_relaxed_u64(&w.f->max64));
-  while (!stopped) {
-    if (!have) {
-      if (sp == 0) break;
-      --sp;
-      if (slb[sp] > best) continue;
-      node = stk[sp];
-    }
-    have = true;
-    if (node & kLeafBit) {
-      const uint64_t p0 = (uint64_t) (node & ~kLeafBit) * w.t.leaf;
-      const uint32_t cnt = (uint32_t) min((uint64_t) w.t.leaf, w.t.n - p0);
-      for (uint32_t t = 0; t < cnt; ++t) {
-        const uint32_t j = __float_as_uint(w.t.pts[p0 + t].w);
-        double y[D];
+  float P = prune32<D>(best, w.rxy);
+  auto read_max = [&]() {
+    unsigned long long m = 0;
+    if (lane == 0) m = ld_relaxed_u64(&w.f->max64);
+    return bits_d(__shfl_sync(0xFFFFFFFFu, m, 0));
+  };
+  // Scans leaf `leaf` on this lane: FP64 distances of its points within P.
+  auto scan_leaf = [&](uint32_t leaf, double& lb, uint32_t& lc) {
+    const uint64_t p0 = (uint64_t) leaf * w.t.leaf;
+    const uint32_t cnt = (uint32_t) min((uint64_t) w.t.leaf, w.t.n - p0);
+    for (uint32_t t = 0; t < cnt; ++t) {
+      const float4 b = w.t.pts[p0 + t];
+      if (d2_32<D>(q, b) > P) continue;
+      const uint32_t j = __float_as_uint(b.w);
+      double y[D];
 #pragma unroll
-        for (int i = 0; i < D; ++i) y[i] = w.Y[(uint64_t) j * D + i];
-        const double d = d2_64<D>(x, y);
-        if (d < best || (d == best && j < col)) {
-          best = d;
-          col = j;
+      for (int i = 0; i < D; ++i) y[i] = w.Y[(uint64_t) j * D + i];
+      const double d = d2_64<D>(x, y);
+      if (d < lb || (d == lb && j < lc)) {
+        lb = d;
+        lc = j;
+      }
+    }
+  };
+  uint32_t root = *w.t.root;
+  if (!(best < INFINITY)) {
+    // No bound yet: lane 0 follows the nearer child down to a leaf, whose
+    // scan gives one.
+    uint32_t node = root;
+    if (lane == 0) {
+      while (!(node & kLeafBit)) {
+        const float4* nd = w.t.nodes + 4 * (uint64_t) node;
+        const float4 n0 = nd[0], n1 = nd[1], n3 = nd[3];
+        const float4 n2 = D == 3 ? nd[2] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float dL = box_d2_32<D>(q, n0, n2.x, n2.y);
+        const float dR = box_d2_32<D>(q, n1, n2.z, n2.w);
+        node = __float_as_uint(dL <= dR ? n3.x : n3.y);
+      }
+    }
+    node = __shfl_sync(0xFFFFFFFFu, node, 0);
+    double lb = INFINITY;
+    uint32_t lc = 0xFFFFFFFFu;
+    if (lane == 0) scan_leaf(node & ~kLeafBit, lb, lc);
+    lb = __shfl_sync(0xFFFFFFFFu, lb, 0);
+    lc = __shfl_sync(0xFFFFFFFFu, lc, 0);
+    best = lb;
+    col = lc;
+    // P stays +inf until a point is found (a leaf scan with P = +inf
+    // evaluates every point, so one was).
+    P = prune32<D>(best, w.rxy);
+  }
+  bool stopped = best < read_max();
+  if (lane == 0) st[0] = root;
+  int sp = 1;
+  __syncwarp();
+  int round = 0;
+  while (sp > 0 && !stopped) {
+    const int take = min(sp, 32);
+    const bool has = lane < take;
+    const uint32_t node = has ? st[sp - take + lane] : 0u;
+    sp -= take;
+    __syncwarp();
+    uint32_t push0 = 0, push1 = 0;
+    int npush = 0;
+    double lb = best;
+    uint32_t lc = col;
+    if (has) {
+      if (node & kLeafBit) {
+        scan_leaf(node & ~kLeafBit, lb, lc);
+      } else {
+        const float4* nd = w.t.nodes + 4 * (uint64_t) node;
+        const float4 n0 = nd[0], n1 = nd[1], n3 = nd[3];
+        const float4 n2 = D == 3 ? nd[2] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float dL = box_d2_32<D>(q, n0, n2.x, n2.y);
+        const float dR = box_d2_32<D>(q, n1, n2.z, n2.w);
+        const uint32_t left = __float_as_uint(n3.x), right = __float_as_uint(n3.y);
+        const bool wL = dL <= P, wR = dR <= P;
+        // Nearer child pushed last, so that it is popped first.
+        if (wL && wR) {
+          push0 = dL <= dR ? right : left;
+          push1 = dL <= dR ? left : right;
+          npush = 2;
+        } else if (wL || wR) {
+          push0 = wL ? left : right;
+          npush = 1;
         }
       }
-      have = false;
-      if (best < bits_d(ld_relaxed_u64(&w.f->max64))) stopped = true;
-      continue;
     }
-    const float4* nd = w.t.nodes + 4 * (uint64_t) node;
-    const float4 n0 = nd[0], n1 = nd[1], n3 = nd[3];
-    const float4 n2 = D == 3 ? nd[2] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const double lbL = box_lb64<D>(x, n0, n2.x, n2.y, w.ry);
-    const double lbR = box_lb64<D>(x, n1, n2.z, n2.w, w.ry);
-    const uint32_t left = __float_as_uint(n3.x), right = __float_as_uint(n3.y);
-    const bool wL = lbL <= best, wR = lbR <= best;
-    if (wL && wR) {
-      if (sp == kWalkStack) {
-        atomicOr(w.status, kErrInternal);
-        stopped = true;
-        break;
-      }
-      const bool nearL = lbL <= lbR;
-      stk[sp] = nearL ? right : left;
-      slb[sp] = nearL ? lbR : lbL;
-      ++sp;
-      node = nearL ? left : right;
-    } else if (wL) {
-      node = left;
-    } else if (wR) {
-      node = right;
-    } else {
-      have = false;
+    warp_min_pair(lb, lc);
+    if (lb < best || (lb == best && lc < col)) {
+      best = lb;
+      col = lc;
+      P = prune32<D>(best, w.rxy);
     }
+    // Compact the pushes: lanes in order, two slots per lane at most.
+    int off = npush;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xFFFFFFFFu, off, o);
+      if (lane >= o) off += v;
+    }
+    const int total = __shfl_sync(0xFFFFFFFFu, off, 31);
+    off -= npush;
+    if (sp + total > kWalkStack) {
+      if (lane == 0) atomicOr(w.status, kErrInternal);
+      stopped = true;
+      break;
+    }
+    if (npush > 0) st[sp + off] = push0;
+    if (npush > 1) st[sp + off + 1] = push1;
+    sp += total;
+    __syncwarp();
+    if ((++round & 7) == 0 && best < read_max()) stopped = true;
   }
+  if (!stopped && best < read_max()) stopped = true;
+  if (lane != 0) return;
   if (stopped) {
     w.row_min[k] = -1.0;
     w.row_col[k] = 0u;
@@ -420,7 +543,7 @@ __global__ void k_f64_pick(const double* __restrict__ row_min, const uint32_t* _
 struct F64Call {
   const double* X[2];
   const double* Y[2];
-  double ry[2], rxy[2];
+  double rxy[2];
   int dims;
   F64Aux* aux;
   double* seed_min;
@@ -429,11 +552,11 @@ struct F64Call {
 
 hd_status launch_walks(Ctx& c, const WalkSets& ws, int count, uint64_t max_rows, int dims) {
   if (max_rows == 0) return HD_OK;
-  const dim3 grid((unsigned) ((max_rows + kWalkThreads - 1) / kWalkThreads), count);
+  const dim3 grid((unsigned) ((max_rows + kWalkWarps - 1) / kWalkWarps), count);
   if (dims == 2)
-    k_f64_walk<2><<<grid, kWalkThreads, 0, c.stream>>>(ws);
+    k_f64_walk<2><<<grid, kWalkWarps * 32, 0, c.stream>>>(ws);
   else
-    k_f64_walk<3><<<grid, kWalkThreads, 0, c.stream>>>(ws);
+    k_f64_walk<3><<<grid, kWalkWarps * 32, 0, c.stream>>>(ws);
   return after_launch(c, "f64_walk");
 }
 
@@ -488,7 +611,6 @@ hd_status f64_seed(Ctx& c, F64Plan& plan, int count) {
     w.t = plan.tree[k];
     w.list = &call.aux->seed[k];
     w.n_rows = 1;
-    w.ry = call.ry[k];
     w.rxy = call.rxy[k];
     w.f = &call.aux->dir[k];
     w.row_min = call.seed_min + k;
@@ -594,10 +716,13 @@ hd_status hd_solve_f64(hd_ctx* c, const double* A, uint64_t n_a, const double* B
                   "coordinates beyond +-1e18 need the eb or brute variant on the FP64 path");
     lbvh = false;
   }
+  // How far a point moves when cut to float: less than one float ulp per
+  // coordinate at the set's largest exponent (2^-126 for tiny magnitudes).
   double rset[2];
   for (int k = 0; k < 2; ++k) {
-    double dm;
-    std::memcpy(&dm, &h->round[k].dmax, sizeof(dm));
+    double dm = 0.0;
+    if (h->round[k].emax) dm = std::ldexp(1.0, (int) h->round[k].emax - 1023 - 23);
+    if (h->round[k].flags & kF64Tiny) dm = std::max(dm, 0x1p-126);
     rset[k] = std::sqrt((double) n_dims) * dm * (1.0 + kMargin);
   }
 
@@ -613,7 +738,6 @@ hd_status hd_solve_f64(hd_ctx* c, const double* A, uint64_t n_a, const double* B
     for (int k = 0; k < ndir; ++k) {
       call.X[k] = d64[k];
       call.Y[k] = d64[1 - k];
-      call.ry[k] = rset[1 - k];
       call.rxy[k] = (rset[0] + rset[1]) * (1.0 + kMargin);
       ins[k] = DirInput{f32[k], nn[k], f32[1 - k], nn[1 - k], n_dims, k,
                         (flags & HD_COUNT_PAIRS) != 0};
@@ -659,7 +783,6 @@ hd_status hd_solve_f64(hd_ctx* c, const double* A, uint64_t n_a, const double* B
       w.t = plan.tree[k];
       w.list = h->dir[k].cand_count <= kListCap ? plan.cand[k] : nullptr;
       w.n_rows = walked[k];
-      w.ry = call.ry[k];
       w.rxy = call.rxy[k];
       w.f = &aux->dir[k];
       w.row_min = row_min + off[k];
