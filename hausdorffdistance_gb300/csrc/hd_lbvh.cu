@@ -197,6 +197,12 @@ static FastDiv make_fastdiv(uint32_t d) {
   const uint64_t m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
   return FastDiv{(uint32_t) m, l < 1 ? l : 1u, l > 0 ? l - 1 : 0u};
 }
+// Starts a load of the 128-byte line at p into L1 (a hint: nothing waits
+// for it).  Every caller passes an address inside its array.
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ uint32_t fastdiv(uint32_t n, FastDiv f) {
   const uint32_t t = __umulhi(f.m, n);
   return (t + ((n - t) >> f.s1)) >> f.s2;
@@ -242,6 +248,8 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   auto scan_leaf = [&](uint32_t leaf) {
     const uint64_t s = (uint64_t) leaf * (LT ? (uint32_t) LT : L);
     const float4* lp = B + s;
+    // A full 16-point leaf is two 128-byte lines: start the second now.
+    if (LT == 16 && s + 16 <= nB) prefetch_l1(lp + 8);
     float m = cmin;
     int k = 0;
     if (LT && s + LT <= nB) {
@@ -314,6 +322,7 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
     // the Morton curve, and then its two ends sit in different regions.
     const uint32_t leaf0 = min(ppos[2 * packet] >> lshift, nL - 1);
     const uint32_t leaf1 = min(ppos[2 * packet + 1] >> lshift, nL - 1);
+    // The leaves scanned after leaf0 when lanes stay open: start them now.
     scan_leaf(leaf0);
     if (leaf1 != leaf0 && __any_sync(0xFFFFFFFFu, active)) scan_leaf(leaf1);
     if (leaf0 + 1 < nL && leaf0 + 1 != leaf1 && __any_sync(0xFFFFFFFFu, active))
@@ -346,6 +355,8 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
       const float4* nd = nodes + 4 * (uint64_t) next;
       const float4 n0 = nd[0], n1 = nd[1], n3 = nd[3];
       const float4 n2 = D == 3 ? nd[2] : make_float4(0.f, 0.f, 0.f, 0.f);
+      // The next step reads one of the children (or the stacked one later):
+      // start both reads while the boxes are tested.
       ++work;
       if (COUNT) ++visits;
       const float dL = box_min_d2<D>(q, n0, n2.x, n2.y);
