@@ -44,6 +44,7 @@ namespace {
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr int kQueryWarps = 4;
 constexpr int kStack = 64;
+constexpr uint32_t kPacket = 64;  // queries per warp packet (two per lane)
 // A packet that has visited `budget` nodes and leaves (an option, tuned)
 // queues its open queries for the deferred pass instead of finishing them
 // alone: a query whose nearest neighbour is far (an outlier) must prove that
@@ -180,10 +181,6 @@ __device__ __forceinline__ float box_max_d2(const float4& q, const float4& xy, f
 // box bound and the FP32 pair formula each carry a few ulps of rounding.
 constexpr float kMaxDistMargin = 1.0f + 1.0f / 65536.0f;
 
-// Warp-packet traversal.  A packet is 32 consecutive Morton-sorted queries
-// (or 32 entries of a sample list).
-// LT: leaf size known at compile time (16, the tuned size), or 0 for a
-// runtime leaf size L.
 // Division of a 32-bit value by a run-time constant d, with the multiplier
 // m and shifts s1, s2 prepared on the host (Granlund and Montgomery,
 // "Division by Invariant Integers using Multiplication", PLDI 1994):
@@ -208,6 +205,9 @@ __device__ __forceinline__ uint32_t fastdiv(uint32_t n, FastDiv f) {
   return (t + ((n - t) >> f.s1)) >> f.s2;
 }
 
+// Warp-packet traversal of kPacket consecutive Morton-sorted queries.
+// LT: leaf size known at compile time (16, the tuned size), or 0 for a
+// runtime leaf size L.
 template <int D, bool COUNT, int LT>
 __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, uint64_t nItems, uint32_t pstride,
                  uint64_t rows, FastDiv rows_div, const uint32_t* __restrict__ ppos,
@@ -217,23 +217,33 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
                  uint32_t cand_cap) {
   __shared__ uint32_t stk[kQueryWarps][kStack];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // Packets (32 consecutive Morton-sorted queries) are visited in a
-  // transposed order: warp w takes packet (w mod rows) * pstride + w / rows.
-  // The first `rows` warps — the first wave — are every pstride-th packet,
-  // spread over the whole Morton range, so the running maximum rises to
-  // nearly its final value while the bulk of the packets is still queued
-  // (the reference samples with EB for the same purpose, hybrid.h:128-168).
-  // 32-bit arithmetic: packet counts stay below 2^27 (point sets < 2^32).
+  const unsigned below = (1u << lane) - 1u;
+  // Packets (kPacket = 64 consecutive Morton-sorted queries, two per lane:
+  // items lane and 32 + lane) are visited in a transposed order: warp w
+  // takes packet (w mod rows) * pstride + w / rows.  The first `rows` warps
+  // — the first wave — are every pstride-th packet, spread over the whole
+  // Morton range, so the running maximum rises to nearly its final value
+  // while the bulk of the packets is still queued (the reference samples
+  // with EB for the same purpose, hybrid.h:128-168).  Two queries per lane
+  // let every broadcast load of a leaf point or a node serve 64 queries and
+  // halve the chains of dependent loads per query.
+  // 32-bit arithmetic: packet counts stay below 2^26 (point sets < 2^32).
   const uint32_t w = blockIdx.x * kQueryWarps + warp;
   const uint32_t r32 = (uint32_t) rows;
   const uint32_t wq = fastdiv(w, rows_div);
   const uint64_t packet = (uint64_t) (w - wq * r32) * pstride + wq;
-  if (packet * 32 >= nItems) return;
-  const uint64_t item = packet * 32 + lane;
-  bool active = item < nItems;
-  float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (active) q = Q[item];
-  float cmin = INFINITY;
+  if (packet * kPacket >= nItems) return;
+  uint64_t item[2];
+  bool act[2];
+  float4 q[2];
+  float cmin[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    item[h] = packet * kPacket + 32 * h + lane;
+    act[h] = item[h] < nItems;
+    q[h] = act[h] ? Q[item[h]] : make_float4(0.f, 0.f, 0.f, 0.f);
+    cmin[h] = INFINITY;
+  }
   float dstk[kStack];
   unsigned long long key = 0;
   if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
@@ -241,143 +251,151 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   unsigned long long pairs = 0, visits = 0, leafv = 0;
   uint32_t work = 0;  // nodes and leaves this packet has visited
   bool may_defer = defer != nullptr;
+  auto open = [&]() { return act[0] || act[1]; };
+  auto count_pairs = [&](uint64_t k) {
+    pairs += k * (uint64_t) (__popc(__ballot_sync(0xFFFFFFFFu, act[0])) +
+                             __popc(__ballot_sync(0xFFFFFFFFu, act[1])));
+  };
 
   // Scans one leaf with every lane of the packet (points read as broadcast
-  // loads, four at a time); stops as soon as no lane still needs a point,
-  // and lets lanes that found a point within the running maximum stop.
+  // loads, four at a time, each tested against both of a lane's queries);
+  // stops as soon as no query still needs a point, and stops the queries
+  // that found a point within the running maximum.
   auto scan_leaf = [&](uint32_t leaf) {
     const uint64_t s = (uint64_t) leaf * (LT ? (uint32_t) LT : L);
     const float4* lp = B + s;
     // A full 16-point leaf is two 128-byte lines: start the second now.
     if (LT == 16 && s + 16 <= nB) prefetch_l1(lp + 8);
-    float m = cmin;
+    float m0 = cmin[0], m1 = cmin[1];
     int k = 0;
+    bool settled = false;  // every open query is within the running maximum
     if (LT && s + LT <= nB) {
       // Full leaf of a compile-time size: fixed offsets, no clamping.
-      bool settled = false;  // every active lane is within the running maximum
 #pragma unroll
       for (int k0 = 0; k0 < (LT ? LT : 4); k0 += 4) {
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const float4 b = __ldg(lp + k0 + u);
-          m = fminf(m, d2_pt_packed<D>(q, b));
+          m0 = fminf(m0, d2_pt_packed<D>(q[0], b));
+          m1 = fminf(m1, d2_pt_packed<D>(q[1], b));
         }
         k = k0 + 4;
-        if (!__any_sync(0xFFFFFFFFu, active && m > thr)) {
+        if (!__any_sync(0xFFFFFFFFu, (act[0] && m0 > thr) || (act[1] && m1 > thr))) {
           settled = true;
           break;
         }
       }
-      if (active) cmin = m;
-      ++work;
-      if (COUNT) {
-        ++leafv;
-        pairs += (unsigned long long) k * __popc(__ballot_sync(0xFFFFFFFFu, active));
-      }
-      // The running maximum is re-read only when some lane is still open.
-      if (!settled) {
-        if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
-        thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
-      }
-      if (active && cmin <= thr) active = false;
-      return;
-    }
-    const int cnt = (int) min((uint64_t) L, nB - s);
-    bool settled = false;
-    for (; k < cnt; k += 4) {
-      // Every lane reads the same point: one broadcast load per point.
+    } else {
+      const int cnt = (int) min((uint64_t) L, nB - s);
+      for (; k < cnt; k += 4) {
+        // Every lane reads the same point: one broadcast load per point.
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const float4 b = __ldg(lp + min(k + u, cnt - 1));
-        m = fminf(m, d2_pt_packed<D>(q, b));
+        for (int u = 0; u < 4; ++u) {
+          const float4 b = __ldg(lp + min(k + u, cnt - 1));
+          m0 = fminf(m0, d2_pt_packed<D>(q[0], b));
+          m1 = fminf(m1, d2_pt_packed<D>(q[1], b));
+        }
+        if (!__any_sync(0xFFFFFFFFu, (act[0] && m0 > thr) || (act[1] && m1 > thr))) {
+          k += 4;
+          settled = true;
+          break;
+        }
       }
-      if (!__any_sync(0xFFFFFFFFu, active && m > thr)) {
-        k += 4;
-        settled = true;
-        break;
-      }
+      k = min(k, cnt);
     }
-    if (active) cmin = m;
+    if (act[0]) cmin[0] = m0;
+    if (act[1]) cmin[1] = m1;
     ++work;
     if (COUNT) {
       ++leafv;
-      pairs += (unsigned long long) min(k, cnt) * __popc(__ballot_sync(0xFFFFFFFFu, active));
+      count_pairs((uint64_t) k);
     }
+    // The running maximum is re-read only when some query is still open.
     if (!settled) {
       if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
       thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
     }
-    if (active && cmin <= thr) active = false;
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+      if (act[h] && cmin[h] <= thr) act[h] = false;
   };
 
   {
     // Warm start: a query's Morton code in B's frame locates it in B's
     // sorted codes, so the B leaves at the packet's position (precomputed
-    // per packet) are spatially close.  Scanning that leaf and its neighbours lets most lanes
-    // stop before any traversal, and gives the others a small running
-    // minimum that prunes the traversal.
+    // per packet) are spatially close.  Scanning that leaf and its
+    // neighbours lets most queries stop before any traversal, and gives the
+    // others a small running minimum that prunes the traversal.
     const uint32_t lshift = __ffs(L) - 1;  // L is a power of two
     const uint32_t nL = (uint32_t) ((nB + L - 1) >> lshift);
     // Both ends of the packet are looked up: a packet can straddle a jump of
     // the Morton curve, and then its two ends sit in different regions.
     const uint32_t leaf0 = min(ppos[2 * packet] >> lshift, nL - 1);
     const uint32_t leaf1 = min(ppos[2 * packet + 1] >> lshift, nL - 1);
-    // The leaves scanned after leaf0 when lanes stay open: start them now.
     scan_leaf(leaf0);
-    if (leaf1 != leaf0 && __any_sync(0xFFFFFFFFu, active)) scan_leaf(leaf1);
-    if (leaf0 + 1 < nL && leaf0 + 1 != leaf1 && __any_sync(0xFFFFFFFFu, active))
+    if (leaf1 != leaf0 && __any_sync(0xFFFFFFFFu, open())) scan_leaf(leaf1);
+    if (leaf0 + 1 < nL && leaf0 + 1 != leaf1 && __any_sync(0xFFFFFFFFu, open()))
       scan_leaf(leaf0 + 1);
-    if (leaf0 > 0 && __any_sync(0xFFFFFFFFu, active)) scan_leaf(leaf0 - 1);
+    if (leaf0 > 0 && __any_sync(0xFFFFFFFFu, open())) scan_leaf(leaf0 - 1);
   }
 
   int sp = 0;
   uint32_t next = root;
   bool have = true;
   for (;;) {
-    if (!__any_sync(0xFFFFFFFFu, active)) break;
+    if (!__any_sync(0xFFFFFFFFu, open())) break;
     if (may_defer && work >= budget) {
       // Over budget: queue the open queries (as many as the queue holds;
-      // lanes beyond it finish here, with no budget).
+      // queries beyond it finish here, with no budget).
       may_defer = false;
-      const unsigned open = __ballot_sync(0xFFFFFFFFu, active);
+      const unsigned o0 = __ballot_sync(0xFFFFFFFFu, act[0]);
+      const unsigned o1 = __ballot_sync(0xFFFFFFFFu, act[1]);
       uint32_t base = 0;
-      if (lane == 0) base = atomicAdd(&sc->heavy_count, (uint32_t) __popc(open));
+      if (lane == 0) base = atomicAdd(&sc->heavy_count, (uint32_t) (__popc(o0) + __popc(o1)));
       base = __shfl_sync(0xFFFFFFFFu, base, 0);
-      const uint32_t slot = base + __popc(open & ((1u << lane) - 1u));
-      if (active && slot < kDeferCap) {
-        defer[slot] = Deferred{(uint32_t) item, __float_as_uint(cmin)};
-        active = false;
-      }
+      const uint32_t slot[2] = {base + __popc(o0 & below),
+                                base + __popc(o0) + __popc(o1 & below)};
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+        if (act[h] && slot[h] < kDeferCap) {
+          defer[slot[h]] = Deferred{(uint32_t) item[h], __float_as_uint(cmin[h])};
+          act[h] = false;
+        }
       continue;
     }
     if (have && !(next & kLeafBit)) {
-      // Internal node: test both children for every lane.
+      // Internal node: test both children for both queries of every lane.
       const float4* nd = nodes + 4 * (uint64_t) next;
       const float4 n0 = nd[0], n1 = nd[1], n3 = nd[3];
       const float4 n2 = D == 3 ? nd[2] : make_float4(0.f, 0.f, 0.f, 0.f);
-      // The next step reads one of the children (or the stacked one later):
-      // start both reads while the boxes are tested.
       ++work;
       if (COUNT) ++visits;
-      const float dL = box_min_d2<D>(q, n0, n2.x, n2.y);
-      const float dR = box_min_d2<D>(q, n1, n2.z, n2.w);
-      if (active && thr >= 0.0f) {
-        const float mL = box_max_d2<D>(q, n0, n2.x, n2.y);
-        const float mR = box_max_d2<D>(q, n1, n2.z, n2.w);
-        if (fminf(mL, mR) * kMaxDistMargin <= thr) active = false;
+      // Per lane: the nearest box distance among its queries that want a
+      // child (+inf when none does).
+      float dLm = INFINITY, dRm = INFINITY;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (act[h] && thr >= 0.0f) {
+          const float mL = box_max_d2<D>(q[h], n0, n2.x, n2.y);
+          const float mR = box_max_d2<D>(q[h], n1, n2.z, n2.w);
+          if (fminf(mL, mR) * kMaxDistMargin <= thr) act[h] = false;
+        }
+        const float dL = box_min_d2<D>(q[h], n0, n2.x, n2.y);
+        const float dR = box_min_d2<D>(q[h], n1, n2.z, n2.w);
+        if (act[h] && dL < cmin[h]) dLm = fminf(dLm, dL);
+        if (act[h] && dR < cmin[h]) dRm = fminf(dRm, dR);
       }
-      const bool wL = active && dL < cmin;
-      const bool wR = active && dR < cmin;
+      const bool wL = dLm < INFINITY, wR = dRm < INFINITY;
       const uint32_t bL = __ballot_sync(0xFFFFFFFFu, wL);
       const uint32_t bR = __ballot_sync(0xFFFFFFFFu, wR);
       const uint32_t left = __float_as_uint(n3.x), right = __float_as_uint(n3.y);
       if (bL && bR) {
-        const int preferL = __popc(__ballot_sync(0xFFFFFFFFu, wL && (!wR || dL <= dR)));
-        const int preferR = __popc(__ballot_sync(0xFFFFFFFFu, wR && (!wL || dR < dL)));
+        const int preferL = __popc(__ballot_sync(0xFFFFFFFFu, wL && (!wR || dLm <= dRm)));
+        const int preferR = __popc(__ballot_sync(0xFFFFFFFFu, wR && (!wL || dRm < dLm)));
         const bool nearL = preferL >= preferR;
         if (sp < kStack) {
           if (lane == 0) stk[warp][sp] = nearL ? right : left;
-          dstk[sp] = nearL ? (wR ? dR : INFINITY) : (wL ? dL : INFINITY);
+          dstk[sp] = nearL ? dRm : dLm;
           ++sp;
         } else if (lane == 0) {
           // Cannot happen: the tree is at most 64 levels deep (distinct
@@ -400,27 +418,35 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
       have = false;
       continue;
     }
-    // Pop the next subtree any lane still needs.
+    // Pop the next subtree any query still needs.  The stacked distance is
+    // the nearest of the lane's wanting queries, so a query with a larger
+    // minimum may revisit a subtree it does not need (never the converse).
     if (sp == 0) break;
     --sp;
     next = stk[warp][sp];
-    const bool want = active && dstk[sp] < cmin;
+    const bool want = (act[0] && dstk[sp] < cmin[0]) || (act[1] && dstk[sp] < cmin[1]);
     have = __any_sync(0xFFFFFFFFu, want);
   }
   if (cand) {
     // Frozen-threshold pass (FP64 refinement): the running maximum is never
     // raised; the rows still open are listed with their FP32 minima.
-    const unsigned open = __ballot_sync(0xFFFFFFFFu, active);
-    if (open) {
+    const unsigned o0 = __ballot_sync(0xFFFFFFFFu, act[0]);
+    const unsigned o1 = __ballot_sync(0xFFFFFFFFu, act[1]);
+    if (o0 | o1) {
       uint32_t base = 0;
-      if (lane == 0) base = atomicAdd(cand_count, (uint32_t) __popc(open));
+      if (lane == 0) base = atomicAdd(cand_count, (uint32_t) (__popc(o0) + __popc(o1)));
       base = __shfl_sync(0xFFFFFFFFu, base, 0);
-      const uint32_t slot = base + __popc(open & ((1u << lane) - 1u));
-      if (active && slot < cand_cap)
-        cand[slot] = RowEntry{__float_as_uint(q.w), __float_as_uint(cmin)};
+      const uint32_t slot[2] = {base + __popc(o0 & below),
+                                base + __popc(o0) + __popc(o1 & below)};
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+        if (act[h] && slot[h] < cand_cap)
+          cand[slot[h]] = RowEntry{__float_as_uint(q[h].w), __float_as_uint(cmin[h])};
     }
-  } else if (active) {
-    atomicMax(&sc->max_key, pack_max(cmin, __float_as_uint(q.w)));
+  } else {
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+      if (act[h]) atomicMax(&sc->max_key, pack_max(cmin[h], __float_as_uint(q[h].w)));
   }
   if (COUNT && lane == 0) {
     atomicAdd(&sc->pairs, pairs);
@@ -441,8 +467,8 @@ __device__ __forceinline__ void packet_pos_body(const float4* __restrict__ Q,
                                                 uint32_t* __restrict__ pos) {
   const uint64_t t = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
   const uint64_t p = t >> 1;
-  if (p * 32 >= nQ) return;
-  const uint64_t q = (t & 1) ? min(p * 32 + 31, nQ - 1) : p * 32;
+  if (p * kPacket >= nQ) return;
+  const uint64_t q = (t & 1) ? min(p * kPacket + kPacket - 1, nQ - 1) : p * kPacket;
   uint32_t target;
   if (qcodes) {
     target = qcodes[q] & kSortedMask;
@@ -719,7 +745,7 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count, F64Plan* 
   QuerySets qs;
   uint64_t packets[2], maxppos = 0;
   for (int k = 0; k < count; ++k) {
-    packets[k] = (q[k]->n + 31) / 32;
+    packets[k] = (q[k]->n + kPacket - 1) / kPacket;
     maxppos += 2 * packets[k];
   }
   void* ppos;
