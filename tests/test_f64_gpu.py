@@ -172,3 +172,41 @@ def test_f64_reference_mirror_class(built_lib):
     assert isinstance(got, np.float64)
     assert got == math.sqrt(hd_oracle.exact_f64(a, b, n_threads=CORES)[0])
     assert {"Algorithm", "Execution", "ReportedTime"} <= set(h.get_stats())
+
+
+EDGE = {
+    "single_points": lambda rng: (np.array([[0.25, -1.5, 3.0]]), np.array([[1.0, 2.0, -0.5]])),
+    "one_vs_many": lambda rng: (np.array([[0.5, 0.5, 0.5]]), rng.random((5000, 3))),
+    "many_vs_one": lambda rng: (rng.random((5000, 3)), np.array([[0.5, 0.5, 0.5]])),
+    "all_identical": lambda rng: (np.full((3000, 3), 0.3), np.full((2000, 3), 0.3)),
+    "duplicates_with_ties": lambda rng: (np.repeat(rng.random((50, 2)), 40, axis=0),
+                                         np.repeat(rng.random((60, 2)), 30, axis=0)),
+    # Float rounding (ulp 0.0625 at 1e6) swamps the distances: every row is
+    # listed and settled in FP64.
+    "large_offset": lambda rng: (1e6 + clusters(100_000, 3, seed=41, sigma=0.001),
+                                 1e6 + clusters(80_000, 3, seed=42, sigma=0.001) + 0.0005),
+    "negative_coords": lambda rng: (-5.0 + clusters(60_000, 2, seed=43),
+                                    -5.0 + clusters(50_000, 2, seed=44) - 0.002),
+    # A exactly float-valued, B genuinely double.
+    "mixed_precision": lambda rng: (clusters(70_000, 3, seed=45).astype(np.float32).astype(np.float64),
+                                    clusters(60_000, 3, seed=46) + 1e-9),
+}
+
+
+@pytest.mark.parametrize("case", sorted(EDGE))
+def test_f64_edge_cases(engine, case):
+    rng = np.random.default_rng(7)
+    a, b = EDGE[case](rng)
+    for undirected in (False, True):
+        r = engine.solve_f64(a, b, undirected=undirected, count_pairs=True, timing=True)
+        check(r, oracle(a, b, undirected))
+        assert r.ms > 0
+
+
+def test_f64_repeated_calls_and_sizes(engine):
+    # Buffers grow and shrink across calls; results stay exact.
+    for n, m, seed in [(200_000, 150_000, 51), (3_000, 9_000, 52), (400_000, 20, 53)]:
+        a = clusters(n, 3, seed=seed)
+        b = clusters(m, 3, seed=seed + 100) + 0.001
+        r = engine.solve_f64(a, b, undirected=True)
+        check(r, oracle(a, b, True))
