@@ -39,7 +39,8 @@ struct GridParams {
   uint32_t cpa;    // cells per axis
   uint32_t shift;  // d * g
   uint32_t ncells;
-  uint32_t pad[3];
+  uint32_t mask;   // the target set's sorted code bits
+  uint32_t pad[2];
 };
 
 constexpr uint32_t kMaxCells = 1u << 24;
@@ -62,7 +63,7 @@ __device__ __forceinline__ uint32_t compact3(uint32_t x) {
 }
 
 __global__ void k_grid_params(const Frame* __restrict__ fr, const uint32_t* __restrict__ ordB,
-                              uint64_t nB, int dims, uint32_t k, GridParams* gp) {
+                              uint64_t nB, int dims, uint32_t k, int low_bits, GridParams* gp) {
   if (threadIdx.x != 0) return;
   const int bits = fr->bits;
   // Reference resolution rule on B's own box (zero extents -> 1e-5,
@@ -77,11 +78,14 @@ __global__ void k_grid_params(const Frame* __restrict__ fr, const uint32_t* __re
   int g = (int) floor(log2(fmax(s / fine, 1.0)) + 0.5);
   const int cap_bits = dims == 2 ? 12 : 8;  // cells per axis <= 2^(24/d)
   g = max(g, bits - cap_bits);
+  // A cell must be a run of the sort: its code drops every unsorted bit.
+  g = max(g, (low_bits + dims - 1) / dims);
   g = min(max(g, 0), bits);
   gp->g = (uint32_t) g;
   gp->shift = (uint32_t) (dims * g);
   gp->cpa = 1u << (bits - g);
   gp->ncells = dims == 2 ? gp->cpa * gp->cpa : gp->cpa * gp->cpa * gp->cpa;
+  gp->mask = sorted_mask(low_bits);
   gp->side = (float) ((double) (1u << g) * fine);
   for (int d = 0; d < 3; ++d) gp->lo[d] = fr->lo[d];
   float mag = 0.0f;
@@ -102,12 +106,12 @@ __device__ __forceinline__ uint32_t cell_linear(uint32_t cellcode, int dims, uin
 
 __global__ void k_grid_runs(const uint32_t* __restrict__ codes, uint64_t n, int dims,
                             const GridParams* __restrict__ gp, uint2* __restrict__ table) {
-  const uint32_t shift = gp->shift, cpa = gp->cpa;
+  const uint32_t shift = gp->shift, cpa = gp->cpa, mask = gp->mask;
   for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
        i += (uint64_t) gridDim.x * blockDim.x) {
-    const uint32_t c = (codes[i] & kSortedMask) >> shift;
-    const bool first = i == 0 || ((codes[i - 1] & kSortedMask) >> shift) != c;
-    const bool last = i + 1 == n || ((codes[i + 1] & kSortedMask) >> shift) != c;
+    const uint32_t c = (codes[i] & mask) >> shift;
+    const bool first = i == 0 || ((codes[i - 1] & mask) >> shift) != c;
+    const bool last = i + 1 == n || ((codes[i + 1] & mask) >> shift) != c;
     if (first || last) {
       const uint32_t lin = cell_linear(c, dims, cpa);
       if (first) table[lin].x = (uint32_t) i;
@@ -246,7 +250,8 @@ template <int D>
 __global__ void __launch_bounds__(256)
     k_grid_deferred(const float4* __restrict__ Q, const Frame* __restrict__ tframe,
                     const float4* __restrict__ B, const uint32_t* __restrict__ bcodes, uint64_t nB,
-                    const Deferred* __restrict__ list, const uint32_t* count, DevScalars* sc) {
+                    uint32_t mask, const Deferred* __restrict__ list, const uint32_t* count,
+                    DevScalars* sc) {
   __shared__ float red[8];
   __shared__ float s_thr;
   constexpr uint64_t kChunk = 256 * 64;
@@ -254,13 +259,13 @@ __global__ void __launch_bounds__(256)
   for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
     const Deferred dfr = list[e];
     const float4 q = Q[dfr.qpos];
-    const uint32_t code = frame_code<D>(*tframe, q.x, q.y, q.z) & kSortedMask;
+    const uint32_t code = frame_code<D>(*tframe, q.x, q.y, q.z) & mask;
     // First B position whose code is >= the query's (every thread finds the
     // same one).
     uint64_t lo = 0, hi = nB;
     while (lo < hi) {
       const uint64_t mid = (lo + hi) >> 1;
-      if ((bcodes[mid] & kSortedMask) < code) lo = mid + 1;
+      if ((bcodes[mid] & mask) < code) lo = mid + 1;
       else hi = mid;
     }
     const uint64_t p0 = lo;
@@ -325,7 +330,7 @@ hd_status run_grid(Ctx& c, const DirInput& in) {
   // The set this grid indexes is the call's A for direction 1, B otherwise.
   const uint32_t* ordT = &scalars(c, 0)->mbr_ord[t == &c.sorted[0] ? 0 : 1][0][0];
   const uint32_t k = c.opt.n_points_cell ? c.opt.n_points_cell : 8;
-  k_grid_params<<<1, 32, 0, c.stream>>>(t->frame, ordT, t->n, in.dims, k, gp);
+  k_grid_params<<<1, 32, 0, c.stream>>>(t->frame, ordT, t->n, in.dims, k, t->low_bits, gp);
   if ((s = after_launch(c, "grid_params")) != HD_OK) return s;
   cudaError_t e = cudaMemsetAsync(defer_count, 0, 4, c.stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "memset");
@@ -374,10 +379,12 @@ hd_status run_grid(Ctx& c, const DirInput& in) {
   mark(c, 4);
   if (in.dims == 2)
     k_grid_deferred<2><<<c.num_sms * 2, 256, 0, c.stream>>>(q->pts, t->frame, t->pts, t->codes, t->n,
-                                                           (const Deferred*) defl, defer_count, sc);
+                                                           t->mask, (const Deferred*) defl,
+                                                           defer_count, sc);
   else
     k_grid_deferred<3><<<c.num_sms * 2, 256, 0, c.stream>>>(q->pts, t->frame, t->pts, t->codes, t->n,
-                                                           (const Deferred*) defl, defer_count, sc);
+                                                           t->mask, (const Deferred*) defl,
+                                                           defer_count, sc);
   if ((s = after_launch(c, "grid_deferred")) != HD_OK) return s;
   return certify(c, in);
 }

@@ -13,12 +13,17 @@ namespace hdg {
 // Bits of a sorted key that hold the Morton code (bit 30 marks the set in
 // the fused sort of small sets).
 constexpr uint32_t kCodeMask = (1u << 30) - 1u;
-// Code bits below kSortLowBits are left out of the sort of large sets (one
-// radix pass fewer): the sorted order is exact only above them, so every
-// consumer compares codes through kSortedMask (cells of 2^-8 of the frame per
-// axis in 3-D, 2^-12 in 2-D; grid levels never go finer).
-constexpr int kSortLowBits = 6;
-constexpr uint32_t kSortedMask = kCodeMask & ~((1u << kSortLowBits) - 1u);
+// Code bits below a sorted set's low_bits are left out of its sort (three
+// radix passes of 8 bits): the sorted order is exact only above them, so
+// every consumer compares codes through the set's mask.  Per-set sorts of
+// large sets keep 24 code bits (cells of 2^-8 of the frame per axis in 3-D,
+// 2^-12 in 2-D); the fused sort of small sets keeps 23 code bits and the set
+// bit 30.  Grid levels never go finer than the sorted bits.
+constexpr int kSortLowBitsSplit = 6;
+constexpr int kSortLowBitsFused = 7;
+__host__ __device__ constexpr uint32_t sorted_mask(int low_bits) {
+  return kCodeMask & ~((1u << low_bits) - 1u);
+}
 // From this many points (|A| + |B|) the two sets are sorted as independent
 // chains, each in its own frame (and, for host inputs, A's sort overlaps
 // B's copy); below it one fused chain in a common frame has fewer launches
@@ -154,6 +159,8 @@ struct SortedSet {
   uint64_t n = 0;
   int dims = 0;
   const float* src = nullptr;  // device pointer it was sorted from
+  int low_bits = kSortLowBitsSplit;                // code bits left out of the sort
+  uint32_t mask = sorted_mask(kSortLowBitsSplit);  // the sorted code bits
 };
 
 struct Ctx {

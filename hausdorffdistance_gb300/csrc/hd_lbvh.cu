@@ -63,10 +63,9 @@ struct Deferred {
 // leaf's key is its first point's sorted Morton code with the leaf index
 // appended, which makes every key distinct.
 __device__ __forceinline__ int leaf_delta(const uint32_t* __restrict__ codes, uint32_t L,
-                                          uint32_t i) {
-  const uint64_t ki = ((uint64_t) (codes[(uint64_t) i * L] & kSortedMask) << 32) | (uint64_t) i;
-  const uint64_t kj =
-      ((uint64_t) (codes[(uint64_t) (i + 1) * L] & kSortedMask) << 32) | (uint64_t) (i + 1);
+                                          uint32_t i, uint32_t mask) {
+  const uint64_t ki = ((uint64_t) (codes[(uint64_t) i * L] & mask) << 32) | (uint64_t) i;
+  const uint64_t kj = ((uint64_t) (codes[(uint64_t) (i + 1) * L] & mask) << 32) | (uint64_t) (i + 1);
   return __clzll(ki ^ kj);
 }
 
@@ -96,7 +95,7 @@ __device__ __forceinline__ void agglomerate_body(const uint32_t* __restrict__ co
                                                  uint32_t nL,
                                                  const float4* __restrict__ leaf_boxes,
                                                  uint32_t* flags, uint32_t* bound, uint32_t* root,
-                                                 float4* nodes) {
+                                                 float4* nodes, uint32_t mask) {
   const uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
   if (nL == 1) {
     // Single leaf: a root whose right child is an empty box (never visited).
@@ -114,8 +113,8 @@ __device__ __forceinline__ void agglomerate_body(const uint32_t* __restrict__ co
   float4 lo = leaf_boxes[2 * (uint64_t) leaf], hi = leaf_boxes[2 * (uint64_t) leaf + 1];
   uint32_t l = leaf, r = leaf, me = leaf | kLeafBit;
   for (;;) {
-    const bool left_child = l == 0 || (r != nL - 1 && leaf_delta(codes, L, r) >
-                                                           leaf_delta(codes, L, l - 1));
+    const bool left_child = l == 0 || (r != nL - 1 && leaf_delta(codes, L, r, mask) >
+                                                           leaf_delta(codes, L, l - 1, mask));
     const uint32_t p = left_child ? r : l - 1;
     const int side = left_child ? 0 : 1;
     float4* o = nodes + 4 * (uint64_t) p;
@@ -464,22 +463,22 @@ __device__ __forceinline__ void packet_pos_body(const float4* __restrict__ Q,
                                                 const uint32_t* __restrict__ qcodes, uint64_t nQ,
                                                 const Frame* __restrict__ tframe,
                                                 const uint32_t* __restrict__ bcodes, uint64_t nB,
-                                                uint32_t* __restrict__ pos) {
+                                                uint32_t mask, uint32_t* __restrict__ pos) {
   const uint64_t t = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
   const uint64_t p = t >> 1;
   if (p * kPacket >= nQ) return;
   const uint64_t q = (t & 1) ? min(p * kPacket + kPacket - 1, nQ - 1) : p * kPacket;
   uint32_t target;
   if (qcodes) {
-    target = qcodes[q] & kSortedMask;
+    target = qcodes[q] & mask;
   } else {
     const float4 qp = Q[q];
-    target = frame_code<D>(*tframe, qp.x, qp.y, qp.z) & kSortedMask;
+    target = frame_code<D>(*tframe, qp.x, qp.y, qp.z) & mask;
   }
   uint64_t lo = 0, hi = nB;
   while (lo < hi) {
     const uint64_t mid = (lo + hi) >> 1;
-    if ((bcodes[mid] & kSortedMask) < target)
+    if ((bcodes[mid] & mask) < target)
       lo = mid + 1;
     else
       hi = mid;
@@ -500,6 +499,7 @@ struct BuildSet {
   uint32_t* bound;   // two range bounds per internal node
   uint32_t* root;    // the root's internal node index
   float4* nodes;
+  uint32_t mask;     // the set's sorted code bits
 };
 struct BuildSets {
   BuildSet s[2];
@@ -509,7 +509,7 @@ struct BuildSets {
 // SM) matters more than a few spilled values.
 __global__ void __launch_bounds__(256, 8) k_agglomerate(BuildSets b) {
   const BuildSet& S = b.s[blockIdx.y];
-  agglomerate_body(S.codes, S.L, S.nL, S.leaf_boxes, S.flags, S.bound, S.root, S.nodes);
+  agglomerate_body(S.codes, S.L, S.nL, S.leaf_boxes, S.flags, S.bound, S.root, S.nodes, S.mask);
 }
 
 struct QuerySet {
@@ -530,6 +530,7 @@ struct QuerySet {
   const Frame* tframe;      // frame of the target set's codes
   const uint32_t* qcodes;   // the query set's sorted codes when in that frame, else null
   const uint32_t* bcodes;
+  uint32_t mask;            // the target set's sorted code bits
   // Frozen-threshold pass only (else null): open rows are listed here
   // instead of raising the maximum.
   RowEntry* cand;
@@ -674,7 +675,8 @@ __global__ void __launch_bounds__(kDeferWarps * 32) k_lbvh_defer(QuerySets qs) {
 template <int D>
 __global__ void k_packet_pos(QuerySets qs) {
   const QuerySet& S = qs.d[blockIdx.y];
-  packet_pos_body<D>(S.Q, S.qcodes, S.nQ, S.tframe, S.bcodes, S.nB, const_cast<uint32_t*>(S.ppos));
+  packet_pos_body<D>(S.Q, S.qcodes, S.nQ, S.tframe, S.bcodes, S.nB, S.mask,
+                     const_cast<uint32_t*>(S.ppos));
 }
 
 }  // namespace
@@ -718,6 +720,7 @@ static hd_status build_lbvhs(Ctx& c, const SortedSet* const* sets, int count, Bu
     b.bound = bound_base + 2 * off_int;
     b.root = roots + k;
     b.nodes = (float4*) nodes;
+    b.mask = sets[k]->mask;
     off_int += nI[k];
     maxL = std::max(maxL, nL[k]);
   }
@@ -766,6 +769,7 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count, F64Plan* 
     d.tframe = t[k]->frame;
     d.qcodes = q[k]->frame == t[k]->frame ? q[k]->codes : nullptr;
     d.bcodes = t[k]->codes;
+    d.mask = t[k]->mask;
     d.cand = nullptr;
     d.cand_count = nullptr;
     d.cand_cap = 0;

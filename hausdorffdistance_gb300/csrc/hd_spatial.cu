@@ -314,7 +314,8 @@ hd_status sort_scratch(Ctx& c, uint64_t nA, uint64_t nB, bool fused, SortScratch
   cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, (const uint32_t*) keys, (uint32_t*) keys2,
                                   (const uint32_t*) vals, (uint32_t*) vals2,
                                   (int64_t) (fused ? n : std::max(nA, nB)),
-                                  fused ? 0 : kSortLowBits, fused ? 31 : 30, c.stream);
+                                  fused ? kSortLowBitsFused : kSortLowBitsSplit, fused ? 31 : 30,
+                                  c.stream);
   const size_t stride = (tmp_bytes + 255) & ~(size_t) 255;
   if ((s = ensure(c, kBufCubTemp, (fused ? 1 : 2) * stride, &tmp)) != HD_OK) return s;
   *x = SortScratch{(uint32_t*) keys, (uint32_t*) keys2, (uint32_t*) vals, (uint32_t*) vals2,
@@ -346,7 +347,7 @@ hd_status sort_set(Ctx& c, int k, const float* P, uint64_t n, int dims, const So
   size_t tb = x.tmp_bytes;
   cudaError_t e = cub::DeviceRadixSort::SortPairs(
       x.tmp + (size_t) k * x.tmp_stride, tb, (const uint32_t*) x.keys + base, x.keys2 + base,
-      (const uint32_t*) x.vals + base, x.vals2 + base, (int64_t) n, kSortLowBits, 30, st);
+      (const uint32_t*) x.vals + base, x.vals2 + base, (int64_t) n, kSortLowBitsSplit, 30, st);
   if (e != cudaSuccess) return cuda_fail(c, e, "radix sort");
   float4* lb = x.lboxes + (k ? 2 * x.leaves_a : 0);
   k_gather1<<<grid_for(c, n), 256, 0, st>>>(P, n, dims, x.vals2 + base, x.pts + base, x.L, lb);
@@ -360,6 +361,8 @@ hd_status sort_set(Ctx& c, int k, const float* P, uint64_t n, int dims, const So
   o.n = n;
   o.dims = dims;
   o.src = P;
+  o.low_bits = kSortLowBitsSplit;
+  o.mask = sorted_mask(kSortLowBitsSplit);
   return HD_OK;
 }
 
@@ -391,13 +394,16 @@ static hd_status spatial_sort_fused(Ctx& c, const float* A, uint64_t nA, const f
   size_t tb = x.tmp_bytes;
   cudaError_t e = cub::DeviceRadixSort::SortPairs(x.tmp, tb, (const uint32_t*) x.keys, x.keys2,
                                                   (const uint32_t*) x.vals, x.vals2,
-                                                  (int64_t) (nA + nB), 0, 31, c.stream);
+                                                  (int64_t) (nA + nB), kSortLowBitsFused, 31,
+                                                  c.stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "radix sort");
   k_gather2<<<dim3(grid_for(c, std::max(nA, nB)), 2), 256, 0, c.stream>>>(
       A, nA, B, nB, dims, x.vals2, x.pts, x.L, x.lboxes, x.leaves_a);
   if ((s = after_launch(c, "gather")) != HD_OK) return s;
-  *sa = SortedSet{x.pts, x.keys2, fr, x.lboxes, x.L, nA, dims, A};
-  *sb = SortedSet{x.pts + nA, x.keys2 + nA, fr, x.lboxes + 2 * x.leaves_a, x.L, nB, dims, B};
+  const uint32_t mask = sorted_mask(kSortLowBitsFused);
+  *sa = SortedSet{x.pts, x.keys2, fr, x.lboxes, x.L, nA, dims, A, kSortLowBitsFused, mask};
+  *sb = SortedSet{x.pts + nA, x.keys2 + nA, fr, x.lboxes + 2 * x.leaves_a, x.L, nB, dims, B,
+                  kSortLowBitsFused, mask};
   return HD_OK;
 }
 
