@@ -703,9 +703,9 @@ def bench_f64(eng, name, n, steps, warmup, args, ctx):
         "instrumented_ms": float(ri.ms),
         "e2e": {"value": 1.0 / t_e2e, "unit": "solves/s",
                 "h2d_bytes_per_step": int(a.nbytes + b.nbytes),
-                # three read-backs of the FP64 scalars (456 B) and one of the
+                # three read-backs of the FP64 scalars (152 B) and one of the
                 # FP32 stage's two DevScalars (152 B each)
-                "d2h_bytes_per_step": 3 * 456 + 2 * 152, "ms_per_step": t_e2e * 1e3},
+                "d2h_bytes_per_step": 3 * 152 + 2 * 152, "ms_per_step": t_e2e * 1e3},
         "cpu_baseline": None,
         "cpu_baseline_note": "not measured: the reference has no double build of its CPU "
                              "path (its -is_double dispatch is disabled)",

@@ -14,15 +14,20 @@
 //     moves by at most rX = sqrt(D)·dX, and the exact distances of a cut pair
 //     and of the original pair differ by at most r = rX + rY.
 //  2. The FP32 LBVH solve of the cut sets certifies a row i* and its FP32
-//     nearest squared distance.
+//     nearest squared distance M (the FP32 max-min of the cut sets).
 //  3. Seed: the exact FP64 nearest neighbour of x_{i*} (the walk below)
 //     gives L = min_j d64(x_{i*}, y_j)^2 <= h64^2.
 //  4. A float threshold T is derived from L so that every cut pair with FP32
-//     squared distance <= T has FP64 squared distance < L.  A second query
-//     pass over the same trees, with the running maximum frozen at T, stops
-//     each row that has such a pair and lists the others with their FP32
-//     minima; every row whose FP64 nearest distance is >= L is listed.
-//  5. Each listed row's FP64 nearest neighbour is found by a walk of the
+//     squared distance <= T has FP64 squared distance < L: rows with an FP32
+//     minimum <= T are settled.  The query pass of step 2 cannot know T, but
+//     T >= G(M) >= G(running maximum) for a G that needs M alone (every cut
+//     pair of x_{i*} is at FP32 squared distance >= M, which bounds L from
+//     below; hd_lbvh.cu's soft_stop computes G rounding toward zero:
+//     sqrt(G + a) = sqrt(thr - a)(1 - 1e-5) - 2.01 r, a the absolute term).
+//     So that pass stops a row only at or below G(running maximum) and lists
+//     every row that stays open with its FP32 minimum; each row with an FP32
+//     minimum > T is listed.
+//  5. Each listed row with an FP32 minimum > T FP64 nearest neighbour is found by a walk of the
 //     same tree, one warp per row: boxes and points are tested in FP32
 //     against a float threshold P derived from the row's best FP64 distance
 //     (anything above P is provably farther in FP64), and only points within
@@ -74,15 +79,16 @@ struct F64Dir {
   unsigned long long pick;   // (row << 32) | column of the answer (atomicMin)
   double seed_d2;            // the seed row's FP64 nearest squared distance
   uint32_t seed_row, seed_col;
-  uint32_t cand_count;       // rows listed by the frozen pass (may exceed the cap)
-  float thr;                 // frozen threshold (-1: none)
+  uint32_t cand_count;       // rows listed by the query pass (may exceed the cap)
+  float thr;                 // T: listed rows at or below it are settled (-1: none)
+  uint32_t status;           // kErr* of the FP64 kernels
+  uint32_t walked;           // rows whose nearest neighbour was searched in FP64
 };
 
 // Device layout of kBufF64Aux; the two candidate lists follow it.
 struct F64Aux {
   RoundStats round[2];  // per set: 0 = A, 1 = B
   F64Dir dir[2];
-  DevScalars frozen[2];
   RowEntry seed[2];
   double seed_min[2];
   uint32_t seed_col[2];
@@ -216,6 +222,8 @@ __global__ void k_f64_init(F64Aux* aux) {
     z.seed_row = z.seed_col = 0u;
     z.cand_count = 0u;
     z.thr = -1.0f;
+    z.status = 0u;
+    z.walked = 0u;
     aux->dir[k] = z;
     aux->round[k].emax = 0u;
     aux->round[k].flags = 0u;
@@ -281,7 +289,18 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_f64_walk(WalkSets ws) {
   if (w.list) {
     const RowEntry e = w.list[k];
     row = e.row;
+    // Listed rows at or below T are settled below the seed (the seed walk
+    // itself runs before T exists: thr is -1 then).
+    const float T = w.f->thr;
+    if (T >= 0.0f && __uint_as_float(e.min32) <= T) {
+      if (lane == 0) {
+        w.row_min[k] = -1.0;
+        w.row_col[k] = 0u;
+      }
+      return;
+    }
     best = upper_from32<D>(__uint_as_float(e.min32), w.rxy);
+    if (lane == 0) atomicAdd(&w.f->walked, 1u);
   } else {
     row = (uint32_t) k;
   }
@@ -426,17 +445,14 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_f64_walk(WalkSets ws) {
   atomicMax(&w.f->max64, dbits(best));
 }
 
-// Frozen thresholds from the seeds (thread per direction).
+// T from the seeds (thread per direction).
 __global__ void k_f64_prepare(F64Aux* aux, int count, int D, double rxy0, double rxy1) {
   const int k = threadIdx.x;
   if (k >= count) return;
   const double rxy = k == 0 ? rxy0 : rxy1;
   F64Dir& f = aux->dir[k];
   const double L = aux->seed_min[k];
-  DevScalars z;
-  memset(&z, 0, sizeof(z));
-  z.min_key = ~0ull;
-  if (L < 0.0) z.status = kErrInternal;  // a seed walk cannot stop
+  if (L < 0.0) f.status |= kErrInternal;  // a seed walk cannot stop
   f.seed_d2 = L;
   f.seed_row = aux->seed[k].row;
   f.seed_col = aux->seed_col[k];
@@ -450,8 +466,6 @@ __global__ void k_f64_prepare(F64Aux* aux, int count, int D, double rxy0, double
     }
   }
   f.thr = T;
-  z.max_key = T >= 0.0f ? pack_max(T, 0u) : 0ull;
-  aux->frozen[k] = z;
 }
 
 // FP64 scan: thread per row of X, every warp visiting Y from its own start
@@ -596,7 +610,7 @@ hd_status status_of(Ctx& c, uint32_t st) {
 
 }  // namespace
 
-// Seed walks and frozen thresholds (called by the LBVH solve once the FP32
+// Seed walks and T (called by the LBVH solve once the FP32
 // directions are certified).
 hd_status f64_seed(Ctx& c, F64Plan& plan, int count) {
   F64Call& call = *reinterpret_cast<F64Call*>(plan.state);
@@ -615,9 +629,7 @@ hd_status f64_seed(Ctx& c, F64Plan& plan, int count) {
     w.f = &call.aux->dir[k];
     w.row_min = call.seed_min + k;
     w.row_col = call.seed_col + k;
-    // k_f64_prepare rewrites the frozen scalars after this walk: its errors
-    // go to the direction's own scalars.
-    w.status = &scalars(c, k)->status;
+    w.status = &call.aux->dir[k].status;
   }
   if (count == 1) ws.d[1] = ws.d[0];
   if ((s = launch_walks(c, ws, count, 1, call.dims)) != HD_OK) return s;
@@ -747,9 +759,12 @@ hd_status hd_solve_f64(hd_ctx* c, const double* A, uint64_t n_a, const double* B
     plan.cand_cap = kListCap;
     plan.state = &call;
     for (int k = 0; k < ndir; ++k) {
-      plan.frozen[k] = &aux->frozen[k];
       plan.cand[k] = lists + (size_t) k * kListCap;
       plan.cand_count[k] = &aux->dir[k].cand_count;
+      // The bound as a float, rounded up.
+      float rf = (float) call.rxy[k];
+      if ((double) rf < call.rxy[k]) rf = std::nextafter(rf, INFINITY);
+      plan.soft_r[k] = rf;
     }
     if ((s = run_lbvh_f64(*c, ins, ndir, &plan)) != HD_OK) return s;
     if ((s = read_aux()) != HD_OK) return s;
@@ -757,7 +772,7 @@ hd_status hd_solve_f64(hd_ctx* c, const double* A, uint64_t n_a, const double* B
     cudaError_t e = cudaMemcpy(hs, scalars(*c, 0), sizeof(hs), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(*c, e, "f64 read-back");
     for (int k = 0; k < ndir; ++k) {
-      if ((s = status_of(*c, hs[k].status | h->frozen[k].status)) != HD_OK) return s;
+      if ((s = status_of(*c, hs[k].status | h->dir[k].status)) != HD_OK) return s;
       out->visited_pairs += hs[k].pairs;
       out->visited_nodes += hs[k].nodes;
       out->visited_leaves += hs[k].leaves;
@@ -787,7 +802,7 @@ hd_status hd_solve_f64(hd_ctx* c, const double* A, uint64_t n_a, const double* B
       w.f = &aux->dir[k];
       w.row_min = row_min + off[k];
       w.row_col = row_col + off[k];
-      w.status = &aux->frozen[k].status;
+      w.status = &aux->dir[k].status;
     }
     if (ndir == 1) ws.d[1] = ws.d[0];
     if ((s = launch_walks(*c, ws, ndir, std::max(walked[0], walked[1]), n_dims)) != HD_OK)
@@ -826,7 +841,7 @@ hd_status hd_solve_f64(hd_ctx* c, const double* A, uint64_t n_a, const double* B
   if ((s = read_aux()) != HD_OK) return s;
   if (lbvh)
     for (int k = 0; k < ndir; ++k)
-      if ((s = status_of(*c, h->frozen[k].status)) != HD_OK) return s;
+      if ((s = status_of(*c, h->dir[k].status)) != HD_OK) return s;
   double v[2] = {-1.0, -1.0};
   for (int k = 0; k < ndir; ++k) {
     std::memcpy(&v[k], &h->dir[k].max64, sizeof(double));
@@ -845,6 +860,11 @@ hd_status hd_solve_f64(hd_ctx* c, const double* A, uint64_t n_a, const double* B
   out->ib = h->dir[win].pick & 0xFFFFFFFFull;
   out->variant_used = used;
   out->variant_used_ba = undirected ? used : -1;
+  if (lbvh)
+    // Rows searched in FP64: the seed, the listed rows above T, or every row
+    // when a list overflowed.
+    for (int k = 0; k < ndir; ++k)
+      walked[k] = h->dir[k].walked + (h->dir[k].cand_count > kListCap ? nn[k] : 0);
   out->rechecked = walked[0] + walked[1];
   if (c->timing) {
     float t = 0;

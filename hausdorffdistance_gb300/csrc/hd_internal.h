@@ -299,18 +299,18 @@ struct LbvhTree {
   uint64_t n;
   uint32_t leaf;
 };
-// run_lbvh_f64 solves the rounded sets in FP32, records each direction's
-// tree, calls f64_seed (which leaves frozen[k]->max_key at direction k's
-// frozen threshold), then re-runs the query pass with those scalars: rows
-// that stay open are listed in cand[k] (count in *cand_count[k], at most
-// cand_cap stored).
+// run_lbvh_f64 solves the cut sets in FP32 with a listing query pass (a row
+// stops only once its minimum is at or below soft_stop(running maximum,
+// soft_r[k]); rows that stay open are listed in cand[k] with their FP32
+// minima, count in *cand_count[k], at most cand_cap stored), records each
+// direction's tree and calls f64_seed after certification.
 struct F64Plan {
   LbvhTree tree[2];
-  DevScalars* frozen[2];
   RowEntry* cand[2];
   uint32_t* cand_count[2];
   uint32_t cand_cap;
-  void* state;  // the FP64 solve's own data (hd_f64.cu)
+  float soft_r[2];  // bound on |d(x, y) - d(cut x, cut y)|, rounded up
+  void* state;      // the FP64 solve's own data (hd_f64.cu)
 };
 hd_status run_lbvh_f64(Ctx& c, const DirInput* ins, int count, F64Plan* plan);
 hd_status f64_seed(Ctx& c, F64Plan& plan, int count);

@@ -180,6 +180,22 @@ __device__ __forceinline__ float box_max_d2(const float4& q, const float4& xy, f
 // box bound and the FP32 pair formula each carry a few ulps of rounding.
 constexpr float kMaxDistMargin = 1.0f + 1.0f / 65536.0f;
 
+// The FP64 input path's listing pass stops a row only below soft_stop(thr):
+// a lower bound, from the running maximum thr alone, of the threshold under
+// which an FP32 distance proves an FP64 distance below the final answer's
+// seed (the bound is derived in hd_f64.cu; every step here rounds toward
+// zero, r = how far a cut pair's distance can move).  -1: no row stops.
+__device__ __forceinline__ float soft_stop(float thr, float r) {
+  if (!(thr >= 0.0f)) return -1.0f;
+  const float abs32 = 5.0f * 0x1p-126f;  // (n_dims + 2) 2^-126, n_dims <= 3
+  const float base = __fsub_rd(thr, abs32);
+  if (!(base > 0.0f)) return -1.0f;
+  const float sg = __fsub_rd(__fmul_rd(__fsqrt_rd(base), 0.99999f), __fmul_ru(2.01f, r));
+  if (!(sg > 0.0f)) return -1.0f;
+  const float g = __fsub_rd(__fmul_rd(__fmul_rd(sg, sg), 0.999999f), abs32);
+  return g > 0.0f ? g : -1.0f;
+}
+
 // Division of a 32-bit value by a run-time constant d, with the multiplier
 // m and shifts s1, s2 prepared on the host (Granlund and Montgomery,
 // "Division by Invariant Integers using Multiplication", PLDI 1994):
@@ -213,7 +229,7 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
                  const float4* __restrict__ nodes, const float4* __restrict__ B, uint64_t nB,
                  uint32_t L, DevScalars* sc, Deferred* __restrict__ defer, uint32_t budget,
                  uint32_t root, RowEntry* __restrict__ cand, uint32_t* cand_count,
-                 uint32_t cand_cap) {
+                 uint32_t cand_cap, float soft_r) {
   __shared__ uint32_t stk[kQueryWarps][kStack];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
@@ -247,6 +263,9 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   unsigned long long key = 0;
   if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
   float thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
+  // A query stops once its minimum is at or below `stop`: the running
+  // maximum, or in the listing pass its soft bound.
+  float stop = cand ? soft_stop(thr, soft_r) : thr;
   unsigned long long pairs = 0, visits = 0, leafv = 0;
   uint32_t work = 0;  // nodes and leaves this packet has visited
   bool may_defer = defer != nullptr;
@@ -279,7 +298,7 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
           m1 = fminf(m1, d2_pt_packed<D>(q[1], b));
         }
         k = k0 + 4;
-        if (!__any_sync(0xFFFFFFFFu, (act[0] && m0 > thr) || (act[1] && m1 > thr))) {
+        if (!__any_sync(0xFFFFFFFFu, (act[0] && m0 > stop) || (act[1] && m1 > stop))) {
           settled = true;
           break;
         }
@@ -294,7 +313,7 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
           m0 = fminf(m0, d2_pt_packed<D>(q[0], b));
           m1 = fminf(m1, d2_pt_packed<D>(q[1], b));
         }
-        if (!__any_sync(0xFFFFFFFFu, (act[0] && m0 > thr) || (act[1] && m1 > thr))) {
+        if (!__any_sync(0xFFFFFFFFu, (act[0] && m0 > stop) || (act[1] && m1 > stop))) {
           k += 4;
           settled = true;
           break;
@@ -313,10 +332,11 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
     if (!settled) {
       if (lane == 0) key = ld_relaxed_u64(&sc->max_key);
       thr = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
+      stop = cand ? soft_stop(thr, soft_r) : thr;
     }
 #pragma unroll
     for (int h = 0; h < 2; ++h)
-      if (act[h] && cmin[h] <= thr) act[h] = false;
+      if (act[h] && cmin[h] <= stop) act[h] = false;
   };
 
   {
@@ -374,10 +394,10 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
       float dLm = INFINITY, dRm = INFINITY;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        if (act[h] && thr >= 0.0f) {
+        if (act[h] && stop >= 0.0f) {
           const float mL = box_max_d2<D>(q[h], n0, n2.x, n2.y);
           const float mR = box_max_d2<D>(q[h], n1, n2.z, n2.w);
-          if (fminf(mL, mR) * kMaxDistMargin <= thr) act[h] = false;
+          if (fminf(mL, mR) * kMaxDistMargin <= stop) act[h] = false;
         }
         const float dL = box_min_d2<D>(q[h], n0, n2.x, n2.y);
         const float dR = box_min_d2<D>(q[h], n1, n2.z, n2.w);
@@ -427,8 +447,8 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
     have = __any_sync(0xFFFFFFFFu, want);
   }
   if (cand) {
-    // Frozen-threshold pass (FP64 refinement): the running maximum is never
-    // raised; the rows still open are listed with their FP32 minima.
+    // Listing pass (FP64 refinement): the rows still open are listed with
+    // their FP32 minima (and raise the maximum like any other).
     const unsigned o0 = __ballot_sync(0xFFFFFFFFu, act[0]);
     const unsigned o1 = __ballot_sync(0xFFFFFFFFu, act[1]);
     if (o0 | o1) {
@@ -442,11 +462,10 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
         if (act[h] && slot[h] < cand_cap)
           cand[slot[h]] = RowEntry{__float_as_uint(q[h].w), __float_as_uint(cmin[h])};
     }
-  } else {
-#pragma unroll
-    for (int h = 0; h < 2; ++h)
-      if (act[h]) atomicMax(&sc->max_key, pack_max(cmin[h], __float_as_uint(q[h].w)));
   }
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
+    if (act[h]) atomicMax(&sc->max_key, pack_max(cmin[h], __float_as_uint(q[h].w)));
   if (COUNT && lane == 0) {
     atomicAdd(&sc->pairs, pairs);
     atomicAdd(&sc->nodes, visits);
@@ -531,11 +550,13 @@ struct QuerySet {
   const uint32_t* qcodes;   // the query set's sorted codes when in that frame, else null
   const uint32_t* bcodes;
   uint32_t mask;            // the target set's sorted code bits
-  // Frozen-threshold pass only (else null): open rows are listed here
-  // instead of raising the maximum.
+  // Listing pass of the FP64 input path only (else null): rows that stay
+  // open are also listed here, and rows stop only below soft_stop(thr,
+  // soft_r).
   RowEntry* cand;
   uint32_t* cand_count;
   uint32_t cand_cap;
+  float soft_r;
 };
 struct QuerySets {
   QuerySet d[2];
@@ -546,7 +567,7 @@ __global__ void __launch_bounds__(kQueryWarps * 32) k_lbvh_query(QuerySets qs) {
   const QuerySet& S = qs.d[blockIdx.y];
   lbvh_query_body<D, COUNT, LT>(S.Q, S.nQ, S.pstride, S.rows, S.rows_div, S.ppos, S.nodes, S.B,
                                 S.nB, S.L, S.sc, S.defer, S.budget, *S.root, S.cand,
-                                S.cand_count, S.cand_cap);
+                                S.cand_count, S.cand_cap, S.soft_r);
 }
 
 // Deferred pass: one warp per queued query walks the tree with 32 stack
@@ -570,10 +591,14 @@ __global__ void __launch_bounds__(kDeferWarps * 32) k_lbvh_defer(QuerySets qs) {
   unsigned long long pairs = 0, visits = 0, leafv = 0;
   // The running maximum is read by lane 0 and broadcast: the walk below must
   // see one value per warp.
+  // The stop level of the pass (the running maximum, or in the listing pass
+  // its soft bound), read by lane 0 and broadcast: the walk below must see
+  // one value per warp.
   auto read_thr = [&]() {
     unsigned long long key = 0;
     if (lane == 0) key = ld_relaxed_u64(&S.sc->max_key);
-    return threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
+    const float t = threshold_of(__shfl_sync(0xFFFFFFFFu, key, 0));
+    return S.cand ? soft_stop(t, S.soft_r) : t;
   };
   for (uint32_t e = blockIdx.x * kDeferWarps + warp; e < cnt; e += nw) {
     const Deferred de = S.defer[e];
@@ -647,13 +672,13 @@ __global__ void __launch_bounds__(kDeferWarps * 32) k_lbvh_defer(QuerySets qs) {
       __syncwarp();
       if ((++round & 15) == 0) thr = read_thr();
     }
-    if (lane == 0 && m > threshold_of(ld_relaxed_u64(&S.sc->max_key))) {
+    thr = read_thr();
+    if (lane == 0 && m > thr) {
       if (S.cand) {
         const uint32_t slot = atomicAdd(S.cand_count, 1u);
         if (slot < S.cand_cap) S.cand[slot] = RowEntry{__float_as_uint(q.w), __float_as_uint(m)};
-      } else {
-        atomicMax(&S.sc->max_key, pack_max(m, __float_as_uint(q.w)));
       }
+      atomicMax(&S.sc->max_key, pack_max(m, __float_as_uint(q.w)));
     }
     __syncwarp();
   }
@@ -733,10 +758,9 @@ static hd_status build_lbvhs(Ctx& c, const SortedSet* const* sets, int count, Bu
 }
 
 // Directed LBVH solves of `count` directions (1, or 2 for an undirected solve)
-// with shared launches.  With a plan (the FP64 input path), the certified
-// FP32 solve is followed by f64_seed and a second query pass over the same
-// trees with the plan's frozen thresholds, which lists the rows that stay
-// open.
+// with shared launches.  With a plan (the FP64 input path), the query pass
+// is the listing pass (rows stop only below the soft bound and the open ones
+// are listed), and the certified FP32 solve is followed by f64_seed.
 static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count, F64Plan* plan) {
   const int dims = ins[0].dims;
   if (dims != 2 && dims != 3) return fail(c, HD_ERR_UNSUPPORTED, "LBVH needs n_dims 2 or 3");
@@ -770,9 +794,10 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count, F64Plan* 
     d.qcodes = q[k]->frame == t[k]->frame ? q[k]->codes : nullptr;
     d.bcodes = t[k]->codes;
     d.mask = t[k]->mask;
-    d.cand = nullptr;
-    d.cand_count = nullptr;
-    d.cand_cap = 0;
+    d.cand = plan ? plan->cand[k] : nullptr;
+    d.cand_count = plan ? plan->cand_count[k] : nullptr;
+    d.cand_cap = plan ? plan->cand_cap : 0u;
+    d.soft_r = plan ? plan->soft_r[k] : 0.0f;
     off += 2 * packets[k];
     max_pos_threads = std::max<uint64_t>(max_pos_threads, 2 * packets[k]);
   }
@@ -848,15 +873,6 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count, F64Plan* 
     for (int k = 0; k < count; ++k)
       plan->tree[k] = LbvhTree{bs.s[k].nodes, bs.s[k].root, t[k]->pts, t[k]->n, bs.s[k].L};
     if ((s = f64_seed(c, *plan, count)) != HD_OK) return s;
-    for (int k = 0; k < count; ++k) {
-      QuerySet& d = qs.d[k];
-      d.sc = plan->frozen[k];
-      d.cand = plan->cand[k];
-      d.cand_count = plan->cand_count[k];
-      d.cand_cap = plan->cand_cap;
-    }
-    if (count == 1) qs.d[1] = qs.d[0];
-    if ((s = launch_queries(false)) != HD_OK) return s;
   }
   return HD_OK;
 }

@@ -103,7 +103,7 @@ def test_f64_lattice_translate_all_rows_tie(engine):
     r = engine.solve_f64(a, b)
     want = oracle(a, b, False)
     check(r, want)
-    assert r.rechecked == a.shape[0]
+    assert r.rechecked >= a.shape[0]
 
 
 @pytest.mark.parametrize("variant", ["eb", "brute"])
