@@ -44,7 +44,10 @@ namespace {
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr int kQueryWarps = 4;
 constexpr int kStack = 64;
-constexpr uint32_t kPacket = 64;  // queries per warp packet (two per lane)
+// Queries per lane of a warp packet (QPL): two for large query sets, where
+// every broadcast load then serves 64 queries; one for small sets, whose
+// packets would otherwise be too few to fill the GPU.
+constexpr uint64_t kQplTwoMinQueries = 4000000;
 // A packet that has visited `budget` nodes and leaves (an option, tuned)
 // queues its open queries for the deferred pass instead of finishing them
 // alone: a query whose nearest neighbour is far (an outlier) must prove that
@@ -220,10 +223,10 @@ __device__ __forceinline__ uint32_t fastdiv(uint32_t n, FastDiv f) {
   return (t + ((n - t) >> f.s1)) >> f.s2;
 }
 
-// Warp-packet traversal of kPacket consecutive Morton-sorted queries.
+// Warp-packet traversal of 32 * QPL consecutive Morton-sorted queries.
 // LT: leaf size known at compile time (16, the tuned size), or 0 for a
 // runtime leaf size L.
-template <int D, bool COUNT, int LT>
+template <int D, bool COUNT, int LT, int QPL>
 __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, uint64_t nItems, uint32_t pstride,
                  uint64_t rows, FastDiv rows_div, const uint32_t* __restrict__ ppos,
                  const float4* __restrict__ nodes, const float4* __restrict__ B, uint64_t nB,
@@ -233,8 +236,8 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   __shared__ uint32_t stk[kQueryWarps][kStack];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
-  // Packets (kPacket = 64 consecutive Morton-sorted queries, two per lane:
-  // items lane and 32 + lane) are visited in a transposed order: warp w
+  // Packets (kP = 32 * QPL consecutive Morton-sorted queries, QPL per lane:
+  // items lane, 32 + lane, ...) are visited in a transposed order: warp w
   // takes packet (w mod rows) * pstride + w / rows.  The first `rows` warps
   // — the first wave — are every pstride-th packet, spread over the whole
   // Morton range, so the running maximum rises to nearly its final value
@@ -242,19 +245,20 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   // with EB for the same purpose, hybrid.h:128-168).  Two queries per lane
   // let every broadcast load of a leaf point or a node serve 64 queries and
   // halve the chains of dependent loads per query.
-  // 32-bit arithmetic: packet counts stay below 2^26 (point sets < 2^32).
+  // 32-bit arithmetic: packet counts stay below 2^27 (point sets < 2^32).
+  constexpr uint64_t kP = 32 * QPL;
   const uint32_t w = blockIdx.x * kQueryWarps + warp;
   const uint32_t r32 = (uint32_t) rows;
   const uint32_t wq = fastdiv(w, rows_div);
   const uint64_t packet = (uint64_t) (w - wq * r32) * pstride + wq;
-  if (packet * kPacket >= nItems) return;
-  uint64_t item[2];
-  bool act[2];
-  float4 q[2];
-  float cmin[2];
+  if (packet * kP >= nItems) return;
+  uint64_t item[QPL];
+  bool act[QPL];
+  float4 q[QPL];
+  float cmin[QPL];
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    item[h] = packet * kPacket + 32 * h + lane;
+  for (int h = 0; h < QPL; ++h) {
+    item[h] = packet * kP + 32 * h + lane;
     act[h] = item[h] < nItems;
     q[h] = act[h] ? Q[item[h]] : make_float4(0.f, 0.f, 0.f, 0.f);
     cmin[h] = INFINITY;
@@ -269,10 +273,41 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
   unsigned long long pairs = 0, visits = 0, leafv = 0;
   uint32_t work = 0;  // nodes and leaves this packet has visited
   bool may_defer = defer != nullptr;
-  auto open = [&]() { return act[0] || act[1]; };
+  auto open = [&]() {
+    bool o = false;
+#pragma unroll
+    for (int h = 0; h < QPL; ++h) o = o || act[h];
+    return o;
+  };
   auto count_pairs = [&](uint64_t k) {
-    pairs += k * (uint64_t) (__popc(__ballot_sync(0xFFFFFFFFu, act[0])) +
-                             __popc(__ballot_sync(0xFFFFFFFFu, act[1])));
+#pragma unroll
+    for (int h = 0; h < QPL; ++h) pairs += k * (uint64_t) __popc(__ballot_sync(0xFFFFFFFFu, act[h]));
+  };
+  // Some open query of this lane is above the stop level.
+  auto needs = [&](const float* m) {
+    bool o = false;
+#pragma unroll
+    for (int h = 0; h < QPL; ++h) o = o || (act[h] && m[h] > stop);
+    return o;
+  };
+  // Slots of this lane's open queries in a list counted by *counter: one
+  // atomic per warp; the open queries of copy h follow those of copy h - 1.
+  auto list_slots = [&](uint32_t* counter, uint32_t* slot) {
+    unsigned o[QPL];
+    uint32_t total = 0;
+#pragma unroll
+    for (int h = 0; h < QPL; ++h) {
+      o[h] = __ballot_sync(0xFFFFFFFFu, act[h]);
+      total += __popc(o[h]);
+    }
+    uint32_t base = 0;
+    if (lane == 0 && total) base = atomicAdd(counter, total);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+#pragma unroll
+    for (int h = 0; h < QPL; ++h) {
+      slot[h] = base + __popc(o[h] & below);
+      base += __popc(o[h]);
+    }
   };
 
   // Scans one leaf with every lane of the packet (points read as broadcast
@@ -284,7 +319,9 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
     const float4* lp = B + s;
     // A full 16-point leaf is two 128-byte lines: start the second now.
     if (LT == 16 && s + 16 <= nB) prefetch_l1(lp + 8);
-    float m0 = cmin[0], m1 = cmin[1];
+    float m[QPL];
+#pragma unroll
+    for (int h = 0; h < QPL; ++h) m[h] = cmin[h];
     int k = 0;
     bool settled = false;  // every open query is within the running maximum
     if (LT && s + LT <= nB) {
@@ -294,11 +331,11 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const float4 b = __ldg(lp + k0 + u);
-          m0 = fminf(m0, d2_pt_packed<D>(q[0], b));
-          m1 = fminf(m1, d2_pt_packed<D>(q[1], b));
+#pragma unroll
+          for (int h = 0; h < QPL; ++h) m[h] = fminf(m[h], d2_pt_packed<D>(q[h], b));
         }
         k = k0 + 4;
-        if (!__any_sync(0xFFFFFFFFu, (act[0] && m0 > stop) || (act[1] && m1 > stop))) {
+        if (!__any_sync(0xFFFFFFFFu, needs(m))) {
           settled = true;
           break;
         }
@@ -310,10 +347,10 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const float4 b = __ldg(lp + min(k + u, cnt - 1));
-          m0 = fminf(m0, d2_pt_packed<D>(q[0], b));
-          m1 = fminf(m1, d2_pt_packed<D>(q[1], b));
+#pragma unroll
+          for (int h = 0; h < QPL; ++h) m[h] = fminf(m[h], d2_pt_packed<D>(q[h], b));
         }
-        if (!__any_sync(0xFFFFFFFFu, (act[0] && m0 > stop) || (act[1] && m1 > stop))) {
+        if (!__any_sync(0xFFFFFFFFu, needs(m))) {
           k += 4;
           settled = true;
           break;
@@ -321,8 +358,9 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
       }
       k = min(k, cnt);
     }
-    if (act[0]) cmin[0] = m0;
-    if (act[1]) cmin[1] = m1;
+#pragma unroll
+    for (int h = 0; h < QPL; ++h)
+      if (act[h]) cmin[h] = m[h];
     ++work;
     if (COUNT) {
       ++leafv;
@@ -335,7 +373,7 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
       stop = cand ? soft_stop(thr, soft_r) : thr;
     }
 #pragma unroll
-    for (int h = 0; h < 2; ++h)
+    for (int h = 0; h < QPL; ++h)
       if (act[h] && cmin[h] <= stop) act[h] = false;
   };
 
@@ -367,15 +405,10 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
       // Over budget: queue the open queries (as many as the queue holds;
       // queries beyond it finish here, with no budget).
       may_defer = false;
-      const unsigned o0 = __ballot_sync(0xFFFFFFFFu, act[0]);
-      const unsigned o1 = __ballot_sync(0xFFFFFFFFu, act[1]);
-      uint32_t base = 0;
-      if (lane == 0) base = atomicAdd(&sc->heavy_count, (uint32_t) (__popc(o0) + __popc(o1)));
-      base = __shfl_sync(0xFFFFFFFFu, base, 0);
-      const uint32_t slot[2] = {base + __popc(o0 & below),
-                                base + __popc(o0) + __popc(o1 & below)};
+      uint32_t slot[QPL];
+      list_slots(&sc->heavy_count, slot);
 #pragma unroll
-      for (int h = 0; h < 2; ++h)
+      for (int h = 0; h < QPL; ++h)
         if (act[h] && slot[h] < kDeferCap) {
           defer[slot[h]] = Deferred{(uint32_t) item[h], __float_as_uint(cmin[h])};
           act[h] = false;
@@ -393,7 +426,7 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
       // child (+inf when none does).
       float dLm = INFINITY, dRm = INFINITY;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
+      for (int h = 0; h < QPL; ++h) {
         if (act[h] && stop >= 0.0f) {
           const float mL = box_max_d2<D>(q[h], n0, n2.x, n2.y);
           const float mR = box_max_d2<D>(q[h], n1, n2.z, n2.w);
@@ -443,28 +476,23 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
     if (sp == 0) break;
     --sp;
     next = stk[warp][sp];
-    const bool want = (act[0] && dstk[sp] < cmin[0]) || (act[1] && dstk[sp] < cmin[1]);
+    bool want = false;
+#pragma unroll
+    for (int h = 0; h < QPL; ++h) want = want || (act[h] && dstk[sp] < cmin[h]);
     have = __any_sync(0xFFFFFFFFu, want);
   }
   if (cand) {
     // Listing pass (FP64 refinement): the rows still open are listed with
     // their FP32 minima (and raise the maximum like any other).
-    const unsigned o0 = __ballot_sync(0xFFFFFFFFu, act[0]);
-    const unsigned o1 = __ballot_sync(0xFFFFFFFFu, act[1]);
-    if (o0 | o1) {
-      uint32_t base = 0;
-      if (lane == 0) base = atomicAdd(cand_count, (uint32_t) (__popc(o0) + __popc(o1)));
-      base = __shfl_sync(0xFFFFFFFFu, base, 0);
-      const uint32_t slot[2] = {base + __popc(o0 & below),
-                                base + __popc(o0) + __popc(o1 & below)};
+    uint32_t slot[QPL];
+    list_slots(cand_count, slot);
 #pragma unroll
-      for (int h = 0; h < 2; ++h)
-        if (act[h] && slot[h] < cand_cap)
-          cand[slot[h]] = RowEntry{__float_as_uint(q[h].w), __float_as_uint(cmin[h])};
-    }
+    for (int h = 0; h < QPL; ++h)
+      if (act[h] && slot[h] < cand_cap)
+        cand[slot[h]] = RowEntry{__float_as_uint(q[h].w), __float_as_uint(cmin[h])};
   }
 #pragma unroll
-  for (int h = 0; h < 2; ++h)
+  for (int h = 0; h < QPL; ++h)
     if (act[h]) atomicMax(&sc->max_key, pack_max(cmin[h], __float_as_uint(q[h].w)));
   if (COUNT && lane == 0) {
     atomicAdd(&sc->pairs, pairs);
@@ -478,15 +506,15 @@ __device__ __forceinline__ void lbvh_query_body(const float4* __restrict__ Q, ui
 // The query's code in the target set's frame: its own sorted code when both
 // sets share one frame (qcodes != null), else computed from the point.
 template <int D>
-__device__ __forceinline__ void packet_pos_body(const float4* __restrict__ Q,
+__device__ __forceinline__ void packet_pos_body(uint32_t kp, const float4* __restrict__ Q,
                                                 const uint32_t* __restrict__ qcodes, uint64_t nQ,
                                                 const Frame* __restrict__ tframe,
                                                 const uint32_t* __restrict__ bcodes, uint64_t nB,
                                                 uint32_t mask, uint32_t* __restrict__ pos) {
   const uint64_t t = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
   const uint64_t p = t >> 1;
-  if (p * kPacket >= nQ) return;
-  const uint64_t q = (t & 1) ? min(p * kPacket + kPacket - 1, nQ - 1) : p * kPacket;
+  if (p * kp >= nQ) return;
+  const uint64_t q = (t & 1) ? min(p * kp + kp - 1, nQ - 1) : p * kp;
   uint32_t target;
   if (qcodes) {
     target = qcodes[q] & mask;
@@ -550,6 +578,7 @@ struct QuerySet {
   const uint32_t* qcodes;   // the query set's sorted codes when in that frame, else null
   const uint32_t* bcodes;
   uint32_t mask;            // the target set's sorted code bits
+  uint32_t kp;              // queries per packet: 32 x queries per lane
   // Listing pass of the FP64 input path only (else null): rows that stay
   // open are also listed here, and rows stop only below soft_stop(thr,
   // soft_r).
@@ -562,10 +591,10 @@ struct QuerySets {
   QuerySet d[2];
 };
 
-template <int D, bool COUNT, int LT>
+template <int D, bool COUNT, int LT, int QPL>
 __global__ void __launch_bounds__(kQueryWarps * 32) k_lbvh_query(QuerySets qs) {
   const QuerySet& S = qs.d[blockIdx.y];
-  lbvh_query_body<D, COUNT, LT>(S.Q, S.nQ, S.pstride, S.rows, S.rows_div, S.ppos, S.nodes, S.B,
+  lbvh_query_body<D, COUNT, LT, QPL>(S.Q, S.nQ, S.pstride, S.rows, S.rows_div, S.ppos, S.nodes, S.B,
                                 S.nB, S.L, S.sc, S.defer, S.budget, *S.root, S.cand,
                                 S.cand_count, S.cand_cap, S.soft_r);
 }
@@ -700,7 +729,7 @@ __global__ void __launch_bounds__(kDeferWarps * 32) k_lbvh_defer(QuerySets qs) {
 template <int D>
 __global__ void k_packet_pos(QuerySets qs) {
   const QuerySet& S = qs.d[blockIdx.y];
-  packet_pos_body<D>(S.Q, S.qcodes, S.nQ, S.tframe, S.bcodes, S.nB, S.mask,
+  packet_pos_body<D>(S.kp, S.Q, S.qcodes, S.nQ, S.tframe, S.bcodes, S.nB, S.mask,
                      const_cast<uint32_t*>(S.ppos));
 }
 
@@ -770,9 +799,15 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count, F64Plan* 
     if ((s = spatial_prepare(c, ins[k], &q[k], &t[k])) != HD_OK) return s;
   mark(c, 1);
   QuerySets qs;
+  // Two queries per lane when the launch answers at least
+  // kQplTwoMinQueries queries.
+  uint64_t total_queries = 0;
+  for (int k = 0; k < count; ++k) total_queries += q[k]->n;
+  const bool qpl2 = total_queries >= kQplTwoMinQueries;
+  const uint32_t kp = qpl2 ? 64u : 32u;
   uint64_t packets[2], maxppos = 0;
   for (int k = 0; k < count; ++k) {
-    packets[k] = (q[k]->n + kPacket - 1) / kPacket;
+    packets[k] = (q[k]->n + kp - 1) / kp;
     maxppos += 2 * packets[k];
   }
   void* ppos;
@@ -794,6 +829,7 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count, F64Plan* 
     d.qcodes = q[k]->frame == t[k]->frame ? q[k]->codes : nullptr;
     d.bcodes = t[k]->codes;
     d.mask = t[k]->mask;
+    d.kp = kp;
     d.cand = plan ? plan->cand[k] : nullptr;
     d.cand_count = plan ? plan->cand_count[k] : nullptr;
     d.cand_cap = plan ? plan->cand_cap : 0u;
@@ -835,16 +871,19 @@ static hd_status run_lbvh_dirs(Ctx& c, const DirInput* ins, int count, F64Plan* 
   if (count == 1) qs.d[1] = qs.d[0];
   mark(c, 3);
   const dim3 grid((unsigned) ((max_warps + kQueryWarps - 1) / kQueryWarps), count);
-  // Kernel per (n_dims, counting, leaf size 16 or any).
   const bool l16 = bs.s[0].L == 16;
   auto launch_queries = [&](bool cnt) -> hd_status {
-    const void* fn;
-    if (dims == 2)
-      fn = cnt ? (l16 ? (const void*) k_lbvh_query<2, true, 16> : (const void*) k_lbvh_query<2, true, 0>)
-               : (l16 ? (const void*) k_lbvh_query<2, false, 16> : (const void*) k_lbvh_query<2, false, 0>);
-    else
-      fn = cnt ? (l16 ? (const void*) k_lbvh_query<3, true, 16> : (const void*) k_lbvh_query<3, true, 0>)
-               : (l16 ? (const void*) k_lbvh_query<3, false, 16> : (const void*) k_lbvh_query<3, false, 0>);
+    // Kernel per (n_dims, counting, leaf size 16 or any, queries per lane).
+    static const void* const table[2][2][2][2] = {
+        {{{(const void*) k_lbvh_query<2, false, 0, 1>, (const void*) k_lbvh_query<2, false, 0, 2>},
+          {(const void*) k_lbvh_query<2, false, 16, 1>, (const void*) k_lbvh_query<2, false, 16, 2>}},
+         {{(const void*) k_lbvh_query<2, true, 0, 1>, (const void*) k_lbvh_query<2, true, 0, 2>},
+          {(const void*) k_lbvh_query<2, true, 16, 1>, (const void*) k_lbvh_query<2, true, 16, 2>}}},
+        {{{(const void*) k_lbvh_query<3, false, 0, 1>, (const void*) k_lbvh_query<3, false, 0, 2>},
+          {(const void*) k_lbvh_query<3, false, 16, 1>, (const void*) k_lbvh_query<3, false, 16, 2>}},
+         {{(const void*) k_lbvh_query<3, true, 0, 1>, (const void*) k_lbvh_query<3, true, 0, 2>},
+          {(const void*) k_lbvh_query<3, true, 16, 1>, (const void*) k_lbvh_query<3, true, 16, 2>}}}};
+    const void* fn = table[dims == 3][cnt][l16][qpl2];
     void* qargs[] = {&qs};
     cudaLaunchKernel(fn, grid, dim3(kQueryWarps * 32), qargs, 0, c.stream);
     hd_status r;
