@@ -89,7 +89,7 @@ enum BufSlot {
   kBufGroupOffs,  // offsets of a grouped host-input batch (device copy)
   kBufF64A,       // FP64 input path: caller's double A / B on the device
   kBufF64B,
-  kBufF64Aux,     // FP64 scalars, frozen-pass scalars, candidate lists
+  kBufF64Aux,     // FP64 scalars and candidate lists
   kBufF64Rows,    // FP64 nearest distance and column of every walked row
   kNumBufs
 };
