@@ -51,6 +51,13 @@ constexpr uint32_t kWaitLimit = 1u << 26;
 constexpr uint32_t kListChunks = 64;  // B chunks per group in the list scan, at least
 constexpr int kHeavySlots = 4;        // deferred points a CTA carries at once
 constexpr uint32_t kHeavyStepTiles = 32;  // tiles between a CTA's reductions
+// Checkpoints of the main pass: after the first 1/16 of the visit order
+// (when each part is at least one full wave of the grid), the deferred
+// points listed so far are finished before the pass goes on.  Measured on
+// the 10M mixtures: one checkpoint at 1/16 beats 1/8, {1/16, 1/4} and
+// {1/16, 1/2} (clusters3d 38.6 against 42.7, 44.6, 45.1 ms).
+constexpr uint64_t kEbCheckDiv[] = {16};
+constexpr int kEbMaxParts = (int) (sizeof(kEbCheckDiv) / sizeof(kEbCheckDiv[0])) + 1;
 
 template <int D>
 struct EbPt;
@@ -454,7 +461,7 @@ template <int D>
 __global__ void __launch_bounds__(kEbThreads)
     k_eb_heavy(const float* __restrict__ A, const typename EbPt<D>::T* __restrict__ Bp,
                uint32_t nTiles, DevScalars* sc, const HeavyEntry* __restrict__ list,
-               const uint32_t* n_dev, uint32_t cap) {
+               const uint32_t* n_dev, uint32_t cap, const uint32_t* first_dev) {
   constexpr int P = kHeavySlots;
   __shared__ float red[kEbThreads / 32][P];
   __shared__ float s_thr;
@@ -463,7 +470,8 @@ __global__ void __launch_bounds__(kEbThreads)
   float ax[P], ay[P], az[P], cmin[P];
   uint32_t ia[P], done[P];
   bool act[P];
-  uint32_t next = blockIdx.x;  // next list entry of this CTA
+  // Entries [first, n): an earlier deferred pass finished those below first.
+  uint32_t next = (first_dev ? *first_dev : 0u) + blockIdx.x;  // next list entry of this CTA
   auto take = [&](int s) {
     act[s] = next < n;
     if (act[s]) {
@@ -560,6 +568,14 @@ __global__ void __launch_bounds__(kEbThreads)
     __syncthreads();
   }
   if (tid == 0 && pairs) atomicAdd(&sc->pairs, pairs * kEbTile);
+}
+
+// Between the early checkpoint and the bulk of the main pass: the deferred
+// entries listed so far are finished, and the bulk's visit counter starts
+// again at zero.
+__global__ void k_eb_mark_heavy(DevScalars* sc) {
+  sc->heavy_mark = sc->heavy_count;
+  sc->next = 0;
 }
 
 // The seed list: the first n visit positions of A, nothing scanned yet.
@@ -663,16 +679,44 @@ hd_status run_eb_dim(Ctx& c, const DirInput& in) {
     const PT* b_ptr = (const PT*) pb;
     HeavyEntry* h_ptr = (HeavyEntry*) ph;
     uint32_t heavy_cap = (uint32_t) (in.nA - n_seed);
-    uint64_t a_begin = n_seed, a_end = in.nA;
-    void* args[] = {&a_ptr, &pA, &a_begin, &a_end, &b_ptr, (void*) &nTiles, &capTiles, &sc,
-                    &h_ptr, &heavy_cap};
-    cudaLaunchKernel(fns[pick], dim3(grid), dim3(kEbThreads), args, 0, c.stream);
-    if ((s = after_launch(c, "eb_main")) != HD_OK) return s;
-    mark(c, 4);
-    k_eb_heavy<D><<<c.num_sms * 4, kEbThreads, 0, c.stream>>>(in.A, (const PT*) pb, nTiles, sc,
-                                                               (const HeavyEntry*) ph,
-                                                               &sc->heavy_count, heavy_cap);
-    if ((s = after_launch(c, "eb_deferred")) != HD_OK) return s;
+    // Checkpoints: the main pass runs in parts; after each part the points
+    // it deferred are finished before the next part starts.  Deferred points
+    // include the outliers, whose distances are the ones that lift the
+    // running maximum to its final level; finished early, they let the rest
+    // break sooner (clusters3d 10M 49.5 -> 38.6 ms with one checkpoint at
+    // 1/16).  A checkpoint is kept only when every part fills a full wave.
+    const uint64_t wave = (uint64_t) grid * per_cta;
+    uint64_t ends[kEbMaxParts];
+    int parts = 0;
+    uint64_t last = n_seed;
+    for (uint64_t div : kEbCheckDiv) {
+      const uint64_t e = n_seed + rest / div;
+      if (e >= last + wave && in.nA >= e + wave) {
+        ends[parts++] = e;
+        last = e;
+      }
+    }
+    ends[parts++] = in.nA;
+    uint64_t a_begin = n_seed;
+    for (int part = 0; part < parts; ++part) {
+      uint64_t a_end = ends[part];
+      if (part > 0) {
+        // A fresh visit counter, and the deferred pass starts after the
+        // entries the earlier passes finished.
+        k_eb_mark_heavy<<<1, 1, 0, c.stream>>>(sc);
+        if ((s = after_launch(c, "eb_mark")) != HD_OK) return s;
+      }
+      void* args[] = {&a_ptr, &pA, &a_begin, &a_end, &b_ptr, (void*) &nTiles, &capTiles, &sc,
+                      &h_ptr, &heavy_cap};
+      cudaLaunchKernel(fns[pick], dim3(grid), dim3(kEbThreads), args, 0, c.stream);
+      if ((s = after_launch(c, "eb_main")) != HD_OK) return s;
+      if (part == parts - 1) mark(c, 4);
+      k_eb_heavy<D><<<c.num_sms * 4, kEbThreads, 0, c.stream>>>(
+          in.A, (const PT*) pb, nTiles, sc, (const HeavyEntry*) ph, &sc->heavy_count, heavy_cap,
+          part > 0 ? &sc->heavy_mark : nullptr);
+      if ((s = after_launch(c, "eb_deferred")) != HD_OK) return s;
+      a_begin = a_end;
+    }
   } else {
     mark(c, 4);
   }
@@ -788,7 +832,7 @@ cudaError_t noalloc_direction(cudaStream_t st, int num_sms, const float* A, uint
     if ((e = cudaLaunchKernel(fns[pick], dim3(g), dim3(kEbThreads), args, 0, st)) != cudaSuccess)
       return e;
     k_eb_heavy<D><<<num_sms * 4, kEbThreads, 0, st>>>(A, pb, nTiles, sc, heavy, &sc->heavy_count,
-                                                      heavy_cap);
+                                                      heavy_cap, nullptr);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return certify_on_stream(st, num_sms, A, B, nB, D, sc);

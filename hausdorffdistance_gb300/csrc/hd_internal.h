@@ -41,7 +41,7 @@ struct DevScalars {
   uint32_t heavy_count;           // deferred points
   uint32_t status;                // error bits (kErr*)
   uint32_t sample_count;
-  uint32_t pad;
+  uint32_t heavy_mark;            // EB: deferred entries already finished
   // Finalised result written by the finalize kernel.
   double d2_64;                   // FP64 squared distance of (ia, ib)
   float d2;                       // FP32 squared distance (max-min)
