@@ -86,6 +86,40 @@ def test_cpu_execution_is_double(exe, double_inputs, undirected, tmp_path):
     assert json.loads(out.read_text())["HDResult"] == want
 
 
+@pytest.mark.parametrize("fmt", ["off", "ply"])
+def test_cpu_execution_is_double_off_ply(exe, fmt, tmp_path):
+    """-is_double through the OFF loader (each number parsed once as float,
+    once as double) and the ASCII PLY loader (doubles shifted so that every
+    axis starts at 0, as the reference's PLY loader does): the CPU
+    early-break gives the oracle's exact FP64 distance of the parsed doubles."""
+    import hd_oracle
+    rng = np.random.default_rng(12)
+    a = 3.0 + rng.random((700, 3))
+    b = 3.0 + rng.random((600, 3)) * 1.05
+    paths = []
+    for name, pts in (("a", a), ("b", b)):
+        p = str(tmp_path / f"{name}.{fmt}")
+        with open(p, "w") as f:
+            if fmt == "off":
+                f.write(f"OFF\n{len(pts)} 0 0\n")
+            else:
+                f.write(f"ply\nformat ascii 1.0\nelement vertex {len(pts)}\nproperty double x\n"
+                        "property double y\nproperty double z\nend_header\n")
+            for q in pts:
+                f.write(" ".join("%.17g" % v for v in q) + "\n")
+        paths.append(p)
+    if fmt == "ply":
+        # The PLY loader shifts each set to its own minimum per axis.
+        a, b = a - a.min(0), b - b.min(0)
+    want = float(np.sqrt(hd_oracle.exact_f64(a, b)[0]))
+    r = subprocess.run([exe, "-input1", paths[0], "-input2", paths[1], "-input_type", fmt,
+                        "-n_dims", "3", "-execution", "cpu", "-is_double", "-repeat", "1"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("HausdorffDistance")][0]
+    assert float(line.split()[-1]) == want
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("variant", ["hybrid", "rt", "eb"])
 def test_hd_exec_is_double(exe, double_inputs, variant, tmp_path):
