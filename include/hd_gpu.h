@@ -267,7 +267,9 @@ HD_API hd_status hd_solve_batch_plain(hd_ctx* ctx, const float* A, uint64_t tota
  * stays right after a device reset or under another context.  The call waits
  * for its stream to finish its own work before it returns (it reads the result
  * back and synchronises the stream); if a launch fails part-way, it also waits
- * for the kernels it already queued before returning the error.  Every call
+ * for the kernels it already queued before returning the error.  Because it
+ * synchronises, it cannot be recorded into a CUDA graph: do not call it while
+ * its stream (or any stream, under a global-mode capture) is capturing.  Every call
  * shares the one array, which keeps the last call's contents (each call resets
  * what must start at zero): calls that overlap on the GPU — from two host
  * threads, or on two streams — race on it and must be serialised by the
