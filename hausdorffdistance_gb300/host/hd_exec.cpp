@@ -10,7 +10,8 @@
 // together, get the reference's "Grid", "MBR" and "Density" statistics
 // (run_hausdorff_distance.cu:150-185) from hd_compute_stats on the GPU.
 // Differences: -undirected computes max(h(A,B), h(B,A)) in one call;
-// -input_type also accepts "bin" (the reference's point-cache layout);
+// -input_type also accepts "bin" (the reference's point-cache layout), and
+// "image" reads NIfTI-1 (.nii) and MetaImage (.mha/.mhd) files without ITK;
 // -variant accepts eb | hybrid | auto | rt | lbvh | grid | bf16 | brute; the
 // grid statistics' "NonEmptyCells" is the non-empty fraction as a real number
 // (the reference divides two integers there, which truncates it to 0).
@@ -114,7 +115,7 @@ std::string now_string() {
 
 void usage(const char* argv0) {
   std::fprintf(stderr,
-               "Usage: %s -input1 A -input2 B -input_type wkt|off|ply|bin -n_dims 2|3|<d> "
+               "Usage: %s -input1 A -input2 B -input_type wkt|off|ply|image|bin -n_dims 2|3|<d> "
                "[-variant eb|hybrid|rt|lbvh|grid|bf16|brute] [-execution gpu|cpu] [-repeat 5] "
                "[-seed 0] [-check] [-json out.json] [-serialize dir] [-limit n] [-normalize] "
                "[-translate r] [-undirected] [-sample_rate 0.01] [-n_points_cell 8] "
@@ -141,7 +142,8 @@ int main(int argc, char** argv) {
   Flags fl = parse(argc, argv);
   const std::string input1 = fl.get("input1", ""), input2 = fl.get("input2", "");
   const std::string input_type = lower(fl.get("input_type", ""));
-  if (input_type != "wkt" && input_type != "off" && input_type != "ply" && input_type != "bin") {
+  if (input_type != "wkt" && input_type != "off" && input_type != "ply" && input_type != "image" &&
+      input_type != "bin") {
     std::fprintf(stderr, "Unsupported input type: %s\n", input_type.c_str());
     return 1;
   }
@@ -150,7 +152,7 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "Wrong number of dimensions: %d\n", dims);
     return 1;
   }
-  if ((input_type == "wkt" || input_type == "off" || input_type == "ply") && dims != 2 && dims != 3) {
+  if (input_type != "bin" && dims != 2 && dims != 3) {
     std::fprintf(stderr, "%s inputs have 2 or 3 dimensions\n", input_type.c_str());
     return 1;
   }

@@ -339,16 +339,278 @@ inline void SaveBin(const std::string& path, const PointSet& ps) {
     ofs.write((const char*) ps.xyz.data(), (std::streamsize) (ps.xyz.size() * sizeof(float)));
 }
 
+// ---------------------------------------------------------------------------
+// Images.  The reference reads them with ITK
+// (src/loaders/img_loader.h:13-63: ImageFileReader<Image<unsigned char, N>>,
+// then every voxel whose pixel is > 0 becomes the point of its index, index[0]
+// fastest, until `limit` points).  ITK is not available here, so the header +
+// raw formats are read directly: NIfTI-1 single files (.nii; the format of
+// the reference's medical-image runs, expr/running_time.sh:132-160) and
+// MetaImage (.mha with LOCAL data, .mhd with a raw file beside it).
+namespace img {
+
+enum class Elem { U8, I8, U16, I16, U32, I32, U64, I64, F32, F64 };
+
+inline size_t elem_bytes(Elem e) {
+  switch (e) {
+    case Elem::U8: case Elem::I8: return 1;
+    case Elem::U16: case Elem::I16: return 2;
+    case Elem::U32: case Elem::I32: case Elem::F32: return 4;
+    default: return 8;
+  }
+}
+
+struct Volume {
+  int ndim = 0;
+  uint64_t size[8] = {1, 1, 1, 1, 1, 1, 1, 1};
+  Elem elem = Elem::U8;
+  bool swap = false;            // data in the other byte order than this host's
+  std::string data_path;        // file holding the voxels
+  uint64_t data_offset = 0;     // byte offset of the first voxel there
+  bool rescale = false;         // NIfTI scl_slope / scl_inter in effect
+  double slope = 1.0, inter = 0.0;
+};
+
+inline bool host_little_endian() {
+  const uint16_t one = 1;
+  unsigned char b;
+  std::memcpy(&b, &one, 1);
+  return b == 1;
+}
+
+// A real pixel value converted to unsigned char as a C++ static_cast does on
+// the machines the reference ran on (truncation toward zero to a 32-bit
+// integer, then its low byte); values outside the 32-bit range and NaN give 0.
+inline uint8_t real_to_byte(double v) {
+  if (!(v > -2147483649.0 && v < 2147483648.0)) return 0;
+  return (uint8_t) (uint32_t) (int32_t) v;
+}
+
+// One voxel's value as ITK's reader hands it to the unsigned-char image: the
+// stored value converted with a static_cast (integers keep their low byte).
+// With a NIfTI rescale, ITK first scales into float (double for double data):
+// value * slope + inter in double, rounded to the buffer type.
+inline uint8_t voxel_byte(const unsigned char* p, const Volume& v) {
+  unsigned char b[8];
+  const size_t nb = elem_bytes(v.elem);
+  for (size_t i = 0; i < nb; ++i) b[i] = v.swap ? p[nb - 1 - i] : p[i];
+  double real = 0.0;
+  uint64_t bits = 0;
+  bool is_real = false;
+  switch (v.elem) {
+    case Elem::U8: bits = b[0]; real = b[0]; break;
+    case Elem::I8: { int8_t x; std::memcpy(&x, b, 1); bits = (uint64_t) (int64_t) x; real = x; break; }
+    case Elem::U16: { uint16_t x; std::memcpy(&x, b, 2); bits = x; real = x; break; }
+    case Elem::I16: { int16_t x; std::memcpy(&x, b, 2); bits = (uint64_t) (int64_t) x; real = x; break; }
+    case Elem::U32: { uint32_t x; std::memcpy(&x, b, 4); bits = x; real = x; break; }
+    case Elem::I32: { int32_t x; std::memcpy(&x, b, 4); bits = (uint64_t) (int64_t) x; real = x; break; }
+    case Elem::U64: { uint64_t x; std::memcpy(&x, b, 8); bits = x; real = (double) x; break; }
+    case Elem::I64: { int64_t x; std::memcpy(&x, b, 8); bits = (uint64_t) x; real = (double) x; break; }
+    case Elem::F32: { float x; std::memcpy(&x, b, 4); real = x; is_real = true; break; }
+    case Elem::F64: { double x; std::memcpy(&x, b, 8); real = x; is_real = true; break; }
+  }
+  if (v.rescale) {
+    if (v.elem == Elem::F64) return real_to_byte(real * v.slope + v.inter);
+    const double s = (double) (float) real * v.slope + v.inter;
+    return real_to_byte((double) (float) s);
+  }
+  return is_real ? real_to_byte(real) : (uint8_t) bits;
+}
+
+template <typename T>
+inline T rd(const unsigned char* h, size_t off, bool swap) {
+  unsigned char b[sizeof(T)];
+  for (size_t i = 0; i < sizeof(T); ++i) b[i] = swap ? h[off + sizeof(T) - 1 - i] : h[off + i];
+  T x;
+  std::memcpy(&x, b, sizeof(T));
+  return x;
+}
+
+// NIfTI-1 (the public nifti1.h layout): a 348-byte header, dim[] at byte 40,
+// datatype at 70, vox_offset at 108, scl_slope/scl_inter at 112/116, magic
+// "n+1" at 344 for a single file; either byte order (sizeof_hdr tells).
+inline Volume ReadNifti(const std::string& path) {
+  std::ifstream ifs(path, std::ios::binary);
+  if (!ifs) load_fail("cannot open " + path);
+  unsigned char h[348];
+  ifs.read((char*) h, sizeof(h));
+  if (!ifs) load_fail("truncated NIfTI header: " + path);
+  if (h[0] == 0x1F && h[1] == 0x8B) load_fail("compressed images are not supported: " + path);
+  Volume v;
+  v.swap = rd<int32_t>(h, 0, false) != 348;
+  if (v.swap && rd<int32_t>(h, 0, true) != 348)
+    load_fail("not a NIfTI-1 file (sizeof_hdr != 348): " + path);
+  if (std::memcmp(h + 344, "n+1", 4) != 0)
+    load_fail("only single-file NIfTI-1 images (magic n+1) are supported: " + path);
+  const int nd = rd<int16_t>(h, 40, v.swap);
+  if (nd < 1 || nd > 7) load_fail("bad NIfTI dimension count: " + path);
+  v.ndim = nd;
+  for (int d = 0; d < nd; ++d) {
+    const int s = rd<int16_t>(h, 42 + 2 * d, v.swap);
+    if (s < 1) load_fail("bad NIfTI image size: " + path);
+    v.size[d] = (uint64_t) s;
+  }
+  switch (rd<int16_t>(h, 70, v.swap)) {
+    case 2: v.elem = Elem::U8; break;
+    case 4: v.elem = Elem::I16; break;
+    case 8: v.elem = Elem::I32; break;
+    case 16: v.elem = Elem::F32; break;
+    case 64: v.elem = Elem::F64; break;
+    case 256: v.elem = Elem::I8; break;
+    case 512: v.elem = Elem::U16; break;
+    case 768: v.elem = Elem::U32; break;
+    case 1024: v.elem = Elem::I64; break;
+    case 1280: v.elem = Elem::U64; break;
+    default: load_fail("unsupported NIfTI datatype (complex or RGB): " + path);
+  }
+  const float off = rd<float>(h, 108, v.swap);
+  v.data_offset = off < 352.0f ? 352 : (uint64_t) off;
+  const float slope = rd<float>(h, 112, v.swap), inter = rd<float>(h, 116, v.swap);
+  // Rescaled when the slope is set (non-zero) and the pair is not the identity.
+  v.rescale = std::isfinite(slope) && std::isfinite(inter) && slope != 0.0f &&
+              (slope != 1.0f || inter != 0.0f);
+  v.slope = slope;
+  v.inter = inter;
+  v.data_path = path;
+  return v;
+}
+
+// MetaImage: "Key = Value" lines ending with ElementDataFile; LOCAL means the
+// voxels follow that line (.mha), else they are in the named file beside the
+// header (.mhd).  HeaderSize skips bytes at the start of the data.
+inline Volume ReadMeta(const std::string& path) {
+  std::ifstream ifs(path, std::ios::binary);
+  if (!ifs) load_fail("cannot open " + path);
+  Volume v;
+  bool msb = false, have_type = false, have_file = false;
+  std::string line, file;
+  long long header_size = 0;
+  int channels = 1;
+  while (!have_file && std::getline(ifs, line)) {
+    const size_t eq = line.find('=');
+    if (eq == std::string::npos) continue;
+    auto trim = [](std::string s) {
+      const size_t a = s.find_first_not_of(" \t\r"), b = s.find_last_not_of(" \t\r");
+      return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+    };
+    const std::string key = trim(line.substr(0, eq)), val = trim(line.substr(eq + 1));
+    std::string lval = val;
+    for (char& ch : lval) ch = (char) std::tolower((unsigned char) ch);
+    if (key == "NDims") {
+      v.ndim = std::atoi(val.c_str());
+      if (v.ndim < 1 || v.ndim > 8) load_fail("bad MetaImage NDims: " + path);
+    } else if (key == "DimSize") {
+      std::istringstream ss(val);
+      for (int d = 0; d < 8; ++d) {
+        long long s;
+        if (!(ss >> s)) break;
+        if (s < 1) load_fail("bad MetaImage DimSize: " + path);
+        v.size[d] = (uint64_t) s;
+      }
+    } else if (key == "ElementType") {
+      have_type = true;
+      if (val == "MET_UCHAR") v.elem = Elem::U8;
+      else if (val == "MET_CHAR") v.elem = Elem::I8;
+      else if (val == "MET_USHORT") v.elem = Elem::U16;
+      else if (val == "MET_SHORT") v.elem = Elem::I16;
+      else if (val == "MET_UINT") v.elem = Elem::U32;
+      else if (val == "MET_INT") v.elem = Elem::I32;
+      else if (val == "MET_ULONG_LONG") v.elem = Elem::U64;
+      else if (val == "MET_LONG_LONG") v.elem = Elem::I64;
+      else if (val == "MET_FLOAT") v.elem = Elem::F32;
+      else if (val == "MET_DOUBLE") v.elem = Elem::F64;
+      else load_fail("unsupported MetaImage ElementType " + val + ": " + path);
+    } else if (key == "BinaryDataByteOrderMSB" || key == "ElementByteOrderMSB") {
+      msb = lval == "true";
+    } else if (key == "CompressedData") {
+      if (lval == "true") load_fail("compressed images are not supported: " + path);
+    } else if (key == "BinaryData") {
+      if (lval == "false") load_fail("ASCII MetaImage data is not supported: " + path);
+    } else if (key == "ElementNumberOfChannels") {
+      channels = std::atoi(val.c_str());
+    } else if (key == "HeaderSize") {
+      header_size = std::atoll(val.c_str());
+    } else if (key == "ElementDataFile") {
+      have_file = true;
+      file = val;
+    }
+  }
+  if (!have_file || !have_type || v.ndim == 0)
+    load_fail("MetaImage header lacks NDims, ElementType or ElementDataFile: " + path);
+  if (channels != 1) load_fail("multi-channel images are not supported: " + path);
+  if (header_size < 0) load_fail("MetaImage HeaderSize -1 is not supported: " + path);
+  v.swap = msb == host_little_endian() && elem_bytes(v.elem) > 1;
+  if (file == "LOCAL") {
+    v.data_path = path;
+    v.data_offset = (uint64_t) ifs.tellg() + (uint64_t) header_size;
+  } else {
+    if (file == "LIST" || file.find('%') != std::string::npos)
+      load_fail("MetaImage slice lists are not supported: " + path);
+    const size_t slash = path.find_last_of('/');
+    v.data_path = file[0] == '/' || slash == std::string::npos ? file
+                                                                : path.substr(0, slash + 1) + file;
+    v.data_offset = (uint64_t) header_size;
+  }
+  return v;
+}
+
+}  // namespace img
+
+// Image inputs (src/loaders/img_loader.h:13-63): every voxel whose value,
+// converted to unsigned char as ITK's reader converts pixel buffers (a
+// static_cast; img::voxel_byte), is non-zero gives the point of its index,
+// index 0 fastest, the first `limit` such voxels.  An image with fewer
+// dimensions than `dims` has the missing indices 0 (ITK reads it as size 1
+// there); extra dimensions must have size 1.
+inline PointSet LoadImage(const std::string& path, int dims, size_t limit, bool keep64 = false) {
+  std::string low = path;
+  for (char& ch : low) ch = (char) std::tolower((unsigned char) ch);
+  auto ends = [&](const char* s) {
+    const size_t n = std::strlen(s);
+    return low.size() >= n && low.compare(low.size() - n, n, s) == 0;
+  };
+  img::Volume v;
+  if (ends(".nii"))
+    v = img::ReadNifti(path);
+  else if (ends(".mha") || ends(".mhd"))
+    v = img::ReadMeta(path);
+  else
+    load_fail("unsupported image format (.nii, .mha or .mhd; compressed files are not read): " +
+              path);
+  for (int d = dims; d < v.ndim; ++d)
+    if (v.size[d] != 1) load_fail("image has more than " + std::to_string(dims) + " dimensions: " + path);
+  uint64_t count = 1;
+  for (int d = 0; d < v.ndim; ++d) count *= v.size[d];
+  const size_t eb = img::elem_bytes(v.elem);
+  std::ifstream ifs(v.data_path, std::ios::binary);
+  if (!ifs) load_fail("cannot open " + v.data_path);
+  ifs.seekg((std::streamoff) v.data_offset);
+  std::vector<unsigned char> raw(count * eb);
+  ifs.read((char*) raw.data(), (std::streamsize) raw.size());
+  if (!ifs) load_fail("truncated image data: " + v.data_path);
+  PointSet ps;
+  ps.dims = dims;
+  ps.keep64 = keep64;
+  const uint64_t sx = v.size[0], sy = v.ndim > 1 ? v.size[1] : 1;
+  for (uint64_t i = 0; i < count && ps.size() < limit; ++i) {
+    if (img::voxel_byte(&raw[i * eb], v) == 0) continue;
+    const double idx[3] = {(double) (i % sx), (double) ((i / sx) % sy), (double) (i / (sx * sy))};
+    for (int d = 0; d < dims; ++d) ps.push(d < 3 ? idx[d] : 0.0);
+  }
+  return ps;
+}
+
 // Loads with the reference's -serialize cache (loader.h:188-234): the cache
 // file <folder>/points_<path with '/' as '_'>_limit_<limit>.bin is read when
 // present, else written after loading (a separate "_f64" cache holds
-// doubles).  type: wkt | off | ply | bin.
+// doubles).  type: wkt | off | ply | image | bin.  Like the reference
+// (run_hausdorff_distance.cu:91-111), PLY and image inputs bypass the cache.
 inline PointSet LoadPoints(const std::string& path, const std::string& type, int dims,
                            long long limit, const std::string& cache_folder,
                            bool keep64 = false) {
   const size_t lim = limit > 0 ? (size_t) limit : std::numeric_limits<size_t>::max();
   std::string cache;
-  if (!cache_folder.empty() && type != "bin") {
+  if (!cache_folder.empty() && (type == "wkt" || type == "off")) {
     std::string esc = path;
     std::replace(esc.begin(), esc.end(), '/', '_');
     if (mkdir(cache_folder.c_str(), 0755) != 0 && errno != EEXIST)
@@ -364,6 +626,8 @@ inline PointSet LoadPoints(const std::string& path, const std::string& type, int
     ps = LoadOFF(path, dims, lim, keep64);
   else if (type == "ply")
     ps = LoadPLY(path, dims, lim, keep64);
+  else if (type == "image")
+    ps = LoadImage(path, dims, lim, keep64);
   else if (type == "bin")
     ps = LoadBin(path, dims, lim, keep64);
   else

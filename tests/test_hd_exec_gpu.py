@@ -120,6 +120,61 @@ def test_cpu_execution_is_double_off_ply(exe, fmt, tmp_path):
     assert float(line.split()[-1]) == want
 
 
+@pytest.fixture(scope="module")
+def image_inputs(tmp_path_factory):
+    """Two 3-D int16 volumes shaped like the reference's medical-image inputs
+    (NIfTI-1 files, a noisy ellipsoid of intensities in each, some of them
+    multiples of 256 that the unsigned-char conversion drops), with the point
+    sets the loader must take from them and the oracle's FP32 distances."""
+    import hd_oracle
+    from image_files import image_points, write_nifti
+    d = tmp_path_factory.mktemp("img")
+    rng = np.random.default_rng(21)
+    z, y, x = np.meshgrid(np.arange(30), np.arange(34), np.arange(38), indexing="ij")
+    vols = []
+    for c, r in (((15, 17, 19), (11, 13, 15)), ((14, 18, 20), (12, 12, 16))):
+        inside = ((z - c[0]) / r[0]) ** 2 + ((y - c[1]) / r[1]) ** 2 + ((x - c[2]) / r[2]) ** 2 < 1
+        v = np.where(inside, rng.integers(1, 1200, inside.shape), 0)
+        v[rng.random(inside.shape) < 0.002] = 700  # stray voxels outside the body
+        v[inside & (rng.random(inside.shape) < 0.05)] = 512
+        vols.append(v.astype(np.int16))
+    paths = [str(d / "a.nii"), str(d / "b.nii")]
+    for pth, v in zip(paths, vols):
+        write_nifti(pth, v)
+    a, b = (image_points(v, 3).astype(np.float32) for v in vols)
+    h_ab = np.sqrt(np.float32(hd_oracle.exact(a, b, 32)[0]))
+    h_ba = np.sqrt(np.float32(hd_oracle.exact(b, a, 32)[0]))
+    return paths, len(a), len(b), h_ab, max(h_ab, h_ba)
+
+
+@pytest.mark.parametrize("undirected", [False, True])
+def test_cpu_execution_image(exe, image_inputs, undirected, tmp_path):
+    """-input_type image -execution cpu on NIfTI volumes: the voxel points the
+    reference's ITK loader takes, and the oracle's FP32 distance bit for bit."""
+    paths, na, nb, h_ab, h_und = image_inputs
+    out = tmp_path / "run.json"
+    r = subprocess.run([exe, "-input1", paths[0], "-input2", paths[1], "-input_type", "image",
+                        "-n_dims", "3", "-execution", "cpu", "-repeat", "1", "-json", str(out)]
+                       + (["-undirected"] if undirected else []), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    st = json.loads(out.read_text())
+    assert [f["NumPoints"] for f in st["Input"]["Files"]] == [na, nb]
+    assert bits(st["HDResult"]) == bits(h_und if undirected else h_ab)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", ["hybrid", "eb"])
+def test_hd_exec_image(exe, image_inputs, variant, tmp_path):
+    """-input_type image on the GPU: the oracle's FP32 distance bit for bit."""
+    paths, _, _, _, h_und = image_inputs
+    out = tmp_path / "run.json"
+    r = subprocess.run([exe, "-input1", paths[0], "-input2", paths[1], "-input_type", "image",
+                        "-n_dims", "3", "-variant", variant, "-undirected", "-repeat", "2",
+                        "-json", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert bits(json.loads(out.read_text())["HDResult"]) == bits(h_und)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("variant", ["hybrid", "rt", "eb"])
 def test_hd_exec_is_double(exe, double_inputs, variant, tmp_path):

@@ -93,3 +93,111 @@ def test_bad_inputs(probe, tmp_path):
         run(probe, p, "wkt", 2)
     with pytest.raises(RuntimeError):
         run(probe, tmp_path / "missing.off", "off", 3)
+
+
+# Image inputs (-input_type image): NIfTI-1 and MetaImage read without ITK.
+from image_files import image_points, write_meta, write_nifti  # noqa: E402
+
+
+def test_nifti_uint8_mask(probe, tmp_path):
+    rng = np.random.default_rng(3)
+    vol = ((rng.random((5, 6, 7)) < 0.3) * rng.integers(1, 256, (5, 6, 7))).astype(np.uint8)
+    p = tmp_path / "m.nii"
+    write_nifti(p, vol)
+    got = run(probe, p, "image", 3)
+    assert len(got) == np.count_nonzero(vol)
+    assert np.array_equal(got, image_points(vol, 3))
+    # -limit keeps the first points in index order (x fastest).
+    assert np.array_equal(run(probe, p, "image", 3, limit=10), image_points(vol, 3, limit=10))
+
+
+def test_nifti_int16_low_byte_big_endian(probe, tmp_path):
+    """Values reach the unsigned-char image through a static_cast: 256, 512
+    and -256 have a zero low byte and give no point; 300 and -1 do."""
+    vol = np.array([[[0, 256, 300, -1], [512, -256, 1, 255]]], np.int16)
+    p = tmp_path / "be.nii"
+    write_nifti(p, vol, big_endian=True)
+    got = run(probe, p, "image", 3)
+    assert np.array_equal(got, [[2, 0, 0], [3, 0, 0], [2, 1, 0], [3, 1, 0]])
+    assert np.array_equal(got, image_points(vol, 3))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int16, np.uint16, np.int32])
+def test_nifti_rescaled(probe, tmp_path, dtype):
+    """scl_slope / scl_inter applied before the conversion (in float for all
+    but double data), reals truncated toward zero."""
+    rng = np.random.default_rng(5)
+    if np.dtype(dtype).kind == "f":
+        vol = (rng.random((3, 4, 5)) * 300 - 20).astype(dtype)
+        vol.reshape(-1)[:4] = [0.5, 0.4, 1.0, 128.5]
+    else:
+        vol = rng.integers(0, 400, (3, 4, 5)).astype(dtype)
+    p = tmp_path / "s.nii"
+    write_nifti(p, vol, slope=2.0, inter=-1.0)
+    got = run(probe, p, "image", 3)
+    assert np.array_equal(got, image_points(vol, 3, slope=2.0, inter=-1.0))
+    # Slope 1 and intercept 0 is no rescale.
+    write_nifti(p, vol, slope=1.0, inter=0.0)
+    assert np.array_equal(run(probe, p, "image", 3), image_points(vol, 3))
+
+
+def test_image_dimensions(probe, tmp_path):
+    rng = np.random.default_rng(6)
+    flat = (rng.random((6, 9)) < 0.5).astype(np.uint8)
+    p = tmp_path / "flat.nii"
+    write_nifti(p, flat)
+    got = run(probe, p, "image", 3)  # a 2-D image read as 3-D: k = 0
+    assert np.array_equal(got, image_points(flat, 3)) and not got[:, 2].any()
+    assert np.array_equal(run(probe, p, "image", 2), image_points(flat, 2))
+    one = flat[None]  # 3-D with a single slice reads as 2-D
+    q = tmp_path / "one.nii"
+    write_nifti(q, one)
+    assert np.array_equal(run(probe, q, "image", 2), image_points(flat, 2))
+    thick = np.stack([flat, flat])
+    r = tmp_path / "thick.nii"
+    write_nifti(r, thick)
+    with pytest.raises(RuntimeError, match="more than 2 dimensions"):
+        run(probe, r, "image", 2)
+
+
+@pytest.mark.parametrize("big_endian", [False, True])
+def test_metaimage(probe, tmp_path, big_endian):
+    rng = np.random.default_rng(7)
+    vol = (rng.integers(-3, 3, (4, 5, 6)) * 128).astype(np.int16)
+    p = tmp_path / "v.mha"
+    write_meta(p, vol, big_endian=big_endian)
+    assert np.array_equal(run(probe, p, "image", 3), image_points(vol, 3))
+    fl = (rng.random((4, 5, 6)) * 3).astype(np.float32)
+    q = tmp_path / "v.mhd"
+    write_meta(q, fl, big_endian=big_endian, local=False, header_size=16,
+               extra="ElementSpacing = 1 1 1\n")
+    assert np.array_equal(run(probe, q, "image", 3), image_points(fl, 3))
+
+
+def test_image_errors(probe, tmp_path):
+    vol = np.ones((2, 3, 4), np.uint8)
+    gz = tmp_path / "c.nii"
+    gz.write_bytes(b"\x1f\x8b" + b"\0" * 400)
+    with pytest.raises(RuntimeError, match="compressed"):
+        run(probe, gz, "image", 3)
+    cx = tmp_path / "cx.nii"
+    write_nifti(cx, vol, datatype=32)  # complex64
+    with pytest.raises(RuntimeError, match="datatype"):
+        run(probe, cx, "image", 3)
+    cm = tmp_path / "cm.mha"
+    write_meta(cm, vol, extra="CompressedData = True\n")
+    with pytest.raises(RuntimeError, match="compressed"):
+        run(probe, cm, "image", 3)
+    ch = tmp_path / "ch.mha"
+    write_meta(ch, vol, extra="ElementNumberOfChannels = 3\n")
+    with pytest.raises(RuntimeError, match="multi-channel"):
+        run(probe, ch, "image", 3)
+    png = tmp_path / "x.png"
+    png.write_bytes(b"\x89PNG")
+    with pytest.raises(RuntimeError, match="unsupported image format"):
+        run(probe, png, "image", 2)
+    short = tmp_path / "short.nii"
+    write_nifti(short, vol)
+    short.write_bytes(short.read_bytes()[:-5])
+    with pytest.raises(RuntimeError, match="truncated"):
+        run(probe, short, "image", 3)
