@@ -119,8 +119,15 @@ void usage(const char* argv0) {
                "[-variant eb|hybrid|rt|lbvh|grid|bf16|brute] [-execution gpu|cpu] [-repeat 5] "
                "[-seed 0] [-check] [-json out.json] [-serialize dir] [-limit n] [-normalize] "
                "[-translate r] [-undirected] [-sample_rate 0.01] [-n_points_cell 8] "
-               "[-eb_only_threshold 0] [-device 0] [-parallelism n] [-stats_n_points_cell 10]\n",
+               "[-eb_only_threshold 0] [-max_hit 256] [-auto_tune] [-device 0] [-parallelism n] "
+               "[-stats_n_points_cell 10]\n",
                argv0);
+}
+
+// -max_hit as an LBVH traversal budget: 0 means no cap, as in the reference.
+uint32_t budget_from_max_hit(long long max_hit) {
+  if (max_hit <= 0 || max_hit >= 0xFFFFFFFFll) return 0xFFFFFFFFu;
+  return (uint32_t) max_hit;
 }
 
 std::vector<double> split_doubles(const std::string& s) {
@@ -216,6 +223,20 @@ int main(int argc, char** argv) {
   opt.sample_rate = fl.getd("sample_rate", 0.01);
   opt.n_points_cell = (uint32_t) fl.geti("n_points_cell", 8);
   opt.eb_only_threshold = (uint32_t) fl.geti("eb_only_threshold", 0);
+  // The hybrid's RT knobs (hausdorff_distance_hybrid.h:286-295,708-778):
+  // -max_hit caps the index work of one query before it falls back to the
+  // early-break scan, 0 meaning no cap; here it caps the nodes and leaves an
+  // LBVH packet visits before its open queries go to the deferred pass.
+  // Without the flag, and under -auto_tune / -auto_tune_max_hit (the
+  // reference's model predictions), the tuned table decides; likewise
+  // -auto_tune / -auto_tune_eb_only_threshold leave the EB-only choice to it.
+  // -fast_build_bvh, -rebuild_bvh, -rt_prune, -rt_eb, -max_reg and -bit_count
+  // configure OptiX builds and are logged only.
+  const bool auto_tune = fl.getb("auto_tune", false);
+  if (auto_tune || fl.getb("auto_tune_eb_only_threshold", false)) opt.eb_only_threshold = 0;
+  const long long max_hit = fl.geti("max_hit", 256);
+  if (fl.v.count("max_hit") && !auto_tune && !fl.getb("auto_tune_max_hit", false))
+    opt.lbvh_budget = budget_from_max_hit(max_hit);
 
   hd::Json stats = hd::Json::Object();
   int dev = opt.device;
@@ -247,7 +268,7 @@ int main(int argc, char** argv) {
   input["SerializationPrefix"] = fl.get("serialize", "");
   input["Limit"] = limit;
   input["NumDims"] = dims;
-  input["Type"] = "Float";
+  input["Type"] = is_double ? "Double" : "Float";
 
   // Per-file and combined point statistics on the GPU (the reference's
   // write_points_stats).
@@ -374,6 +395,11 @@ int main(int argc, char** argv) {
     run_json["SampleRate"] = o.sample_rate;
     run_json["NumPointsPerCell"] = o.n_points_cell;
     run_json["EBOnlyThreshold"] = o.eb_only_threshold;
+    run_json["MaxHit"] = max_hit;
+    run_json["LBVHBudget"] = (unsigned long long) o.lbvh_budget;  // 0: tuned table
+    run_json["AutoTune"] = auto_tune;
+    run_json["FastBuildBVH"] = fl.getb("fast_build_bvh", false);
+    run_json["RebuildBVH"] = fl.getb("rebuild_bvh", false);
     run_json["Undirected"] = undirected;
     run_json["Repeats"] = repeats;
     run_json["AvgTime"] = total / repeat;
@@ -452,23 +478,28 @@ int main(int argc, char** argv) {
     const auto rates = split_doubles(fl.get("sample_rate_list", "0.01"));
     const auto thresholds = split_doubles(fl.get("eb_only_threshold_list", "0"));
     const auto cells = split_doubles(fl.get("n_points_cell_list", "8"));
+    const auto hits = split_doubles(fl.get("max_hit_list", "256"));
     for (double sr : rates)
       for (double th : thresholds)
-        for (double np : cells) {
-          hd_options o = opt;
-          o.sample_rate = sr;
-          o.eb_only_threshold = (uint32_t) th;
-          o.n_points_cell = (uint32_t) np;
-          hd::Json st = stats;
-          double dist = 0.0;
-          if (run(o, st["Running"], &dist)) return 1;
-          st["HDResult"] = dist;
-          if (!json_path.empty()) {
-            std::ostringstream name;
-            name << json_path << "_sr" << sr << "_th" << th << "_np" << np << ".json";
-            std::ofstream(name.str()) << st.dump(4);
+        for (double np : cells)
+          for (double mh : hits) {
+            hd_options o = opt;
+            o.sample_rate = sr;
+            o.eb_only_threshold = (uint32_t) th;
+            o.n_points_cell = (uint32_t) np;
+            o.lbvh_budget = budget_from_max_hit((long long) mh);
+            hd::Json st = stats;
+            double dist = 0.0;
+            if (run(o, st["Running"], &dist)) return 1;
+            st["Running"]["MaxHit"] = (long long) mh;
+            st["HDResult"] = dist;
+            if (!json_path.empty()) {
+              std::ostringstream name;
+              name << json_path << "_sr" << sr << "_th" << th << "_np" << np << "_mh" << mh
+                   << ".json";
+              std::ofstream(name.str()) << st.dump(4);
+            }
           }
-        }
     return 0;
   }
 

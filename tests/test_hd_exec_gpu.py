@@ -83,7 +83,9 @@ def test_cpu_execution_is_double(exe, double_inputs, undirected, tmp_path):
     want = h_und if undirected else h_ab
     line = [ln for ln in r.stdout.splitlines() if ln.startswith("HausdorffDistance")][0]
     assert float(line.split()[-1]) == want
-    assert json.loads(out.read_text())["HDResult"] == want
+    st = json.loads(out.read_text())
+    assert st["HDResult"] == want
+    assert st["Input"]["Type"] == "Double"
 
 
 @pytest.mark.parametrize("fmt", ["off", "ply"])
@@ -173,6 +175,46 @@ def test_hd_exec_image(exe, image_inputs, variant, tmp_path):
                         "-json", str(out)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert bits(json.loads(out.read_text())["HDResult"]) == bits(h_und)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("max_hit", [0, 1, 40])
+def test_hd_exec_max_hit(exe, max_hit, tmp_path):
+    """-max_hit caps an LBVH packet's visits before its open queries go to the
+    deferred pass (0: no cap, as in the reference; 1: every packet deferred):
+    the distance stays the oracle's, and the JSON logs the cap."""
+    import hd_oracle
+    rng = np.random.default_rng(31)
+    c = rng.random((12, 3))
+    a = (c[rng.integers(0, 12, 20000)] + rng.normal(0, 0.01, (20000, 3))).astype(np.float32)
+    b = (c[rng.integers(0, 12, 18000)] + rng.normal(0, 0.01, (18000, 3)) + [0.02, 0, 0]).astype(np.float32)
+    paths = []
+    for name, pts in (("a", a), ("b", b)):
+        p = str(tmp_path / f"{name}.bin")
+        with open(p, "wb") as f:
+            f.write(np.uint64(len(pts)).tobytes() + pts.tobytes())
+        paths.append(p)
+    h = max(np.sqrt(np.float32(hd_oracle.exact(a, b, 32)[0])),
+            np.sqrt(np.float32(hd_oracle.exact(b, a, 32)[0])))
+    out = tmp_path / "run.json"
+    r = subprocess.run([exe, "-input1", paths[0], "-input2", paths[1], "-input_type", "bin",
+                        "-n_dims", "3", "-variant", "rt", "-undirected", "-repeat", "2",
+                        "-max_hit", str(max_hit), "-json", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    st = json.loads(out.read_text())
+    assert bits(st["HDResult"]) == bits(h)
+    assert st["Running"]["MaxHit"] == max_hit
+    assert st["Running"]["LBVHBudget"] == (max_hit or 0xFFFFFFFF)
+    # The sweep form: one JSON file per -max_hit_list entry.
+    prefix = str(tmp_path / "sweep")
+    r = subprocess.run([exe, "-input1", paths[0], "-input2", paths[1], "-input_type", "bin",
+                        "-n_dims", "3", "-variant", "rt", "-undirected", "-repeat", "1",
+                        "-vary_params", "-max_hit_list", f"{max_hit},7", "-json", prefix],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for mh in (max_hit, 7):
+        sw = json.loads(open(f"{prefix}_sr0.01_th0_np8_mh{mh}.json").read())
+        assert bits(sw["HDResult"]) == bits(h) and sw["Running"]["MaxHit"] == mh
 
 
 @pytest.mark.gpu
