@@ -19,6 +19,26 @@ them with the shapes, sizes and value distributions of the five workloads:
               N(0, 0.02) along the normal; B = A rotated 1 degree about z
               around the centroid, then 0.1% replaced by U[0,100]^3.
 
+The reference's own synthetic experiments (expr/for_the_paper/data_gen.sh)
+draw single point sets from the Spider generator of Katiyar et al.
+(SpiderWeb, SIGSPATIAL 2020), one file per seed, and pair the seeds; ``spider``
+restates its point distributions in the unit cube:
+
+  uniform     every coordinate U[0,1).
+  gaussian    every coordinate N(0.5, 0.1); points with a coordinate outside
+              [0,1] are drawn again.
+  bit         every coordinate sum_{i=1..digits} Bernoulli(prob) * 2^-i (the
+              experiments use prob 0.2, digits 10): a skewed lattice with heavy
+              exact duplicates.
+  diagonal    with probability `prob` a point of the diagonal (c, c, ...),
+              else c plus alternating +-N(0, buffer/5)/sqrt(2) per coordinate
+              (buffer 0.5), points outside the cube drawn again.
+  sierpinski  the chaos game on the triangle (0,0), (1,0), (1/2, sqrt(3)/2):
+              the first three points are its corners, each next point the
+              midpoint of the previous one and a corner chosen with
+              probabilities 2/5, 2/5, 1/5.  Two-dimensional whatever the
+              requested dimension, as in the generator.
+
 Every generator draws from numpy's PCG64 with the given seed and returns
 C-contiguous float32 arrays of shape (n, n_dims).  ``write_bin``/``read_bin``
 use the reference's point-cache layout (src/loaders/loader.h:150-185): a
@@ -149,6 +169,50 @@ WORKLOADS = {
     "unit64": unit64,
     "planes3d": planes3d,
 }
+
+
+SPIDER = ("uniform", "gaussian", "bit", "diagonal", "sierpinski")
+
+
+def spider(dist: str, n: int, dims: int = 3, seed: int = 1, prob: float = 0.2,
+           digits: int = 10, buffer: float = 0.5) -> np.ndarray:
+    """One Spider point set (see the module docstring), float32 (n, dims);
+    (n, 2) for sierpinski."""
+    rng = _rng(seed)
+    if dist == "uniform":
+        out = rng.random((n, dims))
+    elif dist in ("gaussian", "diagonal"):
+        out = np.empty((0, dims))
+        while len(out) < n:
+            m = n - len(out) + 64
+            if dist == "gaussian":
+                p = rng.normal(0.5, 0.1, (m, dims))
+            else:
+                c = rng.random((m, 1))
+                on = rng.random(m) < prob
+                d = rng.normal(0.0, buffer / 5.0, (m, 1)) / np.sqrt(2.0)
+                sign = 1.0 - 2.0 * (np.arange(dims) % 2)
+                p = np.where(on[:, None], np.repeat(c, dims, 1), c + sign * d)
+            p = p[np.all((p >= 0.0) & (p <= 1.0), axis=1)]
+            out = np.concatenate([out, p])[:n]
+    elif dist == "bit":
+        weights = 0.5 ** np.arange(1, digits + 1)
+        out = np.zeros((n, dims))
+        for w in weights:
+            out += (rng.random((n, dims)) < prob) * w
+    elif dist == "sierpinski":
+        corners = np.array([[0.0, 0.0], [1.0, 0.0], [0.5, np.sqrt(3.0) / 2.0]])
+        pick = np.minimum(rng.integers(0, 5, n) // 2, 2)  # 2/5, 2/5, 1/5
+        # Unrolled recurrence p_i = (p_{i-1} + v_i) / 2: p_i is the sum of
+        # v_{i-k} / 2^(k+1); 60 terms exhaust double precision.
+        v = corners[pick]
+        out = np.zeros((n, 2))
+        for k in range(60):
+            out[k:] += v[: n - k] * 0.5 ** (k + 1)
+        out[: min(n, 3)] = corners[: min(n, 3)]
+    else:
+        raise ValueError(f"unknown Spider distribution {dist!r}")
+    return np.ascontiguousarray(out, np.float32)
 
 
 def write_bin(path: str, pts: np.ndarray) -> None:
