@@ -73,6 +73,13 @@ def cases():
     add("offset_large_3d", rng.random((800, 3)) * 10 + 1.0e4,
         rng.random((700, 3)) * 10 + 1.0e4 - 3.0, 3, 0)
     add("negative_2d", -rng.random((600, 2)) * 5, -rng.random((900, 2)) * 5 + 0.25, 2, 0)
+    # The Spider distributions of the reference's synthetic experiments
+    # (expr/for_the_paper/data_gen.sh), seed 1 against seed 2.
+    for dist, n in (("uniform", 4000), ("gaussian", 4000), ("bit", 5000), ("diagonal", 4000),
+                    ("sierpinski", 5000)):
+        dims = 2 if dist == "sierpinski" else 3
+        add(f"spider_{dist}_{dims}d", synth.spider(dist, n, dims, seed=1),
+            synth.spider(dist, n, dims, seed=2), dims, 0)
     return out
 
 
