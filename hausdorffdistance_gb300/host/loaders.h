@@ -580,7 +580,10 @@ inline PointSet LoadImage(const std::string& path, int dims, size_t limit, bool 
   for (int d = dims; d < v.ndim; ++d)
     if (v.size[d] != 1) load_fail("image has more than " + std::to_string(dims) + " dimensions: " + path);
   uint64_t count = 1;
-  for (int d = 0; d < v.ndim; ++d) count *= v.size[d];
+  for (int d = 0; d < v.ndim; ++d) {
+    if (v.size[d] > (uint64_t(1) << 40) / count) load_fail("image too large: " + path);
+    count *= v.size[d];
+  }
   const size_t eb = img::elem_bytes(v.elem);
   std::ifstream ifs(v.data_path, std::ios::binary);
   if (!ifs) load_fail("cannot open " + v.data_path);

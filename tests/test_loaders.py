@@ -201,3 +201,11 @@ def test_image_errors(probe, tmp_path):
     short.write_bytes(short.read_bytes()[:-5])
     with pytest.raises(RuntimeError, match="truncated"):
         run(probe, short, "image", 3)
+
+
+def test_metaimage_oversized_header(probe, tmp_path):
+    p = tmp_path / "huge.mha"
+    p.write_bytes(b"NDims = 3\nDimSize = 100000 100000 100000\nElementType = MET_UCHAR\n"
+                  b"ElementDataFile = LOCAL\n")
+    with pytest.raises(RuntimeError, match="too large"):
+        run(probe, p, "image", 3)
