@@ -42,7 +42,11 @@ inline void load_fail(const std::string& msg) { throw std::runtime_error(msg); }
 // LINESTRING, MULTILINESTRING, POLYGON and MULTIPOLYGON contribute their
 // vertices (polygons only their outer ring); GEOMETRYCOLLECTION lines are
 // skipped; any other geometry is an error.  The first `dims` coordinates of
-// each vertex are used.
+// each vertex are used.  `limit` acts as in the reference, which tests it
+// after each vertex it adds and then leaves only the innermost loop: a ring
+// or linestring stops once the count reaches the limit, but every later one
+// (the next polygon of a MULTIPOLYGON, the next line) still adds its first
+// vertex; a POINT line that ends at or beyond the limit ends the file.
 inline PointSet LoadWKT(const std::string& path, int dims, size_t limit, bool keep64 = false) {
   std::ifstream ifs(path);
   if (!ifs) load_fail("cannot open " + path);
@@ -51,7 +55,7 @@ inline PointSet LoadWKT(const std::string& path, int dims, size_t limit, bool ke
   ps.keep64 = keep64;
   std::string line;
   auto starts = [](const std::string& s, const char* p) { return s.rfind(p, 0) == 0; };
-  while (std::getline(ifs, line) && ps.size() < limit) {
+  while (std::getline(ifs, line)) {
     size_t b = line.find_first_not_of(" \t\r");
     if (b == std::string::npos) continue;
     line = line.substr(b);
@@ -75,13 +79,16 @@ inline PointSet LoadWKT(const std::string& path, int dims, size_t limit, bool ke
       load_fail("unsupported WKT geometry in " + path + ": " + line.substr(0, 40));
     }
     int depth = 0;
-    int ring_index = 0;  // index of the ring within its enclosing group
+    int ring_index = 0;    // index of the ring within its enclosing group
+    bool ring_full = false;  // this ring reached the limit: skip its rest
     std::vector<double> tuple;
     auto flush_tuple = [&]() {
       if (tuple.empty()) return;
       if ((int) tuple.size() < dims) load_fail("WKT vertex with too few coordinates in " + path);
-      if (ps.size() < limit)
+      if (!ring_full) {
         for (int k = 0; k < dims; ++k) ps.push(tuple[k]);
+        ring_full = ps.size() >= limit;
+      }
       tuple.clear();
     };
     const char* p = line.c_str();
@@ -90,6 +97,7 @@ inline PointSet LoadWKT(const std::string& path, int dims, size_t limit, bool ke
       if (ch == '(') {
         ++depth;
         if (depth == want_depth - 1) ring_index = 0;
+        if (depth == want_depth) ring_full = false;
         ++p;
       } else if (ch == ')') {
         if (depth == want_depth) {
@@ -117,6 +125,7 @@ inline PointSet LoadWKT(const std::string& path, int dims, size_t limit, bool ke
         ++p;
       }
     }
+    if (starts(line, "POINT") && ps.size() >= limit) break;
   }
   return ps;
 }

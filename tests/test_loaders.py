@@ -44,7 +44,25 @@ def test_wkt_geometries(probe, tmp_path):
             [10, 10], [11, 10], [10, 11], [10, 10], [20, 20], [21, 20], [20, 21], [20, 20],
             [7, 7], [8, 8], [9, 9], [-10, 3.5]]
     assert np.array_equal(got, np.array(want, float))
-    assert len(run(probe, p, "wkt", 2, limit=5)) == 5
+    # -limit as the reference applies it (src/loaders/loader.h:38-96): the
+    # count is tested after each vertex and only the innermost loop is left,
+    # so each later ring or linestring still adds its first vertex.
+    lim5 = [[1, 2], [0, 0], [1, 1], [2, 0.5], [0, 0], [10, 10], [20, 20], [7, 7], [9, 9]]
+    assert np.array_equal(run(probe, p, "wkt", 2, limit=5), np.array(lim5, float))
+
+
+def test_wkt_limit_stops_at_a_point_line(probe, tmp_path):
+    """A POINT line that reaches the limit ends the file; polygons before it
+    go on adding one vertex per ring."""
+    p = tmp_path / "l.wkt"
+    p.write_text("POLYGON ((0 0, 1 0, 1 1, 0 0))\n"
+                 "POLYGON ((5 5, 6 5, 6 6, 5 5))\n"
+                 "POINT (9 9)\n"
+                 "POINT (8 8)\n"
+                 "LINESTRING (3 3, 4 4)\n")
+    assert np.array_equal(run(probe, p, "wkt", 2, limit=2), [[0, 0], [1, 0], [5, 5], [9, 9]])
+    assert np.array_equal(run(probe, p, "wkt", 2, limit=7),
+                          [[0, 0], [1, 0], [1, 1], [0, 0], [5, 5], [6, 5], [6, 6]] + [[9, 9]])
 
 
 def test_off(probe, tmp_path):
