@@ -173,6 +173,10 @@ inline PointSet LoadOFF(const std::string& path, int dims, size_t limit, bool ke
 // PLY (src/loaders/ply_loader.h:37-101): the x, y (, z) properties of the
 // "vertex" element, ASCII or binary (either byte order), read as doubles,
 // shifted so that the minimum of every axis is 0, then stored as float.
+// `limit` keeps the first vertices.  (The reference's read callback returns
+// 0 once its countdown reaches the limit, which aborts rply's read, so with a
+// limit at or below the vertex count it loads no points at all and its driver
+// stops on the empty set.)
 inline PointSet LoadPLY(const std::string& path, int dims, size_t limit, bool keep64 = false) {
   std::ifstream ifs(path, std::ios::binary);
   if (!ifs) load_fail("cannot open " + path);
