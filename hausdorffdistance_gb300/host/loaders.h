@@ -702,8 +702,13 @@ inline void TranslatePoints(PointSet& ps, int dim, double ratio) {
     lo = std::min(lo, ps.xyz[i * ps.dims + dim]);
     hi = std::max(hi, ps.xyz[i * ps.dims + dim]);
   }
+  // The reference adds the double product to the float coordinate
+  // (`p += extent * ratio`): the sum is formed in double and rounded once.
   const double shift = (double) (hi - lo) * ratio;
-  for (size_t i = 0; i < n; ++i) ps.xyz[i * ps.dims + dim] += (float) shift;
+  for (size_t i = 0; i < n; ++i) {
+    float& v = ps.xyz[i * ps.dims + dim];
+    v = (float) ((double) v + shift);
+  }
 }
 
 }  // namespace hd

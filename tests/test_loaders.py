@@ -227,3 +227,18 @@ def test_metaimage_oversized_header(probe, tmp_path):
                   b"ElementDataFile = LOCAL\n")
     with pytest.raises(RuntimeError, match="too large"):
         run(probe, p, "image", 3)
+
+
+def test_translate_rounds_once_like_the_reference(probe, tmp_path):
+    """-translate adds extent * ratio (a double) to each float coordinate and
+    rounds the sum once, as the reference's `p += extent * ratio` does.  With
+    extent 1 and ratio 2^-24 + 2^-49, x = 1 lands just above the halfway point
+    to the next float: rounding the shift to float first would give 1.0."""
+    pts = np.array([[0, 0], [1, 0]], np.float32)
+    p = tmp_path / "t.bin"
+    with open(p, "wb") as f:
+        f.write(np.uint64(2).tobytes() + pts.tobytes())
+    ratio = 2.0 ** -24 + 2.0 ** -49
+    got = run(probe, p, "bin", 2, translate=repr(ratio))
+    assert np.float32(got[1, 0]) == np.float32(1.0 + 2.0 ** -23)
+    assert np.float32(got[0, 0]) == np.float32(ratio)
