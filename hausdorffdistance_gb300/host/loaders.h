@@ -30,8 +30,11 @@ struct PointSet {
   bool keep64 = false;        // also keep the coordinates as doubles
   std::vector<double> xyz64;  // n * dims when keep64
   size_t size() const { return dims ? xyz.size() / dims : 0; }
-  void push(double v) {
-    xyz.push_back((float) v);
+  void push(double v) { push(v, (float) v); }
+  // A coordinate parsed twice from text: f straight to float (correctly
+  // rounded, as the reference's float loaders read it), v to double.
+  void push(double v, float f) {
+    xyz.push_back(f);
     if (keep64) xyz64.push_back(v);
   }
 };
@@ -82,14 +85,16 @@ inline PointSet LoadWKT(const std::string& path, int dims, size_t limit, bool ke
     int ring_index = 0;    // index of the ring within its enclosing group
     bool ring_full = false;  // this ring reached the limit: skip its rest
     std::vector<double> tuple;
+    std::vector<float> tuple32;
     auto flush_tuple = [&]() {
       if (tuple.empty()) return;
       if ((int) tuple.size() < dims) load_fail("WKT vertex with too few coordinates in " + path);
       if (!ring_full) {
-        for (int k = 0; k < dims; ++k) ps.push(tuple[k]);
+        for (int k = 0; k < dims; ++k) ps.push(tuple[k], tuple32[k]);
         ring_full = ps.size() >= limit;
       }
       tuple.clear();
+      tuple32.clear();
     };
     const char* p = line.c_str();
     while (*p) {
@@ -104,6 +109,7 @@ inline PointSet LoadWKT(const std::string& path, int dims, size_t limit, bool ke
           const bool take = !outer_only || ring_index == 0;
           if (take) flush_tuple();
           tuple.clear();
+          tuple32.clear();
           ++ring_index;
         }
         --depth;
@@ -111,15 +117,21 @@ inline PointSet LoadWKT(const std::string& path, int dims, size_t limit, bool ke
       } else if (ch == ',') {
         if (depth == want_depth && (!outer_only || ring_index == 0)) flush_tuple();
         tuple.clear();
+        tuple32.clear();
         ++p;
       } else if (std::isdigit((unsigned char) ch) || ch == '-' || ch == '+' || ch == '.') {
+        // boost.geometry's WKT reader (the reference's) converts each token
+        // straight to the coordinate type: float directly, not via double.
         char* end = nullptr;
         const double v = std::strtod(p, &end);
         if (end == p) {
           ++p;
           continue;
         }
-        if (depth == want_depth) tuple.push_back(v);
+        if (depth == want_depth) {
+          tuple.push_back(v);
+          tuple32.push_back(std::strtof(p, nullptr));
+        }
         p = end;
       } else {
         ++p;

@@ -242,3 +242,14 @@ def test_translate_rounds_once_like_the_reference(probe, tmp_path):
     got = run(probe, p, "bin", 2, translate=repr(ratio))
     assert np.float32(got[1, 0]) == np.float32(1.0 + 2.0 ** -23)
     assert np.float32(got[0, 0]) == np.float32(ratio)
+
+
+def test_wkt_parses_floats_directly(probe, tmp_path):
+    """A coordinate just above the midpoint of two floats whose nearest double
+    is the midpoint itself: parsed straight to float (as boost.geometry's
+    reader does for float points) it rounds up; via double it would tie down."""
+    p = tmp_path / "mid.wkt"
+    p.write_text("POINT (1.00000005960464477539062500000000001 2)\n")
+    assert float("1.00000005960464477539062500000000001") == 1.0 + 2.0 ** -24
+    got = run(probe, p, "wkt", 2)
+    assert np.float32(got[0, 0]) == np.float32(1.0 + 2.0 ** -23)
