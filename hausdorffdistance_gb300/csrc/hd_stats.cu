@@ -10,8 +10,10 @@
 // on order-preserving integers), one counter per grid cell (atomic
 // increments into a dense array), the largest count and the number of
 // non-empty cells, then a histogram of the per-cell counts.  The host turns
-// that histogram into the Gini index, the median and the percentile table:
-// the counts' sorted order is the histogram's order, so nothing is sorted.
+// that histogram into the Gini index, the median and the percentile table
+// (the counts' sorted order is the histogram's order, so nothing is sorted);
+// the grid's shape and the percentile table follow the reference's own
+// arithmetic and its HdrHistogram output (hd_stats_host.h).
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -20,6 +22,7 @@
 
 #include "hd_common.cuh"
 #include "hd_internal.h"
+#include "hd_stats_host.h"
 
 namespace hdg {
 namespace {
@@ -104,35 +107,6 @@ __global__ void k_stats_hist(const uint32_t* __restrict__ counts, uint64_t cells
   }
 }
 
-// Percentile table in the shape HdrHistogram's percentile iteration prints
-// (ticks_per_half_distance ticks in each half of the remaining distance to
-// 100 %), from the histogram of per-cell counts: the value at each
-// percentile, the percentile as a fraction, and the cumulative count there.
-void percentile_table(const std::vector<uint32_t>& hist, uint64_t total, int ticks,
-                      hd_point_stats* out) {
-  out->n_hist = 0;
-  if (total == 0) return;
-  std::vector<uint64_t> cum(hist.size());
-  uint64_t run = 0;
-  for (size_t v = 0; v < hist.size(); ++v) cum[v] = run += hist[v];
-  double p = 0.0;
-  for (int row = 0; row < HD_STATS_HIST_ROWS; ++row) {
-    // The smallest value whose cumulative count reaches p of the total.
-    const uint64_t need = std::max<uint64_t>(1, (uint64_t) std::ceil(p / 100.0 * (double) total));
-    const size_t v = (size_t) (std::lower_bound(cum.begin(), cum.end(), need) - cum.begin());
-    out->hist_value[row] = (double) v;
-    out->hist_percentile[row] = (double) cum[v] / (double) total;
-    out->hist_count[row] = cum[v];
-    out->n_hist = (uint32_t) row + 1;
-    if (cum[v] >= total) break;
-    // Next percentile: the distance to 100 % halves every `ticks` rows.
-    p = 100.0 * (double) cum[v] / (double) total;
-    const double half = std::pow(2.0, std::floor(std::log2(100.0 / std::max(100.0 - p, 1e-12))) + 1);
-    p += 100.0 / (ticks * half);
-    p = std::min(p, 100.0);
-  }
-}
-
 }  // namespace
 }  // namespace hdg
 
@@ -189,36 +163,29 @@ extern "C" hd_status hd_compute_stats(hd_ctx* c, const float* P, uint64_t n, int
           cudaSuccess ||
       (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
     return cuda_fail(*c, e, "stats box");
-  // The reference's resolution rule on the non-empty box (a zero extent
-  // becomes 1e-5): s = (volume * n_points_cell / n)^(1/d), ceil(extent / s)
-  // cells per axis.
+  // The reference's grid shape on its non-empty box, in its arithmetic
+  // (hd_stats_host.h).
+  float lo32[3], hi32[3];
+  for (int k = 0; k < n_dims; ++k) {
+    lo32[k] = ord2f(ord[k]);
+    hi32[k] = ord2f(ord[4 + k]);
+  }
+  stats::GridShape shape;
+  if (!stats::grid_shape(lo32, hi32, n_dims, n, n_points_cell, kStatsMaxCells, &shape))
+    return fail(*c, HD_ERR_UNSUPPORTED, "statistics grid too large");
   StatsGrid grid{};
-  double volume = 1.0, ext[3] = {0, 0, 0};
   for (int k = 0; k < n_dims; ++k) {
-    const double lo = ord2f(ord[k]), hi = ord2f(ord[4 + k]);
-    ext[k] = hi > lo ? hi - lo : 1e-5;
-    out->lower[k] = lo;
-    out->upper[k] = lo + ext[k];
-    volume *= ext[k];
+    out->lower[k] = shape.lower[k];
+    out->upper[k] = shape.upper[k];
+    out->grid_size[k] = shape.size[k];
+    grid.size[k] = shape.size[k];
+    grid.lo[k] = shape.lower[k];
+    grid.scale[k] = (float) ((double) shape.size[k] / (double) shape.extent[k]);
   }
-  out->density = (double) n / volume;
-  const double side = std::pow(volume * n_points_cell / (double) n, 1.0 / n_dims);
-  uint64_t cells = 1;
-  double diag2 = 0.0;
-  for (int k = 0; k < n_dims; ++k) {
-    const double sz = std::max(1.0, std::ceil(ext[k] / side));
-    if (sz > 4294967295.0) return fail(*c, HD_ERR_UNSUPPORTED, "statistics grid too large");
-    grid.size[k] = (uint32_t) sz;
-    grid.lo[k] = (float) out->lower[k];
-    grid.scale[k] = (float) (sz / ext[k]);
-    out->grid_size[k] = grid.size[k];
-    cells *= grid.size[k];
-    const double unit = ext[k] / sz;
-    diag2 += unit * unit;
-    if (cells > kStatsMaxCells) return fail(*c, HD_ERR_UNSUPPORTED, "statistics grid too large");
-  }
+  const uint64_t cells = shape.total_cells;
+  out->density = shape.density;
   out->total_cells = cells;
-  out->cell_diagonal = std::sqrt(diag2);
+  out->cell_diagonal = shape.cell_diagonal;
   void* cv;
   if ((s = ensure(*c, kBufKeys, cells * 4, &cv)) != HD_OK) return s;
   uint32_t* counts = (uint32_t*) cv;
@@ -274,6 +241,13 @@ extern "C" hd_status hd_compute_stats(hd_ctx* c, const float* P, uint64_t n, int
   }
   out->gini_index = (m > 0 && total > 0) ? weighted / (m * total) : 0.0;
   out->median_points = median;
-  percentile_table(hist, out->nonempty_cells, 3, out);
+  // The percentile table as the reference's HdrHistogram prints it.
+  const auto rows = stats::hdr_percentiles(hist.data(), nbins, out->nonempty_cells, 3);
+  out->n_hist = (uint32_t) std::min<size_t>(rows.size(), HD_STATS_HIST_ROWS);
+  for (uint32_t r = 0; r < out->n_hist; ++r) {
+    out->hist_value[r] = rows[r].value;
+    out->hist_percentile[r] = rows[r].percentile;
+    out->hist_count[r] = rows[r].count;
+  }
   return HD_OK;
 }

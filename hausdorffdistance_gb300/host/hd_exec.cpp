@@ -301,9 +301,14 @@ int main(int argc, char** argv) {
       grid["MedianPointsPerCell"] = (unsigned long long) ps.median_points;
       hd::Json hist = hd::Json::Array();
       for (uint32_t r = 0; r < ps.n_hist; ++r) {
+        // The reference parses HdrHistogram's printed table back
+        // (running_stats.h:106-140): the percentile carries the six
+        // decimals of "%f".
+        char pct[64];
+        std::snprintf(pct, sizeof(pct), "%f", ps.hist_percentile[r]);
         hd::Json row = hd::Json::Object();
         row["value"] = ps.hist_value[r];
-        row["percentile"] = ps.hist_percentile[r];
+        row["percentile"] = std::strtod(pct, nullptr);
         row["count"] = (unsigned long long) ps.hist_count[r];
         hist.push_back(row);
       }

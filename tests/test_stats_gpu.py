@@ -17,28 +17,58 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def expected(P, npc):
+    """The reference's statistics in its arithmetic (float box and extents, a
+    flat axis widened by 1e-5 in float, cell side sqrt/cbrt in double, float
+    density and cell diagonal), cells counted as the library's kernel
+    assigns them (floor((p - lower) * float(size / extent)))."""
     n, d = P.shape
-    lo = P.min(0).astype(np.float64)
-    hi = P.max(0).astype(np.float64)
-    ext = np.where(hi > lo, hi - lo, 1e-5)
-    vol = float(np.prod(ext))
-    side = (vol * npc / n) ** (1.0 / d)
-    size = np.maximum(1, np.ceil(ext / side)).astype(np.int64)
-    scale = (size / ext).astype(np.float32)
-    lo32 = lo.astype(np.float32)
+    lo = P.min(0)
+    hi = P.max(0)
+    hi = np.where(hi - lo == 0, (lo.astype(np.float64) + 1e-5).astype(np.float32), hi)
+    hi = np.where(hi - lo == 0, np.nextafter(lo, np.float32(np.inf)), hi)
+    ext = hi - lo
+    vol, vol32 = 1.0, np.float32(1)
+    for e in ext:
+        vol *= float(e)
+        vol32 = np.float32(vol32 * e)
+    q = vol * npc / n
+    side = np.sqrt(q) if d == 2 else np.cbrt(q)
+    size = np.array([max(1, int(np.ceil(float(e) / side))) for e in ext], np.int64)
+    scale = (size / ext.astype(np.float64)).astype(np.float32)
     cells = np.zeros(n, np.int64)
     for k in reversed(range(d)):
-        c = np.floor((P[:, k] - lo32[k]) * scale[k])
+        c = np.floor((P[:, k] - lo[k]) * scale[k])
         c = np.clip(c, 0, size[k] - 1).astype(np.int64)
         cells = cells * size[k] + c
     counts = np.bincount(cells, minlength=int(np.prod(size)))
     ne = np.sort(counts[counts > 0]).astype(np.float64)
     m = len(ne)
     gini = float(((2 * np.arange(m) - m + 1) * ne).sum() / (m * ne.sum()))
-    return {"lower": lo, "upper": lo + ext, "density": n / vol, "size": size,
+    sum2 = np.float32(0)
+    for e, z in zip(ext, size):
+        u = np.float32(e / np.float32(z))
+        sum2 = np.float32(sum2 + np.float32(u * u))
+    # HdrHistogram (hdr_init(1, non-empty cells, 3)) records only values below
+    # the smallest power-of-two multiple of 2048 beyond the non-empty count.
+    untrackable = 2048
+    while untrackable <= max(m, 2):
+        untrackable <<= 1
+    rec = ne[ne < untrackable].astype(np.int64)
+    return {"lower": lo.astype(np.float64), "upper": hi.astype(np.float64),
+            "hdr_first": hdr_highest_equivalent(int(rec[0])),
+            "hdr_last": hdr_highest_equivalent(int(rec[-1])), "hdr_total": len(rec),
+            "density": float(np.float32(np.float32(n) / vol32)), "size": size,
             "total": int(np.prod(size)), "nonempty": m, "max": int(ne[-1]),
-            "median": int(ne[m // 2]), "gini": gini,
-            "diag": float(np.sqrt(((ext / size) ** 2).sum()))}
+            "median": int(ne[m // 2]), "gini": gini, "diag": float(np.sqrt(sum2))}
+
+
+def hdr_highest_equivalent(v):
+    """HdrHistogram with 3 significant figures: values from 2048 on share
+    buckets of 2^b values and are reported as the bucket's highest."""
+    if v < 2048:
+        return v
+    b = v.bit_length() - 11
+    return ((v >> b) << b) + (1 << b) - 1
 
 
 @pytest.mark.parametrize("name", ["uniform2d", "clusters3d", "planes3d"])
@@ -53,21 +83,25 @@ def test_point_stats_match_numpy(engine, name):
     want = expected(P, 10)
     d = P.shape[1]
     assert np.array_equal(np.array(st.lower[:d]), want["lower"])
-    assert np.allclose(np.array(st.upper[:d]), want["upper"], rtol=0, atol=1e-12)
-    assert st.density == pytest.approx(want["density"], rel=1e-12)
+    assert np.array_equal(np.array(st.upper[:d]), want["upper"])
+    assert st.density == want["density"]
     assert list(st.grid_size[:d]) == list(want["size"])
     assert st.total_cells == want["total"]
     assert st.nonempty_cells == want["nonempty"]
     assert st.max_points == want["max"] and st.median_points == want["median"]
     assert st.gini_index == pytest.approx(want["gini"], rel=1e-9, abs=1e-12)
-    assert st.cell_diagonal == pytest.approx(want["diag"], rel=1e-12)
-    # Percentile table: ascending values and percentiles, ending at the
-    # largest count with every non-empty cell counted.
+    assert st.cell_diagonal == want["diag"]
+    # Percentile table (HdrHistogram's iteration; its exact rows are pinned to
+    # the reference's logs in test_stats_host.py): values ascending, possibly
+    # repeated, at strictly rising targets from 0, ending at the largest
+    # recorded count (in its HdrHistogram bucket) with every recorded cell
+    # counted.
     k = st.n_hist
     vals = np.array(st.hist_value[:k])
     pct = np.array(st.hist_percentile[:k])
     assert k >= 2 and np.all(np.diff(vals) >= 0) and np.all(np.diff(pct) > 0)
-    assert vals[-1] == want["max"] and st.hist_count[k - 1] == want["nonempty"]
+    assert pct[0] == 0.0 and vals[0] == want["hdr_first"]
+    assert vals[-1] == want["hdr_last"] and st.hist_count[k - 1] == want["hdr_total"]
     assert pct[-1] == 1.0
 
 
