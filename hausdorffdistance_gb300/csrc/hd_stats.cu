@@ -56,8 +56,11 @@ __global__ void k_stats_mbr(const float* __restrict__ P, uint64_t n, uint32_t* _
   }
 }
 
+// A point's cell per axis as the reference computes it
+// (UniformGrid::CalculateCellPos, src/index/uniform_grid.h:138-159):
+// (p - lo) / extent * size in float, clamped to [0, size - 1], truncated.
 struct StatsGrid {
-  float lo[3], scale[3];  // cell = floor((p - lo) * scale), clamped
+  float lo[3], extent[3];
   uint32_t size[3];
 };
 
@@ -69,9 +72,10 @@ __global__ void k_stats_count(const float* __restrict__ P, uint64_t n, StatsGrid
     uint64_t cell = 0;
 #pragma unroll
     for (int k = D - 1; k >= 0; --k) {
-      float c = floorf((P[i * D + k] - g.lo[k]) * g.scale[k]);
-      c = fminf(fmaxf(c, 0.0f), (float) (g.size[k] - 1));
-      cell = cell * g.size[k] + (uint64_t) c;
+      const float norm = __fdiv_rn(__fsub_rn(P[i * D + k], g.lo[k]), g.extent[k]);
+      float c = __fmul_rn(norm, (float) g.size[k]);
+      c = fminf(fmaxf(c, 0.0f), __fsub_rn((float) g.size[k], 1.0f));
+      cell = cell * g.size[k] + (uint32_t) c;
     }
     atomicAdd(&counts[cell], 1u);
   }
@@ -180,7 +184,7 @@ extern "C" hd_status hd_compute_stats(hd_ctx* c, const float* P, uint64_t n, int
     out->grid_size[k] = shape.size[k];
     grid.size[k] = shape.size[k];
     grid.lo[k] = shape.lower[k];
-    grid.scale[k] = (float) ((double) shape.size[k] / (double) shape.extent[k]);
+    grid.extent[k] = shape.extent[k];
   }
   const uint64_t cells = shape.total_cells;
   out->density = shape.density;

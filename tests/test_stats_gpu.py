@@ -19,8 +19,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def expected(P, npc):
     """The reference's statistics in its arithmetic (float box and extents, a
     flat axis widened by 1e-5 in float, cell side sqrt/cbrt in double, float
-    density and cell diagonal), cells counted as the library's kernel
-    assigns them (floor((p - lower) * float(size / extent)))."""
+    density and cell diagonal; a point's cell (p - lower) / extent * size in
+    float, clamped and truncated)."""
     n, d = P.shape
     lo = P.min(0)
     hi = P.max(0)
@@ -34,12 +34,11 @@ def expected(P, npc):
     q = vol * npc / n
     side = np.sqrt(q) if d == 2 else np.cbrt(q)
     size = np.array([max(1, int(np.ceil(float(e) / side))) for e in ext], np.int64)
-    scale = (size / ext.astype(np.float64)).astype(np.float32)
     cells = np.zeros(n, np.int64)
     for k in reversed(range(d)):
-        c = np.floor((P[:, k] - lo[k]) * scale[k])
-        c = np.clip(c, 0, size[k] - 1).astype(np.int64)
-        cells = cells * size[k] + c
+        c = ((P[:, k] - lo[k]) / ext[k]) * np.float32(size[k])
+        c = np.minimum(np.maximum(c, np.float32(0)), np.float32(size[k]) - np.float32(1))
+        cells = cells * size[k] + c.astype(np.int64)
     counts = np.bincount(cells, minlength=int(np.prod(size)))
     ne = np.sort(counts[counts > 0]).astype(np.float64)
     m = len(ne)
