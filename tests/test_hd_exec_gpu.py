@@ -44,6 +44,7 @@ def test_cpu_execution_matches_reference_golden(exe, case, tmp_path):
     rep = st["Running"]["Repeats"][0]
     assert rep["Execution"] == "CPU" and rep["Algorithm"] == "Early Break"
     assert rep["ComparedPairs"] == case["compared_pairs_t1"]
+    assert {"Threads", "ShuffleTime", "ComputeTime", "ReportedTime"} <= set(rep)
 
 
 def write_wkt(path, pts):
