@@ -435,9 +435,11 @@ inline uint8_t voxel_byte(const unsigned char* p, const Volume& v) {
     case Elem::F64: { double x; std::memcpy(&x, b, 8); real = x; is_real = true; break; }
   }
   if (v.rescale) {
-    if (v.elem == Elem::F64) return real_to_byte(real * v.slope + v.inter);
-    const double s = (double) (float) real * v.slope + v.inter;
-    return real_to_byte((double) (float) s);
+    // ITK rounds the product before adding the intercept; the volatile keeps
+    // a compiler from fusing the two into one FMA.
+    volatile double prod = (v.elem == Elem::F64 ? real : (double) (float) real) * v.slope;
+    const double s = prod + v.inter;
+    return real_to_byte(v.elem == Elem::F64 ? s : (double) (float) s);
   }
   return is_real ? real_to_byte(real) : (uint8_t) bits;
 }
