@@ -704,7 +704,9 @@ inline void TranslatePoints(PointSet& ps, int dim, double ratio) {
       lo = std::min(lo, ps.xyz64[i * ps.dims + dim]);
       hi = std::max(hi, ps.xyz64[i * ps.dims + dim]);
     }
-    const double shift = (hi - lo) * ratio;
+    // Read through a volatile so the product is rounded before each add (no FMA).
+    volatile double shift_v = (hi - lo) * ratio;
+    const double shift = shift_v;
     for (size_t i = 0; i < n; ++i) {
       ps.xyz64[i * ps.dims + dim] += shift;
       ps.xyz[i * ps.dims + dim] = (float) ps.xyz64[i * ps.dims + dim];
@@ -718,7 +720,8 @@ inline void TranslatePoints(PointSet& ps, int dim, double ratio) {
   }
   // The reference adds the double product to the float coordinate
   // (`p += extent * ratio`): the sum is formed in double and rounded once.
-  const double shift = (double) (hi - lo) * ratio;
+  volatile double shift_v = (double) (hi - lo) * ratio;  // rounded before the adds (no FMA)
+  const double shift = shift_v;
   for (size_t i = 0; i < n; ++i) {
     float& v = ps.xyz[i * ps.dims + dim];
     v = (float) ((double) v + shift);
