@@ -7,7 +7,9 @@ For every case it writes the two inputs in the reference's point-cache layout
 (inputs/<name>_{a,b}.bin) and records, in golden.json, what the reference
 returned: the float distance (and its bit pattern) and the compared-pair
 count for n_threads=1 (deterministic: it depends only on the seeded shuffle),
-and the distance for n_threads=4.
+and the distance for n_threads=4.  It also runs some of those inputs through
+the reference's -normalize / -translate preprocessing (oracle/_ref/ref_prep)
+and records a SHA-256 of each result's float32 points.
 
 Run from the repository root, in a container that has the reference sources:
     oracle/build_ref.sh <reference src directory> && python tests/golden/make_golden.py
@@ -28,6 +30,13 @@ sys.path.insert(0, ROOT)
 from hausdorffdistance_gb300 import synth  # noqa: E402
 
 REF = os.path.join(ROOT, "oracle", "_ref", "ref_eb")
+REF_PREP = os.path.join(ROOT, "oracle", "_ref", "ref_prep")
+
+# -normalize / -translate settings run through the reference's own
+# NormalizePoints / TranslatePoints (src/loaders/translate_points.h:42-79).
+PREP_CASES = ["uniform2d_3k_ab", "clusters3d_4k_ab", "offset_large_3d", "negative_2d",
+              "coplanar_3d", "all_equal_2d", "collinear_2d", "planes3d_3k_ab"]
+PREP_SETTINGS = [(1, 0.0), (0, 0.37), (1, 0.1234567), (0, -2.5)]
 
 
 def cases():
@@ -90,6 +99,29 @@ def run_ref(a_path, b_path, dims, seed, threads):
     return json.loads(line)["runs"][0]
 
 
+def run_prep(records, inp):
+    """The reference's preprocessing of each input file of PREP_CASES under
+    PREP_SETTINGS, recorded as a SHA-256 of the resulting float32 points."""
+    import hashlib
+    import tempfile
+    out = []
+    by_name = {r["name"]: r for r in records}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name in PREP_CASES:
+            rec = by_name[name]
+            for side in ("a", "b"):
+                src = os.path.join(HERE, rec[side])
+                for normalize, translate in PREP_SETTINGS:
+                    dst = os.path.join(tmp, "out.bin")
+                    subprocess.run([REF_PREP, src, dst, str(rec["dims"]), str(normalize),
+                                    repr(translate)], check=True)
+                    pts = synth.read_bin(dst, rec["dims"])
+                    out.append({"input": rec[side], "dims": rec["dims"], "normalize": normalize,
+                                "translate": translate, "n": int(pts.shape[0]),
+                                "sha256": hashlib.sha256(pts.tobytes()).hexdigest()})
+    return out
+
+
 def main():
     if not os.path.exists(REF):
         sys.exit("oracle/_ref/ref_eb is missing: run oracle/build_ref.sh <reference src directory> first")
@@ -112,11 +144,15 @@ def main():
             "hd_bits_t4": r4["hd_bits"],
         })
         print(name, r1["hd"], r1["compared_pairs"])
+    prep = run_prep(records, inp) if os.path.exists(REF_PREP) else []
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py",
                    "reference": "src/hd_impl/hausdorff_distance_early_break.h:44-115 "
                                 "built by oracle/build_ref.sh",
-                   "cases": records}, f, indent=1)
+                   "cases": records,
+                   "preprocessing_reference": "src/loaders/translate_points.h:42-79 "
+                                              "(ref_prep, built by oracle/build_ref.sh)",
+                   "preprocessing": prep}, f, indent=1)
 
 
 if __name__ == "__main__":

@@ -253,3 +253,22 @@ def test_wkt_parses_floats_directly(probe, tmp_path):
     assert float("1.00000005960464477539062500000000001") == 1.0 + 2.0 ** -24
     got = run(probe, p, "wkt", 2)
     assert np.float32(got[0, 0]) == np.float32(1.0 + 2.0 ** -23)
+
+
+GOLDEN_JSON = os.path.join(ROOT, "tests", "golden", "golden.json")
+PREP = __import__("json").load(open(GOLDEN_JSON)).get("preprocessing", [])
+
+
+@pytest.mark.parametrize("rec", PREP, ids=[f"{r['input'].split('/')[-1][:-4]}-n{r['normalize']}-t{r['translate']}"
+                                          for r in PREP])
+def test_normalize_translate_match_the_reference(probe, rec):
+    """-normalize and -translate give the float32 points the reference's own
+    NormalizePoints / TranslatePoints give (golden hashes made by running
+    them, built from the reference sources)."""
+    import hashlib
+    path = os.path.join(ROOT, "tests", "golden", rec["input"])
+    got = run(probe, path, "bin", rec["dims"], normalize=rec["normalize"],
+              translate=rec["translate"] if rec["translate"] != 0 else None)
+    pts = np.ascontiguousarray(got, np.float32)
+    assert len(pts) == rec["n"]
+    assert hashlib.sha256(pts.tobytes()).hexdigest() == rec["sha256"]
