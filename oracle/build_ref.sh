@@ -1,7 +1,8 @@
 #!/usr/bin/env bash
-# Builds the reference's own CPU early-break path and its -normalize /
-# -translate preprocessing from its sources where they lie (read-only) into
-# oracle/_ref/ref_eb and oracle/_ref/ref_prep.  Test infrastructure: used to pin
+# Builds the reference's own CPU early-break path, its -normalize /
+# -translate preprocessing and the host side of its statistics grid from its
+# sources where they lie (read-only) into oracle/_ref/ (ref_eb, ref_prep,
+# ref_stats).  Test infrastructure: used to pin
 # the oracle restatement and to generate tests/golden/.  Needs nvcc (the
 # reference header mixes host code with thrust/CUDA device lambdas).  The
 # shims in oracle/shim/ stand in for glog, nlohmann::json, HdrHistogram and
@@ -36,3 +37,10 @@ nvcc -std=c++17 -O2 --extended-lambda --expt-relaxed-constexpr --fmad=false \
   -I "$here/shim" -I "$ref" -include "$here/shim/prelude.h" \
   "$here/ref_prep_main.cu" -o "$here/_ref/ref_prep"
 echo "built $here/_ref/ref_prep"
+# The host-side grid shape of the reference's per-file statistics.
+nvcc -std=c++17 -O2 --extended-lambda --expt-relaxed-constexpr --fmad=false \
+  -Xcompiler -ffp-contract=off \
+  -gencode arch=compute_103a,code=sm_103a \
+  -I "$here/shim" -I "$ref" -include "$here/shim/prelude.h" \
+  "$here/ref_stats_main.cu" -o "$here/_ref/ref_stats"
+echo "built $here/_ref/ref_stats"

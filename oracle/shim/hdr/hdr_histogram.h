@@ -1,6 +1,6 @@
 // Stand-in declarations for HdrHistogram_c (absent from this image).  The
-// reference only calls these under its PROFILING define, which the oracle
-// build leaves off; the declarations just have to parse.
+// reference headers the oracle's drivers include mention these, but no
+// driver calls them; the declarations just have to parse.
 #pragma once
 #include <cstdint>
 #include <cstdio>
@@ -14,3 +14,4 @@ inline int hdr_percentiles_print(hdr_histogram*, FILE*, int, double, format_type
 inline int hdr_init(int64_t, int64_t, int, hdr_histogram**) { return 0; }
 inline bool hdr_record_value(hdr_histogram*, int64_t) { return true; }
 inline void hdr_reset(hdr_histogram*) {}
+inline void hdr_close(hdr_histogram*) {}

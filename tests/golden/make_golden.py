@@ -9,7 +9,8 @@ returned: the float distance (and its bit pattern) and the compared-pair
 count for n_threads=1 (deterministic: it depends only on the seeded shuffle),
 and the distance for n_threads=4.  It also runs some of those inputs through
 the reference's -normalize / -translate preprocessing (oracle/_ref/ref_prep)
-and records a SHA-256 of each result's float32 points.
+and records a SHA-256 of each result's float32 points, and records the
+reference's statistics-grid shape of every input (oracle/_ref/ref_stats).
 
 Run from the repository root, in a container that has the reference sources:
     oracle/build_ref.sh <reference src directory> && python tests/golden/make_golden.py
@@ -31,6 +32,7 @@ from hausdorffdistance_gb300 import synth  # noqa: E402
 
 REF = os.path.join(ROOT, "oracle", "_ref", "ref_eb")
 REF_PREP = os.path.join(ROOT, "oracle", "_ref", "ref_prep")
+REF_STATS = os.path.join(ROOT, "oracle", "_ref", "ref_stats")
 
 # -normalize / -translate settings run through the reference's own
 # NormalizePoints / TranslatePoints (src/loaders/translate_points.h:42-79).
@@ -122,6 +124,26 @@ def run_prep(records, inp):
     return out
 
 
+def run_stats(records):
+    """The reference's statistics-grid shape (non-empty box, resolution,
+    density) of every input file, for n_points_cell 10 (hd_exec's default)
+    and, on the first cases, 8."""
+    out = []
+    for i, rec in enumerate(records):
+        for side in ("a", "b"):
+            for npc in ((10, 8) if i < 6 else (10,)):
+                r = subprocess.run([REF_STATS, os.path.join(HERE, rec[side]), str(rec["dims"]),
+                                    str(npc)], check=True, capture_output=True, text=True)
+                v = r.stdout.split()
+                d = rec["dims"]
+                out.append({"input": rec[side], "dims": d, "n_points_cell": npc,
+                            "lower": [float(x) for x in v[:d]],
+                            "upper": [float(x) for x in v[d:2 * d]],
+                            "size": [int(x) for x in v[2 * d:3 * d]],
+                            "density": float(v[3 * d])})
+    return out
+
+
 def main():
     if not os.path.exists(REF):
         sys.exit("oracle/_ref/ref_eb is missing: run oracle/build_ref.sh <reference src directory> first")
@@ -145,6 +167,7 @@ def main():
         })
         print(name, r1["hd"], r1["compared_pairs"])
     prep = run_prep(records, inp) if os.path.exists(REF_PREP) else []
+    stats = run_stats(records) if os.path.exists(REF_STATS) else []
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py",
                    "reference": "src/hd_impl/hausdorff_distance_early_break.h:44-115 "
@@ -152,7 +175,11 @@ def main():
                    "cases": records,
                    "preprocessing_reference": "src/loaders/translate_points.h:42-79 "
                                               "(ref_prep, built by oracle/build_ref.sh)",
-                   "preprocessing": prep}, f, indent=1)
+                   "preprocessing": prep,
+                   "stats_grid_reference": "src/geoms/mbr.h:288-296, "
+                                           "src/index/uniform_grid.h:222-244 "
+                                           "(ref_stats, built by oracle/build_ref.sh)",
+                   "stats_grid": stats}, f, indent=1)
 
 
 if __name__ == "__main__":

@@ -113,3 +113,22 @@ def test_grid_shape_matches_the_reference_rule(probe, dims, n, npc, lo, hi):
     assert got[0] == want[0] and got[2] == want[2]
     assert np.array_equal(np.float32(got[1]), np.float32(want[1]))  # %.9g round-trips float
     assert got[3] == want[3] and got[4] == want[4]
+
+
+GRID = json.load(open(os.path.join(ROOT, "tests", "golden", "golden.json"))).get("stats_grid", [])
+
+
+@pytest.mark.parametrize("rec", GRID, ids=[f"{r['input'].split('/')[-1][:-4]}-k{r['n_points_cell']}"
+                                          for r in GRID])
+def test_grid_shape_matches_the_reference_build(probe, rec):
+    """The statistics grid's non-empty box, resolution and density equal what
+    the reference's own Mbr::ToNonemptyMBR / CalculateGridResolution /
+    get_volume give on the golden inputs (built from its sources)."""
+    from hausdorffdistance_gb300 import synth
+    d = rec["dims"]
+    P = synth.read_bin(os.path.join(ROOT, "tests", "golden", rec["input"]), d)
+    size, upper, _, density, _ = grid(probe, d, len(P), rec["n_points_cell"],
+                                      [float(x) for x in P.min(0)], [float(x) for x in P.max(0)])
+    assert size == rec["size"]
+    assert np.array_equal(np.float32(upper), np.float32(rec["upper"]))
+    assert np.float32(density) == np.float32(rec["density"])
