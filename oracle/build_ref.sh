@@ -1,8 +1,8 @@
 #!/usr/bin/env bash
 # Builds the reference's own CPU early-break path, its -normalize /
 # -translate preprocessing and the host side of its statistics grid from its
-# sources where they lie (read-only) into oracle/_ref/ (ref_eb, ref_prep,
-# ref_stats).  Test infrastructure: used to pin
+# sources where they lie (read-only) into oracle/_ref/ (ref_eb and, in the
+# double instantiation, ref_eb64; ref_prep; ref_stats).  Test infrastructure: used to pin
 # the oracle restatement and to generate tests/golden/.  Needs nvcc (the
 # reference header mixes host code with thrust/CUDA device lambdas).  The
 # shims in oracle/shim/ stand in for glog, nlohmann::json, HdrHistogram and
@@ -29,6 +29,13 @@ nvcc -std=c++17 -O2 --extended-lambda --expt-relaxed-constexpr --fmad=false \
   -I "$here/shim" -I "$ref" -include "$here/shim/prelude.h" \
   "$here/ref_eb_main.cu" -o "$here/_ref/ref_eb"
 echo "built $here/_ref/ref_eb"
+# The same early-break in the reference's double instantiation.
+nvcc -std=c++17 -O2 --extended-lambda --expt-relaxed-constexpr --fmad=false \
+  -Xcompiler -ffp-contract=off -Xcompiler -pthread -DREF_COORD=double \
+  -gencode arch=compute_103a,code=sm_103a \
+  -I "$here/shim" -I "$ref" -include "$here/shim/prelude.h" \
+  "$here/ref_eb_main.cu" -o "$here/_ref/ref_eb64"
+echo "built $here/_ref/ref_eb64"
 # The reference's -normalize / -translate preprocessing (translate_points.h),
 # for the golden vectors of hd_exec's same options.
 nvcc -std=c++17 -O2 --extended-lambda --expt-relaxed-constexpr --fmad=false \

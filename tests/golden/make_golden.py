@@ -7,7 +7,9 @@ For every case it writes the two inputs in the reference's point-cache layout
 (inputs/<name>_{a,b}.bin) and records, in golden.json, what the reference
 returned: the float distance (and its bit pattern) and the compared-pair
 count for n_threads=1 (deterministic: it depends only on the seeded shuffle),
-and the distance for n_threads=4.  It also runs some of those inputs through
+and the distance for n_threads=4; likewise, for double inputs, the
+reference's double instantiation (oracle/_ref/ref_eb64).  It also runs some of
+those float inputs through
 the reference's -normalize / -translate preprocessing (oracle/_ref/ref_prep)
 and records a SHA-256 of each result's float32 points, and records the
 reference's statistics-grid shape of every input (oracle/_ref/ref_stats).
@@ -31,6 +33,7 @@ sys.path.insert(0, ROOT)
 from hausdorffdistance_gb300 import synth  # noqa: E402
 
 REF = os.path.join(ROOT, "oracle", "_ref", "ref_eb")
+REF64 = os.path.join(ROOT, "oracle", "_ref", "ref_eb64")
 REF_PREP = os.path.join(ROOT, "oracle", "_ref", "ref_prep")
 REF_STATS = os.path.join(ROOT, "oracle", "_ref", "ref_stats")
 
@@ -94,8 +97,41 @@ def cases():
     return out
 
 
-def run_ref(a_path, b_path, dims, seed, threads):
-    r = subprocess.run([REF, a_path, b_path, str(dims), str(seed), str(threads)],
+def cases_f64():
+    """Double inputs for the reference's double instantiation (ref_eb64):
+    values that need double precision, points distinct only below float
+    precision, exact ties, large offsets, a single point."""
+    rng = np.random.Generator(np.random.PCG64(20261204))
+    out = []
+
+    def add(name, a, b, dims, seed=0):
+        out.append((name, np.ascontiguousarray(a, np.float64),
+                    np.ascontiguousarray(b, np.float64), dims, seed))
+
+    a, b = synth.clusters3d(3000, seed=21)
+    a = a.astype(np.float64) + rng.normal(0.0, 1e-9, a.shape)
+    b = b.astype(np.float64) + rng.normal(0.0, 1e-9, b.shape)
+    add("f64_clusters3d_3k_ab", a, b, 3, 0)
+    add("f64_clusters3d_3k_ba", b, a, 3, 3)
+    add("f64_uniform2d_2500x2000", rng.random((2500, 2)), rng.random((2000, 2)) * 1.05, 2, 1)
+    base = rng.random((1500, 3))
+    add("f64_subfloat_3d", base, base + rng.normal(0.0, 3e-9, base.shape), 3, 0)
+    g = np.stack(np.meshgrid(np.arange(10), np.arange(10)), -1).reshape(-1, 2).astype(np.float64)
+    add("f64_lattice_ties_2d", g, g + 0.5, 2, 0)
+    add("f64_offset_3d", rng.random((1200, 3)) * 10 + 1.0e6, rng.random((1000, 3)) * 10 + 1.0e6 - 2.0,
+        3, 5)
+    add("f64_single_vs_many_3d", [[0.1, 0.2, 0.3]], rng.random((300, 3)), 3, 0)
+    return out
+
+
+def write_bin64(path, pts):
+    with open(path, "wb") as f:
+        f.write(np.uint64(len(pts)).tobytes())
+        f.write(np.ascontiguousarray(pts, np.float64).tobytes())
+
+
+def run_ref(a_path, b_path, dims, seed, threads, exe=REF):
+    r = subprocess.run([exe, a_path, b_path, str(dims), str(seed), str(threads)],
                        check=True, capture_output=True, text=True)
     line = [ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1]
     return json.loads(line)["runs"][0]
@@ -166,6 +202,24 @@ def main():
             "hd_bits_t4": r4["hd_bits"],
         })
         print(name, r1["hd"], r1["compared_pairs"])
+    records64 = []
+    if os.path.exists(REF64):
+        for name, a, b, dims, seed in cases_f64():
+            pa = os.path.join(inp, f"{name}_a.bin")
+            pb = os.path.join(inp, f"{name}_b.bin")
+            write_bin64(pa, a)
+            write_bin64(pb, b)
+            r1 = run_ref(pa, pb, dims, seed, 1, REF64)
+            r4 = run_ref(pa, pb, dims, seed, 4, REF64)
+            records64.append({
+                "name": name, "dims": dims, "seed": seed,
+                "n_a": int(a.shape[0]), "n_b": int(b.shape[0]),
+                "a": f"inputs/{name}_a.bin", "b": f"inputs/{name}_b.bin",
+                "hd": r1["hd"], "hd_bits": r1["hd_bits"],
+                "compared_pairs_t1": r1["compared_pairs"],
+                "hd_bits_t4": r4["hd_bits"],
+            })
+            print(name, r1["hd"], r1["compared_pairs"])
     prep = run_prep(records, inp) if os.path.exists(REF_PREP) else []
     stats = run_stats(records) if os.path.exists(REF_STATS) else []
     with open(os.path.join(HERE, "golden.json"), "w") as f:
@@ -173,6 +227,9 @@ def main():
                    "reference": "src/hd_impl/hausdorff_distance_early_break.h:44-115 "
                                 "built by oracle/build_ref.sh",
                    "cases": records,
+                   "reference_f64": "the same early-break in the reference's double "
+                                    "instantiation (ref_eb64); inputs hold doubles",
+                   "cases_f64": records64,
                    "preprocessing_reference": "src/loaders/translate_points.h:42-79 "
                                               "(ref_prep, built by oracle/build_ref.sh)",
                    "preprocessing": prep,

@@ -11,6 +11,7 @@ a lattice and its translate (every row ties: the candidate list overflows and
 every row is walked), the scan route (eb, brute, other n_dims, coordinates
 beyond the LBVH route's range), device pointers, and the errors.
 """
+import json
 import math
 import os
 
@@ -210,3 +211,22 @@ def test_f64_repeated_calls_and_sizes(engine):
         b = clusters(m, 3, seed=seed + 100) + 0.001
         r = engine.solve_f64(a, b, undirected=True)
         check(r, oracle(a, b, True))
+
+
+GOLDEN64 = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                       "golden.json"))).get("cases_f64", [])
+
+
+@pytest.mark.parametrize("case", GOLDEN64, ids=[c["name"] for c in GOLDEN64])
+def test_f64_matches_reference_double_golden(engine, case):
+    """hd_solve_f64 returns, bit for bit, the distance of the reference's own
+    double instantiation (golden vectors of oracle/_ref/ref_eb64)."""
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+    def rd(p):
+        with open(os.path.join(here, p), "rb") as f:
+            n = int(np.frombuffer(f.read(8), np.uint64)[0])
+            return np.frombuffer(f.read(), np.float64)[: n * case["dims"]].reshape(n, case["dims"])
+    a, b = rd(case["a"]).copy(), rd(case["b"]).copy()
+    r = engine.solve_f64(a, b)
+    assert int(np.float64(r.hd).view(np.uint64)) == case["hd_bits"]

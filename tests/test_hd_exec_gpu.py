@@ -47,6 +47,26 @@ def test_cpu_execution_matches_reference_golden(exe, case, tmp_path):
     assert {"Threads", "ShuffleTime", "ComputeTime", "ReportedTime"} <= set(rep)
 
 
+GOLDEN64 = json.load(open(os.path.join(HERE, "golden", "golden.json"))).get("cases_f64", [])
+
+
+@pytest.mark.parametrize("case", GOLDEN64, ids=[c["name"] for c in GOLDEN64])
+def test_cpu_execution_is_double_matches_reference_golden(exe, case, tmp_path):
+    """-is_double -execution cpu gives the distance bits of the reference's own
+    double instantiation and, on one thread, its compared-pair count.  Needs
+    no GPU."""
+    out = tmp_path / "run.json"
+    r = subprocess.run([exe, "-input1", os.path.join(HERE, "golden", case["a"]), "-input2",
+                        os.path.join(HERE, "golden", case["b"]), "-input_type", "bin",
+                        "-n_dims", str(case["dims"]), "-execution", "cpu", "-is_double",
+                        "-repeat", "1", "-parallelism", "1", "-seed", str(case["seed"]),
+                        "-json", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    st = json.load(open(out))
+    assert int(np.float64(st["HDResult"]).view(np.uint64)) == case["hd_bits"]
+    assert st["Running"]["Repeats"][0]["ComparedPairs"] == case["compared_pairs_t1"]
+
+
 def write_wkt(path, pts):
     with open(path, "w") as f:
         for p in pts:

@@ -114,3 +114,26 @@ def test_bounded_sample_eb():
     part = hd_oracle.eb(a, b, n_threads=2, limit_a=500)
     assert part["compared_pairs"] < full["compared_pairs"]
     assert part["hd"] <= full["hd"]
+
+
+CASES64 = GOLDEN.get("cases_f64", [])
+
+
+def load_case64(c):
+    def rd(p):
+        with open(os.path.join(HERE, "golden", p), "rb") as f:
+            n = int(np.frombuffer(f.read(8), np.uint64)[0])
+            return np.frombuffer(f.read(), np.float64)[: n * c["dims"]].reshape(n, c["dims"])
+    return rd(c["a"]), rd(c["b"])
+
+
+@pytest.mark.parametrize("case", CASES64, ids=[c["name"] for c in CASES64])
+def test_exact_f64_oracle_matches_reference_double_build(case):
+    """The FP64 oracle's exact max-min equals, bit for bit, what the
+    reference's own early-break returns in its double instantiation (built
+    from its sources as oracle/_ref/ref_eb64), including points distinct only
+    below float precision, exact ties and large offsets."""
+    a, b = load_case64(case)
+    h2, ia, ib = hd_oracle.exact_f64(a, b)
+    assert int(np.float64(np.sqrt(h2)).view(np.uint64)) == case["hd_bits"]
+    assert case["hd_bits_t4"] == case["hd_bits"]
