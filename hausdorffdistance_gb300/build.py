@@ -111,11 +111,14 @@ REFERENCE_SRC = os.environ.get("HD_REFERENCE_SRC", "/root/reference/src")
 
 
 def build_reference() -> None:
-    """Builds the reference's own CPU early-break path into oracle/_ref when the
-    reference sources are present (test infrastructure only)."""
+    """Builds the reference's own CPU early-break path (float and double), its
+    -normalize/-translate preprocessing and its statistics-grid shape into
+    oracle/_ref when the reference sources are present (test infrastructure
+    only: they generate tests/golden/)."""
     script = os.path.join(ORACLE, "build_ref.sh")
-    target = os.path.join(ORACLE, "_ref", "ref_eb")
-    if os.path.exists(target) or not os.path.isdir(REFERENCE_SRC):
+    targets = [os.path.join(ORACLE, "_ref", t) for t in ("ref_eb", "ref_eb64", "ref_prep",
+                                                          "ref_stats")]
+    if all(os.path.exists(t) for t in targets) or not os.path.isdir(REFERENCE_SRC):
         return
     subprocess.run(["bash", script, REFERENCE_SRC], check=False, capture_output=True)
 
