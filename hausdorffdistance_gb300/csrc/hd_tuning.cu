@@ -1,3 +1,8 @@
+// The autotuned constants (hd_tuning_table.h, written by
+// hausdorffdistance_gb300/autotune.py from its sweep) as the one Tuning
+// struct the selector, the batched solver and the launch code read.  Stands in
+// for the reference's parameter models (src/models/*, chosen through
+// src/hd_impl/hausdorff_distance_hybrid.h:708-778).
 #include "hd_tuning.h"
 #include "hd_tuning_table.h"
 
