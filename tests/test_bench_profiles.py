@@ -47,3 +47,22 @@ def test_every_profile_names_its_command(name):
     assert "ncu " in text and "--clock-control none" in text
     assert not any(f.endswith((".ncu-rep", ".nsys-rep", ".qdrep"))
                    for f in os.listdir(os.path.join(ROOT, "profiles")))
+
+
+def test_lbvh_algorithmic_bytes_follow_their_definitions():
+    """Sort: per set the points read twice, two 16-byte key/index passes, the
+    sorted points written; build: 2 n/16 nodes of 32 B per set; query: the
+    queries' coordinates, 32 B per visited node, the visited leaves' points."""
+    class Counts:
+        visited_nodes = 1_000
+        visited_leaves = 300
+
+    n = 10_000_000
+    phases = dict((tag, b) for tag, b, _ in
+                  bench._lbvh_phases(n, n, 3, True, Counts, [0.8, 0.2, 0.0, 0.4]))
+    assert phases["morton_sort"] == 2 * n * (12 * 2 + 32 + 12) == 1_360_000_000
+    assert phases["lbvh_build"] == 2 * (2 * (n // 16)) * 32
+    assert phases["lbvh_query"] == 2 * n * 12 + 1_000 * 32 + 300 * 16 * 12
+    directed = dict((tag, b) for tag, b, _ in
+                    bench._lbvh_phases(n, n // 2, 2, False, Counts, [0.8, 0.2, 0.0, 0.4]))
+    assert directed["lbvh_query"] == n * 8 + 1_000 * 32 + 300 * 16 * 8
