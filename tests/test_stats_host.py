@@ -132,3 +132,21 @@ def test_grid_shape_matches_the_reference_build(probe, rec):
     assert size == rec["size"]
     assert np.array_equal(np.float32(upper), np.float32(rec["upper"]))
     assert np.float32(density) == np.float32(rec["density"])
+
+
+LOGGED = json.load(open(os.path.join(ROOT, "tests", "golden", "log_grid_stats.json")))["records"]
+
+
+def test_grid_shape_matches_the_reference_logs(probe):
+    """The statistics grid's cells per axis, cell diagonal and (per file)
+    density equal what the reference logged in its real runs for the same
+    box, point count and n_points_cell (tests/golden/log_grid_stats.json)."""
+    assert len(LOGGED) >= 150
+    for r in LOGGED:
+        d = len(r["lower"])
+        size, _, _, density, diag = grid(probe, d, r["n"], r["n_points_cell"],
+                                         r["lower"], r["upper"])
+        assert size == r["grid_size"], r["log"]
+        assert np.float32(diag) == np.float32(r["cell_diagonal"]), r["log"]
+        if "density" in r:
+            assert np.float32(density) == np.float32(r["density"]), r["log"]
