@@ -357,6 +357,21 @@ int main(int argc, char** argv) {
       std::printf("HausdorffDistance: distance is %.9g\n", d);
   };
 
+  // The configuration keys the reference writes into "Running" whatever the
+  // execution (run_hausdorff_distance.cu:206-215), plus this driver's own.
+  auto write_run_config = [&](hd::Json& run_json, const hd_options& o) {
+    run_json["Seed"] = (unsigned long long) o.seed;
+    run_json["FastBuildBVH"] = fl.getb("fast_build_bvh", false);
+    run_json["RebuildBVH"] = fl.getb("rebuild_bvh", false);
+    run_json["SampleRate"] = o.sample_rate;
+    run_json["NumPointsPerCell"] = o.n_points_cell;
+    run_json["MaxHit"] = max_hit;
+    run_json["EBOnlyThreshold"] = o.eb_only_threshold;
+    run_json["AutoTune"] = auto_tune;
+    run_json["LBVHBudget"] = (unsigned long long) o.lbvh_budget;  // 0: tuned table
+    run_json["Undirected"] = undirected;
+  };
+
   auto run = [&](const hd_options& o, hd::Json& run_json, double* out_dist) -> int {
     hd_ctx* ctx = nullptr;
     hd_status s = hd_create(&ctx, &o);
@@ -396,16 +411,7 @@ int main(int argc, char** argv) {
     }
     const double wall =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    run_json["Seed"] = (unsigned long long) o.seed;
-    run_json["SampleRate"] = o.sample_rate;
-    run_json["NumPointsPerCell"] = o.n_points_cell;
-    run_json["EBOnlyThreshold"] = o.eb_only_threshold;
-    run_json["MaxHit"] = max_hit;
-    run_json["LBVHBudget"] = (unsigned long long) o.lbvh_budget;  // 0: tuned table
-    run_json["AutoTune"] = auto_tune;
-    run_json["FastBuildBVH"] = fl.getb("fast_build_bvh", false);
-    run_json["RebuildBVH"] = fl.getb("rebuild_bvh", false);
-    run_json["Undirected"] = undirected;
+    write_run_config(run_json, o);
     run_json["Repeats"] = repeats;
     run_json["AvgTime"] = total / repeat;
     run_json["AvgWallTime"] = wall / repeat;
@@ -467,8 +473,7 @@ int main(int argc, char** argv) {
       total += ms;
       repeats.push_back(rep);
     }
-    run_json["Seed"] = (unsigned long long) opt.seed;
-    run_json["Undirected"] = undirected;
+    write_run_config(run_json, opt);
     run_json["Repeats"] = repeats;
     run_json["AvgTime"] = total / repeat;
     stats["HDResult"] = dist;

@@ -45,6 +45,12 @@ def test_cpu_execution_matches_reference_golden(exe, case, tmp_path):
     assert rep["Execution"] == "CPU" and rep["Algorithm"] == "Early Break"
     assert rep["ComparedPairs"] == case["compared_pairs_t1"]
     assert {"Threads", "ShuffleTime", "ComputeTime", "ReportedTime"} <= set(rep)
+    # The reference's "Running" configuration keys, whatever the execution.
+    assert {"Seed", "FastBuildBVH", "RebuildBVH", "SampleRate", "NumPointsPerCell", "MaxHit",
+            "EBOnlyThreshold", "AutoTune", "Repeats", "AvgTime"} <= set(st["Running"])
+    assert {"DateTime", "Input", "Running", "HDResult"} <= set(st)
+    assert {"Files", "Normalize", "Translate", "SerializationPrefix", "Limit", "NumDims",
+            "Type"} <= set(st["Input"])
 
 
 GOLDEN64 = json.load(open(os.path.join(HERE, "golden", "golden.json"))).get("cases_f64", [])
