@@ -274,6 +274,27 @@ def test_bad_flags_rejected(exe):
     assert r.returncode == 1 and "variant" in r.stderr
 
 
+@pytest.mark.parametrize("style", [
+    ["-input_type", "bin", "-seed", "{seed}", "-parallelism", "1", "-execution", "cpu"],
+    ["--input_type=bin", "--seed={seed}", "-parallelism=1", "--execution", "cpu"],
+    ["-input_type=BIN", "-seed", "{seed}", "--parallelism", "1", "-execution=CPU", "-nocheck"],
+])
+def test_cpu_execution_gflags_syntax(exe, tmp_path, style):
+    """The reference's flags are gflags: -name value, -name=value,
+    --name=value and -noboolflag all parse, and give the same run."""
+    c = GOLDEN[1]
+    out = tmp_path / "run.json"
+    args = [a.format(seed=c["seed"]) for a in style]
+    r = subprocess.run([exe, "-input1", os.path.join(HERE, "golden", c["a"]), "-input2",
+                        os.path.join(HERE, "golden", c["b"]), "-n_dims", str(c["dims"]),
+                        "-repeat", "1", "-json", str(out)] + args, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    st = json.load(open(out))
+    assert bits(st["HDResult"]) == c["hd_bits"]
+    assert st["Running"]["Repeats"][0]["ComparedPairs"] == c["compared_pairs_t1"]
+    assert st["Running"]["Seed"] == c["seed"]
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("variant", ["eb", "hybrid", "rt", "grid"])
 @pytest.mark.parametrize("case", GOLDEN[:8], ids=[c["name"] for c in GOLDEN[:8]])
