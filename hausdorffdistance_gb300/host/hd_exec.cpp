@@ -52,11 +52,13 @@ struct Flags {
     auto it = v.find(k);
     return it == v.end() ? def : std::atof(it->second.c_str());
   }
+  // gflags' boolean values: 1/t/true/y/yes and 0/f/false/n/no, any case.
   bool getb(const std::string& k, bool def) const {
     auto it = v.find(k);
     if (it == v.end()) return def;
-    const std::string& s = it->second;
-    return !(s == "false" || s == "0" || s == "no");
+    std::string s = it->second;
+    for (auto& ch : s) ch = (char) std::tolower((unsigned char) ch);
+    return !(s == "false" || s == "0" || s == "no" || s == "f" || s == "n");
   }
 };
 

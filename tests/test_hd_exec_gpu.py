@@ -278,6 +278,8 @@ def test_bad_flags_rejected(exe):
     ["-input_type", "bin", "-seed", "{seed}", "-parallelism", "1", "-execution", "cpu"],
     ["--input_type=bin", "--seed={seed}", "-parallelism=1", "--execution", "cpu"],
     ["-input_type=BIN", "-seed", "{seed}", "--parallelism", "1", "-execution=CPU", "-nocheck"],
+    ["-input_type", "bin", "-seed={seed}", "-parallelism", "1", "-execution", "cpu",
+     "-check=F", "-normalize=False", "-v=1", "-rt_prune=false"],
 ])
 def test_cpu_execution_gflags_syntax(exe, tmp_path, style):
     """The reference's flags are gflags: -name value, -name=value,
