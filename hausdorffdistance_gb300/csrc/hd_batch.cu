@@ -332,7 +332,7 @@ __device__ __forceinline__ void seed_item(const BatchArgs& a, const Cursor& cu, 
   for (uint32_t j = lo + lane; j < hi; j += 32) {
     float y[D];
 #pragma unroll
-    for (int t = 0; t < D; ++t) y[t] = Y[j * D + t];
+    for (int t = 0; t < D; ++t) y[t] = Y[(uint64_t) j * D + t];  // sets reach 2^32 - 2 points
 #pragma unroll
     for (int k = 0; k < kSlots; ++k) {
       if constexpr (D == 2)
